@@ -1,0 +1,150 @@
+"""ctypes binding of libfe_gb300.so (declared in include/fe_gb300.h).
+
+The library is the only compute path: importing this module without the built
+library, or calling into it without a CUDA device, raises -- nothing falls back to
+the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfe_gb300.so")
+
+FE_OK, FE_MAXITER, FE_BREAKDOWN, FE_NONFINITE, FE_BAD_INPUT, FE_CUDA_ERR, FE_NOT_READY = range(7)
+FE_KIND_ELASTIC_TRI, FE_KIND_MAGNETIC_TRI = 1, 2
+FE_PLANE_STRESS, FE_PLANE_STRAIN = 1, 2
+FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F = 1, 2, 4
+FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
+FE_PREC_FP64, FE_PREC_MIXED = 0, 1
+FE_FLAG_ACCEPT_STAGNATION = 1
+
+STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",
+                FE_NONFINITE: "FE_NONFINITE", FE_BAD_INPUT: "FE_BAD_INPUT",
+                FE_CUDA_ERR: "FE_CUDA_ERR", FE_NOT_READY: "FE_NOT_READY"}
+
+
+class FeError(RuntimeError):
+    """A failing status from the C ABI, with the library's message."""
+
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("cheb_degree", C.c_int32), ("max_iter", C.c_int32),
+                ("max_outer", C.c_int32), ("tol", C.c_double), ("inner_tol", C.c_double),
+                ("cheb_ratio", C.c_double), ("x0", C.c_void_p), ("x0_device", C.c_int32),
+                ("lanes", C.c_int32), ("chunk", C.c_int32), ("flags", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
+                ("spmv", C.c_int32), ("relres", C.c_double), ("bnorm", C.c_double),
+                ("solve_ms", C.c_double), ("assemble_ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_P = C.c_void_p
+_I32, _I64, _D = C.c_int32, C.c_int64, C.c_double
+_PD, _PI32, _PI64 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+
+_SIGNATURES = {
+    "fe_version": ([], C.c_int),
+    "fe_status_string": ([C.c_int], C.c_char_p),
+    "fe_last_error": ([], C.c_char_p),
+    "fe_mesh_create": ([_I32, _I64, _I64, _P, _P, C.POINTER(_P)], C.c_int),
+    "fe_destroy": ([_P], C.c_int),
+    "fe_set_elastic_materials": ([_P, _P, _P, _P, _P, _I32], C.c_int),
+    "fe_set_mu": ([_P, _P], C.c_int),
+    "fe_set_node_loads": ([_P, _I64, _P, _P, _P], C.c_int),
+    "fe_set_element_loads": ([_P, _I64, _P, _P, _P, _P, _I64], C.c_int),
+    "fe_set_dirichlet": ([_P, _I64, _P, _P], C.c_int),
+    "fe_element_node_factors": ([_P, _I64, _P, _P], C.c_int),
+    "fe_assemble": ([_P, _I32], C.c_int),
+    "fe_export_sizes": ([_P, _I32, _PI64, _PI64, _PI64], C.c_int),
+    "fe_export_csr": ([_P, _I32, _P, _P, _P], C.c_int),
+    "fe_export_rhs": ([_P, _P], C.c_int),
+    "fe_export_element_matrices": ([_P, _I32, _P], C.c_int),
+    "fe_solve": ([_P, C.POINTER(SolveOpts), _P, C.POINTER(SolveStats)], C.c_int),
+    "fe_get_solution": ([_P, _P], C.c_int),
+    "fe_solution_device_ptr": ([_P, C.POINTER(_P)], C.c_int),
+    "fe_info": ([_P, _PI64, _PI64, _PI64], C.c_int),
+    "fe_event_record": ([_P, _I32], C.c_int),
+    "fe_event_elapsed_ms": ([_P, _I32, _I32, _PD], C.c_int),
+    "fe_synchronize": ([_P], C.c_int),
+    "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
+    "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
+}
+
+_lib = None
+
+
+def load():
+    """Load libfe_gb300.so once; raise if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with "
+                          "`python -m finite_elements_gb300.build` (nvcc, sm_103a)")
+    lib = C.CDLL(LIB_PATH)
+    for name, (args, res) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def check(status, what=""):
+    if status != FE_OK:
+        msg = load().fe_last_error().decode(errors="replace")
+        raise FeError(status, f"{what}: {msg}" if what else msg)
+    return status
+
+
+def ptr(a):
+    """Address of a C-contiguous numpy array (None for None)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "arrays crossing the C ABI must be contiguous"
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Handle:
+    """Owns one fe_handle (device buffers of one problem); freed on close / GC."""
+
+    def __init__(self, kind, coords, conn):
+        lib = load()
+        self._lib = lib
+        coords = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 2)
+        conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 3)
+        h = C.c_void_p()
+        check(lib.fe_mesh_create(kind, coords.shape[0], conn.shape[0], ptr(coords), ptr(conn),
+                                 C.byref(h)), "fe_mesh_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.fe_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:   # interpreter shutdown
+            pass
+
+    def call(self, name, *args):
+        return check(getattr(self._lib, name)(self.h, *args), name)

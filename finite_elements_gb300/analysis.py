@@ -1,0 +1,238 @@
+"""Drop-in ``FiniteElementAnalysis`` running the assembly-and-solve path on the GPU.
+
+Same constructor, methods, return types and error behaviour as the reference's
+``finite_elements.analysis.FiniteElementAnalysis`` (finite_elements/analysis.py:141-173,
+:580-830) for what it solves:
+
+* ``create_matrix()`` -> scipy CSR of the augmented system [[K, C^T], [C, 0]], same
+  pattern (explicit zeros kept), same indices, values to rounding (analysis.py:617-663);
+* ``create_source_matrix()`` -> (n*dim + n_bc, 1) array (analysis.py:665-708);
+* ``solve()`` -> ``Result(mesh, list)`` with u then the multipliers (analysis.py:798-830);
+* ``k_matrix_sparse()`` / ``m_matrix_sparse()`` -> scipy CSC (analysis.py:345-405).
+
+Instead of scipy's sparse LU on the saddle system, the GPU eliminates the Dirichlet
+DOFs, solves the SPD system with PCG and recovers each multiplier from the first
+block row, lambda_i = (F - K u)[dof_i].  Continuity conditions and magnet loads are
+not on this path and raise NotImplementedError.
+"""
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+import scipy.sparse.linalg as spla
+
+from .engine import GpuSystem, check_plane_flags
+from .mesh import ArrayMesh
+from .problem import ELASTIC, MAGNETIC, ElementLoadSet, Problem
+from .results import Result
+
+DEFAULT_SOLVER = {"precision": "fp64", "tol": 1e-12, "accept_stagnation": True, "cheb_degree": 0}
+
+
+class SolverConvergenceError(RuntimeError):
+    """PCG stopped at its iteration cap above the requested tolerance."""
+
+
+def _element_kind(element):
+    if hasattr(element, "mu_total"):
+        return MAGNETIC
+    if hasattr(element, "elasticity_modulus"):
+        return ELASTIC
+    raise NotImplementedError(f"element type {type(element).__name__} is not a linear triangle "
+                              "of the GPU path")
+
+
+class FiniteElementAnalysis:
+    """See the module docstring.  ``solver`` (optional) overrides the solve options
+    (``precision`` "fp64" / "mixed", ``tol``, ``cheb_degree``, ``max_iter``, ``x0`` ...)."""
+
+    def __init__(self, mesh, element_loads, edge_loads, node_loads, magnet_loads,
+                 continuity_conditions, node_boundary_conditions, edge_boundary_conditions,
+                 element_boundary_conditions, plane_strain: bool = None, plane_stress: bool = None,
+                 solver=None):
+        self.mesh = mesh
+        self.element_loads = element_loads
+        self.edge_loads = edge_loads
+        self.node_loads = node_loads
+        self.magnet_loads = magnet_loads
+        self.continuity_conditions = continuity_conditions
+        self.node_boundary_conditions = node_boundary_conditions
+        self.edge_boundary_conditions = edge_boundary_conditions
+        self.element_boundary_conditions = element_boundary_conditions
+        self.plane_strain = plane_strain
+        self.plane_stress = plane_stress
+        self.solver = dict(DEFAULT_SOLVER, **(solver or {}))
+        self._problem = None
+        self._system = None
+        self._boundary_conditions = None
+        self._positions = None
+        self.last_stats = None
+
+    @classmethod
+    def from_problem(cls, problem: Problem, mesh=None, solver=None):
+        """Analysis of an array-only Problem (no per-element Python objects)."""
+        if mesh is None:
+            mesh = ArrayMesh(problem.coords, problem.conn)
+        obj = cls(mesh, [], [], [], [], [], [], [], [], problem.plane_strain, problem.plane_stress,
+                  solver=solver)
+        obj._problem = problem
+        return obj
+
+    # ------------------------------------------------------------ reference properties
+
+    @property
+    def dimension(self):
+        if self._problem is not None and isinstance(self.mesh, ArrayMesh):
+            return self._problem.dim
+        return self.mesh.elements_groups[0].elements[0].dimension
+
+    @property
+    def elements_name(self):
+        return self.mesh.elements_groups[0].elements[0].__class__.__name__
+
+    @property
+    def positions(self):
+        if not self._positions:
+            d, n = self.dimension, len(self.mesh.nodes)
+            self._positions = {(i, j + 1): i * d + j for i in range(n) for j in range(d)}
+        return self._positions
+
+    # ------------------------------------------------------------ flattening
+
+    def problem(self) -> Problem:
+        """The analysis as arrays (mesh walk of analysis.py:326-338, :714-735)."""
+        if self._problem is not None:
+            return self._problem
+        if self.continuity_conditions:
+            raise NotImplementedError("continuity conditions are not part of the GPU path")
+        if self.magnet_loads:
+            raise NotImplementedError("magnet loads are not part of the GPU path")
+        mesh = self.mesh
+        nodes = mesh.nodes
+        index = mesh.node_to_index
+        coords = np.array([[float(p[0]), float(p[1])] for p in nodes], dtype=np.float64).reshape(-1, 2)
+        elements = [el for g in mesh.elements_groups for el in g.elements]
+        if not elements:
+            raise ValueError("the mesh has no element")
+        kind = _element_kind(elements[0])
+        conn = np.array([[index[p] for p in el.points] for el in elements], dtype=np.int32).reshape(-1, 3)
+        by_id = {id(el): k for k, el in enumerate(elements)}
+        by_points = {}
+
+        def element_index(el):
+            k = by_id.get(id(el))
+            if k is None:
+                if not by_points:
+                    by_points.update({tuple(r): k for k, r in enumerate(conn.tolist())})
+                k = by_points.get(tuple(index[p] for p in el.points))
+                if k is None:
+                    raise ValueError("an element of a load or condition is not part of the mesh")
+            return k
+
+        kw = {}
+        if kind == ELASTIC:
+            kw = dict(E=[el.elasticity_modulus for el in elements],
+                      nu=[el.poisson_ratio for el in elements],
+                      thickness=[getattr(el, "thickness", 1.0) for el in elements],
+                      plane_strain=self.plane_strain, plane_stress=self.plane_stress)
+            rho = [el.mass_density for el in elements]
+            if all(r is not None for r in rho):
+                kw["rho"] = rho
+        else:
+            kw = dict(mu=[el.mu_total for el in elements])
+        nl = self.node_loads
+        el_loads = [ElementLoadSet(np.array([element_index(e) for e in ld.elements], np.int64),
+                                   ld.value, ld.dimension) for ld in self.element_loads]
+        prob = Problem(
+            kind, coords, conn, **kw,
+            node_load_node=[index[ld.node] for ld in nl], node_load_dim=[ld.dimension for ld in nl],
+            node_load_value=[ld.value for ld in nl], element_loads=el_loads,
+            edge_load_nodes=[[index[ld.edge.start], index[ld.edge.end]] for ld in self.edge_loads],
+            edge_load_dim=[ld.dimension for ld in self.edge_loads],
+            edge_load_value=[ld.value for ld in self.edge_loads],
+            node_bc_node=[index[c.application] for c in self.node_boundary_conditions],
+            node_bc_dim=[c.dimension for c in self.node_boundary_conditions],
+            node_bc_value=[c.value for c in self.node_boundary_conditions],
+            element_bc_element=[element_index(c.application) for c in self.element_boundary_conditions],
+            element_bc_dim=[c.dimension for c in self.element_boundary_conditions],
+            element_bc_value=[c.value for c in self.element_boundary_conditions],
+            edge_bc_nodes=[[index[c.application.start], index[c.application.end]]
+                           for c in self.edge_boundary_conditions],
+            edge_bc_dim=[c.dimension for c in self.edge_boundary_conditions],
+            edge_bc_value=[c.value for c in self.edge_boundary_conditions])
+        self._problem = prob
+        return prob
+
+    def system(self) -> GpuSystem:
+        if self._system is None:
+            prob = self.problem()
+            if prob.kind == ELASTIC:
+                check_plane_flags(self.plane_strain, self.plane_stress)
+                prob.plane_strain, prob.plane_stress = self.plane_strain, self.plane_stress
+            self._system = GpuSystem(prob)
+        return self._system
+
+    # ------------------------------------------------------------ reference API
+
+    def create_matrix(self):
+        sysm = self.system()
+        self._boundary_conditions = list(zip(sysm.bc_dof.tolist(), sysm.bc_value.tolist()))
+        return sysm.create_matrix()
+
+    def create_source_matrix(self):
+        if self._boundary_conditions is None:
+            # the reference sizes F with len(self._boundary_conditions), which only
+            # create_matrix sets (analysis.py:737-739)
+            raise TypeError("object of type 'NoneType' has no len()")
+        return self.system().create_source_matrix()
+
+    def k_matrix_sparse(self):
+        return self.system().k_matrix_sparse()
+
+    def m_matrix_sparse(self):
+        if self.problem().kind != ELASTIC:
+            raise AttributeError("'MagneticElement2D' object has no attribute 'elementary_mass_matrix'")
+        return self.system().m_matrix_sparse()
+
+    def k_matrix(self, method_name):
+        if method_name == 'dense':
+            return self.k_matrix_sparse().toarray()
+        if method_name == 'sparse':
+            return self.k_matrix_sparse()
+        raise NotImplementedError(
+            f'Class {self.__class__.__name__} does not implement {method_name} k matrix')
+
+    def m_matrix(self, method_name):
+        if method_name == 'dense':
+            return self.m_matrix_sparse().toarray()
+        if method_name == 'sparse':
+            return self.m_matrix_sparse()
+        raise NotImplementedError(
+            f'Class {self.__class__.__name__} does not implement {method_name} m matrix')
+
+    def element_matrices(self, which="K"):
+        """(E, (3*dim)^2) row-major element matrices from the GPU element kernels."""
+        return self.system().element_matrices(which)
+
+    def solve(self):
+        """PCG on the GPU in place of spsolve (analysis.py:798-830)."""
+        sysm = self.system()
+        self._boundary_conditions = list(zip(sysm.bc_dof.tolist(), sysm.bc_value.tolist()))
+        opts = dict(self.solver)
+        x, st = sysm.solve(**opts)
+        self.last_stats = st.as_dict()
+        from . import _lib
+        if st.status in (_lib.FE_BREAKDOWN, _lib.FE_NONFINITE):
+            # scipy's spsolve warns and returns NaN for an exactly singular matrix; the
+            # reference turns the warning into NotImplementedError when it is raised
+            try:
+                warnings.warn("Matrix is exactly singular", spla.MatrixRankWarning)
+            except spla.MatrixRankWarning as exc:
+                print('MatricRankWarning')
+                raise NotImplementedError from exc
+            x = np.full(x.shape, np.nan)
+        elif st.status == _lib.FE_MAXITER:
+            raise SolverConvergenceError(
+                f"PCG stopped after {st.iterations} iterations at relative residual {st.relres:.3e}")
+        return Result(self.mesh, list(x))

@@ -1,0 +1,999 @@
+// Assembly on the device: element kernels, the sort-based pattern build, the
+// segmented reduction of element blocks into node-block CSR slots, loads with the
+// reference's last-wins semantics, Dirichlet elimination, and the exports in the
+// exact layouts scipy builds (finite_elements/analysis.py:617-708, :345-405).
+//
+// Layout in HBM.  DOFs are interleaved node-major (dof = node*d + comp,
+// finite_elements/core.py:89-108), so K is stored as a CSR of d x d node blocks:
+// blk_ptr[n_nodes+1], blk_col[nnzb], values [nnzb][d][d] row-major.  The scalar CSR
+// scipy returns is this matrix with every block row expanded and the multiplier
+// entries appended; the export kernels produce it on the device.
+#include <algorithm>
+#include <vector>
+
+#include "fe_internal.h"
+
+namespace fe {
+namespace {
+
+// ---------------------------------------------------------------- rounding helpers
+// Element arithmetic is written with explicit round-to-nearest operations in the
+// reference's evaluation order, so that no multiply-add is contracted and the
+// element values round exactly as the reference's numpy expressions do.
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+struct Tri {
+    double x1, y1, x2, y2, x3, y3;
+};
+
+__device__ __forceinline__ Tri load_tri(const double *__restrict__ coords, const int32_t *__restrict__ conn,
+                                        int64_t e) {
+    int n0 = conn[3 * e], n1 = conn[3 * e + 1], n2 = conn[3 * e + 2];
+    double2 p0 = reinterpret_cast<const double2 *>(coords)[n0];
+    double2 p1 = reinterpret_cast<const double2 *>(coords)[n1];
+    double2 p2 = reinterpret_cast<const double2 *>(coords)[n2];
+    return Tri{p0.x, p0.y, p1.x, p1.y, p2.x, p2.y};
+}
+
+// (x2-x1)(y3-y1) - (x3-x1)(y2-y1): twice the signed area in the vertex order used by
+// element_to_node_factors (elements.py:33) and the triangle area.
+__device__ __forceinline__ double det_123(const Tri &t) {
+    return sub(mul(sub(t.x2, t.x1), sub(t.y3, t.y1)), mul(sub(t.x3, t.x1), sub(t.y2, t.y1)));
+}
+
+__device__ __forceinline__ double tri_area(const Tri &t) { return dvd(fabs(det_123(t)), 2.0); }
+
+// Shape-function coefficients (a_i, b_i, c_i), N_i(p_j) = delta_ij.
+__device__ __forceinline__ void form_functions(const Tri &t, double a[3], double b[3], double c[3]) {
+    double det = det_123(t);
+    a[0] = dvd(sub(mul(t.x2, t.y3), mul(t.x3, t.y2)), det);
+    a[1] = dvd(sub(mul(t.x3, t.y1), mul(t.x1, t.y3)), det);
+    a[2] = dvd(sub(mul(t.x1, t.y2), mul(t.x2, t.y1)), det);
+    b[0] = dvd(sub(t.y2, t.y3), det);
+    b[1] = dvd(sub(t.y3, t.y1), det);
+    b[2] = dvd(sub(t.y1, t.y2), det);
+    c[0] = dvd(sub(t.x3, t.x2), det);
+    c[1] = dvd(sub(t.x1, t.x3), det);
+    c[2] = dvd(sub(t.x2, t.x1), det);
+}
+
+// |detJ| * (a_i + 0.5 b_i x2 + 0.5 c_i y2 + 0.5 b_i x3 + 0.5 c_i y3), term order of
+// elements.py:46-51.
+__device__ __forceinline__ void node_factors(const Tri &t, double f[3]) {
+    double a[3], b[3], c[3];
+    form_functions(t, a, b, c);
+    double dj = fabs(det_123(t));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double hb = mul(0.5, b[i]), hc = mul(0.5, c[i]);
+        double s = add(a[i], mul(hb, t.x2));
+        s = add(s, mul(hc, t.y2));
+        s = add(s, mul(hb, t.x3));
+        s = add(s, mul(hc, t.y3));
+        f[i] = mul(dj, s);
+    }
+}
+
+// ---------------------------------------------------------------- mesh checks
+
+__global__ void k_validate_conn(const int32_t *__restrict__ conn, int64_t n3, int64_t n_nodes,
+                                int *err, int *max_node) {
+    int local_max = -1;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n3;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int v = conn[k];
+        if (v < 0 || v >= n_nodes) atomicOr(err, ERR_CONN_RANGE);
+        local_max = max(local_max, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) local_max = max(local_max, __shfl_xor_sync(0xffffffffu, local_max, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(max_node, local_max);
+}
+
+// ---------------------------------------------------------------- pattern build
+// Counting sort of the 3E (element, local vertex) incidences by node, a per-node sort
+// of each incidence list (element order), then per node the sorted set of nodes
+// sharing an element with it: the block columns of that node's block row.
+
+__global__ void k_count_incidence(const int32_t *__restrict__ conn, int64_t n3, int32_t *cnt) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n3;
+         k += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[conn[k]], 1);
+}
+
+__global__ void k_fill_incidence(const int32_t *__restrict__ conn, int64_t n3,
+                                 const int32_t *__restrict__ inc_ptr, int32_t *cursor,
+                                 int32_t *__restrict__ inc) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n3;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int node = conn[k];
+        int pos = inc_ptr[node] + atomicAdd(&cursor[node], 1);
+        inc[pos] = (int32_t)k;   // element*3 + local vertex
+    }
+}
+
+__device__ __forceinline__ void insertion_sort(int32_t *a, int n) {
+    for (int i = 1; i < n; ++i) {
+        int32_t v = a[i];
+        int j = i - 1;
+        while (j >= 0 && a[j] > v) {
+            a[j + 1] = a[j];
+            --j;
+        }
+        a[j + 1] = v;
+    }
+}
+
+// Sort each node's incidence list, gather the nodes of its elements into cand[]
+// (3 per incidence), sort them and count the distinct ones.
+__global__ void k_node_neighbours(int64_t n_nodes, const int32_t *__restrict__ conn,
+                                  const int32_t *__restrict__ inc_ptr, int32_t *__restrict__ inc,
+                                  int32_t *__restrict__ cand, int32_t *__restrict__ nb_cnt) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        int s = inc_ptr[r], e = inc_ptr[r + 1], d = e - s;
+        insertion_sort(inc + s, d);
+        int32_t *c = cand + 3 * (int64_t)s;
+        for (int t = 0; t < d; ++t) {
+            int el = inc[s + t] / 3;
+            c[3 * t] = conn[3 * el];
+            c[3 * t + 1] = conn[3 * el + 1];
+            c[3 * t + 2] = conn[3 * el + 2];
+        }
+        insertion_sort(c, 3 * d);
+        int u = 0;
+        for (int t = 0; t < 3 * d; ++t)
+            if (t == 0 || c[t] != c[t - 1]) ++u;
+        nb_cnt[r] = u;
+    }
+}
+
+__global__ void k_write_pattern(int64_t n_nodes, const int32_t *__restrict__ inc_ptr,
+                                const int32_t *__restrict__ cand, const int32_t *__restrict__ blk_ptr,
+                                int32_t *__restrict__ blk_col, int32_t *__restrict__ blk_row) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        int s = inc_ptr[r], d = inc_ptr[r + 1] - s;
+        const int32_t *c = cand + 3 * (int64_t)s;
+        int o = blk_ptr[r];
+        for (int t = 0; t < 3 * d; ++t)
+            if (t == 0 || c[t] != c[t - 1]) {
+                blk_col[o] = c[t];
+                blk_row[o] = (int32_t)r;
+                ++o;
+            }
+    }
+}
+
+// ---------------------------------------------------------------- element kernels
+
+// Plane-elasticity Ke (elements.py:395-453, :466-511).  B uses the signed
+// detJ = (x1-x3)(y2-y3) - (y1-y3)(x2-x3); the zero entries of B and D contribute
+// exact zeros, so Ke[2i+a][2j+b] reduces to two products per entry in the order of
+// (B^T D) B.  Ke = (t * area) * M, area = |detJ|/2.  128 elements per block are
+// staged in shared memory and written back as one contiguous, coalesced range.
+constexpr int kElemBlock = 128;
+
+__global__ void __launch_bounds__(kElemBlock)
+k_elastic_ke(int64_t n_elem, const double *__restrict__ coords, const int32_t *__restrict__ conn,
+             const double *__restrict__ E, const double *__restrict__ nu,
+             const double *__restrict__ thick, int plane_strain, double *__restrict__ ke_out,
+             int *err) {
+    __shared__ double tile[kElemBlock * 36];
+    for (int64_t base = (int64_t)blockIdx.x * kElemBlock; base < n_elem;
+         base += (int64_t)gridDim.x * kElemBlock) {
+        int64_t e = base + threadIdx.x;
+        double *my = tile + threadIdx.x * 36;
+        if (e < n_elem) {
+            Tri t = load_tri(coords, conn, e);
+            double det = sub(mul(sub(t.x1, t.x3), sub(t.y2, t.y3)), mul(sub(t.y1, t.y3), sub(t.x2, t.x3)));
+            double inv = dvd(1.0, det);
+            // beta_i = y-differences / det, gamma_i = x-differences / det
+            double be[3] = {mul(inv, sub(t.y2, t.y3)), mul(inv, sub(t.y3, t.y1)), mul(inv, sub(t.y1, t.y2))};
+            double ga[3] = {mul(inv, sub(t.x3, t.x2)), mul(inv, sub(t.x1, t.x3)), mul(inv, sub(t.x2, t.x1))};
+            double Em = E[e], v = nu[e];
+            double a = plane_strain ? dvd(mul(Em, v), mul(add(1.0, v), sub(1.0, mul(2.0, v))))
+                                    : dvd(mul(Em, v), sub(1.0, mul(v, v)));
+            double bb = dvd(Em, mul(2.0, add(1.0, v)));
+            double c = add(a, mul(2.0, bb));
+            double ta = mul(thick[e], tri_area(t));
+            if (!isfinite(ta) || !isfinite(inv) || !isfinite(c)) atomicOr(err, ERR_NONFINITE);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                // rows 2i and 2i+1 of B^T D
+                double r0c = mul(be[i], c), r0a = mul(be[i], a), r0b = mul(ga[i], bb);
+                double r1a = mul(ga[i], a), r1c = mul(ga[i], c), r1b = mul(be[i], bb);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    double m00 = add(mul(r0c, be[j]), mul(r0b, ga[j]));
+                    double m01 = add(mul(r0a, ga[j]), mul(r0b, be[j]));
+                    double m10 = add(mul(r1a, be[j]), mul(r1b, ga[j]));
+                    double m11 = add(mul(r1c, ga[j]), mul(r1b, be[j]));
+                    my[(2 * i) * 6 + 2 * j] = mul(ta, m00);
+                    my[(2 * i) * 6 + 2 * j + 1] = mul(ta, m01);
+                    my[(2 * i + 1) * 6 + 2 * j] = mul(ta, m10);
+                    my[(2 * i + 1) * 6 + 2 * j + 1] = mul(ta, m11);
+                }
+            }
+        }
+        __syncthreads();
+        int64_t cnt = min((int64_t)kElemBlock, n_elem - base) * 36;
+        double *dst = ke_out + base * 36;
+        for (int64_t k = threadIdx.x; k < cnt; k += kElemBlock) dst[k] = tile[k];
+        __syncthreads();
+    }
+}
+
+// Magnetostatic Ke_ij = ((1/mu) * (b_i b_j + c_i c_j)) * area (elements.py:93-118).
+__global__ void __launch_bounds__(kElemBlock)
+k_magnetic_ke(int64_t n_elem, const double *__restrict__ coords, const int32_t *__restrict__ conn,
+              const double *__restrict__ mu, double *__restrict__ ke_out, int *err) {
+    __shared__ double tile[kElemBlock * 9];
+    for (int64_t base = (int64_t)blockIdx.x * kElemBlock; base < n_elem;
+         base += (int64_t)gridDim.x * kElemBlock) {
+        int64_t e = base + threadIdx.x;
+        double *my = tile + threadIdx.x * 9;
+        if (e < n_elem) {
+            Tri t = load_tri(coords, conn, e);
+            double a[3], b[3], c[3];
+            form_functions(t, a, b, c);
+            double area = tri_area(t);
+            double im = dvd(1.0, mu[e]);
+            if (!isfinite(area) || !isfinite(im) || !isfinite(b[0])) atomicOr(err, ERR_NONFINITE);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    my[3 * i + j] = mul(mul(im, add(mul(b[i], b[j]), mul(c[i], c[j]))), area);
+        }
+        __syncthreads();
+        int64_t cnt = min((int64_t)kElemBlock, n_elem - base) * 9;
+        double *dst = ke_out + base * 9;
+        for (int64_t k = threadIdx.x; k < cnt; k += kElemBlock) dst[k] = tile[k];
+        __syncthreads();
+    }
+}
+
+// Mass scale (rho * area * t) / 12 of elements.py:530-531; Me = scale * P.
+__global__ void k_mass_scale(int64_t n_elem, const double *__restrict__ coords,
+                             const int32_t *__restrict__ conn, const double *__restrict__ rho,
+                             const double *__restrict__ thick, double *__restrict__ out) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        Tri t = load_tri(coords, conn, e);
+        out[e] = dvd(mul(mul(rho[e], tri_area(t)), thick[e]), 12.0);
+    }
+}
+
+__global__ void k_node_factors(int64_t n, const int64_t *__restrict__ elems, int64_t n_elem,
+                               const double *__restrict__ coords, const int32_t *__restrict__ conn,
+                               double *__restrict__ out, int *err) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t e = elems[k];
+        if (e < 0 || e >= n_elem) {
+            atomicOr(err, ERR_ELEM_RANGE);
+            continue;
+        }
+        double f[3];
+        node_factors(load_tri(coords, conn, e), f);
+        out[3 * k] = f[0];
+        out[3 * k + 1] = f[1];
+        out[3 * k + 2] = f[2];
+    }
+}
+
+// ---------------------------------------------------------------- segmented reduction
+// One thread per block slot (row node r, column node m): walk r's incidence list in
+// element order and add block (i, j) of every element whose vertex j is m.  The sum
+// runs in element order, as the reference's dict merge does (analysis.py:390-395),
+// with no atomics: the result is the same on every run.
+template <int D>
+__global__ void k_reduce_stiffness(int64_t nnzb, const int32_t *__restrict__ blk_row,
+                                   const int32_t *__restrict__ blk_col, const int32_t *__restrict__ inc_ptr,
+                                   const int32_t *__restrict__ inc, const int32_t *__restrict__ conn,
+                                   const double *__restrict__ ke, double *__restrict__ kval) {
+    constexpr int NL = 3 * D;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nnzb;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        int r = blk_row[s], m = blk_col[s];
+        double acc[D * D];
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) acc[k] = 0.0;
+        int a0 = inc_ptr[r], a1 = inc_ptr[r + 1];
+        for (int t = a0; t < a1; ++t) {
+            int code = inc[t];
+            int e = code / 3, i = code - 3 * e;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                if (conn[3 * e + j] == m) {
+                    const double *blk = ke + (int64_t)e * NL * NL + (i * D) * NL + j * D;
+#pragma unroll
+                    for (int a = 0; a < D; ++a)
+#pragma unroll
+                        for (int b = 0; b < D; ++b) acc[a * D + b] = __dadd_rn(acc[a * D + b], blk[a * NL + b]);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) kval[s * D * D + k] = acc[k];
+    }
+}
+
+// Mass blocks: Me block (i, j) = scale * (i == j ? 2 : 1) * I_2 (elements.py:514-519).
+__global__ void k_reduce_mass(int64_t nnzb, const int32_t *__restrict__ blk_row,
+                              const int32_t *__restrict__ blk_col, const int32_t *__restrict__ inc_ptr,
+                              const int32_t *__restrict__ inc, const int32_t *__restrict__ conn,
+                              const double *__restrict__ scale, double *__restrict__ mval) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nnzb;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        int r = blk_row[s], m = blk_col[s];
+        double diag = 0.0;
+        int a0 = inc_ptr[r], a1 = inc_ptr[r + 1];
+        for (int t = a0; t < a1; ++t) {
+            int code = inc[t];
+            int e = code / 3, i = code - 3 * e;
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                if (conn[3 * e + j] == m) diag = __dadd_rn(diag, __dmul_rn(scale[e], i == j ? 2.0 : 1.0));
+        }
+        // the off-diagonal entries of the 2x2 block are sums of exact zeros
+        mval[s * 4 + 0] = diag;
+        mval[s * 4 + 1] = 0.0;
+        mval[s * 4 + 2] = 0.0;
+        mval[s * 4 + 3] = diag;
+    }
+}
+
+// ---------------------------------------------------------------- loads
+// The reference keeps, per (node, dimension), the last load of its list
+// (analysis.py:71-110).  Every load carries its list position as seq; an atomicMax
+// picks the winner, then the winner alone writes F.
+
+__global__ void k_init_loads(int64_t n_dof, double *F, long long *seq) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_dof;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        F[k] = 0.0;
+        seq[k] = -1;
+    }
+}
+
+__global__ void k_node_load_seq(int64_t n, const int64_t *__restrict__ dof, const int64_t *__restrict__ sq,
+                                int64_t n_dof, long long *seq, int *err) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t d = dof[k];
+        if (d < 0 || d >= n_dof) {
+            atomicOr(err, ERR_DOF_RANGE);
+            continue;
+        }
+        atomicMax(&seq[d], (long long)sq[k]);
+    }
+}
+
+__global__ void k_node_load_write(int64_t n, const int64_t *__restrict__ dof, const int64_t *__restrict__ sq,
+                                  const double *__restrict__ val, int64_t n_dof,
+                                  const long long *__restrict__ seq, double *F) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t d = dof[k];
+        if (d < 0 || d >= n_dof) continue;
+        if (seq[d] == sq[k]) F[d] = val[k];
+    }
+}
+
+// Set of each element occurrence (binary search of the set pointers).
+__global__ void k_load_set_of(int64_t n_occ, const int64_t *__restrict__ set_ptr, int64_t n_sets,
+                              int32_t *__restrict__ set_of) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_occ;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = n_sets - 1;
+        while (lo < hi) {
+            int64_t mid = (lo + hi + 1) / 2;
+            if (set_ptr[mid] <= k) lo = mid;
+            else hi = mid - 1;
+        }
+        set_of[k] = (int32_t)lo;
+    }
+}
+
+// sum(elem.area for elem in elements) of loads.py:32, left to right, one thread per
+// set so that the rounding is that of the reference's sequential sum.
+__global__ void k_load_area_total(int64_t n_sets, const int64_t *__restrict__ set_ptr,
+                                  const int64_t *__restrict__ elems, int64_t n_elem,
+                                  const double *__restrict__ coords, const int32_t *__restrict__ conn,
+                                  double *__restrict__ total, int *err) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_sets;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int64_t k = set_ptr[s]; k < set_ptr[s + 1]; ++k) {
+            int64_t e = elems[k];
+            if (e < 0 || e >= n_elem) {
+                atomicOr(err, ERR_ELEM_RANGE);
+                continue;
+            }
+            acc = __dadd_rn(acc, tri_area(load_tri(coords, conn, e)));
+        }
+        total[s] = acc;
+    }
+}
+
+template <bool WRITE>
+__global__ void k_element_loads(int64_t n_occ, const int32_t *__restrict__ set_of,
+                                const int64_t *__restrict__ elems, const double *__restrict__ set_val,
+                                const int32_t *__restrict__ set_dim, const double *__restrict__ total,
+                                int64_t seq_base, int D, int64_t n_elem,
+                                const double *__restrict__ coords, const int32_t *__restrict__ conn,
+                                long long *seq, double *F, int *err) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_occ;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t e = elems[k];
+        if (e < 0 || e >= n_elem) continue;
+        int s = set_of[k];
+        int dm = set_dim[s];
+        if (dm < 1 || dm > D) {
+            atomicOr(err, ERR_DOF_RANGE);
+            continue;
+        }
+        double f[3] = {0, 0, 0}, per = 0.0;
+        if (WRITE) {
+            Tri t = load_tri(coords, conn, e);
+            node_factors(t, f);
+            per = dvd(mul(set_val[s], tri_area(t)), total[s]);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            int64_t dof = (int64_t)conn[3 * e + p] * D + (dm - 1);
+            long long sq = seq_base + 3 * k + p;
+            if (!WRITE) atomicMax(&seq[dof], sq);
+            else if (seq[dof] == sq) F[dof] = mul(per, f[p]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Dirichlet elimination
+
+__global__ void k_bc_map(int64_t n_bc, const int64_t *__restrict__ dof, int64_t n_dof,
+                         int32_t *bc_of_dof, int *err) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_bc;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t d = dof[k];
+        if (d < 0 || d >= n_dof) {
+            atomicOr(err, ERR_DOF_RANGE);
+            continue;
+        }
+        bc_of_dof[d] = (int32_t)k;
+    }
+}
+
+// A = K with every constrained row and column replaced by the identity's.
+template <int D>
+__global__ void k_eliminate(int64_t nnzb, const int32_t *__restrict__ blk_row,
+                            const int32_t *__restrict__ blk_col, const int32_t *__restrict__ bc_of_dof,
+                            const double *__restrict__ kval, double *__restrict__ aval,
+                            float *__restrict__ aval32) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nnzb;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        int r = blk_row[s], m = blk_col[s];
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = 0; b < D; ++b) {
+                int64_t rd = (int64_t)r * D + a, cd = (int64_t)m * D + b;
+                double v = kval[s * D * D + a * D + b];
+                if (bc_of_dof[rd] >= 0 || bc_of_dof[cd] >= 0) v = (rd == cd) ? 1.0 : 0.0;
+                aval[s * D * D + a * D + b] = v;
+                aval32[s * D * D + a * D + b] = (float)v;
+            }
+    }
+}
+
+// FP32 copy of A in difference form for the mixed solver: every block keeps its
+// value except the diagonal one, which becomes the block row sum S_r = sum_m A_rm
+// (summed in FP64).  Then (A x)_r = sum_{m != r} A_rm (x_m - x_r) + S_r x_r.
+template <int D>
+__global__ void k_diff_form32(int64_t n_nodes, const int32_t *__restrict__ blk_ptr,
+                              const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
+                              float *__restrict__ aval32) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        double S[D * D];
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) S[k] = 0.0;
+        int diag = -1;
+        for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
+            if (blk_col[s] == (int)r) diag = s;
+#pragma unroll
+            for (int k = 0; k < D * D; ++k) S[k] += aval[(int64_t)s * D * D + k];
+        }
+        if (diag >= 0)
+#pragma unroll
+            for (int k = 0; k < D * D; ++k) aval32[(int64_t)diag * D * D + k] = (float)S[k];
+    }
+}
+
+// b = F - K[:, c] g on free rows, b = g on constrained rows.
+template <int D>
+__global__ void k_eliminated_rhs(int64_t n_nodes, const int32_t *__restrict__ blk_ptr,
+                                 const int32_t *__restrict__ blk_col, const int32_t *__restrict__ bc_of_dof,
+                                 const double *__restrict__ bc_val, const double *__restrict__ kval,
+                                 const double *__restrict__ F, double *__restrict__ b) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
+         r += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            int64_t rd = r * D + a;
+            int k = bc_of_dof[rd];
+            if (k >= 0) {
+                b[rd] = bc_val[k];
+                continue;
+            }
+            double acc = F[rd];
+            for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
+                int m = blk_col[s];
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    int kc = bc_of_dof[(int64_t)m * D + c];
+                    if (kc >= 0) acc -= kval[(int64_t)s * D * D + a * D + c] * bc_val[kc];
+                }
+            }
+            b[rd] = acc;
+        }
+    }
+}
+
+__device__ __forceinline__ int find_col(const int32_t *__restrict__ cols, int lo, int hi, int key) {
+    // first index in [lo, hi) with cols[idx] == key, or -1
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (cols[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Inverse of every diagonal block of A (node-block Jacobi).
+template <int D>
+__global__ void k_block_jacobi(int64_t n_nodes, const int32_t *__restrict__ blk_ptr,
+                               const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
+                               double *__restrict__ dinv, float *__restrict__ dinv32, int *err) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        int lo = blk_ptr[r], hi = blk_ptr[r + 1];
+        int s = find_col(blk_col, lo, hi, (int)r);
+        bool found = s < hi && blk_col[s] == (int)r;
+        if (D == 1) {
+            double v = found ? aval[s] : 0.0;
+            double inv = 1.0 / v;
+            if (!found || v == 0.0 || !isfinite(inv)) {
+                atomicOr(err, ERR_SINGULAR_BLOCK);
+                inv = 0.0;
+            }
+            dinv[r] = inv;
+            dinv32[r] = (float)inv;
+        } else {
+            double a = 0, b = 0, c = 0, d = 0;
+            if (found) {
+                a = aval[(int64_t)s * 4];
+                b = aval[(int64_t)s * 4 + 1];
+                c = aval[(int64_t)s * 4 + 2];
+                d = aval[(int64_t)s * 4 + 3];
+            }
+            double det = a * d - b * c;
+            double id = 1.0 / det;
+            double i00 = d * id, i01 = -b * id, i10 = -c * id, i11 = a * id;
+            if (!found || det == 0.0 || !isfinite(id)) {
+                atomicOr(err, ERR_SINGULAR_BLOCK);
+                i00 = i01 = i10 = i11 = 0.0;
+            }
+            dinv[r * 4] = i00;
+            dinv[r * 4 + 1] = i01;
+            dinv[r * 4 + 2] = i10;
+            dinv[r * 4 + 3] = i11;
+            dinv32[r * 4] = (float)i00;
+            dinv32[r * 4 + 1] = (float)i01;
+            dinv32[r * 4 + 2] = (float)i10;
+            dinv32[r * 4 + 3] = (float)i11;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- exports
+// Augmented CSR of create_matrix: DOF row (r, a) holds the d*deg(r) block columns in
+// order, then its multiplier column n_dof + k if the DOF is constrained; multiplier row
+// k holds column dof_k.  Row lengths first, then a scan, then the fill.
+
+__global__ void k_aug_row_len(int64_t n_rows_dof, int D, const int32_t *__restrict__ blk_ptr,
+                              const int32_t *__restrict__ bc_of_dof, int64_t n_bc, int64_t n_rows,
+                              int32_t *__restrict__ len) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < n_rows_dof) {
+            int64_t r = i / D;
+            len[i] = D * (blk_ptr[r + 1] - blk_ptr[r]) + (bc_of_dof && bc_of_dof[i] >= 0 ? 1 : 0);
+        } else {
+            len[i] = 1;
+        }
+    }
+}
+
+// transpose = 1: write the value of (col, row) in place of (row, col) -- CSC of a
+// matrix whose pattern is symmetric.
+__global__ void k_aug_fill(int64_t n_rows_dof, int D, int64_t n_dof, const int32_t *__restrict__ blk_ptr,
+                           const int32_t *__restrict__ blk_col, const double *__restrict__ val,
+                           const int32_t *__restrict__ bc_of_dof, const int64_t *__restrict__ bc_dof,
+                           int64_t n_rows, const int32_t *__restrict__ row_off, int transpose,
+                           int32_t *__restrict__ indices, double *__restrict__ data, int *err) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t o = row_off[i];
+        if (i < n_rows_dof) {
+            int64_t r = i / D;
+            int a = (int)(i - r * D);
+            for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
+                int m = blk_col[s];
+                int st = s;
+                if (transpose) {
+                    int lo = blk_ptr[m], hi = blk_ptr[m + 1];
+                    st = find_col(blk_col, lo, hi, (int)r);
+                    if (st >= hi || blk_col[st] != (int)r) {
+                        atomicOr(err, ERR_PATTERN);
+                        st = s;
+                    }
+                }
+                for (int b = 0; b < D; ++b) {
+                    indices[o] = m * D + b;
+                    data[o] = transpose ? val[(int64_t)st * D * D + b * D + a]
+                                        : val[(int64_t)st * D * D + a * D + b];
+                    ++o;
+                }
+            }
+            if (bc_of_dof && bc_of_dof[i] >= 0) {
+                indices[o] = (int32_t)(n_dof + bc_of_dof[i]);
+                data[o] = 1.0;
+            }
+        } else {
+            int64_t k = i - n_dof;
+            indices[o] = (int32_t)bc_dof[k];
+            data[o] = 1.0;
+        }
+    }
+}
+
+int sync_err(fe_handle_s *h) {
+    FE_CUDA(cudaMemcpyAsync(h->err_host, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    return FE_OK;
+}
+
+}  // namespace
+
+int check_error_word(fe_handle_s *h, const char *where) {
+    FE_CHECK(sync_err(h));
+    int e = *h->err_host;
+    if (!e) return FE_OK;
+    FE_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
+    std::string msg = std::string(where) + ":";
+    if (e & ERR_CONN_RANGE) msg += " connectivity index out of range;";
+    if (e & ERR_DOF_RANGE) msg += " load/condition DOF or dimension out of range;";
+    if (e & ERR_ELEM_RANGE) msg += " element index out of range;";
+    if (e & ERR_NONFINITE) msg += " non-finite element value (degenerate element or bad material);";
+    if (e & ERR_SINGULAR_BLOCK) msg += " singular diagonal block (node without stiffness);";
+    if (e & ERR_PATTERN) msg += " inconsistent pattern;";
+    set_error(msg);
+    if (e & ERR_NONFINITE) return FE_NONFINITE;
+    if (e & ERR_SINGULAR_BLOCK) return FE_BREAKDOWN;
+    return FE_BAD_INPUT;
+}
+
+int validate_mesh(fe_handle_s *h) {
+    DBuf<int32_t> mx;
+    FE_CHECK(dalloc(mx, 1));
+    int init = -1;
+    FE_CUDA(cudaMemcpyAsync(mx.p, &init, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    int64_t n3 = h->n_elem * 3;
+    if (n3 > 0) {
+        k_validate_conn<<<grid_for(n3), kThreads, 0, h->stream>>>(h->conn.p, n3, h->n_nodes, h->err.p, mx.p);
+        FE_LAUNCH_CHECK();
+    }
+    int m = -1;
+    FE_CUDA(cudaMemcpyAsync(&m, mx.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    int st = check_error_word(h, "fe_mesh_create");
+    dfree(mx);
+    h->max_node = m;
+    return st;
+}
+
+int build_pattern(fe_handle_s *h) {
+    if (h->pattern_ready) return FE_OK;
+    cudaStream_t s = h->stream;
+    int64_t n = h->n_nodes, n3 = h->n_elem * 3;
+    FE_CHECK(dalloc(h->counts, (size_t)n + 1));
+    FE_CHECK(dalloc(h->inc_ptr, (size_t)n + 1));
+    FE_CHECK(dalloc(h->inc, (size_t)std::max<int64_t>(n3, 1)));
+    FE_CHECK(dalloc(h->cand, (size_t)std::max<int64_t>(3 * n3, 1)));
+    FE_CUDA(cudaMemsetAsync(h->counts.p, 0, (n + 1) * sizeof(int32_t), s));
+    if (n3 > 0) {
+        k_count_incidence<<<grid_for(n3), kThreads, 0, s>>>(h->conn.p, n3, h->counts.p);
+        FE_LAUNCH_CHECK();
+    }
+    int64_t tot = 0;
+    FE_CHECK(exclusive_scan_i32(h->counts.p, h->inc_ptr.p, n, &tot, h->scan_tmp, s));
+    FE_CUDA(cudaMemsetAsync(h->counts.p, 0, (n + 1) * sizeof(int32_t), s));
+    if (n3 > 0) {
+        k_fill_incidence<<<grid_for(n3), kThreads, 0, s>>>(h->conn.p, n3, h->inc_ptr.p, h->counts.p, h->inc.p);
+        FE_LAUNCH_CHECK();
+    }
+    k_node_neighbours<<<grid_for(n), kThreads, 0, s>>>(n, h->conn.p, h->inc_ptr.p, h->inc.p, h->cand.p,
+                                                        h->counts.p);
+    FE_LAUNCH_CHECK();
+    FE_CHECK(dalloc(h->blk_ptr, (size_t)n + 1));
+    int64_t nnzb = 0;
+    FE_CHECK(exclusive_scan_i32(h->counts.p, h->blk_ptr.p, n, &nnzb, h->scan_tmp, s));
+    FE_CHECK(dalloc(h->blk_col, (size_t)std::max<int64_t>(nnzb, 1)));
+    FE_CHECK(dalloc(h->blk_row, (size_t)std::max<int64_t>(nnzb, 1)));
+    k_write_pattern<<<grid_for(n), kThreads, 0, s>>>(n, h->inc_ptr.p, h->cand.p, h->blk_ptr.p, h->blk_col.p,
+                                                      h->blk_row.p);
+    FE_LAUNCH_CHECK();
+    h->nnzb = nnzb;
+    dfree(h->cand);
+    h->pattern_ready = true;
+    return FE_OK;
+}
+
+int assemble_stiffness(fe_handle_s *h) {
+    cudaStream_t s = h->stream;
+    const int D = h->dim, NL = 3 * D;
+    FE_CHECK(dalloc(h->ke, (size_t)std::max<int64_t>(h->n_elem * NL * NL, 1)));
+    if (h->n_elem > 0) {
+        int g = grid_for(h->n_elem, kElemBlock, 152 * 64);
+        if (h->kind == FE_KIND_ELASTIC_TRI)
+            k_elastic_ke<<<g, kElemBlock, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->E.p, h->nu.p, h->thick.p,
+                                                  h->plane == FE_PLANE_STRAIN, h->ke.p, h->err.p);
+        else
+            k_magnetic_ke<<<g, kElemBlock, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->mu.p, h->ke.p, h->err.p);
+        FE_LAUNCH_CHECK();
+    }
+    FE_CHECK(dalloc(h->kval, (size_t)std::max<int64_t>(h->nnzb * D * D, 1)));
+    if (h->nnzb > 0) {
+        int g = grid_for(h->nnzb, kThreads, 152 * 64);
+        if (D == 2)
+            k_reduce_stiffness<2><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p,
+                                                         h->inc.p, h->conn.p, h->ke.p, h->kval.p);
+        else
+            k_reduce_stiffness<1><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p,
+                                                         h->inc.p, h->conn.p, h->ke.p, h->kval.p);
+        FE_LAUNCH_CHECK();
+    }
+    h->k_ready = true;
+    return FE_OK;
+}
+
+int assemble_mass(fe_handle_s *h) {
+    if (h->kind != FE_KIND_ELASTIC_TRI || !h->have_rho) {
+        set_error("mass matrices need elasticity elements with a mass density");
+        return FE_NOT_READY;
+    }
+    cudaStream_t s = h->stream;
+    FE_CHECK(dalloc(h->me_scale, (size_t)std::max<int64_t>(h->n_elem, 1)));
+    if (h->n_elem > 0) {
+        k_mass_scale<<<grid_for(h->n_elem), kThreads, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->rho.p,
+                                                              h->thick.p, h->me_scale.p);
+        FE_LAUNCH_CHECK();
+    }
+    FE_CHECK(dalloc(h->mval, (size_t)std::max<int64_t>(h->nnzb * 4, 1)));
+    if (h->nnzb > 0) {
+        k_reduce_mass<<<grid_for(h->nnzb, kThreads, 152 * 64), kThreads, 0, s>>>(
+            h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p, h->inc.p, h->conn.p, h->me_scale.p, h->mval.p);
+        FE_LAUNCH_CHECK();
+    }
+    h->m_ready = true;
+    return FE_OK;
+}
+
+int assemble_loads(fe_handle_s *h) {
+    cudaStream_t s = h->stream;
+    FE_CHECK(dalloc(h->F, (size_t)std::max<int64_t>(h->n_dof, 1)));
+    FE_CHECK(dalloc(h->load_seq, (size_t)std::max<int64_t>(h->n_dof, 1)));
+    k_init_loads<<<grid_for(h->n_dof), kThreads, 0, s>>>(h->n_dof, h->F.p, h->load_seq.p);
+    FE_LAUNCH_CHECK();
+    if (h->n_node_loads > 0) {
+        k_node_load_seq<<<grid_for(h->n_node_loads), kThreads, 0, s>>>(h->n_node_loads, h->nl_dof.p, h->nl_seq.p,
+                                                                       h->n_dof, h->load_seq.p, h->err.p);
+        FE_LAUNCH_CHECK();
+    }
+    if (h->n_load_elems > 0) {
+        FE_CHECK(dalloc(h->ls_of_occ, (size_t)h->n_load_elems));
+        FE_CHECK(dalloc(h->ls_area_total, (size_t)h->n_load_sets));
+        k_load_set_of<<<grid_for(h->n_load_elems), kThreads, 0, s>>>(h->n_load_elems, h->ls_ptr.p, h->n_load_sets,
+                                                                     h->ls_of_occ.p);
+        FE_LAUNCH_CHECK();
+        k_load_area_total<<<grid_for(h->n_load_sets, 32), 32, 0, s>>>(h->n_load_sets, h->ls_ptr.p, h->ls_elems.p,
+                                                                      h->n_elem, h->coords.p, h->conn.p,
+                                                                      h->ls_area_total.p, h->err.p);
+        FE_LAUNCH_CHECK();
+        k_element_loads<false><<<grid_for(h->n_load_elems), kThreads, 0, s>>>(
+            h->n_load_elems, h->ls_of_occ.p, h->ls_elems.p, h->ls_val.p, h->ls_dim.p, h->ls_area_total.p,
+            h->load_seq_base, h->dim, h->n_elem, h->coords.p, h->conn.p, h->load_seq.p, h->F.p, h->err.p);
+        FE_LAUNCH_CHECK();
+    }
+    if (h->n_node_loads > 0) {
+        k_node_load_write<<<grid_for(h->n_node_loads), kThreads, 0, s>>>(
+            h->n_node_loads, h->nl_dof.p, h->nl_seq.p, h->nl_val.p, h->n_dof, h->load_seq.p, h->F.p);
+        FE_LAUNCH_CHECK();
+    }
+    if (h->n_load_elems > 0) {
+        k_element_loads<true><<<grid_for(h->n_load_elems), kThreads, 0, s>>>(
+            h->n_load_elems, h->ls_of_occ.p, h->ls_elems.p, h->ls_val.p, h->ls_dim.p, h->ls_area_total.p,
+            h->load_seq_base, h->dim, h->n_elem, h->coords.p, h->conn.p, h->load_seq.p, h->F.p, h->err.p);
+        FE_LAUNCH_CHECK();
+    }
+    h->f_ready = true;
+    return FE_OK;
+}
+
+int apply_dirichlet(fe_handle_s *h) {
+    cudaStream_t s = h->stream;
+    const int D = h->dim;
+    FE_CHECK(dalloc(h->bc_of_dof, (size_t)std::max<int64_t>(h->n_dof, 1)));
+    FE_CUDA(cudaMemsetAsync(h->bc_of_dof.p, 0xff, h->n_dof * sizeof(int32_t), s));
+    if (h->n_bc > 0) {
+        k_bc_map<<<grid_for(h->n_bc), kThreads, 0, s>>>(h->n_bc, h->bc_dof.p, h->n_dof, h->bc_of_dof.p, h->err.p);
+        FE_LAUNCH_CHECK();
+    }
+    size_t nv = (size_t)std::max<int64_t>(h->nnzb * D * D, 1);
+    FE_CHECK(dalloc(h->aval, nv));
+    FE_CHECK(dalloc(h->aval32, nv));
+    FE_CHECK(dalloc(h->b, (size_t)std::max<int64_t>(h->n_dof, 1)));
+    FE_CHECK(dalloc(h->dinv, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
+    FE_CHECK(dalloc(h->dinv32, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
+    int gs = grid_for(h->nnzb, kThreads, 152 * 64), gn = grid_for(h->n_nodes, kThreads, 152 * 64);
+    if (D == 2) {
+        if (h->nnzb > 0)
+            k_eliminate<2><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
+                                                   h->aval.p, h->aval32.p);
+        k_diff_form32<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->aval32.p);
+        k_eliminated_rhs<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
+                                                    h->bc_val.p, h->kval.p, h->F.p, h->b.p);
+        k_block_jacobi<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
+                                                  h->dinv32.p, h->err.p);
+    } else {
+        if (h->nnzb > 0)
+            k_eliminate<1><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
+                                                   h->aval.p, h->aval32.p);
+        k_diff_form32<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->aval32.p);
+        k_eliminated_rhs<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
+                                                    h->bc_val.p, h->kval.p, h->F.p, h->b.p);
+        k_block_jacobi<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
+                                                  h->dinv32.p, h->err.p);
+    }
+    FE_LAUNCH_CHECK();
+    h->sys_ready = true;
+    return FE_OK;
+}
+
+int element_node_factors(fe_handle_s *h, int64_t n, const int64_t *elems_dev, double *out_dev) {
+    if (n <= 0) return FE_OK;
+    k_node_factors<<<grid_for(n), kThreads, 0, h->stream>>>(n, elems_dev, h->n_elem, h->coords.p, h->conn.p,
+                                                            out_dev, h->err.p);
+    FE_LAUNCH_CHECK();
+    return check_error_word(h, "fe_element_node_factors");
+}
+
+// Shapes follow scipy's inference from the largest index present
+// (analysis.py:661 and :401): the augmented matrix spans n_dof + n_bc when there is a
+// condition, otherwise the DOFs of the largest node any element uses.
+int export_sizes(fe_handle_s *h, int which, int64_t *nrows, int64_t *ncols, int64_t *nnz) {
+    const int D = h->dim;
+    int64_t elem_dofs = (int64_t)(h->max_node + 1) * D;
+    int64_t dof_nnz = h->nnzb * D * D;  // every stored block expands to D*D entries
+    if (which == FE_MAT_K_AUGMENTED) {
+        int64_t n = h->n_bc > 0 ? h->n_dof + h->n_bc : elem_dofs;
+        *nrows = *ncols = n;
+        *nnz = dof_nnz + 2 * h->n_bc;
+    } else if (which == FE_MAT_K_CSC || which == FE_MAT_M_CSC) {
+        *nrows = *ncols = elem_dofs;
+        *nnz = dof_nnz;
+    } else {
+        set_error("unknown matrix selector");
+        return FE_BAD_INPUT;
+    }
+    return FE_OK;
+}
+
+int export_csr(fe_handle_s *h, int which, int64_t *indptr_host, int32_t *indices_host, double *data_host) {
+    cudaStream_t s = h->stream;
+    const int D = h->dim;
+    int64_t nrows, ncols, nnz;
+    FE_CHECK(export_sizes(h, which, &nrows, &ncols, &nnz));
+    const double *val = nullptr;
+    bool aug = which == FE_MAT_K_AUGMENTED;
+    if (which == FE_MAT_M_CSC) {
+        if (!h->m_ready) {
+            set_error("mass matrix not assembled");
+            return FE_NOT_READY;
+        }
+        val = h->mval.p;
+    } else {
+        if (!h->k_ready) {
+            set_error("stiffness matrix not assembled");
+            return FE_NOT_READY;
+        }
+        val = h->kval.p;
+    }
+    if (aug && h->n_bc > 0 && !h->bc_of_dof.p) {
+        set_error("conditions not applied");
+        return FE_NOT_READY;
+    }
+    int64_t n_rows_dof = aug && h->n_bc > 0 ? h->n_dof : nrows;
+    DBuf<int32_t> len, off, idx;
+    DBuf<double> dat;
+    FE_CHECK(dalloc(len, (size_t)nrows + 1));
+    FE_CHECK(dalloc(off, (size_t)nrows + 1));
+    FE_CHECK(dalloc(idx, (size_t)std::max<int64_t>(nnz, 1)));
+    FE_CHECK(dalloc(dat, (size_t)std::max<int64_t>(nnz, 1)));
+    const int32_t *bcmap = aug && h->n_bc > 0 ? h->bc_of_dof.p : nullptr;
+    if (nrows > 0) {
+        k_aug_row_len<<<grid_for(nrows), kThreads, 0, s>>>(n_rows_dof, D, h->blk_ptr.p, bcmap, h->n_bc, nrows,
+                                                           len.p);
+        FE_LAUNCH_CHECK();
+    }
+    int64_t total = 0;
+    FE_CHECK(exclusive_scan_i32(len.p, off.p, nrows, &total, h->scan_tmp, s));
+    if (total != nnz) {
+        dfree(len), dfree(off), dfree(idx), dfree(dat);
+        set_error("export size mismatch");
+        return FE_BAD_INPUT;
+    }
+    if (nrows > 0) {
+        k_aug_fill<<<grid_for(nrows), kThreads, 0, s>>>(n_rows_dof, D, h->n_dof, h->blk_ptr.p, h->blk_col.p, val,
+                                                        bcmap, h->bc_dof.p, nrows, off.p, aug ? 0 : 1, idx.p,
+                                                        dat.p, h->err.p);
+        FE_LAUNCH_CHECK();
+    }
+    std::vector<int32_t> off_h((size_t)nrows + 1);
+    FE_CUDA(cudaMemcpyAsync(off_h.data(), off.p, (nrows + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (nnz > 0) {
+        FE_CUDA(cudaMemcpyAsync(indices_host, idx.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaMemcpyAsync(data_host, dat.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    int st = check_error_word(h, "fe_export_csr");
+    for (int64_t i = 0; i <= nrows; ++i) indptr_host[i] = off_h[i];
+    dfree(len), dfree(off), dfree(idx), dfree(dat);
+    return st;
+}
+
+int export_element_matrices(fe_handle_s *h, int which, double *out_host) {
+    const int NL = 3 * h->dim;
+    if (which == FE_ASSEMBLE_K) {
+        if (!h->k_ready) {
+            set_error("stiffness not assembled");
+            return FE_NOT_READY;
+        }
+        FE_CUDA(cudaMemcpyAsync(out_host, h->ke.p, h->n_elem * NL * NL * sizeof(double), cudaMemcpyDeviceToHost,
+                                h->stream));
+        FE_CUDA(cudaStreamSynchronize(h->stream));
+        return FE_OK;
+    }
+    if (which == FE_ASSEMBLE_M) {
+        if (!h->m_ready) {
+            set_error("mass not assembled");
+            return FE_NOT_READY;
+        }
+        std::vector<double> sc((size_t)h->n_elem);
+        FE_CUDA(cudaMemcpyAsync(sc.data(), h->me_scale.p, h->n_elem * sizeof(double), cudaMemcpyDeviceToHost,
+                                h->stream));
+        FE_CUDA(cudaStreamSynchronize(h->stream));
+        static const double P[36] = {2, 0, 1, 0, 1, 0, 0, 2, 0, 1, 0, 1, 1, 0, 2, 0, 1, 0,
+                                     0, 1, 0, 2, 0, 1, 1, 0, 1, 0, 2, 0, 0, 1, 0, 1, 0, 2};
+        for (int64_t e = 0; e < h->n_elem; ++e)
+            for (int k = 0; k < 36; ++k) out_host[e * 36 + k] = sc[e] * P[k];
+        return FE_OK;
+    }
+    set_error("unknown element matrix selector");
+    return FE_BAD_INPUT;
+}
+
+}  // namespace fe

@@ -1,0 +1,209 @@
+// Internal state of one assembly-and-solve handle and the helpers shared by the
+// translation units of libfe_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/fe_gb300.h"
+
+namespace fe {
+
+// ---------------------------------------------------------------- error plumbing
+
+void set_error(const std::string &msg);
+
+#define FE_CUDA(...)                                                                   \
+    do {                                                                               \
+        cudaError_t _e = (__VA_ARGS__);                                                \
+        if (_e != cudaSuccess) {                                                       \
+            ::fe::set_error(std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(_e)); \
+            return FE_CUDA_ERR;                                                        \
+        }                                                                              \
+    } while (0)
+
+#define FE_CHECK(...)                                \
+    do {                                             \
+        int _s = (__VA_ARGS__);                      \
+        if (_s != FE_OK) return _s;                  \
+    } while (0)
+
+#define FE_LAUNCH_CHECK() FE_CUDA(cudaGetLastError())
+
+// device error word bits (set by kernels, read by the host after a step)
+enum : int {
+    ERR_CONN_RANGE = 1,      // connectivity index outside [0, n_nodes)
+    ERR_DOF_RANGE = 2,       // load / condition DOF outside [0, n_dof)
+    ERR_ELEM_RANGE = 4,      // element index outside [0, n_elem)
+    ERR_NONFINITE = 8,       // NaN / Inf met
+    ERR_SINGULAR_BLOCK = 16, // zero determinant in a diagonal block
+    ERR_PATTERN = 32,        // a block expected in the pattern was not found
+};
+
+constexpr int kThreads = 256;
+
+inline int grid_for(int64_t n, int threads = kThreads, int cap = 152 * 16) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+// ---------------------------------------------------------------- buffers
+
+template <typename T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+};
+
+template <typename T>
+int dalloc(DBuf<T> &b, size_t n) {
+    if (b.p && b.n >= n) return FE_OK;
+    if (b.p) {
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.n = 0;
+    }
+    if (n == 0) return FE_OK;
+    FE_CUDA(cudaMalloc((void **)&b.p, n * sizeof(T)));
+    b.n = n;
+    return FE_OK;
+}
+
+template <typename T>
+void dfree(DBuf<T> &b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+}
+
+// PCG scalars live in device memory so that every decision of the iteration is
+// taken on the device (no host round trip per iteration).
+struct PcgScalars {
+    double rz;        // r.z of the current iterate
+    double pq;        // p.Ap
+    double rr;        // r.r
+    double bb;        // b.b (of the system the loop solves)
+    double alpha, beta;
+    double tol2;      // stop when rr <= tol2 * bb
+    double cheb_theta, cheb_delta;   // Chebyshev interval centre / half-width
+    int iter;         // iterations done in this loop
+    int max_iter;
+    int done;         // 1: converged or stopped, remaining launches return at once
+    int status;       // FE_OK / FE_MAXITER / FE_BREAKDOWN / FE_NONFINITE
+    unsigned int ticket[8];          // last-block counters, one per reducing kernel
+    double hist_alpha[64], hist_beta[64];   // first iterations, for the Lanczos estimate
+};
+
+struct SolverWork {
+    // FP64 vectors (n_dof each): solution, residual, preconditioned residual,
+    // direction, A p, a second z for Chebyshev ping-pong, the Chebyshev update d
+    DBuf<double> x, r, z, p, q, t, dch;
+    // FP32 vectors of the mixed inner solve (d32 is its solution, the correction)
+    DBuf<float> r32, z32, p32, q32, d32, zc32, c32;
+    DBuf<double> partials;   // per-block partial sums of the reductions
+    DBuf<PcgScalars> sc;
+    PcgScalars *sc_host = nullptr;       // pinned mirror
+    double lmax[2] = {0.0, 0.0};         // largest eigenvalue of D^-1 A, [FP64, FP32]
+    int lanes[2] = {0, 0};               // autotuned SpMV lanes, [FP64, FP32]
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // captured chunk, [FP64, FP32]
+    // what each captured graph was built for
+    struct Key {
+        int k = -1, G = -1, chunk = -1;
+        const void *x = nullptr;
+        double theta = 0, delta = 0;
+    } key[2];
+};
+
+}  // namespace fe
+
+struct fe_handle_s {
+    int kind = 0;            // FE_KIND_*
+    int dim = 0;             // DOF per node
+    int64_t n_nodes = 0, n_elem = 0, n_dof = 0;
+    int32_t max_node = -1;   // largest node index used by an element
+    cudaStream_t stream = nullptr;
+    cudaEvent_t events[8] = {};
+
+    // inputs
+    fe::DBuf<double> coords;      // [n_nodes][2]
+    fe::DBuf<int32_t> conn;       // [n_elem][3]
+    fe::DBuf<double> E, nu, thick, rho, mu;
+    int plane = 0;
+    bool have_material = false, have_rho = false;
+
+    // loads
+    int64_t n_node_loads = 0;
+    fe::DBuf<int64_t> nl_dof, nl_seq;
+    fe::DBuf<double> nl_val;
+    int64_t n_load_sets = 0, n_load_elems = 0, load_seq_base = 0;
+    fe::DBuf<int64_t> ls_ptr, ls_elems;
+    fe::DBuf<double> ls_val, ls_area_total;
+    fe::DBuf<int32_t> ls_dim, ls_of_occ;
+
+    // Dirichlet conditions
+    int64_t n_bc = 0;
+    fe::DBuf<int64_t> bc_dof;
+    fe::DBuf<double> bc_val;
+    fe::DBuf<int32_t> bc_of_dof;  // [n_dof] multiplier index or -1
+
+    // pattern: node-block CSR
+    bool pattern_ready = false;
+    fe::DBuf<int32_t> inc_ptr, inc;       // node -> (element*3 + local) incidence, sorted
+    int64_t nnzb = 0;
+    fe::DBuf<int32_t> blk_ptr, blk_col, blk_row;
+    fe::DBuf<int32_t> cand;               // scratch for the pattern build
+    fe::DBuf<int32_t> counts;             // scratch counts
+    fe::DBuf<int64_t> scan_tmp;
+
+    // values
+    bool k_ready = false, m_ready = false, f_ready = false, sys_ready = false;
+    fe::DBuf<double> ke;                  // [n_elem][(3d)^2]
+    fe::DBuf<double> me_scale;            // [n_elem] rho*A*t/12
+    fe::DBuf<double> kval, mval;          // [nnzb][d][d] full K / M
+    fe::DBuf<double> aval;                // eliminated K (FP64)
+    fe::DBuf<float> aval32;               // eliminated K (FP32, difference form)
+    fe::DBuf<double> dinv;                // [n_nodes][d][d] inverse diagonal blocks
+    fe::DBuf<float> dinv32;
+    fe::DBuf<double> F;                   // loads [n_dof]
+    fe::DBuf<double> b;                   // eliminated right-hand side [n_dof]
+    fe::DBuf<long long> load_seq;         // [n_dof] winning load sequence
+    fe::DBuf<double> lambda;              // [n_bc]
+    fe::DBuf<int> err;                    // device error word
+    int *err_host = nullptr;              // pinned
+    double last_assemble_ms = 0.0;
+    bool have_solution = false;
+
+    fe::SolverWork w;
+};
+
+namespace fe {
+
+// assembly (fe_assembly.cu)
+int build_pattern(fe_handle_s *h);
+int assemble_stiffness(fe_handle_s *h);
+int assemble_mass(fe_handle_s *h);
+int assemble_loads(fe_handle_s *h);
+int apply_dirichlet(fe_handle_s *h);
+int element_node_factors(fe_handle_s *h, int64_t n, const int64_t *elems_dev, double *out_dev);
+int export_sizes(fe_handle_s *h, int which, int64_t *nrows, int64_t *ncols, int64_t *nnz);
+int export_csr(fe_handle_s *h, int which, int64_t *indptr, int32_t *indices, double *data);
+int export_element_matrices(fe_handle_s *h, int which, double *out_host);
+int check_error_word(fe_handle_s *h, const char *where);
+int validate_mesh(fe_handle_s *h);
+
+// scan (fe_scan.cu): exclusive scan of n int32 counts into int32 offsets (n+1 values)
+int exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, int64_t *total,
+                       DBuf<int64_t> &tmp, cudaStream_t s);
+
+// solver (fe_solver.cu)
+int solve(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
+int recover_multipliers(fe_handle_s *h);
+int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);
+int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);
+void release_solver(fe_handle_s *h);
+
+}  // namespace fe

@@ -1,0 +1,1101 @@
+// Preconditioned conjugate gradients on the eliminated system, replacing
+// scipy.sparse.linalg.spsolve in FiniteElementAnalysis.solve
+// (finite_elements/analysis.py:816-830).
+//
+// * SpMV: node-block CSR (d x d blocks), G lanes per block row (G = 1, 2, 4, 8 chosen
+//   by an autotuner), vector loads of blocks (32 B for 2x2 FP64) and of the node
+//   vector (16 B), FP64 or FP32 values.
+// * One PCG iteration is three kernels: q = A p with p.q, the fused update
+//   x += alpha p, r -= alpha q, z = M^-1 r with r.z and r.r, and p = z + beta p.
+//   Each reduction ends in the last block to finish (ticket counter), which sums the
+//   per-block partials in a fixed order and takes the iteration's scalar decisions on
+//   the device, so results are identical run to run and the host never waits inside
+//   the loop.  Chunks of iterations are captured once in a CUDA graph and replayed.
+// * Preconditioner: node-block Jacobi (inverse d x d diagonal blocks), optionally
+//   followed by k-1 Chebyshev steps on D^-1 A; the Chebyshev interval comes from a
+//   Lanczos estimate of the largest eigenvalue built from the first PCG coefficients.
+// * Mixed precision: FP32 SpMV, preconditioner and Krylov vectors, with FP64 kept for
+//   the solution x, the reduction trees, and the refinement step: whenever the FP32
+//   recurrence residual has fallen by a factor 10, the FP64 true residual b - A x
+//   replaces it and the iteration continues along the same search direction
+//   (iterative refinement with reliable updates: the Krylov space is not restarted).
+//   The FP32 SpMV uses the difference form y_r = sum_{m != r} A_rm (x_m - x_r) + S_r x_r,
+//   S_r the block row sum (zero at interior nodes: K annihilates translations), so
+//   FP32 rounding scales with the variation of x between neighbours instead of with
+//   x itself; smooth error modes are no longer swamped by rounding.
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "fe_internal.h"
+
+namespace fe {
+namespace {
+
+constexpr int kVecThreads = 256;
+
+inline int vec_grid(int64_t n_nodes) { return grid_for(n_nodes, kVecThreads, 152 * 8); }
+
+// ---------------------------------------------------------------- reductions
+
+template <int NV>
+__device__ __forceinline__ void block_reduce(double (&v)[NV]) {
+    __shared__ double sh[NV][kVecThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh[k][warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = lane < (int)(blockDim.x >> 5) ? sh[k][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            v[k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// Block partial sums -> partials[k * gridDim.x + block]; the last block to arrive sums
+// them in block order and returns true in every thread of that block, with the totals
+// in thread 0's out[].
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, unsigned int *ticket,
+                                            double (&out)[NV]) {
+    __shared__ bool is_last;
+    block_reduce<NV>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned int t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (unsigned int i = threadIdx.x; i < gridDim.x; i += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += __ldcg(partials + k * gridDim.x + i);
+    block_reduce<NV>(acc);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) out[k] = acc[k];
+        *ticket = 0;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------- node vectors
+
+template <int D, typename T>
+struct NodeVec {
+    T v[D];
+};
+
+template <int D, typename T>
+__device__ __forceinline__ NodeVec<D, T> ld(const T *__restrict__ a, int64_t r) {
+    NodeVec<D, T> o;
+    if constexpr (D == 2 && sizeof(T) == 8) {
+        double2 t = reinterpret_cast<const double2 *>(a)[r];
+        o.v[0] = t.x, o.v[1] = t.y;
+    } else if constexpr (D == 2) {
+        float2 t = reinterpret_cast<const float2 *>(a)[r];
+        o.v[0] = t.x, o.v[1] = t.y;
+    } else {
+        o.v[0] = a[r];
+    }
+    return o;
+}
+
+template <int D, typename T>
+__device__ __forceinline__ void st(T *__restrict__ a, int64_t r, const NodeVec<D, T> &o) {
+    if constexpr (D == 2 && sizeof(T) == 8) {
+        reinterpret_cast<double2 *>(a)[r] = make_double2(o.v[0], o.v[1]);
+    } else if constexpr (D == 2) {
+        reinterpret_cast<float2 *>(a)[r] = make_float2(o.v[0], o.v[1]);
+    } else {
+        a[r] = o.v[0];
+    }
+}
+
+// y = M^-1 x for one node (M^-1 stored row-major per node)
+template <int D, typename T>
+__device__ __forceinline__ NodeVec<D, T> apply_dinv(const T *__restrict__ dinv, int64_t r, const NodeVec<D, T> &x) {
+    NodeVec<D, T> y;
+    if constexpr (D == 2) {
+        if constexpr (sizeof(T) == 8) {
+            const double2 m0 = reinterpret_cast<const double2 *>(dinv)[2 * r];
+            const double2 m1 = reinterpret_cast<const double2 *>(dinv)[2 * r + 1];
+            y.v[0] = m0.x * x.v[0] + m0.y * x.v[1];
+            y.v[1] = m1.x * x.v[0] + m1.y * x.v[1];
+        } else {
+            const float4 m = reinterpret_cast<const float4 *>(dinv)[r];
+            y.v[0] = m.x * x.v[0] + m.y * x.v[1];
+            y.v[1] = m.z * x.v[0] + m.w * x.v[1];
+        }
+    } else {
+        y.v[0] = dinv[r] * x.v[0];
+    }
+    return y;
+}
+
+// ---------------------------------------------------------------- SpMV row kernel
+// Row r of A x, with G lanes of the warp sharing the row.  Blocks are read with
+// 16-byte loads; the node vector x is read as one 16-byte (FP64) or 8-byte (FP32)
+// load per block column.  The sum over the G lanes is a shuffle reduction.
+// FP32 values are stored in difference form (see the header): the diagonal slot holds
+// the block row sum S_r and every other block multiplies x_m - x_r.
+// Every lane of the warp calls this (the shuffles need all 32); a lane whose row is
+// past the end passes valid = false and contributes nothing.
+template <int D, typename T, int G>
+__device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, const int32_t *__restrict__ ptr,
+                                                     const int32_t *__restrict__ col,
+                                                     const T *__restrict__ val, const T *__restrict__ x,
+                                                     int sub) {
+    constexpr bool DIFF = sizeof(T) == 4;
+    NodeVec<D, T> acc, xr;
+#pragma unroll
+    for (int a = 0; a < D; ++a) acc.v[a] = T(0), xr.v[a] = T(0);
+    const int k0 = valid ? ptr[r] : 0, k1 = valid ? ptr[r + 1] : 0;
+    if (DIFF && valid) xr = ld<D, T>(x, r);
+    for (int k = k0 + sub; k < k1; k += G) {
+        const int c = __ldg(col + k);
+        NodeVec<D, T> xv = ld<D, T>(x, c);
+        if (DIFF && c != (int)r) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) xv.v[a] -= xr.v[a];
+        }
+        if constexpr (D == 2) {
+            if constexpr (sizeof(T) == 8) {
+                const double2 b0 = __ldg(reinterpret_cast<const double2 *>(val) + 2 * (int64_t)k);
+                const double2 b1 = __ldg(reinterpret_cast<const double2 *>(val) + 2 * (int64_t)k + 1);
+                acc.v[0] += b0.x * xv.v[0] + b0.y * xv.v[1];
+                acc.v[1] += b1.x * xv.v[0] + b1.y * xv.v[1];
+            } else {
+                const float4 b = __ldg(reinterpret_cast<const float4 *>(val) + k);
+                acc.v[0] += b.x * xv.v[0] + b.y * xv.v[1];
+                acc.v[1] += b.z * xv.v[0] + b.w * xv.v[1];
+            }
+        } else {
+            acc.v[0] += __ldg(val + k) * xv.v[0];
+        }
+    }
+    if constexpr (G > 1) {
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc.v[a] += __shfl_xor_sync(0xffffffffu, acc.v[a], o);
+    }
+    return acc;
+}
+
+// Block rows handled by this thread's group of G lanes: row = global_thread / G,
+// grid-stride.  Every thread runs the same number of trips (rows_padded is a
+// multiple of the stride) so that the warp shuffles always see all 32 lanes.
+#define FE_ROW_LOOP(G)                                                                      \
+    const int sub = threadIdx.x & ((G)-1);                                                  \
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / (G);                         \
+    const int64_t rows_padded = ((n_nodes + groups - 1) / groups) * groups;                 \
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (G); row < rows_padded; row += groups)
+
+// ---------------------------------------------------------------- kernels
+
+// y = A x (timing)
+template <int D, typename T, int G>
+__global__ void __launch_bounds__(kVecThreads)
+k_spmv(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+       const T *__restrict__ val, const T *__restrict__ x, T *__restrict__ y) {
+    FE_ROW_LOOP(G) {
+        const bool valid = row < n_nodes;
+        NodeVec<D, T> v = row_product<D, T, G>(row, valid, ptr, col, val, x, sub);
+        if (valid && sub == 0) st<D, T>(y, row, v);
+    }
+}
+
+// FP64 residual r = b - A x of the eliminated system (x == nullptr: r = b), stored as
+// OUT (double, or float for the mixed solver's residual replacement), and r.r in FP64.
+template <int D, int G, typename OUT>
+__global__ void __launch_bounds__(kVecThreads)
+k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+           const double *__restrict__ val, const double *__restrict__ b, const double *__restrict__ x,
+           OUT *__restrict__ r, double *partials, unsigned int *ticket, double *out) {
+    double lrr = 0.0;
+    FE_ROW_LOOP(G) {
+        const bool valid = row < n_nodes;
+        NodeVec<D, double> v;
+        if (x) {
+            v = row_product<D, double, G>(row, valid, ptr, col, val, x, sub);
+        } else {
+#pragma unroll
+            for (int a = 0; a < D; ++a) v.v[a] = 0.0;
+        }
+        if (valid && sub == 0) {
+            NodeVec<D, double> bv = ld<D, double>(b, row);
+            NodeVec<D, OUT> o;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                bv.v[a] -= v.v[a];
+                lrr += bv.v[a] * bv.v[a];
+                o.v[a] = (OUT)bv.v[a];
+            }
+            st<D, OUT>(r, row, o);
+        }
+    }
+    double loc[1] = {lrr}, tot[1];
+    if (grid_reduce<1>(loc, partials, ticket, tot) && threadIdx.x == 0) *out = tot[0];
+}
+
+// q = A p and p.q; the last block sets alpha = r.z / p.q or stops the loop.
+template <int D, typename T, int G>
+__global__ void __launch_bounds__(kVecThreads)
+k_pcg_spmv(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+           const T *__restrict__ val, const T *__restrict__ p, T *__restrict__ q, double *partials,
+           PcgScalars *sc) {
+    if (sc->done) return;
+    T lt = T(0);
+    FE_ROW_LOOP(G) {
+        const bool valid = row < n_nodes;
+        NodeVec<D, T> y = row_product<D, T, G>(row, valid, ptr, col, val, p, sub);
+        if (valid && sub == 0) {
+            st<D, T>(q, row, y);
+            NodeVec<D, T> pv = ld<D, T>(p, row);
+#pragma unroll
+            for (int a = 0; a < D; ++a) lt += pv.v[a] * y.v[a];
+        }
+    }
+    double loc[1] = {(double)lt}, tot[1];
+    if (grid_reduce<1>(loc, partials, &sc->ticket[0], tot) && threadIdx.x == 0) {
+        double pq = tot[0];
+        sc->pq = pq;
+        if (!isfinite(pq)) {
+            sc->status = FE_NONFINITE;
+            sc->done = 1;
+        } else if (!(pq > 0.0)) {
+            sc->status = FE_BREAKDOWN;
+            sc->done = 1;
+        } else {
+            sc->alpha = sc->rz / pq;
+        }
+    }
+}
+
+// Convergence test, iteration count and beta, once r.z (and r.r) of the new iterate
+// are known.
+__device__ __forceinline__ void finish_iteration(PcgScalars *sc, double rz_new) {
+    int it = sc->iter;
+    if (it < 64) sc->hist_alpha[it] = sc->alpha;
+    sc->iter = it + 1;
+    if (!isfinite(rz_new) || !isfinite(sc->rr)) {
+        sc->status = FE_NONFINITE;
+        sc->done = 1;
+        return;
+    }
+    if (sc->rr <= sc->tol2 * sc->bb) {
+        sc->status = FE_OK;
+        sc->done = 1;
+        return;
+    }
+    if (sc->iter >= sc->max_iter) {
+        sc->status = FE_MAXITER;
+        sc->done = 1;
+        return;
+    }
+    if (!(rz_new > 0.0)) {
+        sc->status = FE_BREAKDOWN;
+        sc->done = 1;
+        return;
+    }
+    sc->beta = rz_new / sc->rz;
+    if (it < 64) sc->hist_beta[it] = sc->beta;
+    sc->rz = rz_new;
+}
+
+// x += alpha p (x in FP64); r -= alpha q; then z = M^-1 r (Jacobi) or, with CHEB,
+// the first Chebyshev term z = d = M^-1 r / theta.  Reduces r.z and r.r.
+template <int D, typename T, bool CHEB>
+__global__ void __launch_bounds__(kVecThreads)
+k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+             const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z, T *__restrict__ dch,
+             double *partials, PcgScalars *sc) {
+    if (sc->done) return;
+    const double alpha = sc->alpha;
+    const T alpha_t = (T)alpha;
+    const T inv_theta = CHEB ? (T)(1.0 / sc->cheb_theta) : T(1);
+    T lrz = T(0), lrr = T(0);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        NodeVec<D, double> xv = ld<D, double>(x, i);
+        NodeVec<D, T> rv = ld<D, T>(r, i), pv = ld<D, T>(p, i), qv = ld<D, T>(q, i);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            xv.v[a] += alpha * (double)pv.v[a];
+            rv.v[a] -= alpha_t * qv.v[a];
+        }
+        st<D, double>(x, i, xv);
+        st<D, T>(r, i, rv);
+        NodeVec<D, T> zv = apply_dinv<D, T>(dinv, i, rv);
+        if (CHEB) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
+            st<D, T>(dch, i, zv);
+        }
+        st<D, T>(z, i, zv);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            lrz += rv.v[a] * zv.v[a];
+            lrr += rv.v[a] * rv.v[a];
+        }
+    }
+    double loc[2] = {(double)lrz, (double)lrr}, tot[2];
+    if (grid_reduce<2>(loc, partials, &sc->ticket[1], tot) && threadIdx.x == 0) {
+        sc->rr = tot[1];
+        if (CHEB) {
+            // r.z comes from the last Chebyshev step; stop here already if r is small.
+            if (!isfinite(tot[1])) {
+                sc->status = FE_NONFINITE;
+                sc->done = 1;
+            } else if (tot[1] <= sc->tol2 * sc->bb) {
+                sc->iter += 1;
+                sc->status = FE_OK;
+                sc->done = 1;
+            }
+        } else {
+            finish_iteration(sc, tot[0]);
+        }
+    }
+}
+
+// One Chebyshev step on D^-1 A z = D^-1 r:
+//   d = c1 d + c2 M^-1 (r - A z_in);   z_out = z_in + d.
+// MODE 0: at the start of a loop (no reduction, runs even when done is set);
+// MODE 1: last step of an iteration (reduces r.z_out, finishes the iteration);
+// MODE 2: intermediate step.
+template <int D, typename T, int G, int MODE>
+__global__ void __launch_bounds__(kVecThreads)
+k_cheb_step(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+            const T *__restrict__ val, const T *__restrict__ dinv, const T *__restrict__ rres,
+            const T *__restrict__ z_in, T *__restrict__ z_out, T *__restrict__ dch, double c1, double c2,
+            double *partials, PcgScalars *sc) {
+    if (MODE != 0 && sc->done) return;
+    T lrz = T(0);
+    FE_ROW_LOOP(G) {
+        const bool valid = row < n_nodes;
+        NodeVec<D, T> az = row_product<D, T, G>(row, valid, ptr, col, val, z_in, sub);
+        if (valid && sub == 0) {
+            NodeVec<D, T> rv = ld<D, T>(rres, row), zv = ld<D, T>(z_in, row), dv = ld<D, T>(dch, row);
+            NodeVec<D, T> res;
+#pragma unroll
+            for (int a = 0; a < D; ++a) res.v[a] = rv.v[a] - az.v[a];
+            NodeVec<D, T> mr = apply_dinv<D, T>(dinv, row, res);
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                dv.v[a] = (T)c1 * dv.v[a] + (T)c2 * mr.v[a];
+                zv.v[a] += dv.v[a];
+                lrz += rv.v[a] * zv.v[a];
+            }
+            st<D, T>(dch, row, dv);
+            st<D, T>(z_out, row, zv);
+        }
+    }
+    if (MODE == 1) {
+        double loc[1] = {(double)lrz}, tot[1];
+        if (grid_reduce<1>(loc, partials, &sc->ticket[2], tot) && threadIdx.x == 0) finish_iteration(sc, tot[0]);
+    }
+}
+
+// p = z + beta p
+template <int D, typename T>
+__global__ void __launch_bounds__(kVecThreads)
+k_pcg_direction(int64_t n_nodes, const T *__restrict__ z, T *__restrict__ p, PcgScalars *sc) {
+    if (sc->done) return;
+    const T beta = (T)sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        NodeVec<D, T> zv = ld<D, T>(z, i), pv = ld<D, T>(p, i);
+#pragma unroll
+        for (int a = 0; a < D; ++a) pv.v[a] = zv.v[a] + beta * pv.v[a];
+        st<D, T>(p, i, pv);
+    }
+}
+
+// Start of a loop, given r: z = M^-1 r (times 1/theta and d = z with CHEB).
+template <int D, typename T, bool CHEB>
+__global__ void __launch_bounds__(kVecThreads)
+k_start_precond(int64_t n_nodes, const T *__restrict__ r, const T *__restrict__ dinv, T *__restrict__ z,
+                T *__restrict__ dch, double theta) {
+    const T inv_theta = CHEB ? (T)(1.0 / theta) : T(1);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        NodeVec<D, T> zv = apply_dinv<D, T>(dinv, i, ld<D, T>(r, i));
+        if (CHEB) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
+            st<D, T>(dch, i, zv);
+        }
+        st<D, T>(z, i, zv);
+    }
+}
+
+// Start of a loop, after z: r.z and r.r, then p = z (fresh start) or, when the loop
+// continues after a residual replacement, p = z + (r.z / r.z_previous) p so that the
+// search direction is kept.  Stops at once if r is already below the tolerance.
+template <int D, typename T, bool CONT>
+__global__ void __launch_bounds__(kVecThreads)
+k_start_finish(int64_t n_nodes, const T *__restrict__ r, const T *__restrict__ z, T *__restrict__ p,
+               double *partials, PcgScalars *sc) {
+    // reduction first (needed for beta), then the direction in a second sweep by the
+    // same threads: r.z over the block partials is only known to the last block, so
+    // with CONT the direction update reads beta from a kernel that runs after this one
+    T lrz = T(0), lrr = T(0);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        NodeVec<D, T> rv = ld<D, T>(r, i), zv = ld<D, T>(z, i);
+        if (!CONT) st<D, T>(p, i, zv);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            lrz += rv.v[a] * zv.v[a];
+            lrr += rv.v[a] * rv.v[a];
+        }
+    }
+    double loc[2] = {(double)lrz, (double)lrr}, tot[2];
+    if (grid_reduce<2>(loc, partials, &sc->ticket[3], tot) && threadIdx.x == 0) {
+        double rz_old = sc->rz;
+        sc->rz = tot[0];
+        sc->rr = tot[1];
+        sc->beta = CONT && rz_old > 0.0 ? tot[0] / rz_old : 0.0;
+        sc->iter = 0;
+        sc->status = FE_OK;
+        sc->done = 0;
+        if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+            sc->status = FE_NONFINITE;
+            sc->done = 1;
+        } else if (tot[1] <= sc->tol2 * sc->bb) {
+            sc->done = 1;
+        } else if (!(tot[0] > 0.0)) {
+            sc->status = FE_BREAKDOWN;
+            sc->done = 1;
+        } else if (sc->max_iter <= 0) {
+            sc->status = FE_MAXITER;
+            sc->done = 1;
+        }
+    }
+}
+
+// p = z + beta p after a residual replacement (beta set by k_start_finish<CONT>),
+// run whether or not the loop is done so the direction stays consistent.
+template <int D, typename T>
+__global__ void __launch_bounds__(kVecThreads)
+k_continue_direction(int64_t n_nodes, const T *__restrict__ z, T *__restrict__ p, const PcgScalars *sc) {
+    const T beta = (T)sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        NodeVec<D, T> zv = ld<D, T>(z, i), pv = ld<D, T>(p, i);
+#pragma unroll
+        for (int a = 0; a < D; ++a) pv.v[a] = zv.v[a] + beta * pv.v[a];
+        st<D, T>(p, i, pv);
+    }
+}
+
+// lambda_k = F[p_k] - (K u)[p_k], K the full (not eliminated) stiffness: the first
+// block row of the reference's saddle system, K u + C^T lambda = F.
+template <int D>
+__global__ void k_multipliers(int64_t n_bc, const int64_t *__restrict__ bc_dof, const int32_t *__restrict__ ptr,
+                              const int32_t *__restrict__ col, const double *__restrict__ kval,
+                              const double *__restrict__ F, const double *__restrict__ u, double *__restrict__ lam) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_bc;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = bc_dof[k];
+        int64_t r = p / D;
+        int a = (int)(p - r * D);
+        double acc = 0.0;
+        for (int s = ptr[r]; s < ptr[r + 1]; ++s) {
+            int m = col[s];
+#pragma unroll
+            for (int b = 0; b < D; ++b) acc += kval[(int64_t)s * D * D + a * D + b] * u[(int64_t)m * D + b];
+        }
+        lam[k] = F[p] - acc;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+template <typename T>
+struct Sys {
+    const T *val = nullptr, *dinv = nullptr;
+    double *x = nullptr;
+    T *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *zc = nullptr, *dch = nullptr;
+};
+
+struct Cheb {
+    int k = 1;                 // Chebyshev terms (1 = plain node-block Jacobi)
+    double theta = 1, delta = 1;
+    double c1[16], c2[16];     // coefficients of steps 1..k-1
+};
+
+Cheb make_cheb(int degree, double lmax, double ratio) {
+    Cheb c;
+    c.k = std::max(1, std::min(degree, 16));
+    if (c.k <= 1 || !(lmax > 0)) {
+        c.k = 1;
+        return c;
+    }
+    double hi = lmax * 1.05, lo = hi / ratio;
+    c.theta = 0.5 * (hi + lo);
+    c.delta = 0.5 * (hi - lo);
+    double sigma = c.theta / c.delta, rho = 1.0 / sigma;
+    for (int s = 1; s < c.k; ++s) {
+        double rn = 1.0 / (2.0 * sigma - rho);
+        c.c1[s] = rn * rho;
+        c.c2[s] = 2.0 * rn / c.delta;
+        rho = rn;
+    }
+    return c;
+}
+
+template <int D, typename T>
+Sys<T> make_sys(fe_handle_s *h) {
+    Sys<T> s;
+    SolverWork &w = h->w;
+    s.x = w.x.p;
+    if constexpr (sizeof(T) == 8) {
+        s.val = h->aval.p, s.dinv = h->dinv.p;
+        s.r = w.r.p, s.p = w.p.p, s.q = w.q.p, s.z = w.z.p, s.zc = w.t.p, s.dch = w.dch.p;
+    } else {
+        s.val = h->aval32.p, s.dinv = h->dinv32.p;
+        s.r = w.r32.p, s.p = w.p32.p, s.q = w.q32.p, s.z = w.z32.p, s.zc = w.zc32.p, s.dch = w.c32.p;
+    }
+    return s;
+}
+
+template <int D, typename T, int G>
+void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part, int grid,
+                        bool start, T **z_final) {
+    T *zin = s.z, *zout = s.zc;
+    for (int k = 1; k < cb.k; ++k) {
+        const bool last = (k == cb.k - 1);
+        if (start)
+            k_cheb_step<D, T, G, 0><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p,
+                                                                         s.val, s.dinv, s.r, zin, zout, s.dch,
+                                                                         cb.c1[k], cb.c2[k], part, sc);
+        else if (last)
+            k_cheb_step<D, T, G, 1><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p,
+                                                                         s.val, s.dinv, s.r, zin, zout, s.dch,
+                                                                         cb.c1[k], cb.c2[k], part, sc);
+        else
+            k_cheb_step<D, T, G, 2><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p,
+                                                                         s.val, s.dinv, s.r, zin, zout, s.dch,
+                                                                         cb.c1[k], cb.c2[k], part, sc);
+        std::swap(zin, zout);
+    }
+    *z_final = zin;
+}
+
+template <int D, typename T, int G>
+void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part) {
+    const int gv = vec_grid(h->n_nodes);
+    const int gs = vec_grid(h->n_nodes * G);
+    k_pcg_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, s.p, s.q,
+                                                           part, sc);
+    T *zf = s.z;
+    if (cb.k > 1) {
+        k_pcg_update<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z, s.dch,
+                                                                    part, sc);
+        enqueue_cheb_steps<D, T, G>(h, s, cb, sc, part, gs, false, &zf);
+    } else {
+        k_pcg_update<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z,
+                                                                     s.dch, part, sc);
+    }
+    k_pcg_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
+}
+
+// Start (or continue, CONT) a loop: s.r holds the residual of s.x.  z = P r, then
+// p = z (start) or p = z + beta p (continue after a residual replacement).
+template <int D, typename T, int G, bool CONT>
+int enqueue_start(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part) {
+    const int gv = vec_grid(h->n_nodes);
+    const int gs = vec_grid(h->n_nodes * G);
+    T *zf = s.z;
+    if (cb.k > 1) {
+        k_start_precond<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, s.dch, cb.theta);
+        enqueue_cheb_steps<D, T, G>(h, s, cb, sc, part, gs, true, &zf);
+    } else {
+        k_start_precond<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, s.dch, 1.0);
+    }
+    k_start_finish<D, T, CONT><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, zf, s.p, part, sc);
+    if (CONT) k_continue_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+// FP64 residual r = b - A x (x may be nullptr) written as OUT, r.r into *out.
+template <int D, int G, typename OUT>
+int residual(fe_handle_s *h, const double *x, OUT *r, double *out) {
+    const int gs = vec_grid(h->n_nodes * G);
+    PcgScalars *sc = h->w.sc.p;
+    k_residual<D, G, OUT><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p,
+                                                             h->b.p, x, r, h->w.partials.p, &sc->ticket[4], out);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+int read_scalars(fe_handle_s *h) {
+    FE_CUDA(cudaMemcpyAsync(h->w.sc_host, h->w.sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, h->stream));
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    return FE_OK;
+}
+
+// Run PCG iterations until the device says done, replaying a captured chunk of
+// iterations (captured once per configuration and reused across solves).
+template <int D, typename T, int G>
+int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk) {
+    SolverWork &w = h->w;
+    PcgScalars *sc = w.sc.p;
+    const int slot = sizeof(T) == 8 ? 0 : 1;
+    SolverWork::Key &kk = w.key[slot];
+    bool same = w.graph[slot] && kk.k == cb.k && kk.G == G && kk.chunk == chunk && kk.x == (const void *)s.p &&
+                kk.theta == cb.theta && kk.delta == cb.delta;
+    if (!same) {
+        if (w.graph[slot]) {
+            cudaGraphExecDestroy(w.graph[slot]);
+            w.graph[slot] = nullptr;
+        }
+        cudaGraph_t g;
+        FE_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < chunk; ++i) enqueue_iteration<D, T, G>(h, s, cb, sc, w.partials.p);
+        cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+        if (ce != cudaSuccess) {
+            set_error(std::string("graph capture: ") + cudaGetErrorString(ce));
+            return FE_CUDA_ERR;
+        }
+        ce = cudaGraphInstantiate(&w.graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            w.graph[slot] = nullptr;
+            set_error(std::string("graph instantiate: ") + cudaGetErrorString(ce));
+            return FE_CUDA_ERR;
+        }
+        kk.k = cb.k, kk.G = G, kk.chunk = chunk, kk.x = s.p, kk.theta = cb.theta, kk.delta = cb.delta;
+    }
+    for (;;) {
+        FE_CHECK(read_scalars(h));
+        if (w.sc_host->done) break;
+        FE_CUDA(cudaGraphLaunch(w.graph[slot], h->stream));
+    }
+    return FE_OK;
+}
+
+// Largest eigenvalue of the tridiagonal Lanczos matrix built from CG coefficients,
+// by bisection on the Sturm sequence.
+double lanczos_lmax(const double *alpha, const double *beta, int m) {
+    if (m <= 0) return 0.0;
+    std::vector<double> dg(m), off(m > 1 ? m - 1 : 1);
+    for (int j = 0; j < m; ++j) {
+        dg[j] = 1.0 / alpha[j] + (j > 0 ? beta[j - 1] / alpha[j - 1] : 0.0);
+        if (j + 1 < m) off[j] = sqrt(std::max(beta[j], 0.0)) / alpha[j];
+    }
+    double hi = 0.0;
+    for (int j = 0; j < m; ++j) {
+        double rr = fabs(dg[j]) + (j > 0 ? fabs(off[j - 1]) : 0) + (j + 1 < m ? fabs(off[j]) : 0);
+        hi = std::max(hi, rr);
+    }
+    double lo = 0.0;
+    auto count_below = [&](double x) {
+        int c = 0;
+        double q = dg[0] - x;
+        if (q < 0) ++c;
+        for (int j = 1; j < m; ++j) {
+            if (q == 0) q = 1e-300;
+            q = dg[j] - x - off[j - 1] * off[j - 1] / q;
+            if (q < 0) ++c;
+        }
+        return c;
+    };
+    for (int it = 0; it < 200; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (count_below(mid) < m) lo = mid;
+        else hi = mid;
+    }
+    return hi;
+}
+
+template <typename F>
+int dispatch_lanes(int lanes, F &&f) {
+    switch (lanes) {
+        case 1: return f(std::integral_constant<int, 1>{});
+        case 2: return f(std::integral_constant<int, 2>{});
+        case 4: return f(std::integral_constant<int, 4>{});
+        default: return f(std::integral_constant<int, 8>{});
+    }
+}
+
+int ensure_work(fe_handle_s *h, bool mixed) {
+    SolverWork &w = h->w;
+    size_t n = (size_t)std::max<int64_t>(h->n_dof, 1);
+    FE_CHECK(dalloc(w.x, n));
+    FE_CHECK(dalloc(w.r, n));
+    FE_CHECK(dalloc(w.t, n));
+    if (!mixed) {
+        FE_CHECK(dalloc(w.z, n));
+        FE_CHECK(dalloc(w.p, n));
+        FE_CHECK(dalloc(w.q, n));
+        FE_CHECK(dalloc(w.dch, n));
+    } else {
+        FE_CHECK(dalloc(w.r32, n));
+        FE_CHECK(dalloc(w.z32, n));
+        FE_CHECK(dalloc(w.p32, n));
+        FE_CHECK(dalloc(w.q32, n));
+        FE_CHECK(dalloc(w.zc32, n));
+        FE_CHECK(dalloc(w.c32, n));
+    }
+    FE_CHECK(dalloc(w.partials, (size_t)4 * 152 * 8 + 64));
+    if (!w.sc.p) {
+        FE_CHECK(dalloc(w.sc, 1));
+        FE_CUDA(cudaMemsetAsync(w.sc.p, 0, sizeof(PcgScalars), h->stream));
+    }
+    if (!w.sc_host) FE_CUDA(cudaMallocHost((void **)&w.sc_host, sizeof(PcgScalars)));
+    return FE_OK;
+}
+
+// Write the loop parameters (tolerance, cap, b.b, Chebyshev centre) to the device
+// scalars; tickets and running values are left alone.
+int set_params(fe_handle_s *h, double tol2, int max_iter, double bb, double theta) {
+    PcgScalars *hs = h->w.sc_host, *ds = h->w.sc.p;
+    hs->tol2 = tol2;
+    hs->max_iter = max_iter;
+    hs->bb = bb;
+    hs->cheb_theta = theta;
+    FE_CUDA(cudaMemcpyAsync(&ds->tol2, &hs->tol2, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    FE_CUDA(cudaMemcpyAsync(&ds->max_iter, &hs->max_iter, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    FE_CUDA(cudaMemcpyAsync(&ds->bb, &hs->bb, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    FE_CUDA(cudaMemcpyAsync(&ds->cheb_theta, &hs->cheb_theta, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    // the copies read the pinned mirror asynchronously: keep it stable until done
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    return FE_OK;
+}
+
+template <int D, typename T, int G>
+int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
+    Sys<T> s = make_sys<D, T>(h);
+    T *x = s.p, *y = s.q;
+    FE_CUDA(cudaMemsetAsync(x, 0, h->n_dof * sizeof(T), h->stream));
+    const int gs = vec_grid(h->n_nodes * G);
+    for (int i = 0; i < 2; ++i)
+        k_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, x, y);
+    FE_CUDA(cudaEventRecord(h->events[6], h->stream));
+    for (int i = 0; i < reps; ++i)
+        k_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, x, y);
+    FE_CUDA(cudaEventRecord(h->events[7], h->stream));
+    FE_LAUNCH_CHECK();
+    FE_CUDA(cudaEventSynchronize(h->events[7]));
+    float t = 0;
+    FE_CUDA(cudaEventElapsedTime(&t, h->events[6], h->events[7]));
+    *ms = (double)t / std::max(reps, 1);
+    return FE_OK;
+}
+
+int time_spmv_any(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {
+    bool f32 = precision == FE_PREC_MIXED;
+    FE_CHECK(ensure_work(h, f32));
+    return dispatch_lanes(lanes, [&](auto g) {
+        constexpr int G = decltype(g)::value;
+        if (h->dim == 2) return f32 ? time_spmv_impl<2, float, G>(h, reps, ms) : time_spmv_impl<2, double, G>(h, reps, ms);
+        return f32 ? time_spmv_impl<1, float, G>(h, reps, ms) : time_spmv_impl<1, double, G>(h, reps, ms);
+    });
+}
+
+int pick_lanes(fe_handle_s *h, int precision, int requested, int *out) {
+    if (requested == 1 || requested == 2 || requested == 4 || requested == 8) {
+        *out = requested;
+        return FE_OK;
+    }
+    int slot = precision == FE_PREC_MIXED ? 1 : 0;
+    if (!h->w.lanes[slot]) {
+        double best = 1e300;
+        int bl = 1;
+        for (int g : {1, 2, 4, 8}) {
+            double ms = 0;
+            FE_CHECK(time_spmv_any(h, precision, g, 5, &ms));
+            if (ms < best) best = ms, bl = g;
+        }
+        h->w.lanes[slot] = bl;
+    }
+    *out = h->w.lanes[slot];
+    return FE_OK;
+}
+
+// Largest eigenvalue of D^-1 A from a short Jacobi-PCG probe on b (Lanczos matrix of
+// the CG coefficients).  Leaves x, r, p, q, z of the system overwritten.
+template <int D, typename T, int G>
+int estimate_lmax(fe_handle_s *h, const Sys<T> &s, double bb, int chunk, double *lmax) {
+    const int probe = 40;
+    PcgScalars *sc = h->w.sc.p;
+    FE_CUDA(cudaMemsetAsync(s.x, 0, h->n_dof * sizeof(double), h->stream));
+    FE_CHECK(residual<D, G, T>(h, nullptr, s.r, &sc->rr));
+    Cheb jac;
+    FE_CHECK(set_params(h, 0.0, probe, bb, 1.0));
+    FE_CHECK((enqueue_start<D, T, G, false>(h, s, jac, sc, h->w.partials.p)));
+    FE_CHECK((run_loop<D, T, G>(h, s, jac, chunk)));
+    int m = std::min(h->w.sc_host->iter, 64);
+    if (m > 1) m -= 1;
+    double lm = lanczos_lmax(h->w.sc_host->hist_alpha, h->w.sc_host->hist_beta, m);
+    *lmax = lm > 0 ? lm : 2.0;
+    return FE_OK;
+}
+
+template <int D, int G>
+int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
+    SolverWork &w = h->w;
+    Sys<double> s = make_sys<D, double>(h);
+    const int chunk = o->chunk > 0 ? o->chunk : 16;
+    const int max_iter = o->max_iter > 0 ? o->max_iter : 200000;
+    const int max_restart = o->max_outer > 0 ? o->max_outer : 8;
+    const double tol = o->tol > 0 ? o->tol : 1e-10;
+    const bool accept_stagnation = (o->flags & 1) != 0;
+    PcgScalars *sc = w.sc.p;
+    FE_CHECK((residual<D, G, double>(h, nullptr, w.t.p, &sc->bb)));
+    FE_CHECK(read_scalars(h));
+    const double bb = w.sc_host->bb;
+    st->bnorm = sqrt(bb);
+    Cheb cb;
+    if (o->cheb_degree >= 2) {
+        if (!(w.lmax[0] > 0)) FE_CHECK((estimate_lmax<D, double, G>(h, s, bb, chunk, &w.lmax[0])));
+        cb = make_cheb(o->cheb_degree, w.lmax[0], o->cheb_ratio > 0 ? o->cheb_ratio : 20.0);
+    }
+    if (o->x0 && bb != 0.0)
+        FE_CUDA(cudaMemcpyAsync(s.x, o->x0, h->n_dof * sizeof(double),
+                                o->x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    else
+        FE_CUDA(cudaMemsetAsync(s.x, 0, h->n_dof * sizeof(double), h->stream));
+    if (bb == 0.0) {
+        st->relres = 0.0;
+        st->status = FE_OK;
+        return FE_OK;
+    }
+    int total = 0, restarts = 0, status = FE_OK;
+    double relres = 0, prev = 1e300;
+    FE_CHECK((residual<D, G, double>(h, o->x0 ? s.x : nullptr, s.r, &sc->rr)));
+    st->spmv += o->x0 ? 1 : 0;
+    for (;;) {
+        FE_CHECK(set_params(h, tol * tol, max_iter - total, bb, cb.theta));
+        FE_CHECK((enqueue_start<D, double, G, false>(h, s, cb, sc, w.partials.p)));
+        FE_CHECK((run_loop<D, double, G>(h, s, cb, chunk)));
+        const int it = w.sc_host->iter, stv = w.sc_host->status;
+        total += it;
+        st->spmv += it * cb.k + (cb.k - 1);
+        // true residual, which also seeds a restart
+        FE_CHECK((residual<D, G, double>(h, s.x, s.r, &sc->rr)));
+        st->spmv += 1;
+        FE_CHECK(read_scalars(h));
+        relres = sqrt(w.sc_host->rr / bb);
+        status = stv;
+        if (relres <= tol) {
+            status = FE_OK;
+            break;
+        }
+        if (stv == FE_NONFINITE || stv == FE_BREAKDOWN) break;
+        if (total >= max_iter) {
+            status = FE_MAXITER;
+            break;
+        }
+        // the recurrence reached the tolerance but the true residual did not: rounding
+        // floor of the FP64 iteration.  Restart from the true residual while that
+        // still gains; with accept_stagnation a floor that no restart lowers is final.
+        if (relres > 0.5 * prev || restarts >= max_restart) {
+            status = accept_stagnation ? FE_OK : FE_MAXITER;
+            break;
+        }
+        prev = relres;
+        ++restarts;
+    }
+    st->iterations = total;
+    st->outer = restarts;
+    st->relres = relres;
+    st->status = status;
+    return FE_OK;
+}
+
+// Mixed precision: one Krylov run in FP32 (difference-form SpMV, FP32 Jacobi /
+// Chebyshev, FP32 r, p, q, z) accumulating the solution in FP64.  Each time the FP32
+// residual has fallen by `delta` since the last refinement step, the FP64 true
+// residual b - A x replaces it (refinement step) and the iteration continues with the
+// same search direction.  The solve ends when the FP64 true residual meets tol.
+template <int D, int G>
+int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
+    SolverWork &w = h->w;
+    Sys<float> s = make_sys<D, float>(h);
+    const int chunk = o->chunk > 0 ? o->chunk : 16;
+    const int max_iter = o->max_iter > 0 ? o->max_iter : 400000;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 200;
+    const double tol = o->tol > 0 ? o->tol : 1e-8;
+    const double delta = o->inner_tol > 0 ? o->inner_tol : 0.1;
+    PcgScalars *sc = w.sc.p;
+    FE_CHECK((residual<D, G, double>(h, nullptr, w.t.p, &sc->bb)));
+    FE_CHECK(read_scalars(h));
+    const double bb = w.sc_host->bb;
+    st->bnorm = sqrt(bb);
+    Cheb cb;
+    if (o->cheb_degree >= 2) {
+        if (!(w.lmax[1] > 0)) FE_CHECK((estimate_lmax<D, float, G>(h, s, bb, chunk, &w.lmax[1])));
+        cb = make_cheb(o->cheb_degree, w.lmax[1], o->cheb_ratio > 0 ? o->cheb_ratio : 20.0);
+    }
+    if (o->x0 && bb != 0.0)
+        FE_CUDA(cudaMemcpyAsync(s.x, o->x0, h->n_dof * sizeof(double),
+                                o->x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    else
+        FE_CUDA(cudaMemsetAsync(s.x, 0, h->n_dof * sizeof(double), h->stream));
+    if (bb == 0.0) {
+        st->relres = 0;
+        st->status = FE_OK;
+        return FE_OK;
+    }
+    // r32 = b - A x (FP64 residual, stored in FP32)
+    FE_CHECK((residual<D, G, float>(h, o->x0 ? s.x : nullptr, s.r, &sc->rr)));
+    FE_CHECK(read_scalars(h));
+    double rr_true = w.sc_host->rr;
+    st->spmv += o->x0 ? 1 : 0;
+    int total = 0, outer = 0, status = FE_OK;
+    double relres = sqrt(rr_true / bb);
+    bool first = true;
+    while (relres > tol) {
+        if (outer >= max_outer || total >= max_iter) {
+            status = FE_MAXITER;
+            break;
+        }
+        // the FP32 loop runs until its residual has fallen by delta (or to 0.5 tol)
+        double target = std::max(delta * delta * rr_true, 0.25 * tol * tol * bb);
+        FE_CHECK(set_params(h, target / bb, max_iter - total, bb, cb.theta));
+        if (first)
+            FE_CHECK((enqueue_start<D, float, G, false>(h, s, cb, sc, w.partials.p)));
+        else
+            FE_CHECK((enqueue_start<D, float, G, true>(h, s, cb, sc, w.partials.p)));
+        first = false;
+        FE_CHECK((run_loop<D, float, G>(h, s, cb, chunk)));
+        const int it = w.sc_host->iter, stv = w.sc_host->status;
+        total += it;
+        st->spmv += it * cb.k + (cb.k - 1);
+        ++outer;
+        // refinement step: FP64 true residual replaces the FP32 recurrence residual
+        FE_CHECK((residual<D, G, float>(h, s.x, s.r, &sc->rr)));
+        st->spmv += 1;
+        FE_CHECK(read_scalars(h));
+        double rr_new = w.sc_host->rr;
+        if (!isfinite(rr_new)) {
+            status = FE_NONFINITE;
+            relres = rr_new;
+            break;
+        }
+        relres = sqrt(rr_new / bb);
+        if (relres <= tol) break;
+        if (stv == FE_NONFINITE) {
+            status = stv;
+            break;
+        }
+        if (stv == FE_BREAKDOWN) {
+            // lost positive definiteness in FP32: restart the Krylov space from the
+            // true residual once; give up if that makes no progress either
+            if (it == 0) {
+                status = stv;
+                break;
+            }
+            first = true;
+        }
+        rr_true = rr_new;
+    }
+    if (relres <= tol) status = FE_OK;
+    st->iterations = total;
+    st->outer = outer;
+    st->relres = relres;
+    st->status = status;
+    return FE_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- entry points
+
+int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
+    if (!h->sys_ready) {
+        set_error("fe_solve: the system is not assembled (call fe_assemble with K and F)");
+        return FE_NOT_READY;
+    }
+    const bool mixed = o->precision == FE_PREC_MIXED;
+    if (o->precision != FE_PREC_FP64 && !mixed) {
+        set_error("fe_solve: unknown precision");
+        return FE_BAD_INPUT;
+    }
+    FE_CHECK(ensure_work(h, mixed));
+    int lanes = 1;
+    FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
+    FE_CUDA(cudaEventRecord(h->events[4], h->stream));
+    int rc = dispatch_lanes(lanes, [&](auto g) {
+        constexpr int G = decltype(g)::value;
+        if (h->dim == 2) return mixed ? solve_mixed<2, G>(h, o, st) : solve_fp64<2, G>(h, o, st);
+        return mixed ? solve_mixed<1, G>(h, o, st) : solve_fp64<1, G>(h, o, st);
+    });
+    FE_CHECK(rc);
+    FE_CHECK(recover_multipliers(h));
+    FE_CUDA(cudaEventRecord(h->events[5], h->stream));
+    FE_CUDA(cudaEventSynchronize(h->events[5]));
+    float ms = 0;
+    FE_CUDA(cudaEventElapsedTime(&ms, h->events[4], h->events[5]));
+    st->solve_ms = ms;
+    st->assemble_ms = h->last_assemble_ms;
+    h->have_solution = true;
+    return FE_OK;
+}
+
+int recover_multipliers(fe_handle_s *h) {
+    FE_CHECK(dalloc(h->lambda, (size_t)std::max<int64_t>(h->n_bc, 1)));
+    if (h->n_bc == 0) return FE_OK;
+    int g = grid_for(h->n_bc);
+    if (h->dim == 2)
+        k_multipliers<2><<<g, kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->blk_ptr.p, h->blk_col.p, h->kval.p,
+                                                        h->F.p, h->w.x.p, h->lambda.p);
+    else
+        k_multipliers<1><<<g, kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->blk_ptr.p, h->blk_col.p, h->kval.p,
+                                                        h->F.p, h->w.x.p, h->lambda.p);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms) {
+    if (!h->sys_ready) {
+        set_error("assemble first");
+        return FE_NOT_READY;
+    }
+    int slot = precision == FE_PREC_MIXED ? 1 : 0;
+    h->w.lanes[slot] = 0;
+    FE_CHECK(pick_lanes(h, precision, 0, lanes));
+    return time_spmv_any(h, precision, *lanes, 10, ms);
+}
+
+int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {
+    if (!h->sys_ready) {
+        set_error("assemble first");
+        return FE_NOT_READY;
+    }
+    return time_spmv_any(h, precision, lanes, reps, ms);
+}
+
+void release_solver(fe_handle_s *h) {
+    SolverWork &w = h->w;
+    for (int i = 0; i < 2; ++i)
+        if (w.graph[i]) cudaGraphExecDestroy(w.graph[i]), w.graph[i] = nullptr;
+    dfree(w.x), dfree(w.r), dfree(w.z), dfree(w.p), dfree(w.q), dfree(w.t), dfree(w.dch);
+    dfree(w.r32), dfree(w.z32), dfree(w.p32), dfree(w.q32), dfree(w.d32), dfree(w.zc32), dfree(w.c32);
+    dfree(w.partials), dfree(w.sc);
+    if (w.sc_host) cudaFreeHost(w.sc_host), w.sc_host = nullptr;
+}
+
+}  // namespace fe

@@ -1,0 +1,222 @@
+"""One problem on the GPU: the host-side ordering logic of the reference plus calls
+into libfe_gb300.so for every piece of arithmetic.
+
+Host work here is list bookkeeping only, O(number of loads and conditions):
+
+* Dirichlet conditions are de-duplicated exactly as the reference's dict round trip
+  does (finite_elements/analysis.py:28-68, :249-265): a Python dict keyed by
+  (node, dimension), filled in list order, so the LAST value wins and the multiplier
+  order is that of first insertion.  Element conditions get their values from the
+  device (element_to_node_factors, elements.py:18-53).
+* Loads keep their list position as a sequence number (user NodeLoads, then element
+  loads, then edge loads, analysis.py:465-469); the device keeps the last one per
+  (node, dimension) (analysis.py:71-110) and does all the arithmetic.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from ._lib import Handle, SolveOpts, SolveStats, ptr
+from .problem import ELASTIC, Problem
+
+
+def check_plane_flags(plane_strain, plane_stress):
+    """The checks and messages of ElasticityElement.d_matrix (elements.py:265-273)."""
+    if plane_strain and plane_stress:
+        raise ValueError('just one of plane_strain or plane_stress can be True')
+    if not plane_strain and not plane_stress:
+        raise ValueError('one of plane_strain or plane_stress must be True')
+
+
+def _index_dtype(n):
+    return np.int32 if n < 2 ** 31 else np.int64
+
+
+class GpuSystem:
+    """Device handle of one Problem, assembled on construction (K and F; M on demand)."""
+
+    def __init__(self, prob: Problem, assemble=True):
+        self.prob = prob
+        self.dim = prob.dim
+        if prob.kind == ELASTIC:
+            check_plane_flags(prob.plane_strain, prob.plane_stress)
+            kind = _lib.FE_KIND_ELASTIC_TRI
+        else:
+            kind = _lib.FE_KIND_MAGNETIC_TRI
+        self.handle = Handle(kind, prob.coords, prob.conn)
+        h = self.handle
+        if prob.kind == ELASTIC:
+            mode = _lib.FE_PLANE_STRAIN if prob.plane_strain else _lib.FE_PLANE_STRESS
+            rho = prob.rho if prob.rho is not None else None
+            h.call("fe_set_elastic_materials", ptr(prob.E), ptr(prob.nu), ptr(prob.thickness),
+                   ptr(rho), mode)
+        else:
+            h.call("fe_set_mu", ptr(prob.mu))
+        self.bc_dof, self.bc_value = self._dirichlet()
+        h.call("fe_set_dirichlet", len(self.bc_dof), ptr(self.bc_dof), ptr(self.bc_value))
+        self._set_loads()
+        self.m_assembled = False
+        if assemble:
+            self.assemble()
+
+    # ------------------------------------------------------------ host bookkeeping
+
+    def _dof(self, node, dim):
+        """positions[(node_index, dim)] (core.py:89-108): KeyError outside the table."""
+        node = int(node)
+        dim = int(dim)
+        if not (0 <= node < self.prob.n_nodes) or not (1 <= dim <= self.dim):
+            raise KeyError((node, dim))
+        return node * self.dim + dim - 1
+
+    def _element_factors(self, elements):
+        elements = np.ascontiguousarray(elements, dtype=np.int64)
+        out = np.empty((elements.size, 3))
+        if elements.size:
+            self.handle.call("fe_element_node_factors", elements.size, ptr(elements), ptr(out))
+        return out
+
+    def _dirichlet(self):
+        p = self.prob
+        table = {}
+        for n, d, v in zip(p.node_bc_node.tolist(), p.node_bc_dim.tolist(), p.node_bc_value.tolist()):
+            table[self._dof(n, d)] = v
+        if p.element_bc_element.size:
+            fac = self._element_factors(p.element_bc_element)
+            for k, (e, d, v) in enumerate(zip(p.element_bc_element.tolist(), p.element_bc_dim.tolist(),
+                                              p.element_bc_value.tolist())):
+                for i, node in enumerate(p.conn[e].tolist()):
+                    table[self._dof(node, d)] = v * fac[k, i]
+        for (a, b), d, v in zip(p.edge_bc_nodes.tolist(), p.edge_bc_dim.tolist(), p.edge_bc_value.tolist()):
+            table[self._dof(a, d)] = v * 0.5
+            table[self._dof(b, d)] = v * 0.5
+        dof = np.fromiter(table.keys(), dtype=np.int64, count=len(table))
+        val = np.fromiter(table.values(), dtype=np.float64, count=len(table))
+        return dof, val
+
+    def _set_loads(self):
+        p = self.prob
+        n_user = p.node_load_node.size
+        dofs = [self._dof(n, d) for n, d in zip(p.node_load_node.tolist(), p.node_load_dim.tolist())]
+        vals = list(p.node_load_value.tolist())
+        seqs = list(range(n_user))
+        # element loads: sets in order, occurrence k, point i -> seq n_user + 3k + i
+        n_occ = 0
+        if p.element_loads:
+            set_ptr = np.zeros(len(p.element_loads) + 1, np.int64)
+            for s, ls in enumerate(p.element_loads):
+                if not (1 <= ls.dimension <= self.dim):
+                    raise KeyError((int(ls.elements[0]) if ls.elements.size else -1, ls.dimension))
+                set_ptr[s + 1] = set_ptr[s] + ls.elements.size
+            elems = np.ascontiguousarray(np.concatenate([ls.elements for ls in p.element_loads]), np.int64)
+            values = np.array([ls.value for ls in p.element_loads], np.float64)
+            dims = np.array([ls.dimension for ls in p.element_loads], np.int32)
+            n_occ = int(set_ptr[-1])
+            self.handle.call("fe_set_element_loads", len(p.element_loads), ptr(set_ptr), ptr(elems),
+                             ptr(values), ptr(dims), n_user)
+        else:
+            self.handle.call("fe_set_element_loads", 0, None, None, None, None, n_user)
+        # edge loads: half the value to each end point, after every element load
+        base = n_user + 3 * n_occ
+        for j, ((a, b), d, v) in enumerate(zip(p.edge_load_nodes.tolist(), p.edge_load_dim.tolist(),
+                                               p.edge_load_value.tolist())):
+            dofs += [self._dof(a, d), self._dof(b, d)]
+            vals += [v * 0.5, v * 0.5]
+            seqs += [base + 2 * j, base + 2 * j + 1]
+        dof_a = np.array(dofs, np.int64)
+        val_a = np.array(vals, np.float64)
+        seq_a = np.array(seqs, np.int64)
+        self.handle.call("fe_set_node_loads", dof_a.size, ptr(dof_a), ptr(val_a), ptr(seq_a))
+
+    # ------------------------------------------------------------ device work
+
+    def assemble(self, mass=False):
+        flags = _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
+        if mass:
+            flags |= _lib.FE_ASSEMBLE_M
+            self.m_assembled = True
+        self.handle.call("fe_assemble", flags)
+
+    def _export(self, which):
+        nr, nc, nnz = _i64(), _i64(), _i64()
+        self.handle.call("fe_export_sizes", which, nr, nc, nnz)
+        nrows, ncols, nz = nr.value, nc.value, nnz.value
+        indptr = np.empty(nrows + 1, np.int64)
+        indices = np.empty(max(nz, 1), np.int32)
+        data = np.empty(max(nz, 1), np.float64)
+        self.handle.call("fe_export_csr", which, ptr(indptr), ptr(indices), ptr(data))
+        idt = _index_dtype(max(nz, nrows, ncols))
+        return (data[:nz], indices[:nz].astype(idt, copy=False), indptr.astype(idt)), (nrows, ncols)
+
+    def create_matrix(self):
+        arrays, shape = self._export(_lib.FE_MAT_K_AUGMENTED)
+        return sp.csr_matrix(arrays, shape=shape)
+
+    def create_source_matrix(self):
+        n = self.prob.n_dof + len(self.bc_dof)
+        out = np.empty(n, np.float64)
+        self.handle.call("fe_export_rhs", ptr(out))
+        return out.reshape(-1, 1)
+
+    def k_matrix_sparse(self):
+        arrays, shape = self._export(_lib.FE_MAT_K_CSC)
+        return sp.csc_matrix(arrays, shape=shape)
+
+    def m_matrix_sparse(self):
+        if not self.m_assembled:
+            self.assemble(mass=True)
+        arrays, shape = self._export(_lib.FE_MAT_M_CSC)
+        return sp.csc_matrix(arrays, shape=shape)
+
+    def element_matrices(self, which="K"):
+        nl = 3 * self.dim
+        out = np.empty((self.prob.n_elements, nl * nl))
+        if which == "M" and not self.m_assembled:
+            self.assemble(mass=True)
+        sel = _lib.FE_ASSEMBLE_K if which == "K" else _lib.FE_ASSEMBLE_M
+        self.handle.call("fe_export_element_matrices", sel, ptr(out))
+        return out
+
+    def solve(self, precision="fp64", tol=None, cheb_degree=0, max_iter=0, x0=None, lanes=0,
+              accept_stagnation=False, inner_tol=0.0, cheb_ratio=0.0, chunk=0, max_outer=0,
+              want_host=True):
+        """Solve the eliminated system on the GPU.  Returns (x, stats): x holds
+        n_dof + n_bc values (u then the multipliers) or None with want_host=False."""
+        o = SolveOpts()
+        o.precision = _lib.FE_PREC_MIXED if precision == "mixed" else _lib.FE_PREC_FP64
+        o.cheb_degree = cheb_degree
+        o.max_iter = max_iter
+        o.max_outer = max_outer
+        o.tol = tol if tol is not None else (1e-8 if precision == "mixed" else 1e-12)
+        o.inner_tol = inner_tol
+        o.cheb_ratio = cheb_ratio
+        x0a = None
+        if x0 is not None:
+            x0a = np.ascontiguousarray(x0, dtype=np.float64)[: self.prob.n_dof]
+            o.x0 = x0a.ctypes.data
+        o.lanes = lanes
+        o.chunk = chunk
+        o.flags = _lib.FE_FLAG_ACCEPT_STAGNATION if accept_stagnation else 0
+        st = SolveStats()
+        x = np.empty(self.prob.n_dof + len(self.bc_dof)) if want_host else None
+        lib = _lib.load()
+        status = lib.fe_solve(self.handle.h, o, ptr(x) if want_host else None, st)
+        if status not in (_lib.FE_OK, _lib.FE_MAXITER, _lib.FE_BREAKDOWN, _lib.FE_NONFINITE):
+            _lib.check(status, "fe_solve")
+        return x, st
+
+    def info(self):
+        nd, nb, nblk = _i64(), _i64(), _i64()
+        self.handle.call("fe_info", nd, nb, nblk)
+        return {"n_dof": nd.value, "n_bc": nb.value, "n_blocks": nblk.value}
+
+    def close(self):
+        self.handle.close()
+
+
+def _i64():
+    return ctypes.c_int64()

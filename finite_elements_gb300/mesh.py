@@ -1,0 +1,176 @@
+"""Light mesh types standing in for the parts of ``volmdlr.mesh`` the analysis reads.
+
+The reference builds its meshes from volmdlr objects and the analysis only touches a
+small surface of them:
+
+* ``Mesh.nodes`` / ``Mesh.node_to_index`` / ``Mesh.elements_groups``
+  (finite_elements/analysis.py:274, :487, :716; core.py:89-108);
+* ``ElementsGroup.elements`` (analysis.py:326-327);
+* ``TriangularElement2D.points`` / ``.area`` / ``.form_functions``
+  (elements.py:35-44, :100-116, :508, :530; loads.py:32-34);
+* edge objects with ``.start`` / ``.end`` (analysis.py:232-233, :441-442).
+
+volmdlr is not a dependency of this package, so these classes provide that surface.
+Real volmdlr objects with the same attributes work as well (the analysis only
+duck-types them).  ``ArrayMesh`` is the bulk form: node coordinates and
+connectivity as arrays, so that meshes of millions of triangles never become Python
+objects on the host.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class Point2D:
+    """A 2D point, hashed and compared by its coordinates (like volmdlr.Point2D)."""
+
+    __slots__ = ("x", "y")
+
+    def __init__(self, x, y):
+        self.x = float(x)
+        self.y = float(y)
+
+    def __getitem__(self, i):
+        return (self.x, self.y)[i]
+
+    def __iter__(self):
+        yield self.x
+        yield self.y
+
+    def __len__(self):
+        return 2
+
+    def __hash__(self):
+        return hash((self.x, self.y))
+
+    def __eq__(self, other):
+        return (isinstance(other, Point2D) and self.x == other.x and self.y == other.y)
+
+    def __repr__(self):
+        return f"{type(self).__name__}({self.x!r}, {self.y!r})"
+
+
+class Node2D(Point2D):
+    """A mesh node (volmdlr.mesh.Node2D)."""
+
+
+class LineSegment2D:
+    """An edge between two points; edge loads and edge conditions read ``start``/``end``."""
+
+    def __init__(self, start, end, name=""):
+        self.start = start
+        self.end = end
+        self.name = name
+
+    @property
+    def points(self):
+        return [self.start, self.end]
+
+
+class TriangularElement2D:
+    """A 3-node triangle.
+
+    ``area`` is the unsigned area |detJ|/2 and ``form_functions`` the three rows
+    (a_i, b_i, c_i) of the linear shape functions N_i = a_i + b_i x + c_i y with
+    N_i(p_j) = delta_ij -- the two volmdlr quantities the reference consumes
+    (elements.py:100-116, :35-44, :508, :530).
+    """
+
+    def __init__(self, points, name=""):
+        self.points = list(points)
+        self.name = name
+
+    def _xy(self):
+        return [(float(p[0]), float(p[1])) for p in self.points]
+
+    @property
+    def area(self):
+        (x1, y1), (x2, y2), (x3, y3) = self._xy()
+        return abs((x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)) / 2.0
+
+    @property
+    def form_functions(self):
+        (x1, y1), (x2, y2), (x3, y3) = self._xy()
+        det = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)
+        a = ((x2 * y3 - x3 * y2) / det, (x3 * y1 - x1 * y3) / det, (x1 * y2 - x2 * y1) / det)
+        b = ((y2 - y3) / det, (y3 - y1) / det, (y1 - y2) / det)
+        c = ((x3 - x2) / det, (x1 - x3) / det, (x2 - x1) / det)
+        return [[a[i], b[i], c[i]] for i in range(3)]
+
+    @property
+    def center(self):
+        xy = self._xy()
+        return Point2D(sum(p[0] for p in xy) / 3.0, sum(p[1] for p in xy) / 3.0)
+
+
+class ElementsGroup:
+    """An ordered list of elements (volmdlr.mesh.ElementsGroup)."""
+
+    def __init__(self, elements, name=""):
+        self.elements = list(elements)
+        self.name = name
+
+
+class Mesh:
+    """A mesh of element groups.
+
+    ``nodes`` lists every distinct element point in order of first appearance
+    (group order, element order, point order) and ``node_to_index`` maps a point to
+    its position there.  Callers may overwrite both, as the reference's own scripts do
+    to keep a mesh file's node order (scripts/Elasticity/beam2d_example_3.py:72-73).
+    """
+
+    def __init__(self, elements_groups, name=""):
+        self.elements_groups = list(elements_groups)
+        self.name = name
+        nodes, index = [], {}
+        for group in self.elements_groups:
+            for element in group.elements:
+                for p in element.points:
+                    if p not in index:
+                        index[p] = len(nodes)
+                        nodes.append(p)
+        self.nodes = nodes
+        self.node_to_index = index
+
+
+class ArrayMesh:
+    """A mesh held as arrays: ``coords`` (n, 2) float64 and ``conn`` (E, 3) int32.
+
+    ``group_ptr`` splits the elements into consecutive groups (group g is
+    ``conn[group_ptr[g]:group_ptr[g+1]]``).  Per-element material arrays live in the
+    analysis, not here.  ``nodes`` / ``node_to_index`` are built on first use only.
+    """
+
+    def __init__(self, coords, conn, group_ptr=None, name=""):
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 2)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 3)
+        if group_ptr is None:
+            group_ptr = [0, self.conn.shape[0]]
+        self.group_ptr = np.asarray(group_ptr, dtype=np.int64)
+        self.name = name
+        self._nodes = None
+        self._node_to_index = None
+
+    @property
+    def n_nodes(self):
+        return self.coords.shape[0]
+
+    @property
+    def n_elements(self):
+        return self.conn.shape[0]
+
+    @property
+    def nodes(self):
+        if self._nodes is None:
+            self._nodes = [Node2D(x, y) for x, y in self.coords.tolist()]
+        return self._nodes
+
+    @property
+    def node_to_index(self):
+        if self._node_to_index is None:
+            self._node_to_index = {p: i for i, p in enumerate(self.nodes)}
+        return self._node_to_index
+
+    def as_arrays(self):
+        return self.coords, self.conn

@@ -1,0 +1,169 @@
+/*
+ * fe_gb300.h -- C ABI of the GB300 (sm_103a) assembly-and-solve path for linear
+ * triangles, the drop-in for finite_elements' FiniteElementAnalysis.create_matrix /
+ * create_source_matrix / solve / k_matrix_sparse / m_matrix_sparse.
+ *
+ * All functions return an int status (FE_OK = 0).  Pointers named "host" are plain
+ * host memory owned by the caller; the library copies what it needs.  Every device
+ * buffer belongs to the handle and is released by fe_destroy.  fe_last_error()
+ * returns a message for the last failing call on the calling thread.
+ *
+ * Reference interfaces replaced (paths within the reference project):
+ *   finite_elements/analysis.py:617-663   create_matrix          -> fe_assemble + fe_export_csr(FE_MAT_K_AUGMENTED)
+ *   finite_elements/analysis.py:665-708   create_source_matrix   -> fe_assemble + fe_export_rhs
+ *   finite_elements/analysis.py:798-830   solve (scipy spsolve)  -> fe_assemble + fe_solve
+ *   finite_elements/analysis.py:345-405   k/m_matrix_sparse      -> fe_export_csr(FE_MAT_K_CSC / FE_MAT_M_CSC)
+ *   finite_elements/elements.py:395-536,93-118  element matrices -> fe_assemble (element kernels), fe_export_element_matrices
+ *   finite_elements/elements.py:18-53,156-191   element_to_node_factors -> fe_element_node_factors
+ */
+#ifndef FE_GB300_H
+#define FE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FE_OK          0
+#define FE_MAXITER     1   /* iteration cap reached before the tolerance            */
+#define FE_BREAKDOWN   2   /* p.Ap <= 0 or a singular diagonal block: not SPD        */
+#define FE_NONFINITE   3   /* NaN / Inf in inputs or iterates                        */
+#define FE_BAD_INPUT   4   /* argument or index out of range                         */
+#define FE_CUDA_ERR    5   /* a CUDA call failed                                     */
+#define FE_NOT_READY   6   /* a required earlier step (materials, assembly) missing  */
+
+/* element kinds (finite_elements/elements.py:333 and :56) */
+#define FE_KIND_ELASTIC_TRI   1   /* ElasticityTriangularElement2D, 2 DOF per node */
+#define FE_KIND_MAGNETIC_TRI  2   /* MagneticElement2D, 1 DOF per node             */
+
+/* plane mode (finite_elements/elements.py:251-273) */
+#define FE_PLANE_STRESS  1
+#define FE_PLANE_STRAIN  2
+
+/* fe_assemble flags */
+#define FE_ASSEMBLE_K  1
+#define FE_ASSEMBLE_M  2
+#define FE_ASSEMBLE_F  4
+
+/* matrices for fe_export_sizes / fe_export_csr */
+#define FE_MAT_K_AUGMENTED  1   /* [[K, C^T], [C, 0]] in CSR, as create_matrix returns   */
+#define FE_MAT_K_CSC        2   /* K without multipliers in CSC, as k_matrix_sparse      */
+#define FE_MAT_M_CSC        3   /* M without multipliers in CSC, as m_matrix_sparse      */
+
+/* solver precision */
+#define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
+#define FE_PREC_MIXED  1   /* FP32 SpMV/preconditioner inside FP64 iterative refinement    */
+
+typedef struct fe_handle_s *fe_handle;
+
+typedef struct fe_solve_opts {
+    int32_t precision;     /* FE_PREC_FP64 or FE_PREC_MIXED                              */
+    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it    */
+    int32_t max_iter;      /* cap on PCG iterations, all refinement steps together       */
+    int32_t max_outer;     /* cap on refinement steps (mixed) or restarts (FP64)          */
+    double  tol;           /* target ||b - A x||_2 / ||b||_2, FP64 true residual          */
+    double  inner_tol;     /* mixed: relative residual each FP32 inner solve aims for    */
+    double  cheb_ratio;    /* Chebyshev interval [lmax/ratio, lmax]; <= 0 -> default     */
+    const double *x0;      /* initial guess, n_dof values, or NULL for zero               */
+    int32_t x0_device;     /* 1 if x0 is a device pointer                                 */
+    int32_t lanes;         /* lanes per block row in SpMV: 1,2,4,8; 0 = autotuned         */
+    int32_t chunk;         /* PCG iterations per graph launch; 0 = default                */
+    int32_t flags;         /* reserved, 0                                                 */
+} fe_solve_opts;
+
+typedef struct fe_solve_stats {
+    int32_t status;        /* FE_OK or a failure status                                   */
+    int32_t iterations;    /* PCG iterations (inner iterations summed for mixed)          */
+    int32_t outer;         /* refinement steps (mixed) or true-residual restarts (FP64)   */
+    int32_t spmv;          /* sparse matrix-vector products issued                        */
+    double  relres;        /* final ||b - A x|| / ||b|| recomputed in FP64                 */
+    double  bnorm;         /* ||b||_2 of the eliminated system                            */
+    double  solve_ms;      /* device time of the solve, CUDA events on the handle stream  */
+    double  assemble_ms;   /* device time of the last fe_assemble                         */
+} fe_solve_stats;
+
+int         fe_version(void);
+const char *fe_status_string(int status);
+const char *fe_last_error(void);
+
+/* Mesh: coords_host[2*n_nodes] (x, y per node, mesh.nodes order), conn_host[3*n_elem]
+ * (node indices, groups then elements).  Replaces the mesh walk of
+ * finite_elements/analysis.py:326-338,714-735 and core.py:89-108. */
+int fe_mesh_create(int32_t kind, int64_t n_nodes, int64_t n_elem,
+                   const double *coords_host, const int32_t *conn_host, fe_handle *out);
+int fe_destroy(fe_handle h);
+
+/* Per-element elastic material (elements.py:229-243,380-391): E, nu, thickness,
+ * rho, each n_elem values; plane_mode FE_PLANE_STRESS or FE_PLANE_STRAIN. */
+int fe_set_elastic_materials(fe_handle h, const double *E_host, const double *nu_host,
+                             const double *thickness_host, const double *rho_host,
+                             int32_t plane_mode);
+/* Per-element absolute permeability mu_total (elements.py:74-78). */
+int fe_set_mu(fe_handle h, const double *mu_host);
+
+/* Loads (analysis.py:457-489).  The reference keeps, for every (node, dimension), the
+ * value of the LAST load in its list (analysis.py:71-110).  Each load carries its
+ * position in that list as seq; the device keeps the value with the largest seq.
+ * Explicit loads (user NodeLoads, halves of EdgeLoads): dof, value, seq, n of each. */
+int fe_set_node_loads(fe_handle h, int64_t n, const int64_t *dof_host,
+                      const double *value_host, const int64_t *seq_host);
+/* ElementsLoad sets (loads.py:24-35, analysis.py:407-429): set s covers
+ * elements_host[set_ptr[s] .. set_ptr[s+1]) with total value set_value[s] in 1-based
+ * dimension set_dim[s].  Element occurrence k (counted over all sets in order) gives its
+ * point p the sequence number seq_base + 3k + p. */
+int fe_set_element_loads(fe_handle h, int64_t n_sets, const int64_t *set_ptr_host,
+                         const int64_t *elements_host, const double *set_value_host,
+                         const int32_t *set_dim_host, int64_t seq_base);
+
+/* Dirichlet conditions after the reference's de-duplication (analysis.py:241-279,
+ * :509-543): multiplier i constrains DOF dof_host[i] to value_host[i]. */
+int fe_set_dirichlet(fe_handle h, int64_t n_bc, const int64_t *dof_host,
+                     const double *value_host);
+
+/* element_to_node_factors (elements.py:18-53,156-191) of the listed elements,
+ * 3 values each, written to factors_host[3*n]. */
+int fe_element_node_factors(fe_handle h, int64_t n, const int64_t *elements_host,
+                            double *factors_host);
+
+/* Element kernels, pattern build, segmented reduction, loads and Dirichlet
+ * elimination on the device (create_matrix / create_source_matrix). */
+int fe_assemble(fe_handle h, int32_t flags);
+
+int fe_export_sizes(fe_handle h, int32_t which, int64_t *nrows, int64_t *ncols, int64_t *nnz);
+/* Canonical sorted CSR (or CSC) with explicit zeros kept, as scipy builds it. */
+int fe_export_csr(fe_handle h, int32_t which, int64_t *indptr_host, int32_t *indices_host,
+                  double *data_host);
+/* create_source_matrix: n_dof load entries then n_bc prescribed values. */
+int fe_export_rhs(fe_handle h, double *rhs_host);
+/* Element matrices, row-major (3*dim)^2 per element: which = FE_ASSEMBLE_K or _M. */
+int fe_export_element_matrices(fe_handle h, int32_t which, double *out_host);
+
+/* Solve the eliminated system with PCG and recover the multipliers
+ * lambda_i = (F - K u)[dof_i].  x_host (optional) receives n_dof + n_bc values,
+ * u then lambda, as solve() returns them (analysis.py:816-830). */
+int fe_solve(fe_handle h, const fe_solve_opts *opts, double *x_host, fe_solve_stats *stats);
+/* Copy the last solution (n_dof + n_bc values) to the host. */
+int fe_get_solution(fe_handle h, double *x_host);
+/* Device address of the last solution u (n_dof doubles), valid until the next solve. */
+int fe_solution_device_ptr(fe_handle h, const double **ptr);
+
+/* Sizes of the handle: n_dof, number of Dirichlet conditions, stored 2x2 (or 1x1)
+ * blocks of K. */
+int fe_info(fe_handle h, int64_t *n_dof, int64_t *n_bc, int64_t *n_blocks);
+
+/* CUDA events on the handle's stream, for timing around library calls. */
+int fe_event_record(fe_handle h, int32_t slot);
+int fe_event_elapsed_ms(fe_handle h, int32_t slot_a, int32_t slot_b, double *ms);
+int fe_synchronize(fe_handle h);
+/* Lanes per block row the autotuner chose for SpMV in the given precision. */
+int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double *ms_out);
+/* Average device time of one SpMV with the given lanes (reps repetitions). */
+int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FE_GB300_H */

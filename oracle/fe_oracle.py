@@ -1,0 +1,359 @@
+"""CPU oracle for the finite_elements assembly-and-solve path.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in ``finite_elements_gb300`` imports this module:
+it is the checker that ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
+legs of ``bench.py`` compare the CUDA path against.
+
+It restates, in numpy, what the reference computes (file:line of the reference
+project ``finite_elements``), element by element and list by list, and then calls the
+real scipy routines the reference calls:
+
+* plane-elasticity triangle B, D and Ke = t*A*B^T D B   (elements.py:395-453, :466-511)
+* plane-elasticity triangle mass Me                     (elements.py:513-536)
+* magnetostatic triangle Ke = A/mu * (b_i b_j + c_i c_j) (elements.py:93-118)
+* element -> node factors |detJ| * N_i(mid(p2, p3))     (elements.py:18-53, :156-191)
+* ElementsLoad area split                               (loads.py:24-35)
+* element/edge loads and conditions -> node lists       (analysis.py:201-239, :407-447)
+* (node, dim) de-duplication, last value wins           (analysis.py:28-110)
+* DOF numbering node*dim + (d-1)                        (core.py:89-108)
+* COO triplets in group/element order                   (analysis.py:324-339, :714-735)
+* Lagrange-multiplier rows n*dim + i                    (analysis.py:241-279, :509-543)
+* scipy.sparse.csr_matrix of the triplets               (analysis.py:617-663)
+* F vector                                              (analysis.py:665-708, :737-739)
+* spsolve(K, F, permc_spec='NATURAL', use_umfpack=True) (analysis.py:798-830)
+* dict-merged K / M as csc_matrix                       (analysis.py:345-405)
+
+Two volmdlr quantities are restated from their definitions, because volmdlr is not
+available: the unsigned triangle area |detJ|/2 and the barycentric shape-function
+coefficients (a_i, b_i, c_i).  No reference test pins their values ("parity
+unpinned" for those two); everything downstream of them is pinned by golden vectors
+that ``tests/golden/make_golden.py`` produced by running the reference's own code.
+"""
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from finite_elements_gb300.problem import ELASTIC, MAGNETIC, Problem
+
+# ---------------------------------------------------------------- element level
+
+
+def element_points(prob: Problem):
+    """(E, 3, 2) vertex coordinates of every element, in connectivity order."""
+    return prob.coords[prob.conn]
+
+
+def triangle_area(p):
+    """Unsigned area |detJ|/2 (volmdlr TriangularElement2D.area, restated)."""
+    x1, y1 = p[:, 0, 0], p[:, 0, 1]
+    x2, y2 = p[:, 1, 0], p[:, 1, 1]
+    x3, y3 = p[:, 2, 0], p[:, 2, 1]
+    return np.abs((x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)) / 2.0
+
+
+def form_functions(p):
+    """(E, 3, 3) rows (a_i, b_i, c_i): N_i = a_i + b_i x + c_i y, N_i(p_j) = delta_ij
+    (volmdlr TriangularElement2D.form_functions, restated)."""
+    x1, y1 = p[:, 0, 0], p[:, 0, 1]
+    x2, y2 = p[:, 1, 0], p[:, 1, 1]
+    x3, y3 = p[:, 2, 0], p[:, 2, 1]
+    det = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)
+    ff = np.empty((p.shape[0], 3, 3))
+    ff[:, 0, 0] = (x2 * y3 - x3 * y2) / det
+    ff[:, 1, 0] = (x3 * y1 - x1 * y3) / det
+    ff[:, 2, 0] = (x1 * y2 - x2 * y1) / det
+    ff[:, 0, 1] = (y2 - y3) / det
+    ff[:, 1, 1] = (y3 - y1) / det
+    ff[:, 2, 1] = (y1 - y2) / det
+    ff[:, 0, 2] = (x3 - x2) / det
+    ff[:, 1, 2] = (x1 - x3) / det
+    ff[:, 2, 2] = (x2 - x1) / det
+    return ff
+
+
+def b_matrix(p):
+    """(E, 3, 6) strain-displacement matrix with the reference's signed detJ
+    (elements.py:395-416)."""
+    xs, ys = p[:, :, 0], p[:, :, 1]
+    y23, y31, y12 = ys[:, 1] - ys[:, 2], ys[:, 2] - ys[:, 0], ys[:, 0] - ys[:, 1]
+    x32, x13, x21 = xs[:, 2] - xs[:, 1], xs[:, 0] - xs[:, 2], xs[:, 1] - xs[:, 0]
+    det = (xs[:, 0] - xs[:, 2]) * (ys[:, 1] - ys[:, 2]) - (ys[:, 0] - ys[:, 2]) * (xs[:, 1] - xs[:, 2])
+    z = np.zeros_like(det)
+    data = np.stack([y23, z, y31, z, y12, z,
+                     z, x32, z, x13, z, x21,
+                     x32, y23, x13, y31, x21, y12], axis=1).reshape(-1, 3, 6)
+    return (1.0 / det)[:, None, None] * data
+
+
+def d_matrix(E, nu, plane_strain, plane_stress):
+    """(E, 3, 3) constitutive matrix; the flag checks and messages of
+    elements.py:251-273 and the two formulas of elements.py:418-453."""
+    if plane_strain and plane_stress:
+        raise ValueError('just one of plane_strain or plane_stress can be True')
+    if not plane_strain and not plane_stress:
+        raise ValueError('one of plane_strain or plane_stress must be True')
+    if plane_strain:
+        a = (E * nu) / ((1 + nu) * (1 - 2 * nu))
+    else:
+        a = (E * nu) / (1 - nu ** 2)
+    b = E / (2 * (1 + nu))
+    c = a + 2 * b
+    z = np.zeros_like(E)
+    return np.stack([c, a, z, a, c, z, z, z, b], axis=1).reshape(-1, 3, 3)
+
+
+def elastic_stiffness(prob: Problem):
+    """(E, 36) row-major Ke = t * area * (B^T D) B (elements.py:466-511)."""
+    p = element_points(prob)
+    B = b_matrix(p)
+    D = d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress)
+    ke = np.matmul(np.matmul(np.transpose(B, (0, 2, 1)), D), B)
+    ke *= (prob.thickness * triangle_area(p))[:, None, None]
+    return ke.reshape(-1, 36)
+
+
+_MASS_PATTERN = np.array([2, 0, 1, 0, 1, 0,
+                          0, 2, 0, 1, 0, 1,
+                          1, 0, 2, 0, 1, 0,
+                          0, 1, 0, 2, 0, 1,
+                          1, 0, 1, 0, 2, 0,
+                          0, 1, 0, 1, 0, 2], dtype=np.float64)
+
+
+def elastic_mass(prob: Problem):
+    """(E, 36) Me = rho * area * t / 12 * P (elements.py:513-536)."""
+    p = element_points(prob)
+    s = (prob.rho * triangle_area(p) * prob.thickness) / 12
+    return s[:, None] * _MASS_PATTERN[None, :]
+
+
+def magnetic_stiffness(prob: Problem):
+    """(E, 9) row-major Ke_ij = 1/mu * (b_i b_j + c_i c_j) * area (elements.py:93-118)."""
+    p = element_points(prob)
+    ff = form_functions(p)
+    b, c = ff[:, :, 1], ff[:, :, 2]
+    g = b[:, :, None] * b[:, None, :] + c[:, :, None] * c[:, None, :]
+    return ((1 / prob.mu)[:, None, None] * g * triangle_area(p)[:, None, None]).reshape(-1, 9)
+
+
+def element_stiffness(prob: Problem):
+    return elastic_stiffness(prob) if prob.kind == ELASTIC else magnetic_stiffness(prob)
+
+
+def element_node_factors(prob: Problem, elements=None):
+    """(k, 3) |detJ| * (a_i + b_i (x2+x3)/2 + c_i (y2+y3)/2), written term by term as in
+    elements.py:46-51 (it evaluates to (0, area, area))."""
+    conn = prob.conn if elements is None else prob.conn[np.asarray(elements)]
+    p = prob.coords[conn]
+    x1, y1 = p[:, 0, 0], p[:, 0, 1]
+    x2, y2 = p[:, 1, 0], p[:, 1, 1]
+    x3, y3 = p[:, 2, 0], p[:, 2, 1]
+    detj = np.abs((x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1))
+    ff = form_functions(p)
+    out = np.empty((p.shape[0], 3))
+    for i in range(3):
+        a, b, c = ff[:, i, 0], ff[:, i, 1], ff[:, i, 2]
+        out[:, i] = detj * (a + 0.5 * b * x2 + 0.5 * c * y2 + 0.5 * b * x3 + 0.5 * c * y3)
+    return out
+
+
+# ---------------------------------------------------------------- loads and conditions
+
+
+def dedup_last_wins(keys, values):
+    """Dict round trip of analysis.py:28-110: ``d[key] = value`` for every entry in
+    order, then the items in insertion order.  Returns (unique keys in order of first
+    occurrence, the LAST value seen for each)."""
+    keys = np.asarray(keys, dtype=np.int64)
+    values = np.asarray(values, dtype=np.float64)
+    if keys.size == 0:
+        return keys, values
+    uniq, first = np.unique(keys, return_index=True)
+    _, last_rev = np.unique(keys[::-1], return_index=True)
+    last = keys.size - 1 - last_rev
+    order = np.argsort(first, kind="stable")
+    return uniq[order], values[last[order]]
+
+
+def node_load_list(prob: Problem):
+    """(dof keys, values) before de-duplication, in the order of
+    source_c_matrix_loads (analysis.py:465-469): user NodeLoads, then element loads
+    (analysis.py:407-429 with loads.py:24-35), then edge loads (analysis.py:431-447)."""
+    d = prob.dim
+    keys = [prob.node_load_node * d + (prob.node_load_dim - 1)]
+    vals = [prob.node_load_value]
+    for s in prob.element_loads:
+        conn = prob.conn[s.elements]
+        area = triangle_area(prob.coords[conn])
+        total_area = 0.0
+        for a in area.tolist():          # sum(...) of loads.py:32, left to right
+            total_area += a
+        per_element = s.value * area / total_area
+        fac = element_node_factors(prob, s.elements)
+        keys.append((conn.astype(np.int64) * d + (s.dimension - 1)).reshape(-1))
+        vals.append((per_element[:, None] * fac).reshape(-1))
+    for (na, nb), dim, v in zip(prob.edge_load_nodes.tolist(), prob.edge_load_dim.tolist(),
+                               prob.edge_load_value.tolist()):
+        keys.append(np.array([na * d + dim - 1, nb * d + dim - 1]))
+        vals.append(np.array([v * 0.5, v * 0.5]))
+    return np.concatenate(keys).astype(np.int64), np.concatenate(vals)
+
+
+def boundary_condition_list(prob: Problem):
+    """(dof keys, values) before de-duplication, in the order of
+    c_matrix_boundary_conditions (analysis.py:252-256): node conditions, element
+    conditions (analysis.py:201-220), edge conditions (analysis.py:222-239)."""
+    d = prob.dim
+    keys = [prob.node_bc_node * d + (prob.node_bc_dim - 1)]
+    vals = [prob.node_bc_value]
+    if prob.element_bc_element.size:
+        fac = element_node_factors(prob, prob.element_bc_element)
+        conn = prob.conn[prob.element_bc_element].astype(np.int64)
+        keys.append((conn * d + (prob.element_bc_dim[:, None] - 1)).reshape(-1))
+        vals.append((prob.element_bc_value[:, None] * fac).reshape(-1))
+    if prob.edge_bc_nodes.size:
+        keys.append((prob.edge_bc_nodes * d + (prob.edge_bc_dim[:, None] - 1)).reshape(-1))
+        vals.append(np.repeat(prob.edge_bc_value * 0.5, 2))
+    return np.concatenate(keys).astype(np.int64), np.concatenate(vals)
+
+
+def boundary_conditions(prob: Problem):
+    """De-duplicated (dof, value) of the multiplier rows, in multiplier order."""
+    return dedup_last_wins(*boundary_condition_list(prob))
+
+
+def node_loads(prob: Problem):
+    return dedup_last_wins(*node_load_list(prob))
+
+
+# ---------------------------------------------------------------- global system
+
+
+def k_matrix_data(prob: Problem):
+    """COO triplets of all element matrices (analysis.py:324-339, :714-735):
+    row = repeat(L, len(L)), col = tile(L, len(L)) with L the element's DOFs
+    (node-major, dimension-minor)."""
+    d = prob.dim
+    ke = element_stiffness(prob)
+    L = (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(-1, 3 * d)
+    nl = 3 * d
+    row = np.repeat(L, nl, axis=1).reshape(-1)
+    col = np.tile(L, (1, nl)).reshape(-1)
+    return ke.reshape(-1), row, col
+
+
+def m_matrix_data(prob: Problem):
+    if prob.kind != ELASTIC:
+        raise NotImplementedError("mass matrices exist for elasticity elements only")
+    d = prob.dim
+    me = elastic_mass(prob)
+    L = (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(-1, 3 * d)
+    nl = 3 * d
+    return me.reshape(-1), np.repeat(L, nl, axis=1).reshape(-1), np.tile(L, (1, nl)).reshape(-1)
+
+
+def create_matrix(prob: Problem):
+    """Augmented saddle-point matrix as scipy builds it (analysis.py:617-663)."""
+    data, row, col = k_matrix_data(prob)
+    bc_dof, _ = boundary_conditions(prob)
+    nd = prob.n_dof
+    i = np.arange(bc_dof.size, dtype=np.int64)
+    data = np.concatenate([data, np.ones(2 * bc_dof.size)])
+    row = np.concatenate([row, np.stack([nd + i, bc_dof], axis=1).reshape(-1)])
+    col = np.concatenate([col, np.stack([bc_dof, nd + i], axis=1).reshape(-1)])
+    return sp.csr_matrix((data, (row, col)))
+
+
+def create_source_matrix(prob: Problem):
+    """Dense (n*dim + n_bc, 1) right-hand side (analysis.py:665-708, :737-739)."""
+    lk, lv = node_loads(prob)
+    bc_dof, bc_val = boundary_conditions(prob)
+    nd = prob.n_dof
+    f = np.zeros((nd + bc_dof.size, 1))
+    np.add.at(f[:, 0], lk, lv)
+    f[nd:, 0] += bc_val
+    return f
+
+
+def solve(prob: Problem):
+    """The reference's solve (analysis.py:816-828): spsolve with NATURAL column order
+    (UMFPACK is not installed, so scipy uses SuperLU, as in a default install).
+    Returns the list [u..., lambda...]."""
+    k = create_matrix(prob)
+    f = create_source_matrix(prob)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", sp.SparseEfficiencyWarning)
+        x = spla.spsolve(k, f, permc_spec='NATURAL', use_umfpack=True)
+    return list(x)
+
+
+def _matrix_sparse(data, row, col):
+    """Dict merge then csc_matrix (analysis.py:387-405); the dict sums duplicates
+    in triplet order."""
+    key = row * (max(int(col.max()), 0) + 1) + col if row.size else row
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    starts = np.flatnonzero(np.r_[True, ks[1:] != ks[:-1]]) if ks.size else ks
+    vals = np.empty(starts.size)
+    ds = data[order]
+    ends = np.r_[starts[1:], ks.size]
+    for j, (s, e) in enumerate(zip(starts.tolist(), ends.tolist())):
+        acc = ds[s]
+        for t in range(s + 1, e):
+            acc = acc + ds[t]
+        vals[j] = acc
+    return sp.csc_matrix((vals, (row[order][starts], col[order][starts])))
+
+
+def k_matrix_sparse(prob: Problem):
+    return _matrix_sparse(*k_matrix_data(prob))
+
+
+def m_matrix_sparse(prob: Problem):
+    return _matrix_sparse(*m_matrix_data(prob))
+
+
+# ---------------------------------------------------------------- large sizes
+
+
+def reduced_system(prob: Problem):
+    """Eliminated SPD system: K with the constrained DOFs removed and their values
+    moved to the right-hand side.  Returns (A_ff, b_f, free dofs, bc dofs, bc values,
+    full K (no multipliers), F loads)."""
+    data, row, col = k_matrix_data(prob)
+    nd = prob.n_dof
+    K = sp.csr_matrix((data, (row, col)), shape=(nd, nd))
+    lk, lv = node_loads(prob)
+    F = np.zeros(nd)
+    np.add.at(F, lk, lv)
+    bc_dof, bc_val = boundary_conditions(prob)
+    mask = np.ones(nd, bool)
+    mask[bc_dof] = False
+    free = np.flatnonzero(mask)
+    g = np.zeros(nd)
+    g[bc_dof] = bc_val
+    b = F - K @ g
+    return K[free][:, free].tocsc(), b[free], free, bc_dof, bc_val, K, F
+
+
+def solve_reduced(prob: Problem, method="direct", tol=1e-12, maxiter=200000):
+    """Solution [u..., lambda...] from the eliminated system: SuperLU with COLAMD
+    ("direct") or scipy CG with Jacobi ("cg").  Used where NATURAL spsolve on the
+    saddle system does not fit in host memory; the multipliers come from
+    lambda_k = (F - K u)[p_k], the first block row of the saddle system."""
+    A, b, free, bc_dof, bc_val, K, F = reduced_system(prob)
+    if method == "direct":
+        uf = spla.spsolve(A, b, permc_spec='COLAMD')
+    else:
+        dinv = 1.0 / A.diagonal()
+        M = spla.LinearOperator(A.shape, matvec=lambda v: dinv * v)
+        uf, info = spla.cg(A, b, rtol=tol, atol=0.0, maxiter=maxiter, M=M)
+    u = np.zeros(prob.n_dof)
+    u[free] = uf
+    u[bc_dof] = bc_val
+    lam = (F - K @ u)[bc_dof]
+    return np.concatenate([u, lam])

@@ -1,0 +1,20 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (ROOT, os.path.dirname(os.path.abspath(__file__))):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built library")
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """The built library on a machine with a GPU; GPU tests fail (not skip) without it."""
+    from finite_elements_gb300 import _lib
+    return _lib.load()

@@ -1,0 +1,137 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports every
+function include/fe_gb300.h declares; the Python bindings match; the flattening of
+the drop-in object API reproduces the golden problem arrays."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fe_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(fe_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for must in ("fe_mesh_create", "fe_set_elastic_materials", "fe_set_mu", "fe_set_node_loads",
+                 "fe_set_element_loads", "fe_set_dirichlet", "fe_assemble", "fe_export_csr",
+                 "fe_export_rhs", "fe_solve", "fe_destroy"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from finite_elements_gb300 import _lib
+    lib = _lib.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    exported = set(re.findall(r" T (fe_\w+)", out))
+    assert set(declared_functions()) <= exported
+    # the ctypes table covers the header
+    assert set(declared_functions()) == set(_lib.exported_symbols())
+
+
+def test_library_calls_without_gpu_fail_loudly():
+    """No CPU fallback: on a machine without a CUDA device the first call fails with
+    a CUDA status."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from finite_elements_gb300 import _lib
+    prob, _, _ = gc.load("ex1_stress")
+    with pytest.raises(_lib.FeError) as e:
+        _lib.Handle(_lib.FE_KIND_ELASTIC_TRI, prob.coords, prob.conn)
+    assert e.value.status == _lib.FE_CUDA_ERR
+
+
+def test_status_strings():
+    from finite_elements_gb300 import _lib
+    lib = _lib.load()
+    assert lib.fe_status_string(_lib.FE_MAXITER) == b"FE_MAXITER"
+    assert lib.fe_version() >= 1
+
+
+def build_objects(name):
+    """The golden case as drop-in objects (same construction as make_golden.py)."""
+    from finite_elements_gb300 import conditions as C, elements as El, loads as L, mesh as M
+    prob, groups, ref = gc.load(name)
+    nodes = [M.Node2D(x, y) for x, y in prob.coords.tolist()]
+    tris = [M.TriangularElement2D([nodes[i] for i in row]) for row in prob.conn.tolist()]
+    if prob.kind == "elastic":
+        elems = [El.ElasticityTriangularElement2D(t, prob.E[k], prob.nu[k], prob.rho[k], prob.thickness[k])
+                 for k, t in enumerate(tris)]
+    else:
+        elems = [El.MagneticElement2D(t, prob.mu[k]) for k, t in enumerate(tris)]
+    mesh = M.Mesh([M.ElementsGroup(elems[a:b]) for a, b in zip(groups[:-1], groups[1:])])
+    mesh.nodes = nodes
+    mesh.node_to_index = {p: i for i, p in enumerate(nodes)}
+    kw = dict(
+        node_loads=[L.NodeLoad(nodes[n], v, d) for n, d, v in
+                    zip(prob.node_load_node, prob.node_load_dim, prob.node_load_value)],
+        element_loads=[L.ElementsLoad([elems[k] for k in s.elements], s.value, s.dimension)
+                       for s in prob.element_loads],
+        edge_loads=[L.EdgeLoad(M.LineSegment2D(nodes[a], nodes[b]), v, d) for (a, b), d, v in
+                    zip(prob.edge_load_nodes.tolist(), prob.edge_load_dim, prob.edge_load_value)],
+        magnet_loads=[], continuity_conditions=[],
+        node_boundary_conditions=[C.NodeBoundaryCondition(nodes[n], v, d) for n, d, v in
+                                  zip(prob.node_bc_node, prob.node_bc_dim, prob.node_bc_value)],
+        element_boundary_conditions=[C.ElementBoundaryCondition(elems[k], v, d) for k, d, v in
+                                     zip(prob.element_bc_element, prob.element_bc_dim,
+                                         prob.element_bc_value)],
+        edge_boundary_conditions=[C.EdgeBoundaryCondition(M.LineSegment2D(nodes[a], nodes[b]), v, d)
+                                  for (a, b), d, v in zip(prob.edge_bc_nodes.tolist(), prob.edge_bc_dim,
+                                                          prob.edge_bc_value)])
+    if prob.kind == "elastic":
+        kw.update(plane_strain=prob.plane_strain, plane_stress=prob.plane_stress)
+    return prob, ref, mesh, kw
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_object_api_flattens_to_the_golden_problem(name):
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    prob, ref, mesh, kw = build_objects(name)
+    fea = FiniteElementAnalysis(mesh=mesh, **kw)
+    p = fea.problem()
+    np.testing.assert_array_equal(p.coords, prob.coords)
+    np.testing.assert_array_equal(p.conn, prob.conn)
+    for f in ("node_load_node", "node_load_dim", "node_load_value", "node_bc_node", "node_bc_dim",
+              "node_bc_value", "element_bc_element", "edge_bc_nodes", "edge_load_nodes"):
+        np.testing.assert_array_equal(getattr(p, f), getattr(prob, f))
+    assert len(p.element_loads) == len(prob.element_loads)
+    for a, b in zip(p.element_loads, prob.element_loads):
+        np.testing.assert_array_equal(a.elements, b.elements)
+        assert a.value == b.value and a.dimension == b.dimension
+
+
+def test_out_of_scope_inputs_raise():
+    from finite_elements_gb300 import conditions as C
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    prob, ref, mesh, kw = build_objects("ex1_stress")
+    kw["continuity_conditions"] = [C.ContinuityCondition(mesh.nodes[0], mesh.nodes[1], 1)]
+    with pytest.raises(NotImplementedError):
+        FiniteElementAnalysis(mesh=mesh, **kw).problem()
+
+
+def test_plane_flag_errors_match_reference():
+    from finite_elements_gb300.engine import check_plane_flags
+    with pytest.raises(ValueError, match="just one of plane_strain or plane_stress can be True"):
+        check_plane_flags(True, True)
+    with pytest.raises(ValueError, match="one of plane_strain or plane_stress must be True"):
+        check_plane_flags(False, None)
+
+
+def test_create_source_matrix_before_create_matrix_is_a_type_error():
+    """The reference sizes F from state only create_matrix sets (analysis.py:737-739)."""
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    prob, ref, mesh, kw = build_objects("ex1_stress")
+    with pytest.raises(TypeError):
+        FiniteElementAnalysis(mesh=mesh, **kw).create_source_matrix()

@@ -1,0 +1,150 @@
+"""CUDA path against the reference's golden vectors, through the C ABI.
+
+Tolerances (written here, as the bar for each quantity):
+* CSR pattern (indptr, indices, shape): bit-exact;
+* matrix values, F, element matrices: max |difference| <= 1e-13 * max |reference|;
+* solution [u, lambda] of the FP64 path: ||x - x_ref|| <= 1e-10 ||x_ref||;
+* mixed-precision path to 1e-8 relative residual: ||u - u_ref|| <= 1e-7 ||u_ref||.
+"""
+import warnings
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+VAL_TOL = 1e-13
+SOL_TOL = 1e-10
+MIXED_TOL = 1e-7
+
+
+def relmax(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def systems(gpu_lib):
+    from finite_elements_gb300.engine import GpuSystem
+    out = {}
+    for name in gc.names():
+        prob, groups, ref = gc.load(name)
+        out[name] = (GpuSystem(prob), prob, ref)
+    yield out
+    for s, _, _ in out.values():
+        s.close()
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_create_matrix_pattern_and_values(systems, name):
+    s, prob, ref = systems[name]
+    K = s.create_matrix()
+    assert tuple(K.shape) == tuple(ref["K_shape"])
+    np.testing.assert_array_equal(K.indptr, ref["K_indptr"])
+    np.testing.assert_array_equal(K.indices, ref["K_indices"])
+    assert K.indices.dtype == ref["K_indices"].dtype
+    assert relmax(K.data, ref["K_data"]) <= VAL_TOL
+    assert K.has_canonical_format
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_create_source_matrix(systems, name):
+    s, prob, ref = systems[name]
+    F = s.create_source_matrix()
+    assert F.shape == (ref["F"].size, 1)
+    assert relmax(F[:, 0], ref["F"]) <= VAL_TOL
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_k_and_m_matrix_sparse(systems, name):
+    s, prob, ref = systems[name]
+    ks = s.k_matrix_sparse()
+    assert tuple(ks.shape) == tuple(ref["Ks_shape"])
+    np.testing.assert_array_equal(ks.indptr, ref["Ks_indptr"])
+    np.testing.assert_array_equal(ks.indices, ref["Ks_indices"])
+    assert relmax(ks.data, ref["Ks_data"]) <= VAL_TOL
+    if "Ms_data" in ref:
+        ms = s.m_matrix_sparse()
+        np.testing.assert_array_equal(ms.indptr, ref["Ms_indptr"])
+        np.testing.assert_array_equal(ms.indices, ref["Ms_indices"])
+        assert relmax(ms.data, ref["Ms_data"]) <= VAL_TOL
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_element_matrices(systems, name):
+    s, prob, ref = systems[name]
+    assert relmax(s.element_matrices("K"), ref["Ke"]) <= VAL_TOL
+    if "Me" in ref:
+        assert relmax(s.element_matrices("M"), ref["Me"]) <= VAL_TOL
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_bc_order_and_values(systems, name):
+    s, prob, ref = systems[name]
+    np.testing.assert_array_equal(s.bc_dof, ref["bc_dof"])
+    np.testing.assert_array_equal(s.bc_value, ref["bc_value"])
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_solve_fp64_matches_spsolve(systems, name):
+    s, prob, ref = systems[name]
+    x, st = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    assert st.status == 0, st.as_dict()
+    assert x.shape == ref["x"].shape
+    err = np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])
+    assert err <= SOL_TOL, (err, st.as_dict())
+
+
+@pytest.mark.parametrize("name", gc.names())
+@pytest.mark.parametrize("cheb", [0, 3])
+def test_solve_mixed_matches_spsolve(systems, name, cheb):
+    s, prob, ref = systems[name]
+    x, st = s.solve(precision="mixed", tol=1e-8, cheb_degree=cheb)
+    assert st.status == 0, st.as_dict()
+    assert st.relres <= 1e-8
+    n = prob.n_dof
+    err = np.linalg.norm(x[:n] - ref["x"][:n]) / np.linalg.norm(ref["x"][:n])
+    assert err <= MIXED_TOL, (err, st.as_dict())
+
+
+@pytest.mark.parametrize("name", ["c1_cantilever", "c3_plane_strain_30x15", "c2_magnetostatic_40x20"])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_lanes_and_chebyshev_give_the_same_solution(systems, name, lanes):
+    s, prob, ref = systems[name]
+    for cheb in (0, 2, 4):
+        x, st = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True, lanes=lanes, cheb_degree=cheb)
+        assert st.status == 0
+        assert np.linalg.norm(x - ref["x"]) <= SOL_TOL * np.linalg.norm(ref["x"])
+
+
+def test_solve_is_deterministic(systems):
+    s, prob, ref = systems["c1_cantilever"]
+    x1, _ = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    x2, _ = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    np.testing.assert_array_equal(x1, x2)
+    m1, _ = s.solve(precision="mixed", tol=1e-8)
+    m2, _ = s.solve(precision="mixed", tol=1e-8)
+    np.testing.assert_array_equal(m1, m2)
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_drop_in_analysis(gpu_lib, name):
+    """The reference's user-facing flow on drop-in objects: create_matrix,
+    create_source_matrix, solve -> Result."""
+    from test_abi_host import build_objects
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    from finite_elements_gb300.results import Result
+    prob, ref, mesh, kw = build_objects(name)
+    fea = FiniteElementAnalysis(mesh=mesh, **kw)
+    K = fea.create_matrix()
+    np.testing.assert_array_equal(K.indices, ref["K_indices"])
+    F = fea.create_source_matrix()
+    assert relmax(F[:, 0], ref["F"]) <= VAL_TOL
+    res = fea.solve()
+    assert isinstance(res, Result) and isinstance(res.result_vector, list)
+    assert res.mesh is mesh
+    assert len(res.result_vector) == ref["x"].size
+    x = np.array(res.result_vector)
+    assert np.linalg.norm(x - ref["x"]) <= SOL_TOL * np.linalg.norm(ref["x"])
+    assert res.dimension == prob.dim
