@@ -1,0 +1,349 @@
+#!/usr/bin/env python3
+"""Benchmark of the assembly-and-solve path: seconds per solve to a 1e-8 relative
+residual on the 4M-DOF plane-strain elasticity problem.
+
+One step = one full solve of the reference's FiniteElementAnalysis.solve() kind:
+pattern build, element kernels, segmented reduction, loads, Dirichlet elimination
+and PCG, from inputs already resident in HBM (``value``), and the same through the
+C ABI from host buffers, with the uploads of the mesh, materials, loads and
+conditions and the download of [u, lambda] inside the timed region (``e2e``).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  With N > 1 (torchrun) every rank solves its own
+replica of the problem on its own GPU: the path has no data exchange between GPUs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
+UNIT = "s/solve"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--nx", type=int, default=2000)
+    ap.add_argument("--ny", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--cheb", type=int, default=0, help="Chebyshev degree of the preconditioner")
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
+    ap.add_argument("--cpu-nx", type=int, default=200, help="grid of the bounded CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- multi-process plumbing
+
+class Dist:
+    """Rank bookkeeping; with WORLD_SIZE > 1 a gloo group provides the barrier and the
+    max over ranks (timing only: the solves exchange no data)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for p in self.samples:
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(self.NAMES, p[3:7]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline (oracle)
+
+def cpu_reference_sample(nx, seed):
+    """The reference's path restated by the oracle -- COO triplets, scipy csr_matrix,
+    spsolve(NATURAL) on the saddle system -- timed on one plane-strain nx x nx/2
+    instance of the same family (one host core: SuperLU is single-threaded)."""
+    from finite_elements_gb300 import meshgen
+    from oracle import fe_oracle as O
+    prob = meshgen.plane_strain_random(nx, nx // 2, seed=seed)
+    t0 = time.perf_counter()
+    O.solve(prob)
+    dt = time.perf_counter() - t0
+    return dt, prob.n_dof
+
+
+def cpu_info():
+    try:
+        model = [l.split(":", 1)[1].strip() for l in open("/proc/cpuinfo") if l.lower().startswith(("model name",))]
+        model = model[0] if model else os.uname().machine
+    except OSError:
+        model = os.uname().machine
+    return model, os.cpu_count()
+
+
+# ---------------------------------------------------------------- our path
+
+def run_ours(args, dist):
+    import ctypes
+
+    import numpy as np
+
+    from finite_elements_gb300 import _lib, meshgen
+    from finite_elements_gb300.engine import GpuSystem
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    prob = meshgen.plane_strain_random(args.nx, args.ny, seed=args.seed)
+    s = GpuSystem(prob, assemble=True)           # inputs uploaded: resident in HBM from here
+    h = s.handle
+    step_flags = _lib.FE_ASSEMBLE_PATTERN | _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
+    mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, want_host=False)
+    plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.cheb, want_host=False)
+
+    def device_step(opts):
+        h.call("fe_assemble", step_flags)
+        _, st = s.solve(**opts)
+        if st.status != _lib.FE_OK:
+            raise RuntimeError(f"solve failed: {st.as_dict()}")
+        return st
+
+    def launches():
+        c = ctypes.c_int64()
+        h.call("fe_launch_count", ctypes.byref(c))
+        return c.value
+
+    for _ in range(args.warmup):
+        device_step(mode)
+
+    # ---- headline: mixed precision, inputs resident in HBM
+    clocks = ClockSampler(dist.local_rank)
+    dist.barrier()
+    h.call("fe_synchronize")
+    l0 = launches()
+    clocks.start()
+    h.call("fe_event_record", 0)
+    stats = [device_step(mode) for _ in range(args.steps)]
+    h.call("fe_event_record", 1)
+    h.call("fe_synchronize")
+    clk = clocks.stop()
+    n_launch = launches() - l0
+    ms = ctypes.c_double()
+    h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
+    dist.barrier()
+    t_total = dist.max(ms.value / 1e3)
+    value = t_total / (args.steps * dist.world)
+    x_mixed = np.empty(prob.n_dof + len(s.bc_dof))
+    h.call("fe_get_solution", _lib.ptr(x_mixed))
+
+    # ---- plain FP64 PCG, same step
+    device_step(plain)
+    h.call("fe_synchronize")
+    h.call("fe_event_record", 2)
+    pstats = [device_step(plain) for _ in range(args.plain_steps)]
+    h.call("fe_event_record", 3)
+    h.call("fe_synchronize")
+    h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
+    plain_s = ms.value / 1e3 / max(args.plain_steps, 1)
+
+    # ---- FP64 oracle solution (tight tolerance) for the error of the mixed result
+    x_ref, st_ref = s.solve(precision="fp64", tol=1e-11, accept_stagnation=True)
+    n = prob.n_dof
+    err = float(np.linalg.norm(x_mixed[:n] - x_ref[:n]) / np.linalg.norm(x_ref[:n]))
+
+    # ---- roofline of the dominant kernel: the FP32 block SpMV of the PCG iteration
+    lanes = ctypes.c_int32()
+    spmv_ms = ctypes.c_double()
+    h.call("fe_autotune_spmv", _lib.FE_PREC_MIXED, ctypes.byref(lanes), ctypes.byref(spmv_ms))
+    h.call("fe_time_spmv", _lib.FE_PREC_MIXED, lanes.value, 50, ctypes.byref(spmv_ms))
+    info = s.info()
+    nnzb, n_nodes = info["n_blocks"], prob.n_nodes
+    spmv_bytes = nnzb * (16 + 4) + n_nodes * (4 + 8 + 8)
+    achieved = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
+    spmv64_ms = ctypes.c_double()
+    h.call("fe_time_spmv", _lib.FE_PREC_FP64, 1, 20, ctypes.byref(spmv64_ms))
+    spmv64_bytes = nnzb * (32 + 4) + n_nodes * (4 + 16 + 16)
+    s.close()
+
+    # ---- end to end through the C ABI, host buffers in and out
+    h2d = (prob.coords.nbytes + prob.conn.nbytes + prob.E.nbytes + prob.nu.nbytes + prob.thickness.nbytes
+           + prob.rho.nbytes + prob.node_load_node.size * 24 + prob.node_bc_node.size * 16)
+    e2e_times = []
+    e2e_opts = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, want_host=True)
+    for k in range(args.steps + 1):
+        dist.barrier()
+        t0 = time.perf_counter()
+        se = GpuSystem(prob, assemble=True)
+        x, st = se.solve(**e2e_opts)
+        dt = time.perf_counter() - t0
+        d2h = x.nbytes
+        se.close()
+        if k > 0:      # the first one warms the allocator
+            e2e_times.append(dt)
+    e2e_value = dist.max(sum(e2e_times)) / (len(e2e_times) * dist.world)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov/SpMV + f64 x, residual, reductions",
+        "data": f"synthetic, seeded (seed {args.seed})",
+        "config": {
+            "workload": f"plane strain {args.nx}x{args.ny} grid, {2 * args.nx * args.ny:,} triangles, "
+                        f"{prob.n_dof:,} DOF, E=10^U(9,12) per element, nu~U(0.2,0.45), left edge clamped, "
+                        f"random top-edge traction",
+            "mode": "mixed precision (FP32 diff-form SpMV + node-block Jacobi, FP64 refinement with "
+                    "reliable updates)" + (f", Chebyshev degree {args.cheb}" if args.cheb > 1 else ""),
+            "learned_warm_start": False,
+            "tol": args.tol, "step": "pattern + element kernels + reduction + loads + elimination + PCG",
+            "l2": "inputs larger than L2 (BSR values alone 448 MB FP64 / 224 MB FP32)",
+            "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
+        },
+        "iterations": stats[-1].iterations, "refinement_steps": stats[-1].outer,
+        "relres": stats[-1].relres, "err_vs_fp64": err,
+        "plain_fp64": {"s_per_solve": plain_s, "iterations": pstats[-1].iterations if pstats else None,
+                       "relres": pstats[-1].relres if pstats else None},
+        "speedup_vs_plain": plain_s / value if value > 0 else None,
+        "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv<2,float> (timed as k_spmv<2,float>)",
+                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_source": peak_src,
+                     "bytes_per_launch": spmv_bytes, "launch_us": spmv_ms.value * 1e3,
+                     "lanes": lanes.value, "traffic": None},
+        "fp64_spmv": {"launch_us": spmv64_ms.value * 1e3,
+                      "achieved_gbs": spmv64_bytes / (spmv64_ms.value * 1e-3) / 1e9,
+                      "fp64_tflops": 2 * 4 * nnzb / (spmv64_ms.value * 1e-3) / 1e12},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(n_launch),
+        "clocks": clk,
+    }
+    return out
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    if args.impl == "reference":
+        if dist.rank == 0:
+            model, ncpu = cpu_info()
+            times = []
+            if args.warmup + args.steps > 10 and args.cpu_nx == 200:
+                args.cpu_nx = 120   # keep the whole reference run within a few minutes
+            for k in range(args.warmup + args.steps):
+                dt, ndof = cpu_reference_sample(args.cpu_nx, args.seed + k)
+                if k >= args.warmup:
+                    times.append(dt)
+            v = sum(times) / len(times)
+            sample = (f"plane strain {args.cpu_nx}x{args.cpu_nx // 2} ({ndof:,} DOF) of the same family: "
+                      "the full 4M-DOF NATURAL spsolve does not fit in host memory")
+            print(json.dumps({
+                "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist.world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+                "config": {"workload": sample, "path": "oracle restatement of finite_elements' "
+                           "create_matrix/create_source_matrix + scipy spsolve(permc_spec='NATURAL')"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+                                 "host": f"{model}, {ncpu} cores"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        dist.close()
+        return
+    out = run_ours(args, dist)
+    if dist.rank == 0:
+        if dist.world == 1 and not args.no_cpu_baseline:
+            model, ncpu = cpu_info()
+            dt, ndof = cpu_reference_sample(args.cpu_nx, args.seed)
+            out["cpu_baseline"] = {
+                "value": dt, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"one solve of plane strain {args.cpu_nx}x{args.cpu_nx // 2} ({ndof:,} DOF) "
+                          "through the oracle's restatement of the reference path (COO, csr_matrix, "
+                          "spsolve NATURAL); NATURAL spsolve on 4M DOF does not fit in host memory",
+                "host": f"{model}, {ncpu} cores"}
+        print(json.dumps(out))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

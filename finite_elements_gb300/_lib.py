@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(_HERE, "libfe_gb300.so")
 FE_OK, FE_MAXITER, FE_BREAKDOWN, FE_NONFINITE, FE_BAD_INPUT, FE_CUDA_ERR, FE_NOT_READY = range(7)
 FE_KIND_ELASTIC_TRI, FE_KIND_MAGNETIC_TRI = 1, 2
 FE_PLANE_STRESS, FE_PLANE_STRAIN = 1, 2
-FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F = 1, 2, 4
+FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F, FE_ASSEMBLE_PATTERN = 1, 2, 4, 8
 FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
 FE_PREC_FP64, FE_PREC_MIXED = 0, 1
 FE_FLAG_ACCEPT_STAGNATION = 1
@@ -79,6 +79,7 @@ _SIGNATURES = {
     "fe_event_record": ([_P, _I32], C.c_int),
     "fe_event_elapsed_ms": ([_P, _I32, _I32, _PD], C.c_int),
     "fe_synchronize": ([_P], C.c_int),
+    "fe_launch_count": ([_P, _PI64], C.c_int),
     "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
     "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
 }

@@ -27,7 +27,7 @@ from .mesh import ArrayMesh
 from .problem import ELASTIC, MAGNETIC, ElementLoadSet, Problem
 from .results import Result
 
-DEFAULT_SOLVER = {"precision": "fp64", "tol": 1e-12, "accept_stagnation": True, "cheb_degree": 0}
+DEFAULT_SOLVER = {"precision": "fp64", "tol": 1e-14, "accept_stagnation": True, "cheb_degree": 0}
 
 
 class SolverConvergenceError(RuntimeError):

@@ -187,7 +187,13 @@ int fe_set_element_loads(fe_handle h, int64_t n_sets, const int64_t *set_ptr, co
         set_error("fe_set_element_loads: bad set list");
         return FE_BAD_INPUT;
     }
-    int64_t n_occ = n_sets > 0 ? set_ptr[n_sets] : 0;
+    if (n_sets == 0) {
+        h->n_load_sets = h->n_load_elems = 0;
+        h->load_seq_base = seq_base;
+        h->f_ready = h->sys_ready = false;
+        return FE_OK;
+    }
+    int64_t n_occ = set_ptr[n_sets];
     for (int64_t s = 0; s < n_sets; ++s)
         if (set_ptr[s + 1] < set_ptr[s] || set_ptr[0] != 0) {
             set_error("fe_set_element_loads: set pointers must start at 0 and not decrease");
@@ -249,6 +255,7 @@ int fe_assemble(fe_handle h, int32_t flags) {
         return FE_NOT_READY;
     }
     FE_CUDA(cudaEventRecord(h->events[0], h->stream));
+    if (flags & FE_ASSEMBLE_PATTERN) h->pattern_ready = false;
     FE_CHECK(build_pattern(h));
     if (flags & FE_ASSEMBLE_K) {
         FE_CHECK(assemble_stiffness(h));
@@ -388,6 +395,12 @@ int fe_event_elapsed_ms(fe_handle h, int32_t a, int32_t b, double *ms) {
 int fe_synchronize(fe_handle h) {
     FE_HANDLE_CHECK(h);
     FE_CUDA(cudaStreamSynchronize(h->stream));
+    return FE_OK;
+}
+
+int fe_launch_count(fe_handle h, int64_t *count) {
+    FE_HANDLE_CHECK(h);
+    if (count) *count = h->launches;
     return FE_OK;
 }
 

@@ -697,6 +697,7 @@ int validate_mesh(fe_handle_s *h) {
     if (n3 > 0) {
         k_validate_conn<<<grid_for(n3), kThreads, 0, h->stream>>>(h->conn.p, n3, h->n_nodes, h->err.p, mx.p);
         FE_LAUNCH_CHECK();
+        h->launches += 1;
     }
     int m = -1;
     FE_CUDA(cudaMemcpyAsync(&m, mx.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -738,6 +739,7 @@ int build_pattern(fe_handle_s *h) {
                                                       h->blk_row.p);
     FE_LAUNCH_CHECK();
     h->nnzb = nnzb;
+    h->launches += (n3 > 0 ? 2 : 0) + 2 + 2 * 3;
     dfree(h->cand);
     h->pattern_ready = true;
     return FE_OK;
@@ -756,6 +758,7 @@ int assemble_stiffness(fe_handle_s *h) {
             k_magnetic_ke<<<g, kElemBlock, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->mu.p, h->ke.p, h->err.p);
         FE_LAUNCH_CHECK();
     }
+    if (h->n_elem > 0) h->launches += 1;
     FE_CHECK(dalloc(h->kval, (size_t)std::max<int64_t>(h->nnzb * D * D, 1)));
     if (h->nnzb > 0) {
         int g = grid_for(h->nnzb, kThreads, 152 * 64);
@@ -767,6 +770,7 @@ int assemble_stiffness(fe_handle_s *h) {
                                                          h->inc.p, h->conn.p, h->ke.p, h->kval.p);
         FE_LAUNCH_CHECK();
     }
+    if (h->nnzb > 0) h->launches += 1;
     h->k_ready = true;
     return FE_OK;
 }
@@ -789,6 +793,7 @@ int assemble_mass(fe_handle_s *h) {
             h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p, h->inc.p, h->conn.p, h->me_scale.p, h->mval.p);
         FE_LAUNCH_CHECK();
     }
+    h->launches += (h->n_elem > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0);
     h->m_ready = true;
     return FE_OK;
 }
@@ -830,6 +835,7 @@ int assemble_loads(fe_handle_s *h) {
             h->load_seq_base, h->dim, h->n_elem, h->coords.p, h->conn.p, h->load_seq.p, h->F.p, h->err.p);
         FE_LAUNCH_CHECK();
     }
+    h->launches += 1 + (h->n_node_loads > 0 ? 2 : 0) + (h->n_load_elems > 0 ? 4 : 0);
     h->f_ready = true;
     return FE_OK;
 }
@@ -870,6 +876,7 @@ int apply_dirichlet(fe_handle_s *h) {
                                                   h->dinv32.p, h->err.p);
     }
     FE_LAUNCH_CHECK();
+    h->launches += (h->n_bc > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0) + 3;
     h->sys_ready = true;
     return FE_OK;
 }
@@ -879,6 +886,7 @@ int element_node_factors(fe_handle_s *h, int64_t n, const int64_t *elems_dev, do
     k_node_factors<<<grid_for(n), kThreads, 0, h->stream>>>(n, elems_dev, h->n_elem, h->coords.p, h->conn.p,
                                                             out_dev, h->err.p);
     FE_LAUNCH_CHECK();
+    h->launches += 1;
     return check_error_word(h, "fe_element_node_factors");
 }
 
@@ -959,6 +967,7 @@ int export_csr(fe_handle_s *h, int which, int64_t *indptr_host, int32_t *indices
         FE_CUDA(cudaMemcpyAsync(indices_host, idx.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         FE_CUDA(cudaMemcpyAsync(data_host, dat.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
+    h->launches += (nrows > 0 ? 2 : 0) + 3;
     int st = check_error_word(h, "fe_export_csr");
     for (int64_t i = 0; i <= nrows; ++i) indptr_host[i] = off_h[i];
     dfree(len), dfree(off), dfree(idx), dfree(dat);

@@ -175,6 +175,7 @@ struct fe_handle_s {
     fe::DBuf<int> err;                    // device error word
     int *err_host = nullptr;              // pinned
     double last_assemble_ms = 0.0;
+    int64_t launches = 0;                 // kernels launched (graph nodes included)
     bool have_solution = false;
 
     fe::SolverWork w;

@@ -14,11 +14,14 @@
 // * Preconditioner: node-block Jacobi (inverse d x d diagonal blocks), optionally
 //   followed by k-1 Chebyshev steps on D^-1 A; the Chebyshev interval comes from a
 //   Lanczos estimate of the largest eigenvalue built from the first PCG coefficients.
-// * Mixed precision: FP32 SpMV, preconditioner and Krylov vectors, with FP64 kept for
-//   the solution x, the reduction trees, and the refinement step: whenever the FP32
-//   recurrence residual has fallen by a factor 10, the FP64 true residual b - A x
-//   replaces it and the iteration continues along the same search direction
-//   (iterative refinement with reliable updates: the Krylov space is not restarted).
+// * Mixed precision: FP32 SpMV, preconditioner and Krylov vectors (r, p, q, z), with
+//   FP64 kept for the solution update x += alpha p, the reduction trees and the
+//   refinement step: whenever the FP32 recurrence residual has fallen by a factor 10,
+//   the FP64 true residual b - A x replaces it and the iteration continues along the
+//   same search direction (iterative refinement with reliable updates: the Krylov
+//   space is not restarted).  x stays FP64 because its own rounding would leave a
+//   residual of order eps32 * cond(A); GB300 runs FP64 FMAs at 1/59 of the FP32 rate,
+//   so that one FMA per DOF is the only FP64 arithmetic of the iteration.
 //   The FP32 SpMV uses the difference form y_r = sum_{m != r} A_rm (x_m - x_r) + S_r x_r,
 //   S_r the block row sum (zero at interior nodes: K annihilates translations), so
 //   FP32 rounding scales with the variation of x between neighbours instead of with
@@ -533,7 +536,7 @@ __global__ void k_multipliers(int64_t n_bc, const int64_t *__restrict__ bc_dof, 
 template <typename T>
 struct Sys {
     const T *val = nullptr, *dinv = nullptr;
-    double *x = nullptr;
+    double *x = nullptr;   // the solution, FP64 in both precisions
     T *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *zc = nullptr, *dch = nullptr;
 };
 
@@ -635,6 +638,7 @@ int enqueue_start(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *s
     k_start_finish<D, T, CONT><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, zf, s.p, part, sc);
     if (CONT) k_continue_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
     FE_LAUNCH_CHECK();
+    h->launches += 2 + (cb.k - 1) + (CONT ? 1 : 0);
     return FE_OK;
 }
 
@@ -646,6 +650,7 @@ int residual(fe_handle_s *h, const double *x, OUT *r, double *out) {
     k_residual<D, G, OUT><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p,
                                                              h->b.p, x, r, h->w.partials.p, &sc->ticket[4], out);
     FE_LAUNCH_CHECK();
+    h->launches += 1;
     return FE_OK;
 }
 
@@ -687,10 +692,12 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk) {
         }
         kk.k = cb.k, kk.G = G, kk.chunk = chunk, kk.x = s.p, kk.theta = cb.theta, kk.delta = cb.delta;
     }
+    const int per_iter = 3 + (cb.k - 1);
     for (;;) {
         FE_CHECK(read_scalars(h));
         if (w.sc_host->done) break;
         FE_CUDA(cudaGraphLaunch(w.graph[slot], h->stream));
+        h->launches += (int64_t)chunk * per_iter;
     }
     return FE_OK;
 }
@@ -752,6 +759,7 @@ int ensure_work(fe_handle_s *h, bool mixed) {
         FE_CHECK(dalloc(w.dch, n));
     } else {
         FE_CHECK(dalloc(w.r32, n));
+        FE_CHECK(dalloc(w.d32, n));
         FE_CHECK(dalloc(w.z32, n));
         FE_CHECK(dalloc(w.p32, n));
         FE_CHECK(dalloc(w.q32, n));
@@ -934,6 +942,7 @@ template <int D, int G>
 int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     SolverWork &w = h->w;
     Sys<float> s = make_sys<D, float>(h);
+    double *x64 = s.x;
     const int chunk = o->chunk > 0 ? o->chunk : 16;
     const int max_iter = o->max_iter > 0 ? o->max_iter : 400000;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 200;
@@ -950,17 +959,17 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         cb = make_cheb(o->cheb_degree, w.lmax[1], o->cheb_ratio > 0 ? o->cheb_ratio : 20.0);
     }
     if (o->x0 && bb != 0.0)
-        FE_CUDA(cudaMemcpyAsync(s.x, o->x0, h->n_dof * sizeof(double),
+        FE_CUDA(cudaMemcpyAsync(x64, o->x0, h->n_dof * sizeof(double),
                                 o->x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
     else
-        FE_CUDA(cudaMemsetAsync(s.x, 0, h->n_dof * sizeof(double), h->stream));
+        FE_CUDA(cudaMemsetAsync(x64, 0, h->n_dof * sizeof(double), h->stream));
     if (bb == 0.0) {
         st->relres = 0;
         st->status = FE_OK;
         return FE_OK;
     }
-    // r32 = b - A x (FP64 residual, stored in FP32)
-    FE_CHECK((residual<D, G, float>(h, o->x0 ? s.x : nullptr, s.r, &sc->rr)));
+    // r32 = b - A x64 (FP64 residual, stored in FP32)
+    FE_CHECK((residual<D, G, float>(h, o->x0 ? x64 : nullptr, s.r, &sc->rr)));
     FE_CHECK(read_scalars(h));
     double rr_true = w.sc_host->rr;
     st->spmv += o->x0 ? 1 : 0;
@@ -985,8 +994,8 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         total += it;
         st->spmv += it * cb.k + (cb.k - 1);
         ++outer;
-        // refinement step: FP64 true residual replaces the FP32 recurrence residual
-        FE_CHECK((residual<D, G, float>(h, s.x, s.r, &sc->rr)));
+        // refinement step: the FP64 true residual replaces the FP32 recurrence residual
+        FE_CHECK((residual<D, G, float>(h, x64, s.r, &sc->rr)));
         st->spmv += 1;
         FE_CHECK(read_scalars(h));
         double rr_new = w.sc_host->rr;
@@ -1003,7 +1012,7 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         }
         if (stv == FE_BREAKDOWN) {
             // lost positive definiteness in FP32: restart the Krylov space from the
-            // true residual once; give up if that makes no progress either
+            // true residual; give up if that makes no progress either
             if (it == 0) {
                 status = stv;
                 break;
@@ -1066,6 +1075,7 @@ int recover_multipliers(fe_handle_s *h) {
         k_multipliers<1><<<g, kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->blk_ptr.p, h->blk_col.p, h->kval.p,
                                                         h->F.p, h->w.x.p, h->lambda.p);
     FE_LAUNCH_CHECK();
+    h->launches += 1;
     return FE_OK;
 }
 

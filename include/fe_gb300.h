@@ -46,11 +46,16 @@ extern "C" {
 #define FE_ASSEMBLE_K  1
 #define FE_ASSEMBLE_M  2
 #define FE_ASSEMBLE_F  4
+#define FE_ASSEMBLE_PATTERN 8   /* rebuild the sparsity pattern even if the mesh has one */
 
 /* matrices for fe_export_sizes / fe_export_csr */
 #define FE_MAT_K_AUGMENTED  1   /* [[K, C^T], [C, 0]] in CSR, as create_matrix returns   */
 #define FE_MAT_K_CSC        2   /* K without multipliers in CSC, as k_matrix_sparse      */
 #define FE_MAT_M_CSC        3   /* M without multipliers in CSC, as m_matrix_sparse      */
+
+/* fe_solve_opts.flags */
+#define FE_SOLVE_ACCEPT_STAGNATION 1   /* FP64: a true residual that restarts no longer
+                                          lower (rounding floor) ends the solve with FE_OK */
 
 /* solver precision */
 #define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
@@ -70,7 +75,7 @@ typedef struct fe_solve_opts {
     int32_t x0_device;     /* 1 if x0 is a device pointer                                 */
     int32_t lanes;         /* lanes per block row in SpMV: 1,2,4,8; 0 = autotuned         */
     int32_t chunk;         /* PCG iterations per graph launch; 0 = default                */
-    int32_t flags;         /* reserved, 0                                                 */
+    int32_t flags;         /* FE_SOLVE_ACCEPT_STAGNATION: FP64 rounding floor ends the solve */
 } fe_solve_opts;
 
 typedef struct fe_solve_stats {
@@ -157,6 +162,9 @@ int fe_info(fe_handle h, int64_t *n_dof, int64_t *n_bc, int64_t *n_blocks);
 int fe_event_record(fe_handle h, int32_t slot);
 int fe_event_elapsed_ms(fe_handle h, int32_t slot_a, int32_t slot_b, double *ms);
 int fe_synchronize(fe_handle h);
+/* Number of this library's kernels the handle has launched so far (graph-captured
+ * launches included, counted per kernel node executed). */
+int fe_launch_count(fe_handle h, int64_t *count);
 /* Lanes per block row the autotuner chose for SpMV in the given precision. */
 int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double *ms_out);
 /* Average device time of one SpMV with the given lanes (reps repetitions). */

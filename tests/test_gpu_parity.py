@@ -89,7 +89,7 @@ def test_bc_order_and_values(systems, name):
 @pytest.mark.parametrize("name", gc.names())
 def test_solve_fp64_matches_spsolve(systems, name):
     s, prob, ref = systems[name]
-    x, st = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    x, st = s.solve(precision="fp64", tol=1e-14, accept_stagnation=True)
     assert st.status == 0, st.as_dict()
     assert x.shape == ref["x"].shape
     err = np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])
@@ -113,15 +113,15 @@ def test_solve_mixed_matches_spsolve(systems, name, cheb):
 def test_lanes_and_chebyshev_give_the_same_solution(systems, name, lanes):
     s, prob, ref = systems[name]
     for cheb in (0, 2, 4):
-        x, st = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True, lanes=lanes, cheb_degree=cheb)
+        x, st = s.solve(precision="fp64", tol=1e-14, accept_stagnation=True, lanes=lanes, cheb_degree=cheb)
         assert st.status == 0
         assert np.linalg.norm(x - ref["x"]) <= SOL_TOL * np.linalg.norm(ref["x"])
 
 
 def test_solve_is_deterministic(systems):
     s, prob, ref = systems["c1_cantilever"]
-    x1, _ = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
-    x2, _ = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    x1, _ = s.solve(precision="fp64", tol=1e-14, accept_stagnation=True)
+    x2, _ = s.solve(precision="fp64", tol=1e-14, accept_stagnation=True)
     np.testing.assert_array_equal(x1, x2)
     m1, _ = s.solve(precision="mixed", tol=1e-8)
     m2, _ = s.solve(precision="mixed", tol=1e-8)
