@@ -510,6 +510,16 @@ k_continue_direction(int64_t n_nodes, const T *__restrict__ z, T *__restrict__ p
     }
 }
 
+// x[dof_k] = g_k on every constrained DOF.  The eliminated rows are identity rows
+// decoupled from the free ones, so with this start their residual is exactly zero
+// and node-block Jacobi keeps them exact for the whole solve.
+__global__ void k_set_prescribed(int64_t n_bc, const int64_t *__restrict__ bc_dof,
+                                 const double *__restrict__ bc_val, double *__restrict__ x) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_bc;
+         k += (int64_t)gridDim.x * blockDim.x)
+        x[bc_dof[k]] = bc_val[k];
+}
+
 // lambda_k = F[p_k] - (K u)[p_k], K the full (not eliminated) stiffness: the first
 // block row of the reference's saddle system, K u + C^T lambda = F.
 template <int D>
@@ -651,6 +661,22 @@ int residual(fe_handle_s *h, const double *x, OUT *r, double *out) {
                                                              h->b.p, x, r, h->w.partials.p, &sc->ticket[4], out);
     FE_LAUNCH_CHECK();
     h->launches += 1;
+    return FE_OK;
+}
+
+// Initial solution: x0 (host or device) or zero, with the prescribed values on the
+// constrained DOFs.  Returns whether x is non-zero.
+int init_solution(fe_handle_s *h, const fe_solve_opts *o, double *x) {
+    if (o->x0)
+        FE_CUDA(cudaMemcpyAsync(x, o->x0, h->n_dof * sizeof(double),
+                                o->x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    else
+        FE_CUDA(cudaMemsetAsync(x, 0, h->n_dof * sizeof(double), h->stream));
+    if (h->n_bc > 0) {
+        k_set_prescribed<<<grid_for(h->n_bc), kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->bc_val.p, x);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+    }
     return FE_OK;
 }
 
@@ -880,20 +906,18 @@ int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         if (!(w.lmax[0] > 0)) FE_CHECK((estimate_lmax<D, double, G>(h, s, bb, chunk, &w.lmax[0])));
         cb = make_cheb(o->cheb_degree, w.lmax[0], o->cheb_ratio > 0 ? o->cheb_ratio : 20.0);
     }
-    if (o->x0 && bb != 0.0)
-        FE_CUDA(cudaMemcpyAsync(s.x, o->x0, h->n_dof * sizeof(double),
-                                o->x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
-    else
-        FE_CUDA(cudaMemsetAsync(s.x, 0, h->n_dof * sizeof(double), h->stream));
     if (bb == 0.0) {
+        FE_CUDA(cudaMemsetAsync(s.x, 0, h->n_dof * sizeof(double), h->stream));
         st->relres = 0.0;
         st->status = FE_OK;
         return FE_OK;
     }
+    FE_CHECK(init_solution(h, o, s.x));
+    const bool nonzero = o->x0 || h->n_bc > 0;
     int total = 0, restarts = 0, status = FE_OK;
     double relres = 0, prev = 1e300;
-    FE_CHECK((residual<D, G, double>(h, o->x0 ? s.x : nullptr, s.r, &sc->rr)));
-    st->spmv += o->x0 ? 1 : 0;
+    FE_CHECK((residual<D, G, double>(h, nonzero ? s.x : nullptr, s.r, &sc->rr)));
+    st->spmv += nonzero ? 1 : 0;
     for (;;) {
         FE_CHECK(set_params(h, tol * tol, max_iter - total, bb, cb.theta));
         FE_CHECK((enqueue_start<D, double, G, false>(h, s, cb, sc, w.partials.p)));
@@ -958,21 +982,19 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         if (!(w.lmax[1] > 0)) FE_CHECK((estimate_lmax<D, float, G>(h, s, bb, chunk, &w.lmax[1])));
         cb = make_cheb(o->cheb_degree, w.lmax[1], o->cheb_ratio > 0 ? o->cheb_ratio : 20.0);
     }
-    if (o->x0 && bb != 0.0)
-        FE_CUDA(cudaMemcpyAsync(x64, o->x0, h->n_dof * sizeof(double),
-                                o->x0_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
-    else
-        FE_CUDA(cudaMemsetAsync(x64, 0, h->n_dof * sizeof(double), h->stream));
     if (bb == 0.0) {
+        FE_CUDA(cudaMemsetAsync(x64, 0, h->n_dof * sizeof(double), h->stream));
         st->relres = 0;
         st->status = FE_OK;
         return FE_OK;
     }
+    FE_CHECK(init_solution(h, o, x64));
+    const bool nonzero = o->x0 || h->n_bc > 0;
     // r32 = b - A x64 (FP64 residual, stored in FP32)
-    FE_CHECK((residual<D, G, float>(h, o->x0 ? x64 : nullptr, s.r, &sc->rr)));
+    FE_CHECK((residual<D, G, float>(h, nonzero ? x64 : nullptr, s.r, &sc->rr)));
     FE_CHECK(read_scalars(h));
     double rr_true = w.sc_host->rr;
-    st->spmv += o->x0 ? 1 : 0;
+    st->spmv += nonzero ? 1 : 0;
     int total = 0, outer = 0, status = FE_OK;
     double relres = sqrt(rr_true / bb);
     bool first = true;
