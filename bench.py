@@ -42,7 +42,10 @@ def parse_args():
     ap.add_argument("--ny", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cheb", type=int, default=0, help="Chebyshev degree of the preconditioner")
+    ap.add_argument("--cheb", type=int, default=3, help="Chebyshev degree of the mixed solve's preconditioner")
+    ap.add_argument("--plain-cheb", type=int, default=0, help="Chebyshev degree of the plain FP64 PCG")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline steps only (no plain / oracle / e2e legs), for profiler runs")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--cpu-nx", type=int, default=200, help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -184,7 +187,7 @@ def run_ours(args, dist):
     h = s.handle
     step_flags = _lib.FE_ASSEMBLE_PATTERN | _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
     mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, want_host=False)
-    plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.cheb, want_host=False)
+    plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.plain_cheb, want_host=False)
 
     def device_step(opts):
         h.call("fe_assemble", step_flags)
@@ -220,6 +223,10 @@ def run_ours(args, dist):
     value = t_total / (args.steps * dist.world)
     x_mixed = np.empty(prob.n_dof + len(s.bc_dof))
     h.call("fe_get_solution", _lib.ptr(x_mixed))
+    if args.quick:
+        s.close()
+        return {"metric": METRIC, "value": value, "unit": UNIT, "quick": True,
+                "iterations": stats[-1].iterations, "gpu_launches": int(n_launch)}
 
     # ---- plain FP64 PCG, same step
     device_step(plain)

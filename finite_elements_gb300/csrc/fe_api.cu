@@ -119,7 +119,7 @@ int fe_destroy(fe_handle h) {
     dfree(h->inc_ptr), dfree(h->inc), dfree(h->blk_ptr), dfree(h->blk_col), dfree(h->blk_row);
     dfree(h->cand), dfree(h->counts), dfree(h->scan_tmp);
     dfree(h->ke), dfree(h->me_scale), dfree(h->kval), dfree(h->mval), dfree(h->aval), dfree(h->aval32);
-    dfree(h->dinv), dfree(h->dinv32), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
+    dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
     dfree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
     for (auto &e : h->events)

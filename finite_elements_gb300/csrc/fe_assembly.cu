@@ -490,27 +490,45 @@ __global__ void k_eliminate(int64_t nnzb, const int32_t *__restrict__ blk_row,
     }
 }
 
-// FP32 copy of A in difference form for the mixed solver: every block keeps its
-// value except the diagonal one, which becomes the block row sum S_r = sum_m A_rm
-// (summed in FP64).  Then (A x)_r = sum_{m != r} A_rm (x_m - x_r) + S_r x_r.
+// Difference form of A: (A x)_r = sum_{m != r} A_rm (x_m - x_r) + S_r x_r with the
+// block row sum S_r = sum_m A_rm, which vanishes at interior nodes (K annihilates
+// translations).  Evaluated this way, rounding scales with the differences of x
+// between neighbours instead of with x.  S_r is summed in double-double (TwoSum), so
+// its own error is eps64 * |S_r| rather than eps64 * sum |A_rm|.  Writes S_r in FP64
+// (for the FP64 true residual) and the FP32 copy of A with S_r in the diagonal slot
+// (for the mixed solver's SpMV).
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+    s = __dadd_rn(a, b);
+    double bb = __dsub_rn(s, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+
 template <int D>
-__global__ void k_diff_form32(int64_t n_nodes, const int32_t *__restrict__ blk_ptr,
-                              const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
-                              float *__restrict__ aval32) {
+__global__ void k_diff_form(int64_t n_nodes, const int32_t *__restrict__ blk_ptr,
+                            const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
+                            double *__restrict__ srow, float *__restrict__ aval32) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
          r += (int64_t)gridDim.x * blockDim.x) {
-        double S[D * D];
+        double hi[D * D], lo[D * D];
 #pragma unroll
-        for (int k = 0; k < D * D; ++k) S[k] = 0.0;
+        for (int k = 0; k < D * D; ++k) hi[k] = 0.0, lo[k] = 0.0;
         int diag = -1;
         for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
             if (blk_col[s] == (int)r) diag = s;
 #pragma unroll
-            for (int k = 0; k < D * D; ++k) S[k] += aval[(int64_t)s * D * D + k];
+            for (int k = 0; k < D * D; ++k) {
+                double t, e;
+                two_sum(hi[k], aval[(int64_t)s * D * D + k], t, e);
+                hi[k] = t;
+                lo[k] = __dadd_rn(lo[k], e);
+            }
         }
-        if (diag >= 0)
 #pragma unroll
-            for (int k = 0; k < D * D; ++k) aval32[(int64_t)diag * D * D + k] = (float)S[k];
+        for (int k = 0; k < D * D; ++k) {
+            double S = __dadd_rn(hi[k], lo[k]);
+            srow[r * D * D + k] = S;
+            if (diag >= 0) aval32[(int64_t)diag * D * D + k] = (float)S;
+        }
     }
 }
 
@@ -854,13 +872,15 @@ int apply_dirichlet(fe_handle_s *h) {
     FE_CHECK(dalloc(h->aval32, nv));
     FE_CHECK(dalloc(h->b, (size_t)std::max<int64_t>(h->n_dof, 1)));
     FE_CHECK(dalloc(h->dinv, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
+    FE_CHECK(dalloc(h->srow, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
     FE_CHECK(dalloc(h->dinv32, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
     int gs = grid_for(h->nnzb, kThreads, 152 * 64), gn = grid_for(h->n_nodes, kThreads, 152 * 64);
     if (D == 2) {
         if (h->nnzb > 0)
             k_eliminate<2><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
                                                    h->aval.p, h->aval32.p);
-        k_diff_form32<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->aval32.p);
+        k_diff_form<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
+                                               h->aval32.p);
         k_eliminated_rhs<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
                                                     h->bc_val.p, h->kval.p, h->F.p, h->b.p);
         k_block_jacobi<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
@@ -869,7 +889,8 @@ int apply_dirichlet(fe_handle_s *h) {
         if (h->nnzb > 0)
             k_eliminate<1><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
                                                    h->aval.p, h->aval32.p);
-        k_diff_form32<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->aval32.p);
+        k_diff_form<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
+                                               h->aval32.p);
         k_eliminated_rhs<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
                                                     h->bc_val.p, h->kval.p, h->F.p, h->b.p);
         k_block_jacobi<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,

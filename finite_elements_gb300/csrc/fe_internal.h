@@ -167,6 +167,7 @@ struct fe_handle_s {
     fe::DBuf<double> aval;                // eliminated K (FP64)
     fe::DBuf<float> aval32;               // eliminated K (FP32, difference form)
     fe::DBuf<double> dinv;                // [n_nodes][d][d] inverse diagonal blocks
+    fe::DBuf<double> srow;                // [n_nodes][d][d] block row sums of A (difference form)
     fe::DBuf<float> dinv32;
     fe::DBuf<double> F;                   // loads [n_dof]
     fe::DBuf<double> b;                   // eliminated right-hand side [n_dof]

@@ -27,6 +27,8 @@
 //   FP32 rounding scales with the variation of x between neighbours instead of with
 //   x itself; smooth error modes are no longer swamped by rounding.
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <vector>
@@ -161,12 +163,13 @@ __device__ __forceinline__ NodeVec<D, T> apply_dinv(const T *__restrict__ dinv, 
 // the block row sum S_r and every other block multiplies x_m - x_r.
 // Every lane of the warp calls this (the shuffles need all 32); a lane whose row is
 // past the end passes valid = false and contributes nothing.
-template <int D, typename T, int G>
+// With SROW (FP64 difference form) the diagonal block comes from srow[r] instead of
+// the stored diagonal slot.
+template <int D, typename T, int G, bool DIFF = (sizeof(T) == 4), bool SROW = false>
 __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, const int32_t *__restrict__ ptr,
                                                      const int32_t *__restrict__ col,
                                                      const T *__restrict__ val, const T *__restrict__ x,
-                                                     int sub) {
-    constexpr bool DIFF = sizeof(T) == 4;
+                                                     int sub, const T *__restrict__ srow = nullptr) {
     NodeVec<D, T> acc, xr;
 #pragma unroll
     for (int a = 0; a < D; ++a) acc.v[a] = T(0), xr.v[a] = T(0);
@@ -179,19 +182,20 @@ __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, cons
 #pragma unroll
             for (int a = 0; a < D; ++a) xv.v[a] -= xr.v[a];
         }
+        const T *blk = (SROW && c == (int)r) ? srow + r * D * D : val + (int64_t)k * D * D;
         if constexpr (D == 2) {
             if constexpr (sizeof(T) == 8) {
-                const double2 b0 = __ldg(reinterpret_cast<const double2 *>(val) + 2 * (int64_t)k);
-                const double2 b1 = __ldg(reinterpret_cast<const double2 *>(val) + 2 * (int64_t)k + 1);
+                const double2 b0 = __ldg(reinterpret_cast<const double2 *>(blk));
+                const double2 b1 = __ldg(reinterpret_cast<const double2 *>(blk) + 1);
                 acc.v[0] += b0.x * xv.v[0] + b0.y * xv.v[1];
                 acc.v[1] += b1.x * xv.v[0] + b1.y * xv.v[1];
             } else {
-                const float4 b = __ldg(reinterpret_cast<const float4 *>(val) + k);
+                const float4 b = __ldg(reinterpret_cast<const float4 *>(blk));
                 acc.v[0] += b.x * xv.v[0] + b.y * xv.v[1];
                 acc.v[1] += b.z * xv.v[0] + b.w * xv.v[1];
             }
         } else {
-            acc.v[0] += __ldg(val + k) * xv.v[0];
+            acc.v[0] += __ldg(blk) * xv.v[0];
         }
     }
     if constexpr (G > 1) {
@@ -226,19 +230,20 @@ k_spmv(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restri
     }
 }
 
-// FP64 residual r = b - A x of the eliminated system (x == nullptr: r = b), stored as
-// OUT (double, or float for the mixed solver's residual replacement), and r.r in FP64.
+// FP64 true residual r = b - A x of the eliminated system (x == nullptr: r = b),
+// evaluated in the difference form with the double-double row sums, stored as OUT
+// (double, or float for the mixed solver's residual replacement), and r.r in FP64.
 template <int D, int G, typename OUT>
 __global__ void __launch_bounds__(kVecThreads)
 k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
-           const double *__restrict__ val, const double *__restrict__ b, const double *__restrict__ x,
-           OUT *__restrict__ r, double *partials, unsigned int *ticket, double *out) {
+           const double *__restrict__ val, const double *__restrict__ srow, const double *__restrict__ b,
+           const double *__restrict__ x, OUT *__restrict__ r, double *partials, unsigned int *ticket, double *out) {
     double lrr = 0.0;
     FE_ROW_LOOP(G) {
         const bool valid = row < n_nodes;
         NodeVec<D, double> v;
         if (x) {
-            v = row_product<D, double, G>(row, valid, ptr, col, val, x, sub);
+            v = row_product<D, double, G, true, true>(row, valid, ptr, col, val, x, sub, srow);
         } else {
 #pragma unroll
             for (int a = 0; a < D; ++a) v.v[a] = 0.0;
@@ -658,7 +663,8 @@ int residual(fe_handle_s *h, const double *x, OUT *r, double *out) {
     const int gs = vec_grid(h->n_nodes * G);
     PcgScalars *sc = h->w.sc.p;
     k_residual<D, G, OUT><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p,
-                                                             h->b.p, x, r, h->w.partials.p, &sc->ticket[4], out);
+                                                             h->srow.p, h->b.p, x, r, h->w.partials.p,
+                                                             &sc->ticket[4], out);
     FE_LAUNCH_CHECK();
     h->launches += 1;
     return FE_OK;
@@ -998,6 +1004,9 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     int total = 0, outer = 0, status = FE_OK;
     double relres = sqrt(rr_true / bb);
     bool first = true;
+    const bool restart_each = (o->flags & FE_SOLVE_RESTART_EACH_STEP) != 0;
+    const char *verbose_env = getenv("FE_VERBOSE");
+    const bool verbose = verbose_env && verbose_env[0] == '1';
     while (relres > tol) {
         if (outer >= max_outer || total >= max_iter) {
             status = FE_MAXITER;
@@ -1010,9 +1019,10 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
             FE_CHECK((enqueue_start<D, float, G, false>(h, s, cb, sc, w.partials.p)));
         else
             FE_CHECK((enqueue_start<D, float, G, true>(h, s, cb, sc, w.partials.p)));
-        first = false;
+        first = restart_each;
         FE_CHECK((run_loop<D, float, G>(h, s, cb, chunk)));
         const int it = w.sc_host->iter, stv = w.sc_host->status;
+        const double rr_rec = w.sc_host->rr;
         total += it;
         st->spmv += it * cb.k + (cb.k - 1);
         ++outer;
@@ -1021,6 +1031,9 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         st->spmv += 1;
         FE_CHECK(read_scalars(h));
         double rr_new = w.sc_host->rr;
+        if (verbose)
+            fprintf(stderr, "fe mixed step %d: %d it (status %d) fp32 residual %.3e -> true %.3e\n", outer, it, stv,
+                    sqrt(rr_rec / bb), sqrt(rr_new / bb));
         if (!isfinite(rr_new)) {
             status = FE_NONFINITE;
             relres = rr_new;

@@ -183,7 +183,7 @@ class GpuSystem:
 
     def solve(self, precision="fp64", tol=None, cheb_degree=0, max_iter=0, x0=None, lanes=0,
               accept_stagnation=False, inner_tol=0.0, cheb_ratio=0.0, chunk=0, max_outer=0,
-              want_host=True):
+              want_host=True, restart_each_step=False):
         """Solve the eliminated system on the GPU.  Returns (x, stats): x holds
         n_dof + n_bc values (u then the multipliers) or None with want_host=False."""
         o = SolveOpts()
@@ -200,7 +200,8 @@ class GpuSystem:
             o.x0 = x0a.ctypes.data
         o.lanes = lanes
         o.chunk = chunk
-        o.flags = _lib.FE_FLAG_ACCEPT_STAGNATION if accept_stagnation else 0
+        o.flags = ((_lib.FE_SOLVE_ACCEPT_STAGNATION if accept_stagnation else 0)
+                   | (_lib.FE_SOLVE_RESTART_EACH_STEP if restart_each_step else 0))
         st = SolveStats()
         x = np.empty(self.prob.n_dof + len(self.bc_dof)) if want_host else None
         lib = _lib.load()

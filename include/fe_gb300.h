@@ -56,6 +56,9 @@ extern "C" {
 /* fe_solve_opts.flags */
 #define FE_SOLVE_ACCEPT_STAGNATION 1   /* FP64: a true residual that restarts no longer
                                           lower (rounding floor) ends the solve with FE_OK */
+#define FE_SOLVE_RESTART_EACH_STEP 2   /* mixed: restart the Krylov space at every refinement
+                                          step (classic iterative refinement) instead of
+                                          continuing along the current direction          */
 
 /* solver precision */
 #define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
@@ -75,7 +78,7 @@ typedef struct fe_solve_opts {
     int32_t x0_device;     /* 1 if x0 is a device pointer                                 */
     int32_t lanes;         /* lanes per block row in SpMV: 1,2,4,8; 0 = autotuned         */
     int32_t chunk;         /* PCG iterations per graph launch; 0 = default                */
-    int32_t flags;         /* FE_SOLVE_ACCEPT_STAGNATION: FP64 rounding floor ends the solve */
+    int32_t flags;         /* FE_SOLVE_* bits                                              */
 } fe_solve_opts;
 
 typedef struct fe_solve_stats {
