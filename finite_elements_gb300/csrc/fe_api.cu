@@ -254,7 +254,7 @@ int fe_assemble(fe_handle h, int32_t flags) {
         set_error("fe_assemble: materials not set");
         return FE_NOT_READY;
     }
-    FE_CUDA(cudaEventRecord(h->events[0], h->stream));
+    FE_CUDA(cudaEventRecord(h->events[4], h->stream));
     if (flags & FE_ASSEMBLE_PATTERN) h->pattern_ready = false;
     FE_CHECK(build_pattern(h));
     if (flags & FE_ASSEMBLE_K) {
@@ -267,7 +267,7 @@ int fe_assemble(fe_handle h, int32_t flags) {
         h->sys_ready = false;
     }
     if (h->k_ready && h->f_ready && !h->sys_ready) FE_CHECK(apply_dirichlet(h));
-    FE_CUDA(cudaEventRecord(h->events[1], h->stream));
+    FE_CUDA(cudaEventRecord(h->events[5], h->stream));
     int err = check_error_word(h, "fe_assemble");
     if (err != FE_OK) {
         // nothing assembled from bad input may be used by a later export or solve
@@ -275,7 +275,7 @@ int fe_assemble(fe_handle h, int32_t flags) {
         return err;
     }
     float ms = 0;
-    FE_CUDA(cudaEventElapsedTime(&ms, h->events[0], h->events[1]));
+    FE_CUDA(cudaEventElapsedTime(&ms, h->events[4], h->events[5]));
     h->last_assemble_ms = ms;
     return FE_OK;
 }

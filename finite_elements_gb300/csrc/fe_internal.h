@@ -126,7 +126,9 @@ struct fe_handle_s {
     int64_t n_nodes = 0, n_elem = 0, n_dof = 0;
     int32_t max_node = -1;   // largest node index used by an element
     cudaStream_t stream = nullptr;
-    cudaEvent_t events[8] = {};
+    // events 0..3 belong to callers (fe_event_record); the library times its own
+    // steps with 4..5 (assembly), 6..7 (solve) and 8..9 (SpMV timing)
+    cudaEvent_t events[10] = {};
 
     // inputs
     fe::DBuf<double> coords;      // [n_nodes][2]

@@ -832,14 +832,14 @@ int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
     const int gs = vec_grid(h->n_nodes * G);
     for (int i = 0; i < 2; ++i)
         k_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, x, y);
-    FE_CUDA(cudaEventRecord(h->events[6], h->stream));
+    FE_CUDA(cudaEventRecord(h->events[8], h->stream));
     for (int i = 0; i < reps; ++i)
         k_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, x, y);
-    FE_CUDA(cudaEventRecord(h->events[7], h->stream));
+    FE_CUDA(cudaEventRecord(h->events[9], h->stream));
     FE_LAUNCH_CHECK();
-    FE_CUDA(cudaEventSynchronize(h->events[7]));
+    FE_CUDA(cudaEventSynchronize(h->events[9]));
     float t = 0;
-    FE_CUDA(cudaEventElapsedTime(&t, h->events[6], h->events[7]));
+    FE_CUDA(cudaEventElapsedTime(&t, h->events[8], h->events[9]));
     *ms = (double)t / std::max(reps, 1);
     return FE_OK;
 }
@@ -1081,7 +1081,7 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     FE_CHECK(ensure_work(h, mixed));
     int lanes = 1;
     FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
-    FE_CUDA(cudaEventRecord(h->events[4], h->stream));
+    FE_CUDA(cudaEventRecord(h->events[6], h->stream));
     int rc = dispatch_lanes(lanes, [&](auto g) {
         constexpr int G = decltype(g)::value;
         if (h->dim == 2) return mixed ? solve_mixed<2, G>(h, o, st) : solve_fp64<2, G>(h, o, st);
@@ -1089,10 +1089,10 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     });
     FE_CHECK(rc);
     FE_CHECK(recover_multipliers(h));
-    FE_CUDA(cudaEventRecord(h->events[5], h->stream));
-    FE_CUDA(cudaEventSynchronize(h->events[5]));
+    FE_CUDA(cudaEventRecord(h->events[7], h->stream));
+    FE_CUDA(cudaEventSynchronize(h->events[7]));
     float ms = 0;
-    FE_CUDA(cudaEventElapsedTime(&ms, h->events[4], h->events[5]));
+    FE_CUDA(cudaEventElapsedTime(&ms, h->events[6], h->events[7]));
     st->solve_ms = ms;
     st->assemble_ms = h->last_assemble_ms;
     h->have_solution = true;
