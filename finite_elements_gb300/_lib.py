@@ -82,6 +82,7 @@ _SIGNATURES = {
     "fe_launch_count": ([_P, _PI64], C.c_int),
     "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
     "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
+    "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
 }
 
 _lib = None

@@ -173,6 +173,19 @@ int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double 
 /* Average device time of one SpMV with the given lanes (reps repetitions). */
 int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out);
 
+/* No counterpart in the reference.  Exclusive scan of n int32 counts into n+1 int32
+ * offsets (offsets_dev[0] = 0, offsets_dev[n] = total; -1 there if the total does not
+ * fit in int32) that allocates nothing: for callers who may not call cudaMalloc --
+ * those whose device memory all comes from another owner's pool, or who are on a hot
+ * path where cudaMalloc/cudaFree would synchronise the device.  counts_dev and
+ * offsets_dev are the caller's device buffers; stream is a cudaStream_t (NULL = the
+ * default stream); the call only enqueues work.  The per-tile sums live in one fixed
+ * array inside the library (256 KiB per GPU, kept until exit), so n is limited to
+ * 67,108,864 (FE_BAD_INPUT beyond).  Calls that overlap on the GPU share that array
+ * and race.  The first call on each device looks the array up: make it before any
+ * stream capture.  Same results as the scan behind fe_export_csr's row pointers. */
+int fe_scan_counts_noalloc(const int32_t *counts_dev, int32_t *offsets_dev, int64_t n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
