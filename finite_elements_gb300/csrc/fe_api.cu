@@ -119,7 +119,8 @@ int fe_destroy(fe_handle h) {
     dfree(h->inc_ptr), dfree(h->inc), dfree(h->blk_ptr), dfree(h->blk_col), dfree(h->blk_row);
     dfree(h->cand), dfree(h->counts), dfree(h->scan_tmp);
     dfree(h->ke), dfree(h->me_scale), dfree(h->kval), dfree(h->mval), dfree(h->aval), dfree(h->aval32);
-    dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
+    dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->sell_off), dfree(h->sell_col);
+    dfree(h->sell_val64), dfree(h->sell_val32), dfree(h->diag64), dfree(h->diag32), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
     dfree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
     for (auto &e : h->events)
@@ -266,7 +267,10 @@ int fe_assemble(fe_handle h, int32_t flags) {
         FE_CHECK(assemble_loads(h));
         h->sys_ready = false;
     }
-    if (h->k_ready && h->f_ready && !h->sys_ready) FE_CHECK(apply_dirichlet(h));
+    if (h->k_ready && h->f_ready && !h->sys_ready) {
+        h->singular = false;
+        FE_CHECK(apply_dirichlet(h));
+    }
     FE_CUDA(cudaEventRecord(h->events[5], h->stream));
     int err = check_error_word(h, "fe_assemble");
     if (err != FE_OK) {

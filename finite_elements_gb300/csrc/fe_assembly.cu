@@ -618,6 +618,68 @@ __global__ void k_block_jacobi(int64_t n_nodes, const int32_t *__restrict__ blk_
     }
 }
 
+// ---------------------------------------------------------------- SELL-32 copy for the solver
+// Width of each slice: the largest off-diagonal block count of its 32 rows (rows past
+// the end count 0), stored as 32 * width so that a scan gives the slice offsets.
+__global__ void k_sell_widths(int64_t n_nodes, int64_t n_slices, const int32_t *__restrict__ blk_ptr,
+                              int32_t *__restrict__ len) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t sl = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < n_slices; sl += warps) {
+        int64_t r = sl * 32 + lane;
+        int w = r < n_nodes ? blk_ptr[r + 1] - blk_ptr[r] - 1 : 0;
+        w = max(w, 0);
+        for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
+        if (lane == 0) len[sl] = 32 * w;
+    }
+}
+
+template <int D>
+__global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__restrict__ blk_ptr,
+                            const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
+                            const double *__restrict__ srow, const int32_t *__restrict__ off,
+                            int32_t *__restrict__ col, double *__restrict__ v64, float *__restrict__ v32,
+                            double *__restrict__ d64, float *__restrict__ d32) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_slices * 32;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t sl = r >> 5, lane = r & 31;
+        const int64_t base = off[sl];
+        const int w = (off[sl + 1] - off[sl]) >> 5;
+        int k = 0;
+        if (r < n_nodes) {
+            for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
+                const int c = blk_col[s];
+                if (c == (int)r) {
+#pragma unroll
+                    for (int q = 0; q < D * D; ++q) {
+                        d64[r * D * D + q] = aval[(int64_t)s * D * D + q];
+                        d32[r * D * D + q] = (float)srow[r * D * D + q];
+                    }
+                    continue;
+                }
+                const int64_t e = base + 32 * (int64_t)k + lane;
+                col[e] = c;
+#pragma unroll
+                for (int q = 0; q < D * D; ++q) {
+                    v64[e * D * D + q] = aval[(int64_t)s * D * D + q];
+                    v32[e * D * D + q] = (float)aval[(int64_t)s * D * D + q];
+                }
+                ++k;
+            }
+        }
+        // padding: the row itself (or node 0 past the end) with a zero block
+        for (; k < w; ++k) {
+            const int64_t e = base + 32 * (int64_t)k + lane;
+            col[e] = r < n_nodes ? (int32_t)r : 0;
+#pragma unroll
+            for (int q = 0; q < D * D; ++q) {
+                v64[e * D * D + q] = 0.0;
+                v32[e * D * D + q] = 0.0f;
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------- exports
 // Augmented CSR of create_matrix: DOF row (r, a) holds the d*deg(r) block columns in
 // order, then its multiplier column n_dof + k if the DOF is constrained; multiplier row
@@ -693,6 +755,13 @@ int check_error_word(fe_handle_s *h, const char *where) {
     int e = *h->err_host;
     if (!e) return FE_OK;
     FE_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
+    if (e == ERR_SINGULAR_BLOCK) {
+        // a singular diagonal block (a node no element touches) makes the system
+        // singular, as in the reference, where spsolve then returns NaN: the solve
+        // reports FE_BREAKDOWN instead of the assembly failing
+        h->singular = true;
+        return FE_OK;
+    }
     std::string msg = std::string(where) + ":";
     if (e & ERR_CONN_RANGE) msg += " connectivity index out of range;";
     if (e & ERR_DOF_RANGE) msg += " load/condition DOF or dimension out of range;";
@@ -898,7 +967,46 @@ int apply_dirichlet(fe_handle_s *h) {
     }
     FE_LAUNCH_CHECK();
     h->launches += (h->n_bc > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0) + 3;
+    FE_CHECK(build_sell(h));
     h->sys_ready = true;
+    return FE_OK;
+}
+
+int build_sell(fe_handle_s *h) {
+    cudaStream_t s = h->stream;
+    const int D = h->dim;
+    const int64_t n_slices = (h->n_nodes + 31) / 32;
+    h->n_slices = n_slices;
+    FE_CHECK(dalloc(h->counts, (size_t)std::max<int64_t>(n_slices, h->n_nodes) + 1));
+    FE_CHECK(dalloc(h->sell_off, (size_t)n_slices + 1));
+    if (n_slices > 0) {
+        k_sell_widths<<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->counts.p);
+        FE_LAUNCH_CHECK();
+    }
+    int64_t total = 0;
+    FE_CHECK(exclusive_scan_i32(h->counts.p, h->sell_off.p, n_slices, &total, h->scan_tmp, s));
+    size_t ne = (size_t)std::max<int64_t>(total, 1);
+    FE_CHECK(dalloc(h->sell_col, ne));
+    FE_CHECK(dalloc(h->sell_val64, ne * D * D));
+    FE_CHECK(dalloc(h->sell_val32, ne * D * D));
+    FE_CHECK(dalloc(h->diag64, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
+    FE_CHECK(dalloc(h->diag32, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
+    // a node without elements has no diagonal block to copy: leave zeros there
+    FE_CUDA(cudaMemsetAsync(h->diag64.p, 0, h->n_nodes * D * D * sizeof(double), s));
+    FE_CUDA(cudaMemsetAsync(h->diag32.p, 0, h->n_nodes * D * D * sizeof(float), s));
+    if (n_slices > 0) {
+        int g = grid_for(n_slices * 32, kThreads, 152 * 64);
+        if (D == 2)
+            k_sell_fill<2><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
+                                                  h->srow.p, h->sell_off.p, h->sell_col.p, h->sell_val64.p,
+                                                  h->sell_val32.p, h->diag64.p, h->diag32.p);
+        else
+            k_sell_fill<1><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
+                                                  h->srow.p, h->sell_off.p, h->sell_col.p, h->sell_val64.p,
+                                                  h->sell_val32.p, h->diag64.p, h->diag32.p);
+        FE_LAUNCH_CHECK();
+    }
+    h->launches += (n_slices > 0 ? 2 : 0) + 3;
     return FE_OK;
 }
 

@@ -163,6 +163,7 @@ struct fe_handle_s {
 
     // values
     bool k_ready = false, m_ready = false, f_ready = false, sys_ready = false;
+    bool singular = false;                // a diagonal block could not be inverted
     fe::DBuf<double> ke;                  // [n_elem][(3d)^2]
     fe::DBuf<double> me_scale;            // [n_elem] rho*A*t/12
     fe::DBuf<double> kval, mval;          // [nnzb][d][d] full K / M
@@ -171,6 +172,14 @@ struct fe_handle_s {
     fe::DBuf<double> dinv;                // [n_nodes][d][d] inverse diagonal blocks
     fe::DBuf<double> srow;                // [n_nodes][d][d] block row sums of A (difference form)
     fe::DBuf<float> dinv32;
+    // sliced ELL (SELL-32) copy of A for the PCG SpMVs: slice s holds 32 consecutive
+    // block rows; entry k of row 32 s + l sits at sell_off[s] + 32 k + l (coalesced
+    // per warp).  Off-diagonal blocks only; padding entries point at the row itself
+    // with a zero block.  The diagonal lives in diag64 (A_rr) / diag32 (S_r).
+    int64_t n_slices = 0;
+    fe::DBuf<int32_t> sell_off, sell_col;
+    fe::DBuf<double> sell_val64, diag64;
+    fe::DBuf<float> sell_val32, diag32;
     fe::DBuf<double> F;                   // loads [n_dof]
     fe::DBuf<double> b;                   // eliminated right-hand side [n_dof]
     fe::DBuf<long long> load_seq;         // [n_dof] winning load sequence
@@ -198,6 +207,7 @@ int export_csr(fe_handle_s *h, int which, int64_t *indptr, int32_t *indices, dou
 int export_element_matrices(fe_handle_s *h, int which, double *out_host);
 int check_error_word(fe_handle_s *h, const char *where);
 int validate_mesh(fe_handle_s *h);
+int build_sell(fe_handle_s *h);
 
 // scan (fe_scan.cu): exclusive scan of n int32 counts into int32 offsets (n+1 values)
 int exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, int64_t *total,

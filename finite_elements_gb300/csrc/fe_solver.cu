@@ -216,17 +216,83 @@ __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, cons
     const int64_t rows_padded = ((n_nodes + groups - 1) / groups) * groups;                 \
     for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (G); row < rows_padded; row += groups)
 
+// Row r of A x from the SELL-32 copy: one lane per block row, one warp per slice of
+// 32 rows, entry k of the slice at base + 32 k + lane, so each warp load of columns
+// and blocks is one contiguous segment.  The diagonal block comes from diag (A_rr, or
+// S_r in the FP32 difference form); padding entries point at the row itself.
+template <int D, typename T>
+__device__ __forceinline__ NodeVec<D, T> block_apply(const T *__restrict__ blk, const NodeVec<D, T> &x) {
+    NodeVec<D, T> y;
+    if constexpr (D == 2) {
+        if constexpr (sizeof(T) == 8) {
+            const double2 b0 = __ldg(reinterpret_cast<const double2 *>(blk));
+            const double2 b1 = __ldg(reinterpret_cast<const double2 *>(blk) + 1);
+            y.v[0] = b0.x * x.v[0] + b0.y * x.v[1];
+            y.v[1] = b1.x * x.v[0] + b1.y * x.v[1];
+        } else {
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(blk));
+            y.v[0] = b.x * x.v[0] + b.y * x.v[1];
+            y.v[1] = b.z * x.v[0] + b.w * x.v[1];
+        }
+    } else {
+        y.v[0] = __ldg(blk) * x.v[0];
+    }
+    return y;
+}
+
+struct Sell {
+    const int32_t *off, *col;
+    int64_t n_slices;
+};
+
+template <int D, typename T>
+__device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const Sell &A, const T *__restrict__ val,
+                                                  const T *__restrict__ diag, const T *__restrict__ x) {
+    constexpr bool DIFF = sizeof(T) == 4;
+    NodeVec<D, T> xr, acc;
+#pragma unroll
+    for (int a = 0; a < D; ++a) xr.v[a] = T(0), acc.v[a] = T(0);
+    if (valid) {
+        xr = ld<D, T>(x, r);
+        acc = block_apply<D, T>(diag + r * D * D, xr);
+    }
+    const int64_t sl = r >> 5;
+    const int lane = (int)(r & 31);
+    const int64_t base = A.off[sl];
+    const int w = (A.off[sl + 1] - (int)base) >> 5;
+    for (int k = 0; k < w; ++k) {
+        const int64_t e = base + 32 * (int64_t)k + lane;
+        const int c = __ldg(A.col + e);
+        NodeVec<D, T> xv = ld<D, T>(x, c);
+        if (DIFF) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) xv.v[a] -= xr.v[a];
+        }
+        NodeVec<D, T> t = block_apply<D, T>(val + e * D * D, xv);
+#pragma unroll
+        for (int a = 0; a < D; ++a) acc.v[a] += t.v[a];
+    }
+    return acc;
+}
+
+// Rows of the SELL copy handled by this thread (grid-stride in whole warps, so a
+// warp always covers one slice).
+#define FE_SELL_LOOP                                                                     \
+    const int64_t rows_padded = A.n_slices * 32;                                         \
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < rows_padded; \
+         row += (int64_t)gridDim.x * blockDim.x)
+
 // ---------------------------------------------------------------- kernels
 
 // y = A x (timing)
-template <int D, typename T, int G>
+template <int D, typename T>
 __global__ void __launch_bounds__(kVecThreads)
-k_spmv(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
-       const T *__restrict__ val, const T *__restrict__ x, T *__restrict__ y) {
-    FE_ROW_LOOP(G) {
+k_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ x,
+       T *__restrict__ y) {
+    FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> v = row_product<D, T, G>(row, valid, ptr, col, val, x, sub);
-        if (valid && sub == 0) st<D, T>(y, row, v);
+        NodeVec<D, T> v = sell_row<D, T>(row, valid, A, val, diag, x);
+        if (valid) st<D, T>(y, row, v);
     }
 }
 
@@ -265,17 +331,16 @@ k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__re
 }
 
 // q = A p and p.q; the last block sets alpha = r.z / p.q or stops the loop.
-template <int D, typename T, int G>
+template <int D, typename T>
 __global__ void __launch_bounds__(kVecThreads)
-k_pcg_spmv(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
-           const T *__restrict__ val, const T *__restrict__ p, T *__restrict__ q, double *partials,
-           PcgScalars *sc) {
+k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ p,
+           T *__restrict__ q, double *partials, PcgScalars *sc) {
     if (sc->done) return;
     T lt = T(0);
-    FE_ROW_LOOP(G) {
+    FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> y = row_product<D, T, G>(row, valid, ptr, col, val, p, sub);
-        if (valid && sub == 0) {
+        NodeVec<D, T> y = sell_row<D, T>(row, valid, A, val, diag, p);
+        if (valid) {
             st<D, T>(q, row, y);
             NodeVec<D, T> pv = ld<D, T>(p, row);
 #pragma unroll
@@ -389,18 +454,17 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
 // MODE 0: at the start of a loop (no reduction, runs even when done is set);
 // MODE 1: last step of an iteration (reduces r.z_out, finishes the iteration);
 // MODE 2: intermediate step.
-template <int D, typename T, int G, int MODE>
+template <int D, typename T, int MODE>
 __global__ void __launch_bounds__(kVecThreads)
-k_cheb_step(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
-            const T *__restrict__ val, const T *__restrict__ dinv, const T *__restrict__ rres,
-            const T *__restrict__ z_in, T *__restrict__ z_out, T *__restrict__ dch, double c1, double c2,
-            double *partials, PcgScalars *sc) {
+k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
+            const T *__restrict__ dinv, const T *__restrict__ rres, const T *__restrict__ z_in,
+            T *__restrict__ z_out, T *__restrict__ dch, double c1, double c2, double *partials, PcgScalars *sc) {
     if (MODE != 0 && sc->done) return;
     T lrz = T(0);
-    FE_ROW_LOOP(G) {
+    FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> az = row_product<D, T, G>(row, valid, ptr, col, val, z_in, sub);
-        if (valid && sub == 0) {
+        NodeVec<D, T> az = sell_row<D, T>(row, valid, A, val, diag, z_in);
+        if (valid) {
             NodeVec<D, T> rv = ld<D, T>(rres, row), zv = ld<D, T>(z_in, row), dv = ld<D, T>(dch, row);
             NodeVec<D, T> res;
 #pragma unroll
@@ -550,6 +614,8 @@ __global__ void k_multipliers(int64_t n_bc, const int64_t *__restrict__ bc_dof, 
 
 template <typename T>
 struct Sys {
+    Sell A;                                   // SELL-32 structure
+    const T *sval = nullptr, *diag = nullptr;  // SELL values and diagonal blocks
     const T *val = nullptr, *dinv = nullptr;
     double *x = nullptr;   // the solution, FP64 in both precisions
     T *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *zc = nullptr, *dch = nullptr;
@@ -586,50 +652,51 @@ Sys<T> make_sys(fe_handle_s *h) {
     Sys<T> s;
     SolverWork &w = h->w;
     s.x = w.x.p;
+    s.A = Sell{h->sell_off.p, h->sell_col.p, h->n_slices};
     if constexpr (sizeof(T) == 8) {
+        s.sval = h->sell_val64.p, s.diag = h->diag64.p;
         s.val = h->aval.p, s.dinv = h->dinv.p;
         s.r = w.r.p, s.p = w.p.p, s.q = w.q.p, s.z = w.z.p, s.zc = w.t.p, s.dch = w.dch.p;
     } else {
+        s.sval = h->sell_val32.p, s.diag = h->diag32.p;
         s.val = h->aval32.p, s.dinv = h->dinv32.p;
         s.r = w.r32.p, s.p = w.p32.p, s.q = w.q32.p, s.z = w.z32.p, s.zc = w.zc32.p, s.dch = w.c32.p;
     }
     return s;
 }
 
-template <int D, typename T, int G>
+template <int D, typename T>
 void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part, int grid,
                         bool start, T **z_final) {
     T *zin = s.z, *zout = s.zc;
     for (int k = 1; k < cb.k; ++k) {
         const bool last = (k == cb.k - 1);
         if (start)
-            k_cheb_step<D, T, G, 0><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p,
-                                                                         s.val, s.dinv, s.r, zin, zout, s.dch,
-                                                                         cb.c1[k], cb.c2[k], part, sc);
+            k_cheb_step<D, T, 0><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.r,
+                                                                      zin, zout, s.dch, cb.c1[k], cb.c2[k], part, sc);
         else if (last)
-            k_cheb_step<D, T, G, 1><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p,
-                                                                         s.val, s.dinv, s.r, zin, zout, s.dch,
-                                                                         cb.c1[k], cb.c2[k], part, sc);
+            k_cheb_step<D, T, 1><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.r,
+                                                                      zin, zout, s.dch, cb.c1[k], cb.c2[k], part, sc);
         else
-            k_cheb_step<D, T, G, 2><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p,
-                                                                         s.val, s.dinv, s.r, zin, zout, s.dch,
-                                                                         cb.c1[k], cb.c2[k], part, sc);
+            k_cheb_step<D, T, 2><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.r,
+                                                                      zin, zout, s.dch, cb.c1[k], cb.c2[k], part, sc);
         std::swap(zin, zout);
     }
     *z_final = zin;
 }
 
-template <int D, typename T, int G>
+inline int sell_grid(const fe_handle_s *h) { return grid_for(h->n_slices * 32, kVecThreads, 152 * 8); }
+
+template <int D, typename T>
 void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part) {
     const int gv = vec_grid(h->n_nodes);
-    const int gs = vec_grid(h->n_nodes * G);
-    k_pcg_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, s.p, s.q,
-                                                           part, sc);
+    const int gs = sell_grid(h);
+    k_pcg_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.p, s.q, part, sc);
     T *zf = s.z;
     if (cb.k > 1) {
         k_pcg_update<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z, s.dch,
                                                                     part, sc);
-        enqueue_cheb_steps<D, T, G>(h, s, cb, sc, part, gs, false, &zf);
+        enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, false, &zf);
     } else {
         k_pcg_update<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z,
                                                                      s.dch, part, sc);
@@ -642,11 +709,11 @@ void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScala
 template <int D, typename T, int G, bool CONT>
 int enqueue_start(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part) {
     const int gv = vec_grid(h->n_nodes);
-    const int gs = vec_grid(h->n_nodes * G);
+    const int gs = sell_grid(h);
     T *zf = s.z;
     if (cb.k > 1) {
         k_start_precond<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, s.dch, cb.theta);
-        enqueue_cheb_steps<D, T, G>(h, s, cb, sc, part, gs, true, &zf);
+        enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, true, &zf);
     } else {
         k_start_precond<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, s.dch, 1.0);
     }
@@ -709,7 +776,7 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk) {
         }
         cudaGraph_t g;
         FE_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < chunk; ++i) enqueue_iteration<D, T, G>(h, s, cb, sc, w.partials.p);
+        for (int i = 0; i < chunk; ++i) enqueue_iteration<D, T>(h, s, cb, sc, w.partials.p);
         cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
         if (ce != cudaSuccess) {
             set_error(std::string("graph capture: ") + cudaGetErrorString(ce));
@@ -829,12 +896,12 @@ int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
     Sys<T> s = make_sys<D, T>(h);
     T *x = s.p, *y = s.q;
     FE_CUDA(cudaMemsetAsync(x, 0, h->n_dof * sizeof(T), h->stream));
-    const int gs = vec_grid(h->n_nodes * G);
+    const int gs = sell_grid(h);
     for (int i = 0; i < 2; ++i)
-        k_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, x, y);
+        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, x, y);
     FE_CUDA(cudaEventRecord(h->events[8], h->stream));
     for (int i = 0; i < reps; ++i)
-        k_spmv<D, T, G><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, s.val, x, y);
+        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, x, y);
     FE_CUDA(cudaEventRecord(h->events[9], h->stream));
     FE_LAUNCH_CHECK();
     FE_CUDA(cudaEventSynchronize(h->events[9]));
@@ -854,23 +921,11 @@ int time_spmv_any(fe_handle_s *h, int precision, int lanes, int reps, double *ms
     });
 }
 
+// Lanes per block row of the BSR true-residual kernel (the PCG SpMVs use the SELL
+// copy, one lane per row).
 int pick_lanes(fe_handle_s *h, int precision, int requested, int *out) {
-    if (requested == 1 || requested == 2 || requested == 4 || requested == 8) {
-        *out = requested;
-        return FE_OK;
-    }
-    int slot = precision == FE_PREC_MIXED ? 1 : 0;
-    if (!h->w.lanes[slot]) {
-        double best = 1e300;
-        int bl = 1;
-        for (int g : {1, 2, 4, 8}) {
-            double ms = 0;
-            FE_CHECK(time_spmv_any(h, precision, g, 5, &ms));
-            if (ms < best) best = ms, bl = g;
-        }
-        h->w.lanes[slot] = bl;
-    }
-    *out = h->w.lanes[slot];
+    (void)h, (void)precision;
+    *out = (requested == 1 || requested == 2 || requested == 4 || requested == 8) ? requested : 2;
     return FE_OK;
 }
 
@@ -1079,7 +1134,19 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         return FE_BAD_INPUT;
     }
     FE_CHECK(ensure_work(h, mixed));
-    int lanes = 1;
+    if (h->singular) {
+        // a node without stiffness: the system is singular; like scipy's spsolve the
+        // result is NaN
+        FE_CUDA(cudaMemsetAsync(h->w.x.p, 0xff, h->n_dof * sizeof(double), h->stream));
+        FE_CHECK(dalloc(h->lambda, (size_t)std::max<int64_t>(h->n_bc, 1)));
+        FE_CUDA(cudaMemsetAsync(h->lambda.p, 0xff, std::max<int64_t>(h->n_bc, 1) * sizeof(double), h->stream));
+        FE_CUDA(cudaStreamSynchronize(h->stream));
+        st->status = FE_BREAKDOWN;
+        st->relres = NAN;
+        h->have_solution = true;
+        return FE_OK;
+    }
+    int lanes = 2;
     FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
     FE_CUDA(cudaEventRecord(h->events[6], h->stream));
     int rc = dispatch_lanes(lanes, [&](auto g) {
@@ -1119,10 +1186,8 @@ int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms) {
         set_error("assemble first");
         return FE_NOT_READY;
     }
-    int slot = precision == FE_PREC_MIXED ? 1 : 0;
-    h->w.lanes[slot] = 0;
-    FE_CHECK(pick_lanes(h, precision, 0, lanes));
-    return time_spmv_any(h, precision, *lanes, 10, ms);
+    *lanes = 1;   // SELL-32: one lane per block row, one warp per slice
+    return time_spmv_any(h, precision, 1, 10, ms);
 }
 
 int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {

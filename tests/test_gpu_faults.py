@@ -90,3 +90,23 @@ def test_empty_element_load_set_is_rejected(gpu_lib):
     prob.element_loads = [ElementLoadSet(np.zeros(0, np.int64), 1.0, 1)]
     with pytest.raises(_lib.FeError):
         GpuSystem(prob)
+
+
+def test_node_without_elements_gives_nan_like_spsolve(gpu_lib):
+    """A node no element touches leaves a zero row in K: scipy's spsolve warns that the
+    matrix is singular and returns NaN; the drop-in does the same."""
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    from finite_elements_gb300.problem import Problem
+    prob, _, _ = gc.load("ex2_strain")
+    coords = np.vstack([prob.coords, [[50.0, 50.0]]])
+    p2 = Problem("elastic", coords, prob.conn, E=prob.E, nu=prob.nu, thickness=prob.thickness,
+                 rho=prob.rho, plane_strain=True, plane_stress=False,
+                 node_load_node=prob.node_load_node, node_load_dim=prob.node_load_dim,
+                 node_load_value=prob.node_load_value, node_bc_node=prob.node_bc_node,
+                 node_bc_dim=prob.node_bc_dim, node_bc_value=prob.node_bc_value)
+    fea = FiniteElementAnalysis.from_problem(p2)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        res = fea.solve()
+    assert np.isnan(np.array(res.result_vector)).all()
+    assert any(issubclass(x.category, spla.MatrixRankWarning) for x in w)
