@@ -82,6 +82,16 @@ _SIGNATURES = {
     "fe_launch_count": ([_P, _PI64], C.c_int),
     "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
     "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
+    "fe_gnn_create": ([C.POINTER(_P)], C.c_int),
+    "fe_gnn_destroy": ([_P], C.c_int),
+    "fe_gnn_num_params": ([_PI64], C.c_int),
+    "fe_gnn_set_params": ([_P, _P, _I64], C.c_int),
+    "fe_gnn_get_params": ([_P, _P, _I64], C.c_int),
+    "fe_gnn_features": ([_P, _P, _P], C.c_int),
+    "fe_gnn_predict": ([_P, _P, _P, C.POINTER(_P), _PD], C.c_int),
+    "fe_gnn_target_energy": ([_P, _P, _PD], C.c_int),
+    "fe_gnn_loss_grad": ([_P, _P, _D, _PD, _P], C.c_int),
+    "fe_gnn_adam_step": ([_P, C.c_float, C.c_float, C.c_float, C.c_float], C.c_int),
     "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
 }
 

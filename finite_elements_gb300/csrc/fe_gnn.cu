@@ -1,0 +1,899 @@
+// Learned warm start for PCG: a graph network over the mesh (nodes = mesh nodes,
+// edges = the node pairs that share an element, i.e. the block pattern of K)
+// predicts the shape u_hat of the displacement field; the warm start is
+// x0 = g + s u_hat with g the prescribed values and s = (u_hat . b~) / (u_hat . A u_hat),
+// the scale that minimises the A-norm error along u_hat (b~ = b - A g, zero on the
+// constrained DOFs).  PCG from x0 to the same tolerance stays the judge of accuracy.
+//
+// Network (hidden width 64, 6 layers):
+//   h0 = relu(f W0 + b0)                       f: 16 node features
+//   m_l = mean_{j in N(i)} h_l,j               mesh-neighbour mean (no self)
+//   g_l = mean_i h_l,i                         global mean
+//   z_l = [h_l, m_l] W_l + b_l + g_l U_l
+//   h_{l+1} = h_l + relu(z_l)
+//   u_hat = h_6 Wd + bd, zero on constrained DOFs
+// Loss: the share of the solution's energy the warm start leaves to PCG,
+//   L = 1 - (u_hat . b~)^2 / ((u_hat . A u_hat) (b~ . v*)),  v* = u* - g,
+// so training needs only b~ . v* from a solve of the problem.
+//
+// The dense transforms run as BF16 tensor-core MMAs (mma.sync m16n8k16, FP32
+// accumulation) with FP32 master weights and activations; aggregation, reductions,
+// loss and Adam are FP32 / FP64 CUDA-core kernels.  Elasticity meshes only.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "fe_internal.h"
+
+namespace fe {
+namespace {
+
+constexpr int HID = 64;
+constexpr int NF = 16;
+constexpr int NLAYER = 6;
+constexpr int KC = 2 * HID;   // concatenated [h, m]
+
+// parameter offsets in the FP32 blob; every weight matrix is stored [in][out]
+constexpr int P_W0 = 0;
+constexpr int P_B0 = P_W0 + NF * HID;
+constexpr int P_L0 = P_B0 + HID;
+constexpr int L_W = 0;
+constexpr int L_B = KC * HID;
+constexpr int L_U = L_B + HID;
+constexpr int L_STRIDE = L_U + HID * HID;
+constexpr int P_WD = P_L0 + NLAYER * L_STRIDE;
+constexpr int P_BD = P_WD + HID * 2;
+constexpr int P_TOTAL = P_BD + 2;
+
+constexpr int kT = 256;
+
+inline int g1(int64_t n, int t = kT) { return grid_for(n, t, 152 * 8); }
+
+// ---------------------------------------------------------------- tensor-core GEMM
+// Y[N x NO] = X[N x KI] W[KI x NO], X given as two row-major FP32 halves (columns
+// [0, K1) from X1 and [K1, KI) from X2), W given transposed in BF16 (Wt[n][k]).
+// 4 warps per block, 64 rows per tile, each warp 16 rows x NO columns.
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+enum Epi { EPI_RELU_BIAS = 0, EPI_LAYER = 1, EPI_PLAIN = 2 };
+
+template <int KI, int K1, int NO, int EPI>
+__global__ void __launch_bounds__(128)
+k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, const __nv_bfloat16 *__restrict__ Wt,
+       const float *__restrict__ bias, const float *__restrict__ gterm, const float *__restrict__ hres,
+       float *__restrict__ Z, float *__restrict__ Y) {
+    constexpr int XS = KI + 8, WS = KI + 8;
+    __shared__ __align__(16) __nv_bfloat16 Ws[NO * WS];
+    __shared__ __align__(16) __nv_bfloat16 Xs[64 * XS];
+    for (int i = threadIdx.x; i < NO * KI; i += blockDim.x) {
+        int n = i / KI, k = i - n * KI;
+        Ws[n * WS + k] = Wt[i];
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int64_t tile = blockIdx.x; tile * 64 < N; tile += gridDim.x) {
+        const int64_t row0 = tile * 64;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 64 * KI; i += blockDim.x) {
+            int r = i / KI, k = i - r * KI;
+            int64_t gr = row0 + r;
+            float v = 0.f;
+            if (gr < N) v = k < K1 ? X1[gr * K1 + k] : X2[gr * (KI - K1) + (k - K1)];
+            Xs[r * XS + k] = __float2bfloat16_rn(v);
+        }
+        __syncthreads();
+        float acc[NO / 8][4];
+#pragma unroll
+        for (int j = 0; j < NO / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < KI; kk += 16) {
+            const __nv_bfloat16 *xa = Xs + (warp * 16 + g) * XS + kk + 2 * t;
+            uint32_t a0 = *reinterpret_cast<const uint32_t *>(xa);
+            uint32_t a1 = *reinterpret_cast<const uint32_t *>(xa + 8 * XS);
+            uint32_t a2 = *reinterpret_cast<const uint32_t *>(xa + 8);
+            uint32_t a3 = *reinterpret_cast<const uint32_t *>(xa + 8 * XS + 8);
+#pragma unroll
+            for (int nt = 0; nt < NO / 8; ++nt) {
+                const __nv_bfloat16 *wb = Ws + (nt * 8 + g) * WS + kk + 2 * t;
+                uint32_t b0 = *reinterpret_cast<const uint32_t *>(wb);
+                uint32_t b1 = *reinterpret_cast<const uint32_t *>(wb + 8);
+                mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+            }
+        }
+#pragma unroll
+        for (int nt = 0; nt < NO / 8; ++nt) {
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int64_t r = row0 + warp * 16 + g + 8 * half;
+                if (r >= N) continue;
+                const int c = nt * 8 + 2 * t;
+                float v0 = acc[nt][2 * half], v1 = acc[nt][2 * half + 1];
+                if (EPI == EPI_PLAIN) {
+                    Y[r * NO + c] = v0;
+                    Y[r * NO + c + 1] = v1;
+                } else if (EPI == EPI_RELU_BIAS) {
+                    v0 += bias[c];
+                    v1 += bias[c + 1];
+                    Z[r * NO + c] = v0;
+                    Z[r * NO + c + 1] = v1;
+                    Y[r * NO + c] = fmaxf(v0, 0.f);
+                    Y[r * NO + c + 1] = fmaxf(v1, 0.f);
+                } else {
+                    v0 += bias[c] + gterm[c];
+                    v1 += bias[c + 1] + gterm[c + 1];
+                    Z[r * NO + c] = v0;
+                    Z[r * NO + c + 1] = v1;
+                    Y[r * NO + c] = hres[r * NO + c] + fmaxf(v0, 0.f);
+                    Y[r * NO + c + 1] = hres[r * NO + c + 1] + fmaxf(v1, 0.f);
+                }
+            }
+        }
+    }
+}
+
+// dW[KI x NO] += X^T dZ over all rows: X given as two FP32 halves as above, dZ
+// [N x NO].  Per block: a BF16 tile of 64 rows of X and of dZ (transposed) in shared
+// memory; the reduction over rows runs on the tensor cores, 16 rows per MMA; each
+// block adds its partial dW with FP32 atomics at the end.
+template <int KI, int K1, int NO>
+__global__ void __launch_bounds__(128)
+k_gemm_wgrad(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2,
+             const float *__restrict__ dZ, float *__restrict__ dW) {
+    constexpr int XS = KI + 8, ZS = 64 + 8;
+    constexpr int MT = KI / 16, NT = NO / 8, TILES = MT * NT, PER_WARP = (TILES + 3) / 4;
+    __shared__ __align__(16) __nv_bfloat16 Xs[64 * XS];
+    __shared__ __align__(16) __nv_bfloat16 Zt[NO * ZS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float acc[PER_WARP][4];
+#pragma unroll
+    for (int j = 0; j < PER_WARP; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    for (int64_t tile = blockIdx.x; tile * 64 < N; tile += gridDim.x) {
+        const int64_t row0 = tile * 64;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 64 * KI; i += blockDim.x) {
+            int r = i / KI, k = i - r * KI;
+            int64_t gr = row0 + r;
+            float v = 0.f;
+            if (gr < N) v = k < K1 ? X1[gr * K1 + k] : X2[gr * (KI - K1) + (k - K1)];
+            Xs[r * XS + k] = __float2bfloat16_rn(v);
+        }
+        for (int i = threadIdx.x; i < 64 * NO; i += blockDim.x) {
+            int r = i / NO, n = i - r * NO;
+            int64_t gr = row0 + r;
+            Zt[n * ZS + r] = __float2bfloat16_rn(gr < N ? dZ[gr * NO + n] : 0.f);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PER_WARP; ++j) {
+            const int tid = warp + 4 * j;
+            if (tid >= TILES) break;
+            const int mt = tid / NT, nt = tid - mt * NT;
+#pragma unroll
+            for (int kk = 0; kk < 64; kk += 16) {
+                // A[m][q] = X[row kk+q][feature 16 mt + m]
+                const int m0 = mt * 16 + g;
+                const int q0 = kk + 2 * t;
+                uint32_t a0 = pack2(Xs[q0 * XS + m0], Xs[(q0 + 1) * XS + m0]);
+                uint32_t a1 = pack2(Xs[q0 * XS + m0 + 8], Xs[(q0 + 1) * XS + m0 + 8]);
+                uint32_t a2 = pack2(Xs[(q0 + 8) * XS + m0], Xs[(q0 + 9) * XS + m0]);
+                uint32_t a3 = pack2(Xs[(q0 + 8) * XS + m0 + 8], Xs[(q0 + 9) * XS + m0 + 8]);
+                // B[q][n] = dZ[row kk+q][output 8 nt + n]
+                const __nv_bfloat16 *zb = Zt + (nt * 8 + g) * ZS + q0;
+                uint32_t b0 = *reinterpret_cast<const uint32_t *>(zb);
+                uint32_t b1 = *reinterpret_cast<const uint32_t *>(zb + 8);
+                mma_bf16(acc[j], a0, a1, a2, a3, b0, b1);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PER_WARP; ++j) {
+        const int tid = warp + 4 * j;
+        if (tid >= TILES) break;
+        const int mt = tid / NT, nt = tid - mt * NT;
+        const int m = mt * 16 + g, n = nt * 8 + 2 * t;
+        atomicAdd(&dW[m * NO + n], acc[j][0]);
+        atomicAdd(&dW[m * NO + n + 1], acc[j][1]);
+        atomicAdd(&dW[(m + 8) * NO + n], acc[j][2]);
+        atomicAdd(&dW[(m + 8) * NO + n + 1], acc[j][3]);
+    }
+}
+
+// ---------------------------------------------------------------- graph kernels
+
+// m_r = inv_deg[r] * sum_{c in N(r), c != r} h_c   (TRANSPOSE: out_c += sum inv_deg[r] h_r)
+// one warp per node, two features per lane.
+template <bool TRANSPOSE>
+__global__ void k_aggregate(int64_t n, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                            const float *__restrict__ inv_deg, const float *__restrict__ hin, float *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int s = ptr[r]; s < ptr[r + 1]; ++s) {
+            const int c = col[s];
+            if (c == (int)r) continue;
+            const float w = TRANSPOSE ? inv_deg[c] : 1.f;
+            const float2 v = reinterpret_cast<const float2 *>(hin + (int64_t)c * HID)[lane];
+            acc.x += w * v.x;
+            acc.y += w * v.y;
+        }
+        float2 *o = reinterpret_cast<float2 *>(out + r * HID) + lane;
+        if (TRANSPOSE) {
+            float2 cur = *o;
+            *o = make_float2(cur.x + acc.x, cur.y + acc.y);
+        } else {
+            const float w = inv_deg[r];
+            *o = make_float2(acc.x * w, acc.y * w);
+        }
+    }
+}
+
+__global__ void k_inv_deg(int64_t n, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                          float *__restrict__ inv_deg) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        int d = 0;
+        for (int s = ptr[r]; s < ptr[r + 1]; ++s) d += col[s] != (int)r;
+        inv_deg[r] = d > 0 ? 1.f / (float)d : 0.f;
+    }
+}
+
+// out[64] += column sums of X [n x 64] (out zeroed by the caller)
+__global__ void k_colsum(int64_t n, const float *__restrict__ X, float *__restrict__ out) {
+    __shared__ float sh[kT / 64][64];
+    const int c = threadIdx.x & 63, rg = threadIdx.x >> 6;   // 4 row groups of 64 columns
+    float acc = 0.f;
+    for (int64_t r = (int64_t)blockIdx.x * (kT / 64) + rg; r < n; r += (int64_t)gridDim.x * (kT / 64))
+        acc += X[r * HID + c];
+    sh[rg][c] = acc;
+    __syncthreads();
+    if (rg == 0) {
+        float s = sh[0][c] + sh[1][c] + sh[2][c] + sh[3][c];
+        atomicAdd(&out[c], s);
+    }
+}
+
+// gterm[n] = sum_k (colsum[k] / N) U[k][n]     (one block of 64 threads)
+__global__ void k_gterm(const float *__restrict__ colsum, float inv_n, const float *__restrict__ U,
+                        float *__restrict__ gterm) {
+    const int c = threadIdx.x;
+    float acc = 0.f;
+    for (int k = 0; k < HID; ++k) acc += colsum[k] * inv_n * U[k * HID + c];
+    gterm[c] = acc;
+}
+
+// dZ = dH (.) [z > 0]
+__global__ void k_relu_grad(int64_t n, const float *__restrict__ dH, const float *__restrict__ Z,
+                            float *__restrict__ dZ) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dZ[i] = Z[i] > 0.f ? dH[i] : 0.f;
+}
+
+// dH[:, :] = dH_next + dX[:, :64] + dgb (broadcast)     (dX is [n x 128])
+__global__ void k_layer_back_dh(int64_t n, const float *__restrict__ dHn, const float *__restrict__ dX,
+                                const float *__restrict__ dgb, float *__restrict__ dH) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * HID;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = i / HID;
+        int c = (int)(i - r * HID);
+        dH[i] = dHn[i] + dX[r * KC + c] + dgb[c];
+    }
+}
+
+// dM = dX[:, 64:]
+__global__ void k_split_dm(int64_t n, const float *__restrict__ dX, float *__restrict__ dM) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * HID;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = i / HID;
+        int c = (int)(i - r * HID);
+        dM[i] = dX[r * KC + HID + c];
+    }
+}
+
+// global-term gradients from s = colsum(dZ): dU[k][n] += g[k] s[n], dgb[k] = (1/N) sum_n U[k][n] s[n]
+__global__ void k_gterm_back(const float *__restrict__ colsum_h, float inv_n, const float *__restrict__ U,
+                             const float *__restrict__ s, float *__restrict__ dU, float *__restrict__ dgb) {
+    const int k = threadIdx.x;
+    const float gk = colsum_h[k] * inv_n;
+    float acc = 0.f;
+    for (int c = 0; c < HID; ++c) {
+        dU[k * HID + c] += gk * s[c];
+        acc += U[k * HID + c] * s[c];
+    }
+    dgb[k] = acc * inv_n;
+}
+
+// ---------------------------------------------------------------- features, decoder, loss
+
+struct Bounds {
+    float xmin, xmax, ymin, ymax;
+};
+
+__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
+    // v >= 0: the int order of non-negative floats is their value order
+    atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+}
+__device__ __forceinline__ void atomic_min_f(float *addr, float v) {
+    int old = __float_as_int(*addr);
+    while (__int_as_float(old) > v) {
+        int prev = atomicCAS(reinterpret_cast<int *>(addr), old, __float_as_int(v));
+        if (prev == old) break;
+        old = prev;
+    }
+}
+__device__ __forceinline__ void atomic_max_f(float *addr, float v) {
+    int old = __float_as_int(*addr);
+    while (__int_as_float(old) < v) {
+        int prev = atomicCAS(reinterpret_cast<int *>(addr), old, __float_as_int(v));
+        if (prev == old) break;
+        old = prev;
+    }
+}
+
+// stats[0..3] = bbox, stats[4] = max |b~|, stats[5] = max |D^-1 b~|
+__global__ void k_feature_stats(int64_t n, const double *__restrict__ coords, const double *__restrict__ bt,
+                                const double *__restrict__ dinv, float *__restrict__ stats) {
+    float xmn = 3.4e38f, xmx = -3.4e38f, ymn = 3.4e38f, ymx = -3.4e38f, bm = 0.f, zm = 0.f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        float x = (float)coords[2 * r], y = (float)coords[2 * r + 1];
+        xmn = fminf(xmn, x), xmx = fmaxf(xmx, x), ymn = fminf(ymn, y), ymx = fmaxf(ymx, y);
+        double b0 = bt[2 * r], b1 = bt[2 * r + 1];
+        bm = fmaxf(bm, (float)fmax(fabs(b0), fabs(b1)));
+        double z0 = dinv[4 * r] * b0 + dinv[4 * r + 1] * b1, z1 = dinv[4 * r + 2] * b0 + dinv[4 * r + 3] * b1;
+        zm = fmaxf(zm, (float)fmax(fabs(z0), fabs(z1)));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        xmn = fminf(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
+        xmx = fmaxf(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
+        ymn = fminf(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
+        ymx = fmaxf(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
+        bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+        zm = fmaxf(zm, __shfl_xor_sync(0xffffffffu, zm, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_min_f(&stats[0], xmn);
+        atomic_max_f(&stats[1], xmx);
+        atomic_min_f(&stats[2], ymn);
+        atomic_max_f(&stats[3], ymx);
+        atomic_max_pos(&stats[4], bm);
+        atomic_max_pos(&stats[5], zm);
+    }
+}
+
+// 16 features per node (see fe_gb300.h, fe_gnn_features)
+__global__ void k_features(int64_t n, const double *__restrict__ coords, const int32_t *__restrict__ inc_ptr,
+                           const int32_t *__restrict__ inc, const double *__restrict__ E,
+                           const double *__restrict__ nu, const int32_t *__restrict__ bc_of_dof,
+                           const double *__restrict__ bt, const double *__restrict__ dinv,
+                           const float *__restrict__ stats, float *__restrict__ F) {
+    const float L = fmaxf(fmaxf(stats[1] - stats[0], stats[3] - stats[2]), 1e-30f);
+    const float ib = stats[4] > 0.f ? 1.f / stats[4] : 0.f, iz = stats[5] > 0.f ? 1.f / stats[5] : 0.f;
+    const float PI = 3.14159265358979f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        float xn = ((float)coords[2 * r] - stats[0]) / L, yn = ((float)coords[2 * r + 1] - stats[2]) / L;
+        float le = 0.f, lnu = 0.f;
+        int cnt = inc_ptr[r + 1] - inc_ptr[r];
+        for (int s = inc_ptr[r]; s < inc_ptr[r + 1]; ++s) {
+            int e = inc[s] / 3;
+            le += (float)log10(E[e]);
+            lnu += (float)nu[e];
+        }
+        if (cnt > 0) le /= cnt, lnu /= cnt;
+        double b0 = bt[2 * r], b1 = bt[2 * r + 1];
+        double z0 = dinv[4 * r] * b0 + dinv[4 * r + 1] * b1, z1 = dinv[4 * r + 2] * b0 + dinv[4 * r + 3] * b1;
+        float *f = F + r * NF;
+        f[0] = xn;
+        f[1] = yn;
+        f[2] = sinf(PI * xn);
+        f[3] = cosf(PI * xn);
+        f[4] = sinf(PI * yn);
+        f[5] = cosf(PI * yn);
+        f[6] = sinf(2.f * PI * xn);
+        f[7] = sinf(2.f * PI * yn);
+        f[8] = bc_of_dof[2 * r] >= 0 ? 1.f : 0.f;
+        f[9] = bc_of_dof[2 * r + 1] >= 0 ? 1.f : 0.f;
+        f[10] = (float)b0 * ib;
+        f[11] = (float)b1 * ib;
+        f[12] = cnt > 0 ? le - 10.5f : 0.f;
+        f[13] = cnt > 0 ? (lnu - 0.3f) * 10.f : 0.f;
+        f[14] = (float)z0 * iz;
+        f[15] = (float)z1 * iz;
+    }
+}
+
+// g_ext (prescribed values on constrained DOFs, 0 elsewhere)
+__global__ void k_gext(int64_t n_bc, const int64_t *__restrict__ bc_dof, const double *__restrict__ bc_val,
+                       double *__restrict__ g) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_bc; k += (int64_t)gridDim.x * blockDim.x)
+        g[bc_dof[k]] = bc_val[k];
+}
+
+// b~ = b - A g on free DOFs, 0 on constrained ones (Ag holds A g)
+__global__ void k_btilde(int64_t n_dof, const double *__restrict__ b, const double *__restrict__ Ag,
+                         const int32_t *__restrict__ bc_of_dof, double *__restrict__ bt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        bt[i] = bc_of_dof[i] >= 0 ? 0.0 : b[i] - Ag[i];
+}
+
+// u_hat_i = h_i Wd + bd (two outputs), zero on constrained DOFs; one warp per node
+__global__ void k_decode(int64_t n, const float *__restrict__ Hh, const float *__restrict__ Wd,
+                         const float *__restrict__ bd, const int32_t *__restrict__ bc_of_dof, double *__restrict__ u) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        float2 h = reinterpret_cast<const float2 *>(Hh + r * HID)[lane];
+        int k = 2 * lane;
+        float o0 = h.x * Wd[k * 2] + h.y * Wd[(k + 1) * 2];
+        float o1 = h.x * Wd[k * 2 + 1] + h.y * Wd[(k + 1) * 2 + 1];
+        for (int o = 16; o > 0; o >>= 1) {
+            o0 += __shfl_xor_sync(0xffffffffu, o0, o);
+            o1 += __shfl_xor_sync(0xffffffffu, o1, o);
+        }
+        if (lane == 0) {
+            u[2 * r] = bc_of_dof[2 * r] >= 0 ? 0.0 : (double)(o0 + bd[0]);
+            u[2 * r + 1] = bc_of_dof[2 * r + 1] >= 0 ? 0.0 : (double)(o1 + bd[1]);
+        }
+    }
+}
+
+// acc[0] += u.bt, acc[1] += u.Au  (FP64, block partials then atomics)
+__global__ void k_dots2(int64_t n, const double *__restrict__ u, const double *__restrict__ bt,
+                        const double *__restrict__ Au, double *__restrict__ acc) {
+    __shared__ double sh[2][kT / 32];
+    double s0 = 0, s1 = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        s0 += u[i] * bt[i];
+        s1 += u[i] * Au[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) sh[0][threadIdx.x >> 5] = s0, sh[1][threadIdx.x >> 5] = s1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, c = 0;
+        for (int w = 0; w < kT / 32; ++w) a += sh[0][w], c += sh[1][w];
+        atomicAdd(&acc[0], a);
+        atomicAdd(&acc[1], c);
+    }
+}
+
+// du = ca * bt + cb * Au on free DOFs (0 on constrained), as FP32 per node pair
+__global__ void k_loss_grad_u(int64_t n_dof, const double *__restrict__ bt, const double *__restrict__ Au,
+                              const int32_t *__restrict__ bc_of_dof, double ca, double cb, float *__restrict__ du) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        du[i] = bc_of_dof[i] >= 0 ? 0.f : (float)(ca * bt[i] + cb * Au[i]);
+}
+
+// decoder backward: dH_i = Wd du_i; dWd += h_i du_i^T; dbd += du_i.  One warp per node.
+__global__ void k_decode_back(int64_t n, const float *__restrict__ Hh, const float *__restrict__ Wd,
+                              const float *__restrict__ du, float *__restrict__ dH, float *__restrict__ dWd,
+                              float *__restrict__ dbd) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float w00 = 0, w01 = 0, w10 = 0, w11 = 0, b0 = 0, b1 = 0;
+    const int k = 2 * lane;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const float d0 = du[2 * r], d1 = du[2 * r + 1];
+        float2 h = reinterpret_cast<const float2 *>(Hh + r * HID)[lane];
+        reinterpret_cast<float2 *>(dH + r * HID)[lane] =
+            make_float2(Wd[k * 2] * d0 + Wd[k * 2 + 1] * d1, Wd[(k + 1) * 2] * d0 + Wd[(k + 1) * 2 + 1] * d1);
+        w00 += h.x * d0, w01 += h.x * d1, w10 += h.y * d0, w11 += h.y * d1;
+        if (lane == 0) b0 += d0, b1 += d1;
+    }
+    atomicAdd(&dWd[k * 2], w00);
+    atomicAdd(&dWd[k * 2 + 1], w01);
+    atomicAdd(&dWd[(k + 1) * 2], w10);
+    atomicAdd(&dWd[(k + 1) * 2 + 1], w11);
+    if (lane == 0) {
+        atomicAdd(&dbd[0], b0);
+        atomicAdd(&dbd[1], b1);
+    }
+}
+
+// x0 = g_ext + s u_hat
+__global__ void k_warm_start(int64_t n_dof, const double *__restrict__ g, const double *__restrict__ u, double s,
+                             double *__restrict__ x0) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        x0[i] = g[i] + s * u[i];
+}
+
+// e = b~ . (x - g)   (energy of the solution's free part: b~ = A v* with v* = x - g)
+__global__ void k_energy(int64_t n_dof, const double *__restrict__ bt, const double *__restrict__ x,
+                         const double *__restrict__ g, double *__restrict__ acc) {
+    __shared__ double sh[kT / 32];
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        s += bt[i] * (x[i] - g[i]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0;
+        for (int w = 0; w < kT / 32; ++w) a += sh[w];
+        atomicAdd(acc, a);
+    }
+}
+
+// W [KI][NO] FP32 -> Wt [NO][KI] BF16
+__global__ void k_to_bf16_t(const float *__restrict__ W, int KI, int NO, __nv_bfloat16 *__restrict__ Wt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < KI * NO; i += gridDim.x * blockDim.x) {
+        int n = i / KI, k = i - n * KI;
+        Wt[i] = __float2bfloat16_rn(W[k * NO + n]);
+    }
+}
+
+// W FP32 -> BF16, same layout
+__global__ void k_to_bf16(const float *__restrict__ W, int n, __nv_bfloat16 *__restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = __float2bfloat16_rn(W[i]);
+}
+
+// Adam on the FP32 master weights
+__global__ void k_adam(int n, float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m,
+                       float *__restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float gi = gr[i];
+        float mi = b1 * m[i] + (1.f - b1) * gi;
+        float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+}  // namespace
+}  // namespace fe
+
+// ---------------------------------------------------------------- network state
+
+struct fe_gnn_s {
+    fe::DBuf<float> params, grad, adam_m, adam_v;
+    fe::DBuf<__nv_bfloat16> wt;   // transposed BF16 copies of W0, W_l (in that order)
+    int64_t n_cap = 0;            // nodes the activation buffers hold
+    fe::DBuf<float> F, Z0, H, Z, M, dH, dHn, dX, dZ, dM, inv_deg, colsum, gterm, stats, du, dgb;
+    fe::DBuf<double> gext, Ag, bt, u, Au, x0, acc;
+    double *acc_host = nullptr;
+    int steps = 0;
+    double last_scale = 0.0, last_num = 0.0, last_den = 0.0;
+    cudaStream_t stream = nullptr;
+};
+
+namespace fe {
+namespace {
+
+constexpr int WT_W0 = 0;
+constexpr int WT_L0 = NF * HID;
+
+int gnn_alloc(fe_gnn_s *g, int64_t n) {
+    if (n <= g->n_cap) return FE_OK;
+    size_t N = (size_t)n;
+    FE_CHECK(dalloc(g->F, N * NF));
+    FE_CHECK(dalloc(g->Z0, N * HID));
+    FE_CHECK(dalloc(g->H, N * HID * (NLAYER + 1)));
+    FE_CHECK(dalloc(g->Z, N * HID * NLAYER));
+    FE_CHECK(dalloc(g->M, N * HID * NLAYER));
+    FE_CHECK(dalloc(g->dH, N * HID));
+    FE_CHECK(dalloc(g->dHn, N * HID));
+    FE_CHECK(dalloc(g->dX, N * KC));
+    FE_CHECK(dalloc(g->dZ, N * HID));
+    FE_CHECK(dalloc(g->dM, N * HID));
+    FE_CHECK(dalloc(g->inv_deg, N));
+    FE_CHECK(dalloc(g->du, N * 2));
+    FE_CHECK(dalloc(g->gext, N * 2));
+    FE_CHECK(dalloc(g->Ag, N * 2));
+    FE_CHECK(dalloc(g->bt, N * 2));
+    FE_CHECK(dalloc(g->u, N * 2));
+    FE_CHECK(dalloc(g->Au, N * 2));
+    FE_CHECK(dalloc(g->x0, N * 2));
+    g->n_cap = n;
+    return FE_OK;
+}
+
+int refresh_bf16(fe_gnn_s *g) {
+    k_to_bf16_t<<<4, 256, 0, g->stream>>>(g->params.p + P_W0, NF, HID, g->wt.p + WT_W0);
+    for (int l = 0; l < NLAYER; ++l)
+        k_to_bf16_t<<<16, 256, 0, g->stream>>>(g->params.p + P_L0 + l * L_STRIDE + L_W, KC, HID,
+                                               g->wt.p + WT_L0 + l * KC * HID);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+// Problem-dependent inputs: g_ext, b~, node features, inverse degrees.
+int prepare(fe_gnn_s *g, fe_handle_s *h) {
+    if (h->kind != FE_KIND_ELASTIC_TRI) {
+        set_error("the warm-start network is defined for elasticity meshes");
+        return FE_BAD_INPUT;
+    }
+    if (!h->sys_ready) {
+        set_error("the warm-start network needs an assembled system");
+        return FE_NOT_READY;
+    }
+    const int64_t n = h->n_nodes, nd = h->n_dof;
+    cudaStream_t s = h->stream;
+    g->stream = s;
+    FE_CHECK(gnn_alloc(g, n));
+    FE_CUDA(cudaMemsetAsync(g->gext.p, 0, nd * sizeof(double), s));
+    if (h->n_bc > 0) k_gext<<<g1(h->n_bc), kT, 0, s>>>(h->n_bc, h->bc_dof.p, h->bc_val.p, g->gext.p);
+    FE_CHECK(spmv64(h, g->gext.p, g->Ag.p));
+    k_btilde<<<g1(nd), kT, 0, s>>>(nd, h->b.p, g->Ag.p, h->bc_of_dof.p, g->bt.p);
+    FE_CHECK(dalloc(g->stats, 8));
+    float init[8] = {3.4e38f, -3.4e38f, 3.4e38f, -3.4e38f, 0.f, 0.f, 0.f, 0.f};
+    FE_CUDA(cudaMemcpyAsync(g->stats.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    k_feature_stats<<<g1(n), kT, 0, s>>>(n, h->coords.p, g->bt.p, h->dinv.p, g->stats.p);
+    k_features<<<g1(n), kT, 0, s>>>(n, h->coords.p, h->inc_ptr.p, h->inc.p, h->E.p, h->nu.p, h->bc_of_dof.p, g->bt.p,
+                                    h->dinv.p, g->stats.p, g->F.p);
+    k_inv_deg<<<g1(n), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 6 + (h->n_bc > 0 ? 1 : 0);
+    // the host copy in init must stay valid until the copy ran
+    FE_CUDA(cudaStreamSynchronize(s));
+    return FE_OK;
+}
+
+inline float *Hl(fe_gnn_s *g, int l) { return g->H.p + (size_t)l * g->n_cap * HID; }
+inline float *Zl(fe_gnn_s *g, int l) { return g->Z.p + (size_t)l * g->n_cap * HID; }
+inline float *Ml(fe_gnn_s *g, int l) { return g->M.p + (size_t)l * g->n_cap * HID; }
+
+int forward(fe_gnn_s *g, fe_handle_s *h) {
+    const int64_t n = h->n_nodes;
+    cudaStream_t s = g->stream;
+    const float *P = g->params.p;
+    const int gg = (int)std::min<int64_t>((n + 63) / 64, 152 * 4);
+    k_gemm<NF, NF, HID, EPI_RELU_BIAS><<<gg, 128, 0, s>>>(n, g->F.p, nullptr, g->wt.p + WT_W0, P + P_B0, nullptr,
+                                                          nullptr, g->Z0.p, Hl(g, 0));
+    FE_CHECK(dalloc(g->colsum, (size_t)(NLAYER + 1) * HID));
+    FE_CHECK(dalloc(g->gterm, (size_t)NLAYER * HID));
+    FE_CUDA(cudaMemsetAsync(g->colsum.p, 0, (NLAYER + 1) * HID * sizeof(float), s));
+    for (int l = 0; l < NLAYER; ++l) {
+        const float *LP = P + P_L0 + l * L_STRIDE;
+        k_aggregate<false><<<g1(n * 32), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p, Hl(g, l), Ml(g, l));
+        k_colsum<<<std::min<int64_t>((n + 3) / 4, 152 * 4), kT, 0, s>>>(n, Hl(g, l), g->colsum.p + l * HID);
+        k_gterm<<<1, HID, 0, s>>>(g->colsum.p + l * HID, 1.f / (float)n, LP + L_U, g->gterm.p + l * HID);
+        k_gemm<KC, HID, HID, EPI_LAYER><<<gg, 128, 0, s>>>(n, Hl(g, l), Ml(g, l), g->wt.p + WT_L0 + l * KC * HID,
+                                                           LP + L_B, g->gterm.p + l * HID, Hl(g, l), Zl(g, l),
+                                                           Hl(g, l + 1));
+    }
+    k_decode<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, P + P_BD, h->bc_of_dof.p, g->u.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 3 + NLAYER * 4;
+    // A u_hat and the two dot products u.b~, u.A u
+    FE_CHECK(spmv64(h, g->u.p, g->Au.p));
+    FE_CHECK(dalloc(g->acc, 4));
+    FE_CUDA(cudaMemsetAsync(g->acc.p, 0, 4 * sizeof(double), s));
+    k_dots2<<<g1(h->n_dof), kT, 0, s>>>(h->n_dof, g->u.p, g->bt.p, g->Au.p, g->acc.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    if (!g->acc_host) FE_CUDA(cudaMallocHost((void **)&g->acc_host, 4 * sizeof(double)));
+    FE_CUDA(cudaMemcpyAsync(g->acc_host, g->acc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    g->last_num = g->acc_host[0];
+    g->last_den = g->acc_host[1];
+    g->last_scale = g->last_den > 0 ? g->last_num / g->last_den : 0.0;
+    return FE_OK;
+}
+
+int backward(fe_gnn_s *g, fe_handle_s *h, double energy, double *loss) {
+    const int64_t n = h->n_nodes, nd = h->n_dof;
+    cudaStream_t s = g->stream;
+    const float *P = g->params.p;
+    float *G = g->grad.p;
+    const double a = g->last_num, c = g->last_den;
+    if (!(c > 0) || !(energy > 0)) {
+        set_error("warm-start loss undefined: u_hat . A u_hat or the target energy is not positive");
+        return FE_BREAKDOWN;
+    }
+    *loss = 1.0 - a * a / (c * energy);
+    // dL/du = -2a/(c e) b~ + 2a^2/(c^2 e) A u
+    const double ca = -2.0 * a / (c * energy), cb = 2.0 * a * a / (c * c * energy);
+    FE_CUDA(cudaMemsetAsync(G, 0, P_TOTAL * sizeof(float), s));
+    k_loss_grad_u<<<g1(nd), kT, 0, s>>>(nd, g->bt.p, g->Au.p, h->bc_of_dof.p, ca, cb, g->du.p);
+    k_decode_back<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, g->du.p, g->dHn.p, G + P_WD, G + P_BD);
+    FE_CHECK(dalloc(g->dgb, HID * 2));
+    const int gg = (int)std::min<int64_t>((n + 63) / 64, 152 * 4);
+    const int gw = (int)std::min<int64_t>((n + 63) / 64, 152 * 2);
+    for (int l = NLAYER - 1; l >= 0; --l) {
+        const float *LP = P + P_L0 + l * L_STRIDE;
+        float *LG = G + P_L0 + l * L_STRIDE;
+        // dZ = dH_{l+1} (.) [z_l > 0]
+        k_relu_grad<<<g1(n * HID), kT, 0, s>>>(n * HID, g->dHn.p, Zl(g, l), g->dZ.p);
+        // dX = dZ W_l^T: the GEMM takes its right operand transposed, [out][in], and
+        // (W_l^T)^T = W_l in its stored [128][64] layout, so copy W_l to BF16 as it is
+        __nv_bfloat16 *wl = g->wt.p + (size_t)P_TOTAL;
+        k_to_bf16<<<16, 256, 0, s>>>(LP + L_W, KC * HID, wl);
+        k_gemm<HID, HID, KC, EPI_PLAIN><<<gg, 128, 0, s>>>(n, g->dZ.p, nullptr, wl, nullptr, nullptr, nullptr,
+                                                            nullptr, g->dX.p);
+        // weight gradients
+        k_gemm_wgrad<KC, HID, HID><<<gw, 128, 0, s>>>(n, Hl(g, l), Ml(g, l), g->dZ.p, LG + L_W);
+        FE_CUDA(cudaMemsetAsync(g->dgb.p + HID, 0, HID * sizeof(float), s));
+        k_colsum<<<std::min<int64_t>((n + 3) / 4, 152 * 4), kT, 0, s>>>(n, g->dZ.p, g->dgb.p + HID);
+        k_gterm_back<<<1, HID, 0, s>>>(g->colsum.p + l * HID, 1.f / (float)n, LP + L_U, g->dgb.p + HID, LG + L_U,
+                                       g->dgb.p);
+        // bias gradient = colsum(dZ)
+        FE_CUDA(cudaMemcpyAsync(LG + L_B, g->dgb.p + HID, HID * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        // dH_l = dH_{l+1} + dX[:, :64] + dg / N ;  dM = dX[:, 64:] ; dH_l += agg^T dM
+        k_layer_back_dh<<<g1(n * HID), kT, 0, s>>>(n, g->dHn.p, g->dX.p, g->dgb.p, g->dH.p);
+        k_split_dm<<<g1(n * HID), kT, 0, s>>>(n, g->dX.p, g->dM.p);
+        k_aggregate<true><<<g1(n * 32), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p, g->dM.p, g->dH.p);
+        std::swap(g->dH.p, g->dHn.p);
+        FE_LAUNCH_CHECK();
+    }
+    // encoder: dZ0 = dH_0 (.) [z0 > 0];  dW0 = F^T dZ0;  db0 = colsum(dZ0)
+    k_relu_grad<<<g1(n * HID), kT, 0, s>>>(n * HID, g->dHn.p, g->Z0.p, g->dZ.p);
+    k_gemm_wgrad<NF, NF, HID><<<gw, 128, 0, s>>>(n, g->F.p, nullptr, g->dZ.p, G + P_W0);
+    k_colsum<<<std::min<int64_t>((n + 3) / 4, 152 * 4), kT, 0, s>>>(n, g->dZ.p, G + P_B0);
+    FE_LAUNCH_CHECK();
+    h->launches += 2 + NLAYER * 9 + 3;
+    return FE_OK;
+}
+
+}  // namespace
+}  // namespace fe
+
+using namespace fe;
+
+extern "C" {
+
+int fe_gnn_create(fe_gnn *out) {
+    if (!out) {
+        set_error("fe_gnn_create: null output");
+        return FE_BAD_INPUT;
+    }
+    fe_gnn_s *g = new fe_gnn_s();
+    // BF16 weights: W0 and W_l transposed ([out][in]) for the forward GEMMs, then one
+    // slot holding the current layer's W_l as stored, for the data-gradient GEMM
+    int st = dalloc(g->params, P_TOTAL);
+    if (!st) st = dalloc(g->grad, P_TOTAL);
+    if (!st) st = dalloc(g->adam_m, P_TOTAL);
+    if (!st) st = dalloc(g->adam_v, P_TOTAL);
+    if (!st) st = dalloc(g->wt, (size_t)P_TOTAL + KC * HID);
+    if (st) {
+        fe_gnn_destroy(g);
+        return st;
+    }
+    cudaMemset(g->params.p, 0, P_TOTAL * sizeof(float));
+    cudaMemset(g->adam_m.p, 0, P_TOTAL * sizeof(float));
+    cudaMemset(g->adam_v.p, 0, P_TOTAL * sizeof(float));
+    *out = g;
+    return FE_OK;
+}
+
+int fe_gnn_destroy(fe_gnn g) {
+    if (!g) return FE_OK;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    dfree(g->params), dfree(g->grad), dfree(g->adam_m), dfree(g->adam_v), dfree(g->wt);
+    dfree(g->F), dfree(g->Z0), dfree(g->H), dfree(g->Z), dfree(g->M), dfree(g->dH), dfree(g->dHn), dfree(g->dX);
+    dfree(g->dZ), dfree(g->dM), dfree(g->inv_deg), dfree(g->colsum), dfree(g->gterm), dfree(g->stats);
+    dfree(g->du), dfree(g->dgb), dfree(g->gext), dfree(g->Ag), dfree(g->bt), dfree(g->u), dfree(g->Au);
+    dfree(g->x0), dfree(g->acc);
+    if (g->acc_host) cudaFreeHost(g->acc_host);
+    delete g;
+    return FE_OK;
+}
+
+int fe_gnn_num_params(int64_t *n) {
+    if (n) *n = P_TOTAL;
+    return FE_OK;
+}
+
+int fe_gnn_set_params(fe_gnn g, const float *host, int64_t n) {
+    if (!g || !host || n != P_TOTAL) {
+        set_error("fe_gnn_set_params: expected " + std::to_string(P_TOTAL) + " parameters");
+        return FE_BAD_INPUT;
+    }
+    FE_CUDA(cudaMemcpy(g->params.p, host, n * sizeof(float), cudaMemcpyHostToDevice));
+    FE_CUDA(cudaMemset(g->adam_m.p, 0, P_TOTAL * sizeof(float)));
+    FE_CUDA(cudaMemset(g->adam_v.p, 0, P_TOTAL * sizeof(float)));
+    g->steps = 0;
+    return FE_OK;
+}
+
+int fe_gnn_get_params(fe_gnn g, float *host, int64_t n) {
+    if (!g || !host || n != P_TOTAL) {
+        set_error("fe_gnn_get_params: expected " + std::to_string(P_TOTAL) + " parameters");
+        return FE_BAD_INPUT;
+    }
+    FE_CUDA(cudaDeviceSynchronize());
+    FE_CUDA(cudaMemcpy(host, g->params.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return FE_OK;
+}
+
+int fe_gnn_features(fe_gnn g, fe_handle h, float *host) {
+    if (!g || !h || !host) {
+        set_error("fe_gnn_features: null argument");
+        return FE_BAD_INPUT;
+    }
+    FE_CHECK(prepare(g, h));
+    FE_CUDA(cudaMemcpyAsync(host, g->F.p, h->n_nodes * NF * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    return FE_OK;
+}
+
+int fe_gnn_predict(fe_gnn g, fe_handle h, double *x0_host, const double **x0_dev, double *scale) {
+    if (!g || !h) {
+        set_error("fe_gnn_predict: null argument");
+        return FE_BAD_INPUT;
+    }
+    FE_CHECK(prepare(g, h));
+    g->stream = h->stream;
+    FE_CHECK(refresh_bf16(g));
+    FE_CHECK(forward(g, h));
+    k_warm_start<<<g1(h->n_dof), kT, 0, h->stream>>>(h->n_dof, g->gext.p, g->u.p, g->last_scale, g->x0.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    if (x0_host) {
+        FE_CUDA(cudaMemcpyAsync(x0_host, g->x0.p, h->n_dof * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        FE_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    if (x0_dev) *x0_dev = g->x0.p;
+    if (scale) *scale = g->last_scale;
+    return FE_OK;
+}
+
+int fe_gnn_target_energy(fe_gnn g, fe_handle h, double *energy) {
+    if (!g || !h || !energy) {
+        set_error("fe_gnn_target_energy: null argument");
+        return FE_BAD_INPUT;
+    }
+    if (!h->have_solution) {
+        set_error("fe_gnn_target_energy: solve the problem first");
+        return FE_NOT_READY;
+    }
+    FE_CHECK(prepare(g, h));
+    FE_CHECK(dalloc(g->acc, 4));
+    FE_CUDA(cudaMemsetAsync(g->acc.p + 2, 0, sizeof(double), h->stream));
+    k_energy<<<g1(h->n_dof), kT, 0, h->stream>>>(h->n_dof, g->bt.p, h->w.x.p, g->gext.p, g->acc.p + 2);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    FE_CUDA(cudaMemcpyAsync(energy, g->acc.p + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    return FE_OK;
+}
+
+int fe_gnn_loss_grad(fe_gnn g, fe_handle h, double energy, double *loss, float *grad_host) {
+    if (!g || !h || !loss) {
+        set_error("fe_gnn_loss_grad: null argument");
+        return FE_BAD_INPUT;
+    }
+    FE_CHECK(prepare(g, h));
+    FE_CHECK(refresh_bf16(g));
+    FE_CHECK(forward(g, h));
+    double l = 0;
+    FE_CHECK(backward(g, h, energy, &l));
+    *loss = l;
+    if (grad_host) {
+        FE_CUDA(cudaMemcpyAsync(grad_host, g->grad.p, P_TOTAL * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+        FE_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return FE_OK;
+}
+
+int fe_gnn_adam_step(fe_gnn g, float lr, float beta1, float beta2, float eps) {
+    if (!g) {
+        set_error("fe_gnn_adam_step: null network");
+        return FE_BAD_INPUT;
+    }
+    g->steps += 1;
+    float c1 = 1.f - powf(beta1, (float)g->steps), c2 = 1.f - powf(beta2, (float)g->steps);
+    k_adam<<<64, 256, 0, g->stream>>>(P_TOTAL, g->params.p, g->grad.p, g->adam_m.p, g->adam_v.p, lr, beta1, beta2, eps,
+                                      c1, c2);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+}  // extern "C"

@@ -219,5 +219,6 @@ int recover_multipliers(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);
 int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);
 void release_solver(fe_handle_s *h);
+int spmv64(fe_handle_s *h, const double *x, double *y);
 
 }  // namespace fe

@@ -1198,6 +1198,23 @@ int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {
     return time_spmv_any(h, precision, lanes, reps, ms);
 }
 
+// y = A x with the FP64 SELL copy of the eliminated matrix (used by the warm-start
+// network's loss).  Enqueued on the handle's stream.
+int spmv64(fe_handle_s *h, const double *x, double *y) {
+    if (!h->sys_ready) {
+        set_error("spmv64: the system is not assembled");
+        return FE_NOT_READY;
+    }
+    Sell A{h->sell_off.p, h->sell_col.p, h->n_slices};
+    if (h->dim == 2)
+        k_spmv<2, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p, x, y);
+    else
+        k_spmv<1, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p, x, y);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    return FE_OK;
+}
+
 void release_solver(fe_handle_s *h) {
     SolverWork &w = h->w;
     for (int i = 0; i < 2; ++i)

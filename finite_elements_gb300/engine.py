@@ -183,7 +183,7 @@ class GpuSystem:
 
     def solve(self, precision="fp64", tol=None, cheb_degree=0, max_iter=0, x0=None, lanes=0,
               accept_stagnation=False, inner_tol=0.0, cheb_ratio=0.0, chunk=0, max_outer=0,
-              want_host=True, restart_each_step=False):
+              want_host=True, restart_each_step=False, x0_device_ptr=None):
         """Solve the eliminated system on the GPU.  Returns (x, stats): x holds
         n_dof + n_bc values (u then the multipliers) or None with want_host=False."""
         o = SolveOpts()
@@ -198,6 +198,9 @@ class GpuSystem:
         if x0 is not None:
             x0a = np.ascontiguousarray(x0, dtype=np.float64)[: self.prob.n_dof]
             o.x0 = x0a.ctypes.data
+        elif x0_device_ptr is not None:
+            o.x0 = x0_device_ptr
+            o.x0_device = 1
         o.lanes = lanes
         o.chunk = chunk
         o.flags = ((_lib.FE_SOLVE_ACCEPT_STAGNATION if accept_stagnation else 0)

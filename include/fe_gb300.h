@@ -173,6 +173,31 @@ int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double 
 /* Average device time of one SpMV with the given lanes (reps repetitions). */
 int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out);
 
+/* ---- learned warm start (no counterpart in the reference: an addition on top of the
+ * PCG that replaces spsolve in analysis.py:816-830; PCG from its x0 still decides
+ * the accuracy).  A graph network over the mesh nodes (6 message-passing layers,
+ * hidden width 64, BF16 tensor-core GEMMs with FP32 accumulation) predicts the shape
+ * u_hat of the displacement; x0 = g + s u_hat with s the A-norm optimal scale.
+ * Elasticity meshes only. */
+typedef struct fe_gnn_s *fe_gnn;
+int fe_gnn_create(fe_gnn *out);
+int fe_gnn_destroy(fe_gnn g);
+int fe_gnn_num_params(int64_t *n);
+int fe_gnn_set_params(fe_gnn g, const float *params_host, int64_t n);
+int fe_gnn_get_params(fe_gnn g, float *params_host, int64_t n);
+/* The 16 node features of an assembled handle, n_nodes x 16 FP32. */
+int fe_gnn_features(fe_gnn g, fe_handle h, float *features_host);
+/* Warm start for h: *x0_dev (device, n_dof doubles, owned by g, valid until the next
+ * call; a copy also goes to x0_host when not NULL) and the scale s.  Pass *x0_dev to
+ * fe_solve as opts.x0 with opts.x0_device = 1. */
+int fe_gnn_predict(fe_gnn g, fe_handle h, double *x0_host, const double **x0_dev, double *scale);
+/* Training target of h's last solution: b~ . (x - g), the energy of its free part. */
+int fe_gnn_target_energy(fe_gnn g, fe_handle h, double *energy);
+/* Loss 1 - (u.b~)^2 / ((u.A u) energy) and its gradient w.r.t. every parameter
+ * (kept on the device for fe_gnn_adam_step; copied to grad_host when not NULL). */
+int fe_gnn_loss_grad(fe_gnn g, fe_handle h, double energy, double *loss, float *grad_host);
+int fe_gnn_adam_step(fe_gnn g, float lr, float beta1, float beta2, float eps);
+
 /* No counterpart in the reference.  Exclusive scan of n int32 counts into n+1 int32
  * offsets (offsets_dev[0] = 0, offsets_dev[n] = total; -1 there if the total does not
  * fit in int32) that allocates nothing: for callers who may not call cudaMalloc --
