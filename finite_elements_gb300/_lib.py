@@ -91,6 +91,7 @@ _SIGNATURES = {
     "fe_gnn_predict": ([_P, _P, _P, C.POINTER(_P), _PD], C.c_int),
     "fe_gnn_target_energy": ([_P, _P, _PD], C.c_int),
     "fe_gnn_loss_grad": ([_P, _P, _D, _PD, _P], C.c_int),
+    "fe_gnn_fit_grad": ([_P, _P, _PD, _P], C.c_int),
     "fe_gnn_adam_step": ([_P, C.c_float, C.c_float, C.c_float, C.c_float], C.c_int),
     "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
 }

@@ -11,7 +11,10 @@
 //   g_l = mean_i h_l,i                         global mean
 //   z_l = [h_l, m_l] W_l + b_l + g_l U_l
 //   h_{l+1} = h_l + relu(z_l)
-//   u_hat = h_6 Wd + bd, zero on constrained DOFs
+//   u_hat = (P S)^32 P (h_6 Wd + bd)          P: zero the constrained DOFs,
+//                                              S = (I + mean_nbr) / 2 (low-pass)
+// The fixed smoothing stage keeps u_hat smooth: in the A-norm a rough field is all
+// energy and no overlap with the solution, so it would scale x0 to nothing.
 // Loss: the share of the solution's energy the warm start leaves to PCG,
 //   L = 1 - (u_hat . b~)^2 / ((u_hat . A u_hat) (b~ . v*)),  v* = u* - g,
 // so training needs only b~ . v* from a solve of the problem.
@@ -36,6 +39,7 @@ constexpr int HID = 64;
 constexpr int NF = 16;
 constexpr int NLAYER = 6;
 constexpr int KC = 2 * HID;   // concatenated [h, m]
+constexpr int NSMOOTH = 32;   // lazy neighbour-mean steps applied to the decoded field
 
 // parameter offsets in the FP32 blob; every weight matrix is stored [in][out]
 constexpr int P_W0 = 0;
@@ -429,9 +433,9 @@ __global__ void k_btilde(int64_t n_dof, const double *__restrict__ b, const doub
         bt[i] = bc_of_dof[i] >= 0 ? 0.0 : b[i] - Ag[i];
 }
 
-// u_hat_i = h_i Wd + bd (two outputs), zero on constrained DOFs; one warp per node
+// u_i = h_i Wd + bd (two outputs), zero on constrained DOFs; one warp per node
 __global__ void k_decode(int64_t n, const float *__restrict__ Hh, const float *__restrict__ Wd,
-                         const float *__restrict__ bd, const int32_t *__restrict__ bc_of_dof, double *__restrict__ u) {
+                         const float *__restrict__ bd, const int32_t *__restrict__ bc_of_dof, float *__restrict__ u) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
@@ -444,10 +448,57 @@ __global__ void k_decode(int64_t n, const float *__restrict__ Hh, const float *_
             o1 += __shfl_xor_sync(0xffffffffu, o1, o);
         }
         if (lane == 0) {
-            u[2 * r] = bc_of_dof[2 * r] >= 0 ? 0.0 : (double)(o0 + bd[0]);
-            u[2 * r + 1] = bc_of_dof[2 * r + 1] >= 0 ? 0.0 : (double)(o1 + bd[1]);
+            u[2 * r] = bc_of_dof[2 * r] >= 0 ? 0.f : o0 + bd[0];
+            u[2 * r + 1] = bc_of_dof[2 * r + 1] >= 0 ? 0.f : o1 + bd[1];
         }
     }
+}
+
+// One step of the smoothing stage on the two-component node field:
+//   forward  (TRANSPOSE = false): out = P S in,   S = (I + mean_nbr) / 2
+//   adjoint  (TRANSPOSE = true):  out = S^T P in, S^T = (I + mean_nbr^T) / 2
+// mean_nbr^T gathers in[c] inv_deg[c] over the neighbours c of r (symmetric pattern).
+template <bool TRANSPOSE>
+__global__ void k_smooth(int64_t n, const int32_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                         const float *__restrict__ inv_deg, const int32_t *__restrict__ bc_of_dof,
+                         const float *__restrict__ in, float *__restrict__ out) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        float a0 = 0.f, a1 = 0.f;
+        for (int s = ptr[r]; s < ptr[r + 1]; ++s) {
+            const int c = col[s];
+            if (c == (int)r) continue;
+            float v0 = in[2 * (int64_t)c], v1 = in[2 * (int64_t)c + 1];
+            if (TRANSPOSE) {
+                const float w = inv_deg[c];
+                v0 = bc_of_dof[2 * (int64_t)c] >= 0 ? 0.f : v0 * w;
+                v1 = bc_of_dof[2 * (int64_t)c + 1] >= 0 ? 0.f : v1 * w;
+            }
+            a0 += v0;
+            a1 += v1;
+        }
+        float s0 = in[2 * r], s1 = in[2 * r + 1];
+        if (TRANSPOSE) {
+            if (bc_of_dof[2 * r] >= 0) s0 = 0.f;
+            if (bc_of_dof[2 * r + 1] >= 0) s1 = 0.f;
+            out[2 * r] = 0.5f * (s0 + a0);
+            out[2 * r + 1] = 0.5f * (s1 + a1);
+        } else {
+            const float w = inv_deg[r];
+            out[2 * r] = bc_of_dof[2 * r] >= 0 ? 0.f : 0.5f * (s0 + w * a0);
+            out[2 * r + 1] = bc_of_dof[2 * r + 1] >= 0 ? 0.f : 0.5f * (s1 + w * a1);
+        }
+    }
+}
+
+__global__ void k_f32_to_f64(int64_t n, const float *__restrict__ a, double *__restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
+// zero the constrained DOFs of a two-component field
+__global__ void k_mask2(int64_t n_dof, const int32_t *__restrict__ bc_of_dof, float *__restrict__ v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        if (bc_of_dof[i] >= 0) v[i] = 0.f;
 }
 
 // acc[0] += u.bt, acc[1] += u.Au  (FP64, block partials then atomics)
@@ -503,6 +554,57 @@ __global__ void k_decode_back(int64_t n, const float *__restrict__ Hh, const flo
     if (lane == 0) {
         atomicAdd(&dbd[0], b0);
         atomicAdd(&dbd[1], b1);
+    }
+}
+
+// Fitting loss against a solution x: t = (x - g) / sigma on free DOFs, sigma the RMS
+// of x - g over them.  Pass 1: acc[0] += sum (x - g)^2 and acc[1] += free count over the
+// free DOFs.  Pass 2 (sigma, n_free known): du = 2 (u - t) / n_free, acc[2] += (u - t)^2.
+__global__ void k_fit_stats(int64_t n_dof, const double *__restrict__ x, const double *__restrict__ g,
+                            const int32_t *__restrict__ bc_of_dof, double *__restrict__ acc) {
+    __shared__ double sh[2][kT / 32];
+    double s0 = 0, s1 = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        if (bc_of_dof[i] < 0) {
+            double d = x[i] - g[i];
+            s0 += d * d;
+            s1 += 1.0;
+        }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) sh[0][threadIdx.x >> 5] = s0, sh[1][threadIdx.x >> 5] = s1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, c = 0;
+        for (int w = 0; w < kT / 32; ++w) a += sh[0][w], c += sh[1][w];
+        atomicAdd(&acc[0], a);
+        atomicAdd(&acc[1], c);
+    }
+}
+
+__global__ void k_fit_grad(int64_t n_dof, const double *__restrict__ u, const double *__restrict__ x,
+                           const double *__restrict__ g, const int32_t *__restrict__ bc_of_dof, double inv_sigma,
+                           double inv_n, float *__restrict__ du, double *__restrict__ acc) {
+    __shared__ double sh[kT / 32];
+    double s0 = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x) {
+        if (bc_of_dof[i] >= 0) {
+            du[i] = 0.f;
+            continue;
+        }
+        double e = u[i] - (x[i] - g[i]) * inv_sigma;
+        du[i] = (float)(2.0 * e * inv_n);
+        s0 += e * e;
+    }
+    for (int o = 16; o > 0; o >>= 1) s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0;
+        for (int w = 0; w < kT / 32; ++w) a += sh[w];
+        atomicAdd(acc, a);
     }
 }
 
@@ -567,10 +669,13 @@ struct fe_gnn_s {
     fe::DBuf<__nv_bfloat16> wt;   // transposed BF16 copies of W0, W_l (in that order)
     int64_t n_cap = 0;            // nodes the activation buffers hold
     fe::DBuf<float> F, Z0, H, Z, M, dH, dHn, dX, dZ, dM, inv_deg, colsum, gterm, stats, du, dgb;
+    fe::DBuf<float> us0, us1;     // decoded field and the smoothing ping-pong buffer
     fe::DBuf<double> gext, Ag, bt, u, Au, x0, acc;
     double *acc_host = nullptr;
     int steps = 0;
     double last_scale = 0.0, last_num = 0.0, last_den = 0.0;
+    // stream of the handle the current call works on; valid only during that call
+    // (a handle and its stream may be destroyed before the network)
     cudaStream_t stream = nullptr;
 };
 
@@ -595,6 +700,8 @@ int gnn_alloc(fe_gnn_s *g, int64_t n) {
     FE_CHECK(dalloc(g->dM, N * HID));
     FE_CHECK(dalloc(g->inv_deg, N));
     FE_CHECK(dalloc(g->du, N * 2));
+    FE_CHECK(dalloc(g->us0, N * 2));
+    FE_CHECK(dalloc(g->us1, N * 2));
     FE_CHECK(dalloc(g->gext, N * 2));
     FE_CHECK(dalloc(g->Ag, N * 2));
     FE_CHECK(dalloc(g->bt, N * 2));
@@ -669,9 +776,15 @@ int forward(fe_gnn_s *g, fe_handle_s *h) {
                                                            LP + L_B, g->gterm.p + l * HID, Hl(g, l), Zl(g, l),
                                                            Hl(g, l + 1));
     }
-    k_decode<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, P + P_BD, h->bc_of_dof.p, g->u.p);
+    k_decode<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, P + P_BD, h->bc_of_dof.p, g->us0.p);
+    float *cur = g->us0.p, *nxt = g->us1.p;
+    for (int k = 0; k < NSMOOTH; ++k) {
+        k_smooth<false><<<g1(n), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p, h->bc_of_dof.p, cur, nxt);
+        std::swap(cur, nxt);
+    }
+    k_f32_to_f64<<<g1(2 * n), kT, 0, s>>>(2 * n, cur, g->u.p);
     FE_LAUNCH_CHECK();
-    h->launches += 3 + NLAYER * 4;
+    h->launches += 4 + NLAYER * 4 + NSMOOTH;
     // A u_hat and the two dot products u.b~, u.A u
     FE_CHECK(spmv64(h, g->u.p, g->Au.p));
     FE_CHECK(dalloc(g->acc, 4));
@@ -688,22 +801,51 @@ int forward(fe_gnn_s *g, fe_handle_s *h) {
     return FE_OK;
 }
 
-int backward(fe_gnn_s *g, fe_handle_s *h, double energy, double *loss) {
+// fit = false: energy loss with target energy `energy`; fit = true: mean-squared
+// error against the handle's current solution, normalised by its RMS.
+int backward(fe_gnn_s *g, fe_handle_s *h, double energy, bool fit, double *loss) {
     const int64_t n = h->n_nodes, nd = h->n_dof;
     cudaStream_t s = g->stream;
     const float *P = g->params.p;
     float *G = g->grad.p;
-    const double a = g->last_num, c = g->last_den;
-    if (!(c > 0) || !(energy > 0)) {
-        set_error("warm-start loss undefined: u_hat . A u_hat or the target energy is not positive");
-        return FE_BREAKDOWN;
-    }
-    *loss = 1.0 - a * a / (c * energy);
-    // dL/du = -2a/(c e) b~ + 2a^2/(c^2 e) A u
-    const double ca = -2.0 * a / (c * energy), cb = 2.0 * a * a / (c * c * energy);
     FE_CUDA(cudaMemsetAsync(G, 0, P_TOTAL * sizeof(float), s));
-    k_loss_grad_u<<<g1(nd), kT, 0, s>>>(nd, g->bt.p, g->Au.p, h->bc_of_dof.p, ca, cb, g->du.p);
-    k_decode_back<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, g->du.p, g->dHn.p, G + P_WD, G + P_BD);
+    if (fit) {
+        FE_CUDA(cudaMemsetAsync(g->acc.p, 0, 4 * sizeof(double), s));
+        k_fit_stats<<<g1(nd), kT, 0, s>>>(nd, h->w.x.p, g->gext.p, h->bc_of_dof.p, g->acc.p);
+        FE_CUDA(cudaMemcpyAsync(g->acc_host, g->acc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        const double ss = g->acc_host[0], nf = g->acc_host[1];
+        if (!(ss > 0) || !(nf > 0)) {
+            set_error("warm-start fit: the solution has no free displacement");
+            return FE_BREAKDOWN;
+        }
+        const double sigma = sqrt(ss / nf);
+        k_fit_grad<<<g1(nd), kT, 0, s>>>(nd, g->u.p, h->w.x.p, g->gext.p, h->bc_of_dof.p, 1.0 / sigma, 1.0 / nf,
+                                         g->us0.p, g->acc.p + 2);
+        FE_CUDA(cudaMemcpyAsync(g->acc_host + 2, g->acc.p + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        *loss = g->acc_host[2] / nf;
+        h->launches += 2;
+    } else {
+        const double a = g->last_num, c = g->last_den;
+        if (!(c > 0) || !(energy > 0)) {
+            set_error("warm-start loss undefined: u_hat . A u_hat or the target energy is not positive");
+            return FE_BREAKDOWN;
+        }
+        *loss = 1.0 - a * a / (c * energy);
+        // dL/du = -2a/(c e) b~ + 2a^2/(c^2 e) A u
+        const double ca = -2.0 * a / (c * energy), cb = 2.0 * a * a / (c * c * energy);
+        k_loss_grad_u<<<g1(nd), kT, 0, s>>>(nd, g->bt.p, g->Au.p, h->bc_of_dof.p, ca, cb, g->us0.p);
+        h->launches += 1;
+    }
+    // adjoint of u = (P S)^K P u_dec:  g <- S^T P g, K times, then P
+    float *cur = g->us0.p, *nxt = g->us1.p;
+    for (int k = 0; k < NSMOOTH; ++k) {
+        k_smooth<true><<<g1(n), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p, h->bc_of_dof.p, cur, nxt);
+        std::swap(cur, nxt);
+    }
+    k_mask2<<<g1(nd), kT, 0, s>>>(nd, h->bc_of_dof.p, cur);
+    k_decode_back<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, cur, g->dHn.p, G + P_WD, G + P_BD);
     FE_CHECK(dalloc(g->dgb, HID * 2));
     const int gg = (int)std::min<int64_t>((n + 63) / 64, 152 * 4);
     const int gw = (int)std::min<int64_t>((n + 63) / 64, 152 * 2);
@@ -775,12 +917,12 @@ int fe_gnn_create(fe_gnn *out) {
 
 int fe_gnn_destroy(fe_gnn g) {
     if (!g) return FE_OK;
-    if (g->stream) cudaStreamSynchronize(g->stream);
+    cudaDeviceSynchronize();
     dfree(g->params), dfree(g->grad), dfree(g->adam_m), dfree(g->adam_v), dfree(g->wt);
     dfree(g->F), dfree(g->Z0), dfree(g->H), dfree(g->Z), dfree(g->M), dfree(g->dH), dfree(g->dHn), dfree(g->dX);
     dfree(g->dZ), dfree(g->dM), dfree(g->inv_deg), dfree(g->colsum), dfree(g->gterm), dfree(g->stats);
     dfree(g->du), dfree(g->dgb), dfree(g->gext), dfree(g->Ag), dfree(g->bt), dfree(g->u), dfree(g->Au);
-    dfree(g->x0), dfree(g->acc);
+    dfree(g->x0), dfree(g->acc), dfree(g->us0), dfree(g->us1);
     if (g->acc_host) cudaFreeHost(g->acc_host);
     delete g;
     return FE_OK;
@@ -821,6 +963,7 @@ int fe_gnn_features(fe_gnn g, fe_handle h, float *host) {
     FE_CHECK(prepare(g, h));
     FE_CUDA(cudaMemcpyAsync(host, g->F.p, h->n_nodes * NF * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     FE_CUDA(cudaStreamSynchronize(h->stream));
+    g->stream = nullptr;
     return FE_OK;
 }
 
@@ -840,6 +983,8 @@ int fe_gnn_predict(fe_gnn g, fe_handle h, double *x0_host, const double **x0_dev
         FE_CUDA(cudaMemcpyAsync(x0_host, g->x0.p, h->n_dof * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         FE_CUDA(cudaStreamSynchronize(h->stream));
     }
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    g->stream = nullptr;
     if (x0_dev) *x0_dev = g->x0.p;
     if (scale) *scale = g->last_scale;
     return FE_OK;
@@ -862,6 +1007,7 @@ int fe_gnn_target_energy(fe_gnn g, fe_handle h, double *energy) {
     h->launches += 1;
     FE_CUDA(cudaMemcpyAsync(energy, g->acc.p + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     FE_CUDA(cudaStreamSynchronize(h->stream));
+    g->stream = nullptr;
     return FE_OK;
 }
 
@@ -874,12 +1020,36 @@ int fe_gnn_loss_grad(fe_gnn g, fe_handle h, double energy, double *loss, float *
     FE_CHECK(refresh_bf16(g));
     FE_CHECK(forward(g, h));
     double l = 0;
-    FE_CHECK(backward(g, h, energy, &l));
+    FE_CHECK(backward(g, h, energy, false, &l));
     *loss = l;
-    if (grad_host) {
+    if (grad_host)
         FE_CUDA(cudaMemcpyAsync(grad_host, g->grad.p, P_TOTAL * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
-        FE_CUDA(cudaStreamSynchronize(h->stream));
+    // the gradient is complete before fe_gnn_adam_step (default stream) may read it
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    g->stream = nullptr;
+    return FE_OK;
+}
+
+int fe_gnn_fit_grad(fe_gnn g, fe_handle h, double *loss, float *grad_host) {
+    if (!g || !h || !loss) {
+        set_error("fe_gnn_fit_grad: null argument");
+        return FE_BAD_INPUT;
     }
+    if (!h->have_solution) {
+        set_error("fe_gnn_fit_grad: solve the problem first");
+        return FE_NOT_READY;
+    }
+    FE_CHECK(prepare(g, h));
+    FE_CHECK(refresh_bf16(g));
+    FE_CHECK(forward(g, h));
+    double l = 0;
+    FE_CHECK(backward(g, h, 0.0, true, &l));
+    *loss = l;
+    if (grad_host)
+        FE_CUDA(cudaMemcpyAsync(grad_host, g->grad.p, P_TOTAL * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    // the gradient is complete before fe_gnn_adam_step (default stream) may read it
+    FE_CUDA(cudaStreamSynchronize(h->stream));
+    g->stream = nullptr;
     return FE_OK;
 }
 
@@ -890,9 +1060,12 @@ int fe_gnn_adam_step(fe_gnn g, float lr, float beta1, float beta2, float eps) {
     }
     g->steps += 1;
     float c1 = 1.f - powf(beta1, (float)g->steps), c2 = 1.f - powf(beta2, (float)g->steps);
-    k_adam<<<64, 256, 0, g->stream>>>(P_TOTAL, g->params.p, g->grad.p, g->adam_m.p, g->adam_v.p, lr, beta1, beta2, eps,
-                                      c1, c2);
+    // the gradient call synchronised its handle's stream; run on the default stream and
+    // finish before any later call reads the parameters on another stream
+    k_adam<<<64, 256, 0, 0>>>(P_TOTAL, g->params.p, g->grad.p, g->adam_m.p, g->adam_v.p, lr, beta1, beta2, eps, c1,
+                              c2);
     FE_LAUNCH_CHECK();
+    FE_CUDA(cudaStreamSynchronize(0));
     return FE_OK;
 }
 

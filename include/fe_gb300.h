@@ -196,6 +196,9 @@ int fe_gnn_target_energy(fe_gnn g, fe_handle h, double *energy);
 /* Loss 1 - (u.b~)^2 / ((u.A u) energy) and its gradient w.r.t. every parameter
  * (kept on the device for fe_gnn_adam_step; copied to grad_host when not NULL). */
 int fe_gnn_loss_grad(fe_gnn g, fe_handle h, double energy, double *loss, float *grad_host);
+/* Mean-squared error of u_hat against h's last solution, (x - g) / RMS(x - g) on the
+ * free DOFs, and its gradient (the training loss; gradient kept as above). */
+int fe_gnn_fit_grad(fe_gnn g, fe_handle h, double *loss, float *grad_host);
 int fe_gnn_adam_step(fe_gnn g, float lr, float beta1, float beta2, float eps);
 
 /* No counterpart in the reference.  Exclusive scan of n int32 counts into n+1 int32

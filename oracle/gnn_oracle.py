@@ -10,7 +10,8 @@ the reference project; its definition is the library's (include/fe_gb300.h):
   b~ / max|b~| (2), mean log10 E of the incident elements - 10.5,
   10 (mean nu - 0.3), D^-1 b~ / max|D^-1 b~| (2);
   h0 = relu(f W0 + b0); h_{l+1} = h_l + relu([h_l, mean_nbr h_l] W_l + b_l + mean(h_l) U_l);
-  u_hat = h_6 Wd + bd (0 on constrained DOFs);
+  u_hat = (P S)^32 P (h_6 Wd + bd), P zeroing the constrained DOFs and
+  S = (I + mean_nbr) / 2 a low-pass step;
   loss = 1 - (u.b~)^2 / ((u.A u) e*).
 With bf16=True the GEMM inputs are rounded to bfloat16 as the tensor-core kernels do.
 """
@@ -22,7 +23,7 @@ import torch
 
 from oracle import fe_oracle as O
 
-HID, NF, NLAYER = 64, 16, 6
+HID, NF, NLAYER, NSMOOTH = 64, 16, 6, 32
 
 
 def split_params(p):
@@ -140,8 +141,10 @@ def _bf(x, on):
     return x.to(torch.bfloat16).to(torch.float64) if on else x
 
 
-def loss_and_grad(prob, params, energy, bf16=False):
-    """(loss, gradient in the library's parameter order, u_hat, features)."""
+def loss_and_grad(prob, params, energy, bf16=False, fit_solution=None):
+    """(loss, gradient in the library's parameter order, u_hat, features).  With
+    fit_solution = x the loss is the mean-squared error of u_hat against
+    (x - g) / RMS(x - g) on the free DOFs instead of the energy loss."""
     A, b, g, bt, mask = eliminated_system(prob)
     f = torch.as_tensor(features(prob, A, bt, mask))
     P = {k: v.requires_grad_(True) for k, v in split_params(params).items()}
@@ -153,8 +156,11 @@ def loss_and_grad(prob, params, energy, bf16=False):
         gm = h.mean(dim=0, keepdim=True)
         z = _bf(torch.cat([h, m], dim=1), bf16) @ _bf(P[f"W{l}"], bf16) + P[f"b{l}"] + gm @ P[f"U{l}"]
         h = h + torch.relu(z)
-    u = (h @ P["Wd"] + P["bd"]).reshape(-1)
-    u = torch.where(torch.as_tensor(mask), torch.zeros_like(u), u)
+    keep = torch.as_tensor(~mask.reshape(-1, 2)).to(torch.float64)
+    u = (h @ P["Wd"] + P["bd"]) * keep
+    for _ in range(NSMOOTH):
+        u = 0.5 * (u + torch.sparse.mm(Mt, u)) * keep
+    u = u.reshape(-1)
     At = torch.sparse_csr_tensor(torch.as_tensor(A.indptr, dtype=torch.int64),
                                  torch.as_tensor(A.indices, dtype=torch.int64),
                                  torch.as_tensor(A.data), A.shape)
@@ -162,7 +168,15 @@ def loss_and_grad(prob, params, energy, bf16=False):
     btt = torch.as_tensor(bt)
     a = u @ btt
     c = u @ Au
-    loss = 1.0 - a * a / (c * energy)
+    if fit_solution is not None:
+        free = ~mask
+        d = np.asarray(fit_solution)[: prob.n_dof] - g
+        sigma = np.sqrt(np.mean(d[free] ** 2))
+        t = torch.as_tensor(np.where(free, d / sigma, 0.0))
+        fm = torch.as_tensor(free.astype(np.float64))
+        loss = (((u - t) * fm) ** 2).sum() / free.sum()
+    else:
+        loss = 1.0 - a * a / (c * energy)
     loss.backward()
     return float(loss), flatten_grads(P), u.detach().numpy(), f.numpy()
 

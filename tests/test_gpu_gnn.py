@@ -59,7 +59,7 @@ def test_training_lowers_the_loss(gpu_lib):
     probs = [meshgen.plane_strain_random(40, 20, seed=s) for s in range(4)]
     net = WarmStartNet(seed=0)
     hist = train(probs, net, steps=300, lr=2e-3, log=None)
-    assert np.mean(hist[-30:]) < 0.8 * np.mean(hist[:10]), (hist[:10], hist[-30:])
+    assert np.mean(hist[-30:]) < 0.9 * np.mean(hist[:10]), (hist[:10], hist[-30:])
 
 
 def test_trained_network_gains_over_zero_start(gpu_lib):
@@ -81,3 +81,19 @@ def test_trained_network_gains_over_zero_start(gpu_lib):
     assert st0.status == 0 and st1.status == 0
     assert st1.relres <= 1e-8
     assert st1.iterations < st0.iterations, (st0.iterations, st1.iterations)
+
+
+def test_fit_loss_and_gradient_match_oracle(small):
+    """The training loss: mean-squared error against the normalised solution."""
+    from finite_elements_gb300.warmstart import WarmStartNet, init_params
+    from oracle import gnn_oracle as G
+    prob, s = small
+    p = init_params(seed=4)
+    net = WarmStartNet(params=p)
+    x, _ = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    loss, grad = net.fit_grad(s, want_grad=True)
+    L, gref, _, _ = G.loss_and_grad(prob, p, 1.0, bf16=True, fit_solution=x)
+    assert abs(loss - L) <= 1e-3 * max(abs(L), 1e-3), (loss, L)
+    cos = float(grad @ gref / (np.linalg.norm(grad) * np.linalg.norm(gref)))
+    rel = float(np.linalg.norm(grad - gref) / np.linalg.norm(gref))
+    assert cos >= 0.999 and rel <= 3e-2, (cos, rel)
