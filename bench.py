@@ -42,8 +42,11 @@ def parse_args():
     ap.add_argument("--ny", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cheb", type=int, default=3, help="Chebyshev degree of the mixed solve's preconditioner")
-    ap.add_argument("--plain-cheb", type=int, default=0, help="Chebyshev degree of the plain FP64 PCG")
+    ap.add_argument("--cheb", type=int, default=8, help="Chebyshev degree of the mixed solve's preconditioner")
+    ap.add_argument("--cheb-ratio", type=float, default=1000.0, help="Chebyshev interval lmax/lmin (mixed)")
+    ap.add_argument("--plain-cheb", type=int, default=6, help="Chebyshev degree of the plain FP64 PCG")
+    ap.add_argument("--plain-cheb-ratio", type=float, default=200.0, help="Chebyshev interval (plain FP64)")
+    ap.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="headline steps only (no plain / oracle / e2e legs), for profiler runs")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
@@ -186,12 +189,23 @@ def run_ours(args, dist):
     s = GpuSystem(prob, assemble=True)           # inputs uploaded: resident in HBM from here
     h = s.handle
     step_flags = _lib.FE_ASSEMBLE_PATTERN | _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
-    mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, want_host=False)
-    plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.plain_cheb, want_host=False)
+    mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
+                want_host=False)
+    plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.plain_cheb, cheb_ratio=args.plain_cheb_ratio,
+                 want_host=False)
+    net = None
+    if not args.no_learned:
+        from finite_elements_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartNet
+        if os.path.exists(DEFAULT_WEIGHTS):
+            net = WarmStartNet(weights=DEFAULT_WEIGHTS)
 
-    def device_step(opts):
+    def device_step(opts, learned=False):
         h.call("fe_assemble", step_flags)
-        _, st = s.solve(**opts)
+        if learned and net is not None:
+            ptr, _ = net.predict(s)               # the warm start is part of the step
+            _, st = s.solve(x0_device_ptr=ptr, **opts)
+        else:
+            _, st = s.solve(**opts)
         if st.status != _lib.FE_OK:
             raise RuntimeError(f"solve failed: {st.as_dict()}")
         return st
@@ -202,7 +216,7 @@ def run_ours(args, dist):
         return c.value
 
     for _ in range(args.warmup):
-        device_step(mode)
+        device_step(mode, learned=True)
 
     # ---- headline: mixed precision, inputs resident in HBM
     clocks = ClockSampler(dist.local_rank)
@@ -211,7 +225,7 @@ def run_ours(args, dist):
     l0 = launches()
     clocks.start()
     h.call("fe_event_record", 0)
-    stats = [device_step(mode) for _ in range(args.steps)]
+    stats = [device_step(mode, learned=True) for _ in range(args.steps)]
     h.call("fe_event_record", 1)
     h.call("fe_synchronize")
     clk = clocks.stop()
@@ -228,6 +242,15 @@ def run_ours(args, dist):
         return {"metric": METRIC, "value": value, "unit": UNIT, "quick": True,
                 "iterations": stats[-1].iterations, "gpu_launches": int(n_launch)}
 
+    # ---- mixed precision without the learned warm start, same step
+    h.call("fe_synchronize")
+    h.call("fe_event_record", 2)
+    nstats = [device_step(mode) for _ in range(max(args.plain_steps, 1))]
+    h.call("fe_event_record", 3)
+    h.call("fe_synchronize")
+    h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
+    mixed_only_s = ms.value / 1e3 / max(args.plain_steps, 1)
+
     # ---- plain FP64 PCG, same step
     device_step(plain)
     h.call("fe_synchronize")
@@ -239,7 +262,8 @@ def run_ours(args, dist):
     plain_s = ms.value / 1e3 / max(args.plain_steps, 1)
 
     # ---- FP64 oracle solution (tight tolerance) for the error of the mixed result
-    x_ref, st_ref = s.solve(precision="fp64", tol=1e-11, accept_stagnation=True)
+    x_ref, st_ref = s.solve(precision="fp64", tol=1e-11, cheb_degree=args.plain_cheb,
+                            cheb_ratio=args.plain_cheb_ratio, accept_stagnation=True)
     n = prob.n_dof
     err = float(np.linalg.norm(x_mixed[:n] - x_ref[:n]) / np.linalg.norm(x_ref[:n]))
 
@@ -261,12 +285,17 @@ def run_ours(args, dist):
     h2d = (prob.coords.nbytes + prob.conn.nbytes + prob.E.nbytes + prob.nu.nbytes + prob.thickness.nbytes
            + prob.rho.nbytes + prob.node_load_node.size * 24 + prob.node_bc_node.size * 16)
     e2e_times = []
-    e2e_opts = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, want_host=True)
+    e2e_opts = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
+                    want_host=True)
     for k in range(args.steps + 1):
         dist.barrier()
         t0 = time.perf_counter()
         se = GpuSystem(prob, assemble=True)
-        x, st = se.solve(**e2e_opts)
+        if net is not None:
+            ptr, _ = net.predict(se)
+            x, st = se.solve(x0_device_ptr=ptr, **e2e_opts)
+        else:
+            x, st = se.solve(**e2e_opts)
         dt = time.perf_counter() - t0
         d2h = x.nbytes
         se.close()
@@ -283,9 +312,10 @@ def run_ours(args, dist):
             "workload": f"plane strain {args.nx}x{args.ny} grid, {2 * args.nx * args.ny:,} triangles, "
                         f"{prob.n_dof:,} DOF, E=10^U(9,12) per element, nu~U(0.2,0.45), left edge clamped, "
                         f"random top-edge traction",
-            "mode": "mixed precision (FP32 diff-form SpMV + node-block Jacobi, FP64 refinement with "
-                    "reliable updates)" + (f", Chebyshev degree {args.cheb}" if args.cheb > 1 else ""),
-            "learned_warm_start": False,
+            "mode": "mixed precision (FP32 diff-form SELL SpMV, node-block Jacobi + Chebyshev, FP64 refinement "
+                    "with reliable updates)" + (" + learned warm start" if net is not None else ""),
+            "learned_warm_start": net is not None,
+            "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio]},
             "tol": args.tol, "step": "pattern + element kernels + reduction + loads + elimination + PCG",
             "l2": "inputs larger than L2 (BSR values alone 448 MB FP64 / 224 MB FP32)",
             "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
@@ -295,6 +325,7 @@ def run_ours(args, dist):
         "plain_fp64": {"s_per_solve": plain_s, "iterations": pstats[-1].iterations if pstats else None,
                        "relres": pstats[-1].relres if pstats else None},
         "speedup_vs_plain": plain_s / value if value > 0 else None,
+        "mixed_without_learned": {"s_per_solve": mixed_only_s, "iterations": nstats[-1].iterations},
         "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv<2,float> (timed as k_spmv<2,float>)",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src,

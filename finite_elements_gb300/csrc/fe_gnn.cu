@@ -348,57 +348,77 @@ __device__ __forceinline__ void atomic_max_f(float *addr, float v) {
     }
 }
 
-// stats[0..3] = bbox, stats[4] = max |b~|, stats[5] = max |D^-1 b~|
-__global__ void k_feature_stats(int64_t n, const double *__restrict__ coords, const double *__restrict__ bt,
-                                const double *__restrict__ dinv, float *__restrict__ stats) {
-    float xmn = 3.4e38f, xmx = -3.4e38f, ymn = 3.4e38f, ymx = -3.4e38f, bm = 0.f, zm = 0.f;
+// stats[0..3] = bounding box (FP32 atomics)
+__global__ void k_bbox(int64_t n, const double *__restrict__ coords, float *__restrict__ stats) {
+    float xmn = 3.4e38f, xmx = -3.4e38f, ymn = 3.4e38f, ymx = -3.4e38f;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         float x = (float)coords[2 * r], y = (float)coords[2 * r + 1];
         xmn = fminf(xmn, x), xmx = fmaxf(xmx, x), ymn = fminf(ymn, y), ymx = fmaxf(ymx, y);
-        double b0 = bt[2 * r], b1 = bt[2 * r + 1];
-        bm = fmaxf(bm, (float)fmax(fabs(b0), fabs(b1)));
-        double z0 = dinv[4 * r] * b0 + dinv[4 * r + 1] * b1, z1 = dinv[4 * r + 2] * b0 + dinv[4 * r + 3] * b1;
-        zm = fmaxf(zm, (float)fmax(fabs(z0), fabs(z1)));
     }
     for (int o = 16; o > 0; o >>= 1) {
         xmn = fminf(xmn, __shfl_xor_sync(0xffffffffu, xmn, o));
         xmx = fmaxf(xmx, __shfl_xor_sync(0xffffffffu, xmx, o));
         ymn = fminf(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
         ymx = fmaxf(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
-        bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
-        zm = fmaxf(zm, __shfl_xor_sync(0xffffffffu, zm, o));
     }
     if ((threadIdx.x & 31) == 0) {
         atomic_min_f(&stats[0], xmn);
         atomic_max_f(&stats[1], xmx);
         atomic_min_f(&stats[2], ymn);
         atomic_max_f(&stats[3], ymx);
-        atomic_max_pos(&stats[4], bm);
-        atomic_max_pos(&stats[5], zm);
     }
 }
 
-// 16 features per node (see fe_gb300.h, fe_gnn_features)
-__global__ void k_features(int64_t n, const double *__restrict__ coords, const int32_t *__restrict__ inc_ptr,
-                           const int32_t *__restrict__ inc, const double *__restrict__ E,
-                           const double *__restrict__ nu, const int32_t *__restrict__ bc_of_dof,
-                           const double *__restrict__ bt, const double *__restrict__ dinv,
-                           const float *__restrict__ stats, float *__restrict__ F) {
+// Graph-level load moments (FP64 atomics): gs[0] += sum b~_x, gs[1] += sum b~_y,
+// gs[2] += sum |b~|, gs[3] += sum b~_y x_n, gs[4] += sum b~_x y_n   (normalised
+// coordinates from the bounding box in stats)
+__global__ void k_load_moments(int64_t n, const double *__restrict__ coords, const double *__restrict__ bt,
+                               const float *__restrict__ stats, double *__restrict__ gs) {
+    const double L = fmax(fmax((double)stats[1] - stats[0], (double)stats[3] - stats[2]), 1e-30);
+    double a[5] = {0, 0, 0, 0, 0};
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const double xn = (coords[2 * r] - stats[0]) / L, yn = (coords[2 * r + 1] - stats[2]) / L;
+        const double bx = bt[2 * r], by = bt[2 * r + 1];
+        a[0] += bx, a[1] += by, a[2] += fabs(bx) + fabs(by), a[3] += by * xn, a[4] += bx * yn;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&gs[k], a[k]);
+    }
+}
+
+// Graph-level material means: gs[5] += sum log10 E, gs[6] += sum nu over the elements
+__global__ void k_material_means(int64_t ne, const double *__restrict__ E, const double *__restrict__ nu,
+                                 double *__restrict__ gs) {
+    double a = 0, b = 0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
+        a += log10(E[e]), b += nu[e];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&gs[5], a);
+        atomicAdd(&gs[6], b);
+    }
+}
+
+// 16 features per node: smooth per-node inputs (position, Fourier terms, constraint
+// flags) and graph-level quantities broadcast to every node (total-force direction,
+// load moments, mean log10 E and nu).  No per-node load or material value: those
+// vary from node to node and would make the network's output rough.
+__global__ void k_features(int64_t n, int64_t ne, const double *__restrict__ coords,
+                           const int32_t *__restrict__ bc_of_dof, const float *__restrict__ stats,
+                           const double *__restrict__ gs, float *__restrict__ F) {
     const float L = fmaxf(fmaxf(stats[1] - stats[0], stats[3] - stats[2]), 1e-30f);
-    const float ib = stats[4] > 0.f ? 1.f / stats[4] : 0.f, iz = stats[5] > 0.f ? 1.f / stats[5] : 0.f;
+    const double fn = sqrt(gs[0] * gs[0] + gs[1] * gs[1]);
+    const float fx = fn > 0 ? (float)(gs[0] / fn) : 0.f, fy = fn > 0 ? (float)(gs[1] / fn) : 0.f;
+    const float m1 = gs[2] > 0 ? (float)(gs[3] / gs[2]) : 0.f, m2 = gs[2] > 0 ? (float)(gs[4] / gs[2]) : 0.f;
+    const float le = ne > 0 ? (float)(gs[5] / ne) - 10.5f : 0.f, lnu = ne > 0 ? ((float)(gs[6] / ne) - 0.3f) * 10.f : 0.f;
     const float PI = 3.14159265358979f;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         float xn = ((float)coords[2 * r] - stats[0]) / L, yn = ((float)coords[2 * r + 1] - stats[2]) / L;
-        float le = 0.f, lnu = 0.f;
-        int cnt = inc_ptr[r + 1] - inc_ptr[r];
-        for (int s = inc_ptr[r]; s < inc_ptr[r + 1]; ++s) {
-            int e = inc[s] / 3;
-            le += (float)log10(E[e]);
-            lnu += (float)nu[e];
-        }
-        if (cnt > 0) le /= cnt, lnu /= cnt;
-        double b0 = bt[2 * r], b1 = bt[2 * r + 1];
-        double z0 = dinv[4 * r] * b0 + dinv[4 * r + 1] * b1, z1 = dinv[4 * r + 2] * b0 + dinv[4 * r + 3] * b1;
         float *f = F + r * NF;
         f[0] = xn;
         f[1] = yn;
@@ -410,12 +430,12 @@ __global__ void k_features(int64_t n, const double *__restrict__ coords, const i
         f[7] = sinf(2.f * PI * yn);
         f[8] = bc_of_dof[2 * r] >= 0 ? 1.f : 0.f;
         f[9] = bc_of_dof[2 * r + 1] >= 0 ? 1.f : 0.f;
-        f[10] = (float)b0 * ib;
-        f[11] = (float)b1 * ib;
-        f[12] = cnt > 0 ? le - 10.5f : 0.f;
-        f[13] = cnt > 0 ? (lnu - 0.3f) * 10.f : 0.f;
-        f[14] = (float)z0 * iz;
-        f[15] = (float)z1 * iz;
+        f[10] = fx;
+        f[11] = fy;
+        f[12] = m1;
+        f[13] = m2;
+        f[14] = le;
+        f[15] = lnu;
     }
 }
 
@@ -670,7 +690,7 @@ struct fe_gnn_s {
     int64_t n_cap = 0;            // nodes the activation buffers hold
     fe::DBuf<float> F, Z0, H, Z, M, dH, dHn, dX, dZ, dM, inv_deg, colsum, gterm, stats, du, dgb;
     fe::DBuf<float> us0, us1;     // decoded field and the smoothing ping-pong buffer
-    fe::DBuf<double> gext, Ag, bt, u, Au, x0, acc;
+    fe::DBuf<double> gext, Ag, bt, u, Au, x0, acc, gsum;
     double *acc_host = nullptr;
     int steps = 0;
     double last_scale = 0.0, last_num = 0.0, last_den = 0.0;
@@ -740,14 +760,17 @@ int prepare(fe_gnn_s *g, fe_handle_s *h) {
     FE_CHECK(spmv64(h, g->gext.p, g->Ag.p));
     k_btilde<<<g1(nd), kT, 0, s>>>(nd, h->b.p, g->Ag.p, h->bc_of_dof.p, g->bt.p);
     FE_CHECK(dalloc(g->stats, 8));
+    FE_CHECK(dalloc(g->gsum, 8));
     float init[8] = {3.4e38f, -3.4e38f, 3.4e38f, -3.4e38f, 0.f, 0.f, 0.f, 0.f};
     FE_CUDA(cudaMemcpyAsync(g->stats.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    k_feature_stats<<<g1(n), kT, 0, s>>>(n, h->coords.p, g->bt.p, h->dinv.p, g->stats.p);
-    k_features<<<g1(n), kT, 0, s>>>(n, h->coords.p, h->inc_ptr.p, h->inc.p, h->E.p, h->nu.p, h->bc_of_dof.p, g->bt.p,
-                                    h->dinv.p, g->stats.p, g->F.p);
+    FE_CUDA(cudaMemsetAsync(g->gsum.p, 0, 8 * sizeof(double), s));
+    k_bbox<<<g1(n), kT, 0, s>>>(n, h->coords.p, g->stats.p);
+    k_load_moments<<<g1(n), kT, 0, s>>>(n, h->coords.p, g->bt.p, g->stats.p, g->gsum.p);
+    k_material_means<<<g1(h->n_elem), kT, 0, s>>>(h->n_elem, h->E.p, h->nu.p, g->gsum.p);
+    k_features<<<g1(n), kT, 0, s>>>(n, h->n_elem, h->coords.p, h->bc_of_dof.p, g->stats.p, g->gsum.p, g->F.p);
     k_inv_deg<<<g1(n), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p);
     FE_LAUNCH_CHECK();
-    h->launches += 6 + (h->n_bc > 0 ? 1 : 0);
+    h->launches += 7 + (h->n_bc > 0 ? 1 : 0);
     // the host copy in init must stay valid until the copy ran
     FE_CUDA(cudaStreamSynchronize(s));
     return FE_OK;
@@ -922,7 +945,7 @@ int fe_gnn_destroy(fe_gnn g) {
     dfree(g->F), dfree(g->Z0), dfree(g->H), dfree(g->Z), dfree(g->M), dfree(g->dH), dfree(g->dHn), dfree(g->dX);
     dfree(g->dZ), dfree(g->dM), dfree(g->inv_deg), dfree(g->colsum), dfree(g->gterm), dfree(g->stats);
     dfree(g->du), dfree(g->dgb), dfree(g->gext), dfree(g->Ag), dfree(g->bt), dfree(g->u), dfree(g->Au);
-    dfree(g->x0), dfree(g->acc), dfree(g->us0), dfree(g->us1);
+    dfree(g->x0), dfree(g->acc), dfree(g->us0), dfree(g->us1), dfree(g->gsum);
     if (g->acc_host) cudaFreeHost(g->acc_host);
     delete g;
     return FE_OK;

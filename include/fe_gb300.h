@@ -186,7 +186,7 @@ int fe_gnn_num_params(int64_t *n);
 int fe_gnn_set_params(fe_gnn g, const float *params_host, int64_t n);
 int fe_gnn_get_params(fe_gnn g, float *params_host, int64_t n);
 /* The 16 node features of an assembled handle, n_nodes x 16 FP32. */
-int fe_gnn_features(fe_gnn g, fe_handle h, float *features_host);
+int fe_gnn_features(fe_gnn g, fe_handle h, float *features_host);  /* see fe_gnn.cu k_features */
 /* Warm start for h: *x0_dev (device, n_dof doubles, owned by g, valid until the next
  * call; a copy also goes to x0_host when not NULL) and the scale s.  Pass *x0_dev to
  * fe_solve as opts.x0 with opts.x0_device = 1. */

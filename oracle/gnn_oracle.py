@@ -6,9 +6,10 @@ its hand-written backward against autograd.  The warm start has no counterpart i
 the reference project; its definition is the library's (include/fe_gb300.h):
 
   features (16 per node): x_n, y_n (bounding-box normalised), sin/cos(pi x_n),
-  sin/cos(pi y_n), sin(2 pi x_n), sin(2 pi y_n), constrained flags (x, y),
-  b~ / max|b~| (2), mean log10 E of the incident elements - 10.5,
-  10 (mean nu - 0.3), D^-1 b~ / max|D^-1 b~| (2);
+  sin/cos(pi y_n), sin(2 pi x_n), sin(2 pi y_n), constrained flags (x, y), then
+  graph-level values broadcast to every node: the direction of the total load sum b~,
+  the load moments sum b~_y x_n / sum|b~| and sum b~_x y_n / sum|b~|, the mean of
+  log10 E over the elements - 10.5 and 10 (mean nu - 0.3);
   h0 = relu(f W0 + b0); h_{l+1} = h_l + relu([h_l, mean_nbr h_l] W_l + b_l + mean(h_l) U_l);
   u_hat = (P S)^32 P (h_6 Wd + bd), P zeroing the constrained DOFs and
   S = (I + mean_nbr) / 2 a low-pass step;
@@ -88,37 +89,22 @@ def features(prob, A, bt, mask):
     mx = xy.max(axis=0).astype(np.float32).astype(np.float64)
     L = max(mx[0] - mn[0], mx[1] - mn[1])
     xn, yn = (xy[:, 0] - mn[0]) / L, (xy[:, 1] - mn[1]) / L
-    # block-Jacobi inverse of the 2x2 diagonal blocks of A
-    Ad = A.tocsr()
-    blocks = np.zeros((n, 2, 2))
-    for a in range(2):
-        for c in range(2):
-            blocks[:, a, c] = np.asarray(Ad[np.arange(n) * 2 + a, np.arange(n) * 2 + c]).reshape(-1)
-    dinv = np.linalg.inv(blocks)
     b2 = bt.reshape(n, 2)
-    z = np.einsum("nab,nb->na", dinv, b2)
-    bm = np.abs(b2).max()
-    zm = np.abs(z).max()
-    cnt = np.zeros(n)
-    le = np.zeros(n)
-    lnu = np.zeros(n)
-    for i in range(3):
-        np.add.at(cnt, prob.conn[:, i], 1)
-        np.add.at(le, prob.conn[:, i], np.log10(prob.E))
-        np.add.at(lnu, prob.conn[:, i], prob.nu)
-    has = cnt > 0
-    le = np.where(has, le / np.maximum(cnt, 1), 0.0)
-    lnu = np.where(has, lnu / np.maximum(cnt, 1), 0.0)
+    sx, sy = b2[:, 0].sum(), b2[:, 1].sum()
+    sa = np.abs(b2).sum()
+    fn = np.hypot(sx, sy)
     f = np.zeros((n, NF))
     f[:, 0], f[:, 1] = xn, yn
     f[:, 2], f[:, 3] = np.sin(np.pi * xn), np.cos(np.pi * xn)
     f[:, 4], f[:, 5] = np.sin(np.pi * yn), np.cos(np.pi * yn)
     f[:, 6], f[:, 7] = np.sin(2 * np.pi * xn), np.sin(2 * np.pi * yn)
     f[:, 8], f[:, 9] = mask[0::2], mask[1::2]
-    f[:, 10:12] = b2 / bm if bm > 0 else 0.0
-    f[:, 12] = np.where(has, le - 10.5, 0.0)
-    f[:, 13] = np.where(has, (lnu - 0.3) * 10.0, 0.0)
-    f[:, 14:16] = z / zm if zm > 0 else 0.0
+    f[:, 10] = sx / fn if fn > 0 else 0.0
+    f[:, 11] = sy / fn if fn > 0 else 0.0
+    f[:, 12] = (b2[:, 1] * xn).sum() / sa if sa > 0 else 0.0
+    f[:, 13] = (b2[:, 0] * yn).sum() / sa if sa > 0 else 0.0
+    f[:, 14] = np.log10(prob.E).mean() - 10.5
+    f[:, 15] = (prob.nu.mean() - 0.3) * 10.0
     return f
 
 
