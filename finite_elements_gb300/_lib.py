@@ -93,6 +93,11 @@ _SIGNATURES = {
     "fe_gnn_loss_grad": ([_P, _P, _D, _PD, _P], C.c_int),
     "fe_gnn_fit_grad": ([_P, _P, _PD, _P], C.c_int),
     "fe_gnn_adam_step": ([_P, C.c_float, C.c_float, C.c_float, C.c_float], C.c_int),
+    "fe_batch_create": ([_P, _I32, _P, C.POINTER(_P)], C.c_int),
+    "fe_batch_destroy": ([_P], C.c_int),
+    "fe_batch_set_tiles": ([_P, _I32, _I64], C.c_int),
+    "fe_batch_autotune": ([_P, _PI32, _PI64, _PD], C.c_int),
+    "fe_batch_solve": ([_P, _D, _I32, _P, _P, _P, _P, _PD], C.c_int),
     "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
 }
 

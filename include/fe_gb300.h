@@ -201,6 +201,26 @@ int fe_gnn_loss_grad(fe_gnn g, fe_handle h, double energy, double *loss, float *
 int fe_gnn_fit_grad(fe_gnn g, fe_handle h, double *loss, float *grad_host);
 int fe_gnn_adam_step(fe_gnn g, float lr, float beta1, float beta2, float eps);
 
+/* ---- batched solve of many independent elasticity instances (no counterpart in the
+ * reference, which solves one analysis per spsolve call, analysis.py:816-830).  The
+ * instances are concatenated into one handle (fe_mesh_create on the union mesh with
+ * disjoint node ranges, then the usual setters and fe_assemble); node_ptr_host[i] ..
+ * node_ptr_host[i+1] are instance i's nodes.  The batched FP64 PCG (node-block
+ * Jacobi) runs each phase for all instances in one launch with per-instance
+ * reductions, step sizes and convergence; converged instances drop out. */
+typedef struct fe_batch_s *fe_batch;
+int fe_batch_create(fe_handle h, int32_t n_instances, const int64_t *node_ptr_host, fe_batch *out);
+int fe_batch_destroy(fe_batch b);
+/* Lanes per block row (1, 2, 4) and rows per persistent-kernel chunk. */
+int fe_batch_set_tiles(fe_batch b, int32_t lanes, int64_t rows_per_chunk);
+/* Time 20 iterations for each (lanes, rows per chunk) candidate and keep the fastest. */
+int fe_batch_autotune(fe_batch b, int32_t *lanes_out, int64_t *rows_out, double *us_per_iter_out);
+/* Solve every instance to ||b_i - A_i x_i|| <= tol ||b_i||; per-instance iterations,
+ * status and final true relative residual (each optional), the union solution
+ * (n_dof values, optional) and the device time of the solve. */
+int fe_batch_solve(fe_batch b, double tol, int32_t max_iter, int32_t *iterations_host, int32_t *status_host,
+                   double *relres_host, double *x_host, double *ms_out);
+
 /* No counterpart in the reference.  Exclusive scan of n int32 counts into n+1 int32
  * offsets (offsets_dev[0] = 0, offsets_dev[n] = total; -1 there if the total does not
  * fit in int32) that allocates nothing: for callers who may not call cudaMalloc --
