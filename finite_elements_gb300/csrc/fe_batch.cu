@@ -38,6 +38,27 @@ __device__ __forceinline__ void seg_add(double *sh, int local, double v, double 
     else atomicAdd(&global_acc[inst], v);
 }
 
+// Warp-aggregated segmented add; every lane of the warp calls it.  Lanes with
+// on = false contribute nothing.  When every contributing lane belongs to the same
+// instance (the usual case: a warp covers consecutive rows), the warp sums by
+// shuffles and one lane adds; otherwise each contributing lane adds itself.
+__device__ __forceinline__ void seg_add_warp(double *sh, int local, double v, double *global_acc, int inst,
+                                             bool on) {
+    const unsigned any = __ballot_sync(0xffffffffu, on);
+    if (!any) return;
+    const int leader = __ffs(any) - 1;
+    const int l0 = __shfl_sync(0xffffffffu, local, leader);
+    const bool same = __all_sync(0xffffffffu, !on || local == l0);
+    if (same) {
+        double t = on ? v : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if ((int)(threadIdx.x & 31) == leader) seg_add(sh, local, t, global_acc, inst);
+    } else if (on) {
+        seg_add(sh, local, v, global_acc, inst);
+    }
+}
+
 // Row loop of one chunk: rows [c0, c1) processed in steps of kBT / G rows.
 #define FE_CHUNK_LOOP(G)                                                                  \
     const int sub = threadIdx.x & ((G)-1);                                                \
@@ -95,11 +116,14 @@ kb_spmv(int64_t n_nodes, int64_t R, const int32_t *__restrict__ inst, const int3
             const int ir = in ? inst[r] : i0;
             const bool valid = in && !S.done[ir];
             double2 y = bsr_row<G>(r, valid, ptr, col, val, p, sub);
-            if (valid && sub == 0) {
+            const bool on = valid && sub == 0;
+            double pq = 0.0;
+            if (on) {
                 reinterpret_cast<double2 *>(q)[r] = y;
                 const double2 pv = reinterpret_cast<const double2 *>(p)[r];
-                seg_add(sh, ir - i0, pv.x * y.x + pv.y * y.y, S.pq, ir);
+                pq = pv.x * y.x + pv.y * y.y;
             }
+            seg_add_warp(sh, ir - i0, pq, S.pq, ir, on);
         }
         __syncthreads();
         const int nl = min(inst[c1 - 1] - i0 + 1, kMaxLocal);
@@ -142,23 +166,29 @@ kb_update(int64_t n_nodes, int64_t R, const int32_t *__restrict__ inst, double *
         const int i0 = inst[c0];
         for (int j = threadIdx.x; j < 2 * kMaxLocal; j += kBT) sh[j / kMaxLocal][j % kMaxLocal] = 0.0;
         __syncthreads();
-        for (int64_t r = c0 + threadIdx.x; r < c1; r += kBT) {
-            const int ir = inst[r];
-            if (S.done[ir]) continue;
-            const double a = S.alpha[ir];
-            double2 xv = reinterpret_cast<double2 *>(x)[r], rv = reinterpret_cast<double2 *>(r_)[r];
-            const double2 pv = reinterpret_cast<const double2 *>(p)[r], qv = reinterpret_cast<const double2 *>(q)[r];
-            xv.x += a * pv.x, xv.y += a * pv.y;
-            rv.x -= a * qv.x, rv.y -= a * qv.y;
-            reinterpret_cast<double2 *>(x)[r] = xv;
-            reinterpret_cast<double2 *>(r_)[r] = rv;
-            const double2 m0 = reinterpret_cast<const double2 *>(dinv)[2 * r];
-            const double2 m1 = reinterpret_cast<const double2 *>(dinv)[2 * r + 1];
-            const double2 zv = make_double2(m0.x * rv.x + m0.y * rv.y, m1.x * rv.x + m1.y * rv.y);
-            reinterpret_cast<double2 *>(z)[r] = zv;
-            const int l = ir - i0;
-            seg_add(sh[0], l, rv.x * zv.x + rv.y * zv.y, S.rz_new, ir);
-            seg_add(sh[1], l, rv.x * rv.x + rv.y * rv.y, S.rr, ir);
+        for (int64_t base = c0; base < c1; base += kBT) {
+            const int64_t r = base + threadIdx.x;
+            const int ir = r < c1 ? inst[r] : i0;
+            const bool on = r < c1 && !S.done[ir];
+            double rz = 0.0, rr = 0.0;
+            if (on) {
+                const double a = S.alpha[ir];
+                double2 xv = reinterpret_cast<double2 *>(x)[r], rv = reinterpret_cast<double2 *>(r_)[r];
+                const double2 pv = reinterpret_cast<const double2 *>(p)[r];
+                const double2 qv = reinterpret_cast<const double2 *>(q)[r];
+                xv.x += a * pv.x, xv.y += a * pv.y;
+                rv.x -= a * qv.x, rv.y -= a * qv.y;
+                reinterpret_cast<double2 *>(x)[r] = xv;
+                reinterpret_cast<double2 *>(r_)[r] = rv;
+                const double2 m0 = reinterpret_cast<const double2 *>(dinv)[2 * r];
+                const double2 m1 = reinterpret_cast<const double2 *>(dinv)[2 * r + 1];
+                const double2 zv = make_double2(m0.x * rv.x + m0.y * rv.y, m1.x * rv.x + m1.y * rv.y);
+                reinterpret_cast<double2 *>(z)[r] = zv;
+                rz = rv.x * zv.x + rv.y * zv.y;
+                rr = rv.x * rv.x + rv.y * rv.y;
+            }
+            seg_add_warp(sh[0], ir - i0, rz, S.rz_new, ir, on);
+            seg_add_warp(sh[1], ir - i0, rr, S.rr, ir, on);
         }
         __syncthreads();
         const int nl = min(inst[c1 - 1] - i0 + 1, kMaxLocal);
@@ -226,8 +256,10 @@ kb_start(int64_t n_nodes, int64_t R, const int32_t *__restrict__ inst, const int
             const int64_t r = base + threadIdx.x / G;
             const bool valid = r < c1;
             double2 ax = bsr_row<G>(r, valid, ptr, col, val, x, sub);
-            if (valid && sub == 0) {
-                const int ir = inst[r];
+            const bool on = valid && sub == 0;
+            const int ir = valid ? inst[r] : i0;
+            double rz = 0.0, rr = 0.0, bbv = 0.0;
+            if (on) {
                 const double2 bv = reinterpret_cast<const double2 *>(b)[r];
                 const double2 rv = make_double2(bv.x - ax.x, bv.y - ax.y);
                 reinterpret_cast<double2 *>(r_)[r] = rv;
@@ -236,11 +268,13 @@ kb_start(int64_t n_nodes, int64_t R, const int32_t *__restrict__ inst, const int
                 const double2 zv = make_double2(m0.x * rv.x + m0.y * rv.y, m1.x * rv.x + m1.y * rv.y);
                 reinterpret_cast<double2 *>(z)[r] = zv;
                 reinterpret_cast<double2 *>(p)[r] = zv;
-                const int l = ir - i0;
-                seg_add(sh[0], l, rv.x * zv.x + rv.y * zv.y, S.rz, ir);
-                seg_add(sh[1], l, rv.x * rv.x + rv.y * rv.y, S.rr, ir);
-                seg_add(sh[2], l, bv.x * bv.x + bv.y * bv.y, S.bb, ir);
+                rz = rv.x * zv.x + rv.y * zv.y;
+                rr = rv.x * rv.x + rv.y * rv.y;
+                bbv = bv.x * bv.x + bv.y * bv.y;
             }
+            seg_add_warp(sh[0], ir - i0, rz, S.rz, ir, on);
+            seg_add_warp(sh[1], ir - i0, rr, S.rr, ir, on);
+            seg_add_warp(sh[2], ir - i0, bbv, S.bb, ir, on);
         }
         __syncthreads();
         const int nl = min(inst[c1 - 1] - i0 + 1, kMaxLocal);
@@ -278,21 +312,40 @@ __global__ void kb_set_prescribed(int64_t n_bc, const int64_t *__restrict__ bc_d
         x[bc_dof[k]] = bc_val[k];
 }
 
-// per-instance true residual ||b - A x||^2 (FP64) for the final report
+// per-instance true residual ||b - A x||^2 (FP64) for the final report.  The row loop
+// runs the same number of trips in every lane (rows past the end contribute 0), so the
+// warp shuffles always see all 32 lanes; one atomic per warp when its rows share an
+// instance.
 __global__ void __launch_bounds__(kBT)
 kb_true_residual(int64_t n_nodes, const int32_t *__restrict__ inst, const int32_t *__restrict__ ptr,
                  const int32_t *__restrict__ col, const double *__restrict__ val, const double *__restrict__ b,
                  const double *__restrict__ x, double *__restrict__ acc) {
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        double a0 = 0, a1 = 0;
-        for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
-            const int c = col[k];
-            a0 += val[4 * (int64_t)k] * x[2 * (int64_t)c] + val[4 * (int64_t)k + 1] * x[2 * (int64_t)c + 1];
-            a1 += val[4 * (int64_t)k + 2] * x[2 * (int64_t)c] + val[4 * (int64_t)k + 3] * x[2 * (int64_t)c + 1];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t rows_padded = ((n_nodes + stride - 1) / stride) * stride;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows_padded; r += stride) {
+        const bool in = r < n_nodes;
+        double v = 0.0;
+        int key = -1;
+        if (in) {
+            double a0 = 0, a1 = 0;
+            for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
+                const int c = col[k];
+                a0 += val[4 * (int64_t)k] * x[2 * (int64_t)c] + val[4 * (int64_t)k + 1] * x[2 * (int64_t)c + 1];
+                a1 += val[4 * (int64_t)k + 2] * x[2 * (int64_t)c] + val[4 * (int64_t)k + 3] * x[2 * (int64_t)c + 1];
+            }
+            const double e0 = b[2 * r] - a0, e1 = b[2 * r + 1] - a1;
+            v = e0 * e0 + e1 * e1;
+            key = inst[r];
         }
-        const double e0 = b[2 * r] - a0, e1 = b[2 * r + 1] - a1;
-        atomicAdd(&acc[inst[r]], e0 * e0 + e1 * e1);
+        const int k0 = __shfl_sync(0xffffffffu, key, 0);
+        if (__all_sync(0xffffffffu, !in || key == k0)) {
+            double t = v;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if ((threadIdx.x & 31) == 0 && k0 >= 0) atomicAdd(&acc[k0], t);
+        } else if (in) {
+            atomicAdd(&acc[key], v);
+        }
     }
 }
 
