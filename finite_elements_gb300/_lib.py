@@ -82,6 +82,8 @@ _SIGNATURES = {
     "fe_launch_count": ([_P, _PI64], C.c_int),
     "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
     "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
+    "fe_post_elastic": ([_P, _P, _P, _P, _P], C.c_int),
+    "fe_post_magnetic": ([_P, _P, _P], C.c_int),
     "fe_gnn_create": ([C.POINTER(_P)], C.c_int),
     "fe_gnn_destroy": ([_P], C.c_int),
     "fe_gnn_num_params": ([_PI64], C.c_int),

@@ -213,6 +213,20 @@ class GpuSystem:
             _lib.check(status, "fe_solve")
         return x, st
 
+    def post(self, x=None):
+        """Per-element results of a solution (the handle's last one when x is None):
+        elasticity -> dict(strain (E,3), stress (E,3), energy (E,)); magnetostatics ->
+        dict(field (E,2))."""
+        ne = self.prob.n_elements
+        xa = None if x is None else np.ascontiguousarray(np.asarray(x, np.float64)[: self.prob.n_dof])
+        if self.prob.kind == ELASTIC:
+            strain, stress, energy = np.empty((ne, 3)), np.empty((ne, 3)), np.empty(ne)
+            self.handle.call("fe_post_elastic", ptr(xa), ptr(strain), ptr(stress), ptr(energy))
+            return {"strain": strain, "stress": stress, "energy": energy}
+        field = np.empty((ne, 2))
+        self.handle.call("fe_post_magnetic", ptr(xa), ptr(field))
+        return {"field": field}
+
     def info(self):
         nd, nb, nblk = _i64(), _i64(), _i64()
         self.handle.call("fe_info", nd, nb, nblk)

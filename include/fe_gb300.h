@@ -173,6 +173,14 @@ int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double 
 /* Average device time of one SpMV with the given lanes (reps repetitions). */
 int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out);
 
+/* ---- post-processing of a solution (results.py:809-830 strain/stress, :769-781 and
+ * elements.py:275-292 energy, results.py:121-152 magnetic field).  u_host / a_host:
+ * n_dof values, or NULL for the handle's last solution.  Per element: strain and
+ * stress 3 values each (xx, yy, xy), energy 1; magnetic field 2 (Bx, By). */
+int fe_post_elastic(fe_handle h, const double *u_host, double *strain_host, double *stress_host,
+                    double *energy_host);
+int fe_post_magnetic(fe_handle h, const double *a_host, double *field_host);
+
 /* ---- learned warm start (no counterpart in the reference: an addition on top of the
  * PCG that replaces spsolve in analysis.py:816-830; PCG from its x0 still decides
  * the accuracy).  A graph network over the mesh nodes (6 message-passing layers,

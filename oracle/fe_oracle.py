@@ -357,3 +357,29 @@ def solve_reduced(prob: Problem, method="direct", tol=1e-12, maxiter=200000):
     u[bc_dof] = bc_val
     lam = (F - K @ u)[bc_dof]
     return np.concatenate([u, lam])
+
+
+# ---------------------------------------------------------------- post-processing
+
+
+def elastic_post(prob: Problem, u):
+    """Per-element strain B q, stress (D B) q and energy 0.5 (q^T Ke) q
+    (results.py:809-830, elements.py:275-292)."""
+    q = np.asarray(u)[: prob.n_dof].reshape(-1, 2)[prob.conn].reshape(-1, 6)
+    p = element_points(prob)
+    B = b_matrix(p)
+    D = d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress)
+    strain = np.einsum("eij,ej->ei", B, q)
+    stress = np.einsum("eij,ej->ei", np.matmul(D, B), q)
+    ke = elastic_stiffness(prob).reshape(-1, 6, 6)
+    energy = 0.5 * np.einsum("ei,eij,ej->e", q, ke, q)
+    return strain, stress, energy
+
+
+def magnetic_field(prob: Problem, a):
+    """Per-element (Bx, By) = (sum c_i A_i, -sum b_i A_i) (results.py:121-152)."""
+    ff = form_functions(element_points(prob))
+    A = np.asarray(a)[: prob.n_nodes][prob.conn]
+    bx = (ff[:, :, 2] * A).sum(axis=1)
+    by = -(ff[:, :, 1] * A).sum(axis=1)
+    return np.stack([bx, by], axis=1)

@@ -1,0 +1,90 @@
+"""Full-size configurations: the 1M-triangle magnetostatic problem against the
+oracle's direct solve, and size-independent properties of the 4M-DOF plane-strain
+problem checked on the host from the exported matrices (the oracle's NATURAL spsolve
+does not fit in memory at that size).
+
+Tolerances: magnetostatic solution ||a - a_ref|| <= 1e-8 ||a_ref|| (FP64 PCG to its
+rounding floor); K symmetric to 1e-13 of max|K|; interior row sums (K times a rigid
+translation) <= 1e-12 of the row's max; total mass 1e-12; augmented residual
+||F - K_aug x|| <= 1e-7 ||F|| for the 1e-8 mixed-precision solve; FP64 solves
+bitwise identical run to run."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+pytestmark = pytest.mark.gpu
+
+
+def test_magnetostatic_1m_triangles(gpu_lib):
+    from finite_elements_gb300 import meshgen
+    from finite_elements_gb300.engine import GpuSystem
+    from oracle import fe_oracle as O
+    prob = meshgen.magnetostatic(1000, 500, seed=0)
+    assert prob.n_elements == 1_000_000 and prob.n_dof == 501_501
+    s = GpuSystem(prob)
+    x, st = s.solve(precision="fp64", tol=1e-12, accept_stagnation=True)
+    assert st.status == 0
+    ref = O.solve_reduced(prob, "direct")
+    n = prob.n_dof
+    assert np.linalg.norm(x[:n] - ref[:n]) <= 1e-8 * np.linalg.norm(ref[:n])
+    # multipliers: reactions at the 3,000 boundary nodes
+    assert len(s.bc_dof) == 3000
+    assert np.linalg.norm(x[n:] - ref[n:]) <= 1e-7 * np.linalg.norm(ref[n:])
+    xm, stm = s.solve(precision="mixed", tol=1e-10, cheb_degree=4, cheb_ratio=200)
+    assert stm.status == 0 and stm.relres <= 1e-10
+    assert np.linalg.norm(xm[:n] - ref[:n]) <= 1e-7 * np.linalg.norm(ref[:n])
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def big(gpu_lib):
+    from finite_elements_gb300 import meshgen
+    from finite_elements_gb300.engine import GpuSystem
+    prob = meshgen.plane_strain_random(2000, 1000, seed=0)
+    s = GpuSystem(prob)
+    yield prob, s
+    s.close()
+
+
+def test_4m_stiffness_is_symmetric_and_annihilates_translations(big):
+    prob, s = big
+    ks = s.k_matrix_sparse()                       # CSC of K
+    kr = sp.csr_matrix((ks.data, ks.indices, ks.indptr), shape=ks.shape)   # same arrays read as CSR = K^T
+    K = ks.tocsr()
+    assert ks.shape == (prob.n_dof, prob.n_dof)
+    assert K.nnz == kr.nnz
+    assert abs(K - kr).max() <= 1e-13 * abs(K).max()
+    # rows of nodes with no condition: K (1,0,1,0,...) = 0 and K (0,1,0,1,...) = 0
+    tx = np.tile([1.0, 0.0], prob.n_nodes)
+    ty = np.tile([0.0, 1.0], prob.n_nodes)
+    rowmax = abs(K).max(axis=1).toarray().ravel()
+    for t in (tx, ty):
+        r = np.abs(K @ t)
+        assert (r <= 1e-12 * rowmax + 1e-300).all()
+
+
+def test_4m_total_mass(big):
+    from oracle import fe_oracle as O
+    prob, s = big
+    M = s.m_matrix_sparse()
+    area = O.triangle_area(O.element_points(prob))
+    total = 2.0 * np.sum(prob.rho * area * prob.thickness)
+    assert abs(M.sum() - total) <= 1e-12 * total
+
+
+def test_4m_mixed_solution_meets_the_residual_on_the_host(big):
+    prob, s = big
+    x, st = s.solve(precision="mixed", tol=1e-8, cheb_degree=8, cheb_ratio=1000)
+    assert st.status == 0 and st.relres <= 1e-8
+    K = s.create_matrix()                          # augmented saddle matrix, scipy CSR
+    F = s.create_source_matrix()[:, 0]
+    r = F - K @ x
+    assert np.linalg.norm(r) <= 1e-7 * np.linalg.norm(F)
+
+
+def test_4m_fp64_is_deterministic(big):
+    prob, s = big
+    x1, st1 = s.solve(precision="fp64", tol=1e-6, cheb_degree=0)
+    x2, st2 = s.solve(precision="fp64", tol=1e-6, cheb_degree=0)
+    assert st1.iterations == st2.iterations
+    np.testing.assert_array_equal(x1, x2)
