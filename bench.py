@@ -28,6 +28,11 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# DRAM bytes (read + write) per launch of the roofline kernel from one ncu capture of
+# this workload, keyed by grid (profiles/ holds the capture summary); None when the
+# workload differs from the captured one.
+NCU_TRAFFIC = {}
+
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
 UNIT = "s/solve"
 
@@ -42,13 +47,15 @@ def parse_args():
     ap.add_argument("--ny", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cheb", type=int, default=8, help="Chebyshev degree of the mixed solve's preconditioner")
-    ap.add_argument("--cheb-ratio", type=float, default=1000.0, help="Chebyshev interval lmax/lmin (mixed)")
-    ap.add_argument("--plain-cheb", type=int, default=6, help="Chebyshev degree of the plain FP64 PCG")
-    ap.add_argument("--plain-cheb-ratio", type=float, default=200.0, help="Chebyshev interval (plain FP64)")
+    ap.add_argument("--cheb", type=int, default=12, help="Chebyshev degree of the mixed solve's preconditioner")
+    ap.add_argument("--cheb-ratio", type=float, default=3000.0, help="Chebyshev interval lmax/lmin (mixed)")
+    ap.add_argument("--plain-cheb", type=int, default=16, help="Chebyshev degree of the plain FP64 PCG")
+    ap.add_argument("--plain-cheb-ratio", type=float, default=3000.0, help="Chebyshev interval (plain FP64)")
     ap.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="headline steps only (no plain / oracle / e2e legs), for profiler runs")
+    ap.add_argument("--quick-plain", action="store_true",
+                    help="with --quick: time the plain FP64 PCG step instead of the headline")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--cpu-nx", type=int, default=200, help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -215,6 +222,30 @@ def run_ours(args, dist):
         h.call("fe_launch_count", ctypes.byref(c))
         return c.value
 
+    def profile_read(precision):
+        cm, cn, sm, sn = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+        h.call("fe_profile_read", precision, ctypes.byref(cm), ctypes.byref(cn), ctypes.byref(sm), ctypes.byref(sn))
+        return {"cheb_us": 1e3 * cm.value / max(cn.value, 1), "cheb_n": cn.value,
+                "spmv_us": 1e3 * sm.value / max(sn.value, 1), "spmv_n": sn.value}
+
+    if args.quick and args.quick_plain:
+        # profiler runs of the plain FP64 step: no event records, no other legs
+        for _ in range(args.warmup):
+            device_step(plain)
+        h.call("fe_synchronize")
+        h.call("fe_event_record", 0)
+        pst = [device_step(plain) for _ in range(args.steps)]
+        h.call("fe_event_record", 1)
+        h.call("fe_synchronize")
+        ms = ctypes.c_double()
+        h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
+        s.close()
+        return {"metric": METRIC, "plain_s_per_solve": ms.value / 1e3 / args.steps, "quick": True,
+                "iterations": pst[-1].iterations}
+
+    # event records around the first iteration of every chunk of the captured PCG
+    # loop time the kernels inside the measured solves (not in profiler runs)
+    h.call("fe_profile_kernels", 0 if args.quick else 1)
     for _ in range(args.warmup):
         device_step(mode, learned=True)
 
@@ -222,6 +253,7 @@ def run_ours(args, dist):
     clocks = ClockSampler(dist.local_rank)
     dist.barrier()
     h.call("fe_synchronize")
+    h.call("fe_profile_kernels", 0 if args.quick else 1)   # reset the kernel-time sums
     l0 = launches()
     clocks.start()
     h.call("fe_event_record", 0)
@@ -230,6 +262,7 @@ def run_ours(args, dist):
     h.call("fe_synchronize")
     clk = clocks.stop()
     n_launch = launches() - l0
+    prof_mixed = profile_read(_lib.FE_PREC_MIXED)
     ms = ctypes.c_double()
     h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
     dist.barrier()
@@ -254,12 +287,15 @@ def run_ours(args, dist):
     # ---- plain FP64 PCG, same step
     device_step(plain)
     h.call("fe_synchronize")
+    h.call("fe_profile_kernels", 1)
     h.call("fe_event_record", 2)
     pstats = [device_step(plain) for _ in range(args.plain_steps)]
     h.call("fe_event_record", 3)
     h.call("fe_synchronize")
     h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
     plain_s = ms.value / 1e3 / max(args.plain_steps, 1)
+    prof_plain = profile_read(_lib.FE_PREC_FP64)
+    h.call("fe_profile_kernels", 0)
 
     # ---- FP64 oracle solution (tight tolerance) for the error of the mixed result
     x_ref, st_ref = s.solve(precision="fp64", tol=1e-11, cheb_degree=args.plain_cheb,
@@ -267,18 +303,31 @@ def run_ours(args, dist):
     n = prob.n_dof
     err = float(np.linalg.norm(x_mixed[:n] - x_ref[:n]) / np.linalg.norm(x_ref[:n]))
 
-    # ---- roofline of the dominant kernel: the FP32 block SpMV of the PCG iteration
-    lanes = ctypes.c_int32()
-    spmv_ms = ctypes.c_double()
-    h.call("fe_autotune_spmv", _lib.FE_PREC_MIXED, ctypes.byref(lanes), ctypes.byref(spmv_ms))
-    h.call("fe_time_spmv", _lib.FE_PREC_MIXED, lanes.value, 50, ctypes.byref(spmv_ms))
+    # ---- roofline.  Algorithmic bytes per launch (2x2 node blocks, s = value size):
+    # off-diagonal blocks (4 s + 4 column bytes each) + per node: Chebyshev step --
+    # diagonal slot 4s, block-Jacobi inverse 4s, z_k, r, z_{k-1} read and z_{k+1}
+    # written (2s each); PCG SpMV -- diagonal 4s, p read and q written (2s each);
+    # + 4 bytes of slice offset per 32 rows.
     info = s.info()
     nnzb, n_nodes = info["n_blocks"], prob.n_nodes
-    spmv_bytes = nnzb * (16 + 4) + n_nodes * (4 + 8 + 8)
-    achieved = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
-    spmv64_ms = ctypes.c_double()
-    h.call("fe_time_spmv", _lib.FE_PREC_FP64, 1, 20, ctypes.byref(spmv64_ms))
-    spmv64_bytes = nnzb * (32 + 4) + n_nodes * (4 + 16 + 16)
+    nb_off = nnzb - n_nodes
+    slices = (n_nodes + 31) // 32 + 1
+
+    def cheb_bytes(sz):
+        return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + 4 * sz + 4 * 2 * sz) + slices * 4
+
+    def spmv_bytes(sz):
+        return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + 2 * 2 * sz) + slices * 4
+
+    def roof(bytes_, us):
+        gbs = bytes_ / (us * 1e-6) / 1e9 if us > 0 else None
+        return gbs, (gbs / hbm_peak if gbs else None)
+
+    cheb_gbs, cheb_frac = roof(cheb_bytes(4), prof_mixed["cheb_us"])
+    spmv32_gbs, spmv32_frac = roof(spmv_bytes(4), prof_mixed["spmv_us"])
+    cheb64_gbs, cheb64_frac = roof(cheb_bytes(8), prof_plain["cheb_us"])
+    spmv64_gbs, spmv64_frac = roof(spmv_bytes(8), prof_plain["spmv_us"])
+    traffic = NCU_TRAFFIC.get((args.nx, args.ny))
     s.close()
 
     # ---- end to end through the C ABI, host buffers in and out
@@ -326,14 +375,27 @@ def run_ours(args, dist):
                        "relres": pstats[-1].relres if pstats else None},
         "speedup_vs_plain": plain_s / value if value > 0 else None,
         "mixed_without_learned": {"s_per_solve": mixed_only_s, "iterations": nstats[-1].iterations},
-        "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv<2,float> (timed as k_spmv<2,float>)",
-                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_source": peak_src,
-                     "bytes_per_launch": spmv_bytes, "launch_us": spmv_ms.value * 1e3,
-                     "lanes": lanes.value, "traffic": None},
-        "fp64_spmv": {"launch_us": spmv64_ms.value * 1e3,
-                      "achieved_gbs": spmv64_bytes / (spmv64_ms.value * 1e-3) / 1e9,
-                      "fp64_tflops": 2 * 4 * nnzb / (spmv64_ms.value * 1e-3) / 1e12},
+        "roofline": {"bound": "hbm", "kernel": "k_cheb_step<2,float,2> (intermediate Chebyshev step of the mixed "
+                                                "PCG: 6 of the 12 kernels of an iteration at degree 8)",
+                     "achieved": cheb_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": cheb_frac,
+                     "peak_source": peak_src, "traffic": traffic,
+                     "bytes_per_launch": cheb_bytes(4), "launch_us": prof_mixed["cheb_us"],
+                     "launches_timed": prof_mixed["cheb_n"],
+                     "timing": "CUDA events captured in the PCG graph around the first iteration of each "
+                               "16-iteration chunk, during the timed solves"},
+        "kernels": {
+            "mixed_pcg_spmv": {"kernel": "k_pcg_spmv<2,float>", "launch_us": prof_mixed["spmv_us"],
+                               "bytes_per_launch": spmv_bytes(4), "achieved_gbs": spmv32_gbs,
+                               "frac": spmv32_frac, "launches_timed": prof_mixed["spmv_n"]},
+            "plain_pcg_spmv": {"kernel": "k_pcg_spmv<2,double>", "launch_us": prof_plain["spmv_us"],
+                               "bytes_per_launch": spmv_bytes(8), "achieved_gbs": spmv64_gbs,
+                               "frac": spmv64_frac, "launches_timed": prof_plain["spmv_n"],
+                               "fp64_tflops": (8 * nnzb / (prof_plain["spmv_us"] * 1e-6) / 1e12
+                                               if prof_plain["spmv_us"] > 0 else None)},
+            "plain_cheb_step": {"kernel": "k_cheb_step<2,double,2>", "launch_us": prof_plain["cheb_us"],
+                                "bytes_per_launch": cheb_bytes(8), "achieved_gbs": cheb64_gbs,
+                                "frac": cheb64_frac, "launches_timed": prof_plain["cheb_n"]},
+        },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(n_launch),

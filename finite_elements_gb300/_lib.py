@@ -45,7 +45,8 @@ class SolveOpts(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
                 ("spmv", C.c_int32), ("relres", C.c_double), ("bnorm", C.c_double),
-                ("solve_ms", C.c_double), ("assemble_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("assemble_ms", C.c_double), ("fp64_iterations", C.c_int32),
+                ("reserved", C.c_int32)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -82,6 +83,8 @@ _SIGNATURES = {
     "fe_launch_count": ([_P, _PI64], C.c_int),
     "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
     "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
+    "fe_profile_kernels": ([_P, _I32], C.c_int),
+    "fe_profile_read": ([_P, _I32, _PD, _PI64, _PD, _PI64], C.c_int),
     "fe_post_elastic": ([_P, _P, _P, _P, _P], C.c_int),
     "fe_post_magnetic": ([_P, _P, _P], C.c_int),
     "fe_gnn_create": ([C.POINTER(_P)], C.c_int),

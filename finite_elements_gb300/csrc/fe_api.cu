@@ -423,4 +423,24 @@ int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, do
     return time_spmv(h, precision, lanes, reps, ms_out);
 }
 
+int fe_profile_kernels(fe_handle h, int32_t enable) {
+    FE_HANDLE_CHECK(h);
+    return profile_kernels(h, enable);
+}
+
+int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *cheb_n, double *spmv_ms,
+                    int64_t *spmv_n) {
+    FE_HANDLE_CHECK(h);
+    if (precision != FE_PREC_FP64 && precision != FE_PREC_MIXED) {
+        set_error("fe_profile_read: unknown precision");
+        return FE_BAD_INPUT;
+    }
+    const int slot = precision == FE_PREC_MIXED ? 1 : 0;
+    if (cheb_ms) *cheb_ms = h->w.prof_ms[slot][0];
+    if (cheb_n) *cheb_n = h->w.prof_n[slot][0];
+    if (spmv_ms) *spmv_ms = h->w.prof_ms[slot][1];
+    if (spmv_n) *spmv_n = h->w.prof_n[slot][1];
+    return FE_OK;
+}
+
 }  // extern "C"

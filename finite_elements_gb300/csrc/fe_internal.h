@@ -100,10 +100,10 @@ struct PcgScalars {
 
 struct SolverWork {
     // FP64 vectors (n_dof each): solution, residual, preconditioned residual,
-    // direction, A p, a second z for Chebyshev ping-pong, the Chebyshev update d
-    DBuf<double> x, r, z, p, q, t, dch;
-    // FP32 vectors of the mixed inner solve (d32 is its solution, the correction)
-    DBuf<float> r32, z32, p32, q32, d32, zc32, c32;
+    // direction, A p, a second z for the Chebyshev ping-pong (also scratch)
+    DBuf<double> x, r, z, p, q, t;
+    // FP32 vectors of the mixed inner solve (the solution stays in x, FP64)
+    DBuf<float> r32, z32, p32, q32, zc32;
     DBuf<double> partials;   // per-block partial sums of the reductions
     DBuf<PcgScalars> sc;
     PcgScalars *sc_host = nullptr;       // pinned mirror
@@ -115,7 +115,15 @@ struct SolverWork {
         int k = -1, G = -1, chunk = -1;
         const void *x = nullptr;
         double theta = 0, delta = 0;
+        bool prof = false;
     } key[2];
+    // Kernel timing inside the captured loop (fe_profile_kernels): event records
+    // around the first iteration of every chunk, [slot][0] an intermediate Chebyshev
+    // step, [slot][1] the PCG SpMV; summed durations and launches counted.
+    bool prof = false;
+    cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double prof_ms[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    int64_t prof_n[2][2] = {{0, 0}, {0, 0}};
 };
 
 }  // namespace fe
@@ -218,6 +226,7 @@ int solve(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
 int recover_multipliers(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);
 int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);
+int profile_kernels(fe_handle_s *h, int enable);
 void release_solver(fe_handle_s *h);
 int spmv64(fe_handle_s *h, const double *x, double *y);
 

@@ -216,28 +216,29 @@ __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, cons
     const int64_t rows_padded = ((n_nodes + groups - 1) / groups) * groups;                 \
     for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (G); row < rows_padded; row += groups)
 
-// Row r of A x from the SELL-32 copy: one lane per block row, one warp per slice of
-// 32 rows, entry k of the slice at base + 32 k + lane, so each warp load of columns
-// and blocks is one contiguous segment.  The diagonal block comes from diag (A_rr, or
-// S_r in the FP32 difference form); padding entries point at the row itself.
+// acc += B x for one D x D block, as a chain of fused multiply-adds into the
+// accumulator: 2 D FMAs per block, the least work for the FP64 pipe that bounds the
+// FP64 SpMV on this GPU.
 template <int D, typename T>
-__device__ __forceinline__ NodeVec<D, T> block_apply(const T *__restrict__ blk, const NodeVec<D, T> &x) {
-    NodeVec<D, T> y;
+__device__ __forceinline__ void block_mac(const T *__restrict__ blk, const NodeVec<D, T> &x, NodeVec<D, T> &acc) {
     if constexpr (D == 2) {
         if constexpr (sizeof(T) == 8) {
             const double2 b0 = __ldg(reinterpret_cast<const double2 *>(blk));
             const double2 b1 = __ldg(reinterpret_cast<const double2 *>(blk) + 1);
-            y.v[0] = b0.x * x.v[0] + b0.y * x.v[1];
-            y.v[1] = b1.x * x.v[0] + b1.y * x.v[1];
+            acc.v[0] = fma(b0.x, x.v[0], acc.v[0]);
+            acc.v[1] = fma(b1.x, x.v[0], acc.v[1]);
+            acc.v[0] = fma(b0.y, x.v[1], acc.v[0]);
+            acc.v[1] = fma(b1.y, x.v[1], acc.v[1]);
         } else {
             const float4 b = __ldg(reinterpret_cast<const float4 *>(blk));
-            y.v[0] = b.x * x.v[0] + b.y * x.v[1];
-            y.v[1] = b.z * x.v[0] + b.w * x.v[1];
+            acc.v[0] = fmaf(b.x, x.v[0], acc.v[0]);
+            acc.v[1] = fmaf(b.z, x.v[0], acc.v[1]);
+            acc.v[0] = fmaf(b.y, x.v[1], acc.v[0]);
+            acc.v[1] = fmaf(b.w, x.v[1], acc.v[1]);
         }
     } else {
-        y.v[0] = __ldg(blk) * x.v[0];
+        acc.v[0] = fma(__ldg(blk), x.v[0], acc.v[0]);
     }
-    return y;
 }
 
 struct Sell {
@@ -245,6 +246,10 @@ struct Sell {
     int64_t n_slices;
 };
 
+// Row r of A x from the SELL-32 copy: one lane per block row, one warp per slice of
+// 32 rows, entry k of the slice at base + 32 k + lane, so each warp load of columns
+// and blocks is one contiguous segment.  The diagonal block comes from diag (A_rr, or
+// S_r in the FP32 difference form); padding entries point at the row itself.
 template <int D, typename T>
 __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const Sell &A, const T *__restrict__ val,
                                                   const T *__restrict__ diag, const T *__restrict__ x) {
@@ -254,23 +259,34 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
     for (int a = 0; a < D; ++a) xr.v[a] = T(0), acc.v[a] = T(0);
     if (valid) {
         xr = ld<D, T>(x, r);
-        acc = block_apply<D, T>(diag + r * D * D, xr);
+        block_mac<D, T>(diag + r * D * D, xr, acc);
     }
     const int64_t sl = r >> 5;
     const int lane = (int)(r & 31);
     const int64_t base = A.off[sl];
     const int w = (A.off[sl + 1] - (int)base) >> 5;
-    for (int k = 0; k < w; ++k) {
-        const int64_t e = base + 32 * (int64_t)k + lane;
-        const int c = __ldg(A.col + e);
-        NodeVec<D, T> xv = ld<D, T>(x, c);
-        if (DIFF) {
+    // FP32: four entries per trip, their column loads and then their gathers all in
+    // flight before the first product (entries past w read the row itself and add
+    // 0).  FP64 is bound by the FP64 FMA rate and runs one entry per trip.
+    constexpr int U = sizeof(T) == 4 ? 4 : 1;
+    for (int k = 0; k < w; k += U) {
+        int c[U];
 #pragma unroll
-            for (int a = 0; a < D; ++a) xv.v[a] -= xr.v[a];
+        for (int u = 0; u < U; ++u)
+            c[u] = (k + u < w) ? __ldg(A.col + base + 32 * (int64_t)(k + u) + lane) : (int)r;
+        NodeVec<D, T> xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = ld<D, T>(x, c[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (k + u < w) {
+                if (DIFF) {
+#pragma unroll
+                    for (int a = 0; a < D; ++a) xv[u].v[a] -= xr.v[a];
+                }
+                block_mac<D, T>(val + (base + 32 * (int64_t)(k + u) + lane) * D * D, xv[u], acc);
+            }
         }
-        NodeVec<D, T> t = block_apply<D, T>(val + e * D * D, xv);
-#pragma unroll
-        for (int a = 0; a < D; ++a) acc.v[a] += t.v[a];
     }
     return acc;
 }
@@ -395,12 +411,12 @@ __device__ __forceinline__ void finish_iteration(PcgScalars *sc, double rz_new) 
 }
 
 // x += alpha p (x in FP64); r -= alpha q; then z = M^-1 r (Jacobi) or, with CHEB,
-// the first Chebyshev term z = d = M^-1 r / theta.  Reduces r.z and r.r.
+// the first Chebyshev term z_1 = M^-1 r / theta.  Reduces r.z and r.r.
 template <int D, typename T, bool CHEB>
 __global__ void __launch_bounds__(kVecThreads)
 k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
-             const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z, T *__restrict__ dch,
-             double *partials, PcgScalars *sc) {
+             const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z, double *partials,
+             PcgScalars *sc) {
     if (sc->done) return;
     const double alpha = sc->alpha;
     const T alpha_t = (T)alpha;
@@ -421,7 +437,6 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
         if (CHEB) {
 #pragma unroll
             for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
-            st<D, T>(dch, i, zv);
         }
         st<D, T>(z, i, zv);
 #pragma unroll
@@ -449,35 +464,43 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
     }
 }
 
-// One Chebyshev step on D^-1 A z = D^-1 r:
-//   d = c1 d + c2 M^-1 (r - A z_in);   z_out = z_in + d.
+// One Chebyshev step on D^-1 A z = D^-1 r in three-term form:
+//   z_{k+1} = z_k + c1 (z_k - z_{k-1}) + c2 M^-1 (r - A z_k),
+// with z_0 = 0 (FIRST: step k = 1).  z_{k+1} is written over z_{k-1} in zprev_out:
+// every thread reads and writes only its own rows there, while the gathers of the
+// product read z_k.
 // MODE 0: at the start of a loop (no reduction, runs even when done is set);
-// MODE 1: last step of an iteration (reduces r.z_out, finishes the iteration);
+// MODE 1: last step of an iteration (reduces r.z_{k+1}, finishes the iteration);
 // MODE 2: intermediate step.
-template <int D, typename T, int MODE>
+template <int D, typename T, int MODE, bool FIRST>
 __global__ void __launch_bounds__(kVecThreads)
 k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
             const T *__restrict__ dinv, const T *__restrict__ rres, const T *__restrict__ z_in,
-            T *__restrict__ z_out, T *__restrict__ dch, double c1, double c2, double *partials, PcgScalars *sc) {
+            T *__restrict__ zprev_out, double c1, double c2, double *partials, PcgScalars *sc) {
     if (MODE != 0 && sc->done) return;
+    const T c1t = (T)c1, c2t = (T)c2;
     T lrz = T(0);
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
         NodeVec<D, T> az = sell_row<D, T>(row, valid, A, val, diag, z_in);
         if (valid) {
-            NodeVec<D, T> rv = ld<D, T>(rres, row), zv = ld<D, T>(z_in, row), dv = ld<D, T>(dch, row);
+            NodeVec<D, T> rv = ld<D, T>(rres, row), zv = ld<D, T>(z_in, row), zp;
+            if (FIRST) {
+#pragma unroll
+                for (int a = 0; a < D; ++a) zp.v[a] = T(0);
+            } else {
+                zp = ld<D, T>(zprev_out, row);
+            }
             NodeVec<D, T> res;
 #pragma unroll
             for (int a = 0; a < D; ++a) res.v[a] = rv.v[a] - az.v[a];
             NodeVec<D, T> mr = apply_dinv<D, T>(dinv, row, res);
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                dv.v[a] = (T)c1 * dv.v[a] + (T)c2 * mr.v[a];
-                zv.v[a] += dv.v[a];
+                zv.v[a] += c1t * (zv.v[a] - zp.v[a]) + c2t * mr.v[a];
                 lrz += rv.v[a] * zv.v[a];
             }
-            st<D, T>(dch, row, dv);
-            st<D, T>(z_out, row, zv);
+            st<D, T>(zprev_out, row, zv);
         }
     }
     if (MODE == 1) {
@@ -501,11 +524,12 @@ k_pcg_direction(int64_t n_nodes, const T *__restrict__ z, T *__restrict__ p, Pcg
     }
 }
 
-// Start of a loop, given r: z = M^-1 r (times 1/theta and d = z with CHEB).
+// Start of a loop, given r: z = M^-1 r (times 1/theta with CHEB: the first
+// Chebyshev term z_1).
 template <int D, typename T, bool CHEB>
 __global__ void __launch_bounds__(kVecThreads)
 k_start_precond(int64_t n_nodes, const T *__restrict__ r, const T *__restrict__ dinv, T *__restrict__ z,
-                T *__restrict__ dch, double theta) {
+                double theta) {
     const T inv_theta = CHEB ? (T)(1.0 / theta) : T(1);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -513,7 +537,6 @@ k_start_precond(int64_t n_nodes, const T *__restrict__ r, const T *__restrict__ 
         if (CHEB) {
 #pragma unroll
             for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
-            st<D, T>(dch, i, zv);
         }
         st<D, T>(z, i, zv);
     }
@@ -618,7 +641,7 @@ struct Sys {
     const T *sval = nullptr, *diag = nullptr;  // SELL values and diagonal blocks
     const T *val = nullptr, *dinv = nullptr;
     double *x = nullptr;   // the solution, FP64 in both precisions
-    T *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *zc = nullptr, *dch = nullptr;
+    T *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *zc = nullptr;
 };
 
 struct Cheb {
@@ -656,30 +679,43 @@ Sys<T> make_sys(fe_handle_s *h) {
     if constexpr (sizeof(T) == 8) {
         s.sval = h->sell_val64.p, s.diag = h->diag64.p;
         s.val = h->aval.p, s.dinv = h->dinv.p;
-        s.r = w.r.p, s.p = w.p.p, s.q = w.q.p, s.z = w.z.p, s.zc = w.t.p, s.dch = w.dch.p;
+        s.r = w.r.p, s.p = w.p.p, s.q = w.q.p, s.z = w.z.p, s.zc = w.t.p;
     } else {
         s.sval = h->sell_val32.p, s.diag = h->diag32.p;
         s.val = h->aval32.p, s.dinv = h->dinv32.p;
-        s.r = w.r32.p, s.p = w.p32.p, s.q = w.q32.p, s.z = w.z32.p, s.zc = w.zc32.p, s.dch = w.c32.p;
+        s.r = w.r32.p, s.p = w.p32.p, s.q = w.q32.p, s.z = w.z32.p, s.zc = w.zc32.p;
     }
     return s;
 }
 
+template <int D, typename T, int MODE>
+void launch_cheb_step(fe_handle_s *h, const Sys<T> &s, bool first, const T *zin, T *zout, double c1, double c2,
+                      double *part, PcgScalars *sc, int grid) {
+    if (first)
+        k_cheb_step<D, T, MODE, true><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv,
+                                                                           s.r, zin, zout, c1, c2, part, sc);
+    else
+        k_cheb_step<D, T, MODE, false><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv,
+                                                                            s.r, zin, zout, c1, c2, part, sc);
+}
+
+// Chebyshev steps 1..k-1 after z_1 is in s.z; z ping-pongs between s.z and s.zc
+// (each step overwrites z_{k-1} with z_{k+1}); *z_final is the buffer holding z_k.
 template <int D, typename T>
 void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part, int grid,
-                        bool start, T **z_final) {
+                        bool start, T **z_final, cudaEvent_t *ev = nullptr) {
     T *zin = s.z, *zout = s.zc;
     for (int k = 1; k < cb.k; ++k) {
-        const bool last = (k == cb.k - 1);
+        const bool last = (k == cb.k - 1), first = (k == 1);
+        const bool timed = ev && k == 2 && !last;      // an intermediate step (MODE 2)
+        if (timed) cudaEventRecordWithFlags(ev[2], h->stream, cudaEventRecordExternal);
         if (start)
-            k_cheb_step<D, T, 0><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.r,
-                                                                      zin, zout, s.dch, cb.c1[k], cb.c2[k], part, sc);
+            launch_cheb_step<D, T, 0>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid);
         else if (last)
-            k_cheb_step<D, T, 1><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.r,
-                                                                      zin, zout, s.dch, cb.c1[k], cb.c2[k], part, sc);
+            launch_cheb_step<D, T, 1>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid);
         else
-            k_cheb_step<D, T, 2><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.r,
-                                                                      zin, zout, s.dch, cb.c1[k], cb.c2[k], part, sc);
+            launch_cheb_step<D, T, 2>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid);
+        if (timed) cudaEventRecordWithFlags(ev[3], h->stream, cudaEventRecordExternal);
         std::swap(zin, zout);
     }
     *z_final = zin;
@@ -688,18 +724,21 @@ void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScal
 inline int sell_grid(const fe_handle_s *h) { return grid_for(h->n_slices * 32, kVecThreads, 152 * 8); }
 
 template <int D, typename T>
-void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part) {
+void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part,
+                       cudaEvent_t *ev = nullptr) {
     const int gv = vec_grid(h->n_nodes);
     const int gs = sell_grid(h);
+    if (ev) cudaEventRecordWithFlags(ev[0], h->stream, cudaEventRecordExternal);
     k_pcg_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.p, s.q, part, sc);
+    if (ev) cudaEventRecordWithFlags(ev[1], h->stream, cudaEventRecordExternal);
     T *zf = s.z;
     if (cb.k > 1) {
-        k_pcg_update<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z, s.dch,
+        k_pcg_update<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z,
                                                                     part, sc);
-        enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, false, &zf);
+        enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, false, &zf, ev);
     } else {
         k_pcg_update<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z,
-                                                                     s.dch, part, sc);
+                                                                     part, sc);
     }
     k_pcg_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
 }
@@ -712,10 +751,10 @@ int enqueue_start(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *s
     const int gs = sell_grid(h);
     T *zf = s.z;
     if (cb.k > 1) {
-        k_start_precond<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, s.dch, cb.theta);
+        k_start_precond<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, cb.theta);
         enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, true, &zf);
     } else {
-        k_start_precond<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, s.dch, 1.0);
+        k_start_precond<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, 1.0);
     }
     k_start_finish<D, T, CONT><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, zf, s.p, part, sc);
     if (CONT) k_continue_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
@@ -761,14 +800,25 @@ int read_scalars(fe_handle_s *h) {
 
 // Run PCG iterations until the device says done, replaying a captured chunk of
 // iterations (captured once per configuration and reused across solves).
+// Progress watch of a running loop: the host sees r.r after every chunk; a running
+// minimum that has not improved by 10% (in norm) for `window` iterations marks the
+// loop as stalled and ends it at that chunk boundary (x, r, p stay consistent).
+struct StallWatch {
+    int window = 0;
+    double best = INFINITY;
+    int best_iter = 0;
+    bool stalled = false;
+};
+
 template <int D, typename T, int G>
-int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk) {
+int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk, StallWatch *watch = nullptr) {
     SolverWork &w = h->w;
     PcgScalars *sc = w.sc.p;
     const int slot = sizeof(T) == 8 ? 0 : 1;
     SolverWork::Key &kk = w.key[slot];
+    const bool prof = w.prof && w.pev[0];
     bool same = w.graph[slot] && kk.k == cb.k && kk.G == G && kk.chunk == chunk && kk.x == (const void *)s.p &&
-                kk.theta == cb.theta && kk.delta == cb.delta;
+                kk.theta == cb.theta && kk.delta == cb.delta && kk.prof == prof;
     if (!same) {
         if (w.graph[slot]) {
             cudaGraphExecDestroy(w.graph[slot]);
@@ -776,7 +826,8 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk) {
         }
         cudaGraph_t g;
         FE_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < chunk; ++i) enqueue_iteration<D, T>(h, s, cb, sc, w.partials.p);
+        for (int i = 0; i < chunk; ++i)
+            enqueue_iteration<D, T>(h, s, cb, sc, w.partials.p, (prof && i == 0) ? w.pev : nullptr);
         cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
         if (ce != cudaSuccess) {
             set_error(std::string("graph capture: ") + cudaGetErrorString(ce));
@@ -790,12 +841,36 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk) {
             return FE_CUDA_ERR;
         }
         kk.k = cb.k, kk.G = G, kk.chunk = chunk, kk.x = s.p, kk.theta = cb.theta, kk.delta = cb.delta;
+        kk.prof = prof;
     }
     const int per_iter = 3 + (cb.k - 1);
+    bool launched = false;
+    int it_prev = 0;
     for (;;) {
         FE_CHECK(read_scalars(h));
+        // the chunk's first iteration ran in full when a second one followed it
+        if (prof && launched && w.sc_host->iter - it_prev >= 2) {
+            float a = 0.f;
+            if (cudaEventElapsedTime(&a, w.pev[0], w.pev[1]) == cudaSuccess)
+                w.prof_ms[slot][1] += a, w.prof_n[slot][1] += 1;
+            if (cb.k >= 4 && cudaEventElapsedTime(&a, w.pev[2], w.pev[3]) == cudaSuccess)
+                w.prof_ms[slot][0] += a, w.prof_n[slot][0] += 1;
+        }
         if (w.sc_host->done) break;
+        if (watch) {
+            const double rr = w.sc_host->rr;
+            const int it = w.sc_host->iter;
+            if (rr < 0.81 * watch->best) {
+                watch->best = rr;
+                watch->best_iter = it;
+            } else if (it - watch->best_iter > watch->window) {
+                watch->stalled = true;
+                break;
+            }
+        }
+        it_prev = w.sc_host->iter;
         FE_CUDA(cudaGraphLaunch(w.graph[slot], h->stream));
+        launched = true;
         h->launches += (int64_t)chunk * per_iter;
     }
     return FE_OK;
@@ -855,15 +930,12 @@ int ensure_work(fe_handle_s *h, bool mixed) {
         FE_CHECK(dalloc(w.z, n));
         FE_CHECK(dalloc(w.p, n));
         FE_CHECK(dalloc(w.q, n));
-        FE_CHECK(dalloc(w.dch, n));
     } else {
         FE_CHECK(dalloc(w.r32, n));
-        FE_CHECK(dalloc(w.d32, n));
         FE_CHECK(dalloc(w.z32, n));
         FE_CHECK(dalloc(w.p32, n));
         FE_CHECK(dalloc(w.q32, n));
         FE_CHECK(dalloc(w.zc32, n));
-        FE_CHECK(dalloc(w.c32, n));
     }
     FE_CHECK(dalloc(w.partials, (size_t)4 * 152 * 8 + 64));
     if (!w.sc.p) {
@@ -948,6 +1020,52 @@ int estimate_lmax(fe_handle_s *h, const Sys<T> &s, double bb, int chunk, double 
     return FE_OK;
 }
 
+// FP64 PCG from the solution already in x (its true residual is in s.r) until the
+// FP64 true residual meets tol.  When the recurrence reaches tol but the true
+// residual does not (the recurrence drifts from b - A x by about eps * cond(A)), the
+// Krylov space restarts from the true residual and runs until its recurrence has
+// halved it; a restart that gains less than 2x marks the rounding floor, final with
+// accept_stagnation.  Adds to *total and st->spmv.
+template <int D, int G>
+int fp64_iterate(fe_handle_s *h, const Sys<double> &s, const Cheb &cb, int chunk, double bb, double tol,
+                 int max_iter, int max_restart, bool accept_stagnation, int *total, int *restarts, double *relres, int *status,
+                 fe_solve_stats *st) {
+    SolverWork &w = h->w;
+    PcgScalars *sc = w.sc.p;
+    double prev = 1e300, target = tol;
+    *restarts = 0;
+    for (;;) {
+        FE_CHECK(set_params(h, target * target, max_iter - *total, bb, cb.theta));
+        FE_CHECK((enqueue_start<D, double, G, false>(h, s, cb, sc, w.partials.p)));
+        FE_CHECK((run_loop<D, double, G>(h, s, cb, chunk)));
+        const int it = w.sc_host->iter, stv = w.sc_host->status;
+        *total += it;
+        st->spmv += it * cb.k + (cb.k - 1);
+        // true residual, which also seeds a restart
+        FE_CHECK((residual<D, G, double>(h, s.x, s.r, &sc->rr)));
+        st->spmv += 1;
+        FE_CHECK(read_scalars(h));
+        *relres = sqrt(w.sc_host->rr / bb);
+        *status = stv;
+        if (*relres <= tol) {
+            *status = FE_OK;
+            return FE_OK;
+        }
+        if (stv == FE_NONFINITE || stv == FE_BREAKDOWN) return FE_OK;
+        if (*total >= max_iter) {
+            *status = FE_MAXITER;
+            return FE_OK;
+        }
+        if (*relres > 0.5 * prev || *restarts >= max_restart) {
+            *status = accept_stagnation ? FE_OK : FE_MAXITER;
+            return FE_OK;
+        }
+        prev = *relres;
+        target = std::min(tol, 0.5 * *relres);
+        ++*restarts;
+    }
+}
+
 template <int D, int G>
 int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     SolverWork &w = h->w;
@@ -956,7 +1074,7 @@ int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     const int max_iter = o->max_iter > 0 ? o->max_iter : 200000;
     const int max_restart = o->max_outer > 0 ? o->max_outer : 8;
     const double tol = o->tol > 0 ? o->tol : 1e-10;
-    const bool accept_stagnation = (o->flags & 1) != 0;
+    const bool accept_stagnation = (o->flags & FE_SOLVE_ACCEPT_STAGNATION) != 0;
     PcgScalars *sc = w.sc.p;
     FE_CHECK((residual<D, G, double>(h, nullptr, w.t.p, &sc->bb)));
     FE_CHECK(read_scalars(h));
@@ -975,42 +1093,12 @@ int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     }
     FE_CHECK(init_solution(h, o, s.x));
     const bool nonzero = o->x0 || h->n_bc > 0;
-    int total = 0, restarts = 0, status = FE_OK;
-    double relres = 0, prev = 1e300;
     FE_CHECK((residual<D, G, double>(h, nonzero ? s.x : nullptr, s.r, &sc->rr)));
     st->spmv += nonzero ? 1 : 0;
-    for (;;) {
-        FE_CHECK(set_params(h, tol * tol, max_iter - total, bb, cb.theta));
-        FE_CHECK((enqueue_start<D, double, G, false>(h, s, cb, sc, w.partials.p)));
-        FE_CHECK((run_loop<D, double, G>(h, s, cb, chunk)));
-        const int it = w.sc_host->iter, stv = w.sc_host->status;
-        total += it;
-        st->spmv += it * cb.k + (cb.k - 1);
-        // true residual, which also seeds a restart
-        FE_CHECK((residual<D, G, double>(h, s.x, s.r, &sc->rr)));
-        st->spmv += 1;
-        FE_CHECK(read_scalars(h));
-        relres = sqrt(w.sc_host->rr / bb);
-        status = stv;
-        if (relres <= tol) {
-            status = FE_OK;
-            break;
-        }
-        if (stv == FE_NONFINITE || stv == FE_BREAKDOWN) break;
-        if (total >= max_iter) {
-            status = FE_MAXITER;
-            break;
-        }
-        // the recurrence reached the tolerance but the true residual did not: rounding
-        // floor of the FP64 iteration.  Restart from the true residual while that
-        // still gains; with accept_stagnation a floor that no restart lowers is final.
-        if (relres > 0.5 * prev || restarts >= max_restart) {
-            status = accept_stagnation ? FE_OK : FE_MAXITER;
-            break;
-        }
-        prev = relres;
-        ++restarts;
-    }
+    int total = 0, restarts = 0, status = FE_OK;
+    double relres = 0;
+    FE_CHECK((fp64_iterate<D, G>(h, s, cb, chunk, bb, tol, max_iter, max_restart, accept_stagnation, &total, &restarts,
+                                 &relres, &status, st)));
     st->iterations = total;
     st->outer = restarts;
     st->relres = relres;
@@ -1023,6 +1111,15 @@ int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
 // residual has fallen by `delta` since the last refinement step, the FP64 true
 // residual b - A x replaces it (refinement step) and the iteration continues with the
 // same search direction.  The solve ends when the FP64 true residual meets tol.
+//
+// FP32 arithmetic has a floor: on strongly heterogeneous problems the FP32 operator
+// cannot resolve the smooth, low-stiffness modes that remain near tol, and the FP32
+// iteration stalls above it however often the residual is refreshed.  An FP32 run
+// whose residual has not improved by 10% for max(2000, iterations so far)
+// iterations (50000 for the first run of a Krylov space), or a refinement step that
+// gains less than 2x, counts as stalled: the
+// solve then continues with FP64 PCG from the FP64 solution reached so far, so the
+// tolerance is met in any case.
 template <int D, int G>
 int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     SolverWork &w = h->w;
@@ -1058,7 +1155,7 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     st->spmv += nonzero ? 1 : 0;
     int total = 0, outer = 0, status = FE_OK;
     double relres = sqrt(rr_true / bb);
-    bool first = true;
+    bool first = true, stalled = false;
     const bool restart_each = (o->flags & FE_SOLVE_RESTART_EACH_STEP) != 0;
     const char *verbose_env = getenv("FE_VERBOSE");
     const bool verbose = verbose_env && verbose_env[0] == '1';
@@ -1074,8 +1171,12 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
             FE_CHECK((enqueue_start<D, float, G, false>(h, s, cb, sc, w.partials.p)));
         else
             FE_CHECK((enqueue_start<D, float, G, true>(h, s, cb, sc, w.partials.p)));
+        // the 2-norm residual of a fresh Krylov space may rise for a long while
+        // before it falls; continued runs fall steadily
+        StallWatch watch;
+        watch.window = first ? 50000 : std::max(2000, total);
         first = restart_each;
-        FE_CHECK((run_loop<D, float, G>(h, s, cb, chunk)));
+        FE_CHECK((run_loop<D, float, G>(h, s, cb, chunk, &watch)));
         const int it = w.sc_host->iter, stv = w.sc_host->status;
         const double rr_rec = w.sc_host->rr;
         total += it;
@@ -1100,6 +1201,14 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
             status = stv;
             break;
         }
+        if (total >= max_iter) {
+            status = FE_MAXITER;
+            break;
+        }
+        if (watch.stalled || rr_new > 0.25 * rr_true) {
+            stalled = true;
+            break;
+        }
         if (stv == FE_BREAKDOWN) {
             // lost positive definiteness in FP32: restart the Krylov space from the
             // true residual; give up if that makes no progress either
@@ -1110,6 +1219,24 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
             first = true;
         }
         rr_true = rr_new;
+    }
+    st->fp64_iterations = 0;
+    if (stalled) {
+        // FP64 finish from the FP64 solution; the FP32 Chebyshev bounds describe the
+        // same operator
+        FE_CHECK(ensure_work(h, false));
+        Sys<double> s64 = make_sys<D, double>(h);
+        FE_CHECK((residual<D, G, double>(h, x64, s64.r, &sc->rr)));
+        st->spmv += 1;
+        const int before = total;
+        int restarts = 0;
+        FE_CHECK((fp64_iterate<D, G>(h, s64, cb, chunk, bb, tol, max_iter, 8,
+                                     (o->flags & FE_SOLVE_ACCEPT_STAGNATION) != 0, &total, &restarts, &relres,
+                                     &status, st)));
+        st->fp64_iterations = total - before;
+        if (verbose)
+            fprintf(stderr, "fe mixed: FP32 stalled, FP64 finish %d it -> true %.3e (status %d)\n", total - before,
+                    relres, status);
     }
     if (relres <= tol) status = FE_OK;
     st->iterations = total;
@@ -1215,12 +1342,25 @@ int spmv64(fe_handle_s *h, const double *x, double *y) {
     return FE_OK;
 }
 
+int profile_kernels(fe_handle_s *h, int enable) {
+    SolverWork &w = h->w;
+    if (enable && !w.pev[0])
+        for (int i = 0; i < 4; ++i) FE_CUDA(cudaEventCreate(&w.pev[i]));
+    w.prof = enable != 0;
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) w.prof_ms[a][b] = 0.0, w.prof_n[a][b] = 0;
+    return FE_OK;
+}
+
 void release_solver(fe_handle_s *h) {
     SolverWork &w = h->w;
+    for (int i = 0; i < 4; ++i)
+        if (w.pev[i]) cudaEventDestroy(w.pev[i]), w.pev[i] = nullptr;
+    w.prof = false;
     for (int i = 0; i < 2; ++i)
         if (w.graph[i]) cudaGraphExecDestroy(w.graph[i]), w.graph[i] = nullptr;
-    dfree(w.x), dfree(w.r), dfree(w.z), dfree(w.p), dfree(w.q), dfree(w.t), dfree(w.dch);
-    dfree(w.r32), dfree(w.z32), dfree(w.p32), dfree(w.q32), dfree(w.d32), dfree(w.zc32), dfree(w.c32);
+    dfree(w.x), dfree(w.r), dfree(w.z), dfree(w.p), dfree(w.q), dfree(w.t);
+    dfree(w.r32), dfree(w.z32), dfree(w.p32), dfree(w.q32), dfree(w.zc32);
     dfree(w.partials), dfree(w.sc);
     if (w.sc_host) cudaFreeHost(w.sc_host), w.sc_host = nullptr;
 }

@@ -62,7 +62,9 @@ extern "C" {
 
 /* solver precision */
 #define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
-#define FE_PREC_MIXED  1   /* FP32 SpMV/preconditioner inside FP64 iterative refinement    */
+#define FE_PREC_MIXED  1   /* FP32 SpMV/preconditioner inside FP64 iterative refinement;
+                              an FP32 iteration that stalls above tol (FP32 floor of a
+                              strongly heterogeneous problem) is finished by FP64 PCG    */
 
 typedef struct fe_handle_s *fe_handle;
 
@@ -90,6 +92,9 @@ typedef struct fe_solve_stats {
     double  bnorm;         /* ||b||_2 of the eliminated system                            */
     double  solve_ms;      /* device time of the solve, CUDA events on the handle stream  */
     double  assemble_ms;   /* device time of the last fe_assemble                         */
+    int32_t fp64_iterations; /* mixed: iterations of the FP64 finish (0 when FP32 met tol);
+                                included in iterations                                   */
+    int32_t reserved;
 } fe_solve_stats;
 
 int         fe_version(void);
@@ -172,6 +177,15 @@ int fe_launch_count(fe_handle h, int64_t *count);
 int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double *ms_out);
 /* Average device time of one SpMV with the given lanes (reps repetitions). */
 int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out);
+/* Kernel timing inside the solver's captured PCG loop (no counterpart in the
+ * reference; for measurement).  enable = 1 adds CUDA event records around the first
+ * iteration of every 16-iteration chunk and resets the sums; 0 removes them.
+ * fe_profile_read returns, for the given precision, the summed device time (ms) and
+ * the number of timed launches of an intermediate Chebyshev step (degree >= 4) and of
+ * the PCG SpMV. */
+int fe_profile_kernels(fe_handle h, int32_t enable);
+int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *cheb_n, double *spmv_ms,
+                    int64_t *spmv_n);
 
 /* ---- post-processing of a solution (results.py:809-830 strain/stress, :769-781 and
  * elements.py:275-292 energy, results.py:121-152 magnetic field).  u_host / a_host:

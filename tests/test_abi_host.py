@@ -40,6 +40,33 @@ def test_library_exports_every_declared_symbol():
     assert set(declared_functions()) == set(_lib.exported_symbols())
 
 
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of fe_solve_opts and fe_solve_stats have the header's size
+    and field offsets (a C probe compiled against include/fe_gb300.h)."""
+    import ctypes
+    import shutil
+    from finite_elements_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = []
+    for tag, cls in (("fe_solve_opts", _lib.SolveOpts), ("fe_solve_stats", _lib.SolveStats)):
+        lines.append(f'printf("{tag} size %zu\\n", sizeof({tag}));')
+        for name, _ in cls._fields_:
+            lines.append(f'printf("{tag} {name} %zu\\n", offsetof({tag}, {name}));')
+    src = tmp_path / "probe.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"fe_gb300.h\"\nint main(void) {\n"
+                   + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for tag, cls in (("fe_solve_opts", _lib.SolveOpts), ("fe_solve_stats", _lib.SolveStats)):
+        assert int(got[f"{tag} size"]) == ctypes.sizeof(cls), tag
+        for name, _ in cls._fields_:
+            assert int(got[f"{tag} {name}"]) == getattr(cls, name).offset, (tag, name)
+
+
 def test_library_calls_without_gpu_fail_loudly():
     """No CPU fallback: on a machine without a CUDA device the first call fails with
     a CUDA status."""

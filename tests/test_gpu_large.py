@@ -4,7 +4,8 @@ problem checked on the host from the exported matrices (the oracle's NATURAL sps
 does not fit in memory at that size).
 
 Tolerances: magnetostatic solution ||a - a_ref|| <= 1e-8 ||a_ref|| (FP64 PCG to its
-rounding floor); K symmetric to 1e-13 of max|K|; interior row sums (K times a rigid
+rounding floor) and <= 1e-9 (block-Jacobi) / 3e-9 (mixed, whose residual left near tol sits in the
+lowest modes) ||a_ref|| for the 1e-10 solves; K symmetric to 1e-13 of max|K|; interior row sums (K times a rigid
 translation) <= 1e-12 of the row's max; total mass 1e-12; augmented residual
 ||F - K_aug x|| <= 1e-7 ||F|| for the 1e-8 mixed-precision solve; FP64 solves
 bitwise identical run to run."""
@@ -30,9 +31,17 @@ def test_magnetostatic_1m_triangles(gpu_lib):
     # multipliers: reactions at the 3,000 boundary nodes
     assert len(s.bc_dof) == 3000
     assert np.linalg.norm(x[n:] - ref[n:]) <= 1e-7 * np.linalg.norm(ref[n:])
+    # block-Jacobi PCG to 1e-10, the configuration's own tolerance
+    xj, stj = s.solve(precision="fp64", tol=1e-10, cheb_degree=0)
+    assert stj.status == 0 and stj.relres <= 1e-10
+    assert np.linalg.norm(xj[:n] - ref[:n]) <= 1e-9 * np.linalg.norm(ref[:n])
+    # mixed precision: the FP32 iteration stalls near 2e-10 on this mu_r = 1000
+    # problem (FP32 floor of the iron's low-stiffness modes); the FP64 finish
+    # still meets the tolerance
     xm, stm = s.solve(precision="mixed", tol=1e-10, cheb_degree=4, cheb_ratio=200)
-    assert stm.status == 0 and stm.relres <= 1e-10
-    assert np.linalg.norm(xm[:n] - ref[:n]) <= 1e-7 * np.linalg.norm(ref[:n])
+    assert stm.status == 0 and stm.relres <= 1e-10, stm.as_dict()
+    assert 0 < stm.fp64_iterations < stm.iterations
+    assert np.linalg.norm(xm[:n] - ref[:n]) <= 3e-9 * np.linalg.norm(ref[:n])
     s.close()
 
 
@@ -76,6 +85,7 @@ def test_4m_mixed_solution_meets_the_residual_on_the_host(big):
     prob, s = big
     x, st = s.solve(precision="mixed", tol=1e-8, cheb_degree=8, cheb_ratio=1000)
     assert st.status == 0 and st.relres <= 1e-8
+    assert st.fp64_iterations == 0                 # FP32 alone reaches 1e-8 here
     K = s.create_matrix()                          # augmented saddle matrix, scipy CSR
     F = s.create_source_matrix()[:, 0]
     r = F - K @ x

@@ -1,6 +1,13 @@
 """Per-element post-processing on the GPU against the oracle (results.py:121-152,
 :769-830): strain, stress, energy of elasticity solutions and the magnetic field of
-magnetostatic ones.  Tolerance: max |difference| <= 1e-12 * max |oracle|."""
+magnetostatic ones.
+
+Tolerance: each value agrees with the oracle within 64 eps times the sum of the
+absolute values of the terms that make it (strain: |B| |q|, stress: |D| |B| |q|,
+energy: 0.5 |q|^T |Ke| |q|, field: |b|, |c| times |A|).  That is the rounding bound
+of a short dot product evaluated in another order; a plain relative bound would
+fail on element energies, which are quadratic forms of near-rigid motions and so
+cancel to far below their terms."""
 import numpy as np
 import pytest
 
@@ -8,9 +15,11 @@ import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
 
+EPS = np.finfo(np.float64).eps
 
-def relmax(a, b):
-    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+def within(gpu, ref, scale, c=64.0):
+    return bool(np.all(np.abs(gpu - ref) <= c * EPS * scale))
 
 
 @pytest.mark.parametrize("name", [n for n in gc.names()])
@@ -23,12 +32,23 @@ def test_post_matches_oracle(gpu_lib, name):
     res = s.post(x)
     if prob.kind == "elastic":
         strain, stress, energy = O.elastic_post(prob, x)
-        assert relmax(res["strain"], strain) <= 1e-12
-        assert relmax(res["stress"], stress) <= 1e-12
-        assert relmax(res["energy"], energy) <= 1e-12
+        q = np.abs(x[: prob.n_dof].reshape(-1, 2)[prob.conn].reshape(-1, 6))
+        B = np.abs(O.b_matrix(O.element_points(prob)))
+        D = np.abs(O.d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress))
+        ke = np.abs(O.elastic_stiffness(prob).reshape(-1, 6, 6))
+        assert within(res["strain"], strain, np.einsum("eij,ej->ei", B, q))
+        assert within(res["stress"], stress, np.einsum("eij,ej->ei", np.matmul(D, B), q))
+        assert within(res["energy"], energy, 0.5 * np.einsum("ei,eij,ej->e", q, ke, q))
     else:
-        assert relmax(res["field"], O.magnetic_field(prob, x)) <= 1e-12
+        ff = np.abs(O.form_functions(O.element_points(prob)))
+        A = np.abs(x[: prob.n_nodes][prob.conn])
+        scale = np.stack([(ff[:, :, 2] * A).sum(axis=1), (ff[:, :, 1] * A).sum(axis=1)], axis=1)
+        assert within(res["field"], O.magnetic_field(prob, x), scale)
     s.close()
+
+
+def relmax(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
 def test_results_classes(gpu_lib):
