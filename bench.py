@@ -47,10 +47,13 @@ def parse_args():
     ap.add_argument("--ny", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cheb", type=int, default=12, help="Chebyshev degree of the mixed solve's preconditioner")
-    ap.add_argument("--cheb-ratio", type=float, default=3000.0, help="Chebyshev interval lmax/lmin (mixed)")
-    ap.add_argument("--plain-cheb", type=int, default=16, help="Chebyshev degree of the plain FP64 PCG")
-    ap.add_argument("--plain-cheb-ratio", type=float, default=3000.0, help="Chebyshev interval (plain FP64)")
+    ap.add_argument("--cheb", type=int, default=32, help="Chebyshev degree of the mixed solve's preconditioner")
+    ap.add_argument("--cheb-ratio", type=float, default=10000.0, help="Chebyshev interval lmax/lmin (mixed)")
+    ap.add_argument("--plain-cheb", type=int, default=24, help="Chebyshev degree of the plain FP64 PCG")
+    ap.add_argument("--plain-cheb-ratio", type=float, default=10000.0, help="Chebyshev interval (plain FP64)")
+    ap.add_argument("--ir-cheb", type=int, default=16,
+                    help="Chebyshev degree of the FP32-Krylov + iterative-refinement solve reported beside")
+    ap.add_argument("--ir-cheb-ratio", type=float, default=3000.0)
     ap.add_argument("--no-learned", action="store_true", help="headline without the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="headline steps only (no plain / oracle / e2e legs), for profiler runs")
@@ -196,8 +199,12 @@ def run_ours(args, dist):
     s = GpuSystem(prob, assemble=True)           # inputs uploaded: resident in HBM from here
     h = s.handle
     step_flags = _lib.FE_ASSEMBLE_PATTERN | _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
-    mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
+    # headline: FP64 CG recurrence with the FP32 Chebyshev preconditioner; beside it the
+    # FP32-Krylov + iterative-refinement form and the plain FP64 PCG
+    mode = dict(precision="mixed-cg64", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
                 want_host=False)
+    ir_mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.ir_cheb, cheb_ratio=args.ir_cheb_ratio,
+                   want_host=False)
     plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.plain_cheb, cheb_ratio=args.plain_cheb_ratio,
                  want_host=False)
     net = None
@@ -262,7 +269,7 @@ def run_ours(args, dist):
     h.call("fe_synchronize")
     clk = clocks.stop()
     n_launch = launches() - l0
-    prof_mixed = profile_read(_lib.FE_PREC_MIXED)
+    prof_mixed = profile_read(_lib.FE_PREC_MIXED_CG64)
     ms = ctypes.c_double()
     h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
     dist.barrier()
@@ -283,6 +290,16 @@ def run_ours(args, dist):
     h.call("fe_synchronize")
     h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
     mixed_only_s = ms.value / 1e3 / max(args.plain_steps, 1)
+
+    # ---- FP32 Krylov vectors and SpMV with FP64 iterative refinement, same step
+    device_step(ir_mode)
+    h.call("fe_synchronize")
+    h.call("fe_event_record", 2)
+    istats = [device_step(ir_mode) for _ in range(max(args.plain_steps, 1))]
+    h.call("fe_event_record", 3)
+    h.call("fe_synchronize")
+    h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
+    ir_s = ms.value / 1e3 / max(args.plain_steps, 1)
 
     # ---- plain FP64 PCG, same step
     device_step(plain)
@@ -305,16 +322,18 @@ def run_ours(args, dist):
 
     # ---- roofline.  Algorithmic bytes per launch (2x2 node blocks, s = value size):
     # off-diagonal blocks (4 s + 4 column bytes each) + per node: Chebyshev step --
-    # diagonal slot 4s, block-Jacobi inverse 4s, z_k, r, z_{k-1} read and z_{k+1}
-    # written (2s each); PCG SpMV -- diagonal 4s, p read and q written (2s each);
-    # + 4 bytes of slice offset per 32 rows.
+    # diagonal slot 4s, the block-Jacobi inverse 4s (FP64 only: the FP32 copy is
+    # prescaled by it), z_k, r (D^-1 r in FP32), z_{k-1} read and z_{k+1} written (2s
+    # each); PCG SpMV -- diagonal 4s, p read and q written (2s each); + 4 bytes of
+    # slice offset per 32 rows.
     info = s.info()
     nnzb, n_nodes = info["n_blocks"], prob.n_nodes
     nb_off = nnzb - n_nodes
     slices = (n_nodes + 31) // 32 + 1
 
     def cheb_bytes(sz):
-        return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + 4 * sz + 4 * 2 * sz) + slices * 4
+        dinv = 4 * sz if sz == 8 else 0
+        return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + dinv + 4 * 2 * sz) + slices * 4
 
     def spmv_bytes(sz):
         return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + 2 * 2 * sz) + slices * 4
@@ -324,7 +343,7 @@ def run_ours(args, dist):
         return gbs, (gbs / hbm_peak if gbs else None)
 
     cheb_gbs, cheb_frac = roof(cheb_bytes(4), prof_mixed["cheb_us"])
-    spmv32_gbs, spmv32_frac = roof(spmv_bytes(4), prof_mixed["spmv_us"])
+    spmvmp_gbs, spmvmp_frac = roof(spmv_bytes(8), prof_mixed["spmv_us"])
     cheb64_gbs, cheb64_frac = roof(cheb_bytes(8), prof_plain["cheb_us"])
     spmv64_gbs, spmv64_frac = roof(spmv_bytes(8), prof_plain["spmv_us"])
     traffic = NCU_TRAFFIC.get((args.nx, args.ny))
@@ -334,8 +353,7 @@ def run_ours(args, dist):
     h2d = (prob.coords.nbytes + prob.conn.nbytes + prob.E.nbytes + prob.nu.nbytes + prob.thickness.nbytes
            + prob.rho.nbytes + prob.node_load_node.size * 24 + prob.node_bc_node.size * 16)
     e2e_times = []
-    e2e_opts = dict(precision="mixed", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
-                    want_host=True)
+    e2e_opts = dict(mode, want_host=True)
     for k in range(args.steps + 1):
         dist.barrier()
         t0 = time.perf_counter()
@@ -355,28 +373,32 @@ def run_ours(args, dist):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov/SpMV + f64 x, residual, reductions",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 CG recurrence (x, r, p, q, one SpMV per iteration) + f32 Chebyshev preconditioner",
         "data": f"synthetic, seeded (seed {args.seed})",
         "config": {
             "workload": f"plane strain {args.nx}x{args.ny} grid, {2 * args.nx * args.ny:,} triangles, "
                         f"{prob.n_dof:,} DOF, E=10^U(9,12) per element, nu~U(0.2,0.45), left edge clamped, "
                         f"random top-edge traction",
-            "mode": "mixed precision (FP32 diff-form SELL SpMV, node-block Jacobi + Chebyshev, FP64 refinement "
-                    "with reliable updates)" + (" + learned warm start" if net is not None else ""),
+            "mode": "mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
+                    "preconditioner in FP32 on the prescaled FP32 copy" + (" + learned warm start" if net is not None else ""),
             "learned_warm_start": net is not None,
-            "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio]},
+            "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio],
+                          "fp32_krylov_ir": [args.ir_cheb, args.ir_cheb_ratio]},
             "tol": args.tol, "step": "pattern + element kernels + reduction + loads + elimination + PCG",
             "l2": "inputs larger than L2 (BSR values alone 448 MB FP64 / 224 MB FP32)",
             "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
         },
-        "iterations": stats[-1].iterations, "refinement_steps": stats[-1].outer,
+        "iterations": stats[-1].iterations, "restarts": stats[-1].outer,
         "relres": stats[-1].relres, "err_vs_fp64": err,
         "plain_fp64": {"s_per_solve": plain_s, "iterations": pstats[-1].iterations if pstats else None,
                        "relres": pstats[-1].relres if pstats else None},
         "speedup_vs_plain": plain_s / value if value > 0 else None,
         "mixed_without_learned": {"s_per_solve": mixed_only_s, "iterations": nstats[-1].iterations},
-        "roofline": {"bound": "hbm", "kernel": "k_cheb_step<2,float,2> (intermediate Chebyshev step of the mixed "
-                                                "PCG: 6 of the 12 kernels of an iteration at degree 8)",
+        "fp32_krylov_ir": {"s_per_solve": ir_s, "iterations": istats[-1].iterations,
+                           "refinement_steps": istats[-1].outer},
+        "roofline": {"bound": "hbm", "kernel": "k_cheb_step<2,float,double,2,0> (intermediate FP32 Chebyshev step: "
+                                                f"{max(args.cheb - 2, 0)} of the {args.cheb + 2} kernels of an iteration)",
                      "achieved": cheb_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": cheb_frac,
                      "peak_source": peak_src, "traffic": traffic,
                      "bytes_per_launch": cheb_bytes(4), "launch_us": prof_mixed["cheb_us"],
@@ -384,15 +406,16 @@ def run_ours(args, dist):
                      "timing": "CUDA events captured in the PCG graph around the first iteration of each "
                                "16-iteration chunk, during the timed solves"},
         "kernels": {
-            "mixed_pcg_spmv": {"kernel": "k_pcg_spmv<2,float>", "launch_us": prof_mixed["spmv_us"],
-                               "bytes_per_launch": spmv_bytes(4), "achieved_gbs": spmv32_gbs,
-                               "frac": spmv32_frac, "launches_timed": prof_mixed["spmv_n"]},
+            "mixed_pcg_spmv": {"kernel": "k_pcg_spmv<2,double> (the recurrence's FP64 SpMV)",
+                               "launch_us": prof_mixed["spmv_us"], "bytes_per_launch": spmv_bytes(8),
+                               "achieved_gbs": spmvmp_gbs, "frac": spmvmp_frac,
+                               "launches_timed": prof_mixed["spmv_n"]},
             "plain_pcg_spmv": {"kernel": "k_pcg_spmv<2,double>", "launch_us": prof_plain["spmv_us"],
                                "bytes_per_launch": spmv_bytes(8), "achieved_gbs": spmv64_gbs,
                                "frac": spmv64_frac, "launches_timed": prof_plain["spmv_n"],
                                "fp64_tflops": (8 * nnzb / (prof_plain["spmv_us"] * 1e-6) / 1e12
                                                if prof_plain["spmv_us"] > 0 else None)},
-            "plain_cheb_step": {"kernel": "k_cheb_step<2,double,2>", "launch_us": prof_plain["cheb_us"],
+            "plain_cheb_step": {"kernel": "k_cheb_step<2,double,double,2,0>", "launch_us": prof_plain["cheb_us"],
                                 "bytes_per_launch": cheb_bytes(8), "achieved_gbs": cheb64_gbs,
                                 "frac": cheb64_frac, "launches_timed": prof_plain["cheb_n"]},
         },

@@ -19,7 +19,7 @@ FE_KIND_ELASTIC_TRI, FE_KIND_MAGNETIC_TRI = 1, 2
 FE_PLANE_STRESS, FE_PLANE_STRAIN = 1, 2
 FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F, FE_ASSEMBLE_PATTERN = 1, 2, 4, 8
 FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
-FE_PREC_FP64, FE_PREC_MIXED = 0, 1
+FE_PREC_FP64, FE_PREC_MIXED, FE_PREC_MIXED_CG64 = 0, 1, 2
 FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP = 1, 2
 
 STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",

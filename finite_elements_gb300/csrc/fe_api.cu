@@ -120,7 +120,7 @@ int fe_destroy(fe_handle h) {
     dfree(h->cand), dfree(h->counts), dfree(h->scan_tmp);
     dfree(h->ke), dfree(h->me_scale), dfree(h->kval), dfree(h->mval), dfree(h->aval), dfree(h->aval32);
     dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->sell_off), dfree(h->sell_col);
-    dfree(h->sell_val64), dfree(h->sell_val32), dfree(h->diag64), dfree(h->diag32), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
+    dfree(h->sell_val64), dfree(h->sell_val32), dfree(h->diag64), dfree(h->diag32), dfree(h->dblk32), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
     dfree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
     for (auto &e : h->events)
@@ -431,11 +431,11 @@ int fe_profile_kernels(fe_handle h, int32_t enable) {
 int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *cheb_n, double *spmv_ms,
                     int64_t *spmv_n) {
     FE_HANDLE_CHECK(h);
-    if (precision != FE_PREC_FP64 && precision != FE_PREC_MIXED) {
+    if (precision != FE_PREC_FP64 && precision != FE_PREC_MIXED && precision != FE_PREC_MIXED_CG64) {
         set_error("fe_profile_read: unknown precision");
         return FE_BAD_INPUT;
     }
-    const int slot = precision == FE_PREC_MIXED ? 1 : 0;
+    const int slot = precision;   // graph slots follow the precision codes
     if (cheb_ms) *cheb_ms = h->w.prof_ms[slot][0];
     if (cheb_n) *cheb_n = h->w.prof_n[slot][0];
     if (spmv_ms) *spmv_ms = h->w.prof_ms[slot][1];

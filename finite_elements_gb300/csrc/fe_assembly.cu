@@ -634,12 +634,33 @@ __global__ void k_sell_widths(int64_t n_nodes, int64_t n_slices, const int32_t *
     }
 }
 
+// D^-1 B for one block row (r's inverse diagonal block times block B), in FP64.
+template <int D>
+__device__ __forceinline__ void scale_block(const double *__restrict__ dinv_r, const double *__restrict__ b,
+                                            double *out) {
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) acc = fma(dinv_r[i * D + k], b[k * D + j], acc);
+            out[i * D + j] = acc;
+        }
+}
+
+// SELL-32 fill.  FP64 copy: the eliminated blocks A_rm and the diagonal A_rr.  FP32
+// copy, prescaled by the node-block Jacobi inverse for the Chebyshev steps: blocks
+// D_r^-1 A_rm and, in the diagonal slot, D_r^-1 S_r (S_r the block row sum of the
+// difference form); dblk32 keeps A_rr in FP32 so that a product with the FP32 copy
+// can be scaled back to A x.
 template <int D>
 __global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__restrict__ blk_ptr,
                             const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
-                            const double *__restrict__ srow, const int32_t *__restrict__ off,
-                            int32_t *__restrict__ col, double *__restrict__ v64, float *__restrict__ v32,
-                            double *__restrict__ d64, float *__restrict__ d32) {
+                            const double *__restrict__ srow, const double *__restrict__ dinv,
+                            const int32_t *__restrict__ off, int32_t *__restrict__ col, double *__restrict__ v64,
+                            float *__restrict__ v32, double *__restrict__ d64, float *__restrict__ d32,
+                            float *__restrict__ dblk32) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_slices * 32;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int64_t sl = r >> 5, lane = r & 31;
@@ -647,22 +668,28 @@ __global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__
         const int w = (off[sl + 1] - off[sl]) >> 5;
         int k = 0;
         if (r < n_nodes) {
+            const double *dr = dinv + r * D * D;
+            double sc[D * D];
+            scale_block<D>(dr, srow + r * D * D, sc);
+#pragma unroll
+            for (int q = 0; q < D * D; ++q) d32[r * D * D + q] = (float)sc[q];
             for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
                 const int c = blk_col[s];
                 if (c == (int)r) {
 #pragma unroll
                     for (int q = 0; q < D * D; ++q) {
                         d64[r * D * D + q] = aval[(int64_t)s * D * D + q];
-                        d32[r * D * D + q] = (float)srow[r * D * D + q];
+                        dblk32[r * D * D + q] = (float)aval[(int64_t)s * D * D + q];
                     }
                     continue;
                 }
                 const int64_t e = base + 32 * (int64_t)k + lane;
                 col[e] = c;
+                scale_block<D>(dr, aval + (int64_t)s * D * D, sc);
 #pragma unroll
                 for (int q = 0; q < D * D; ++q) {
                     v64[e * D * D + q] = aval[(int64_t)s * D * D + q];
-                    v32[e * D * D + q] = (float)aval[(int64_t)s * D * D + q];
+                    v32[e * D * D + q] = (float)sc[q];
                 }
                 ++k;
             }
@@ -991,19 +1018,23 @@ int build_sell(fe_handle_s *h) {
     FE_CHECK(dalloc(h->sell_val32, ne * D * D));
     FE_CHECK(dalloc(h->diag64, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
     FE_CHECK(dalloc(h->diag32, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
+    FE_CHECK(dalloc(h->dblk32, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
     // a node without elements has no diagonal block to copy: leave zeros there
     FE_CUDA(cudaMemsetAsync(h->diag64.p, 0, h->n_nodes * D * D * sizeof(double), s));
     FE_CUDA(cudaMemsetAsync(h->diag32.p, 0, h->n_nodes * D * D * sizeof(float), s));
+    FE_CUDA(cudaMemsetAsync(h->dblk32.p, 0, h->n_nodes * D * D * sizeof(float), s));
     if (n_slices > 0) {
         int g = grid_for(n_slices * 32, kThreads, 152 * 64);
         if (D == 2)
             k_sell_fill<2><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
-                                                  h->srow.p, h->sell_off.p, h->sell_col.p, h->sell_val64.p,
-                                                  h->sell_val32.p, h->diag64.p, h->diag32.p);
+                                                  h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
+                                                  h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
+                                                  h->dblk32.p);
         else
             k_sell_fill<1><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
-                                                  h->srow.p, h->sell_off.p, h->sell_col.p, h->sell_val64.p,
-                                                  h->sell_val32.p, h->diag64.p, h->diag32.p);
+                                                  h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
+                                                  h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
+                                                  h->dblk32.p);
         FE_LAUNCH_CHECK();
     }
     h->launches += (n_slices > 0 ? 2 : 0) + 3;

@@ -102,28 +102,30 @@ struct SolverWork {
     // FP64 vectors (n_dof each): solution, residual, preconditioned residual,
     // direction, A p, a second z for the Chebyshev ping-pong (also scratch)
     DBuf<double> x, r, z, p, q, t;
-    // FP32 vectors of the mixed inner solve (the solution stays in x, FP64)
-    DBuf<float> r32, z32, p32, q32, zc32;
+    // FP32 vectors of the mixed inner solve (the solution stays in x, FP64); rh32 is
+    // D^-1 r, the right-hand side of the prescaled FP32 Chebyshev steps
+    DBuf<float> r32, z32, p32, q32, zc32, rh32;
     DBuf<double> partials;   // per-block partial sums of the reductions
     DBuf<PcgScalars> sc;
     PcgScalars *sc_host = nullptr;       // pinned mirror
     double lmax[2] = {0.0, 0.0};         // largest eigenvalue of D^-1 A, [FP64, FP32]
     int lanes[2] = {0, 0};               // autotuned SpMV lanes, [FP64, FP32]
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // captured chunk, [FP64, FP32]
+    // captured chunk, [FP64, FP32, FP64 recurrence + FP32 preconditioner]
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
     // what each captured graph was built for
     struct Key {
         int k = -1, G = -1, chunk = -1;
         const void *x = nullptr;
         double theta = 0, delta = 0;
         bool prof = false;
-    } key[2];
+    } key[3];
     // Kernel timing inside the captured loop (fe_profile_kernels): event records
     // around the first iteration of every chunk, [slot][0] an intermediate Chebyshev
-    // step, [slot][1] the PCG SpMV; summed durations and launches counted.
+    // step, [slot][1] the PCG SpMV (slots as graph[]); summed durations and launches.
     bool prof = false;
     cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
-    double prof_ms[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
-    int64_t prof_n[2][2] = {{0, 0}, {0, 0}};
+    double prof_ms[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+    int64_t prof_n[3][2] = {{0, 0}, {0, 0}, {0, 0}};
 };
 
 }  // namespace fe
@@ -183,11 +185,12 @@ struct fe_handle_s {
     // sliced ELL (SELL-32) copy of A for the PCG SpMVs: slice s holds 32 consecutive
     // block rows; entry k of row 32 s + l sits at sell_off[s] + 32 k + l (coalesced
     // per warp).  Off-diagonal blocks only; padding entries point at the row itself
-    // with a zero block.  The diagonal lives in diag64 (A_rr) / diag32 (S_r).
+    // with a zero block.  The diagonal lives in diag64 (A_rr) / diag32 (D^-1 S_r).
     int64_t n_slices = 0;
     fe::DBuf<int32_t> sell_off, sell_col;
     fe::DBuf<double> sell_val64, diag64;
-    fe::DBuf<float> sell_val32, diag32;
+    fe::DBuf<float> sell_val32, diag32;   // prescaled by the block-Jacobi inverse (D^-1 A_rm, D^-1 S_r)
+    fe::DBuf<float> dblk32;               // [n_nodes][d][d] A_rr in FP32 (scales D^-1 A x back to A x)
     fe::DBuf<double> F;                   // loads [n_dof]
     fe::DBuf<double> b;                   // eliminated right-hand side [n_dof]
     fe::DBuf<long long> load_seq;         // [n_dof] winning load sequence

@@ -303,12 +303,15 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
 // y = A x (timing)
 template <int D, typename T>
 __global__ void __launch_bounds__(kVecThreads)
-k_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ x,
-       T *__restrict__ y) {
+k_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ dscale,
+       const T *__restrict__ x, T *__restrict__ y) {
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
         NodeVec<D, T> v = sell_row<D, T>(row, valid, A, val, diag, x);
-        if (valid) st<D, T>(y, row, v);
+        if (valid) {
+            if (dscale) v = apply_dinv<D, T>(dscale, row, v);   // prescaled copy: A x = A_rr (D^-1 A x)
+            st<D, T>(y, row, v);
+        }
     }
 }
 
@@ -349,14 +352,16 @@ k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__re
 // q = A p and p.q; the last block sets alpha = r.z / p.q or stops the loop.
 template <int D, typename T>
 __global__ void __launch_bounds__(kVecThreads)
-k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ p,
-           T *__restrict__ q, double *partials, PcgScalars *sc) {
+k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
+           const T *__restrict__ dscale, const T *__restrict__ p, T *__restrict__ q, double *partials,
+           PcgScalars *sc) {
     if (sc->done) return;
     T lt = T(0);
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
         NodeVec<D, T> y = sell_row<D, T>(row, valid, A, val, diag, p);
         if (valid) {
+            if (dscale) y = apply_dinv<D, T>(dscale, row, y);   // prescaled copy: A p = A_rr (D^-1 A p)
             st<D, T>(q, row, y);
             NodeVec<D, T> pv = ld<D, T>(p, row);
 #pragma unroll
@@ -411,12 +416,13 @@ __device__ __forceinline__ void finish_iteration(PcgScalars *sc, double rz_new) 
 }
 
 // x += alpha p (x in FP64); r -= alpha q; then z = M^-1 r (Jacobi) or, with CHEB,
-// the first Chebyshev term z_1 = M^-1 r / theta.  Reduces r.z and r.r.
+// the first Chebyshev term z_1 = M^-1 r / theta, and M^-1 r into rh when the
+// Chebyshev steps run on the prescaled copy (rh non-null).  Reduces r.z and r.r.
 template <int D, typename T, bool CHEB>
 __global__ void __launch_bounds__(kVecThreads)
 k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
-             const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z, double *partials,
-             PcgScalars *sc) {
+             const T *__restrict__ q, const T *__restrict__ dinv, T *__restrict__ z, T *__restrict__ rh,
+             double *partials, PcgScalars *sc) {
     if (sc->done) return;
     const double alpha = sc->alpha;
     const T alpha_t = (T)alpha;
@@ -435,6 +441,7 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
         st<D, T>(r, i, rv);
         NodeVec<D, T> zv = apply_dinv<D, T>(dinv, i, rv);
         if (CHEB) {
+            if (rh) st<D, T>(rh, i, zv);
 #pragma unroll
             for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
         }
@@ -465,21 +472,25 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
 }
 
 // One Chebyshev step on D^-1 A z = D^-1 r in three-term form:
-//   z_{k+1} = z_k + c1 (z_k - z_{k-1}) + c2 M^-1 (r - A z_k),
+//   z_{k+1} = z_k + c1 (z_k - z_{k-1}) + c2 D^-1 (r - A z_k),
 // with z_0 = 0 (FIRST: step k = 1).  z_{k+1} is written over z_{k-1} in zprev_out:
 // every thread reads and writes only its own rows there, while the gathers of the
-// product read z_k.
+// product read z_k.  FP64 (unscaled copy): rres = r, D^-1 applied with dinv.  FP32
+// (prescaled copy, val = D^-1 A_rm, diag = D^-1 S_r): rres = D^-1 r and no dinv.
 // MODE 0: at the start of a loop (no reduction, runs even when done is set);
-// MODE 1: last step of an iteration (reduces r.z_{k+1}, finishes the iteration);
+// MODE 1: last step of an iteration (reduces rdot.z_{k+1} in FP64, finishes the
+//         iteration; rdot is the recurrence's residual);
 // MODE 2: intermediate step.
-template <int D, typename T, int MODE, bool FIRST>
+template <int D, typename T, typename RD, int MODE, bool FIRST>
 __global__ void __launch_bounds__(kVecThreads)
 k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
             const T *__restrict__ dinv, const T *__restrict__ rres, const T *__restrict__ z_in,
-            T *__restrict__ zprev_out, double c1, double c2, double *partials, PcgScalars *sc) {
+            T *__restrict__ zprev_out, double c1, double c2, double *partials, PcgScalars *sc,
+            const RD *__restrict__ rdot) {
+    constexpr bool PRE = sizeof(T) == 4;
     if (MODE != 0 && sc->done) return;
     const T c1t = (T)c1, c2t = (T)c2;
-    T lrz = T(0);
+    double lrz = 0.0;
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
         NodeVec<D, T> az = sell_row<D, T>(row, valid, A, val, diag, z_in);
@@ -491,20 +502,22 @@ k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restr
             } else {
                 zp = ld<D, T>(zprev_out, row);
             }
-            NodeVec<D, T> res;
+            NodeVec<D, T> mr;
 #pragma unroll
-            for (int a = 0; a < D; ++a) res.v[a] = rv.v[a] - az.v[a];
-            NodeVec<D, T> mr = apply_dinv<D, T>(dinv, row, res);
+            for (int a = 0; a < D; ++a) mr.v[a] = rv.v[a] - az.v[a];
+            if (!PRE) mr = apply_dinv<D, T>(dinv, row, mr);
 #pragma unroll
-            for (int a = 0; a < D; ++a) {
-                zv.v[a] += c1t * (zv.v[a] - zp.v[a]) + c2t * mr.v[a];
-                lrz += rv.v[a] * zv.v[a];
-            }
+            for (int a = 0; a < D; ++a) zv.v[a] += c1t * (zv.v[a] - zp.v[a]) + c2t * mr.v[a];
             st<D, T>(zprev_out, row, zv);
+            if (MODE == 1) {
+                const NodeVec<D, RD> rd = ld<D, RD>(rdot, row);
+#pragma unroll
+                for (int a = 0; a < D; ++a) lrz += (double)rd.v[a] * (double)zv.v[a];
+            }
         }
     }
     if (MODE == 1) {
-        double loc[1] = {(double)lrz}, tot[1];
+        double loc[1] = {lrz}, tot[1];
         if (grid_reduce<1>(loc, partials, &sc->ticket[2], tot) && threadIdx.x == 0) finish_iteration(sc, tot[0]);
     }
 }
@@ -525,15 +538,16 @@ k_pcg_direction(int64_t n_nodes, const T *__restrict__ z, T *__restrict__ p, Pcg
 }
 
 // Start of a loop, given r: z = M^-1 r (times 1/theta with CHEB: the first
-// Chebyshev term z_1).
+// Chebyshev term z_1), and M^-1 r into rh for prescaled Chebyshev steps.
 template <int D, typename T, bool CHEB>
 __global__ void __launch_bounds__(kVecThreads)
 k_start_precond(int64_t n_nodes, const T *__restrict__ r, const T *__restrict__ dinv, T *__restrict__ z,
-                double theta) {
+                T *__restrict__ rh, double theta) {
     const T inv_theta = CHEB ? (T)(1.0 / theta) : T(1);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
          i += (int64_t)gridDim.x * blockDim.x) {
         NodeVec<D, T> zv = apply_dinv<D, T>(dinv, i, ld<D, T>(r, i));
+        if (CHEB && rh) st<D, T>(rh, i, zv);
         if (CHEB) {
 #pragma unroll
             for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
@@ -602,6 +616,142 @@ k_continue_direction(int64_t n_nodes, const T *__restrict__ z, T *__restrict__ p
     }
 }
 
+// ---- FP64 CG recurrence around an FP32 Chebyshev preconditioner (FE_PREC_MIXED_CG64):
+// x, r, p, q in FP64 and q = A p on the FP64 copy; z and the Chebyshev iterates in
+// FP32, fed with an FP32 copy of r.
+
+// x += alpha p; r -= alpha q (FP64); rh = M^-1 (float) r; z = rh (/ theta with CHEB).
+// Reduces r.z and r.r in FP64.
+template <int D, bool CHEB>
+__global__ void __launch_bounds__(kVecThreads)
+k_mp_update(int64_t n_nodes, double *__restrict__ x, double *__restrict__ r, const double *__restrict__ p,
+            const double *__restrict__ q, const float *__restrict__ dinv, float *__restrict__ rh,
+            float *__restrict__ z, double *partials, PcgScalars *sc) {
+    if (sc->done) return;
+    const double alpha = sc->alpha;
+    const float inv_theta = CHEB ? (float)(1.0 / sc->cheb_theta) : 1.0f;
+    double lrz = 0.0, lrr = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        NodeVec<D, double> xv = ld<D, double>(x, i), rv = ld<D, double>(r, i);
+        const NodeVec<D, double> pv = ld<D, double>(p, i), qv = ld<D, double>(q, i);
+        NodeVec<D, float> rf;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            xv.v[a] = fma(alpha, pv.v[a], xv.v[a]);
+            rv.v[a] = fma(-alpha, qv.v[a], rv.v[a]);
+            rf.v[a] = (float)rv.v[a];
+        }
+        st<D, double>(x, i, xv);
+        st<D, double>(r, i, rv);
+        NodeVec<D, float> zv = apply_dinv<D, float>(dinv, i, rf);
+        if (CHEB) st<D, float>(rh, i, zv);
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            if (CHEB) zv.v[a] *= inv_theta;
+            lrz += rv.v[a] * (double)zv.v[a];
+            lrr += rv.v[a] * rv.v[a];
+        }
+        st<D, float>(z, i, zv);
+    }
+    double loc[2] = {lrz, lrr}, tot[2];
+    if (grid_reduce<2>(loc, partials, &sc->ticket[1], tot) && threadIdx.x == 0) {
+        sc->rr = tot[1];
+        if (CHEB) {
+            if (!isfinite(tot[1])) {
+                sc->status = FE_NONFINITE;
+                sc->done = 1;
+            } else if (tot[1] <= sc->tol2 * sc->bb) {
+                sc->iter += 1;
+                sc->status = FE_OK;
+                sc->done = 1;
+            }
+        } else {
+            finish_iteration(sc, tot[0]);
+        }
+    }
+}
+
+// p = z + beta p with z in FP32, p in FP64.
+template <int D>
+__global__ void __launch_bounds__(kVecThreads)
+k_mp_direction(int64_t n_nodes, const float *__restrict__ z, double *__restrict__ p, PcgScalars *sc) {
+    if (sc->done) return;
+    const double beta = sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const NodeVec<D, float> zv = ld<D, float>(z, i);
+        NodeVec<D, double> pv = ld<D, double>(p, i);
+#pragma unroll
+        for (int a = 0; a < D; ++a) pv.v[a] = fma(beta, pv.v[a], (double)zv.v[a]);
+        st<D, double>(p, i, pv);
+    }
+}
+
+// Start of a loop from the FP64 residual r: rh = M^-1 (float) r, z = rh (/ theta).
+template <int D, bool CHEB>
+__global__ void __launch_bounds__(kVecThreads)
+k_mp_start_precond(int64_t n_nodes, const double *__restrict__ r, const float *__restrict__ dinv,
+                   float *__restrict__ rh, float *__restrict__ z, double theta) {
+    const float inv_theta = CHEB ? (float)(1.0 / theta) : 1.0f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const NodeVec<D, double> rv = ld<D, double>(r, i);
+        NodeVec<D, float> rf;
+#pragma unroll
+        for (int a = 0; a < D; ++a) rf.v[a] = (float)rv.v[a];
+        NodeVec<D, float> zv = apply_dinv<D, float>(dinv, i, rf);
+        if (CHEB) st<D, float>(rh, i, zv);
+        if (CHEB) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
+        }
+        st<D, float>(z, i, zv);
+    }
+}
+
+// After z: p = (double) z, r.z and r.r in FP64, loop scalars reset (a fresh start).
+template <int D>
+__global__ void __launch_bounds__(kVecThreads)
+k_mp_start_finish(int64_t n_nodes, const double *__restrict__ r, const float *__restrict__ z,
+                  double *__restrict__ p, double *partials, PcgScalars *sc) {
+    double lrz = 0.0, lrr = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const NodeVec<D, double> rv = ld<D, double>(r, i);
+        const NodeVec<D, float> zv = ld<D, float>(z, i);
+        NodeVec<D, double> pv;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            pv.v[a] = (double)zv.v[a];
+            lrz += rv.v[a] * pv.v[a];
+            lrr += rv.v[a] * rv.v[a];
+        }
+        st<D, double>(p, i, pv);
+    }
+    double loc[2] = {lrz, lrr}, tot[2];
+    if (grid_reduce<2>(loc, partials, &sc->ticket[3], tot) && threadIdx.x == 0) {
+        sc->rz = tot[0];
+        sc->rr = tot[1];
+        sc->beta = 0.0;
+        sc->iter = 0;
+        sc->status = FE_OK;
+        sc->done = 0;
+        if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+            sc->status = FE_NONFINITE;
+            sc->done = 1;
+        } else if (tot[1] <= sc->tol2 * sc->bb) {
+            sc->done = 1;
+        } else if (!(tot[0] > 0.0)) {
+            sc->status = FE_BREAKDOWN;
+            sc->done = 1;
+        } else if (sc->max_iter <= 0) {
+            sc->status = FE_MAXITER;
+            sc->done = 1;
+        }
+    }
+}
+
 // x[dof_k] = g_k on every constrained DOF.  The eliminated rows are identity rows
 // decoupled from the free ones, so with this start their residual is exactly zero
 // and node-block Jacobi keeps them exact for the whole solve.
@@ -640,19 +790,21 @@ struct Sys {
     Sell A;                                   // SELL-32 structure
     const T *sval = nullptr, *diag = nullptr;  // SELL values and diagonal blocks
     const T *val = nullptr, *dinv = nullptr;
+    const T *dblk = nullptr;  // FP32: A_rr, scales a product with the prescaled copy back to A x
     double *x = nullptr;   // the solution, FP64 in both precisions
     T *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *zc = nullptr;
+    T *rh = nullptr;       // right-hand side of the Chebyshev steps: r (FP64) or D^-1 r (FP32)
 };
 
 struct Cheb {
     int k = 1;                 // Chebyshev terms (1 = plain node-block Jacobi)
     double theta = 1, delta = 1;
-    double c1[16], c2[16];     // coefficients of steps 1..k-1
+    double c1[32], c2[32];     // coefficients of steps 1..k-1
 };
 
 Cheb make_cheb(int degree, double lmax, double ratio) {
     Cheb c;
-    c.k = std::max(1, std::min(degree, 16));
+    c.k = std::max(1, std::min(degree, 32));
     if (c.k <= 1 || !(lmax > 0)) {
         c.k = 1;
         return c;
@@ -680,41 +832,44 @@ Sys<T> make_sys(fe_handle_s *h) {
         s.sval = h->sell_val64.p, s.diag = h->diag64.p;
         s.val = h->aval.p, s.dinv = h->dinv.p;
         s.r = w.r.p, s.p = w.p.p, s.q = w.q.p, s.z = w.z.p, s.zc = w.t.p;
+        s.rh = s.r;
     } else {
         s.sval = h->sell_val32.p, s.diag = h->diag32.p;
-        s.val = h->aval32.p, s.dinv = h->dinv32.p;
+        s.val = h->aval32.p, s.dinv = h->dinv32.p, s.dblk = h->dblk32.p;
         s.r = w.r32.p, s.p = w.p32.p, s.q = w.q32.p, s.z = w.z32.p, s.zc = w.zc32.p;
+        s.rh = w.rh32.p;
     }
     return s;
 }
 
-template <int D, typename T, int MODE>
+template <int D, typename T, typename RD, int MODE>
 void launch_cheb_step(fe_handle_s *h, const Sys<T> &s, bool first, const T *zin, T *zout, double c1, double c2,
-                      double *part, PcgScalars *sc, int grid) {
+                      double *part, PcgScalars *sc, int grid, const RD *rdot) {
     if (first)
-        k_cheb_step<D, T, MODE, true><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv,
-                                                                           s.r, zin, zout, c1, c2, part, sc);
+        k_cheb_step<D, T, RD, MODE, true><<<grid, kVecThreads, 0, h->stream>>>(
+            h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
     else
-        k_cheb_step<D, T, MODE, false><<<grid, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dinv,
-                                                                            s.r, zin, zout, c1, c2, part, sc);
+        k_cheb_step<D, T, RD, MODE, false><<<grid, kVecThreads, 0, h->stream>>>(
+            h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
 }
 
 // Chebyshev steps 1..k-1 after z_1 is in s.z; z ping-pongs between s.z and s.zc
 // (each step overwrites z_{k-1} with z_{k+1}); *z_final is the buffer holding z_k.
-template <int D, typename T>
+// rdot: the residual the last step dots with z (the recurrence's r).
+template <int D, typename T, typename RD>
 void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part, int grid,
-                        bool start, T **z_final, cudaEvent_t *ev = nullptr) {
+                        bool start, T **z_final, cudaEvent_t *ev, const RD *rdot) {
     T *zin = s.z, *zout = s.zc;
     for (int k = 1; k < cb.k; ++k) {
         const bool last = (k == cb.k - 1), first = (k == 1);
         const bool timed = ev && k == 2 && !last;      // an intermediate step (MODE 2)
         if (timed) cudaEventRecordWithFlags(ev[2], h->stream, cudaEventRecordExternal);
         if (start)
-            launch_cheb_step<D, T, 0>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid);
+            launch_cheb_step<D, T, RD, 0>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid, rdot);
         else if (last)
-            launch_cheb_step<D, T, 1>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid);
+            launch_cheb_step<D, T, RD, 1>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid, rdot);
         else
-            launch_cheb_step<D, T, 2>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid);
+            launch_cheb_step<D, T, RD, 2>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid, rdot);
         if (timed) cudaEventRecordWithFlags(ev[3], h->stream, cudaEventRecordExternal);
         std::swap(zin, zout);
     }
@@ -729,16 +884,18 @@ void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScala
     const int gv = vec_grid(h->n_nodes);
     const int gs = sell_grid(h);
     if (ev) cudaEventRecordWithFlags(ev[0], h->stream, cudaEventRecordExternal);
-    k_pcg_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.p, s.q, part, sc);
+    k_pcg_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dblk, s.p, s.q, part,
+                                                         sc);
     if (ev) cudaEventRecordWithFlags(ev[1], h->stream, cudaEventRecordExternal);
     T *zf = s.z;
+    T *rh = s.rh != s.r ? s.rh : nullptr;
     if (cb.k > 1) {
         k_pcg_update<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z,
-                                                                    part, sc);
-        enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, false, &zf, ev);
+                                                                    rh, part, sc);
+        enqueue_cheb_steps<D, T, T>(h, s, cb, sc, part, gs, false, &zf, ev, s.r);
     } else {
         k_pcg_update<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.x, s.r, s.p, s.q, s.dinv, s.z,
-                                                                     part, sc);
+                                                                     rh, part, sc);
     }
     k_pcg_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
 }
@@ -750,16 +907,66 @@ int enqueue_start(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *s
     const int gv = vec_grid(h->n_nodes);
     const int gs = sell_grid(h);
     T *zf = s.z;
+    T *rh = s.rh != s.r ? s.rh : nullptr;
     if (cb.k > 1) {
-        k_start_precond<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, cb.theta);
-        enqueue_cheb_steps<D, T>(h, s, cb, sc, part, gs, true, &zf);
+        k_start_precond<D, T, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, rh, cb.theta);
+        enqueue_cheb_steps<D, T, T>(h, s, cb, sc, part, gs, true, &zf, nullptr, s.r);
     } else {
-        k_start_precond<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, 1.0);
+        k_start_precond<D, T, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, s.dinv, s.z, rh, 1.0);
     }
     k_start_finish<D, T, CONT><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.r, zf, s.p, part, sc);
     if (CONT) k_continue_direction<D, T><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.p, sc);
     FE_LAUNCH_CHECK();
     h->launches += 2 + (cb.k - 1) + (CONT ? 1 : 0);
+    return FE_OK;
+}
+
+// FP64 CG recurrence around the FP32 preconditioner: d holds x, r, p, q and the FP64
+// SELL copy; f holds the prescaled FP32 SELL copy, dinv32, D^-1 r in FP32 (f.rh) and
+// the Chebyshev iterates (f.z, f.zc).
+struct SysMP {
+    Sys<double> d;
+    Sys<float> f;
+};
+
+template <int D>
+void enqueue_iteration_mp(fe_handle_s *h, const SysMP &s, const Cheb &cb, PcgScalars *sc, double *part,
+                          cudaEvent_t *ev = nullptr) {
+    const int gv = vec_grid(h->n_nodes);
+    const int gs = sell_grid(h);
+    if (ev) cudaEventRecordWithFlags(ev[0], h->stream, cudaEventRecordExternal);
+    k_pcg_spmv<D, double><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.d.A, s.d.sval, s.d.diag, nullptr,
+                                                               s.d.p, s.d.q, part, sc);
+    if (ev) cudaEventRecordWithFlags(ev[1], h->stream, cudaEventRecordExternal);
+    float *zf = s.f.z;
+    if (cb.k > 1) {
+        k_mp_update<D, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.d.x, s.d.r, s.d.p, s.d.q, s.f.dinv,
+                                                                 s.f.rh, s.f.z, part, sc);
+        enqueue_cheb_steps<D, float, double>(h, s.f, cb, sc, part, gs, false, &zf, ev, s.d.r);
+    } else {
+        k_mp_update<D, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.d.x, s.d.r, s.d.p, s.d.q, s.f.dinv,
+                                                                  s.f.rh, s.f.z, part, sc);
+    }
+    k_mp_direction<D><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, zf, s.d.p, sc);
+}
+
+// Fresh start from the FP64 residual in s.d.r: z = P r (FP32), p = z.
+template <int D>
+int enqueue_start_mp(fe_handle_s *h, const SysMP &s, const Cheb &cb, PcgScalars *sc, double *part) {
+    const int gv = vec_grid(h->n_nodes);
+    const int gs = sell_grid(h);
+    float *zf = s.f.z;
+    if (cb.k > 1) {
+        k_mp_start_precond<D, true><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.d.r, s.f.dinv, s.f.rh, s.f.z,
+                                                                        cb.theta);
+        enqueue_cheb_steps<D, float, double>(h, s.f, cb, sc, part, gs, true, &zf, nullptr, s.d.r);
+    } else {
+        k_mp_start_precond<D, false><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.d.r, s.f.dinv, s.f.rh, s.f.z,
+                                                                         1.0);
+    }
+    k_mp_start_finish<D><<<gv, kVecThreads, 0, h->stream>>>(h->n_nodes, s.d.r, zf, s.d.p, part, sc);
+    FE_LAUNCH_CHECK();
+    h->launches += 2 + (cb.k - 1);
     return FE_OK;
 }
 
@@ -798,8 +1005,6 @@ int read_scalars(fe_handle_s *h) {
     return FE_OK;
 }
 
-// Run PCG iterations until the device says done, replaying a captured chunk of
-// iterations (captured once per configuration and reused across solves).
 // Progress watch of a running loop: the host sees r.r after every chunk; a running
 // minimum that has not improved by 10% (in norm) for `window` iterations marks the
 // loop as stalled and ends it at that chunk boundary (x, r, p stay consistent).
@@ -810,14 +1015,16 @@ struct StallWatch {
     bool stalled = false;
 };
 
-template <int D, typename T, int G>
-int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk, StallWatch *watch = nullptr) {
+// Run PCG iterations until the device says done, replaying a captured chunk of
+// iterations (captured once per configuration and graph slot, reused across solves).
+// enq(ev) enqueues one iteration, with event records when ev is non-null.
+template <typename Enq>
+int run_chunks(fe_handle_s *h, int slot, const void *key_ptr, int G, const Cheb &cb, int chunk, Enq enq,
+               StallWatch *watch) {
     SolverWork &w = h->w;
-    PcgScalars *sc = w.sc.p;
-    const int slot = sizeof(T) == 8 ? 0 : 1;
     SolverWork::Key &kk = w.key[slot];
     const bool prof = w.prof && w.pev[0];
-    bool same = w.graph[slot] && kk.k == cb.k && kk.G == G && kk.chunk == chunk && kk.x == (const void *)s.p &&
+    bool same = w.graph[slot] && kk.k == cb.k && kk.G == G && kk.chunk == chunk && kk.x == key_ptr &&
                 kk.theta == cb.theta && kk.delta == cb.delta && kk.prof == prof;
     if (!same) {
         if (w.graph[slot]) {
@@ -826,8 +1033,7 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk, StallWa
         }
         cudaGraph_t g;
         FE_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < chunk; ++i)
-            enqueue_iteration<D, T>(h, s, cb, sc, w.partials.p, (prof && i == 0) ? w.pev : nullptr);
+        for (int i = 0; i < chunk; ++i) enq((prof && i == 0) ? w.pev : nullptr);
         cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
         if (ce != cudaSuccess) {
             set_error(std::string("graph capture: ") + cudaGetErrorString(ce));
@@ -840,7 +1046,7 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk, StallWa
             set_error(std::string("graph instantiate: ") + cudaGetErrorString(ce));
             return FE_CUDA_ERR;
         }
-        kk.k = cb.k, kk.G = G, kk.chunk = chunk, kk.x = s.p, kk.theta = cb.theta, kk.delta = cb.delta;
+        kk.k = cb.k, kk.G = G, kk.chunk = chunk, kk.x = key_ptr, kk.theta = cb.theta, kk.delta = cb.delta;
         kk.prof = prof;
     }
     const int per_iter = 3 + (cb.k - 1);
@@ -874,6 +1080,22 @@ int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk, StallWa
         h->launches += (int64_t)chunk * per_iter;
     }
     return FE_OK;
+}
+
+template <int D, typename T, int G>
+int run_loop(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, int chunk, StallWatch *watch = nullptr) {
+    SolverWork &w = h->w;
+    return run_chunks(
+        h, sizeof(T) == 8 ? 0 : 1, s.p, G, cb, chunk,
+        [&](cudaEvent_t *ev) { enqueue_iteration<D, T>(h, s, cb, w.sc.p, w.partials.p, ev); }, watch);
+}
+
+template <int D, int G>
+int run_loop_mp(fe_handle_s *h, const SysMP &s, const Cheb &cb, int chunk) {
+    SolverWork &w = h->w;
+    return run_chunks(
+        h, 2, s.d.p, G, cb, chunk,
+        [&](cudaEvent_t *ev) { enqueue_iteration_mp<D>(h, s, cb, w.sc.p, w.partials.p, ev); }, nullptr);
 }
 
 // Largest eigenvalue of the tridiagonal Lanczos matrix built from CG coefficients,
@@ -920,22 +1142,24 @@ int dispatch_lanes(int lanes, F &&f) {
     }
 }
 
-int ensure_work(fe_handle_s *h, bool mixed) {
+int ensure_work(fe_handle_s *h, bool need64, bool need32) {
     SolverWork &w = h->w;
     size_t n = (size_t)std::max<int64_t>(h->n_dof, 1);
     FE_CHECK(dalloc(w.x, n));
     FE_CHECK(dalloc(w.r, n));
     FE_CHECK(dalloc(w.t, n));
-    if (!mixed) {
+    if (need64) {
         FE_CHECK(dalloc(w.z, n));
         FE_CHECK(dalloc(w.p, n));
         FE_CHECK(dalloc(w.q, n));
-    } else {
+    }
+    if (need32) {
         FE_CHECK(dalloc(w.r32, n));
         FE_CHECK(dalloc(w.z32, n));
         FE_CHECK(dalloc(w.p32, n));
         FE_CHECK(dalloc(w.q32, n));
         FE_CHECK(dalloc(w.zc32, n));
+        FE_CHECK(dalloc(w.rh32, n));
     }
     FE_CHECK(dalloc(w.partials, (size_t)4 * 152 * 8 + 64));
     if (!w.sc.p) {
@@ -970,10 +1194,10 @@ int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
     FE_CUDA(cudaMemsetAsync(x, 0, h->n_dof * sizeof(T), h->stream));
     const int gs = sell_grid(h);
     for (int i = 0; i < 2; ++i)
-        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, x, y);
+        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dblk, x, y);
     FE_CUDA(cudaEventRecord(h->events[8], h->stream));
     for (int i = 0; i < reps; ++i)
-        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, x, y);
+        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dblk, x, y);
     FE_CUDA(cudaEventRecord(h->events[9], h->stream));
     FE_LAUNCH_CHECK();
     FE_CUDA(cudaEventSynchronize(h->events[9]));
@@ -985,7 +1209,7 @@ int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
 
 int time_spmv_any(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {
     bool f32 = precision == FE_PREC_MIXED;
-    FE_CHECK(ensure_work(h, f32));
+    FE_CHECK(ensure_work(h, !f32, f32));
     return dispatch_lanes(lanes, [&](auto g) {
         constexpr int G = decltype(g)::value;
         if (h->dim == 2) return f32 ? time_spmv_impl<2, float, G>(h, reps, ms) : time_spmv_impl<2, double, G>(h, reps, ms);
@@ -1020,29 +1244,30 @@ int estimate_lmax(fe_handle_s *h, const Sys<T> &s, double bb, int chunk, double 
     return FE_OK;
 }
 
-// FP64 PCG from the solution already in x (its true residual is in s.r) until the
-// FP64 true residual meets tol.  When the recurrence reaches tol but the true
-// residual does not (the recurrence drifts from b - A x by about eps * cond(A)), the
-// Krylov space restarts from the true residual and runs until its recurrence has
-// halved it; a restart that gains less than 2x marks the rounding floor, final with
+// PCG with FP64 true residuals from the solution already in x (its true residual
+// in r) until the FP64 true residual meets tol.  start() begins a Krylov space from
+// r, loop() runs it.  When the recurrence reaches tol but the true residual does not
+// (the recurrence drifts from b - A x by about eps * cond(A)), the Krylov space
+// restarts from the true residual and runs until its recurrence has halved it; a
+// restart that gains less than 2x marks the rounding floor, final with
 // accept_stagnation.  Adds to *total and st->spmv.
-template <int D, int G>
-int fp64_iterate(fe_handle_s *h, const Sys<double> &s, const Cheb &cb, int chunk, double bb, double tol,
-                 int max_iter, int max_restart, bool accept_stagnation, int *total, int *restarts, double *relres, int *status,
-                 fe_solve_stats *st) {
+template <int D, int G, typename Start, typename Loop>
+int pcg_restarted(fe_handle_s *h, double *x, double *r, const Cheb &cb, double bb, double tol, int max_iter,
+                  int max_restart, bool accept_stagnation, int *total, int *restarts, double *relres, int *status,
+                  fe_solve_stats *st, Start start, Loop loop) {
     SolverWork &w = h->w;
     PcgScalars *sc = w.sc.p;
     double prev = 1e300, target = tol;
     *restarts = 0;
     for (;;) {
         FE_CHECK(set_params(h, target * target, max_iter - *total, bb, cb.theta));
-        FE_CHECK((enqueue_start<D, double, G, false>(h, s, cb, sc, w.partials.p)));
-        FE_CHECK((run_loop<D, double, G>(h, s, cb, chunk)));
+        FE_CHECK(start());
+        FE_CHECK(loop());
         const int it = w.sc_host->iter, stv = w.sc_host->status;
         *total += it;
         st->spmv += it * cb.k + (cb.k - 1);
         // true residual, which also seeds a restart
-        FE_CHECK((residual<D, G, double>(h, s.x, s.r, &sc->rr)));
+        FE_CHECK((residual<D, G, double>(h, x, r, &sc->rr)));
         st->spmv += 1;
         FE_CHECK(read_scalars(h));
         *relres = sqrt(w.sc_host->rr / bb);
@@ -1064,6 +1289,17 @@ int fp64_iterate(fe_handle_s *h, const Sys<double> &s, const Cheb &cb, int chunk
         target = std::min(tol, 0.5 * *relres);
         ++*restarts;
     }
+}
+
+template <int D, int G>
+int fp64_iterate(fe_handle_s *h, const Sys<double> &s, const Cheb &cb, int chunk, double bb, double tol,
+                 int max_iter, int max_restart, bool accept_stagnation, int *total, int *restarts, double *relres,
+                 int *status, fe_solve_stats *st) {
+    SolverWork &w = h->w;
+    return pcg_restarted<D, G>(
+        h, s.x, s.r, cb, bb, tol, max_iter, max_restart, accept_stagnation, total, restarts, relres, status, st,
+        [&]() { return enqueue_start<D, double, G, false>(h, s, cb, w.sc.p, w.partials.p); },
+        [&]() { return run_loop<D, double, G>(h, s, cb, chunk); });
 }
 
 template <int D, int G>
@@ -1099,6 +1335,56 @@ int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     double relres = 0;
     FE_CHECK((fp64_iterate<D, G>(h, s, cb, chunk, bb, tol, max_iter, max_restart, accept_stagnation, &total, &restarts,
                                  &relres, &status, st)));
+    st->iterations = total;
+    st->outer = restarts;
+    st->relres = relres;
+    st->status = status;
+    return FE_OK;
+}
+
+// FP64 CG recurrence with an FP32 Chebyshev preconditioner: x, r, p, q and the
+// product q = A p are FP64 (one FP64 SpMV per iteration), the node-block Jacobi and
+// the k - 1 Chebyshev SpMVs of the preconditioner run on the FP32 copy of A.  The
+// preconditioner's rounding only makes it a slightly different SPD-like
+// preconditioner; the FP64 recurrence keeps CG's convergence, which an FP32 product
+// A p loses on ill-conditioned problems (its rounding in the smooth modes costs
+// ~40% more iterations at 4M DOF).  The FP64 true residual decides convergence as in
+// the plain solve.
+template <int D, int G>
+int solve_mp(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
+    SolverWork &w = h->w;
+    SysMP s{make_sys<D, double>(h), make_sys<D, float>(h)};
+    const int chunk = o->chunk > 0 ? o->chunk : 16;
+    const int max_iter = o->max_iter > 0 ? o->max_iter : 200000;
+    const int max_restart = o->max_outer > 0 ? o->max_outer : 8;
+    const double tol = o->tol > 0 ? o->tol : 1e-8;
+    const bool accept_stagnation = (o->flags & FE_SOLVE_ACCEPT_STAGNATION) != 0;
+    PcgScalars *sc = w.sc.p;
+    FE_CHECK((residual<D, G, double>(h, nullptr, w.t.p, &sc->bb)));
+    FE_CHECK(read_scalars(h));
+    const double bb = w.sc_host->bb;
+    st->bnorm = sqrt(bb);
+    Cheb cb;
+    if (o->cheb_degree >= 2) {
+        if (!(w.lmax[1] > 0)) FE_CHECK((estimate_lmax<D, float, G>(h, s.f, bb, chunk, &w.lmax[1])));
+        cb = make_cheb(o->cheb_degree, w.lmax[1], o->cheb_ratio > 0 ? o->cheb_ratio : 20.0);
+    }
+    if (bb == 0.0) {
+        FE_CUDA(cudaMemsetAsync(s.d.x, 0, h->n_dof * sizeof(double), h->stream));
+        st->relres = 0.0;
+        st->status = FE_OK;
+        return FE_OK;
+    }
+    FE_CHECK(init_solution(h, o, s.d.x));
+    const bool nonzero = o->x0 || h->n_bc > 0;
+    FE_CHECK((residual<D, G, double>(h, nonzero ? s.d.x : nullptr, s.d.r, &sc->rr)));
+    st->spmv += nonzero ? 1 : 0;
+    int total = 0, restarts = 0, status = FE_OK;
+    double relres = 0;
+    FE_CHECK((pcg_restarted<D, G>(
+        h, s.d.x, s.d.r, cb, bb, tol, max_iter, max_restart, accept_stagnation, &total, &restarts, &relres, &status, st,
+        [&]() { return enqueue_start_mp<D>(h, s, cb, w.sc.p, w.partials.p); },
+        [&]() { return run_loop_mp<D, G>(h, s, cb, chunk); })));
     st->iterations = total;
     st->outer = restarts;
     st->relres = relres;
@@ -1224,7 +1510,7 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     if (stalled) {
         // FP64 finish from the FP64 solution; the FP32 Chebyshev bounds describe the
         // same operator
-        FE_CHECK(ensure_work(h, false));
+        FE_CHECK(ensure_work(h, true, false));
         Sys<double> s64 = make_sys<D, double>(h);
         FE_CHECK((residual<D, G, double>(h, x64, s64.r, &sc->rr)));
         st->spmv += 1;
@@ -1255,12 +1541,12 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         set_error("fe_solve: the system is not assembled (call fe_assemble with K and F)");
         return FE_NOT_READY;
     }
-    const bool mixed = o->precision == FE_PREC_MIXED;
-    if (o->precision != FE_PREC_FP64 && !mixed) {
+    const bool mixed = o->precision == FE_PREC_MIXED, mp = o->precision == FE_PREC_MIXED_CG64;
+    if (o->precision != FE_PREC_FP64 && !mixed && !mp) {
         set_error("fe_solve: unknown precision");
         return FE_BAD_INPUT;
     }
-    FE_CHECK(ensure_work(h, mixed));
+    FE_CHECK(ensure_work(h, !mixed, mixed || mp));
     if (h->singular) {
         // a node without stiffness: the system is singular; like scipy's spsolve the
         // result is NaN
@@ -1278,8 +1564,9 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     FE_CUDA(cudaEventRecord(h->events[6], h->stream));
     int rc = dispatch_lanes(lanes, [&](auto g) {
         constexpr int G = decltype(g)::value;
-        if (h->dim == 2) return mixed ? solve_mixed<2, G>(h, o, st) : solve_fp64<2, G>(h, o, st);
-        return mixed ? solve_mixed<1, G>(h, o, st) : solve_fp64<1, G>(h, o, st);
+        if (h->dim == 2)
+            return mixed ? solve_mixed<2, G>(h, o, st) : mp ? solve_mp<2, G>(h, o, st) : solve_fp64<2, G>(h, o, st);
+        return mixed ? solve_mixed<1, G>(h, o, st) : mp ? solve_mp<1, G>(h, o, st) : solve_fp64<1, G>(h, o, st);
     });
     FE_CHECK(rc);
     FE_CHECK(recover_multipliers(h));
@@ -1334,9 +1621,11 @@ int spmv64(fe_handle_s *h, const double *x, double *y) {
     }
     Sell A{h->sell_off.p, h->sell_col.p, h->n_slices};
     if (h->dim == 2)
-        k_spmv<2, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p, x, y);
+        k_spmv<2, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
+                                                                        nullptr, x, y);
     else
-        k_spmv<1, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p, x, y);
+        k_spmv<1, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
+                                                                        nullptr, x, y);
     FE_LAUNCH_CHECK();
     h->launches += 1;
     return FE_OK;
@@ -1347,7 +1636,7 @@ int profile_kernels(fe_handle_s *h, int enable) {
     if (enable && !w.pev[0])
         for (int i = 0; i < 4; ++i) FE_CUDA(cudaEventCreate(&w.pev[i]));
     w.prof = enable != 0;
-    for (int a = 0; a < 2; ++a)
+    for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 2; ++b) w.prof_ms[a][b] = 0.0, w.prof_n[a][b] = 0;
     return FE_OK;
 }
@@ -1357,10 +1646,10 @@ void release_solver(fe_handle_s *h) {
     for (int i = 0; i < 4; ++i)
         if (w.pev[i]) cudaEventDestroy(w.pev[i]), w.pev[i] = nullptr;
     w.prof = false;
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < 3; ++i)
         if (w.graph[i]) cudaGraphExecDestroy(w.graph[i]), w.graph[i] = nullptr;
     dfree(w.x), dfree(w.r), dfree(w.z), dfree(w.p), dfree(w.q), dfree(w.t);
-    dfree(w.r32), dfree(w.z32), dfree(w.p32), dfree(w.q32), dfree(w.zc32);
+    dfree(w.r32), dfree(w.z32), dfree(w.p32), dfree(w.q32), dfree(w.zc32), dfree(w.rh32);
     dfree(w.partials), dfree(w.sc);
     if (w.sc_host) cudaFreeHost(w.sc_host), w.sc_host = nullptr;
 }

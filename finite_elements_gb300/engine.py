@@ -24,6 +24,11 @@ from ._lib import Handle, SolveOpts, SolveStats, ptr
 from .problem import ELASTIC, Problem
 
 
+# solve precisions: plain FP64 PCG; FP32 Krylov + FP64 iterative refinement; FP64 CG
+# recurrence with the FP32 Chebyshev preconditioner
+PRECISIONS = {"fp64": _lib.FE_PREC_FP64, "mixed": _lib.FE_PREC_MIXED, "mixed-cg64": _lib.FE_PREC_MIXED_CG64}
+
+
 def check_plane_flags(plane_strain, plane_stress):
     """The checks and messages of ElasticityElement.d_matrix (elements.py:265-273)."""
     if plane_strain and plane_stress:
@@ -184,14 +189,17 @@ class GpuSystem:
     def solve(self, precision="fp64", tol=None, cheb_degree=0, max_iter=0, x0=None, lanes=0,
               accept_stagnation=False, inner_tol=0.0, cheb_ratio=0.0, chunk=0, max_outer=0,
               want_host=True, restart_each_step=False, x0_device_ptr=None):
-        """Solve the eliminated system on the GPU.  Returns (x, stats): x holds
-        n_dof + n_bc values (u then the multipliers) or None with want_host=False."""
+        """Solve the eliminated system on the GPU.  precision: "fp64", "mixed" or
+        "mixed-cg64" (see PRECISIONS).  Returns (x, stats): x holds n_dof + n_bc
+        values (u then the multipliers) or None with want_host=False."""
         o = SolveOpts()
-        o.precision = _lib.FE_PREC_MIXED if precision == "mixed" else _lib.FE_PREC_FP64
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        o.precision = PRECISIONS[precision]
         o.cheb_degree = cheb_degree
         o.max_iter = max_iter
         o.max_outer = max_outer
-        o.tol = tol if tol is not None else (1e-8 if precision == "mixed" else 1e-12)
+        o.tol = tol if tol is not None else (1e-12 if precision == "fp64" else 1e-8)
         o.inner_tol = inner_tol
         o.cheb_ratio = cheb_ratio
         x0a = None

@@ -65,12 +65,16 @@ extern "C" {
 #define FE_PREC_MIXED  1   /* FP32 SpMV/preconditioner inside FP64 iterative refinement;
                               an FP32 iteration that stalls above tol (FP32 floor of a
                               strongly heterogeneous problem) is finished by FP64 PCG    */
+#define FE_PREC_MIXED_CG64 2 /* FP64 CG recurrence (x, r, p, q, q = A p on the FP64 copy)
+                              with the block-Jacobi/Chebyshev preconditioner in FP32 on
+                              the FP32 copy: all but one SpMV per iteration in FP32,
+                              FP64 convergence                                         */
 
 typedef struct fe_handle_s *fe_handle;
 
 typedef struct fe_solve_opts {
-    int32_t precision;     /* FE_PREC_FP64 or FE_PREC_MIXED                              */
-    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it    */
+    int32_t precision;     /* FE_PREC_FP64, FE_PREC_MIXED or FE_PREC_MIXED_CG64          */
+    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it (k <= 32) */
     int32_t max_iter;      /* cap on PCG iterations, all refinement steps together       */
     int32_t max_outer;     /* cap on refinement steps (mixed) or restarts (FP64)          */
     double  tol;           /* target ||b - A x||_2 / ||b||_2, FP64 true residual          */

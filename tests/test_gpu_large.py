@@ -42,6 +42,10 @@ def test_magnetostatic_1m_triangles(gpu_lib):
     assert stm.status == 0 and stm.relres <= 1e-10, stm.as_dict()
     assert 0 < stm.fp64_iterations < stm.iterations
     assert np.linalg.norm(xm[:n] - ref[:n]) <= 3e-9 * np.linalg.norm(ref[:n])
+    # FP64 recurrence with the FP32 preconditioner: no FP32 floor
+    xc, stc = s.solve(precision="mixed-cg64", tol=1e-10, cheb_degree=8, cheb_ratio=200)
+    assert stc.status == 0 and stc.relres <= 1e-10, stc.as_dict()
+    assert np.linalg.norm(xc[:n] - ref[:n]) <= 1e-9 * np.linalg.norm(ref[:n])
     s.close()
 
 
@@ -90,6 +94,15 @@ def test_4m_mixed_solution_meets_the_residual_on_the_host(big):
     F = s.create_source_matrix()[:, 0]
     r = F - K @ x
     assert np.linalg.norm(r) <= 1e-7 * np.linalg.norm(F)
+
+
+def test_4m_mixed_cg64_meets_the_residual_on_the_host(big):
+    prob, s = big
+    x, st = s.solve(precision="mixed-cg64", tol=1e-8, cheb_degree=24, cheb_ratio=3000)
+    assert st.status == 0 and st.relres <= 1e-8
+    K = s.create_matrix()
+    F = s.create_source_matrix()[:, 0]
+    assert np.linalg.norm(F - K @ x) <= 1e-7 * np.linalg.norm(F)
 
 
 def test_4m_fp64_is_deterministic(big):

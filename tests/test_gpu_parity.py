@@ -4,6 +4,7 @@ Tolerances (written here, as the bar for each quantity):
 * CSR pattern (indptr, indices, shape): bit-exact;
 * matrix values, F, element matrices: max |difference| <= 1e-13 * max |reference|;
 * solution [u, lambda] of the FP64 path: ||x - x_ref|| <= 1e-10 ||x_ref||;
+* FP64 CG with the FP32 preconditioner ("mixed-cg64") to its floor: as the FP64 path;
 * mixed-precision path: to 1e-9 relative residual ||u - u_ref|| <= 1e-7 ||u_ref||; to
   1e-8, ||u - u_ref|| <= 1e-6 ||u_ref||.  The error of any solve that stops at a
   relative residual r is bounded by cond(A) r, and on quirks_elastic an error just
@@ -111,6 +112,21 @@ def test_solve_mixed_matches_spsolve(systems, name, cheb):
         assert st.relres <= tol
         err = np.linalg.norm(x[:n] - ref["x"][:n]) / np.linalg.norm(ref["x"][:n])
         assert err <= bound, (tol, err, st.as_dict())
+
+
+@pytest.mark.parametrize("name", gc.names())
+@pytest.mark.parametrize("cheb", [0, 4, 24])
+def test_solve_mixed_cg64_matches_spsolve(systems, name, cheb):
+    """FP64 CG recurrence with the FP32 preconditioner: FP64 accuracy."""
+    s, prob, ref = systems[name]
+    x, st = s.solve(precision="mixed-cg64", tol=1e-12, accept_stagnation=True, cheb_degree=cheb)
+    assert st.status == 0, st.as_dict()
+    err = np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"])
+    assert err <= SOL_TOL, (err, st.as_dict())
+    x1, st1 = s.solve(precision="mixed-cg64", tol=1e-8, cheb_degree=cheb)
+    assert st1.status == 0 and st1.relres <= 1e-8
+    x2, _ = s.solve(precision="mixed-cg64", tol=1e-8, cheb_degree=cheb)
+    np.testing.assert_array_equal(x1, x2)
 
 
 @pytest.mark.parametrize("name", ["c1_cantilever", "c3_plane_strain_30x15", "c2_magnetostatic_40x20"])
