@@ -28,10 +28,10 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# DRAM bytes (read + write) per launch of the roofline kernel from one ncu capture of
-# this workload, keyed by grid (profiles/ holds the capture summary); None when the
-# workload differs from the captured one.
-NCU_TRAFFIC = {}
+# DRAM bytes (read + write) per launch of the roofline kernel (the intermediate FP32
+# Chebyshev step) from one ncu capture of this workload, keyed by grid (summary in
+# profiles/cheb_step_fp32_plane_strain_4M.md); None when the workload differs.
+NCU_TRAFFIC = {(2000, 1000): 334_353_408}
 
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
 UNIT = "s/solve"
