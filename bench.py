@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 # DRAM bytes (read + write) per launch of the roofline kernel (the intermediate FP32
 # Chebyshev step) from one ncu capture of this workload, keyed by grid (summary in
 # profiles/cheb_step_fp32_plane_strain_4M.md); None when the workload differs.
-NCU_TRAFFIC = {(2000, 1000): 334_353_408}
+NCU_TRAFFIC = {}
 
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
 UNIT = "s/solve"
@@ -321,22 +321,29 @@ def run_ours(args, dist):
     err = float(np.linalg.norm(x_mixed[:n] - x_ref[:n]) / np.linalg.norm(x_ref[:n]))
 
     # ---- roofline.  Algorithmic bytes per launch (2x2 node blocks, s = value size):
-    # off-diagonal blocks (4 s + 4 column bytes each) + per node: Chebyshev step --
-    # diagonal slot 4s, the block-Jacobi inverse 4s (FP64 only: the FP32 copy is
-    # prescaled by it), z_k, r (D^-1 r in FP32), z_{k-1} read and z_{k+1} written (2s
-    # each); PCG SpMV -- diagonal 4s, p read and q written (2s each); + 4 bytes of
-    # slice offset per 32 rows.
+    # off-diagonal blocks (4 s value bytes + 4 column bytes each, 2 for the FP32 kernels'
+    # 16-bit offsets) + per node: Chebyshev step --
+    # FP64: diagonal block 4s and block-Jacobi inverse 4s; FP32: neither (the copy is
+    # prescaled, in difference form; the ~0.1% of rows next to a Dirichlet condition
+    # carry one more entry, not counted) -- and z_k, r (D^-1 r in FP32), z_{k-1} read
+    # and z_{k+1} written (2s each); PCG SpMV -- diagonal 4s (FP32: A_rr to scale back),
+    # p read and q written (2s each); + 4 bytes of slice offset per 32 rows.
     info = s.info()
     nnzb, n_nodes = info["n_blocks"], prob.n_nodes
     nb_off = nnzb - n_nodes
     slices = (n_nodes + 31) // 32 + 1
 
+    col16 = s.sell_info()["col16"]
+
+    def col_bytes(sz):
+        return 2 if (sz == 4 and col16) else 4     # FP32 kernels read 16-bit column offsets
+
     def cheb_bytes(sz):
-        dinv = 4 * sz if sz == 8 else 0
-        return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + dinv + 4 * 2 * sz) + slices * 4
+        diag_and_dinv = 8 * sz if sz == 8 else 0
+        return nb_off * (4 * sz + col_bytes(sz)) + n_nodes * (diag_and_dinv + 4 * 2 * sz) + slices * 4
 
     def spmv_bytes(sz):
-        return nb_off * (4 * sz + 4) + n_nodes * (4 * sz + 2 * 2 * sz) + slices * 4
+        return nb_off * (4 * sz + col_bytes(sz)) + n_nodes * (4 * sz + 2 * 2 * sz) + slices * 4
 
     def roof(bytes_, us):
         gbs = bytes_ / (us * 1e-6) / 1e9 if us > 0 else None
@@ -403,8 +410,9 @@ def run_ours(args, dist):
                      "peak_source": peak_src, "traffic": traffic,
                      "bytes_per_launch": cheb_bytes(4), "launch_us": prof_mixed["cheb_us"],
                      "launches_timed": prof_mixed["cheb_n"],
-                     "timing": "CUDA events captured in the PCG graph around the first iteration of each "
-                               "16-iteration chunk, during the timed solves"},
+                     "timing": "CUDA events captured in the PCG graph around the run of intermediate "
+                               "Chebyshev steps of the first iteration of each 16-iteration chunk, during the "
+                               "timed solves; launch_us = that time / the launches it covers"},
         "kernels": {
             "mixed_pcg_spmv": {"kernel": "k_pcg_spmv<2,double> (the recurrence's FP64 SpMV)",
                                "launch_us": prof_mixed["spmv_us"], "bytes_per_launch": spmv_bytes(8),

@@ -83,6 +83,7 @@ _SIGNATURES = {
     "fe_launch_count": ([_P, _PI64], C.c_int),
     "fe_autotune_spmv": ([_P, _I32, _PI32, _PD], C.c_int),
     "fe_time_spmv": ([_P, _I32, _I32, _I32, _PD], C.c_int),
+    "fe_sell_info": ([_P, _PI64, _PI32], C.c_int),
     "fe_profile_kernels": ([_P, _I32], C.c_int),
     "fe_profile_read": ([_P, _I32, _PD, _PI64, _PD, _PI64], C.c_int),
     "fe_post_elastic": ([_P, _P, _P, _P, _P], C.c_int),

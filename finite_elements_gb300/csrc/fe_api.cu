@@ -119,7 +119,7 @@ int fe_destroy(fe_handle h) {
     dfree(h->inc_ptr), dfree(h->inc), dfree(h->blk_ptr), dfree(h->blk_col), dfree(h->blk_row);
     dfree(h->cand), dfree(h->counts), dfree(h->scan_tmp);
     dfree(h->ke), dfree(h->me_scale), dfree(h->kval), dfree(h->mval), dfree(h->aval), dfree(h->aval32);
-    dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->sell_off), dfree(h->sell_col);
+    dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->sell_off), dfree(h->sell_col), dfree(h->sell_dcol), dfree(h->sell_over);
     dfree(h->sell_val64), dfree(h->sell_val32), dfree(h->diag64), dfree(h->diag32), dfree(h->dblk32), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
     dfree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
@@ -421,6 +421,20 @@ int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double 
 int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out) {
     FE_HANDLE_CHECK(h);
     return time_spmv(h, precision, lanes, reps, ms_out);
+}
+
+int fe_sell_info(fe_handle h, int64_t *n_entries, int32_t *col16) {
+    FE_HANDLE_CHECK(h);
+    if (!h->sys_ready) {
+        set_error("fe_sell_info: assemble the system first");
+        return FE_NOT_READY;
+    }
+    int32_t last = 0;
+    if (h->n_slices > 0)
+        FE_CUDA(cudaMemcpy(&last, h->sell_off.p + h->n_slices, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (n_entries) *n_entries = last;
+    if (col16) *col16 = h->sell_c16 ? 1 : 0;
+    return FE_OK;
 }
 
 int fe_profile_kernels(fe_handle h, int32_t enable) {

@@ -619,15 +619,37 @@ __global__ void k_block_jacobi(int64_t n_nodes, const int32_t *__restrict__ blk_
 }
 
 // ---------------------------------------------------------------- SELL-32 copy for the solver
-// Width of each slice: the largest off-diagonal block count of its 32 rows (rows past
-// the end count 0), stored as 32 * width so that a scan gives the slice offsets.
+// Row r carries a row-sum entry when its block row sum S_r is not rounding noise: S_r
+// vanishes exactly (K annihilates rigid translations) except on rows that lost
+// columns to the Dirichlet elimination, so a row keeps it when some entry exceeds
+// 1e-12 of the largest diagonal entry.
+template <int D>
+__device__ __forceinline__ bool has_row_sum(const double *__restrict__ srow, const double *__restrict__ d64row) {
+    double smax = 0.0, dmax = 0.0;
+#pragma unroll
+    for (int q = 0; q < D * D; ++q) smax = fmax(smax, fabs(srow[q])), dmax = fmax(dmax, fabs(d64row[q]));
+    return smax > 1e-12 * dmax;
+}
+
+// Width of each slice: the largest entry count of its 32 rows -- off-diagonal blocks
+// plus the row-sum entry -- (rows past the end count 0), stored as 32 * width so that
+// a scan gives the slice offsets.
+template <int D>
 __global__ void k_sell_widths(int64_t n_nodes, int64_t n_slices, const int32_t *__restrict__ blk_ptr,
-                              int32_t *__restrict__ len) {
+                              const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
+                              const double *__restrict__ srow, int32_t *__restrict__ len) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t sl = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < n_slices; sl += warps) {
         int64_t r = sl * 32 + lane;
-        int w = r < n_nodes ? blk_ptr[r + 1] - blk_ptr[r] - 1 : 0;
+        int w = 0;
+        if (r < n_nodes) {
+            const int lo = blk_ptr[r], hi = blk_ptr[r + 1];
+            const int s = find_col(blk_col, lo, hi, (int)r);
+            const bool found = s < hi && blk_col[s] == (int)r;
+            w = hi - lo - (found ? 1 : 0);
+            if (found && has_row_sum<D>(srow + r * D * D, aval + (int64_t)s * D * D)) ++w;
+        }
         w = max(w, 0);
         for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
         if (lane == 0) len[sl] = 32 * w;
@@ -649,18 +671,21 @@ __device__ __forceinline__ void scale_block(const double *__restrict__ dinv_r, c
         }
 }
 
-// SELL-32 fill.  FP64 copy: the eliminated blocks A_rm and the diagonal A_rr.  FP32
-// copy, prescaled by the node-block Jacobi inverse for the Chebyshev steps: blocks
-// D_r^-1 A_rm and, in the diagonal slot, D_r^-1 S_r (S_r the block row sum of the
-// difference form); dblk32 keeps A_rr in FP32 so that a product with the FP32 copy
-// can be scaled back to A x.
+// SELL-32 fill.  Columns as int32 (col) and as 16-bit offsets c - r (dcol, usable when
+// no offset overflows: *dcol_over stays 0).  FP64 copy: the eliminated blocks A_rm and
+// the diagonal A_rr (diag64).
+// FP32 copy, prescaled by the node-block Jacobi inverse for the Chebyshev steps and in
+// difference form: blocks D_r^-1 A_rm applied to x_m - x_r and, where S_r is not
+// rounding noise, a first entry with column r holding D_r^-1 S_r, applied to x_r
+// itself (a zero block in the FP64 copy).  dblk32 keeps A_rr in FP32 so that a product
+// with the FP32 copy can be scaled back to A x.
 template <int D>
 __global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__restrict__ blk_ptr,
                             const int32_t *__restrict__ blk_col, const double *__restrict__ aval,
                             const double *__restrict__ srow, const double *__restrict__ dinv,
                             const int32_t *__restrict__ off, int32_t *__restrict__ col, double *__restrict__ v64,
                             float *__restrict__ v32, double *__restrict__ d64, float *__restrict__ d32,
-                            float *__restrict__ dblk32) {
+                            float *__restrict__ dblk32, int16_t *__restrict__ dcol, int *__restrict__ dcol_over) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_slices * 32;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int64_t sl = r >> 5, lane = r & 31;
@@ -673,6 +698,19 @@ __global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__
             scale_block<D>(dr, srow + r * D * D, sc);
 #pragma unroll
             for (int q = 0; q < D * D; ++q) d32[r * D * D + q] = (float)sc[q];
+            const int lo = blk_ptr[r], hi = blk_ptr[r + 1];
+            const int sd = find_col(blk_col, lo, hi, (int)r);
+            if (sd < hi && blk_col[sd] == (int)r && has_row_sum<D>(srow + r * D * D, aval + (int64_t)sd * D * D)) {
+                const int64_t e = base + lane;
+                col[e] = (int32_t)r;
+                dcol[e] = 0;
+#pragma unroll
+                for (int q = 0; q < D * D; ++q) {
+                    v64[e * D * D + q] = 0.0;
+                    v32[e * D * D + q] = (float)sc[q];
+                }
+                k = 1;
+            }
             for (int s = blk_ptr[r]; s < blk_ptr[r + 1]; ++s) {
                 const int c = blk_col[s];
                 if (c == (int)r) {
@@ -685,6 +723,9 @@ __global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__
                 }
                 const int64_t e = base + 32 * (int64_t)k + lane;
                 col[e] = c;
+                const int64_t off_c = (int64_t)c - r;
+                if (off_c < -32768 || off_c > 32767) atomicOr(dcol_over, 1);
+                dcol[e] = (int16_t)max((int64_t)-32768, min((int64_t)32767, off_c));
                 scale_block<D>(dr, aval + (int64_t)s * D * D, sc);
 #pragma unroll
                 for (int q = 0; q < D * D; ++q) {
@@ -698,6 +739,7 @@ __global__ void k_sell_fill(int64_t n_nodes, int64_t n_slices, const int32_t *__
         for (; k < w; ++k) {
             const int64_t e = base + 32 * (int64_t)k + lane;
             col[e] = r < n_nodes ? (int32_t)r : 0;
+            dcol[e] = r < n_nodes ? (int16_t)0 : (int16_t)max((int64_t)-32768, -r);
 #pragma unroll
             for (int q = 0; q < D * D; ++q) {
                 v64[e * D * D + q] = 0.0;
@@ -1007,13 +1049,23 @@ int build_sell(fe_handle_s *h) {
     FE_CHECK(dalloc(h->counts, (size_t)std::max<int64_t>(n_slices, h->n_nodes) + 1));
     FE_CHECK(dalloc(h->sell_off, (size_t)n_slices + 1));
     if (n_slices > 0) {
-        k_sell_widths<<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->counts.p);
+        if (D == 2)
+            k_sell_widths<2><<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p,
+                                                                         h->blk_col.p, h->aval.p, h->srow.p,
+                                                                         h->counts.p);
+        else
+            k_sell_widths<1><<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p,
+                                                                         h->blk_col.p, h->aval.p, h->srow.p,
+                                                                         h->counts.p);
         FE_LAUNCH_CHECK();
     }
     int64_t total = 0;
     FE_CHECK(exclusive_scan_i32(h->counts.p, h->sell_off.p, n_slices, &total, h->scan_tmp, s));
     size_t ne = (size_t)std::max<int64_t>(total, 1);
     FE_CHECK(dalloc(h->sell_col, ne));
+    FE_CHECK(dalloc(h->sell_dcol, ne));
+    FE_CHECK(dalloc(h->sell_over, 1));
+    FE_CUDA(cudaMemsetAsync(h->sell_over.p, 0, sizeof(int), s));
     FE_CHECK(dalloc(h->sell_val64, ne * D * D));
     FE_CHECK(dalloc(h->sell_val32, ne * D * D));
     FE_CHECK(dalloc(h->diag64, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
@@ -1029,14 +1081,18 @@ int build_sell(fe_handle_s *h) {
             k_sell_fill<2><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
                                                   h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
                                                   h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
-                                                  h->dblk32.p);
+                                                  h->dblk32.p, h->sell_dcol.p, h->sell_over.p);
         else
             k_sell_fill<1><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
                                                   h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
                                                   h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
-                                                  h->dblk32.p);
+                                                  h->dblk32.p, h->sell_dcol.p, h->sell_over.p);
         FE_LAUNCH_CHECK();
     }
+    int over = 1;
+    FE_CUDA(cudaMemcpyAsync(&over, h->sell_over.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    h->sell_c16 = (over == 0);
     h->launches += (n_slices > 0 ? 2 : 0) + 3;
     return FE_OK;
 }

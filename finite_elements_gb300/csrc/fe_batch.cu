@@ -75,8 +75,11 @@ __device__ __forceinline__ double2 bsr_row(int64_t r, bool valid, const int32_t 
         const double2 xv = reinterpret_cast<const double2 *>(x)[c];
         const double2 b0 = __ldg(reinterpret_cast<const double2 *>(val) + 2 * (int64_t)k);
         const double2 b1 = __ldg(reinterpret_cast<const double2 *>(val) + 2 * (int64_t)k + 1);
-        a0 += b0.x * xv.x + b0.y * xv.y;
-        a1 += b1.x * xv.x + b1.y * xv.y;
+        // one FMA chain per output row: 4 FP64 FMAs per block (the FP64 pipe bounds this)
+        a0 = fma(b0.x, xv.x, a0);
+        a1 = fma(b1.x, xv.x, a1);
+        a0 = fma(b0.y, xv.y, a0);
+        a1 = fma(b1.y, xv.y, a1);
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
@@ -330,8 +333,11 @@ kb_true_residual(int64_t n_nodes, const int32_t *__restrict__ inst, const int32_
             double a0 = 0, a1 = 0;
             for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
                 const int c = col[k];
-                a0 += val[4 * (int64_t)k] * x[2 * (int64_t)c] + val[4 * (int64_t)k + 1] * x[2 * (int64_t)c + 1];
-                a1 += val[4 * (int64_t)k + 2] * x[2 * (int64_t)c] + val[4 * (int64_t)k + 3] * x[2 * (int64_t)c + 1];
+                const double x0 = x[2 * (int64_t)c], x1 = x[2 * (int64_t)c + 1];
+                a0 = fma(val[4 * (int64_t)k], x0, a0);
+                a1 = fma(val[4 * (int64_t)k + 2], x0, a1);
+                a0 = fma(val[4 * (int64_t)k + 1], x1, a0);
+                a1 = fma(val[4 * (int64_t)k + 3], x1, a1);
             }
             const double e0 = b[2 * r] - a0, e1 = b[2 * r + 1] - a1;
             v = e0 * e0 + e1 * e1;

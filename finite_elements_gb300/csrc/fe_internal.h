@@ -119,9 +119,10 @@ struct SolverWork {
         double theta = 0, delta = 0;
         bool prof = false;
     } key[3];
-    // Kernel timing inside the captured loop (fe_profile_kernels): event records
-    // around the first iteration of every chunk, [slot][0] an intermediate Chebyshev
-    // step, [slot][1] the PCG SpMV (slots as graph[]); summed durations and launches.
+    // Kernel timing inside the captured loop (fe_profile_kernels): event records in
+    // the first iteration of every chunk, [slot][0] around the run of intermediate
+    // Chebyshev steps 2 .. k-2, [slot][1] around the PCG SpMV (slots as graph[]);
+    // summed durations and the launches they cover.
     bool prof = false;
     cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
     double prof_ms[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
@@ -188,6 +189,9 @@ struct fe_handle_s {
     // with a zero block.  The diagonal lives in diag64 (A_rr) / diag32 (D^-1 S_r).
     int64_t n_slices = 0;
     fe::DBuf<int32_t> sell_off, sell_col;
+    fe::DBuf<int16_t> sell_dcol;          // column offsets c - r, for the FP32 kernels
+    fe::DBuf<int> sell_over;              // set when an offset does not fit in 16 bits
+    bool sell_c16 = false;                // sell_dcol holds every column
     fe::DBuf<double> sell_val64, diag64;
     fe::DBuf<float> sell_val32, diag32;   // prescaled by the block-Jacobi inverse (D^-1 A_rm, D^-1 S_r)
     fe::DBuf<float> dblk32;               // [n_nodes][d][d] A_rr in FP32 (scales D^-1 A x back to A x)

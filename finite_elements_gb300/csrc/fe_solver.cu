@@ -31,6 +31,7 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "fe_internal.h"
@@ -241,16 +242,39 @@ __device__ __forceinline__ void block_mac(const T *__restrict__ blk, const NodeV
     }
 }
 
+// Resident blocks per SM the SELL kernels are compiled for: FP32 8 (32 registers, the
+// 1216-block grid is one wave); FP64 0, i.e. ptxas's default (40-48 registers; a
+// floor of 1 makes it spend ~120 and lose the occupancy, 5 makes the Chebyshev step
+// spill).
+template <typename T>
+constexpr int kSellBlocks = sizeof(T) == 4 ? 8 : 0;
+
 struct Sell {
     const int32_t *off, *col;
+    const int16_t *dcol;   // column offsets c - r when every one fits in 16 bits, else null
     int64_t n_slices;
 };
 
+// Calls f(std::true_type) when an FP32 kernel can read the 16-bit column offsets,
+// else f(std::false_type); FP64 kernels always read the int32 columns.
+template <typename T, typename F>
+void with_col16(const Sell &A, F f) {
+    if constexpr (sizeof(T) == 4) {
+        if (A.dcol) {
+            f(std::true_type{});
+            return;
+        }
+    }
+    f(std::false_type{});
+}
+
 // Row r of A x from the SELL-32 copy: one lane per block row, one warp per slice of
 // 32 rows, entry k of the slice at base + 32 k + lane, so each warp load of columns
-// and blocks is one contiguous segment.  The diagonal block comes from diag (A_rr, or
-// S_r in the FP32 difference form); padding entries point at the row itself.
-template <int D, typename T>
+// and blocks is one contiguous segment.  FP64: the diagonal block comes from diag and
+// every entry multiplies x_c.  FP32 (difference form): an entry with column c != r
+// multiplies x_c - x_r, an entry with column r (the row-sum entry, or padding with a
+// zero block) multiplies x_r; there is no diagonal term.
+template <int D, typename T, bool C16 = false>
 __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const Sell &A, const T *__restrict__ val,
                                                   const T *__restrict__ diag, const T *__restrict__ x) {
     constexpr bool DIFF = sizeof(T) == 4;
@@ -259,7 +283,7 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
     for (int a = 0; a < D; ++a) xr.v[a] = T(0), acc.v[a] = T(0);
     if (valid) {
         xr = ld<D, T>(x, r);
-        block_mac<D, T>(diag + r * D * D, xr, acc);
+        if constexpr (!DIFF) block_mac<D, T>(diag + r * D * D, xr, acc);
     }
     const int64_t sl = r >> 5;
     const int lane = (int)(r & 31);
@@ -273,14 +297,16 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
         int c[U];
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            c[u] = (k + u < w) ? __ldg(A.col + base + 32 * (int64_t)(k + u) + lane) : (int)r;
+            c[u] = (k + u < w) ? (C16 ? (int)r + (int)__ldg(A.dcol + base + 32 * (int64_t)(k + u) + lane)
+                                      : __ldg(A.col + base + 32 * (int64_t)(k + u) + lane))
+                               : (int)r;
         NodeVec<D, T> xv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) xv[u] = ld<D, T>(x, c[u]);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             if (k + u < w) {
-                if (DIFF) {
+                if (DIFF && c[u] != (int)r) {
 #pragma unroll
                     for (int a = 0; a < D; ++a) xv[u].v[a] -= xr.v[a];
                 }
@@ -301,13 +327,13 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
 // ---------------------------------------------------------------- kernels
 
 // y = A x (timing)
-template <int D, typename T>
-__global__ void __launch_bounds__(kVecThreads)
+template <int D, typename T, bool C16 = false>
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<T>)
 k_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ dscale,
        const T *__restrict__ x, T *__restrict__ y) {
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> v = sell_row<D, T>(row, valid, A, val, diag, x);
+        NodeVec<D, T> v = sell_row<D, T, C16>(row, valid, A, val, diag, x);
         if (valid) {
             if (dscale) v = apply_dinv<D, T>(dscale, row, v);   // prescaled copy: A x = A_rr (D^-1 A x)
             st<D, T>(y, row, v);
@@ -350,8 +376,8 @@ k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__re
 }
 
 // q = A p and p.q; the last block sets alpha = r.z / p.q or stops the loop.
-template <int D, typename T>
-__global__ void __launch_bounds__(kVecThreads)
+template <int D, typename T, bool C16 = false>
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<T>)
 k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
            const T *__restrict__ dscale, const T *__restrict__ p, T *__restrict__ q, double *partials,
            PcgScalars *sc) {
@@ -359,7 +385,7 @@ k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restri
     T lt = T(0);
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> y = sell_row<D, T>(row, valid, A, val, diag, p);
+        NodeVec<D, T> y = sell_row<D, T, C16>(row, valid, A, val, diag, p);
         if (valid) {
             if (dscale) y = apply_dinv<D, T>(dscale, row, y);   // prescaled copy: A p = A_rr (D^-1 A p)
             st<D, T>(q, row, y);
@@ -481,8 +507,8 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
 // MODE 1: last step of an iteration (reduces rdot.z_{k+1} in FP64, finishes the
 //         iteration; rdot is the recurrence's residual);
 // MODE 2: intermediate step.
-template <int D, typename T, typename RD, int MODE, bool FIRST>
-__global__ void __launch_bounds__(kVecThreads)
+template <int D, typename T, typename RD, int MODE, bool FIRST, bool C16>
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<T>)   // FP32: 8 blocks per SM, one wave
 k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
             const T *__restrict__ dinv, const T *__restrict__ rres, const T *__restrict__ z_in,
             T *__restrict__ zprev_out, double c1, double c2, double *partials, PcgScalars *sc,
@@ -493,7 +519,7 @@ k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restr
     double lrz = 0.0;
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> az = sell_row<D, T>(row, valid, A, val, diag, z_in);
+        NodeVec<D, T> az = sell_row<D, T, C16>(row, valid, A, val, diag, z_in);
         if (valid) {
             NodeVec<D, T> rv = ld<D, T>(rres, row), zv = ld<D, T>(z_in, row), zp;
             if (FIRST) {
@@ -799,12 +825,12 @@ struct Sys {
 struct Cheb {
     int k = 1;                 // Chebyshev terms (1 = plain node-block Jacobi)
     double theta = 1, delta = 1;
-    double c1[32], c2[32];     // coefficients of steps 1..k-1
+    double c1[64], c2[64];     // coefficients of steps 1..k-1
 };
 
 Cheb make_cheb(int degree, double lmax, double ratio) {
     Cheb c;
-    c.k = std::max(1, std::min(degree, 32));
+    c.k = std::max(1, std::min(degree, 64));
     if (c.k <= 1 || !(lmax > 0)) {
         c.k = 1;
         return c;
@@ -827,7 +853,7 @@ Sys<T> make_sys(fe_handle_s *h) {
     Sys<T> s;
     SolverWork &w = h->w;
     s.x = w.x.p;
-    s.A = Sell{h->sell_off.p, h->sell_col.p, h->n_slices};
+    s.A = Sell{h->sell_off.p, h->sell_col.p, h->sell_c16 ? h->sell_dcol.p : nullptr, h->n_slices};
     if constexpr (sizeof(T) == 8) {
         s.sval = h->sell_val64.p, s.diag = h->diag64.p;
         s.val = h->aval.p, s.dinv = h->dinv.p;
@@ -845,12 +871,15 @@ Sys<T> make_sys(fe_handle_s *h) {
 template <int D, typename T, typename RD, int MODE>
 void launch_cheb_step(fe_handle_s *h, const Sys<T> &s, bool first, const T *zin, T *zout, double c1, double c2,
                       double *part, PcgScalars *sc, int grid, const RD *rdot) {
-    if (first)
-        k_cheb_step<D, T, RD, MODE, true><<<grid, kVecThreads, 0, h->stream>>>(
-            h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
-    else
-        k_cheb_step<D, T, RD, MODE, false><<<grid, kVecThreads, 0, h->stream>>>(
-            h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
+    with_col16<T>(s.A, [&](auto c16) {
+        constexpr bool C = decltype(c16)::value;
+        if (first)
+            k_cheb_step<D, T, RD, MODE, true, C><<<grid, kVecThreads, 0, h->stream>>>(
+                h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
+        else
+            k_cheb_step<D, T, RD, MODE, false, C><<<grid, kVecThreads, 0, h->stream>>>(
+                h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
+    });
 }
 
 // Chebyshev steps 1..k-1 after z_1 is in s.z; z ping-pongs between s.z and s.zc
@@ -862,15 +891,15 @@ void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScal
     T *zin = s.z, *zout = s.zc;
     for (int k = 1; k < cb.k; ++k) {
         const bool last = (k == cb.k - 1), first = (k == 1);
-        const bool timed = ev && k == 2 && !last;      // an intermediate step (MODE 2)
-        if (timed) cudaEventRecordWithFlags(ev[2], h->stream, cudaEventRecordExternal);
+        // the intermediate steps 2 .. k-2 (MODE 2, not FIRST) are timed as one run
+        if (ev && k == 2 && !last) cudaEventRecordWithFlags(ev[2], h->stream, cudaEventRecordExternal);
         if (start)
             launch_cheb_step<D, T, RD, 0>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid, rdot);
         else if (last)
             launch_cheb_step<D, T, RD, 1>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid, rdot);
         else
             launch_cheb_step<D, T, RD, 2>(h, s, first, zin, zout, cb.c1[k], cb.c2[k], part, sc, grid, rdot);
-        if (timed) cudaEventRecordWithFlags(ev[3], h->stream, cudaEventRecordExternal);
+        if (ev && k >= 2 && k == cb.k - 2) cudaEventRecordWithFlags(ev[3], h->stream, cudaEventRecordExternal);
         std::swap(zin, zout);
     }
     *z_final = zin;
@@ -884,8 +913,10 @@ void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScala
     const int gv = vec_grid(h->n_nodes);
     const int gs = sell_grid(h);
     if (ev) cudaEventRecordWithFlags(ev[0], h->stream, cudaEventRecordExternal);
-    k_pcg_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dblk, s.p, s.q, part,
-                                                         sc);
+    with_col16<T>(s.A, [&](auto c16) {
+        k_pcg_spmv<D, T, decltype(c16)::value><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag,
+                                                                                   s.dblk, s.p, s.q, part, sc);
+    });
     if (ev) cudaEventRecordWithFlags(ev[1], h->stream, cudaEventRecordExternal);
     T *zf = s.z;
     T *rh = s.rh != s.r ? s.rh : nullptr;
@@ -1060,7 +1091,7 @@ int run_chunks(fe_handle_s *h, int slot, const void *key_ptr, int G, const Cheb 
             if (cudaEventElapsedTime(&a, w.pev[0], w.pev[1]) == cudaSuccess)
                 w.prof_ms[slot][1] += a, w.prof_n[slot][1] += 1;
             if (cb.k >= 4 && cudaEventElapsedTime(&a, w.pev[2], w.pev[3]) == cudaSuccess)
-                w.prof_ms[slot][0] += a, w.prof_n[slot][0] += 1;
+                w.prof_ms[slot][0] += a, w.prof_n[slot][0] += cb.k - 3;
         }
         if (w.sc_host->done) break;
         if (watch) {
@@ -1194,10 +1225,16 @@ int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
     FE_CUDA(cudaMemsetAsync(x, 0, h->n_dof * sizeof(T), h->stream));
     const int gs = sell_grid(h);
     for (int i = 0; i < 2; ++i)
-        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dblk, x, y);
+        with_col16<T>(s.A, [&](auto c16) {
+            k_spmv<D, T, decltype(c16)::value><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag,
+                                                                                   s.dblk, x, y);
+        });
     FE_CUDA(cudaEventRecord(h->events[8], h->stream));
     for (int i = 0; i < reps; ++i)
-        k_spmv<D, T><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag, s.dblk, x, y);
+        with_col16<T>(s.A, [&](auto c16) {
+            k_spmv<D, T, decltype(c16)::value><<<gs, kVecThreads, 0, h->stream>>>(h->n_nodes, s.A, s.sval, s.diag,
+                                                                                   s.dblk, x, y);
+        });
     FE_CUDA(cudaEventRecord(h->events[9], h->stream));
     FE_LAUNCH_CHECK();
     FE_CUDA(cudaEventSynchronize(h->events[9]));
@@ -1619,7 +1656,7 @@ int spmv64(fe_handle_s *h, const double *x, double *y) {
         set_error("spmv64: the system is not assembled");
         return FE_NOT_READY;
     }
-    Sell A{h->sell_off.p, h->sell_col.p, h->n_slices};
+    Sell A{h->sell_off.p, h->sell_col.p, nullptr, h->n_slices};
     if (h->dim == 2)
         k_spmv<2, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
                                                                         nullptr, x, y);

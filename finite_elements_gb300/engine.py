@@ -235,6 +235,13 @@ class GpuSystem:
         self.handle.call("fe_post_magnetic", ptr(xa), ptr(field))
         return {"field": field}
 
+    def sell_info(self):
+        """Stored SELL-32 entries (padding included) and whether the FP32 kernels use
+        16-bit column offsets."""
+        ne, c16 = _i64(), ctypes.c_int32()
+        self.handle.call("fe_sell_info", ne, c16)
+        return {"entries": ne.value, "col16": bool(c16.value)}
+
     def info(self):
         nd, nb, nblk = _i64(), _i64(), _i64()
         self.handle.call("fe_info", nd, nb, nblk)

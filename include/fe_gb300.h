@@ -74,7 +74,7 @@ typedef struct fe_handle_s *fe_handle;
 
 typedef struct fe_solve_opts {
     int32_t precision;     /* FE_PREC_FP64, FE_PREC_MIXED or FE_PREC_MIXED_CG64          */
-    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it (k <= 32) */
+    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it (k <= 64) */
     int32_t max_iter;      /* cap on PCG iterations, all refinement steps together       */
     int32_t max_outer;     /* cap on refinement steps (mixed) or restarts (FP64)          */
     double  tol;           /* target ||b - A x||_2 / ||b||_2, FP64 true residual          */
@@ -181,12 +181,17 @@ int fe_launch_count(fe_handle h, int64_t *count);
 int fe_autotune_spmv(fe_handle h, int32_t precision, int32_t *lanes_out, double *ms_out);
 /* Average device time of one SpMV with the given lanes (reps repetitions). */
 int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, double *ms_out);
+/* Layout of the solver's SELL-32 copies (no counterpart in the reference): stored
+ * entries (padding included) and whether the FP32 kernels read 16-bit column offsets
+ * (1) or the int32 columns (0, some offset exceeds 32767). */
+int fe_sell_info(fe_handle h, int64_t *n_entries, int32_t *col16);
 /* Kernel timing inside the solver's captured PCG loop (no counterpart in the
- * reference; for measurement).  enable = 1 adds CUDA event records around the first
- * iteration of every 16-iteration chunk and resets the sums; 0 removes them.
- * fe_profile_read returns, for the given precision, the summed device time (ms) and
- * the number of timed launches of an intermediate Chebyshev step (degree >= 4) and of
- * the PCG SpMV. */
+ * reference; for measurement).  enable = 1 adds CUDA event records to the first
+ * iteration of every 16-iteration chunk -- around the run of intermediate Chebyshev
+ * steps 2 .. k-2 (degree >= 4) and around the PCG SpMV -- and resets the sums; 0
+ * removes them.  fe_profile_read returns, for the given precision, the summed device
+ * time (ms) and the number of launches it covers, for the Chebyshev steps and for the
+ * PCG SpMV. */
 int fe_profile_kernels(fe_handle h, int32_t enable);
 int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *cheb_n, double *spmv_ms,
                     int64_t *spmv_n);

@@ -111,3 +111,31 @@ def test_4m_fp64_is_deterministic(big):
     x2, st2 = s.solve(precision="fp64", tol=1e-6, cheb_degree=0)
     assert st1.iterations == st2.iterations
     np.testing.assert_array_equal(x1, x2)
+
+
+def test_permuted_numbering_uses_int32_columns_and_gives_the_same_solution(gpu_lib):
+    """A random node numbering puts column offsets beyond 16 bits: the FP32 kernels then
+    read the int32 columns, and the solution (mapped back) is the same."""
+    import dataclasses
+    from finite_elements_gb300 import meshgen
+    from finite_elements_gb300.engine import GpuSystem
+    prob = meshgen.plane_strain_random(300, 150, seed=3)
+    assert prob.n_nodes > 32768
+    perm = np.random.default_rng(0).permutation(prob.n_nodes)      # old id -> new id
+    coords = np.empty_like(prob.coords)
+    coords[perm] = prob.coords
+    pp = dataclasses.replace(prob, coords=coords, conn=perm[prob.conn].astype(np.int32),
+                             node_load_node=perm[prob.node_load_node], node_bc_node=perm[prob.node_bc_node],
+                             edge_load_nodes=perm[prob.edge_load_nodes], edge_bc_nodes=perm[prob.edge_bc_nodes])
+    s0, s1 = GpuSystem(prob), GpuSystem(pp)
+    assert s0.sell_info()["col16"] and not s1.sell_info()["col16"]
+    n = prob.n_dof
+    for prec in ("mixed-cg64", "mixed"):
+        x0, st0 = s0.solve(precision=prec, tol=1e-10, cheb_degree=8, cheb_ratio=1000)
+        x1, st1 = s1.solve(precision=prec, tol=1e-10, cheb_degree=8, cheb_ratio=1000)
+        assert st0.status == 0 and st1.status == 0, (st0.as_dict(), st1.as_dict())
+        u0 = x0[:n].reshape(-1, 2)
+        u1 = x1[:n].reshape(-1, 2)[perm]
+        assert np.linalg.norm(u1 - u0) <= 1e-8 * np.linalg.norm(u0)
+    s0.close()
+    s1.close()
