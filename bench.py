@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 # DRAM bytes (read + write) per launch of the roofline kernel (the intermediate FP32
 # Chebyshev step) from one ncu capture of this workload, keyed by grid (summary in
 # profiles/cheb_step_fp32_plane_strain_4M.md); None when the workload differs.
-NCU_TRAFFIC = {}
+NCU_TRAFFIC = {(2000, 1000): 278_710_784}
 
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
 UNIT = "s/solve"
@@ -47,10 +47,10 @@ def parse_args():
     ap.add_argument("--ny", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cheb", type=int, default=32, help="Chebyshev degree of the mixed solve's preconditioner")
-    ap.add_argument("--cheb-ratio", type=float, default=10000.0, help="Chebyshev interval lmax/lmin (mixed)")
-    ap.add_argument("--plain-cheb", type=int, default=24, help="Chebyshev degree of the plain FP64 PCG")
-    ap.add_argument("--plain-cheb-ratio", type=float, default=10000.0, help="Chebyshev interval (plain FP64)")
+    ap.add_argument("--cheb", type=int, default=64, help="Chebyshev degree of the mixed solve's preconditioner")
+    ap.add_argument("--cheb-ratio", type=float, default=100000.0, help="Chebyshev interval lmax/lmin (mixed)")
+    ap.add_argument("--plain-cheb", type=int, default=32, help="Chebyshev degree of the plain FP64 PCG")
+    ap.add_argument("--plain-cheb-ratio", type=float, default=30000.0, help="Chebyshev interval (plain FP64)")
     ap.add_argument("--ir-cheb", type=int, default=16,
                     help="Chebyshev degree of the FP32-Krylov + iterative-refinement solve reported beside")
     ap.add_argument("--ir-cheb-ratio", type=float, default=3000.0)
