@@ -217,7 +217,7 @@ def run_ours(args, dist):
         h.call("fe_assemble", step_flags)
         if learned and net is not None:
             ptr, _ = net.predict(s)               # the warm start is part of the step
-            _, st = s.solve(x0_device_ptr=ptr, **opts)
+            _, st = s.solve(x0_device_ptr=ptr, x0_if_better=True, **opts)
         else:
             _, st = s.solve(**opts)
         if st.status != _lib.FE_OK:
@@ -367,7 +367,7 @@ def run_ours(args, dist):
         se = GpuSystem(prob, assemble=True)
         if net is not None:
             ptr, _ = net.predict(se)
-            x, st = se.solve(x0_device_ptr=ptr, **e2e_opts)
+            x, st = se.solve(x0_device_ptr=ptr, x0_if_better=True, **e2e_opts)
         else:
             x, st = se.solve(**e2e_opts)
         dt = time.perf_counter() - t0
@@ -388,7 +388,9 @@ def run_ours(args, dist):
                         f"{prob.n_dof:,} DOF, E=10^U(9,12) per element, nu~U(0.2,0.45), left edge clamped, "
                         f"random top-edge traction",
             "mode": "mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
-                    "preconditioner in FP32 on the prescaled FP32 copy" + (" + learned warm start" if net is not None else ""),
+                    "preconditioner in FP32 on the prescaled FP32 copy"
+                    + (" + learned warm start (predicted every step; kept when its FP64 residual beats the zero "
+                       "start)" if net is not None else ""),
             "learned_warm_start": net is not None,
             "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio],
                           "fp32_krylov_ir": [args.ir_cheb, args.ir_cheb_ratio]},
@@ -396,7 +398,7 @@ def run_ours(args, dist):
             "l2": "inputs larger than L2 (BSR values alone 448 MB FP64 / 224 MB FP32)",
             "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
         },
-        "iterations": stats[-1].iterations, "restarts": stats[-1].outer,
+        "iterations": stats[-1].iterations, "restarts": stats[-1].outer, "learned_x0_used": stats[-1].x0_used,
         "relres": stats[-1].relres, "err_vs_fp64": err,
         "plain_fp64": {"s_per_solve": plain_s, "iterations": pstats[-1].iterations if pstats else None,
                        "relres": pstats[-1].relres if pstats else None},

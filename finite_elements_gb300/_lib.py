@@ -20,7 +20,7 @@ FE_PLANE_STRESS, FE_PLANE_STRAIN = 1, 2
 FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F, FE_ASSEMBLE_PATTERN = 1, 2, 4, 8
 FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
 FE_PREC_FP64, FE_PREC_MIXED, FE_PREC_MIXED_CG64 = 0, 1, 2
-FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP = 1, 2
+FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP, FE_SOLVE_X0_IF_BETTER = 1, 2, 4
 
 STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",
                 FE_NONFINITE: "FE_NONFINITE", FE_BAD_INPUT: "FE_BAD_INPUT",
@@ -46,7 +46,7 @@ class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
                 ("spmv", C.c_int32), ("relres", C.c_double), ("bnorm", C.c_double),
                 ("solve_ms", C.c_double), ("assemble_ms", C.c_double), ("fp64_iterations", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("x0_used", C.c_int32)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -1030,6 +1030,33 @@ int init_solution(fe_handle_s *h, const fe_solve_opts *o, double *x) {
     return FE_OK;
 }
 
+int read_scalars(fe_handle_s *h);
+
+// Starting point of a solve: x0 (or zero) with the prescribed values.  With
+// FE_SOLVE_X0_IF_BETTER a given x0 is kept only when its FP64 true residual is below
+// that of the zero start, so a poor warm start costs two residuals and nothing more.
+template <int D, int G>
+int start_point(fe_handle_s *h, const fe_solve_opts *o, double *x, int *x0_used) {
+    FE_CHECK(init_solution(h, o, x));
+    *x0_used = o->x0 ? 1 : 0;
+    if (!o->x0 || !(o->flags & FE_SOLVE_X0_IF_BETTER)) return FE_OK;
+    PcgScalars *sc = h->w.sc.p;
+    double *tmp = h->w.t.p;
+    FE_CHECK((residual<D, G, double>(h, x, tmp, &sc->rr)));
+    FE_CHECK(read_scalars(h));
+    const double rr_x0 = h->w.sc_host->rr;
+    fe_solve_opts zero = *o;
+    zero.x0 = nullptr;
+    FE_CHECK(init_solution(h, &zero, x));
+    FE_CHECK((residual<D, G, double>(h, h->n_bc > 0 ? x : nullptr, tmp, &sc->rr)));
+    FE_CHECK(read_scalars(h));
+    if (h->w.sc_host->rr <= rr_x0) {
+        *x0_used = 0;
+        return FE_OK;
+    }
+    return init_solution(h, o, x);
+}
+
 int read_scalars(fe_handle_s *h) {
     FE_CUDA(cudaMemcpyAsync(h->w.sc_host, h->w.sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, h->stream));
     FE_CUDA(cudaStreamSynchronize(h->stream));
@@ -1364,8 +1391,10 @@ int solve_fp64(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         st->status = FE_OK;
         return FE_OK;
     }
-    FE_CHECK(init_solution(h, o, s.x));
-    const bool nonzero = o->x0 || h->n_bc > 0;
+    int x0_used = 0;
+    FE_CHECK((start_point<D, G>(h, o, s.x, &x0_used)));
+    st->x0_used = x0_used;
+    const bool nonzero = x0_used || h->n_bc > 0;
     FE_CHECK((residual<D, G, double>(h, nonzero ? s.x : nullptr, s.r, &sc->rr)));
     st->spmv += nonzero ? 1 : 0;
     int total = 0, restarts = 0, status = FE_OK;
@@ -1412,8 +1441,10 @@ int solve_mp(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         st->status = FE_OK;
         return FE_OK;
     }
-    FE_CHECK(init_solution(h, o, s.d.x));
-    const bool nonzero = o->x0 || h->n_bc > 0;
+    int x0_used = 0;
+    FE_CHECK((start_point<D, G>(h, o, s.d.x, &x0_used)));
+    st->x0_used = x0_used;
+    const bool nonzero = x0_used || h->n_bc > 0;
     FE_CHECK((residual<D, G, double>(h, nonzero ? s.d.x : nullptr, s.d.r, &sc->rr)));
     st->spmv += nonzero ? 1 : 0;
     int total = 0, restarts = 0, status = FE_OK;
@@ -1469,8 +1500,10 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         st->status = FE_OK;
         return FE_OK;
     }
-    FE_CHECK(init_solution(h, o, x64));
-    const bool nonzero = o->x0 || h->n_bc > 0;
+    int x0_used = 0;
+    FE_CHECK((start_point<D, G>(h, o, x64, &x0_used)));
+    st->x0_used = x0_used;
+    const bool nonzero = x0_used || h->n_bc > 0;
     // r32 = b - A x64 (FP64 residual, stored in FP32)
     FE_CHECK((residual<D, G, float>(h, nonzero ? x64 : nullptr, s.r, &sc->rr)));
     FE_CHECK(read_scalars(h));

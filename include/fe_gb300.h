@@ -56,6 +56,9 @@ extern "C" {
 /* fe_solve_opts.flags */
 #define FE_SOLVE_ACCEPT_STAGNATION 1   /* FP64: a true residual that restarts no longer
                                           lower (rounding floor) ends the solve with FE_OK */
+#define FE_SOLVE_X0_IF_BETTER     4    /* keep x0 only if its FP64 true residual is below
+                                          that of the zero start (prescribed values only);
+                                          fe_solve_stats.x0_used reports the choice     */
 #define FE_SOLVE_RESTART_EACH_STEP 2   /* mixed: restart the Krylov space at every refinement
                                           step (classic iterative refinement) instead of
                                           continuing along the current direction          */
@@ -98,7 +101,7 @@ typedef struct fe_solve_stats {
     double  assemble_ms;   /* device time of the last fe_assemble                         */
     int32_t fp64_iterations; /* mixed: iterations of the FP64 finish (0 when FP32 met tol);
                                 included in iterations                                   */
-    int32_t reserved;
+    int32_t x0_used;       /* 1 if the solve started from the given x0                    */
 } fe_solve_stats;
 
 int         fe_version(void);

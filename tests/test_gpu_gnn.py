@@ -86,10 +86,15 @@ def test_trained_network_gain_is_measured(gpu_lib):
     _, st0 = s.solve(**kw)
     ptr, scale = net.predict(s)
     _, st1 = s.solve(x0_device_ptr=ptr, **kw)
-    s.close()
     assert st0.status == 0 and st1.status == 0
     assert st1.relres <= 1e-8
     assert st1.iterations <= 1.1 * st0.iterations, (st0.iterations, st1.iterations)
+    # with the acceptance test the warm start is kept only when its residual is smaller
+    _, st2 = s.solve(x0_device_ptr=ptr, x0_if_better=True, **kw)
+    assert st2.status == 0 and st2.relres <= 1e-8
+    if not st2.x0_used:
+        assert st2.iterations == st0.iterations
+    s.close()
 
 
 def test_fit_loss_and_gradient_match_oracle(small):

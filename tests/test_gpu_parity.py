@@ -139,6 +139,23 @@ def test_lanes_and_chebyshev_give_the_same_solution(systems, name, lanes):
         assert np.linalg.norm(x - ref["x"]) <= SOL_TOL * np.linalg.norm(ref["x"])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed-cg64", "mixed"])
+def test_x0_if_better_keeps_good_and_drops_bad_starts(systems, precision):
+    """FE_SOLVE_X0_IF_BETTER: the solution itself is kept as x0 (no iteration needed),
+    a large random x0 is dropped and the solve runs as from the zero start."""
+    s, prob, ref = systems["c1_cantilever"]
+    n = prob.n_dof
+    kw = dict(precision=precision, tol=1e-9, cheb_degree=4, accept_stagnation=True)
+    good = ref["x"][:n]
+    _, stg = s.solve(x0=good, x0_if_better=True, **kw)
+    assert stg.status == 0 and stg.x0_used == 1 and stg.iterations <= 2, stg.as_dict()
+    bad = np.random.default_rng(0).standard_normal(n) * np.abs(good).max() * 10
+    x0, st0 = s.solve(**kw)
+    xb, stb = s.solve(x0=bad, x0_if_better=True, **kw)
+    assert stb.status == 0 and stb.x0_used == 0 and stb.iterations == st0.iterations, stb.as_dict()
+    np.testing.assert_array_equal(xb, x0)
+
+
 def test_solve_is_deterministic(systems):
     s, prob, ref = systems["c1_cantilever"]
     x1, _ = s.solve(precision="fp64", tol=1e-14, accept_stagnation=True)
