@@ -195,6 +195,9 @@ def run_ours(args, dist):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
+    if dist.world > 1:
+        # one process per GPU: this rank's replica runs on its local device
+        _lib.check(_lib.load().fe_set_device(dist.local_rank), "fe_set_device")
     prob = meshgen.plane_strain_random(args.nx, args.ny, seed=args.seed)
     s = GpuSystem(prob, assemble=True)           # inputs uploaded: resident in HBM from here
     h = s.handle

@@ -57,6 +57,7 @@ _I32, _I64, _D = C.c_int32, C.c_int64, C.c_double
 _PD, _PI32, _PI64 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
 
 _SIGNATURES = {
+    "fe_set_device": ([_I32], C.c_int),
     "fe_version": ([], C.c_int),
     "fe_status_string": ([C.c_int], C.c_char_p),
     "fe_last_error": ([], C.c_char_p),

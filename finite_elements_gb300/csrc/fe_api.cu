@@ -50,6 +50,23 @@ extern "C" {
 
 int fe_version(void) { return 1; }
 
+int fe_set_device(int32_t device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        set_error("fe_set_device: no CUDA device");
+        return FE_CUDA_ERR;
+    }
+    if (device < 0 || device >= n) {
+        set_error("fe_set_device: device index out of range");
+        return FE_BAD_INPUT;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        set_error("fe_set_device: cudaSetDevice failed");
+        return FE_CUDA_ERR;
+    }
+    return FE_OK;
+}
+
 const char *fe_status_string(int status) {
     switch (status) {
         case FE_OK: return "FE_OK";

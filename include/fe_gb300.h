@@ -105,6 +105,10 @@ typedef struct fe_solve_stats {
 } fe_solve_stats;
 
 int         fe_version(void);
+/* Select the GPU that the calling thread's later calls (handle creation included) use,
+ * e.g. the local rank's device when one process per GPU runs replicas.  No
+ * counterpart in the reference (CPU only). */
+int         fe_set_device(int32_t device);
 const char *fe_status_string(int status);
 const char *fe_last_error(void);
 
