@@ -273,7 +273,9 @@ void with_col16(const Sell &A, F f) {
 // and blocks is one contiguous segment.  FP64: the diagonal block comes from diag and
 // every entry multiplies x_c.  FP32 (difference form): an entry with column c != r
 // multiplies x_c - x_r, an entry with column r (the row-sum entry, or padding with a
-// zero block) multiplies x_r; there is no diagonal term.
+// zero block) multiplies x_r; there is no diagonal term.  Rows past the last node
+// (padding of the final slice) gather their own padding row -- the solver's vectors
+// are allocated for whole slices -- and their result is discarded.
 template <int D, typename T, bool C16 = false>
 __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const Sell &A, const T *__restrict__ val,
                                                   const T *__restrict__ diag, const T *__restrict__ x) {
@@ -1202,7 +1204,9 @@ int dispatch_lanes(int lanes, F &&f) {
 
 int ensure_work(fe_handle_s *h, bool need64, bool need32) {
     SolverWork &w = h->w;
-    size_t n = (size_t)std::max<int64_t>(h->n_dof, 1);
+    // whole SELL slices: the padding rows of the last slice gather their own (unused)
+    // entries
+    size_t n = (size_t)std::max<int64_t>(std::max<int64_t>(h->n_dof, h->n_slices * 32 * h->dim), 1);
     FE_CHECK(dalloc(w.x, n));
     FE_CHECK(dalloc(w.r, n));
     FE_CHECK(dalloc(w.t, n));
