@@ -706,6 +706,8 @@ constexpr int WT_W0 = 0;
 constexpr int WT_L0 = NF * HID;
 
 int gnn_alloc(fe_gnn_s *g, int64_t n) {
+    // whole 32-row SELL slices: spmv64 reads the padding rows of the last slice
+    n = (n + 31) / 32 * 32;
     if (n <= g->n_cap) return FE_OK;
     size_t N = (size_t)n;
     FE_CHECK(dalloc(g->F, N * NF));
