@@ -18,6 +18,42 @@ class Result:
         return self.mesh.elements_groups[0].elements[0].dimension
 
 
+def mesh_arrays(mesh):
+    """(coords (n, 2), conn (E, 3)) of an ArrayMesh or of a mesh of element objects
+    (nodes in ``mesh.nodes`` order, elements in group order)."""
+    if hasattr(mesh, "as_arrays"):
+        return mesh.as_arrays()
+    index = mesh.node_to_index
+    coords = np.array([[float(p[0]), float(p[1])] for p in mesh.nodes], np.float64).reshape(-1, 2)
+    conn = np.array([[index[p] for p in el.points] for g in mesh.elements_groups for el in g.elements],
+                    np.int64).reshape(-1, 3)
+    return coords, conn
+
+
+def write_vtk(file_name, coords, conn, point_scalars=(), point_vectors=()):
+    """Legacy ASCII VTK unstructured grid of linear triangles (cell type 5) with point
+    data: ``point_scalars`` / ``point_vectors`` are (name, (n,) or (n, 2|3)) pairs."""
+    coords = np.asarray(coords, np.float64)
+    conn = np.asarray(conn, np.int64).reshape(-1, 3)
+    n, e = coords.shape[0], conn.shape[0]
+    out = ["# vtk DataFile Version 3.0", "finite element result", "ASCII", "DATASET UNSTRUCTURED_GRID",
+           f"POINTS {n} double"]
+    out += [f"{x!r} {y!r} 0" for x, y in coords[:, :2].tolist()]
+    out += [f"CELLS {e} {4 * e}"] + [f"3 {a} {b} {c}" for a, b, c in conn.tolist()]
+    out += [f"CELL_TYPES {e}"] + ["5"] * e
+    if point_scalars or point_vectors:
+        out.append(f"POINT_DATA {n}")
+    for name, v in point_scalars:
+        out += [f"SCALARS {name} float 1", "LOOKUP_TABLE default"] + [repr(float(t)) for t in np.asarray(v)]
+    for name, v in point_vectors:
+        v = np.asarray(v, np.float64).reshape(n, -1)
+        if v.shape[1] == 2:
+            v = np.hstack([v, np.zeros((n, 1))])
+        out += [f"VECTORS {name} float"] + [f"{a!r} {b!r} {c!r}" for a, b, c in v.tolist()]
+    with open(file_name, "w", encoding="utf-8") as f:
+        f.write("\n".join(out) + "\n")
+
+
 def _system_for(mesh, plane_strain=None, plane_stress=None):
     """A GPU system for a mesh of elasticity or magnetic elements (stiffness only:
     the post-processing reads element matrices and geometry)."""
@@ -65,6 +101,19 @@ class ElasticityResults2D(Result):
     def displacement_vectors_per_node(self):
         n = len(self.mesh.nodes)
         return np.asarray(self.result_vector[: 2 * n], np.float64).reshape(n, 2)
+
+    def generate_vtk_file(self, file_name_output):
+        """The mesh with the displacement as point data, ``Displacement_Magnitude``
+        (scalars) and ``Displacement_Vectors`` (vectors, z = 0), as the reference's
+        writer appends them (results.py:832-871).  The reference copies the mesh part
+        from Gmsh's own VTK export; here the whole file is written."""
+        if file_name_output[-3:] != "vtk":
+            file_name_output += ".vtk"
+        coords, conn = mesh_arrays(self.mesh)
+        u = self.displacement_vectors_per_node
+        write_vtk(file_name_output, coords, conn, point_scalars=[("Displacement_Magnitude", np.hypot(u[:, 0], u[:, 1]))],
+                  point_vectors=[("Displacement_Vectors", u)])
+        return file_name_output
 
 
 class MagneticResults(Result):

@@ -1,0 +1,75 @@
+"""Gmsh 4.1 reader/writer and the VTK writer, on the CPU: a write/read round trip,
+the reference's own beam meshes (scripts/InputFiles/2D, read where the reference
+checkout is present) with the oracle's tip deflection converging to Euler-Bernoulli,
+and the VTK file's sections."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from beam_cases import ANALYTIC_TIP, beam_problem
+from finite_elements_gb300 import gmsh, meshgen
+
+REF_MESHES = sorted(glob.glob("/root/reference/scripts/InputFiles/2D/beam_2d_*.msh"),
+                    key=lambda f: -float(os.path.basename(f)[8:-4]))
+
+
+def test_write_read_round_trip(tmp_path):
+    coords, conn = meshgen.rect_grid(7, 3, 2.0, 1.0)
+    f = tmp_path / "m.msh"
+    gmsh.write_msh(f, coords, conn, node_tags=np.arange(11, 11 + coords.shape[0]))
+    m = gmsh.read_msh(f)
+    np.testing.assert_array_equal(m.coords[:, :2], coords)
+    np.testing.assert_array_equal(m.triangles, conn)
+    assert list(m.group_ptr) == [0, conn.shape[0]] and m.node_tags[0] == 11
+    am = m.array_mesh()
+    assert am.n_nodes == coords.shape[0] and am.n_elements == conn.shape[0]
+
+
+def test_rejects_other_formats(tmp_path):
+    f = tmp_path / "old.msh"
+    f.write_text("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n")
+    with pytest.raises(ValueError):
+        gmsh.read_msh(f)
+
+
+@pytest.mark.skipif(not REF_MESHES, reason="reference mesh files not present")
+def test_reference_beam_meshes_and_euler_bernoulli():
+    from oracle import fe_oracle as O
+    errors = []
+    for f in REF_MESHES:
+        m = gmsh.read_msh(f)
+        p = m.coords[m.triangles][:, :, :2]
+        area = 0.5 * ((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1])
+                      - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
+        assert area.min() > 0 and abs(area.sum() - 10.0) <= 1e-12
+        prob, tip = beam_problem(m.coords, m.triangles)
+        x = np.array(O.solve(prob))
+        errors.append(abs(x[2 * tip + 1] - ANALYTIC_TIP) / abs(ANALYTIC_TIP))
+    assert all(b < a for a, b in zip(errors, errors[1:])), errors
+    assert errors[-1] < 0.01
+
+
+def test_vtk_file(tmp_path):
+    from finite_elements_gb300.mesh import ArrayMesh
+    from finite_elements_gb300.results import ElasticityResults2D
+    coords, conn = meshgen.rect_grid(3, 2, 3.0, 1.0)
+    n = coords.shape[0]
+    u = np.column_stack([np.arange(n) * 1e-3, -np.arange(n) * 2e-3])
+    res = ElasticityResults2D(ArrayMesh(coords, conn), list(u.reshape(-1)) + [0.0, 0.0], False, True)
+    name = res.generate_vtk_file(str(tmp_path / "out"))
+    assert name.endswith(".vtk")
+    lines = open(name).read().splitlines()
+    i = lines.index(f"POINTS {n} double")
+    assert np.allclose([list(map(float, l.split())) for l in lines[i + 1:i + 1 + n]],
+                       np.column_stack([coords, np.zeros(n)]))
+    i = lines.index(f"CELLS {conn.shape[0]} {4 * conn.shape[0]}")
+    assert [list(map(int, l.split())) for l in lines[i + 1:i + 1 + len(conn)]] == [[3, *c] for c in conn.tolist()]
+    assert lines[lines.index(f"CELL_TYPES {len(conn)}") + 1] == "5"
+    i = lines.index("SCALARS Displacement_Magnitude float 1")
+    assert lines[i + 1] == "LOOKUP_TABLE default"
+    np.testing.assert_allclose([float(v) for v in lines[i + 2:i + 2 + n]], np.hypot(u[:, 0], u[:, 1]))
+    i = lines.index("VECTORS Displacement_Vectors float")
+    np.testing.assert_allclose([list(map(float, l.split())) for l in lines[i + 1:i + 1 + n]],
+                               np.column_stack([u, np.zeros(n)]))
