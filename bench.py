@@ -402,6 +402,7 @@ def run_ours(args, dist):
             "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
         },
         "iterations": stats[-1].iterations, "restarts": stats[-1].outer, "learned_x0_used": stats[-1].x0_used,
+        "assemble_ms": stats[-1].assemble_ms, "solve_ms": stats[-1].solve_ms,
         "relres": stats[-1].relres, "err_vs_fp64": err,
         "plain_fp64": {"s_per_solve": plain_s, "iterations": pstats[-1].iterations if pstats else None,
                        "relres": pstats[-1].relres if pstats else None},

@@ -235,4 +235,4 @@ class FiniteElementAnalysis:
         elif st.status == _lib.FE_MAXITER:
             raise SolverConvergenceError(
                 f"PCG stopped after {st.iterations} iterations at relative residual {st.relres:.3e}")
-        return Result(self.mesh, list(x))
+        return Result(self.mesh, list(x), dimension=self.problem().dim)

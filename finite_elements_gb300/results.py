@@ -7,14 +7,19 @@ import numpy as np
 
 class Result:
     """``mesh`` and ``result_vector``: n_nodes*dim displacements (or potentials)
-    followed by one Lagrange multiplier per Dirichlet condition."""
+    followed by one Lagrange multiplier per Dirichlet condition.  ``dimension`` comes
+    from the mesh's first element (the reference's rule) or, for an array mesh, from
+    the analysis that produced the result."""
 
-    def __init__(self, mesh, result_vector):
+    def __init__(self, mesh, result_vector, dimension=None):
         self.mesh = mesh
         self.result_vector = result_vector
+        self._dimension = dimension
 
     @property
     def dimension(self):
+        if self._dimension is not None:
+            return self._dimension
         return self.mesh.elements_groups[0].elements[0].dimension
 
 
