@@ -20,6 +20,7 @@ FE_PLANE_STRESS, FE_PLANE_STRAIN = 1, 2
 FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F, FE_ASSEMBLE_PATTERN = 1, 2, 4, 8
 FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
 FE_PREC_FP64, FE_PREC_MIXED, FE_PREC_MIXED_CG64 = 0, 1, 2
+FE_MODAL_SMALLEST, FE_MODAL_LARGEST = 0, 1
 FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP, FE_SOLVE_X0_IF_BETTER = 1, 2, 4
 
 STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",
@@ -57,6 +58,7 @@ _I32, _I64, _D = C.c_int32, C.c_int64, C.c_double
 _PD, _PI32, _PI64 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
 
 _SIGNATURES = {
+    "fe_modal": ([_P, _I32, _I32, _D, _I32, _I32, _PD, _PD, _PD], C.c_int),
     "fe_set_device": ([_I32], C.c_int),
     "fe_version": ([], C.c_int),
     "fe_status_string": ([C.c_int], C.c_char_p),

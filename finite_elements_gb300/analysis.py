@@ -79,6 +79,21 @@ class FiniteElementAnalysis:
         obj._problem = problem
         return obj
 
+    # ------------------------------------------------------------ modal analysis
+
+    def modal_analysis(self, order, k, steps=0, precision="fp64"):
+        """k eigenpairs of K v = lambda M v on the matrices without conditions
+        (analysis.py:741-796): ``order`` 'smallest' or 'largest'.  Returns (eigenvalues
+        (k,), eigenvectors (k, n_dof)) by increasing eigenvalue, the vectors of unit
+        2-norm.  The GPU runs shift-invert Lanczos ('smallest') or Lanczos on M^-1 K
+        ('largest') in the M inner product.  Unlike the reference's 'smallest' branch,
+        which inverts K although a free body makes it singular, the values are the
+        exact generalized eigenvalues (rigid-body modes at zero) and real."""
+        if order not in ("largest", "smallest"):
+            raise ValueError("Order parameter should be either 'largest' or 'smallest'")
+        vals, vecs, _ = self.system().modal(k, which=order, steps=steps, precision=precision)
+        return vals, vecs
+
     # ------------------------------------------------------------ reference properties
 
     @property

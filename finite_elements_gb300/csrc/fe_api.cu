@@ -440,6 +440,16 @@ int fe_time_spmv(fe_handle h, int32_t precision, int32_t lanes, int32_t reps, do
     return time_spmv(h, precision, lanes, reps, ms_out);
 }
 
+int fe_modal(fe_handle h, int32_t which, int32_t k, double sigma, int32_t steps, int32_t precision,
+             double *eigvals, double *eigvecs, double *residuals) {
+    FE_HANDLE_CHECK(h);
+    if (!eigvals) {
+        set_error("fe_modal: null eigenvalue output");
+        return FE_BAD_INPUT;
+    }
+    return modal(h, which, k, sigma, steps, precision, eigvals, eigvecs, residuals);
+}
+
 int fe_sell_info(fe_handle h, int64_t *n_entries, int32_t *col16) {
     FE_HANDLE_CHECK(h);
     if (!h->sys_ready) {

@@ -472,8 +472,8 @@ __global__ void k_bc_map(int64_t n_bc, const int64_t *__restrict__ dof, int64_t 
 template <int D>
 __global__ void k_eliminate(int64_t nnzb, const int32_t *__restrict__ blk_row,
                             const int32_t *__restrict__ blk_col, const int32_t *__restrict__ bc_of_dof,
-                            const double *__restrict__ kval, double *__restrict__ aval,
-                            float *__restrict__ aval32) {
+                            const double *__restrict__ kval, const double *__restrict__ mval, double ka,
+                            double mb, double *__restrict__ aval, float *__restrict__ aval32) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nnzb;
          s += (int64_t)gridDim.x * blockDim.x) {
         int r = blk_row[s], m = blk_col[s];
@@ -482,7 +482,9 @@ __global__ void k_eliminate(int64_t nnzb, const int32_t *__restrict__ blk_row,
 #pragma unroll
             for (int b = 0; b < D; ++b) {
                 int64_t rd = (int64_t)r * D + a, cd = (int64_t)m * D + b;
-                double v = kval[s * D * D + a * D + b];
+                // the system matrix ka K + mb M (K alone for the static solve)
+                double v = mval ? ka * kval[s * D * D + a * D + b] + mb * mval[s * D * D + a * D + b]
+                                : kval[s * D * D + a * D + b];
                 if (bc_of_dof[rd] >= 0 || bc_of_dof[cd] >= 0) v = (rd == cd) ? 1.0 : 0.0;
                 aval[s * D * D + a * D + b] = v;
                 aval32[s * D * D + a * D + b] = (float)v;
@@ -996,12 +998,18 @@ int assemble_loads(fe_handle_s *h) {
     return FE_OK;
 }
 
-int apply_dirichlet(fe_handle_s *h) {
+int apply_dirichlet(fe_handle_s *h) { return build_system(h, 1.0, 0.0, true); }
+
+// System matrix ka K + mb M (mb != 0 needs M), with the Dirichlet elimination when
+// use_bc, its difference form, block-Jacobi inverses and the SELL copies; the
+// eliminated right-hand side when the loads are assembled.
+int build_system(fe_handle_s *h, double ka, double mb, bool use_bc) {
     cudaStream_t s = h->stream;
     const int D = h->dim;
+    const double *mv = mb != 0.0 ? h->mval.p : nullptr;
     FE_CHECK(dalloc(h->bc_of_dof, (size_t)std::max<int64_t>(h->n_dof, 1)));
     FE_CUDA(cudaMemsetAsync(h->bc_of_dof.p, 0xff, h->n_dof * sizeof(int32_t), s));
-    if (h->n_bc > 0) {
+    if (use_bc && h->n_bc > 0) {
         k_bc_map<<<grid_for(h->n_bc), kThreads, 0, s>>>(h->n_bc, h->bc_dof.p, h->n_dof, h->bc_of_dof.p, h->err.p);
         FE_LAUNCH_CHECK();
     }
@@ -1016,27 +1024,30 @@ int apply_dirichlet(fe_handle_s *h) {
     if (D == 2) {
         if (h->nnzb > 0)
             k_eliminate<2><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
-                                                   h->aval.p, h->aval32.p);
+                                                   mv, ka, mb, h->aval.p, h->aval32.p);
         k_diff_form<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
                                                h->aval32.p);
-        k_eliminated_rhs<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
-                                                    h->bc_val.p, h->kval.p, h->F.p, h->b.p);
+        if (h->f_ready)
+            k_eliminated_rhs<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
+                                                        h->bc_val.p, h->kval.p, h->F.p, h->b.p);
         k_block_jacobi<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
                                                   h->dinv32.p, h->err.p);
     } else {
         if (h->nnzb > 0)
             k_eliminate<1><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
-                                                   h->aval.p, h->aval32.p);
+                                                   mv, ka, mb, h->aval.p, h->aval32.p);
         k_diff_form<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
                                                h->aval32.p);
-        k_eliminated_rhs<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
-                                                    h->bc_val.p, h->kval.p, h->F.p, h->b.p);
+        if (h->f_ready)
+            k_eliminated_rhs<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
+                                                        h->bc_val.p, h->kval.p, h->F.p, h->b.p);
         k_block_jacobi<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
                                                   h->dinv32.p, h->err.p);
     }
     FE_LAUNCH_CHECK();
-    h->launches += (h->n_bc > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0) + 3;
+    h->launches += (use_bc && h->n_bc > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0) + 2 + (h->f_ready ? 1 : 0);
     FE_CHECK(build_sell(h));
+    h->w.lmax[0] = h->w.lmax[1] = 0.0;   // a new matrix: new Chebyshev bounds
     h->sys_ready = true;
     return FE_OK;
 }

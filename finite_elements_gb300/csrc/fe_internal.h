@@ -216,6 +216,7 @@ int assemble_stiffness(fe_handle_s *h);
 int assemble_mass(fe_handle_s *h);
 int assemble_loads(fe_handle_s *h);
 int apply_dirichlet(fe_handle_s *h);
+int build_system(fe_handle_s *h, double ka, double mb, bool use_bc);
 int element_node_factors(fe_handle_s *h, int64_t n, const int64_t *elems_dev, double *out_dev);
 int export_sizes(fe_handle_s *h, int which, int64_t *nrows, int64_t *ncols, int64_t *nnz);
 int export_csr(fe_handle_s *h, int which, int64_t *indptr, int32_t *indices, double *data);
@@ -230,6 +231,9 @@ int exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, int64_t *tota
 
 // solver (fe_solver.cu)
 int solve(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
+// modal analysis (fe_modal.cu)
+int modal(fe_handle_s *h, int which, int k, double sigma, int steps, int precision, double *eigvals,
+          double *eigvecs, double *resid);
 int recover_multipliers(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);
 int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);

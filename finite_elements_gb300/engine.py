@@ -238,6 +238,22 @@ class GpuSystem:
         self.handle.call("fe_post_magnetic", ptr(xa), ptr(field))
         return {"field": field}
 
+    def modal(self, k, which="smallest", sigma=0.0, steps=0, precision="fp64"):
+        """k eigenpairs of K v = lambda M v (no Dirichlet conditions), by increasing
+        eigenvalue: (eigenvalues (k,), eigenvectors (k, n_dof) of unit 2-norm,
+        relative residuals (k,)).  which: "smallest" (shift-invert, sigma < 0 or 0 for
+        an automatic shift) or "largest"."""
+        if which not in ("smallest", "largest"):
+            raise ValueError("Order parameter should be either 'largest' or 'smallest'")
+        lib = _lib.load()
+        self.handle.call("fe_assemble", _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_M)
+        vals, res = np.empty(k), np.empty(k)
+        vecs = np.empty((k, self.prob.n_dof))
+        status = lib.fe_modal(self.handle.h, _lib.FE_MODAL_SMALLEST if which == "smallest" else _lib.FE_MODAL_LARGEST,
+                              int(k), float(sigma), int(steps), PRECISIONS[precision], ptr(vals), ptr(vecs), ptr(res))
+        _lib.check(status, "fe_modal")
+        return vals, vecs, res
+
     def sell_info(self):
         """Stored SELL-32 entries (padding included) and whether the FP32 kernels use
         16-bit column offsets."""

@@ -203,6 +203,22 @@ int fe_profile_kernels(fe_handle h, int32_t enable);
 int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *cheb_n, double *spmv_ms,
                     int64_t *spmv_n);
 
+/* ---- modal analysis (analysis.py:741-796 modal_analysis: scipy eigsh/eigs on
+ * k_matrix_sparse and m_matrix_sparse, i.e. K and M without Dirichlet conditions).
+ * Needs K and M assembled (FE_ASSEMBLE_K | FE_ASSEMBLE_M).  Shift-invert Lanczos in
+ * the M inner product (which = FE_MODAL_SMALLEST: the k smallest eigenvalues of
+ * K v = lambda M v, rigid-body zeros included; sigma < 0 is the shift, 0 or NaN picks
+ * one) or Lanczos on M^-1 K (FE_MODAL_LARGEST).  Each step solves with the library's
+ * PCG (precision FE_PREC_FP64 or FE_PREC_MIXED_CG64).  steps: Lanczos steps (0 =
+ * default).  Output, by increasing eigenvalue: eigvals_host[k]; eigvecs_host[k][n_dof]
+ * (unit 2-norm) or NULL; residuals_host[k] = ||K x - lambda M x|| /
+ * (||K x|| + |lambda| ||M x||) or NULL.  Leaves the static system to be rebuilt by the
+ * next fe_assemble. */
+#define FE_MODAL_SMALLEST 0
+#define FE_MODAL_LARGEST  1
+int fe_modal(fe_handle h, int32_t which, int32_t k, double sigma, int32_t steps, int32_t precision,
+             double *eigvals_host, double *eigvecs_host, double *residuals_host);
+
 /* ---- post-processing of a solution (results.py:809-830 strain/stress, :769-781 and
  * elements.py:275-292 energy, results.py:121-152 magnetic field).  u_host / a_host:
  * n_dof values, or NULL for the handle's last solution.  Per element: strain and

@@ -383,3 +383,38 @@ def magnetic_field(prob: Problem, a):
     bx = (ff[:, :, 2] * A).sum(axis=1)
     by = -(ff[:, :, 1] * A).sum(axis=1)
     return np.stack([bx, by], axis=1)
+
+
+def modal_analysis(prob: Problem, order, k):
+    """The reference's modal_analysis (analysis.py:741-796) as written: 'largest' is
+    eigsh(K, M=M, which='LM', k) on the matrices without conditions; 'smallest' is
+    eigs(inv(K_dense) M, which='LM', k) and returns 1 / eigenvalues (complex).  K has
+    no conditions here, so for a body that is free to move it is singular and the
+    'smallest' branch inverts it anyway (scipy warns of an ill-conditioned matrix)."""
+    import scipy.linalg
+    K = k_matrix_sparse(prob)
+    M = m_matrix_sparse(prob)
+    if order == "largest":
+        vals, vecs = spla.eigsh(A=K, M=M, which="LM", k=k)
+        return vals, vecs.T
+    if order == "smallest":
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            kinv = sp.csc_matrix(scipy.linalg.inv(K.toarray()))
+        vals, vecs = spla.eigs(kinv @ M, which="LM", k=k)
+        return 1 / vals, vecs.T
+    raise ValueError("Order parameter should be either 'largest' or 'smallest'")
+
+
+def generalized_eigenpairs(prob: Problem, k, which="smallest", sigma=-1.0):
+    """The exact k smallest (shift-invert about sigma < 0) or largest eigenpairs of
+    K v = lambda M v, by increasing eigenvalue: (values, vectors (k, n) of unit 2-norm)."""
+    K = k_matrix_sparse(prob)
+    M = m_matrix_sparse(prob)
+    if which == "smallest":
+        vals, vecs = spla.eigsh(K, k=k, M=M, sigma=sigma, which="LM")
+    else:
+        vals, vecs = spla.eigsh(K, k=k, M=M, which="LM")
+    order = np.argsort(vals)
+    vecs = vecs[:, order].T
+    return vals[order], vecs / np.linalg.norm(vecs, axis=1, keepdims=True)
