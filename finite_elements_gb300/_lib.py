@@ -58,7 +58,7 @@ _I32, _I64, _D = C.c_int32, C.c_int64, C.c_double
 _PD, _PI32, _PI64 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
 
 _SIGNATURES = {
-    "fe_modal": ([_P, _I32, _I32, _D, _I32, _I32, _PD, _PD, _PD], C.c_int),
+    "fe_modal": ([_P, _I32, _I32, _D, _I32, _I32, _P, _P, _P], C.c_int),
     "fe_set_device": ([_I32], C.c_int),
     "fe_version": ([], C.c_int),
     "fe_status_string": ([C.c_int], C.c_char_p),

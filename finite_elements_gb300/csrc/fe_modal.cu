@@ -12,7 +12,9 @@
 // vector, twice (classical Gram-Schmidt twice), which keeps the projected matrix
 // tridiagonal to rounding.  The small tridiagonal matrix is diagonalized on the host
 // (cyclic Jacobi rotations); Ritz vectors are formed on the device and their true
-// residuals ||K x - lambda M x|| / (||K x|| + |lambda| ||M x||) reported.
+// residuals ||K x - lambda M x|| / (||K x|| + max(|lambda|, |lambda|_max) ||M x||)
+// reported (|lambda|_max over the k computed: a rigid-body zero is measured against
+// the spectrum's scale, not against its own rounding).
 #include <math.h>
 #include <string.h>
 
@@ -373,6 +375,10 @@ int modal(fe_handle_s *h, int which, int k, double sigma, int steps, int precisi
     std::vector<int> by_lambda(k);
     std::iota(by_lambda.begin(), by_lambda.end(), 0);
     std::sort(by_lambda.begin(), by_lambda.end(), [&](int a, int b) { return lam[a] < lam[b]; });
+    // eigenvalue scale of the residuals: a zero (rigid-body) eigenvalue is measured
+    // against the largest computed one instead of against its own rounding
+    double lam_ref = 0.0;
+    for (int i = 0; i < k; ++i) lam_ref = std::max(lam_ref, fabs(lam[i]));
     std::vector<double> y(mm);
     for (int t = 0; t < k && rc == FE_OK; ++t) {
         const int i = by_lambda[t];
@@ -399,7 +405,7 @@ int modal(fe_handle_s *h, int which, int k, double sigma, int steps, int precisi
         rc = md.dot(Kx.p, Kx.p, &rr);
         if (rc != FE_OK) break;
         eigvals[t] = lam[i];
-        if (resid) resid[t] = sqrt(rr) / (sqrt(kk) + fabs(lam[i]) * sqrt(mmx) + 1e-300);
+        if (resid) resid[t] = sqrt(rr) / (sqrt(kk) + std::max(fabs(lam[i]), lam_ref) * sqrt(mmx) + 1e-300);
         if (eigvecs)
             FE_CUDA(cudaMemcpyAsync(eigvecs + (size_t)t * n, w.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     }

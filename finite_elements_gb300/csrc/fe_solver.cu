@@ -1611,6 +1611,12 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
 // ---------------------------------------------------------------- entry points
 
 int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
+    if (!h->sys_ready && h->k_ready && h->f_ready) {
+        // K and F are assembled but the system matrix was replaced (fe_modal)
+        h->singular = false;
+        FE_CHECK(apply_dirichlet(h));
+        FE_CHECK(check_error_word(h, "fe_solve"));
+    }
     if (!h->sys_ready) {
         set_error("fe_solve: the system is not assembled (call fe_assemble with K and F)");
         return FE_NOT_READY;

@@ -212,8 +212,8 @@ int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *ch
  * PCG (precision FE_PREC_FP64 or FE_PREC_MIXED_CG64).  steps: Lanczos steps (0 =
  * default).  Output, by increasing eigenvalue: eigvals_host[k]; eigvecs_host[k][n_dof]
  * (unit 2-norm) or NULL; residuals_host[k] = ||K x - lambda M x|| /
- * (||K x|| + |lambda| ||M x||) or NULL.  Leaves the static system to be rebuilt by the
- * next fe_assemble. */
+ * (||K x|| + max(|lambda|, |lambda|max) ||M x||) or NULL, |lambda|max the largest of
+ * the k.  The static system (K with the conditions) is rebuilt by the next fe_solve. */
 #define FE_MODAL_SMALLEST 0
 #define FE_MODAL_LARGEST  1
 int fe_modal(fe_handle h, int32_t which, int32_t k, double sigma, int32_t steps, int32_t precision,

@@ -67,6 +67,22 @@ def test_struct_layouts_match_the_header(tmp_path):
             assert int(got[f"{tag} {name}"]) == getattr(cls, name).offset, (tag, name)
 
 
+def test_bindings_accept_the_engine_argument_types():
+    """ctypes converts arguments before the library runs: calls with the argument kinds
+    the engine passes (numpy arrays through _lib.ptr) on a null handle must reach the
+    library and come back with FE_BAD_INPUT, not fail in the conversion."""
+    import ctypes
+    from finite_elements_gb300 import _lib
+    lib = _lib.load()
+    a = np.zeros(8)
+    assert lib.fe_modal(None, 0, 1, 0.0, 0, 0, _lib.ptr(a), _lib.ptr(a), _lib.ptr(a)) == _lib.FE_BAD_INPUT
+    ne, c16 = ctypes.c_int64(), ctypes.c_int32()
+    assert lib.fe_sell_info(None, ne, c16) == _lib.FE_BAD_INPUT
+    cm, cn = ctypes.c_double(), ctypes.c_int64()
+    assert lib.fe_profile_read(None, 2, ctypes.byref(cm), ctypes.byref(cn), ctypes.byref(cm),
+                               ctypes.byref(cn)) == _lib.FE_BAD_INPUT
+
+
 def test_library_calls_without_gpu_fail_loudly():
     """No CPU fallback: on a machine without a CUDA device the first call fails with
     a CUDA status."""
