@@ -15,7 +15,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libfe_gb300.so")
 
 FE_OK, FE_MAXITER, FE_BREAKDOWN, FE_NONFINITE, FE_BAD_INPUT, FE_CUDA_ERR, FE_NOT_READY = range(7)
-FE_KIND_ELASTIC_TRI, FE_KIND_MAGNETIC_TRI = 1, 2
+FE_KIND_ELASTIC_TRI, FE_KIND_MAGNETIC_TRI, FE_KIND_ELASTIC_TET = 1, 2, 3
 FE_PLANE_STRESS, FE_PLANE_STRAIN = 1, 2
 FE_ASSEMBLE_K, FE_ASSEMBLE_M, FE_ASSEMBLE_F, FE_ASSEMBLE_PATTERN = 1, 2, 4, 8
 FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
@@ -155,8 +155,9 @@ class Handle:
     def __init__(self, kind, coords, conn):
         lib = load()
         self._lib = lib
-        coords = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 2)
-        conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 3)
+        tet = kind == FE_KIND_ELASTIC_TET
+        coords = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3 if tet else 2)
+        conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 4 if tet else 3)
         h = C.c_void_p()
         check(lib.fe_mesh_create(kind, coords.shape[0], conn.shape[0], ptr(coords), ptr(conn),
                                  C.byref(h)), "fe_mesh_create")

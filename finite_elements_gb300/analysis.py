@@ -24,7 +24,7 @@ import scipy.sparse.linalg as spla
 
 from .engine import GpuSystem, check_plane_flags
 from .mesh import ArrayMesh
-from .problem import ELASTIC, MAGNETIC, ElementLoadSet, Problem
+from .problem import ELASTIC, ELASTIC3D, MAGNETIC, ElementLoadSet, Problem
 from .results import Result
 
 DEFAULT_SOLVER = {"precision": "fp64", "tol": 1e-14, "accept_stagnation": True, "cheb_degree": 0}
@@ -38,9 +38,9 @@ def _element_kind(element):
     if hasattr(element, "mu_total"):
         return MAGNETIC
     if hasattr(element, "elasticity_modulus"):
-        return ELASTIC
+        return ELASTIC3D if len(element.points) == 4 else ELASTIC
     raise NotImplementedError(f"element type {type(element).__name__} is not a linear triangle "
-                              "of the GPU path")
+                              "or tetrahedron of the GPU path")
 
 
 class FiniteElementAnalysis:
@@ -126,12 +126,14 @@ class FiniteElementAnalysis:
         mesh = self.mesh
         nodes = mesh.nodes
         index = mesh.node_to_index
-        coords = np.array([[float(p[0]), float(p[1])] for p in nodes], dtype=np.float64).reshape(-1, 2)
         elements = [el for g in mesh.elements_groups for el in g.elements]
         if not elements:
             raise ValueError("the mesh has no element")
         kind = _element_kind(elements[0])
-        conn = np.array([[index[p] for p in el.points] for el in elements], dtype=np.int32).reshape(-1, 3)
+        cdim, npe = (3, 4) if kind == ELASTIC3D else (2, 3)
+        coords = np.array([[float(p[k]) for k in range(cdim)] for p in nodes],
+                          dtype=np.float64).reshape(-1, cdim)
+        conn = np.array([[index[p] for p in el.points] for el in elements], dtype=np.int32).reshape(-1, npe)
         by_id = {id(el): k for k, el in enumerate(elements)}
         by_points = {}
 
@@ -146,7 +148,7 @@ class FiniteElementAnalysis:
             return k
 
         kw = {}
-        if kind == ELASTIC:
+        if kind in (ELASTIC, ELASTIC3D):
             kw = dict(E=[el.elasticity_modulus for el in elements],
                       nu=[el.poisson_ratio for el in elements],
                       thickness=[getattr(el, "thickness", 1.0) for el in elements],
@@ -182,7 +184,7 @@ class FiniteElementAnalysis:
     def system(self) -> GpuSystem:
         if self._system is None:
             prob = self.problem()
-            if prob.kind == ELASTIC:
+            if prob.elastic:
                 check_plane_flags(self.plane_strain, self.plane_stress)
                 prob.plane_strain, prob.plane_stress = self.plane_strain, self.plane_stress
             self._system = GpuSystem(prob)
@@ -206,7 +208,7 @@ class FiniteElementAnalysis:
         return self.system().k_matrix_sparse()
 
     def m_matrix_sparse(self):
-        if self.problem().kind != ELASTIC:
+        if not self.problem().elastic:
             raise AttributeError("'MagneticElement2D' object has no attribute 'elementary_mass_matrix'")
         return self.system().m_matrix_sparse()
 

@@ -89,17 +89,21 @@ int fe_mesh_create(int32_t kind, int64_t n_nodes, int64_t n_elem, const double *
         return FE_BAD_INPUT;
     }
     *out = nullptr;
-    if (kind != FE_KIND_ELASTIC_TRI && kind != FE_KIND_MAGNETIC_TRI) {
+    if (kind != FE_KIND_ELASTIC_TRI && kind != FE_KIND_MAGNETIC_TRI && kind != FE_KIND_ELASTIC_TET) {
         set_error("fe_mesh_create: unknown element kind");
         return FE_BAD_INPUT;
     }
-    if (n_nodes < 0 || n_elem < 0 || n_nodes > 0x3fffffffLL || n_elem > 0x2aaaaaaaLL) {
+    const int npe = kind == FE_KIND_ELASTIC_TET ? 4 : 3;
+    // incidence codes element*npe + local vertex are int32
+    if (n_nodes < 0 || n_elem < 0 || n_nodes > 0x3fffffffLL || n_elem * npe > 0x7fffffffLL) {
         set_error("fe_mesh_create: sizes out of range");
         return FE_BAD_INPUT;
     }
     fe_handle_s *h = new fe_handle_s();
     h->kind = kind;
-    h->dim = kind == FE_KIND_ELASTIC_TRI ? 2 : 1;
+    h->dim = kind == FE_KIND_ELASTIC_TRI ? 2 : kind == FE_KIND_ELASTIC_TET ? 3 : 1;
+    h->npe = npe;
+    h->cdim = kind == FE_KIND_ELASTIC_TET ? 3 : 2;
     h->n_nodes = n_nodes;
     h->n_elem = n_elem;
     h->n_dof = n_nodes * h->dim;
@@ -118,8 +122,8 @@ int fe_mesh_create(int32_t kind, int64_t n_nodes, int64_t n_elem, const double *
     int st = dalloc(h->err, 1);
     if (st) return fail(st);
     if (cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream) != cudaSuccess) return fail(FE_CUDA_ERR);
-    if ((st = upload(h->coords, coords_host, n_nodes * 2, h->stream))) return fail(st);
-    if ((st = upload(h->conn, conn_host, n_elem * 3, h->stream))) return fail(st);
+    if ((st = upload(h->coords, coords_host, n_nodes * h->cdim, h->stream))) return fail(st);
+    if ((st = upload(h->conn, conn_host, n_elem * npe, h->stream))) return fail(st);
     if ((st = validate_mesh(h))) return fail(st);
     *out = h;
     return FE_OK;
@@ -150,7 +154,7 @@ int fe_destroy(fe_handle h) {
 int fe_set_elastic_materials(fe_handle h, const double *E, const double *nu, const double *thickness,
                              const double *rho, int32_t plane_mode) {
     FE_HANDLE_CHECK(h);
-    if (h->kind != FE_KIND_ELASTIC_TRI) {
+    if (h->kind != FE_KIND_ELASTIC_TRI && h->kind != FE_KIND_ELASTIC_TET) {
         set_error("fe_set_elastic_materials: not an elasticity mesh");
         return FE_BAD_INPUT;
     }
@@ -160,7 +164,7 @@ int fe_set_elastic_materials(fe_handle h, const double *E, const double *nu, con
     }
     FE_CHECK(upload(h->E, E, h->n_elem, h->stream));
     FE_CHECK(upload(h->nu, nu, h->n_elem, h->stream));
-    FE_CHECK(upload(h->thick, thickness, h->n_elem, h->stream));
+    if (h->kind == FE_KIND_ELASTIC_TRI || thickness) FE_CHECK(upload(h->thick, thickness, h->n_elem, h->stream));
     h->have_rho = rho != nullptr;
     if (rho) FE_CHECK(upload(h->rho, rho, h->n_elem, h->stream));
     h->plane = plane_mode;
@@ -203,6 +207,11 @@ int fe_set_element_loads(fe_handle h, int64_t n_sets, const int64_t *set_ptr, co
     FE_HANDLE_CHECK(h);
     if (n_sets < 0 || (n_sets > 0 && !set_ptr)) {
         set_error("fe_set_element_loads: bad set list");
+        return FE_BAD_INPUT;
+    }
+    if (n_sets > 0 && h->kind == FE_KIND_ELASTIC_TET) {
+        set_error("fe_set_element_loads: element loads need element_to_node_factors and an area, which the "
+                  "reference defines for triangles only");
         return FE_BAD_INPUT;
     }
     if (n_sets == 0) {
@@ -253,6 +262,10 @@ int fe_set_dirichlet(fe_handle h, int64_t n_bc, const int64_t *dof, const double
 
 int fe_element_node_factors(fe_handle h, int64_t n, const int64_t *elements, double *factors) {
     FE_HANDLE_CHECK(h);
+    if (h->kind == FE_KIND_ELASTIC_TET) {
+        set_error("fe_element_node_factors: the reference defines element_to_node_factors for triangles only");
+        return FE_BAD_INPUT;
+    }
     if (n <= 0) return FE_OK;
     DBuf<int64_t> el;
     DBuf<double> out;

@@ -11,19 +11,12 @@
 #include <algorithm>
 #include <vector>
 
+#include "fe_element.cuh"
 #include "fe_internal.h"
 
 namespace fe {
 namespace {
 
-// ---------------------------------------------------------------- rounding helpers
-// Element arithmetic is written with explicit round-to-nearest operations in the
-// reference's evaluation order, so that no multiply-add is contracted and the
-// element values round exactly as the reference's numpy expressions do.
-__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
 
 struct Tri {
     double x1, y1, x2, y2, x3, y3;
@@ -93,8 +86,8 @@ __global__ void k_validate_conn(const int32_t *__restrict__ conn, int64_t n3, in
 }
 
 // ---------------------------------------------------------------- pattern build
-// Counting sort of the 3E (element, local vertex) incidences by node, a per-node sort
-// of each incidence list (element order), then per node the sorted set of nodes
+// Counting sort of the npe*E (element, local vertex) incidences by node, a per-node
+// sort of each incidence list (element order), then per node the sorted set of nodes
 // sharing an element with it: the block columns of that node's block row.
 
 __global__ void k_count_incidence(const int32_t *__restrict__ conn, int64_t n3, int32_t *cnt) {
@@ -110,7 +103,7 @@ __global__ void k_fill_incidence(const int32_t *__restrict__ conn, int64_t n3,
          k += (int64_t)gridDim.x * blockDim.x) {
         int node = conn[k];
         int pos = inc_ptr[node] + atomicAdd(&cursor[node], 1);
-        inc[pos] = (int32_t)k;   // element*3 + local vertex
+        inc[pos] = (int32_t)k;   // element*npe + local vertex
     }
 }
 
@@ -127,38 +120,36 @@ __device__ __forceinline__ void insertion_sort(int32_t *a, int n) {
 }
 
 // Sort each node's incidence list, gather the nodes of its elements into cand[]
-// (3 per incidence), sort them and count the distinct ones.
-__global__ void k_node_neighbours(int64_t n_nodes, const int32_t *__restrict__ conn,
+// (npe per incidence), sort them and count the distinct ones.
+__global__ void k_node_neighbours(int64_t n_nodes, int npe, const int32_t *__restrict__ conn,
                                   const int32_t *__restrict__ inc_ptr, int32_t *__restrict__ inc,
                                   int32_t *__restrict__ cand, int32_t *__restrict__ nb_cnt) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
          r += (int64_t)gridDim.x * blockDim.x) {
         int s = inc_ptr[r], e = inc_ptr[r + 1], d = e - s;
         insertion_sort(inc + s, d);
-        int32_t *c = cand + 3 * (int64_t)s;
+        int32_t *c = cand + npe * (int64_t)s;
         for (int t = 0; t < d; ++t) {
-            int el = inc[s + t] / 3;
-            c[3 * t] = conn[3 * el];
-            c[3 * t + 1] = conn[3 * el + 1];
-            c[3 * t + 2] = conn[3 * el + 2];
+            int el = inc[s + t] / npe;
+            for (int j = 0; j < npe; ++j) c[npe * t + j] = conn[(int64_t)npe * el + j];
         }
-        insertion_sort(c, 3 * d);
+        insertion_sort(c, npe * d);
         int u = 0;
-        for (int t = 0; t < 3 * d; ++t)
+        for (int t = 0; t < npe * d; ++t)
             if (t == 0 || c[t] != c[t - 1]) ++u;
         nb_cnt[r] = u;
     }
 }
 
-__global__ void k_write_pattern(int64_t n_nodes, const int32_t *__restrict__ inc_ptr,
+__global__ void k_write_pattern(int64_t n_nodes, int npe, const int32_t *__restrict__ inc_ptr,
                                 const int32_t *__restrict__ cand, const int32_t *__restrict__ blk_ptr,
                                 int32_t *__restrict__ blk_col, int32_t *__restrict__ blk_row) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
          r += (int64_t)gridDim.x * blockDim.x) {
         int s = inc_ptr[r], d = inc_ptr[r + 1] - s;
-        const int32_t *c = cand + 3 * (int64_t)s;
+        const int32_t *c = cand + npe * (int64_t)s;
         int o = blk_ptr[r];
-        for (int t = 0; t < 3 * d; ++t)
+        for (int t = 0; t < npe * d; ++t)
             if (t == 0 || c[t] != c[t - 1]) {
                 blk_col[o] = c[t];
                 blk_row[o] = (int32_t)r;
@@ -267,6 +258,69 @@ __global__ void k_mass_scale(int64_t n_elem, const double *__restrict__ coords,
     }
 }
 
+// Tetrahedron elasticity Ke = V (B^T D) B (elements.py:808-827) with the isotropic D
+// of elements.py:779-796: coef = E/((1+nu)(1-2nu)), normal diagonal coef*(1-nu),
+// normal off-diagonal coef*nu, shear coef*((1-2nu)/2).  The zeros of B and D add
+// exact zeros, so entry (3i+a, 3j+b) is a sum of two or three products of row a of
+// B_i^T D with column b of B_j.  32 elements per block are staged in shared memory
+// (144 doubles each) and written back as one contiguous range.
+constexpr int kTetBlock = 32;
+
+__global__ void __launch_bounds__(kTetBlock)
+k_elastic_tet_ke(int64_t n_elem, const double *__restrict__ coords, const int32_t *__restrict__ conn,
+                 const double *__restrict__ E, const double *__restrict__ nu, double *__restrict__ ke_out,
+                 int *err) {
+    __shared__ double tile[kTetBlock * 144];
+    for (int64_t base = (int64_t)blockIdx.x * kTetBlock; base < n_elem; base += (int64_t)gridDim.x * kTetBlock) {
+        const int64_t e = base + threadIdx.x;
+        double *my = tile + threadIdx.x * 144;
+        if (e < n_elem) {
+            const TetGrad t = tet_gradients(coords, conn, e);
+            const double Em = E[e], v = nu[e];
+            const double coef = dvd(Em, mul(add(1.0, v), sub(1.0, mul(2.0, v))));
+            const double cn = mul(coef, sub(1.0, v)), cl = mul(coef, v);
+            const double cg = mul(coef, dvd(sub(1.0, mul(2.0, v)), 2.0));
+            if (!t.finite || !isfinite(t.vol) || !isfinite(cn) || !isfinite(cg)) atomicOr(err, ERR_NONFINITE);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double gx = t.g[i][0], gy = t.g[i][1], gz = t.g[i][2];
+                const double ux = mul(gx, cn), vy = mul(gy, cn), wz = mul(gz, cn);
+                const double lx = mul(gx, cl), ly = mul(gy, cl), lz = mul(gz, cl);
+                const double sx = mul(gx, cg), sy = mul(gy, cg), sz = mul(gz, cg);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const double hx = t.g[j][0], hy = t.g[j][1], hz = t.g[j][2];
+                    double *row0 = my + (3 * i) * 12 + 3 * j, *row1 = row0 + 12, *row2 = row1 + 12;
+                    row0[0] = mul(t.vol, add(add(mul(ux, hx), mul(sy, hy)), mul(sz, hz)));
+                    row0[1] = mul(t.vol, add(mul(lx, hy), mul(sy, hx)));
+                    row0[2] = mul(t.vol, add(mul(lx, hz), mul(sz, hx)));
+                    row1[0] = mul(t.vol, add(mul(ly, hx), mul(sx, hy)));
+                    row1[1] = mul(t.vol, add(add(mul(vy, hy), mul(sx, hx)), mul(sz, hz)));
+                    row1[2] = mul(t.vol, add(mul(ly, hz), mul(sz, hy)));
+                    row2[0] = mul(t.vol, add(mul(lz, hx), mul(sx, hz)));
+                    row2[1] = mul(t.vol, add(mul(lz, hy), mul(sy, hz)));
+                    row2[2] = mul(t.vol, add(add(mul(wz, hz), mul(sy, hy)), mul(sx, hx)));
+                }
+            }
+        }
+        __syncthreads();
+        const int64_t cnt = min((int64_t)kTetBlock, n_elem - base) * 144;
+        double *dst = ke_out + base * 144;
+        for (int64_t k = threadIdx.x; k < cnt; k += kTetBlock) dst[k] = tile[k];
+        __syncthreads();
+    }
+}
+
+// Tetrahedron mass scale (rho * V) / 20 of elements.py:845-858; Me = scale * P12,
+// P12 block (i, j) = (i == j ? 2 : 1) * I_3.
+__global__ void k_mass_scale_tet(int64_t n_elem, const double *__restrict__ coords,
+                                 const int32_t *__restrict__ conn, const double *__restrict__ rho,
+                                 double *__restrict__ out) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem;
+         e += (int64_t)gridDim.x * blockDim.x)
+        out[e] = dvd(mul(rho[e], tet_gradients(coords, conn, e).vol), 20.0);
+}
+
 __global__ void k_node_factors(int64_t n, const int64_t *__restrict__ elems, int64_t n_elem,
                                const double *__restrict__ coords, const int32_t *__restrict__ conn,
                                double *__restrict__ out, int *err) {
@@ -290,12 +344,12 @@ __global__ void k_node_factors(int64_t n, const int64_t *__restrict__ elems, int
 // element order and add block (i, j) of every element whose vertex j is m.  The sum
 // runs in element order, as the reference's dict merge does (analysis.py:390-395),
 // with no atomics: the result is the same on every run.
-template <int D>
+template <int D, int NPE>
 __global__ void k_reduce_stiffness(int64_t nnzb, const int32_t *__restrict__ blk_row,
                                    const int32_t *__restrict__ blk_col, const int32_t *__restrict__ inc_ptr,
                                    const int32_t *__restrict__ inc, const int32_t *__restrict__ conn,
                                    const double *__restrict__ ke, double *__restrict__ kval) {
-    constexpr int NL = 3 * D;
+    constexpr int NL = NPE * D;
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nnzb;
          s += (int64_t)gridDim.x * blockDim.x) {
         int r = blk_row[s], m = blk_col[s];
@@ -305,10 +359,10 @@ __global__ void k_reduce_stiffness(int64_t nnzb, const int32_t *__restrict__ blk
         int a0 = inc_ptr[r], a1 = inc_ptr[r + 1];
         for (int t = a0; t < a1; ++t) {
             int code = inc[t];
-            int e = code / 3, i = code - 3 * e;
+            int e = code / NPE, i = code - NPE * e;
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                if (conn[3 * e + j] == m) {
+            for (int j = 0; j < NPE; ++j) {
+                if (conn[NPE * (int64_t)e + j] == m) {
                     const double *blk = ke + (int64_t)e * NL * NL + (i * D) * NL + j * D;
 #pragma unroll
                     for (int a = 0; a < D; ++a)
@@ -322,7 +376,9 @@ __global__ void k_reduce_stiffness(int64_t nnzb, const int32_t *__restrict__ blk
     }
 }
 
-// Mass blocks: Me block (i, j) = scale * (i == j ? 2 : 1) * I_2 (elements.py:514-519).
+// Mass blocks: Me block (i, j) = scale * (i == j ? 2 : 1) * I_D (elements.py:514-519,
+// :830-843).
+template <int D, int NPE>
 __global__ void k_reduce_mass(int64_t nnzb, const int32_t *__restrict__ blk_row,
                               const int32_t *__restrict__ blk_col, const int32_t *__restrict__ inc_ptr,
                               const int32_t *__restrict__ inc, const int32_t *__restrict__ conn,
@@ -334,16 +390,16 @@ __global__ void k_reduce_mass(int64_t nnzb, const int32_t *__restrict__ blk_row,
         int a0 = inc_ptr[r], a1 = inc_ptr[r + 1];
         for (int t = a0; t < a1; ++t) {
             int code = inc[t];
-            int e = code / 3, i = code - 3 * e;
+            int e = code / NPE, i = code - NPE * e;
 #pragma unroll
-            for (int j = 0; j < 3; ++j)
-                if (conn[3 * e + j] == m) diag = __dadd_rn(diag, __dmul_rn(scale[e], i == j ? 2.0 : 1.0));
+            for (int j = 0; j < NPE; ++j)
+                if (conn[NPE * (int64_t)e + j] == m) diag = __dadd_rn(diag, __dmul_rn(scale[e], i == j ? 2.0 : 1.0));
         }
-        // the off-diagonal entries of the 2x2 block are sums of exact zeros
-        mval[s * 4 + 0] = diag;
-        mval[s * 4 + 1] = 0.0;
-        mval[s * 4 + 2] = 0.0;
-        mval[s * 4 + 3] = diag;
+        // the off-diagonal entries of the block are sums of exact zeros
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = 0; b < D; ++b) mval[s * D * D + a * D + b] = a == b ? diag : 0.0;
     }
 }
 
@@ -574,6 +630,31 @@ __device__ __forceinline__ int find_col(const int32_t *__restrict__ cols, int lo
     return lo;
 }
 
+// Inverse of one D x D block (row-major): 1/v, the 2 x 2 adjugate formula, or the
+// 3 x 3 cofactors over the determinant.  False when the block is singular.
+template <int D>
+__device__ __forceinline__ bool invert_block(const double *a, double *o) {
+    if constexpr (D == 1) {
+        const double inv = 1.0 / a[0];
+        o[0] = inv;
+        return a[0] != 0.0 && isfinite(inv);
+    } else if constexpr (D == 2) {
+        const double det = a[0] * a[3] - a[1] * a[2];
+        const double id = 1.0 / det;
+        o[0] = a[3] * id, o[1] = -a[1] * id, o[2] = -a[2] * id, o[3] = a[0] * id;
+        return det != 0.0 && isfinite(id);
+    } else {
+        const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8];
+        const double c02 = a[3] * a[7] - a[4] * a[6];
+        const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+        const double id = 1.0 / det;
+        o[0] = c00 * id, o[1] = (a[2] * a[7] - a[1] * a[8]) * id, o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+        o[3] = c01 * id, o[4] = (a[0] * a[8] - a[2] * a[6]) * id, o[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+        o[6] = c02 * id, o[7] = (a[1] * a[6] - a[0] * a[7]) * id, o[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+        return det != 0.0 && isfinite(id);
+    }
+}
+
 // Inverse of every diagonal block of A (node-block Jacobi).
 template <int D>
 __global__ void k_block_jacobi(int64_t n_nodes, const int32_t *__restrict__ blk_ptr,
@@ -584,38 +665,18 @@ __global__ void k_block_jacobi(int64_t n_nodes, const int32_t *__restrict__ blk_
         int lo = blk_ptr[r], hi = blk_ptr[r + 1];
         int s = find_col(blk_col, lo, hi, (int)r);
         bool found = s < hi && blk_col[s] == (int)r;
-        if (D == 1) {
-            double v = found ? aval[s] : 0.0;
-            double inv = 1.0 / v;
-            if (!found || v == 0.0 || !isfinite(inv)) {
-                atomicOr(err, ERR_SINGULAR_BLOCK);
-                inv = 0.0;
-            }
-            dinv[r] = inv;
-            dinv32[r] = (float)inv;
-        } else {
-            double a = 0, b = 0, c = 0, d = 0;
-            if (found) {
-                a = aval[(int64_t)s * 4];
-                b = aval[(int64_t)s * 4 + 1];
-                c = aval[(int64_t)s * 4 + 2];
-                d = aval[(int64_t)s * 4 + 3];
-            }
-            double det = a * d - b * c;
-            double id = 1.0 / det;
-            double i00 = d * id, i01 = -b * id, i10 = -c * id, i11 = a * id;
-            if (!found || det == 0.0 || !isfinite(id)) {
-                atomicOr(err, ERR_SINGULAR_BLOCK);
-                i00 = i01 = i10 = i11 = 0.0;
-            }
-            dinv[r * 4] = i00;
-            dinv[r * 4 + 1] = i01;
-            dinv[r * 4 + 2] = i10;
-            dinv[r * 4 + 3] = i11;
-            dinv32[r * 4] = (float)i00;
-            dinv32[r * 4 + 1] = (float)i01;
-            dinv32[r * 4 + 2] = (float)i10;
-            dinv32[r * 4 + 3] = (float)i11;
+        double a[D * D], o[D * D];
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) a[k] = found ? aval[(int64_t)s * D * D + k] : 0.0;
+        if (!invert_block<D>(a, o) || !found) {
+            atomicOr(err, ERR_SINGULAR_BLOCK);
+#pragma unroll
+            for (int k = 0; k < D * D; ++k) o[k] = 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) {
+            dinv[r * D * D + k] = o[k];
+            dinv32[r * D * D + k] = (float)o[k];
         }
     }
 }
@@ -851,7 +912,7 @@ int validate_mesh(fe_handle_s *h) {
     FE_CHECK(dalloc(mx, 1));
     int init = -1;
     FE_CUDA(cudaMemcpyAsync(mx.p, &init, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    int64_t n3 = h->n_elem * 3;
+    int64_t n3 = h->n_elem * h->npe;
     if (n3 > 0) {
         k_validate_conn<<<grid_for(n3), kThreads, 0, h->stream>>>(h->conn.p, n3, h->n_nodes, h->err.p, mx.p);
         FE_LAUNCH_CHECK();
@@ -868,11 +929,12 @@ int validate_mesh(fe_handle_s *h) {
 int build_pattern(fe_handle_s *h) {
     if (h->pattern_ready) return FE_OK;
     cudaStream_t s = h->stream;
-    int64_t n = h->n_nodes, n3 = h->n_elem * 3;
+    const int npe = h->npe;
+    int64_t n = h->n_nodes, n3 = h->n_elem * npe;
     FE_CHECK(dalloc(h->counts, (size_t)n + 1));
     FE_CHECK(dalloc(h->inc_ptr, (size_t)n + 1));
     FE_CHECK(dalloc(h->inc, (size_t)std::max<int64_t>(n3, 1)));
-    FE_CHECK(dalloc(h->cand, (size_t)std::max<int64_t>(3 * n3, 1)));
+    FE_CHECK(dalloc(h->cand, (size_t)std::max<int64_t>(npe * n3, 1)));
     FE_CUDA(cudaMemsetAsync(h->counts.p, 0, (n + 1) * sizeof(int32_t), s));
     if (n3 > 0) {
         k_count_incidence<<<grid_for(n3), kThreads, 0, s>>>(h->conn.p, n3, h->counts.p);
@@ -885,7 +947,7 @@ int build_pattern(fe_handle_s *h) {
         k_fill_incidence<<<grid_for(n3), kThreads, 0, s>>>(h->conn.p, n3, h->inc_ptr.p, h->counts.p, h->inc.p);
         FE_LAUNCH_CHECK();
     }
-    k_node_neighbours<<<grid_for(n), kThreads, 0, s>>>(n, h->conn.p, h->inc_ptr.p, h->inc.p, h->cand.p,
+    k_node_neighbours<<<grid_for(n), kThreads, 0, s>>>(n, npe, h->conn.p, h->inc_ptr.p, h->inc.p, h->cand.p,
                                                         h->counts.p);
     FE_LAUNCH_CHECK();
     FE_CHECK(dalloc(h->blk_ptr, (size_t)n + 1));
@@ -893,7 +955,7 @@ int build_pattern(fe_handle_s *h) {
     FE_CHECK(exclusive_scan_i32(h->counts.p, h->blk_ptr.p, n, &nnzb, h->scan_tmp, s));
     FE_CHECK(dalloc(h->blk_col, (size_t)std::max<int64_t>(nnzb, 1)));
     FE_CHECK(dalloc(h->blk_row, (size_t)std::max<int64_t>(nnzb, 1)));
-    k_write_pattern<<<grid_for(n), kThreads, 0, s>>>(n, h->inc_ptr.p, h->cand.p, h->blk_ptr.p, h->blk_col.p,
+    k_write_pattern<<<grid_for(n), kThreads, 0, s>>>(n, npe, h->inc_ptr.p, h->cand.p, h->blk_ptr.p, h->blk_col.p,
                                                       h->blk_row.p);
     FE_LAUNCH_CHECK();
     h->nnzb = nnzb;
@@ -905,27 +967,32 @@ int build_pattern(fe_handle_s *h) {
 
 int assemble_stiffness(fe_handle_s *h) {
     cudaStream_t s = h->stream;
-    const int D = h->dim, NL = 3 * D;
+    const int D = h->dim, NL = h->npe * D;
     FE_CHECK(dalloc(h->ke, (size_t)std::max<int64_t>(h->n_elem * NL * NL, 1)));
     if (h->n_elem > 0) {
-        int g = grid_for(h->n_elem, kElemBlock, 152 * 64);
         if (h->kind == FE_KIND_ELASTIC_TRI)
-            k_elastic_ke<<<g, kElemBlock, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->E.p, h->nu.p, h->thick.p,
-                                                  h->plane == FE_PLANE_STRAIN, h->ke.p, h->err.p);
+            k_elastic_ke<<<grid_for(h->n_elem, kElemBlock, 152 * 64), kElemBlock, 0, s>>>(
+                h->n_elem, h->coords.p, h->conn.p, h->E.p, h->nu.p, h->thick.p, h->plane == FE_PLANE_STRAIN, h->ke.p,
+                h->err.p);
+        else if (h->kind == FE_KIND_ELASTIC_TET)
+            k_elastic_tet_ke<<<grid_for(h->n_elem, kTetBlock, 152 * 64), kTetBlock, 0, s>>>(
+                h->n_elem, h->coords.p, h->conn.p, h->E.p, h->nu.p, h->ke.p, h->err.p);
         else
-            k_magnetic_ke<<<g, kElemBlock, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->mu.p, h->ke.p, h->err.p);
+            k_magnetic_ke<<<grid_for(h->n_elem, kElemBlock, 152 * 64), kElemBlock, 0, s>>>(
+                h->n_elem, h->coords.p, h->conn.p, h->mu.p, h->ke.p, h->err.p);
         FE_LAUNCH_CHECK();
     }
     if (h->n_elem > 0) h->launches += 1;
     FE_CHECK(dalloc(h->kval, (size_t)std::max<int64_t>(h->nnzb * D * D, 1)));
     if (h->nnzb > 0) {
         int g = grid_for(h->nnzb, kThreads, 152 * 64);
-        if (D == 2)
-            k_reduce_stiffness<2><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p,
-                                                         h->inc.p, h->conn.p, h->ke.p, h->kval.p);
-        else
-            k_reduce_stiffness<1><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p,
-                                                         h->inc.p, h->conn.p, h->ke.p, h->kval.p);
+        FE_CHECK(with_dim(D, [&](auto dc) {
+            constexpr int DD = decltype(dc)::value;
+            constexpr int NPE = DD == 3 ? 4 : 3;   // tetrahedra carry 3 DOF per node, triangles 1 or 2
+            k_reduce_stiffness<DD, NPE><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p,
+                                                               h->inc.p, h->conn.p, h->ke.p, h->kval.p);
+            return FE_OK;
+        }));
         FE_LAUNCH_CHECK();
     }
     if (h->nnzb > 0) h->launches += 1;
@@ -934,21 +1001,31 @@ int assemble_stiffness(fe_handle_s *h) {
 }
 
 int assemble_mass(fe_handle_s *h) {
-    if (h->kind != FE_KIND_ELASTIC_TRI || !h->have_rho) {
+    if ((h->kind != FE_KIND_ELASTIC_TRI && h->kind != FE_KIND_ELASTIC_TET) || !h->have_rho) {
         set_error("mass matrices need elasticity elements with a mass density");
         return FE_NOT_READY;
     }
     cudaStream_t s = h->stream;
+    const int D = h->dim;
     FE_CHECK(dalloc(h->me_scale, (size_t)std::max<int64_t>(h->n_elem, 1)));
     if (h->n_elem > 0) {
-        k_mass_scale<<<grid_for(h->n_elem), kThreads, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->rho.p,
-                                                              h->thick.p, h->me_scale.p);
+        if (h->kind == FE_KIND_ELASTIC_TET)
+            k_mass_scale_tet<<<grid_for(h->n_elem), kThreads, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->rho.p,
+                                                                      h->me_scale.p);
+        else
+            k_mass_scale<<<grid_for(h->n_elem), kThreads, 0, s>>>(h->n_elem, h->coords.p, h->conn.p, h->rho.p,
+                                                                  h->thick.p, h->me_scale.p);
         FE_LAUNCH_CHECK();
     }
-    FE_CHECK(dalloc(h->mval, (size_t)std::max<int64_t>(h->nnzb * 4, 1)));
+    FE_CHECK(dalloc(h->mval, (size_t)std::max<int64_t>(h->nnzb * D * D, 1)));
     if (h->nnzb > 0) {
-        k_reduce_mass<<<grid_for(h->nnzb, kThreads, 152 * 64), kThreads, 0, s>>>(
-            h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p, h->inc.p, h->conn.p, h->me_scale.p, h->mval.p);
+        const int g = grid_for(h->nnzb, kThreads, 152 * 64);
+        if (h->kind == FE_KIND_ELASTIC_TET)
+            k_reduce_mass<3, 4><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p, h->inc.p,
+                                                       h->conn.p, h->me_scale.p, h->mval.p);
+        else
+            k_reduce_mass<2, 3><<<g, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->inc_ptr.p, h->inc.p,
+                                                       h->conn.p, h->me_scale.p, h->mval.p);
         FE_LAUNCH_CHECK();
     }
     h->launches += (h->n_elem > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0);
@@ -1021,29 +1098,20 @@ int build_system(fe_handle_s *h, double ka, double mb, bool use_bc) {
     FE_CHECK(dalloc(h->srow, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
     FE_CHECK(dalloc(h->dinv32, (size_t)std::max<int64_t>(h->n_nodes * D * D, 1)));
     int gs = grid_for(h->nnzb, kThreads, 152 * 64), gn = grid_for(h->n_nodes, kThreads, 152 * 64);
-    if (D == 2) {
+    FE_CHECK(with_dim(D, [&](auto dc) {
+        constexpr int DD = decltype(dc)::value;
         if (h->nnzb > 0)
-            k_eliminate<2><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
-                                                   mv, ka, mb, h->aval.p, h->aval32.p);
-        k_diff_form<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
-                                               h->aval32.p);
+            k_eliminate<DD><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
+                                                    mv, ka, mb, h->aval.p, h->aval32.p);
+        k_diff_form<DD><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
+                                                h->aval32.p);
         if (h->f_ready)
-            k_eliminated_rhs<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
-                                                        h->bc_val.p, h->kval.p, h->F.p, h->b.p);
-        k_block_jacobi<2><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
-                                                  h->dinv32.p, h->err.p);
-    } else {
-        if (h->nnzb > 0)
-            k_eliminate<1><<<gs, kThreads, 0, s>>>(h->nnzb, h->blk_row.p, h->blk_col.p, h->bc_of_dof.p, h->kval.p,
-                                                   mv, ka, mb, h->aval.p, h->aval32.p);
-        k_diff_form<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->srow.p,
-                                               h->aval32.p);
-        if (h->f_ready)
-            k_eliminated_rhs<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
-                                                        h->bc_val.p, h->kval.p, h->F.p, h->b.p);
-        k_block_jacobi<1><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
-                                                  h->dinv32.p, h->err.p);
-    }
+            k_eliminated_rhs<DD><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->bc_of_dof.p,
+                                                         h->bc_val.p, h->kval.p, h->F.p, h->b.p);
+        k_block_jacobi<DD><<<gn, kThreads, 0, s>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, h->aval.p, h->dinv.p,
+                                                   h->dinv32.p, h->err.p);
+        return FE_OK;
+    }));
     FE_LAUNCH_CHECK();
     h->launches += (use_bc && h->n_bc > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0) + 2 + (h->f_ready ? 1 : 0);
     FE_CHECK(build_sell(h));
@@ -1060,14 +1128,13 @@ int build_sell(fe_handle_s *h) {
     FE_CHECK(dalloc(h->counts, (size_t)std::max<int64_t>(n_slices, h->n_nodes) + 1));
     FE_CHECK(dalloc(h->sell_off, (size_t)n_slices + 1));
     if (n_slices > 0) {
-        if (D == 2)
-            k_sell_widths<2><<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p,
-                                                                         h->blk_col.p, h->aval.p, h->srow.p,
-                                                                         h->counts.p);
-        else
-            k_sell_widths<1><<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p,
-                                                                         h->blk_col.p, h->aval.p, h->srow.p,
-                                                                         h->counts.p);
+        FE_CHECK(with_dim(D, [&](auto dc) {
+            constexpr int DD = decltype(dc)::value;
+            k_sell_widths<DD><<<grid_for(n_slices * 32), kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p,
+                                                                          h->blk_col.p, h->aval.p, h->srow.p,
+                                                                          h->counts.p);
+            return FE_OK;
+        }));
         FE_LAUNCH_CHECK();
     }
     int64_t total = 0;
@@ -1088,16 +1155,14 @@ int build_sell(fe_handle_s *h) {
     FE_CUDA(cudaMemsetAsync(h->dblk32.p, 0, h->n_nodes * D * D * sizeof(float), s));
     if (n_slices > 0) {
         int g = grid_for(n_slices * 32, kThreads, 152 * 64);
-        if (D == 2)
-            k_sell_fill<2><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
-                                                  h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
-                                                  h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
-                                                  h->dblk32.p, h->sell_dcol.p, h->sell_over.p);
-        else
-            k_sell_fill<1><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
-                                                  h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
-                                                  h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
-                                                  h->dblk32.p, h->sell_dcol.p, h->sell_over.p);
+        FE_CHECK(with_dim(D, [&](auto dc) {
+            constexpr int DD = decltype(dc)::value;
+            k_sell_fill<DD><<<g, kThreads, 0, s>>>(h->n_nodes, n_slices, h->blk_ptr.p, h->blk_col.p, h->aval.p,
+                                                   h->srow.p, h->dinv.p, h->sell_off.p, h->sell_col.p,
+                                                   h->sell_val64.p, h->sell_val32.p, h->diag64.p, h->diag32.p,
+                                                   h->dblk32.p, h->sell_dcol.p, h->sell_over.p);
+            return FE_OK;
+        }));
         FE_LAUNCH_CHECK();
     }
     int over = 1;
@@ -1202,7 +1267,7 @@ int export_csr(fe_handle_s *h, int which, int64_t *indptr_host, int32_t *indices
 }
 
 int export_element_matrices(fe_handle_s *h, int which, double *out_host) {
-    const int NL = 3 * h->dim;
+    const int NL = h->npe * h->dim;
     if (which == FE_ASSEMBLE_K) {
         if (!h->k_ready) {
             set_error("stiffness not assembled");
@@ -1222,10 +1287,14 @@ int export_element_matrices(fe_handle_s *h, int which, double *out_host) {
         FE_CUDA(cudaMemcpyAsync(sc.data(), h->me_scale.p, h->n_elem * sizeof(double), cudaMemcpyDeviceToHost,
                                 h->stream));
         FE_CUDA(cudaStreamSynchronize(h->stream));
-        static const double P[36] = {2, 0, 1, 0, 1, 0, 0, 2, 0, 1, 0, 1, 1, 0, 2, 0, 1, 0,
-                                     0, 1, 0, 2, 0, 1, 1, 0, 1, 0, 2, 0, 0, 1, 0, 1, 0, 2};
+        // P = (1 + delta_ij) per node pair times I_D (elements.py:514-519, :830-843)
+        const int D = h->dim;
         for (int64_t e = 0; e < h->n_elem; ++e)
-            for (int k = 0; k < 36; ++k) out_host[e * 36 + k] = sc[e] * P[k];
+            for (int r = 0; r < NL; ++r)
+                for (int c = 0; c < NL; ++c) {
+                    const double p = (r % D != c % D) ? 0.0 : (r / D == c / D ? 2.0 : 1.0);
+                    out_host[e * NL * NL + r * NL + c] = sc[e] * p;
+                }
         return FE_OK;
     }
     set_error("unknown element matrix selector");

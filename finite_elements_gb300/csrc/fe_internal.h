@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <type_traits>
 
 #include "../../include/fe_gb300.h"
 
@@ -49,6 +50,18 @@ inline int grid_for(int64_t n, int threads = kThreads, int cap = 152 * 16) {
     if (g < 1) g = 1;
     if (g > cap) g = cap;
     return (int)g;
+}
+
+// Calls f(std::integral_constant<int, D>{}) for the DOF count per node d (1, 2 or 3)
+// and returns its status: one place turns the runtime d into a template argument.
+template <typename F>
+int with_dim(int d, F f) {
+    switch (d) {
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
+    case 3: return f(std::integral_constant<int, 3>{});
+    default: return FE_BAD_INPUT;
+    }
 }
 
 // ---------------------------------------------------------------- buffers
@@ -134,6 +147,8 @@ struct SolverWork {
 struct fe_handle_s {
     int kind = 0;            // FE_KIND_*
     int dim = 0;             // DOF per node
+    int npe = 3;             // nodes per element: 3 (triangles) or 4 (tetrahedra)
+    int cdim = 2;            // coordinates per node: 2 or 3
     int64_t n_nodes = 0, n_elem = 0, n_dof = 0;
     int32_t max_node = -1;   // largest node index used by an element
     cudaStream_t stream = nullptr;
@@ -142,8 +157,8 @@ struct fe_handle_s {
     cudaEvent_t events[10] = {};
 
     // inputs
-    fe::DBuf<double> coords;      // [n_nodes][2]
-    fe::DBuf<int32_t> conn;       // [n_elem][3]
+    fe::DBuf<double> coords;      // [n_nodes][cdim]
+    fe::DBuf<int32_t> conn;       // [n_elem][npe]
     fe::DBuf<double> E, nu, thick, rho, mu;
     int plane = 0;
     bool have_material = false, have_rho = false;
@@ -165,7 +180,7 @@ struct fe_handle_s {
 
     // pattern: node-block CSR
     bool pattern_ready = false;
-    fe::DBuf<int32_t> inc_ptr, inc;       // node -> (element*3 + local) incidence, sorted
+    fe::DBuf<int32_t> inc_ptr, inc;       // node -> (element*npe + local) incidence, sorted
     int64_t nnzb = 0;
     fe::DBuf<int32_t> blk_ptr, blk_col, blk_row;
     fe::DBuf<int32_t> cand;               // scratch for the pattern build

@@ -116,10 +116,11 @@ __global__ void __launch_bounds__(kMT) km_start(int64_t n, double *__restrict__ 
 // a smooth, non-rigid test field for the automatic shift: ((x - xmin) / L)^2 in every
 // component
 __global__ void __launch_bounds__(kMT)
-km_smooth(int64_t n_nodes, int D, const double *__restrict__ coords, double xmin, double inv_len, double *__restrict__ v) {
+km_smooth(int64_t n_nodes, int D, int cdim, const double *__restrict__ coords, double xmin, double inv_len,
+          double *__restrict__ v) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_nodes;
          r += (int64_t)gridDim.x * blockDim.x) {
-        const double t = (coords[2 * r] - xmin) * inv_len;
+        const double t = (coords[cdim * r] - xmin) * inv_len;
         for (int a = 0; a < D; ++a) v[r * D + a] = t * t;
     }
 }
@@ -140,10 +141,11 @@ struct Modal {
     }
 
     int spmv(const DBuf<double> &A, const double *x, double *y) {
-        if (h->dim == 2)
-            km_bsr_spmv<2><<<grid1(h->n_nodes), kMT, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, A.p, x, y);
-        else
-            km_bsr_spmv<1><<<grid1(h->n_nodes), kMT, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, A.p, x, y);
+        FE_CHECK(with_dim(h->dim, [&](auto dc) {
+            constexpr int D = decltype(dc)::value;
+            km_bsr_spmv<D><<<grid1(h->n_nodes), kMT, 0, h->stream>>>(h->n_nodes, h->blk_ptr.p, h->blk_col.p, A.p, x, y);
+            return FE_OK;
+        }));
         FE_LAUNCH_CHECK();
         h->launches += 1;
         return FE_OK;
@@ -252,13 +254,14 @@ int modal(fe_handle_s *h, int which, int k, double sigma, int steps, int precisi
 
     // automatic shift: 1% of the Rayleigh quotient of a smooth field, below zero
     if (which == FE_MODAL_SMALLEST && !(sigma < 0.0)) {
-        std::vector<double> xy(2 * h->n_nodes);
+        const int cd = h->cdim;
+        std::vector<double> xy(cd * h->n_nodes);
         FE_CUDA(cudaMemcpyAsync(xy.data(), h->coords.p, xy.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
         FE_CUDA(cudaStreamSynchronize(s));
         double xmin = INFINITY, xmax = -INFINITY;
-        for (int64_t i = 0; i < h->n_nodes; ++i) xmin = std::min(xmin, xy[2 * i]), xmax = std::max(xmax, xy[2 * i]);
+        for (int64_t i = 0; i < h->n_nodes; ++i) xmin = std::min(xmin, xy[cd * i]), xmax = std::max(xmax, xy[cd * i]);
         const double len = xmax > xmin ? xmax - xmin : 1.0;
-        km_smooth<<<grid1(h->n_nodes), kMT, 0, s>>>(h->n_nodes, h->dim, h->coords.p, xmin, 1.0 / len, w.p);
+        km_smooth<<<grid1(h->n_nodes), kMT, 0, s>>>(h->n_nodes, h->dim, cd, h->coords.p, xmin, 1.0 / len, w.p);
         FE_LAUNCH_CHECK();
         double vkv = 0, vmv = 0;
         FE_CHECK(md.spmv(h->kval, w.p, Mw.p));

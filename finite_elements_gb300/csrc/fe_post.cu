@@ -5,15 +5,12 @@
 // q is the element's DOF vector gathered from the solution (node-major, dimension
 // minor).  One thread per element; the arithmetic follows the reference's evaluation
 // order with explicit round-to-nearest operations, like the element kernels.
+#include "fe_element.cuh"
 #include "fe_internal.h"
 
 namespace fe {
 namespace {
 
-__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
 
 __global__ void k_post_elastic(int64_t n_elem, const double *__restrict__ coords, const int32_t *__restrict__ conn,
                                const double *__restrict__ E, const double *__restrict__ nu, int plane_strain,
@@ -86,6 +83,65 @@ __global__ void k_post_elastic(int64_t n_elem, const double *__restrict__ coords
     }
 }
 
+// Tetrahedron: strain = B q with the rows (xx, yy, zz, xy, yz, zx) of elements.py:743-748
+// (the zeros of B dropped), stress = D strain with the isotropic D of
+// elements.py:779-796, energy = 0.5 (q^T Ke) q.
+__global__ void k_post_elastic_tet(int64_t n_elem, const double *__restrict__ coords,
+                                   const int32_t *__restrict__ conn, const double *__restrict__ E,
+                                   const double *__restrict__ nu, const double *__restrict__ ke,
+                                   const double *__restrict__ u, double *__restrict__ strain,
+                                   double *__restrict__ stress, double *__restrict__ energy) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const TetGrad t = tet_gradients(coords, conn, e);
+        double q[12];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int64_t n = conn[4 * e + i];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) q[3 * i + a] = u[3 * n + a];
+        }
+        double eps[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const double gx = t.g[i][0], gy = t.g[i][1], gz = t.g[i][2];
+            const double ui = q[3 * i], vi = q[3 * i + 1], wi = q[3 * i + 2];
+            eps[0] = add(eps[0], mul(gx, ui));
+            eps[1] = add(eps[1], mul(gy, vi));
+            eps[2] = add(eps[2], mul(gz, wi));
+            eps[3] = add(eps[3], add(mul(gy, ui), mul(gx, vi)));
+            eps[4] = add(eps[4], add(mul(gz, vi), mul(gy, wi)));
+            eps[5] = add(eps[5], add(mul(gz, ui), mul(gx, wi)));
+        }
+        const double Em = E[e], v = nu[e];
+        const double coef = dvd(Em, mul(add(1.0, v), sub(1.0, mul(2.0, v))));
+        const double cn = mul(coef, sub(1.0, v)), cl = mul(coef, v);
+        const double cg = mul(coef, dvd(sub(1.0, mul(2.0, v)), 2.0));
+        double sig[6];
+        sig[0] = add(add(mul(cn, eps[0]), mul(cl, eps[1])), mul(cl, eps[2]));
+        sig[1] = add(add(mul(cl, eps[0]), mul(cn, eps[1])), mul(cl, eps[2]));
+        sig[2] = add(add(mul(cl, eps[0]), mul(cl, eps[1])), mul(cn, eps[2]));
+        sig[3] = mul(cg, eps[3]);
+        sig[4] = mul(cg, eps[4]);
+        sig[5] = mul(cg, eps[5]);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            strain[6 * e + k] = eps[k];
+            stress[6 * e + k] = sig[k];
+        }
+        const double *K = ke + e * 144;
+        double en = 0.0;
+#pragma unroll 1
+        for (int j = 0; j < 12; ++j) {
+            double w = 0.0;
+#pragma unroll
+            for (int i = 0; i < 12; ++i) w = add(w, mul(q[i], K[i * 12 + j]));
+            en = add(en, mul(w, q[j]));
+        }
+        energy[e] = mul(0.5, en);
+    }
+}
+
 __global__ void k_post_magnetic(int64_t n_elem, const double *__restrict__ coords, const int32_t *__restrict__ conn,
                                 const double *__restrict__ A, double *__restrict__ Bf) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem;
@@ -122,7 +178,7 @@ int fe_post_elastic(fe_handle h, const double *u_host, double *strain_host, doub
         set_error("fe_post_elastic: null argument");
         return FE_BAD_INPUT;
     }
-    if (h->kind != FE_KIND_ELASTIC_TRI || !h->k_ready) {
+    if ((h->kind != FE_KIND_ELASTIC_TRI && h->kind != FE_KIND_ELASTIC_TET) || !h->k_ready) {
         set_error("fe_post_elastic: needs an assembled elasticity handle");
         return FE_NOT_READY;
     }
@@ -131,8 +187,9 @@ int fe_post_elastic(fe_handle h, const double *u_host, double *strain_host, doub
         return FE_NOT_READY;
     }
     const int64_t ne = h->n_elem;
+    const int nc = h->kind == FE_KIND_ELASTIC_TET ? 6 : 3;   // strain / stress components
     DBuf<double> ud, out;
-    int st = dalloc(out, (size_t)std::max<int64_t>(7 * ne, 1));
+    int st = dalloc(out, (size_t)std::max<int64_t>((2 * nc + 1) * ne, 1));
     const double *u = h->w.x.p;
     if (!st && u_host) {
         st = dalloc(ud, (size_t)std::max<int64_t>(h->n_dof, 1));
@@ -142,16 +199,22 @@ int fe_post_elastic(fe_handle h, const double *u_host, double *strain_host, doub
         u = ud.p;
     }
     if (!st && ne > 0) {
-        k_post_elastic<<<grid_for(ne), kThreads, 0, h->stream>>>(ne, h->coords.p, h->conn.p, h->E.p, h->nu.p,
-                                                                h->plane == FE_PLANE_STRAIN, h->ke.p, u, out.p,
-                                                                out.p + 3 * ne, out.p + 6 * ne);
+        if (nc == 6)
+            k_post_elastic_tet<<<grid_for(ne), kThreads, 0, h->stream>>>(ne, h->coords.p, h->conn.p, h->E.p, h->nu.p,
+                                                                        h->ke.p, u, out.p, out.p + 6 * ne,
+                                                                        out.p + 12 * ne);
+        else
+            k_post_elastic<<<grid_for(ne), kThreads, 0, h->stream>>>(ne, h->coords.p, h->conn.p, h->E.p, h->nu.p,
+                                                                    h->plane == FE_PLANE_STRAIN, h->ke.p, u, out.p,
+                                                                    out.p + 3 * ne, out.p + 6 * ne);
         if (cudaGetLastError() != cudaSuccess) st = FE_CUDA_ERR;
         h->launches += 1;
     }
     if (!st && ne > 0 &&
-        (cudaMemcpyAsync(strain_host, out.p, 3 * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream) ||
-         cudaMemcpyAsync(stress_host, out.p + 3 * ne, 3 * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream) ||
-         cudaMemcpyAsync(energy_host, out.p + 6 * ne, ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream)))
+        (cudaMemcpyAsync(strain_host, out.p, nc * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream) ||
+         cudaMemcpyAsync(stress_host, out.p + nc * ne, nc * ne * sizeof(double), cudaMemcpyDeviceToHost,
+                         h->stream) ||
+         cudaMemcpyAsync(energy_host, out.p + 2 * nc * ne, ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream)))
         st = FE_CUDA_ERR;
     if (!st && cudaStreamSynchronize(h->stream) != cudaSuccess) st = FE_CUDA_ERR;
     if (st == FE_CUDA_ERR) set_error("fe_post_elastic: CUDA failure");

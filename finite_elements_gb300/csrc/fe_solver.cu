@@ -119,7 +119,8 @@ __device__ __forceinline__ NodeVec<D, T> ld(const T *__restrict__ a, int64_t r) 
         float2 t = reinterpret_cast<const float2 *>(a)[r];
         o.v[0] = t.x, o.v[1] = t.y;
     } else {
-        o.v[0] = a[r];
+#pragma unroll
+        for (int k = 0; k < D; ++k) o.v[k] = a[r * D + k];
     }
     return o;
 }
@@ -131,7 +132,8 @@ __device__ __forceinline__ void st(T *__restrict__ a, int64_t r, const NodeVec<D
     } else if constexpr (D == 2) {
         reinterpret_cast<float2 *>(a)[r] = make_float2(o.v[0], o.v[1]);
     } else {
-        a[r] = o.v[0];
+#pragma unroll
+        for (int k = 0; k < D; ++k) a[r * D + k] = o.v[k];
     }
 }
 
@@ -151,7 +153,13 @@ __device__ __forceinline__ NodeVec<D, T> apply_dinv(const T *__restrict__ dinv, 
             y.v[1] = m.z * x.v[0] + m.w * x.v[1];
         }
     } else {
-        y.v[0] = dinv[r] * x.v[0];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            T acc = dinv[r * D * D + i * D] * x.v[0];
+#pragma unroll
+            for (int k = 1; k < D; ++k) acc += dinv[r * D * D + i * D + k] * x.v[k];
+            y.v[i] = acc;
+        }
     }
     return y;
 }
@@ -196,7 +204,10 @@ __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, cons
                 acc.v[1] += b.z * xv.v[0] + b.w * xv.v[1];
             }
         } else {
-            acc.v[0] += __ldg(blk) * xv.v[0];
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b = 0; b < D; ++b) acc.v[a] += __ldg(blk + a * D + b) * xv.v[b];
         }
     }
     if constexpr (G > 1) {
@@ -238,16 +249,21 @@ __device__ __forceinline__ void block_mac(const T *__restrict__ blk, const NodeV
             acc.v[1] = fmaf(b.w, x.v[1], acc.v[1]);
         }
     } else {
-        acc.v[0] = fma(__ldg(blk), x.v[0], acc.v[0]);
+        // column by column, as the D = 2 chains
+#pragma unroll
+        for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc.v[a] = fma(__ldg(blk + a * D + b), x.v[b], acc.v[a]);
     }
 }
 
-// Resident blocks per SM the SELL kernels are compiled for: FP32 8 (32 registers, the
-// 1216-block grid is one wave); FP64 0, i.e. ptxas's default (40-48 registers; a
-// floor of 1 makes it spend ~120 and lose the occupancy, 5 makes the Chebyshev step
-// spill).
-template <typename T>
-constexpr int kSellBlocks = sizeof(T) == 4 ? 8 : 0;
+// Resident blocks per SM the SELL kernels are compiled for: FP32 with 1 or 2 DOF per
+// node 8 (32 registers, the 1216-block grid is one wave); FP64, and FP32 with 3 DOF
+// per node (whose 3 x 3 blocks and 3-vectors do not fit 32 registers), 0, i.e.
+// ptxas's default (for FP64 40-48 registers; a floor of 1 makes it spend ~120 and
+// lose the occupancy, 5 makes the Chebyshev step spill).
+template <int D, typename T>
+constexpr int kSellBlocks = (sizeof(T) == 4 && D <= 2) ? 8 : 0;
 
 struct Sell {
     const int32_t *off, *col;
@@ -330,7 +346,7 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
 
 // y = A x (timing)
 template <int D, typename T, bool C16 = false>
-__global__ void __launch_bounds__(kVecThreads, kSellBlocks<T>)
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<D, T>)
 k_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag, const T *__restrict__ dscale,
        const T *__restrict__ x, T *__restrict__ y) {
     FE_SELL_LOOP {
@@ -379,7 +395,7 @@ k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__re
 
 // q = A p and p.q; the last block sets alpha = r.z / p.q or stops the loop.
 template <int D, typename T, bool C16 = false>
-__global__ void __launch_bounds__(kVecThreads, kSellBlocks<T>)
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<D, T>)
 k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
            const T *__restrict__ dscale, const T *__restrict__ p, T *__restrict__ q, double *partials,
            PcgScalars *sc) {
@@ -510,7 +526,7 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
 //         iteration; rdot is the recurrence's residual);
 // MODE 2: intermediate step.
 template <int D, typename T, typename RD, int MODE, bool FIRST, bool C16>
-__global__ void __launch_bounds__(kVecThreads, kSellBlocks<T>)   // FP32: 8 blocks per SM, one wave
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<D, T>)   // FP32: 8 blocks per SM, one wave
 k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
             const T *__restrict__ dinv, const T *__restrict__ rres, const T *__restrict__ z_in,
             T *__restrict__ zprev_out, double c1, double c2, double *partials, PcgScalars *sc,
@@ -1278,6 +1294,8 @@ int time_spmv_impl(fe_handle_s *h, int reps, double *ms) {
 int time_spmv_any(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {
     bool f32 = precision == FE_PREC_MIXED;
     FE_CHECK(ensure_work(h, !f32, f32));
+    // 3 DOF per node: one instantiation, 2 lanes per block row in the BSR kernel
+    if (h->dim == 3) return f32 ? time_spmv_impl<3, float, 2>(h, reps, ms) : time_spmv_impl<3, double, 2>(h, reps, ms);
     return dispatch_lanes(lanes, [&](auto g) {
         constexpr int G = decltype(g)::value;
         if (h->dim == 2) return f32 ? time_spmv_impl<2, float, G>(h, reps, ms) : time_spmv_impl<2, double, G>(h, reps, ms);
@@ -1642,12 +1660,16 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     int lanes = 2;
     FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
     FE_CUDA(cudaEventRecord(h->events[6], h->stream));
-    int rc = dispatch_lanes(lanes, [&](auto g) {
-        constexpr int G = decltype(g)::value;
-        if (h->dim == 2)
-            return mixed ? solve_mixed<2, G>(h, o, st) : mp ? solve_mp<2, G>(h, o, st) : solve_fp64<2, G>(h, o, st);
-        return mixed ? solve_mixed<1, G>(h, o, st) : mp ? solve_mp<1, G>(h, o, st) : solve_fp64<1, G>(h, o, st);
-    });
+    int rc = h->dim == 3
+                 ? (mixed ? solve_mixed<3, 2>(h, o, st) : mp ? solve_mp<3, 2>(h, o, st) : solve_fp64<3, 2>(h, o, st))
+                 : dispatch_lanes(lanes, [&](auto g) {
+                       constexpr int G = decltype(g)::value;
+                       if (h->dim == 2)
+                           return mixed ? solve_mixed<2, G>(h, o, st)
+                                        : mp ? solve_mp<2, G>(h, o, st) : solve_fp64<2, G>(h, o, st);
+                       return mixed ? solve_mixed<1, G>(h, o, st) : mp ? solve_mp<1, G>(h, o, st)
+                                                                         : solve_fp64<1, G>(h, o, st);
+                   });
     FE_CHECK(rc);
     FE_CHECK(recover_multipliers(h));
     FE_CUDA(cudaEventRecord(h->events[7], h->stream));
@@ -1664,12 +1686,12 @@ int recover_multipliers(fe_handle_s *h) {
     FE_CHECK(dalloc(h->lambda, (size_t)std::max<int64_t>(h->n_bc, 1)));
     if (h->n_bc == 0) return FE_OK;
     int g = grid_for(h->n_bc);
-    if (h->dim == 2)
-        k_multipliers<2><<<g, kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->blk_ptr.p, h->blk_col.p, h->kval.p,
+    FE_CHECK(with_dim(h->dim, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        k_multipliers<D><<<g, kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->blk_ptr.p, h->blk_col.p, h->kval.p,
                                                         h->F.p, h->w.x.p, h->lambda.p);
-    else
-        k_multipliers<1><<<g, kThreads, 0, h->stream>>>(h->n_bc, h->bc_dof.p, h->blk_ptr.p, h->blk_col.p, h->kval.p,
-                                                        h->F.p, h->w.x.p, h->lambda.p);
+        return FE_OK;
+    }));
     FE_LAUNCH_CHECK();
     h->launches += 1;
     return FE_OK;
@@ -1700,12 +1722,12 @@ int spmv64(fe_handle_s *h, const double *x, double *y) {
         return FE_NOT_READY;
     }
     Sell A{h->sell_off.p, h->sell_col.p, nullptr, h->n_slices};
-    if (h->dim == 2)
-        k_spmv<2, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
+    FE_CHECK(with_dim(h->dim, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        k_spmv<D, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
                                                                         nullptr, x, y);
-    else
-        k_spmv<1, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
-                                                                        nullptr, x, y);
+        return FE_OK;
+    }));
     FE_LAUNCH_CHECK();
     h->launches += 1;
     return FE_OK;

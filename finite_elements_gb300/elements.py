@@ -7,7 +7,7 @@ numpy matrices of the reference are not recomputed here: use
 """
 from __future__ import annotations
 
-from .mesh import TriangularElement2D
+from .mesh import TetrahedralElement, TriangularElement2D
 
 
 class Element2D(TriangularElement2D):
@@ -65,3 +65,18 @@ class ElasticityTriangularElement2D(ElasticityElement, Element2D):
     @property
     def dimension(self):
         return 2
+
+
+class ElasticityTetrahedralElement3D(ElasticityElement, TetrahedralElement):
+    """Linear elasticity tetrahedron (elements.py:663-876); three DOFs per node, the
+    isotropic 3D D whichever plane flag the analysis sets."""
+
+    def __init__(self, mesh_element, elasticity_modulus, poisson_ratio, mass_density,
+                 displacements=None, stress=None, strain=None, name: str = ''):
+        ElasticityElement.__init__(self, mesh_element, elasticity_modulus, poisson_ratio,
+                                   mass_density, displacements, stress, strain, name)
+        TetrahedralElement.__init__(self, mesh_element.points, name=name)
+
+    @property
+    def dimension(self):
+        return 3

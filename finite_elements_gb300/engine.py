@@ -21,7 +21,7 @@ import scipy.sparse as sp
 
 from . import _lib
 from ._lib import Handle, SolveOpts, SolveStats, ptr
-from .problem import ELASTIC, Problem
+from .problem import ELASTIC, ELASTIC3D, Problem
 
 
 # solve precisions: plain FP64 PCG; FP32 Krylov + FP64 iterative refinement; FP64 CG
@@ -47,17 +47,22 @@ class GpuSystem:
     def __init__(self, prob: Problem, assemble=True):
         self.prob = prob
         self.dim = prob.dim
-        if prob.kind == ELASTIC:
+        if prob.elastic:
             check_plane_flags(prob.plane_strain, prob.plane_stress)
-            kind = _lib.FE_KIND_ELASTIC_TRI
-        else:
-            kind = _lib.FE_KIND_MAGNETIC_TRI
+        if prob.kind == ELASTIC3D and (prob.element_loads or prob.element_bc_element.size):
+            # element loads and conditions go through element_to_node_factors (and an
+            # area), which the reference defines on triangles only (elements.py:18-53)
+            raise AttributeError("'ElasticityTetrahedralElement3D' object has no attribute "
+                                 "'element_to_node_factors'")
+        kind = {ELASTIC: _lib.FE_KIND_ELASTIC_TRI, ELASTIC3D: _lib.FE_KIND_ELASTIC_TET}.get(
+            prob.kind, _lib.FE_KIND_MAGNETIC_TRI)
         self.handle = Handle(kind, prob.coords, prob.conn)
         h = self.handle
-        if prob.kind == ELASTIC:
+        if prob.elastic:
             mode = _lib.FE_PLANE_STRAIN if prob.plane_strain else _lib.FE_PLANE_STRESS
             rho = prob.rho if prob.rho is not None else None
-            h.call("fe_set_elastic_materials", ptr(prob.E), ptr(prob.nu), ptr(prob.thickness),
+            thick = prob.thickness if prob.kind == ELASTIC else None
+            h.call("fe_set_elastic_materials", ptr(prob.E), ptr(prob.nu), ptr(thick),
                    ptr(rho), mode)
         else:
             h.call("fe_set_mu", ptr(prob.mu))
@@ -109,7 +114,7 @@ class GpuSystem:
         dofs = [self._dof(n, d) for n, d in zip(p.node_load_node.tolist(), p.node_load_dim.tolist())]
         vals = list(p.node_load_value.tolist())
         seqs = list(range(n_user))
-        # element loads: sets in order, occurrence k, point i -> seq n_user + 3k + i
+        # element loads (triangles): sets in order, occurrence k, point i -> seq n_user + 3k + i
         n_occ = 0
         if p.element_loads:
             set_ptr = np.zeros(len(p.element_loads) + 1, np.int64)
@@ -178,7 +183,7 @@ class GpuSystem:
         return sp.csc_matrix(arrays, shape=shape)
 
     def element_matrices(self, which="K"):
-        nl = 3 * self.dim
+        nl = self.prob.npe * self.dim
         out = np.empty((self.prob.n_elements, nl * nl))
         if which == "M" and not self.m_assembled:
             self.assemble(mass=True)
@@ -226,12 +231,14 @@ class GpuSystem:
 
     def post(self, x=None):
         """Per-element results of a solution (the handle's last one when x is None):
-        elasticity -> dict(strain (E,3), stress (E,3), energy (E,)); magnetostatics ->
+        elasticity -> dict(strain (E,3), stress (E,3), energy (E,)), with 6 strain and
+        stress components (xx, yy, zz, xy, yz, zx) on tetrahedra; magnetostatics ->
         dict(field (E,2))."""
         ne = self.prob.n_elements
         xa = None if x is None else np.ascontiguousarray(np.asarray(x, np.float64)[: self.prob.n_dof])
-        if self.prob.kind == ELASTIC:
-            strain, stress, energy = np.empty((ne, 3)), np.empty((ne, 3)), np.empty(ne)
+        if self.prob.elastic:
+            nc = 6 if self.prob.kind == ELASTIC3D else 3
+            strain, stress, energy = np.empty((ne, nc)), np.empty((ne, nc)), np.empty(ne)
             self.handle.call("fe_post_elastic", ptr(xa), ptr(strain), ptr(stress), ptr(energy))
             return {"strain": strain, "stress": stress, "energy": energy}
         field = np.empty((ne, 2))

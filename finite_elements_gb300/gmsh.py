@@ -1,6 +1,7 @@
-"""Gmsh 4.1 ASCII meshes: reading the triangle meshes the reference's scripts load
-(scripts/InputFiles/2D/*.msh through volmdlr's GmshParser, e.g.
-scripts/Elasticity/beam2d_example_3.py:52-73) and writing them back.
+"""Gmsh 4.1 ASCII meshes: reading the triangle and tetrahedron meshes the reference's
+scripts load (scripts/InputFiles/2D/*.msh and 3D/*.msh through volmdlr's GmshParser,
+e.g. scripts/Elasticity/beam2d_example_3.py:52-73, beam3d_example_2.py:75-93) and
+writing them back.
 
 The reader follows the published MSH 4.1 ASCII layout:
 
@@ -9,11 +10,12 @@ The reader follows the published MSH 4.1 ASCII layout:
   ``x y z`` line per node;
 * ``$Elements``: ``numEntityBlocks numElements minElementTag maxElementTag``, then per
   block ``entityDim entityTag elementType numElementsInBlock`` and one line per element,
-  ``elementTag nodeTag ...``.  Type 2 is the 3-node triangle.
+  ``elementTag nodeTag ...``.  Type 2 is the 3-node triangle, type 4 the 4-node
+  tetrahedron; the other types (points, lines) are skipped.
 
 Nodes keep the file's order (the reference's scripts set ``mesh.nodes =
-gmsh.nodes['all_nodes']`` "to keep Gmsh order"); triangles keep file order, one group
-per surface entity.
+gmsh.nodes['all_nodes']`` "to keep Gmsh order"); triangles and tetrahedra keep file
+order, one group per surface (volume) entity.
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ import numpy as np
 from .mesh import ArrayMesh
 
 TRIANGLE = 2
+TETRAHEDRON = 4
 
 
 @dataclass
@@ -33,9 +36,16 @@ class GmshMesh:
     triangles: np.ndarray       # (E, 3) int32 indices into coords
     group_ptr: np.ndarray       # (G+1,) triangles of surface entity g: group_ptr[g]:group_ptr[g+1]
     group_tags: np.ndarray      # (G,) the surface entity tags
+    tetrahedra: np.ndarray = None      # (T, 4) int32 indices into coords
+    tet_group_ptr: np.ndarray = None   # (V+1,) tetrahedra of volume entity v
+    tet_group_tags: np.ndarray = None  # (V,) the volume entity tags
 
     def array_mesh(self) -> ArrayMesh:
-        """The planar mesh (x, y) for the analysis; one element group per surface."""
+        """The mesh for the analysis: the tetrahedra with (x, y, z) when the file has
+        any (define_tetrahedron_element_mesh), else the planar triangles with (x, y);
+        one element group per volume (surface) entity."""
+        if self.tetrahedra is not None and self.tetrahedra.shape[0] > 0:
+            return ArrayMesh(self.coords, self.tetrahedra, self.tet_group_ptr)
         return ArrayMesh(self.coords[:, :2], self.triangles, self.group_ptr)
 
 
@@ -86,37 +96,47 @@ def read_msh(path) -> GmshMesh:
     if elems is None:
         raise ValueError(f"{path}: no $Elements section")
     n_blocks = int(elems[0].split()[0])
-    tris, ptr, group_tags = [], [0], []
+    found = {TRIANGLE: ([], [0], []), TETRAHEDRON: ([], [0], [])}
     pos = 1
     for _ in range(n_blocks):
         dim, entity, etype, count = (int(v) for v in elems[pos].split())
         pos += 1
-        if etype == TRIANGLE:
+        if etype in found:
+            rows, ptr, group_tags = found[etype]
+            nn = 3 if etype == TRIANGLE else 4
             for j in range(count):
                 v = elems[pos + j].split()
-                tris.append([index[int(v[1])], index[int(v[2])], index[int(v[3])]])
-            ptr.append(len(tris))
+                rows.append([index[int(t)] for t in v[1:1 + nn]])
+            ptr.append(len(rows))
             group_tags.append(entity)
         pos += count
-    triangles = np.array(tris, dtype=np.int32).reshape(-1, 3)
-    return GmshMesh(coords, tags, triangles, np.array(ptr, np.int64), np.array(group_tags, np.int64))
+    tri, tri_ptr, tri_tags = found[TRIANGLE]
+    tet, tet_ptr, tet_tags = found[TETRAHEDRON]
+    return GmshMesh(coords, tags, np.array(tri, dtype=np.int32).reshape(-1, 3), np.array(tri_ptr, np.int64),
+                    np.array(tri_tags, np.int64), np.array(tet, dtype=np.int32).reshape(-1, 4),
+                    np.array(tet_ptr, np.int64), np.array(tet_tags, np.int64))
 
 
-def write_msh(path, coords, triangles, node_tags=None):
-    """Write a triangle mesh as Gmsh 4.1 ASCII: one node block and one triangle block
-    on surface entity 1 (no geometric entities section, which MSH 4.1 allows)."""
+def write_msh(path, coords, elements, node_tags=None):
+    """Write a triangle mesh ((E, 3) elements, one block on surface entity 1) or a
+    tetrahedron mesh ((E, 4) elements, one block on volume entity 1) as Gmsh 4.1 ASCII:
+    one node block, one element block, no geometric entities section (which MSH 4.1
+    allows)."""
     coords = np.asarray(coords, np.float64)
     if coords.shape[1] == 2:
         coords = np.hstack([coords, np.zeros((coords.shape[0], 1))])
-    tri = np.asarray(triangles, np.int64).reshape(-1, 3)
-    n, e = coords.shape[0], tri.shape[0]
+    el = np.asarray(elements, np.int64)
+    nn = el.shape[1] if el.ndim == 2 else 3
+    el = el.reshape(-1, nn)
+    etype, edim = (TETRAHEDRON, 3) if nn == 4 else (TRIANGLE, 2)
+    n, e = coords.shape[0], el.shape[0]
     tags = np.arange(1, n + 1) if node_tags is None else np.asarray(node_tags, np.int64)
     out = ["$MeshFormat", "4.1 0 8", "$EndMeshFormat", "$Nodes",
-           f"1 {n} {int(tags.min()) if n else 0} {int(tags.max()) if n else 0}", f"2 1 0 {n}"]
+           f"1 {n} {int(tags.min()) if n else 0} {int(tags.max()) if n else 0}", f"{edim} 1 0 {n}"]
     out += [str(int(t)) for t in tags]
     out += [f"{x!r} {y!r} {z!r}" for x, y, z in coords.tolist()]
-    out += ["$EndNodes", "$Elements", f"1 {e} 1 {e}", f"2 1 {TRIANGLE} {e}"]
-    out += [f"{k + 1} {tags[a]} {tags[b]} {tags[c]}" for k, (a, b, c) in enumerate(tri.tolist())]
+    out += ["$EndNodes", "$Elements", f"1 {e} 1 {e}", f"{edim} 1 {etype} {e}"]
+    out += [f"{k + 1} " + " ".join(str(tags[i]) for i in row) for k, row in enumerate(el.tolist())]
     out += ["$EndElements"]
     with open(path, "w", encoding="utf-8") as f:
         f.write("\n".join(out) + "\n")

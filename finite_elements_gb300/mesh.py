@@ -8,6 +8,8 @@ small surface of them:
 * ``ElementsGroup.elements`` (analysis.py:326-327);
 * ``TriangularElement2D.points`` / ``.area`` / ``.form_functions``
   (elements.py:35-44, :100-116, :508, :530; loads.py:32-34);
+* ``TetrahedralElement.points`` / ``.volume`` / ``.form_functions``
+  (elements.py:719-748, :808-858);
 * edge objects with ``.start`` / ``.end`` (analysis.py:232-233, :441-442).
 
 volmdlr is not a dependency of this package, so these classes provide that surface.
@@ -52,6 +54,42 @@ class Point2D:
 
 class Node2D(Point2D):
     """A mesh node (volmdlr.mesh.Node2D)."""
+
+
+class Point3D:
+    """A 3D point, hashed and compared by its coordinates (like volmdlr.Point3D)."""
+
+    __slots__ = ("x", "y", "z")
+
+    def __init__(self, x, y, z):
+        self.x = float(x)
+        self.y = float(y)
+        self.z = float(z)
+
+    def __getitem__(self, i):
+        return (self.x, self.y, self.z)[i]
+
+    def __iter__(self):
+        yield self.x
+        yield self.y
+        yield self.z
+
+    def __len__(self):
+        return 3
+
+    def __hash__(self):
+        return hash((self.x, self.y, self.z))
+
+    def __eq__(self, other):
+        return (isinstance(other, Point3D) and self.x == other.x and self.y == other.y
+                and self.z == other.z)
+
+    def __repr__(self):
+        return f"{type(self).__name__}({self.x!r}, {self.y!r}, {self.z!r})"
+
+
+class Node3D(Point3D):
+    """A 3D mesh node (volmdlr.mesh.Node3D)."""
 
 
 class LineSegment2D:
@@ -103,6 +141,41 @@ class TriangularElement2D:
         return Point2D(sum(p[0] for p in xy) / 3.0, sum(p[1] for p in xy) / 3.0)
 
 
+class TetrahedralElement:
+    """A 4-node linear tetrahedron.
+
+    ``volume`` is the unsigned volume |det[p1-p0, p2-p0, p3-p0]|/6 and
+    ``form_functions`` the four rows (a_i, b_i, c_i, d_i) with
+    N_i = (a_i + b_i x + c_i y + d_i z) / (6 V), N_i(p_j) = delta_ij: the convention under
+    which the reference's B = (1/(6V)) [b_i, c_i, d_i ...] (elements.py:719-748) is the
+    matrix of shape-function gradients.
+    """
+
+    def __init__(self, points, name=""):
+        self.points = list(points)
+        self.name = name
+
+    def _xyz(self):
+        return np.array([[float(p[0]), float(p[1]), float(p[2])] for p in self.points])
+
+    @property
+    def volume(self):
+        p = self._xyz()
+        a, n = p[1] - p[0], np.cross(p[2] - p[0], p[3] - p[0])
+        return abs(a[0] * n[0] + a[1] * n[1] + a[2] * n[2]) / 6.0
+
+    @property
+    def form_functions(self):
+        p = self._xyz()
+        coef = np.linalg.inv(np.hstack([np.ones((4, 1)), p]))   # column i: N_i = coef[:, i] . (1, x, y, z)
+        return [list(6.0 * self.volume * coef[:, i]) for i in range(4)]
+
+    @property
+    def center(self):
+        c = self._xyz().mean(axis=0)
+        return Point3D(*c)
+
+
 class ElementsGroup:
     """An ordered list of elements (volmdlr.mesh.ElementsGroup)."""
 
@@ -135,7 +208,8 @@ class Mesh:
 
 
 class ArrayMesh:
-    """A mesh held as arrays: ``coords`` (n, 2) float64 and ``conn`` (E, 3) int32.
+    """A mesh held as arrays: ``coords`` (n, 2) float64 and ``conn`` (E, 3) int32, or
+    ``coords`` (n, 3) and ``conn`` (E, 4) for tetrahedra.
 
     ``group_ptr`` splits the elements into consecutive groups (group g is
     ``conn[group_ptr[g]:group_ptr[g+1]]``).  Per-element material arrays live in the
@@ -143,8 +217,12 @@ class ArrayMesh:
     """
 
     def __init__(self, coords, conn, group_ptr=None, name=""):
-        self.coords = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 2)
-        self.conn = np.ascontiguousarray(conn, dtype=np.int32).reshape(-1, 3)
+        coords = np.asarray(coords, dtype=np.float64)
+        conn = np.asarray(conn, dtype=np.int32)
+        cdim = coords.shape[1] if coords.ndim == 2 else 2
+        npe = conn.shape[1] if conn.ndim == 2 else 3
+        self.coords = np.ascontiguousarray(coords).reshape(-1, cdim)
+        self.conn = np.ascontiguousarray(conn).reshape(-1, npe)
         if group_ptr is None:
             group_ptr = [0, self.conn.shape[0]]
         self.group_ptr = np.asarray(group_ptr, dtype=np.int64)
@@ -163,7 +241,8 @@ class ArrayMesh:
     @property
     def nodes(self):
         if self._nodes is None:
-            self._nodes = [Node2D(x, y) for x, y in self.coords.tolist()]
+            node = Node3D if self.coords.shape[1] == 3 else Node2D
+            self._nodes = [node(*c) for c in self.coords.tolist()]
         return self._nodes
 
     @property

@@ -218,3 +218,57 @@ def grf_elasticity(nx, ny, seed=0, lx=None, ly=1.0):
                    node_load_dim=np.repeat(np.array([1, 2], np.int64), ln.size),
                    node_load_value=f.reshape(-1),
                    node_bc_node=bn, node_bc_dim=bd, node_bc_value=bv)
+
+
+# ---------------------------------------------------------------- 3D: linear tetrahedra
+
+# Kuhn split of a hexahedral cell into 6 tetrahedra: corner bits (x=1, y=2, z=4), one
+# tetrahedron per axis order, 000 -> +axis1 -> +axis2 -> 111.  Every cell uses the same
+# split, so faces match between neighbours.  The odd axis orders give negatively
+# oriented tetrahedra (both orientations are exercised).
+_KUHN = np.array([[0, 1, 3, 7], [0, 1, 5, 7], [0, 2, 3, 7],
+                  [0, 2, 6, 7], [0, 4, 5, 7], [0, 4, 6, 7]], np.int64)
+
+
+def box_tets(nx, ny, nz, lx, ly, lz, jitter=0.0, rng=None):
+    """Structured nx-by-ny-by-nz cell grid on [0,lx]x[0,ly]x[0,lz] split into 6 tetrahedra
+    per cell -> (coords (n,3), conn (6*nx*ny*nz,4)), node id = (k*(ny+1) + j)*(nx+1) + i.
+
+    With ``jitter`` > 0 the interior nodes move by U(-jitter, jitter) cell sizes; boundary
+    nodes stay put."""
+    xs, ys, zs = np.linspace(0.0, lx, nx + 1), np.linspace(0.0, ly, ny + 1), np.linspace(0.0, lz, nz + 1)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")              # (nz+1, ny+1, nx+1)
+    coords = np.stack([X.reshape(-1), Y.reshape(-1), Z.reshape(-1)], axis=1)
+    if jitter > 0:
+        h = np.array([lx / nx, ly / ny, lz / nz])
+        d = rng.uniform(-jitter, jitter, size=coords.shape) * h
+        k, j, i = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+        inner = ((i > 0) & (i < nx) & (j > 0) & (j < ny) & (k > 0) & (k < nz)).reshape(-1)
+        coords = coords + d * inner[:, None]
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    base = ((k * (ny + 1) + j) * (nx + 1) + i).reshape(-1)
+    sx, sy, sz = 1, nx + 1, (nx + 1) * (ny + 1)
+    corner = np.array([(b & 1) * sx + ((b >> 1) & 1) * sy + ((b >> 2) & 1) * sz for b in range(8)], np.int64)
+    conn = (base[:, None, None] + corner[_KUHN][None, :, :]).reshape(-1, 4).astype(np.int32)
+    return coords, conn
+
+
+def cantilever_3d(nx, ny, nz, length=10.0, width=2.0, height=2.0, E=210e9, nu=0.25, rho=7860.0,
+                  load=-1000.0, jitter=0.0, seed=0):
+    """A solid cantilever of linear tetrahedra, as the reference's 3D beam scripts set it
+    up (scripts/Elasticity/beam3d_example_2.py): every node of the face x = 0 clamped
+    in dimensions 1, 2 and 3, a NodeLoad ``load`` in dimension 3 at every node of the
+    free end's top edge (x = length, z = height)."""
+    rng = np.random.default_rng(seed)
+    coords, conn = box_tets(nx, ny, nz, length, width, height, jitter, rng)
+    ne = conn.shape[0]
+    x, z = coords[:, 0], coords[:, 2]
+    clamped = np.flatnonzero(x == 0.0)
+    tip = np.flatnonzero((x == length) & (z == height))
+    from .problem import ELASTIC3D
+    return Problem(ELASTIC3D, coords, conn, E=np.full(ne, E), nu=np.full(ne, nu), rho=np.full(ne, rho),
+                   plane_strain=False, plane_stress=True,
+                   node_load_node=tip, node_load_dim=np.full(tip.size, 3, np.int64),
+                   node_load_value=np.full(tip.size, load),
+                   node_bc_node=np.repeat(clamped, 3), node_bc_dim=np.tile([1, 2, 3], clamped.size),
+                   node_bc_value=np.zeros(3 * clamped.size))

@@ -15,6 +15,11 @@ import numpy as np
 
 ELASTIC = "elastic"
 MAGNETIC = "magnetic"
+ELASTIC3D = "elastic3d"
+
+# DOF per node, nodes per element and coordinates per node of each kind
+_DIM = {ELASTIC: 2, MAGNETIC: 1, ELASTIC3D: 3}
+_NPE = {ELASTIC: 3, MAGNETIC: 3, ELASTIC3D: 4}
 
 
 def _f64(a, n=None):
@@ -42,10 +47,13 @@ class ElementLoadSet:
 class Problem:
     """Everything the GPU path needs for one analysis, as arrays.
 
-    kind            "elastic" (2 DOF per node) or "magnetic" (1 DOF per node)
-    coords          (n, 2) float64 node coordinates, in ``mesh.nodes`` order
-    conn            (E, 3) int32 node indices, groups then elements in mesh order
-    E, nu, thickness, rho   (E,) float64 elastic material per element
+    kind            "elastic" (plane triangles, 2 DOF per node), "magnetic" (triangles,
+                    1 DOF per node) or "elastic3d" (linear tetrahedra, 3 DOF per node)
+    coords          (n, 2) float64 node coordinates, in ``mesh.nodes`` order ((n, 3)
+                    for "elastic3d")
+    conn            (E, 3) int32 node indices, groups then elements in mesh order ((E, 4)
+                    for "elastic3d")
+    E, nu, thickness, rho   (E,) float64 elastic material per element (no thickness in 3D)
     mu              (E,) float64 absolute permeability per element (magnetic)
     plane_strain, plane_stress   the reference's two flags (elements.py:251-273)
     node_loads      (node, dim, value) triples in user order
@@ -84,8 +92,11 @@ class Problem:
     edge_bc_value: np.ndarray = field(default_factory=lambda: np.zeros(0))
 
     def __post_init__(self):
-        self.coords = np.ascontiguousarray(np.asarray(self.coords, np.float64).reshape(-1, 2))
-        self.conn = np.ascontiguousarray(np.asarray(self.conn, np.int32).reshape(-1, 3))
+        if self.kind not in _DIM:
+            raise ValueError(f"unknown problem kind {self.kind!r}")
+        cdim = 3 if self.kind == ELASTIC3D else 2
+        self.coords = np.ascontiguousarray(np.asarray(self.coords, np.float64).reshape(-1, cdim))
+        self.conn = np.ascontiguousarray(np.asarray(self.conn, np.int32).reshape(-1, _NPE[self.kind]))
         ne = self.conn.shape[0]
         for name in ("E", "nu", "thickness", "rho", "mu"):
             v = getattr(self, name)
@@ -104,7 +115,16 @@ class Problem:
 
     @property
     def dim(self) -> int:
-        return 2 if self.kind == ELASTIC else 1
+        return _DIM[self.kind]
+
+    @property
+    def npe(self) -> int:
+        """Nodes per element."""
+        return _NPE[self.kind]
+
+    @property
+    def elastic(self) -> bool:
+        return self.kind in (ELASTIC, ELASTIC3D)
 
     @property
     def n_nodes(self) -> int:

@@ -24,28 +24,35 @@ class Result:
 
 
 def mesh_arrays(mesh):
-    """(coords (n, 2), conn (E, 3)) of an ArrayMesh or of a mesh of element objects
+    """(coords (n, 2|3), conn (E, 3|4)) of an ArrayMesh or of a mesh of element objects
     (nodes in ``mesh.nodes`` order, elements in group order)."""
     if hasattr(mesh, "as_arrays"):
         return mesh.as_arrays()
     index = mesh.node_to_index
-    coords = np.array([[float(p[0]), float(p[1])] for p in mesh.nodes], np.float64).reshape(-1, 2)
+    first = mesh.elements_groups[0].elements[0]
+    npe = len(first.points)
+    cdim = 3 if npe == 4 else 2
+    coords = np.array([[float(p[k]) for k in range(cdim)] for p in mesh.nodes], np.float64).reshape(-1, cdim)
     conn = np.array([[index[p] for p in el.points] for g in mesh.elements_groups for el in g.elements],
-                    np.int64).reshape(-1, 3)
+                    np.int64).reshape(-1, npe)
     return coords, conn
 
 
 def write_vtk(file_name, coords, conn, point_scalars=(), point_vectors=()):
-    """Legacy ASCII VTK unstructured grid of linear triangles (cell type 5) with point
-    data: ``point_scalars`` / ``point_vectors`` are (name, (n,) or (n, 2|3)) pairs."""
+    """Legacy ASCII VTK unstructured grid of linear triangles (cell type 5) or linear
+    tetrahedra (cell type 10, when conn has 4 columns) with point data:
+    ``point_scalars`` / ``point_vectors`` are (name, (n,) or (n, 2|3)) pairs."""
     coords = np.asarray(coords, np.float64)
-    conn = np.asarray(conn, np.int64).reshape(-1, 3)
+    conn = np.asarray(conn, np.int64)
+    npe = conn.shape[1] if conn.ndim == 2 else 3
+    conn = conn.reshape(-1, npe)
     n, e = coords.shape[0], conn.shape[0]
+    xyz = coords if coords.shape[1] == 3 else np.hstack([coords[:, :2], np.zeros((n, 1))])
     out = ["# vtk DataFile Version 3.0", "finite element result", "ASCII", "DATASET UNSTRUCTURED_GRID",
            f"POINTS {n} double"]
-    out += [f"{x!r} {y!r} 0" for x, y in coords[:, :2].tolist()]
-    out += [f"CELLS {e} {4 * e}"] + [f"3 {a} {b} {c}" for a, b, c in conn.tolist()]
-    out += [f"CELL_TYPES {e}"] + ["5"] * e
+    out += [f"{x!r} {y!r} {z!r}" for x, y, z in xyz.tolist()]
+    out += [f"CELLS {e} {(npe + 1) * e}"] + [f"{npe} " + " ".join(map(str, row)) for row in conn.tolist()]
+    out += [f"CELL_TYPES {e}"] + (["10"] if npe == 4 else ["5"]) * e
     if point_scalars or point_vectors:
         out.append(f"POINT_DATA {n}")
     for name, v in point_scalars:
@@ -70,7 +77,10 @@ def _system_for(mesh, plane_strain=None, plane_stress=None):
 class ElasticityResults2D(Result):
     """Per-element strain, stress and energy of a plane-elasticity solution
     (finite_elements/results.py:930, :700-830), computed by the GPU kernels.
-    Arrays follow the mesh's element order (groups, then elements)."""
+    Arrays follow the mesh's element order (groups, then elements).  Strain and stress
+    rows are (xx, yy, xy)."""
+
+    _ncomp = 2
 
     def __init__(self, mesh, result_vector, plane_strain, plane_stress, system=None):
         Result.__init__(self, mesh, result_vector)
@@ -104,21 +114,81 @@ class ElasticityResults2D(Result):
 
     @property
     def displacement_vectors_per_node(self):
-        n = len(self.mesh.nodes)
-        return np.asarray(self.result_vector[: 2 * n], np.float64).reshape(n, 2)
+        n, d = len(self.mesh.nodes), self._ncomp
+        return np.asarray(self.result_vector[: d * n], np.float64).reshape(n, d)
+
+    def displacement_per_node_x(self):
+        return self.displacement_vectors_per_node[:, 0]
+
+    def displacement_per_node_y(self):
+        return self.displacement_vectors_per_node[:, 1]
+
+    def axial_strain_x(self):
+        return self.strain[:, 0]
+
+    def axial_strain_y(self):
+        return self.strain[:, 1]
+
+    def axial_stress_x(self):
+        return self.stress[:, 0]
+
+    def axial_stress_y(self):
+        return self.stress[:, 1]
+
+    def shear_strain_xy(self):
+        return self.strain[:, 2]
+
+    def shear_stress_xy(self):
+        return self.stress[:, 2]
 
     def generate_vtk_file(self, file_name_output):
         """The mesh with the displacement as point data, ``Displacement_Magnitude``
-        (scalars) and ``Displacement_Vectors`` (vectors, z = 0), as the reference's
-        writer appends them (results.py:832-871).  The reference copies the mesh part
-        from Gmsh's own VTK export; here the whole file is written."""
+        (scalars) and ``Displacement_Vectors`` (vectors, z = 0 in 2D), as the
+        reference's writer appends them (results.py:832-871).  The reference copies the
+        mesh part from Gmsh's own VTK export; here the whole file is written."""
         if file_name_output[-3:] != "vtk":
             file_name_output += ".vtk"
         coords, conn = mesh_arrays(self.mesh)
         u = self.displacement_vectors_per_node
-        write_vtk(file_name_output, coords, conn, point_scalars=[("Displacement_Magnitude", np.hypot(u[:, 0], u[:, 1]))],
+        write_vtk(file_name_output, coords, conn,
+                  point_scalars=[("Displacement_Magnitude", np.sqrt(np.sum(u * u, axis=1)))],
                   point_vectors=[("Displacement_Vectors", u)])
         return file_name_output
+
+
+class ElasticityResults3D(ElasticityResults2D):
+    """Per-element strain, stress and energy of a linear-tetrahedron solution
+    (finite_elements/results.py:1468-1680); strain and stress rows are
+    (xx, yy, zz, xy, yz, zx), the rows of the 3D B (elements.py:743-748)."""
+
+    _ncomp = 3
+
+    def displacement_per_node_z(self):
+        return self.displacement_vectors_per_node[:, 2]
+
+    def axial_strain_z(self):
+        return self.strain[:, 2]
+
+    def axial_stress_z(self):
+        return self.stress[:, 2]
+
+    def shear_strain_xy(self):
+        return self.strain[:, 3]
+
+    def shear_strain_yz(self):
+        return self.strain[:, 4]
+
+    def shear_strain_zx(self):
+        return self.strain[:, 5]
+
+    def shear_stress_xy(self):
+        return self.stress[:, 3]
+
+    def shear_stress_yz(self):
+        return self.stress[:, 4]
+
+    def shear_stress_zx(self):
+        return self.stress[:, 5]
 
 
 class MagneticResults(Result):

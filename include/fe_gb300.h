@@ -37,6 +37,8 @@ extern "C" {
 /* element kinds (finite_elements/elements.py:333 and :56) */
 #define FE_KIND_ELASTIC_TRI   1   /* ElasticityTriangularElement2D, 2 DOF per node */
 #define FE_KIND_MAGNETIC_TRI  2   /* MagneticElement2D, 1 DOF per node             */
+#define FE_KIND_ELASTIC_TET   3   /* ElasticityTetrahedralElement3D (elements.py:663-876),
+                                     3 DOF per node, 4 nodes per element              */
 
 /* plane mode (finite_elements/elements.py:251-273) */
 #define FE_PLANE_STRESS  1
@@ -113,14 +115,18 @@ const char *fe_status_string(int status);
 const char *fe_last_error(void);
 
 /* Mesh: coords_host[2*n_nodes] (x, y per node, mesh.nodes order), conn_host[3*n_elem]
- * (node indices, groups then elements).  Replaces the mesh walk of
- * finite_elements/analysis.py:326-338,714-735 and core.py:89-108. */
+ * (node indices, groups then elements) for the triangle kinds; coords_host[3*n_nodes]
+ * (x, y, z) and conn_host[4*n_elem] for FE_KIND_ELASTIC_TET.  Replaces the mesh walk
+ * of finite_elements/analysis.py:326-338,714-735 and core.py:89-108. */
 int fe_mesh_create(int32_t kind, int64_t n_nodes, int64_t n_elem,
                    const double *coords_host, const int32_t *conn_host, fe_handle *out);
 int fe_destroy(fe_handle h);
 
 /* Per-element elastic material (elements.py:229-243,380-391): E, nu, thickness,
- * rho, each n_elem values; plane_mode FE_PLANE_STRESS or FE_PLANE_STRAIN. */
+ * rho, each n_elem values; plane_mode FE_PLANE_STRESS or FE_PLANE_STRAIN.  For
+ * tetrahedra thickness is not used (may be null) and both plane modes give the same
+ * isotropic 3D D (elements.py:779-796), but one must be chosen, as in the reference
+ * (elements.py:265-273). */
 int fe_set_elastic_materials(fe_handle h, const double *E_host, const double *nu_host,
                              const double *thickness_host, const double *rho_host,
                              int32_t plane_mode);
@@ -147,7 +153,9 @@ int fe_set_dirichlet(fe_handle h, int64_t n_bc, const int64_t *dof_host,
                      const double *value_host);
 
 /* element_to_node_factors (elements.py:18-53,156-191) of the listed elements,
- * 3 values each, written to factors_host[3*n]. */
+ * 3 values each, written to factors_host[3*n].  Triangles only: the reference defines
+ * no such factors (nor an area) for tetrahedra, so element loads and element
+ * conditions on an FE_KIND_ELASTIC_TET handle return FE_BAD_INPUT. */
 int fe_element_node_factors(fe_handle h, int64_t n, const int64_t *elements_host,
                             double *factors_host);
 
@@ -222,7 +230,9 @@ int fe_modal(fe_handle h, int32_t which, int32_t k, double sigma, int32_t steps,
 /* ---- post-processing of a solution (results.py:809-830 strain/stress, :769-781 and
  * elements.py:275-292 energy, results.py:121-152 magnetic field).  u_host / a_host:
  * n_dof values, or NULL for the handle's last solution.  Per element: strain and
- * stress 3 values each (xx, yy, xy), energy 1; magnetic field 2 (Bx, By). */
+ * stress 3 values each (xx, yy, xy), energy 1; magnetic field 2 (Bx, By).  On a
+ * tetrahedral handle strain and stress have 6 values each (xx, yy, zz, xy, yz, zx:
+ * the rows of the 3D B, elements.py:719-748). */
 int fe_post_elastic(fe_handle h, const double *u_host, double *strain_host, double *stress_host,
                     double *energy_host);
 int fe_post_magnetic(fe_handle h, const double *a_host, double *field_host);

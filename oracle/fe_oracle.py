@@ -10,6 +10,8 @@ real scipy routines the reference calls:
 
 * plane-elasticity triangle B, D and Ke = t*A*B^T D B   (elements.py:395-453, :466-511)
 * plane-elasticity triangle mass Me                     (elements.py:513-536)
+* linear tetrahedron B, isotropic 3D D, Ke = V B^T D B   (elements.py:719-827)
+* linear tetrahedron mass Me = rho V / 20 * P12          (elements.py:829-858)
 * magnetostatic triangle Ke = A/mu * (b_i b_j + c_i c_j) (elements.py:93-118)
 * element -> node factors |detJ| * N_i(mid(p2, p3))     (elements.py:18-53, :156-191)
 * ElementsLoad area split                               (loads.py:24-35)
@@ -28,6 +30,14 @@ available: the unsigned triangle area |detJ|/2 and the barycentric shape-functio
 coefficients (a_i, b_i, c_i).  No reference test pins their values ("parity
 unpinned" for those two); everything downstream of them is pinned by golden vectors
 that ``tests/golden/make_golden.py`` produced by running the reference's own code.
+
+The tetrahedron's volmdlr quantities are restated the same way: the unsigned volume
+and the form-function rows (a_i, b_i, c_i, d_i) = 6V (coefficients of N_i), the
+convention under which the reference's B = (1/(6V)) [b c d ...] is the gradient
+matrix of the linear shape functions.  No reference test or fixture pins that
+convention or any 3D value: the tetrahedron path is "parity unpinned"; its golden
+vectors come from the reference's own 3D element code run on these restated
+quantities.
 """
 from __future__ import annotations
 
@@ -37,7 +47,7 @@ import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-from finite_elements_gb300.problem import ELASTIC, MAGNETIC, Problem
+from finite_elements_gb300.problem import ELASTIC, ELASTIC3D, MAGNETIC, Problem
 
 # ---------------------------------------------------------------- element level
 
@@ -140,7 +150,83 @@ def magnetic_stiffness(prob: Problem):
     return ((1 / prob.mu)[:, None, None] * g * triangle_area(p)[:, None, None]).reshape(-1, 9)
 
 
+def tet_volume(p):
+    """Unsigned volume |det[p1-p0, p2-p0, p3-p0]| / 6 (volmdlr TetrahedralElement.volume,
+    restated)."""
+    a = p[:, 1] - p[:, 0]
+    n = np.cross(p[:, 2] - p[:, 0], p[:, 3] - p[:, 0])
+    return np.abs(a[:, 0] * n[:, 0] + a[:, 1] * n[:, 1] + a[:, 2] * n[:, 2]) / 6.0
+
+
+def tet_form_functions(p):
+    """(E, 4, 4) rows (a_i, b_i, c_i, d_i) = 6V (coefficients of N_i): N_i = (a_i + b_i x +
+    c_i y + d_i z) / (6V), N_i(p_j) = delta_ij, V the unsigned volume (volmdlr
+    TetrahedralElement.form_functions, restated in the convention the reference's B of
+    elements.py:719-748 divides by 6V)."""
+    A = np.concatenate([np.ones(p.shape[:2] + (1,)), p], axis=2)       # rows [1, x_j, y_j, z_j]
+    C = np.linalg.inv(A)                                                # column i: coefficients of N_i
+    return (6.0 * tet_volume(p))[:, None, None] * np.transpose(C, (0, 2, 1))
+
+
+def tet_b_matrix(p):
+    """(E, 6, 12) B of elements.py:719-748: rows xx, yy, zz, xy, yz, zx, scaled by
+    1 / (6 V)."""
+    ff = tet_form_functions(p)
+    b, c, d = ff[:, :, 1], ff[:, :, 2], ff[:, :, 3]
+    z = np.zeros_like(b[:, 0])
+    rows = [[], [], [], [], [], []]
+    for i in range(4):
+        rows[0] += [b[:, i], z, z]
+        rows[1] += [z, c[:, i], z]
+        rows[2] += [z, z, d[:, i]]
+        rows[3] += [c[:, i], b[:, i], z]
+        rows[4] += [z, d[:, i], c[:, i]]
+        rows[5] += [d[:, i], z, b[:, i]]
+    data = np.stack([np.stack(r, axis=1) for r in rows], axis=1)
+    return (1 / (6 * tet_volume(p)))[:, None, None] * data
+
+
+def d_matrix_3d(E, nu, plane_strain, plane_stress):
+    """(E, 6, 6) isotropic D of elements.py:779-796 (both plane flags give it; the flag
+    checks of elements.py:265-273 still apply)."""
+    if plane_strain and plane_stress:
+        raise ValueError('just one of plane_strain or plane_stress can be True')
+    if not plane_strain and not plane_stress:
+        raise ValueError('one of plane_strain or plane_stress must be True')
+    ca = 1 - nu
+    cb = (1 - 2 * nu) / 2
+    z = np.zeros_like(E)
+    data = np.stack([ca, nu, nu, z, z, z,
+                     nu, ca, nu, z, z, z,
+                     nu, nu, ca, z, z, z,
+                     z, z, z, cb, z, z,
+                     z, z, z, z, cb, z,
+                     z, z, z, z, z, cb], axis=1).reshape(-1, 6, 6)
+    coeff = E / ((1 + nu) * (1 - 2 * nu))
+    return coeff[:, None, None] * data
+
+
+def tet_stiffness(prob: Problem):
+    """(E, 144) row-major Ke = V * ((B^T D) B) (elements.py:808-827)."""
+    p = element_points(prob)
+    B = tet_b_matrix(p)
+    D = d_matrix_3d(prob.E, prob.nu, prob.plane_strain, prob.plane_stress)
+    ke = tet_volume(p)[:, None, None] * np.matmul(np.matmul(np.transpose(B, (0, 2, 1)), D), B)
+    return ke.reshape(-1, 144)
+
+
+_TET_MASS_PATTERN = np.kron(np.ones((4, 4)) + np.eye(4), np.eye(3)).reshape(-1)
+
+
+def tet_mass(prob: Problem):
+    """(E, 144) Me = ((rho * V) / 20) * P12 (elements.py:829-858)."""
+    s = (prob.rho * tet_volume(element_points(prob))) / 20
+    return s[:, None] * _TET_MASS_PATTERN[None, :]
+
+
 def element_stiffness(prob: Problem):
+    if prob.kind == ELASTIC3D:
+        return tet_stiffness(prob)
     return elastic_stiffness(prob) if prob.kind == ELASTIC else magnetic_stiffness(prob)
 
 
@@ -186,6 +272,9 @@ def node_load_list(prob: Problem):
     d = prob.dim
     keys = [prob.node_load_node * d + (prob.node_load_dim - 1)]
     vals = [prob.node_load_value]
+    if prob.kind == ELASTIC3D and prob.element_loads:
+        raise AttributeError("'ElasticityTetrahedralElement3D' object has no attribute "
+                             "'element_to_node_factors'")
     for s in prob.element_loads:
         conn = prob.conn[s.elements]
         area = triangle_area(prob.coords[conn])
@@ -210,6 +299,9 @@ def boundary_condition_list(prob: Problem):
     d = prob.dim
     keys = [prob.node_bc_node * d + (prob.node_bc_dim - 1)]
     vals = [prob.node_bc_value]
+    if prob.kind == ELASTIC3D and prob.element_bc_element.size:
+        raise AttributeError("'ElasticityTetrahedralElement3D' object has no attribute "
+                             "'element_to_node_factors'")
     if prob.element_bc_element.size:
         fac = element_node_factors(prob, prob.element_bc_element)
         conn = prob.conn[prob.element_bc_element].astype(np.int64)
@@ -239,20 +331,20 @@ def k_matrix_data(prob: Problem):
     (node-major, dimension-minor)."""
     d = prob.dim
     ke = element_stiffness(prob)
-    L = (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(-1, 3 * d)
-    nl = 3 * d
+    nl = prob.npe * d
+    L = (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(-1, nl)
     row = np.repeat(L, nl, axis=1).reshape(-1)
     col = np.tile(L, (1, nl)).reshape(-1)
     return ke.reshape(-1), row, col
 
 
 def m_matrix_data(prob: Problem):
-    if prob.kind != ELASTIC:
+    if not prob.elastic:
         raise NotImplementedError("mass matrices exist for elasticity elements only")
     d = prob.dim
-    me = elastic_mass(prob)
-    L = (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(-1, 3 * d)
-    nl = 3 * d
+    me = tet_mass(prob) if prob.kind == ELASTIC3D else elastic_mass(prob)
+    nl = prob.npe * d
+    L = (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(-1, nl)
     return me.reshape(-1), np.repeat(L, nl, axis=1).reshape(-1), np.tile(L, (1, nl)).reshape(-1)
 
 
@@ -365,13 +457,18 @@ def solve_reduced(prob: Problem, method="direct", tol=1e-12, maxiter=200000):
 def elastic_post(prob: Problem, u):
     """Per-element strain B q, stress (D B) q and energy 0.5 (q^T Ke) q
     (results.py:809-830, elements.py:275-292)."""
-    q = np.asarray(u)[: prob.n_dof].reshape(-1, 2)[prob.conn].reshape(-1, 6)
+    d, nl = prob.dim, prob.npe * prob.dim
+    q = np.asarray(u)[: prob.n_dof].reshape(-1, d)[prob.conn].reshape(-1, nl)
     p = element_points(prob)
-    B = b_matrix(p)
-    D = d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress)
+    if prob.kind == ELASTIC3D:
+        B = tet_b_matrix(p)
+        D = d_matrix_3d(prob.E, prob.nu, prob.plane_strain, prob.plane_stress)
+    else:
+        B = b_matrix(p)
+        D = d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress)
     strain = np.einsum("eij,ej->ei", B, q)
     stress = np.einsum("eij,ej->ei", np.matmul(D, B), q)
-    ke = elastic_stiffness(prob).reshape(-1, 6, 6)
+    ke = element_stiffness(prob).reshape(-1, nl, nl)
     energy = 0.5 * np.einsum("ei,eij,ej->e", q, ke, q)
     return strain, stress, energy
 

@@ -12,7 +12,7 @@ the reference checkout and runs ``create_matrix()``, ``create_source_matrix()``,
 Each case is stored as ``<name>.npz`` holding the problem as arrays (the inputs the
 GPU path takes) and the reference's outputs.  Run from the repository root:
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference [case ...]]
 """
 from __future__ import annotations
 
@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 
 from finite_elements_gb300 import mesh as fmesh          # noqa: E402
 from finite_elements_gb300 import meshgen                # noqa: E402
-from finite_elements_gb300.problem import ELASTIC, ElementLoadSet, Problem  # noqa: E402
+from finite_elements_gb300.problem import ELASTIC, ELASTIC3D, ElementLoadSet, Problem  # noqa: E402
 
 
 class _Anything:
@@ -59,9 +59,10 @@ def install_stubs():
     dc = _permissive_module("dessia_common")
     dcc = _permissive_module("dessia_common.core", DessiaObject=DessiaObject)
     dc.core = dcc
-    vm = _permissive_module("volmdlr", Point2D=fmesh.Point2D)
-    vmm = _permissive_module("volmdlr.mesh", Node2D=fmesh.Node2D,
+    vm = _permissive_module("volmdlr", Point2D=fmesh.Point2D, Point3D=fmesh.Point3D)
+    vmm = _permissive_module("volmdlr.mesh", Node2D=fmesh.Node2D, Node3D=fmesh.Node3D,
                              TriangularElement2D=fmesh.TriangularElement2D,
+                             TetrahedralElement=fmesh.TetrahedralElement,
                              ElementsGroup=fmesh.ElementsGroup, Mesh=fmesh.Mesh)
     vm.mesh = vmm
     mpl = _permissive_module("matplotlib")
@@ -78,14 +79,20 @@ def install_stubs():
 def reference_objects(fe, prob: Problem, groups):
     """Build the reference's object graph for ``prob``: nodes, elements (wrapped as
     the reference's element classes), groups, mesh, loads and conditions."""
-    nodes = [fmesh.Node2D(x, y) for x, y in prob.coords.tolist()]
-    tris = [fmesh.TriangularElement2D([nodes[i] for i in row]) for row in prob.conn.tolist()]
-    if prob.kind == ELASTIC:
-        elems = [fe.elements.ElasticityTriangularElement2D(
-            t, float(prob.E[k]), float(prob.nu[k]), float(prob.rho[k]), float(prob.thickness[k]))
-            for k, t in enumerate(tris)]
+    if prob.kind == ELASTIC3D:
+        nodes = [fmesh.Node3D(*c) for c in prob.coords.tolist()]
+        tets = [fmesh.TetrahedralElement([nodes[i] for i in row]) for row in prob.conn.tolist()]
+        elems = [fe.elements.ElasticityTetrahedralElement3D(
+            t, float(prob.E[k]), float(prob.nu[k]), float(prob.rho[k])) for k, t in enumerate(tets)]
     else:
-        elems = [fe.elements.MagneticElement2D(t, float(prob.mu[k])) for k, t in enumerate(tris)]
+        nodes = [fmesh.Node2D(x, y) for x, y in prob.coords.tolist()]
+        tris = [fmesh.TriangularElement2D([nodes[i] for i in row]) for row in prob.conn.tolist()]
+        if prob.kind == ELASTIC:
+            elems = [fe.elements.ElasticityTriangularElement2D(
+                t, float(prob.E[k]), float(prob.nu[k]), float(prob.rho[k]), float(prob.thickness[k]))
+                for k, t in enumerate(tris)]
+        else:
+            elems = [fe.elements.MagneticElement2D(t, float(prob.mu[k])) for k, t in enumerate(tris)]
     egroups = [fmesh.ElementsGroup(elems[a:b], f"g{g}") for g, (a, b) in
                enumerate(zip(groups[:-1], groups[1:]))]
     mesh = fmesh.Mesh(egroups)
@@ -112,7 +119,7 @@ def reference_objects(fe, prob: Problem, groups):
 def run_reference(fe, prob: Problem, groups):
     mesh, elems, nl, el, edl, nbc, ebc, edbc = reference_objects(fe, prob, groups)
     kw = {}
-    if prob.kind == ELASTIC:
+    if prob.elastic:
         kw = dict(plane_strain=prob.plane_strain, plane_stress=prob.plane_stress)
     analysis = fe.analysis.FiniteElementAnalysis(
         mesh=mesh, element_loads=el, edge_loads=edl, node_loads=nl, magnet_loads=[],
@@ -128,7 +135,7 @@ def run_reference(fe, prob: Problem, groups):
     ks = analysis.k_matrix_sparse()
     out["Ks_indptr"], out["Ks_indices"], out["Ks_data"] = ks.indptr, ks.indices, ks.data
     out["Ks_shape"] = np.array(ks.shape)
-    if prob.kind == ELASTIC:
+    if prob.elastic:
         ms = analysis.m_matrix_sparse()
         out["Ms_indptr"], out["Ms_indices"], out["Ms_data"] = ms.indptr, ms.indices, ms.data
         out["Ms_shape"] = np.array(ms.shape)
@@ -137,7 +144,8 @@ def run_reference(fe, prob: Problem, groups):
         out["Me"] = np.array([e.elementary_mass_matrix() for e in elems])
     else:
         out["Ke"] = np.array([e.elementary_matrix() for e in elems])
-    out["factors"] = np.array([e.element_to_node_factors() for e in elems])
+    if prob.kind != ELASTIC3D:
+        out["factors"] = np.array([e.element_to_node_factors() for e in elems])
     bcs = analysis._boundary_conditions
     out["bc_dof"] = np.array([analysis.positions[(mesh.node_to_index[b.application],
                                                   b.dimension)] for b in bcs], np.int64)
@@ -274,6 +282,48 @@ def case_quirks_magnetic():
     return prob, [0, 40, ne]
 
 
+def case_tet_single():
+    """scripts/Elasticity/beam3d_example_1.py:20-33: one tetrahedron (2,3,4), (6,3,2),
+    (2,5,1), (4,3,6), E=210e9, nu=0.25, rho=7860, plane strain; the script stops at
+    create_matrix, so three clamped vertices and a load on the fourth are added."""
+    coords = [(2, 3, 4), (6, 3, 2), (2, 5, 1), (4, 3, 6)]
+    prob = Problem(ELASTIC3D, coords, [[0, 1, 2, 3]], E=210e9, nu=0.25, rho=7860.0,
+                   plane_strain=True, plane_stress=False,
+                   node_load_node=[3, 3], node_load_dim=[3, 1], node_load_value=[-1000.0, 250.0],
+                   node_bc_node=np.repeat([0, 1, 2], 3), node_bc_dim=np.tile([1, 2, 3], 3),
+                   node_bc_value=np.zeros(9))
+    return prob, [0, 1]
+
+
+def case_tet_cantilever():
+    """The solid cantilever of scripts/Elasticity/beam3d_example_2.py (x = 0 clamped,
+    -1000 in dimension 3 on the x = 10, z = 2 edge, E=30e6, nu=0.25, rho=2.7, plane
+    stress) on a jittered 5x2x2 Kuhn grid, in two groups."""
+    p = meshgen.cantilever_3d(5, 2, 2, E=30e6, nu=0.25, rho=2.7, jitter=0.25, seed=5)
+    return p, [0, 24, p.n_elements]
+
+
+def case_tet_quirks():
+    """Repeated node loads and conditions (the last value wins), edge loads and edge
+    conditions, non-zero prescribed values and per-element E on a jittered 3x2x2 grid."""
+    rng = np.random.default_rng(11)
+    coords, conn = meshgen.box_tets(3, 2, 2, 1.5, 1.0, 1.0, jitter=0.2, rng=rng)
+    ne = conn.shape[0]
+    x = coords[:, 0]
+    left = np.flatnonzero(x == 0.0)
+    prob = Problem(ELASTIC3D, coords, conn, E=rng.uniform(50e9, 250e9, ne), nu=0.3, rho=2700.0,
+                   plane_stress=True, plane_strain=False,
+                   node_load_node=[35, 20, 35, 23, 11], node_load_dim=[3, 1, 3, 2, 1],
+                   node_load_value=[-500.0, 40.0, -800.0, 75.0, 10.0],
+                   edge_load_nodes=[[35, 31], [23, 19]], edge_load_dim=[3, 2],
+                   edge_load_value=[-300.0, 55.0],
+                   node_bc_node=np.r_[np.repeat(left, 3), left[0]],
+                   node_bc_dim=np.r_[np.tile([1, 2, 3], left.size), 1],
+                   node_bc_value=np.r_[np.zeros(3 * left.size), 2e-5],
+                   edge_bc_nodes=[[3, 7]], edge_bc_dim=[2], edge_bc_value=[4e-5])
+    return prob, [0, 30, ne]
+
+
 def cases():
     yield "ex1_stress", case_ex1("stress")
     yield "ex1_strain", case_ex1("strain")
@@ -287,6 +337,9 @@ def cases():
     yield "c2_magnetostatic_40x20", (p, [0, p.n_elements])
     p = meshgen.plane_strain_random(30, 15, seed=2)
     yield "c3_plane_strain_30x15", (p, [0, p.n_elements])
+    yield "tet_single", case_tet_single()
+    yield "tet_cantilever", case_tet_cantilever()
+    yield "tet_quirks", case_tet_quirks()
 
 
 def main():
@@ -298,7 +351,10 @@ def main():
     import finite_elements.elements      # noqa: F401
     import finite_elements.loads         # noqa: F401
     fe = sys.modules["finite_elements"]
+    only = set(sys.argv[2:])
     for name, (prob, groups) in cases():
+        if only and name not in only:
+            continue
         out = run_reference(fe, prob, groups)
         arrays = problem_arrays(prob, groups)
         arrays.update({"ref_" + k: v for k, v in out.items()})

@@ -107,13 +107,19 @@ def build_objects(name):
     """The golden case as drop-in objects (same construction as make_golden.py)."""
     from finite_elements_gb300 import conditions as C, elements as El, loads as L, mesh as M
     prob, groups, ref = gc.load(name)
-    nodes = [M.Node2D(x, y) for x, y in prob.coords.tolist()]
-    tris = [M.TriangularElement2D([nodes[i] for i in row]) for row in prob.conn.tolist()]
-    if prob.kind == "elastic":
-        elems = [El.ElasticityTriangularElement2D(t, prob.E[k], prob.nu[k], prob.rho[k], prob.thickness[k])
-                 for k, t in enumerate(tris)]
+    if prob.kind == "elastic3d":
+        nodes = [M.Node3D(*c) for c in prob.coords.tolist()]
+        tets = [M.TetrahedralElement([nodes[i] for i in row]) for row in prob.conn.tolist()]
+        elems = [El.ElasticityTetrahedralElement3D(t, prob.E[k], prob.nu[k], prob.rho[k])
+                 for k, t in enumerate(tets)]
     else:
-        elems = [El.MagneticElement2D(t, prob.mu[k]) for k, t in enumerate(tris)]
+        nodes = [M.Node2D(x, y) for x, y in prob.coords.tolist()]
+        tris = [M.TriangularElement2D([nodes[i] for i in row]) for row in prob.conn.tolist()]
+        if prob.kind == "elastic":
+            elems = [El.ElasticityTriangularElement2D(t, prob.E[k], prob.nu[k], prob.rho[k], prob.thickness[k])
+                     for k, t in enumerate(tris)]
+        else:
+            elems = [El.MagneticElement2D(t, prob.mu[k]) for k, t in enumerate(tris)]
     mesh = M.Mesh([M.ElementsGroup(elems[a:b]) for a, b in zip(groups[:-1], groups[1:])])
     mesh.nodes = nodes
     mesh.node_to_index = {p: i for i, p in enumerate(nodes)}
@@ -133,7 +139,7 @@ def build_objects(name):
         edge_boundary_conditions=[C.EdgeBoundaryCondition(M.LineSegment2D(nodes[a], nodes[b]), v, d)
                                   for (a, b), d, v in zip(prob.edge_bc_nodes.tolist(), prob.edge_bc_dim,
                                                           prob.edge_bc_value)])
-    if prob.kind == "elastic":
+    if prob.elastic:
         kw.update(plane_strain=prob.plane_strain, plane_stress=prob.plane_stress)
     return prob, ref, mesh, kw
 

@@ -30,12 +30,17 @@ def test_post_matches_oracle(gpu_lib, name):
     s = GpuSystem(prob)
     x = ref["x"]
     res = s.post(x)
-    if prob.kind == "elastic":
+    if prob.elastic:
         strain, stress, energy = O.elastic_post(prob, x)
-        q = np.abs(x[: prob.n_dof].reshape(-1, 2)[prob.conn].reshape(-1, 6))
-        B = np.abs(O.b_matrix(O.element_points(prob)))
-        D = np.abs(O.d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress))
-        ke = np.abs(O.elastic_stiffness(prob).reshape(-1, 6, 6))
+        d, nl = prob.dim, prob.npe * prob.dim
+        q = np.abs(x[: prob.n_dof].reshape(-1, d)[prob.conn].reshape(-1, nl))
+        if prob.kind == "elastic3d":
+            B = np.abs(O.tet_b_matrix(O.element_points(prob)))
+            D = np.abs(O.d_matrix_3d(prob.E, prob.nu, prob.plane_strain, prob.plane_stress))
+        else:
+            B = np.abs(O.b_matrix(O.element_points(prob)))
+            D = np.abs(O.d_matrix(prob.E, prob.nu, prob.plane_strain, prob.plane_stress))
+        ke = np.abs(O.element_stiffness(prob).reshape(-1, nl, nl))
         assert within(res["strain"], strain, np.einsum("eij,ej->ei", B, q))
         assert within(res["stress"], stress, np.einsum("eij,ej->ei", np.matmul(D, B), q))
         assert within(res["energy"], energy, 0.5 * np.einsum("ei,eij,ej->e", q, ke, q))
