@@ -71,6 +71,8 @@ _SIGNATURES = {
     "fe_set_element_loads": ([_P, _I64, _P, _P, _P, _P, _I64], C.c_int),
     "fe_set_dirichlet": ([_P, _I64, _P, _P], C.c_int),
     "fe_element_node_factors": ([_P, _I64, _P, _P], C.c_int),
+    "fe_set_rhs_additions": ([_P, _I64, _P, _P], C.c_int),
+    "fe_set_continuity": ([_P, _I64, _P, _P, _P], C.c_int),
     "fe_assemble": ([_P, _I32], C.c_int),
     "fe_export_sizes": ([_P, _I32, _PI64, _PI64, _PI64], C.c_int),
     "fe_export_csr": ([_P, _I32, _P, _P, _P], C.c_int),

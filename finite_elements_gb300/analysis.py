@@ -12,8 +12,13 @@ Same constructor, methods, return types and error behaviour as the reference's
 
 Instead of scipy's sparse LU on the saddle system, the GPU eliminates the Dirichlet
 DOFs, solves the SPD system with PCG and recovers each multiplier from the first
-block row, lambda_i = (F - K u)[dof_i].  Continuity conditions and magnet loads are
-not on this path and raise NotImplementedError.
+block row, lambda_i = (F - K u)[dof_i].  Magnet loads become additive right-hand-side
+entries (analysis.py:556-577).  Continuity conditions enter create_matrix at the
+reference's own rows n_nodes + len(node_loads) + i (analysis.py:175-199), and solve()
+raises scipy's dimension-mismatch ValueError wherever those rows make the matrix and
+the right-hand side disagree in size, as spsolve does; where they agree (the rows
+follow the Dirichlet rows) the GPU solves with a projected FP64 PCG and returns the
+continuity multipliers after the Dirichlet ones.
 """
 from __future__ import annotations
 
@@ -22,9 +27,9 @@ import warnings
 import numpy as np
 import scipy.sparse.linalg as spla
 
-from .engine import GpuSystem, check_plane_flags
+from .engine import GpuSystem, check_plane_flags, dirichlet_count
 from .mesh import ArrayMesh
-from .problem import ELASTIC, ELASTIC3D, MAGNETIC, ElementLoadSet, Problem
+from .problem import ELASTIC, ELASTIC3D, MAGNETIC, ElementLoadSet, MagnetLoadSet, Problem
 from .results import Result
 
 DEFAULT_SOLVER = {"precision": "fp64", "tol": 1e-14, "accept_stagnation": True, "cheb_degree": 0}
@@ -119,10 +124,6 @@ class FiniteElementAnalysis:
         """The analysis as arrays (mesh walk of analysis.py:326-338, :714-735)."""
         if self._problem is not None:
             return self._problem
-        if self.continuity_conditions:
-            raise NotImplementedError("continuity conditions are not part of the GPU path")
-        if self.magnet_loads:
-            raise NotImplementedError("magnet loads are not part of the GPU path")
         mesh = self.mesh
         nodes = mesh.nodes
         index = mesh.node_to_index
@@ -161,6 +162,11 @@ class FiniteElementAnalysis:
         nl = self.node_loads
         el_loads = [ElementLoadSet(np.array([element_index(e) for e in ld.elements], np.int64),
                                    ld.value, ld.dimension) for ld in self.element_loads]
+        magnets = [MagnetLoadSet(np.array([element_index(e) for e in ml.elements], np.int64),
+                                 np.array([index[p] for p in ml.non_contour_nodes], np.int64),
+                                 (float(ml.magnetization_vector[0]), float(ml.magnetization_vector[1])))
+                   for ml in self.magnet_loads]
+        cc = self.continuity_conditions
         prob = Problem(
             kind, coords, conn, **kw,
             node_load_node=[index[ld.node] for ld in nl], node_load_dim=[ld.dimension for ld in nl],
@@ -177,7 +183,9 @@ class FiniteElementAnalysis:
             edge_bc_nodes=[[index[c.application.start], index[c.application.end]]
                            for c in self.edge_boundary_conditions],
             edge_bc_dim=[c.dimension for c in self.edge_boundary_conditions],
-            edge_bc_value=[c.value for c in self.edge_boundary_conditions])
+            edge_bc_value=[c.value for c in self.edge_boundary_conditions],
+            magnet_loads=magnets, cont_node1=[index[c.node1] for c in cc],
+            cont_node2=[index[c.node2] for c in cc], cont_value=[c.value for c in cc])
         self._problem = prob
         return prob
 
@@ -232,8 +240,27 @@ class FiniteElementAnalysis:
         """(E, (3*dim)^2) row-major element matrices from the GPU element kernels."""
         return self.system().element_matrices(which)
 
+    def _check_shapes(self):
+        """spsolve's check of the reference's create_matrix against its
+        create_source_matrix: with continuity conditions the matrix spans its largest
+        row index + 1 (analysis.py:186-199, :656), the right-hand side
+        n*dim + n_cont + n_bc rows (analysis.py:737-739)."""
+        prob = self.problem()
+        if not prob.n_cont:
+            return
+        n_bc = dirichlet_count(prob)
+        top = max(int(prob.conn.max()) + 1 if prob.conn.size else 0, 0) * prob.dim
+        if n_bc:
+            top = max(top, prob.n_dof + n_bc)
+        top = max(top, prob.n_nodes + prob.node_load_node.size + prob.n_cont,
+                  int(max(prob.cont_node1.max(), prob.cont_node2.max())) + 1)
+        n_f = prob.n_dof + prob.n_cont + n_bc
+        if top != n_f:
+            raise ValueError(f"matrix - rhs dimension mismatch (({top}, {top}) - {n_f})")
+
     def solve(self):
         """PCG on the GPU in place of spsolve (analysis.py:798-830)."""
+        self._check_shapes()
         sysm = self.system()
         self._boundary_conditions = list(zip(sysm.bc_dof.tolist(), sysm.bc_value.tolist()))
         opts = dict(self.solver)

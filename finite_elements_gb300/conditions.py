@@ -42,8 +42,9 @@ class ElementBoundaryCondition(BoundaryCondition):
 
 
 class ContinuityCondition:
-    """Periodic / anti-periodic link of two nodes (conditions.py:196-241).  Not part of
-    the GPU path: an analysis given one raises NotImplementedError."""
+    """Periodic (value 1) or anti-periodic (value -1) link of two nodes,
+    A(node1) = value * A(node2) (conditions.py:196-241); one multiplier row in the
+    analysis (analysis.py:175-199)."""
 
     def __init__(self, node1, node2, value):
         self.node1 = node1

@@ -142,6 +142,7 @@ int fe_destroy(fe_handle h) {
     dfree(h->ke), dfree(h->me_scale), dfree(h->kval), dfree(h->mval), dfree(h->aval), dfree(h->aval32);
     dfree(h->dinv), dfree(h->dinv32), dfree(h->srow), dfree(h->sell_off), dfree(h->sell_col), dfree(h->sell_dcol), dfree(h->sell_over);
     dfree(h->sell_val64), dfree(h->sell_val32), dfree(h->diag64), dfree(h->diag32), dfree(h->dblk32), dfree(h->F), dfree(h->b), dfree(h->load_seq), dfree(h->lambda);
+    dfree(h->add_dof), dfree(h->add_ptr), dfree(h->add_val), dfree(h->comp_ptr), dfree(h->comp_dof), dfree(h->comp_s);
     dfree(h->err);
     if (h->err_host) cudaFreeHost(h->err_host);
     for (auto &e : h->events)
@@ -252,6 +253,7 @@ int fe_set_dirichlet(fe_handle h, int64_t n_bc, const int64_t *dof, const double
     }
     FE_CHECK(upload(h->bc_dof, dof, n_bc, h->stream));
     FE_CHECK(upload(h->bc_val, value, n_bc, h->stream));
+    h->bc_dof_host.assign(dof, dof + n_bc);
     h->n_bc = n_bc;
     h->sys_ready = false;
     h->have_solution = false;
@@ -382,6 +384,8 @@ int fe_get_solution(fe_handle h, double *x) {
         FE_CUDA(cudaMemcpyAsync(x + h->n_dof, h->lambda.p, h->n_bc * sizeof(double), cudaMemcpyDeviceToHost,
                                 h->stream));
     FE_CUDA(cudaStreamSynchronize(h->stream));
+    // continuity multipliers after the Dirichlet ones (rows n_dof + n_bc + k)
+    for (int64_t k = 0; k < h->n_cont; ++k) x[h->n_dof + h->n_bc + k] = h->mu_host[(size_t)k];
     return FE_OK;
 }
 

@@ -1070,6 +1070,8 @@ int assemble_loads(fe_handle_s *h) {
             h->load_seq_base, h->dim, h->n_elem, h->coords.p, h->conn.p, h->load_seq.p, h->F.p, h->err.p);
         FE_LAUNCH_CHECK();
     }
+    // magnet-load contributions, added after the loads (analysis.py:681-708)
+    FE_CHECK(apply_rhs_additions(h));
     h->launches += 1 + (h->n_node_loads > 0 ? 2 : 0) + (h->n_load_elems > 0 ? 4 : 0);
     h->f_ready = true;
     return FE_OK;

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 #include <type_traits>
 
 #include "../../include/fe_gb300.h"
@@ -177,6 +178,26 @@ struct fe_handle_s {
     fe::DBuf<int64_t> bc_dof;
     fe::DBuf<double> bc_val;
     fe::DBuf<int32_t> bc_of_dof;  // [n_dof] multiplier index or -1
+    std::vector<int64_t> bc_dof_host;
+
+    // additive right-hand-side entries (magnet loads): unique DOFs, and per DOF the
+    // values in list order, add_ptr[k] .. add_ptr[k+1]
+    int64_t n_add_dofs = 0;
+    fe::DBuf<int64_t> add_dof, add_ptr;
+    fe::DBuf<double> add_val;
+
+    // continuity conditions u[dof1] = value * u[dof2], grouped into trees of linked
+    // DOFs: on a tree the admissible vectors are t * s (s_root = 1); comp_* on the
+    // device for the projection, the host keeps each tree in BFS order for the
+    // multipliers
+    int64_t n_cont = 0, n_comp = 0;
+    std::vector<int64_t> cont_d1, cont_d2;
+    std::vector<double> cont_v;
+    std::vector<int64_t> comp_ptr_h, comp_dof_h, comp_edge_h;   // edge to the BFS parent (-1 at roots)
+    std::vector<double> comp_s_h;
+    fe::DBuf<int64_t> comp_ptr, comp_dof;
+    fe::DBuf<double> comp_s;
+    std::vector<double> mu_host;   // continuity multipliers of the last solve
 
     // pattern: node-block CSR
     bool pattern_ready = false;
@@ -250,6 +271,11 @@ int solve(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
 int modal(fe_handle_s *h, int which, int k, double sigma, int steps, int precision, double *eigvals,
           double *eigvecs, double *resid);
 int recover_multipliers(fe_handle_s *h);
+// Continuity conditions (fe_continuity.cu): host set-up and the projected FP64 PCG
+int set_continuity(fe_handle_s *h, int64_t n, const int64_t *dof1, const int64_t *dof2, const double *value);
+int solve_continuity(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
+int set_rhs_additions(fe_handle_s *h, int64_t n, const int64_t *dof, const double *value);
+int apply_rhs_additions(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);
 int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);
 int profile_kernels(fe_handle_s *h, int enable);

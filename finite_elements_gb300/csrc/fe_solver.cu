@@ -1652,11 +1652,14 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         FE_CHECK(dalloc(h->lambda, (size_t)std::max<int64_t>(h->n_bc, 1)));
         FE_CUDA(cudaMemsetAsync(h->lambda.p, 0xff, std::max<int64_t>(h->n_bc, 1) * sizeof(double), h->stream));
         FE_CUDA(cudaStreamSynchronize(h->stream));
+        h->mu_host.assign((size_t)h->n_cont, NAN);
         st->status = FE_BREAKDOWN;
         st->relres = NAN;
         h->have_solution = true;
         return FE_OK;
     }
+    // continuity conditions: the projected FP64 PCG, whatever the precision asked
+    if (h->n_cont > 0) return solve_continuity(h, o, st);
     int lanes = 2;
     FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
     FE_CUDA(cudaEventRecord(h->events[6], h->stream));

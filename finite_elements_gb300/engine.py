@@ -37,6 +37,17 @@ def check_plane_flags(plane_strain, plane_stress):
         raise ValueError('one of plane_strain or plane_stress must be True')
 
 
+def dirichlet_count(prob: Problem):
+    """Number of multiplier rows: the distinct (node, dimension) keys of the node,
+    element and edge conditions (analysis.py:28-68, :249-265)."""
+    d = prob.dim
+    keys = set((prob.node_bc_node * d + prob.node_bc_dim - 1).tolist())
+    for e, dm in zip(prob.element_bc_element.tolist(), prob.element_bc_dim.tolist()):
+        keys.update((prob.conn[e].astype(np.int64) * d + dm - 1).tolist())
+    keys.update((prob.edge_bc_nodes * d + prob.edge_bc_dim[:, None] - 1).reshape(-1).tolist())
+    return len(keys)
+
+
 def _index_dtype(n):
     return np.int32 if n < 2 ** 31 else np.int64
 
@@ -69,6 +80,7 @@ class GpuSystem:
         self.bc_dof, self.bc_value = self._dirichlet()
         h.call("fe_set_dirichlet", len(self.bc_dof), ptr(self.bc_dof), ptr(self.bc_value))
         self._set_loads()
+        self._set_continuity()
         self.m_assembled = False
         if assemble:
             self.assemble()
@@ -141,6 +153,21 @@ class GpuSystem:
         val_a = np.array(vals, np.float64)
         seq_a = np.array(seqs, np.int64)
         self.handle.call("fe_set_node_loads", dof_a.size, ptr(dof_a), ptr(val_a), ptr(seq_a))
+        # magnet loads: added after the loads, indexed by node (analysis.py:556-577)
+        if p.magnet_loads:
+            from .loads import magnet_contributions
+            parts = [magnet_contributions(p.coords, p.conn, m.elements, m.non_contour_nodes, m.magnetization)
+                     for m in p.magnet_loads]
+            nodes = np.ascontiguousarray(np.concatenate([a for a, _ in parts]), np.int64)
+            vals = np.ascontiguousarray(np.concatenate([v for _, v in parts]), np.float64)
+            self.handle.call("fe_set_rhs_additions", nodes.size, ptr(nodes), ptr(vals))
+
+    def _set_continuity(self):
+        """Continuity conditions, DOF = node index as in analysis.py:186-189."""
+        p = self.prob
+        if p.n_cont:
+            self.handle.call("fe_set_continuity", p.n_cont, ptr(p.cont_node1), ptr(p.cont_node2),
+                             ptr(p.cont_value))
 
     # ------------------------------------------------------------ device work
 
@@ -162,15 +189,35 @@ class GpuSystem:
         idt = _index_dtype(max(nz, nrows, ncols))
         return (data[:nz], indices[:nz].astype(idt, copy=False), indptr.astype(idt)), (nrows, ncols)
 
+    def continuity_triplets(self):
+        """(data, row, col) of c_matrix_continuity_conditions (analysis.py:175-199):
+        row n_nodes + len(node_loads) + i, columns the two node indices, data
+        (1, 1, -value, -value)."""
+        p = self.prob
+        i = np.arange(p.n_cont, dtype=np.int64)
+        row_c = p.n_nodes + p.node_load_node.size + i
+        data = np.stack([np.ones(p.n_cont), np.ones(p.n_cont), -p.cont_value, -p.cont_value], 1).reshape(-1)
+        row = np.stack([row_c, p.cont_node1, row_c, p.cont_node2], 1).reshape(-1)
+        col = np.stack([p.cont_node1, row_c, p.cont_node2, row_c], 1).reshape(-1)
+        return data, row, col
+
     def create_matrix(self):
         arrays, shape = self._export(_lib.FE_MAT_K_AUGMENTED)
-        return sp.csr_matrix(arrays, shape=shape)
+        m = sp.csr_matrix(arrays, shape=shape)
+        if self.prob.n_cont:
+            # the continuity entries at the reference's own rows, then scipy's duplicate
+            # summation and shape inference from the largest index
+            coo = m.tocoo()
+            d, r, c = self.continuity_triplets()
+            m = sp.csr_matrix((np.r_[coo.data, d], (np.r_[coo.row, r], np.r_[coo.col, c])))
+        return m
 
     def create_source_matrix(self):
         n = self.prob.n_dof + len(self.bc_dof)
         out = np.empty(n, np.float64)
         self.handle.call("fe_export_rhs", ptr(out))
-        return out.reshape(-1, 1)
+        # n*dim + n_cont + n_bc rows; the continuity rows have no source (analysis.py:737-739)
+        return np.r_[out, np.zeros(self.prob.n_cont)].reshape(-1, 1)
 
     def k_matrix_sparse(self):
         arrays, shape = self._export(_lib.FE_MAT_K_CSC)
@@ -222,7 +269,7 @@ class GpuSystem:
                    | (_lib.FE_SOLVE_RESTART_EACH_STEP if restart_each_step else 0)
                    | (_lib.FE_SOLVE_X0_IF_BETTER if x0_if_better else 0))
         st = SolveStats()
-        x = np.empty(self.prob.n_dof + len(self.bc_dof)) if want_host else None
+        x = np.empty(self.prob.n_dof + len(self.bc_dof) + self.prob.n_cont) if want_host else None
         lib = _lib.load()
         status = lib.fe_solve(self.handle.h, o, ptr(x) if want_host else None, st)
         if status not in (_lib.FE_OK, _lib.FE_MAXITER, _lib.FE_BREAKDOWN, _lib.FE_NONFINITE):

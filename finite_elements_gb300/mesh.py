@@ -10,7 +10,10 @@ small surface of them:
   (elements.py:35-44, :100-116, :508, :530; loads.py:32-34);
 * ``TetrahedralElement.points`` / ``.volume`` / ``.form_functions``
   (elements.py:719-748, :808-858);
-* edge objects with ``.start`` / ``.end`` (analysis.py:232-233, :441-442).
+* edge objects with ``.start`` / ``.end`` (analysis.py:232-233, :441-442);
+* for magnet loads, ``TriangularElement2D.linear_elements`` with ``.points``,
+  ``.interior_normal`` and ``.length()``, and ``Vector2D.Dot`` (loads.py:129-147,
+  analysis.py:556-577).
 
 volmdlr is not a dependency of this package, so these classes provide that surface.
 Real volmdlr objects with the same attributes work as well (the analysis only
@@ -19,6 +22,8 @@ connectivity as arrays, so that meshes of millions of triangles never become Pyt
 objects on the host.
 """
 from __future__ import annotations
+
+import math
 
 import numpy as np
 
@@ -54,6 +59,48 @@ class Point2D:
 
 class Node2D(Point2D):
     """A mesh node (volmdlr.mesh.Node2D)."""
+
+
+class Vector2D(Point2D):
+    """A 2D vector (volmdlr.Vector2D): the dot product and the scaling MagnetLoad uses.
+    Built from (x, y) or from one (x, y) sequence."""
+
+    def __init__(self, x, y=None):
+        if y is None:
+            x, y = x
+        Point2D.__init__(self, x, y)
+
+    def Dot(self, other):
+        return self.x * other[0] + self.y * other[1]
+
+    def __truediv__(self, k):
+        return Vector2D(self.x / k, self.y / k)
+
+    def __neg__(self):
+        return Vector2D(-self.x, -self.y)
+
+
+class LinearElement:
+    """An edge of a triangle with the unit normal pointing into that triangle
+    (volmdlr.mesh.LinearElement).  Two edges are equal when they join the same two
+    points, in either direction, so that counting edges over a set of triangles finds
+    its contour (loads.py:129-147)."""
+
+    def __init__(self, start, end, interior_normal):
+        self.points = [start, end]
+        self.interior_normal = interior_normal
+
+    def length(self):
+        (x1, y1), (x2, y2) = self.points
+        return math.sqrt((x2 - x1) ** 2 + (y2 - y1) ** 2)
+
+    def __hash__(self):
+        return hash(self.points[0]) + hash(self.points[1])
+
+    def __eq__(self, other):
+        a, b = self.points
+        c, d = other.points
+        return (a == c and b == d) or (a == d and b == c)
 
 
 class Point3D:
@@ -139,6 +186,28 @@ class TriangularElement2D:
     def center(self):
         xy = self._xy()
         return Point2D(sum(p[0] for p in xy) / 3.0, sum(p[1] for p in xy) / 3.0)
+
+    @property
+    def linear_elements(self):
+        """The edges (p1, p2), (p2, p3), (p3, p1), each with its unit normal turned
+        towards the opposite vertex."""
+        out = []
+        for i in range(3):
+            a, b, c = self.points[i], self.points[(i + 1) % 3], self.points[(i + 2) % 3]
+            n = interior_normal(a, b, c)
+            out.append(LinearElement(a, b, Vector2D(n[0], n[1])))
+        return out
+
+
+def interior_normal(a, b, c):
+    """Unit normal of the edge a -> b pointing to the side of c: the edge direction
+    turned by +90 degrees, negated when it points away from c."""
+    tx, ty = float(b[0]) - float(a[0]), float(b[1]) - float(a[1])
+    length = math.sqrt(tx * tx + ty * ty)
+    nx, ny = -ty / length, tx / length
+    if nx * (float(c[0]) - float(a[0])) + ny * (float(c[1]) - float(a[1])) < 0:
+        nx, ny = -nx, -ny
+    return nx, ny
 
 
 class TetrahedralElement:

@@ -44,6 +44,16 @@ class ElementLoadSet:
 
 
 @dataclass
+class MagnetLoadSet:
+    """One ``MagnetLoad`` (loads.py:105-147): its triangles, the nodes that are not on
+    the magnet's contour, and the magnetization vector (mx, my)."""
+
+    elements: np.ndarray
+    non_contour_nodes: np.ndarray
+    magnetization: tuple
+
+
+@dataclass
 class Problem:
     """Everything the GPU path needs for one analysis, as arrays.
 
@@ -62,6 +72,10 @@ class Problem:
     node_bcs        (node, dim, value) in user order
     element_bcs     (element, dim, value) in user order
     edge_bcs        (node_a, node_b, dim, value) in user order
+    magnet_loads    list of MagnetLoadSet in user order (triangles)
+    continuity      (node1, node2, value) in user order: u[node1] = value * u[node2],
+                    the reference indexing the DOF by the node index
+                    (analysis.py:175-199)
     """
 
     kind: str
@@ -90,6 +104,10 @@ class Problem:
     edge_bc_nodes: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
     edge_bc_dim: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     edge_bc_value: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    magnet_loads: list = field(default_factory=list)
+    cont_node1: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
+    cont_node2: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
+    cont_value: np.ndarray = field(default_factory=lambda: np.zeros(0))
 
     def __post_init__(self):
         if self.kind not in _DIM:
@@ -103,15 +121,19 @@ class Problem:
             if v is not None:
                 setattr(self, name, _f64(v, ne))
         for name in ("node_load_node", "node_load_dim", "node_bc_node", "node_bc_dim",
-                     "element_bc_element", "element_bc_dim", "edge_load_dim", "edge_bc_dim"):
+                     "element_bc_element", "element_bc_dim", "edge_load_dim", "edge_bc_dim",
+                     "cont_node1", "cont_node2"):
             setattr(self, name, _i64(getattr(self, name)))
         for name in ("node_load_value", "node_bc_value", "element_bc_value",
-                     "edge_load_value", "edge_bc_value"):
+                     "edge_load_value", "edge_bc_value", "cont_value"):
             setattr(self, name, _f64(getattr(self, name)))
         self.edge_load_nodes = _i64(self.edge_load_nodes).reshape(-1, 2)
         self.edge_bc_nodes = _i64(self.edge_bc_nodes).reshape(-1, 2)
         self.element_loads = [ElementLoadSet(_i64(s.elements), float(s.value), int(s.dimension))
                               for s in self.element_loads]
+        self.magnet_loads = [MagnetLoadSet(_i64(s.elements), _i64(s.non_contour_nodes),
+                                           (float(s.magnetization[0]), float(s.magnetization[1])))
+                             for s in self.magnet_loads]
 
     @property
     def dim(self) -> int:
@@ -137,3 +159,7 @@ class Problem:
     @property
     def n_dof(self) -> int:
         return self.n_nodes * self.dim
+
+    @property
+    def n_cont(self) -> int:
+        return self.cont_node1.size

@@ -152,6 +152,23 @@ int fe_set_element_loads(fe_handle h, int64_t n_sets, const int64_t *set_ptr_hos
 int fe_set_dirichlet(fe_handle h, int64_t n_bc, const int64_t *dof_host,
                      const double *value_host);
 
+/* Additive right-hand-side entries: F[dof_k] += value_k after the loads, in list
+ * order per DOF.  These are the magnet-load contributions that create_source_matrix
+ * adds with += (analysis.py:556-577, :681-708; loads.py:129-147).  The reference
+ * indexes them by node index, whatever the dimension. */
+int fe_set_rhs_additions(fe_handle h, int64_t n, const int64_t *dof_host, const double *value_host);
+
+/* Continuity conditions (conditions.py:196-241, analysis.py:175-199):
+ * u[dof1_k] = value_k * u[dof2_k], one multiplier each; the reference uses the node
+ * index as the DOF.  The conditions must link DOFs as trees (no cycle), with a finite,
+ * non-zero value, and on DOFs without a Dirichlet condition (FE_BAD_INPUT at
+ * fe_solve otherwise).  fe_solve then runs a projected FP64 PCG from x = 0 with the
+ * node-block Jacobi preconditioner, whatever the precision, Chebyshev degree or x0
+ * asked, and the solution holds n_dof + n_bc + n continuity values: u, the Dirichlet
+ * multipliers, then these multipliers. */
+int fe_set_continuity(fe_handle h, int64_t n, const int64_t *dof1_host, const int64_t *dof2_host,
+                      const double *value_host);
+
 /* element_to_node_factors (elements.py:18-53,156-191) of the listed elements,
  * 3 values each, written to factors_host[3*n].  Triangles only: the reference defines
  * no such factors (nor an area) for tetrahedra, so element loads and element
@@ -169,14 +186,16 @@ int fe_export_csr(fe_handle h, int32_t which, int64_t *indptr_host, int32_t *ind
                   double *data_host);
 /* create_source_matrix: n_dof load entries then n_bc prescribed values. */
 int fe_export_rhs(fe_handle h, double *rhs_host);
-/* Element matrices, row-major (3*dim)^2 per element: which = FE_ASSEMBLE_K or _M. */
+/* Element matrices, row-major (npe*dim)^2 per element (npe = 3 nodes per triangle, 4
+ * per tetrahedron): which = FE_ASSEMBLE_K or _M. */
 int fe_export_element_matrices(fe_handle h, int32_t which, double *out_host);
 
 /* Solve the eliminated system with PCG and recover the multipliers
  * lambda_i = (F - K u)[dof_i].  x_host (optional) receives n_dof + n_bc values,
- * u then lambda, as solve() returns them (analysis.py:816-830). */
+ * u then lambda, as solve() returns them (analysis.py:816-830), followed by the
+ * n_cont continuity multipliers when fe_set_continuity set any. */
 int fe_solve(fe_handle h, const fe_solve_opts *opts, double *x_host, fe_solve_stats *stats);
-/* Copy the last solution (n_dof + n_bc values) to the host. */
+/* Copy the last solution (n_dof + n_bc [+ n_cont] values) to the host. */
 int fe_get_solution(fe_handle h, double *x_host);
 /* Device address of the last solution u (n_dof doubles), valid until the next solve. */
 int fe_solution_device_ptr(fe_handle h, const double **ptr);

@@ -23,6 +23,8 @@ real scipy routines the reference calls:
 * scipy.sparse.csr_matrix of the triplets               (analysis.py:617-663)
 * F vector                                              (analysis.py:665-708, :737-739)
 * spsolve(K, F, permc_spec='NATURAL', use_umfpack=True) (analysis.py:798-830)
+* magnet loads: contour edges, (M . t) L / 2 per end    (loads.py:129-147, analysis.py:556-577)
+* continuity rows n + len(node_loads) + i, (1,1,-v,-v)  (analysis.py:175-199, conditions.py:196-241)
 * dict-merged K / M as csc_matrix                       (analysis.py:345-405)
 
 Two volmdlr quantities are restated from their definitions, because volmdlr is not
@@ -348,26 +350,90 @@ def m_matrix_data(prob: Problem):
     return me.reshape(-1), np.repeat(L, nl, axis=1).reshape(-1), np.tile(L, (1, nl)).reshape(-1)
 
 
+def continuity_matrix_data(prob: Problem):
+    """c_matrix_continuity_conditions (analysis.py:175-199) as written: condition i at
+    row len(nodes) + len(node_loads) + i (user NodeLoads only), columns the two node
+    indices, data ContinuityCondition.c_matrix() = (1, 1, -value, -value)."""
+    data, row, col = [], [], []
+    base = prob.n_nodes + prob.node_load_node.size
+    for i, (a, b, v) in enumerate(zip(prob.cont_node1.tolist(), prob.cont_node2.tolist(),
+                                      prob.cont_value.tolist())):
+        data += [1, 1, -v, -v]
+        row += [base + i, a, base + i, b]
+        col += [a, base + i, b, base + i]
+    return np.array(data, np.float64), np.array(row, np.int64), np.array(col, np.int64)
+
+
 def create_matrix(prob: Problem):
-    """Augmented saddle-point matrix as scipy builds it (analysis.py:617-663)."""
+    """Augmented saddle-point matrix as scipy builds it (analysis.py:617-663): the
+    triplets of k_matrix_data, c_matrix_continuity_conditions and
+    c_matrix_boundary_conditions in that order."""
     data, row, col = k_matrix_data(prob)
+    cd, cr, cc = continuity_matrix_data(prob)
     bc_dof, _ = boundary_conditions(prob)
     nd = prob.n_dof
     i = np.arange(bc_dof.size, dtype=np.int64)
-    data = np.concatenate([data, np.ones(2 * bc_dof.size)])
-    row = np.concatenate([row, np.stack([nd + i, bc_dof], axis=1).reshape(-1)])
-    col = np.concatenate([col, np.stack([bc_dof, nd + i], axis=1).reshape(-1)])
+    data = np.concatenate([data, cd, np.ones(2 * bc_dof.size)])
+    row = np.concatenate([row, cr, np.stack([nd + i, bc_dof], axis=1).reshape(-1)])
+    col = np.concatenate([col, cc, np.stack([bc_dof, nd + i], axis=1).reshape(-1)])
     return sp.csr_matrix((data, (row, col)))
 
 
+def _interior_normal(a, b, c):
+    tx, ty = b[0] - a[0], b[1] - a[1]
+    length = np.sqrt(tx * tx + ty * ty)
+    nx, ny = -ty / length, tx / length
+    if nx * (c[0] - a[0]) + ny * (c[1] - a[1]) < 0:
+        nx, ny = -nx, -ny
+    return nx, ny
+
+
+def magnet_source(prob: Problem):
+    """(rows, values) of source_c_matrix_magnet_loads (analysis.py:556-577), in its order:
+    per MagnetLoad the contour edges of contour_linear_elements (loads.py:129-147) --
+    a dict of edges counted over the triangles' edges (p1,p2), (p2,p3), (p3,p1), kept
+    when counted once and not both points non-contour -- each adding
+    M . (-n_y, n_x) * length / 2 at its two points, n the edge's unit normal pointing
+    into its triangle (volmdlr's LinearElement.interior_normal, restated)."""
+    rows, vals = [], []
+    for ml in prob.magnet_loads:
+        count, info = {}, {}
+        for e in ml.elements.tolist():
+            t = prob.conn[e].tolist()
+            for i in range(3):
+                a, b, c = t[i], t[(i + 1) % 3], t[(i + 2) % 3]
+                key = (min(a, b), max(a, b))
+                if key not in count:
+                    count[key] = 1
+                    info[key] = (a, b, c)
+                else:
+                    count[key] += 1
+        nc = set(ml.non_contour_nodes.tolist())
+        mx, my = ml.magnetization
+        for key, k in count.items():
+            a, b, c = info[key]
+            if k == 1 and (a not in nc or b not in nc):
+                pa, pb, pc = prob.coords[a], prob.coords[b], prob.coords[c]
+                nx, ny = _interior_normal(pa, pb, pc)
+                length = np.sqrt((pb[0] - pa[0]) ** 2 + (pb[1] - pa[1]) ** 2)
+                v = (mx * -ny + my * nx) * length / 2
+                rows += [a, b]
+                vals += [v, v]
+    return np.array(rows, np.int64), np.array(vals, np.float64)
+
+
 def create_source_matrix(prob: Problem):
-    """Dense (n*dim + n_bc, 1) right-hand side (analysis.py:665-708, :737-739)."""
+    """Dense (n*dim + n_cont + n_bc, 1) right-hand side (analysis.py:665-708,
+    :737-739): the de-duplicated loads, then += each magnet contribution in order,
+    then the prescribed values at rows n*dim + i."""
     lk, lv = node_loads(prob)
     bc_dof, bc_val = boundary_conditions(prob)
     nd = prob.n_dof
-    f = np.zeros((nd + bc_dof.size, 1))
+    f = np.zeros((nd + prob.n_cont + bc_dof.size, 1))
     np.add.at(f[:, 0], lk, lv)
-    f[nd:, 0] += bc_val
+    for r, v in zip(*magnet_source(prob)):
+        f[r, 0] += v
+    f[nd:nd + bc_dof.size, 0] += bc_val
     return f
 
 
@@ -422,6 +488,8 @@ def reduced_system(prob: Problem):
     lk, lv = node_loads(prob)
     F = np.zeros(nd)
     np.add.at(F, lk, lv)
+    for r, v in zip(*magnet_source(prob)):
+        F[r] += v
     bc_dof, bc_val = boundary_conditions(prob)
     mask = np.ones(nd, bool)
     mask[bc_dof] = False

@@ -28,7 +28,8 @@ sys.path.insert(0, ROOT)
 
 from finite_elements_gb300 import mesh as fmesh          # noqa: E402
 from finite_elements_gb300 import meshgen                # noqa: E402
-from finite_elements_gb300.problem import ELASTIC, ELASTIC3D, ElementLoadSet, Problem  # noqa: E402
+from finite_elements_gb300.problem import (ELASTIC, ELASTIC3D, ElementLoadSet, MagnetLoadSet,  # noqa: E402
+                                          Problem)
 
 
 class _Anything:
@@ -59,7 +60,7 @@ def install_stubs():
     dc = _permissive_module("dessia_common")
     dcc = _permissive_module("dessia_common.core", DessiaObject=DessiaObject)
     dc.core = dcc
-    vm = _permissive_module("volmdlr", Point2D=fmesh.Point2D, Point3D=fmesh.Point3D)
+    vm = _permissive_module("volmdlr", Point2D=fmesh.Point2D, Point3D=fmesh.Point3D, Vector2D=fmesh.Vector2D)
     vmm = _permissive_module("volmdlr.mesh", Node2D=fmesh.Node2D, Node3D=fmesh.Node3D,
                              TriangularElement2D=fmesh.TriangularElement2D,
                              TetrahedralElement=fmesh.TetrahedralElement,
@@ -113,25 +114,33 @@ def reference_objects(fe, prob: Problem, groups):
     edge_bcs = [C.EdgeBoundaryCondition(fmesh.LineSegment2D(nodes[a], nodes[b]), float(v), int(d))
                 for (a, b), d, v in zip(prob.edge_bc_nodes.tolist(), prob.edge_bc_dim,
                                         prob.edge_bc_value)]
-    return mesh, elems, node_loads, element_loads, edge_loads, node_bcs, elem_bcs, edge_bcs
+    magnets = [fe.loads.MagnetLoad([elems[k] for k in m.elements.tolist()],
+                                   [nodes[k] for k in m.non_contour_nodes.tolist()],
+                                   fmesh.Vector2D(*m.magnetization)) for m in prob.magnet_loads]
+    conts = [C.ContinuityCondition(nodes[a], nodes[b], float(v)) for a, b, v in
+             zip(prob.cont_node1.tolist(), prob.cont_node2.tolist(), prob.cont_value.tolist())]
+    return mesh, elems, node_loads, element_loads, edge_loads, node_bcs, elem_bcs, edge_bcs, magnets, conts
 
 
 def run_reference(fe, prob: Problem, groups):
-    mesh, elems, nl, el, edl, nbc, ebc, edbc = reference_objects(fe, prob, groups)
+    mesh, elems, nl, el, edl, nbc, ebc, edbc, mag, cont = reference_objects(fe, prob, groups)
     kw = {}
     if prob.elastic:
         kw = dict(plane_strain=prob.plane_strain, plane_stress=prob.plane_stress)
     analysis = fe.analysis.FiniteElementAnalysis(
-        mesh=mesh, element_loads=el, edge_loads=edl, node_loads=nl, magnet_loads=[],
-        continuity_conditions=[], node_boundary_conditions=nbc,
+        mesh=mesh, element_loads=el, edge_loads=edl, node_loads=nl, magnet_loads=mag,
+        continuity_conditions=cont, node_boundary_conditions=nbc,
         edge_boundary_conditions=edbc, element_boundary_conditions=ebc, **kw)
     out = {}
     K = analysis.create_matrix()
     out["K_indptr"], out["K_indices"], out["K_data"] = K.indptr, K.indices, K.data
     out["K_shape"] = np.array(K.shape)
     out["F"] = analysis.create_source_matrix()[:, 0]
-    res = analysis.solve()
-    out["x"] = np.array(res.result_vector)
+    try:
+        res = analysis.solve()
+        out["x"] = np.array(res.result_vector)
+    except ValueError as exc:          # scipy's shape check of spsolve
+        out["solve_error"] = np.array(str(exc))
     ks = analysis.k_matrix_sparse()
     out["Ks_indptr"], out["Ks_indices"], out["Ks_data"] = ks.indptr, ks.indices, ks.data
     out["Ks_shape"] = np.array(ks.shape)
@@ -172,6 +181,13 @@ def problem_arrays(prob: Problem, groups):
         a[f"element_load_{k}_elements"] = s.elements
         a[f"element_load_{k}_value"] = np.array(s.value)
         a[f"element_load_{k}_dim"] = np.array(s.dimension)
+    a["n_magnet_loads"] = np.array(len(prob.magnet_loads))
+    for k, m in enumerate(prob.magnet_loads):
+        a[f"magnet_load_{k}_elements"] = m.elements
+        a[f"magnet_load_{k}_non_contour"] = m.non_contour_nodes
+        a[f"magnet_load_{k}_m"] = np.array(m.magnetization)
+    for name in ("cont_node1", "cont_node2", "cont_value"):
+        a[name] = getattr(prob, name)
     return a
 
 
@@ -324,6 +340,81 @@ def case_tet_quirks():
     return prob, [0, 30, ne]
 
 
+def _grid_boundary(nx, ny):
+    w = nx + 1
+    left = [j * w for j in range(ny + 1)]
+    right = [j * w + nx for j in range(ny + 1)]
+    bottom = list(range(w))
+    top = [ny * w + i for i in range(w)]
+    return left, right, bottom, top
+
+
+def case_mag_magnet():
+    """A magnetostatic 10x6 grid with two magnets (magnetisation (8e5, 2e5) on a block
+    of 12 triangles whose bottom edge from node 25 to node 26 is declared non-contour;
+    (-3e5, 6e5) on 4 triangles), an element current load and A = 0 on the outer
+    boundary."""
+    nx, ny = 10, 6
+    coords, conn = meshgen.rect_grid(nx, ny, 0.1, 0.06)
+    ne = conn.shape[0]
+    mu = np.where(np.arange(ne) % 5 == 0, 1000.0, 1.0) * meshgen.MU0
+    left, right, bottom, top = _grid_boundary(nx, ny)
+    boundary = sorted(set(left + right + bottom + top))
+    block = [2 * (j * nx + i) + t for j in (2, 3) for i in (3, 4, 5) for t in (0, 1)]
+    prob = Problem("magnetic", coords, conn, mu=mu,
+                   element_loads=[ElementLoadSet(np.array([50, 51, 70]), 2e3, 1)],
+                   node_bc_node=boundary, node_bc_dim=np.ones(len(boundary), np.int64),
+                   node_bc_value=np.zeros(len(boundary)),
+                   magnet_loads=[MagnetLoadSet(np.array(block), np.array([2 * 11 + 3, 2 * 11 + 4]), (8e5, 2e5)),
+                                 MagnetLoadSet(np.array([2 * (4 * nx + 6), 2 * (4 * nx + 6) + 1,
+                                                         2 * (2 * nx + 6), 2 * (2 * nx + 6) + 1]),
+                                               np.array([], np.int64), (-3e5, 6e5))])
+    return prob, [0, ne]
+
+
+def case_mag_periodic():
+    """A magnetostatic 8x5 grid with periodic (value 1) and anti-periodic (value -1)
+    conditions between the interior nodes of its left and right edges, A = 0 on the
+    bottom and top edges, a current load, and as many user NodeLoads as Dirichlet
+    conditions -- the one arrangement in which the reference's continuity rows
+    n + len(node_loads) + i land after the Dirichlet rows and spsolve accepts the
+    system (analysis.py:186-189, :276)."""
+    nx, ny = 8, 5
+    rng = np.random.default_rng(21)
+    coords, conn = meshgen.rect_grid(nx, ny, 0.08, 0.05, jitter=0.2, rng=rng)
+    ne = conn.shape[0]
+    left, right, bottom, top = _grid_boundary(nx, ny)
+    bc = bottom + top
+    inner_l, inner_r = left[1:-1], right[1:-1]
+    interior = [j * (nx + 1) + i for j in range(1, ny) for i in range(1, nx)]
+    nl_nodes = [interior[k % len(interior)] for k in range(len(bc))]
+    prob = Problem("magnetic", coords, conn, mu=np.full(ne, meshgen.MU0),
+                   element_loads=[ElementLoadSet(np.array([30, 31, 44, 45]), 5e2, 1)],
+                   node_load_node=nl_nodes, node_load_dim=np.ones(len(bc), np.int64),
+                   node_load_value=np.linspace(-1.0, 1.0, len(bc)),
+                   node_bc_node=bc, node_bc_dim=np.ones(len(bc), np.int64), node_bc_value=np.zeros(len(bc)),
+                   cont_node1=inner_l, cont_node2=inner_r,
+                   cont_value=[1.0 if k % 2 == 0 else -1.0 for k in range(len(inner_l))])
+    return prob, [0, ne]
+
+
+def case_elastic_cont_mismatch():
+    """Plane stress with one continuity condition and the usual few NodeLoads: the
+    reference's continuity row n + len(node_loads) lands inside the DOF rows, the
+    matrix and the right-hand side differ in size, and spsolve raises ValueError."""
+    nx, ny = 4, 2
+    coords, conn = meshgen.rect_grid(nx, ny, 2.0, 1.0)
+    ne = conn.shape[0]
+    left, right, _, _ = _grid_boundary(nx, ny)
+    prob = Problem(ELASTIC, coords, conn, E=200e9, nu=0.3, thickness=0.01, rho=7800.0,
+                   plane_stress=True, plane_strain=False,
+                   node_load_node=[right[1]], node_load_dim=[2], node_load_value=[-100.0],
+                   node_bc_node=np.repeat(left, 2), node_bc_dim=np.tile([1, 2], len(left)),
+                   node_bc_value=np.zeros(2 * len(left)),
+                   cont_node1=[right[0]], cont_node2=[right[2]], cont_value=[1.0])
+    return prob, [0, ne]
+
+
 def cases():
     yield "ex1_stress", case_ex1("stress")
     yield "ex1_strain", case_ex1("strain")
@@ -340,6 +431,9 @@ def cases():
     yield "tet_single", case_tet_single()
     yield "tet_cantilever", case_tet_cantilever()
     yield "tet_quirks", case_tet_quirks()
+    yield "mag_magnet", case_mag_magnet()
+    yield "mag_periodic", case_mag_periodic()
+    yield "elastic_cont_mismatch", case_elastic_cont_mismatch()
 
 
 def main():

@@ -130,7 +130,6 @@ def build_objects(name):
                        for s in prob.element_loads],
         edge_loads=[L.EdgeLoad(M.LineSegment2D(nodes[a], nodes[b]), v, d) for (a, b), d, v in
                     zip(prob.edge_load_nodes.tolist(), prob.edge_load_dim, prob.edge_load_value)],
-        magnet_loads=[], continuity_conditions=[],
         node_boundary_conditions=[C.NodeBoundaryCondition(nodes[n], v, d) for n, d, v in
                                   zip(prob.node_bc_node, prob.node_bc_dim, prob.node_bc_value)],
         element_boundary_conditions=[C.ElementBoundaryCondition(elems[k], v, d) for k, d, v in
@@ -139,6 +138,12 @@ def build_objects(name):
         edge_boundary_conditions=[C.EdgeBoundaryCondition(M.LineSegment2D(nodes[a], nodes[b]), v, d)
                                   for (a, b), d, v in zip(prob.edge_bc_nodes.tolist(), prob.edge_bc_dim,
                                                           prob.edge_bc_value)])
+    kw["magnet_loads"] = [L.MagnetLoad([elems[k] for k in m.elements.tolist()],
+                                       [nodes[k] for k in m.non_contour_nodes.tolist()],
+                                       M.Vector2D(*m.magnetization)) for m in prob.magnet_loads]
+    kw["continuity_conditions"] = [C.ContinuityCondition(nodes[a], nodes[b], v) for a, b, v in
+                                   zip(prob.cont_node1.tolist(), prob.cont_node2.tolist(),
+                                       prob.cont_value.tolist())]
     if prob.elastic:
         kw.update(plane_strain=prob.plane_strain, plane_stress=prob.plane_stress)
     return prob, ref, mesh, kw
@@ -161,13 +166,29 @@ def test_object_api_flattens_to_the_golden_problem(name):
         assert a.value == b.value and a.dimension == b.dimension
 
 
-def test_out_of_scope_inputs_raise():
-    from finite_elements_gb300 import conditions as C
+def test_magnet_and_continuity_flatten_to_the_golden_problem():
     from finite_elements_gb300.analysis import FiniteElementAnalysis
-    prob, ref, mesh, kw = build_objects("ex1_stress")
-    kw["continuity_conditions"] = [C.ContinuityCondition(mesh.nodes[0], mesh.nodes[1], 1)]
-    with pytest.raises(NotImplementedError):
-        FiniteElementAnalysis(mesh=mesh, **kw).problem()
+    for name in ("mag_magnet", "mag_periodic"):
+        prob, ref, mesh, kw = build_objects(name)
+        p = FiniteElementAnalysis(mesh=mesh, **kw).problem()
+        for f in ("cont_node1", "cont_node2", "cont_value"):
+            np.testing.assert_array_equal(getattr(p, f), getattr(prob, f))
+        assert len(p.magnet_loads) == len(prob.magnet_loads)
+        for a, b in zip(p.magnet_loads, prob.magnet_loads):
+            np.testing.assert_array_equal(a.elements, b.elements)
+            np.testing.assert_array_equal(a.non_contour_nodes, b.non_contour_nodes)
+            assert a.magnetization == b.magnetization
+
+
+def test_continuity_size_mismatch_raises_like_spsolve():
+    """Where the reference's continuity rows make create_matrix and
+    create_source_matrix disagree in size, solve() raises scipy's ValueError before
+    any device work."""
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    prob, ref, mesh, kw = build_objects("elastic_cont_mismatch")
+    with pytest.raises(ValueError) as e:
+        FiniteElementAnalysis(mesh=mesh, **kw).solve()
+    assert str(e.value) == str(ref["solve_error"])
 
 
 def test_plane_flag_errors_match_reference():

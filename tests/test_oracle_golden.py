@@ -22,8 +22,13 @@ def test_oracle_matches_reference(name):
     F = O.create_source_matrix(prob)[:, 0]
     assert F.shape == ref["F"].shape
     assert np.abs(F - ref["F"]).max() <= 1e-14 * max(np.abs(ref["F"]).max(), 1e-300)
-    x = np.array(O.solve(prob))
-    assert np.linalg.norm(x - ref["x"]) <= 1e-12 * np.linalg.norm(ref["x"])
+    if "x" in ref:
+        x = np.array(O.solve(prob))
+        assert np.linalg.norm(x - ref["x"]) <= 1e-12 * np.linalg.norm(ref["x"])
+    else:
+        with pytest.raises(ValueError) as e:
+            O.solve(prob)
+        assert str(e.value) == str(ref["solve_error"])
     ks = O.k_matrix_sparse(prob)
     np.testing.assert_array_equal(ks.indptr, ref["Ks_indptr"])
     np.testing.assert_array_equal(ks.indices, ref["Ks_indices"])
@@ -52,6 +57,20 @@ def test_factor_quirk_is_zero_area_area():
     np.testing.assert_allclose(ref["factors"][:, 1], area, rtol=1e-12)
     np.testing.assert_allclose(ref["factors"][:, 2], area, rtol=1e-12)
     assert np.abs(ref["factors"][:, 0]).max() <= 1e-12 * area.max()
+
+
+def test_magnet_source_matches_the_host_contour_code():
+    """The drop-in's vectorised contour extraction (loads.magnet_contributions) gives
+    the oracle's loop restatement of loads.py:129-147 entry for entry."""
+    from finite_elements_gb300.loads import magnet_contributions
+    prob, _, ref = gc.load("mag_magnet")
+    rows, vals = O.magnet_source(prob)
+    parts = [magnet_contributions(prob.coords, prob.conn, m.elements, m.non_contour_nodes, m.magnetization)
+             for m in prob.magnet_loads]
+    np.testing.assert_array_equal(np.concatenate([a for a, _ in parts]), rows)
+    np.testing.assert_array_equal(np.concatenate([v for _, v in parts]), vals)
+    # the non-contour edge 25-26 is skipped; the magnets add a net zero (closed contours)
+    assert not any({a, b} == {25, 26} for a, b in rows.reshape(-1, 2).tolist())
 
 
 def test_last_value_wins_dedup():
