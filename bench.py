@@ -9,6 +9,7 @@ C ABI from host buffers, with the uploads of the mesh, materials, loads and
 conditions and the download of [u, lambda] inside the timed region (``e2e``).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --workload tet      # secondary: 4M-DOF tetrahedral elasticity
 
 Prints one JSON line (rank 0).  With N > 1 (torchrun) every rank solves its own
 replica of the problem on its own GPU: the path has no data exchange between GPUs.
@@ -62,6 +63,12 @@ def parse_args():
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--cpu-nx", type=int, default=200, help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=("plane_strain", "tet"), default="plane_strain",
+                    help="tet: the secondary 3D line (solid cantilever of linear tetrahedra)")
+    ap.add_argument("--tet-dims", type=int, nargs=3, default=(320, 64, 64),
+                    help="cells of the tetrahedral cantilever (6 tetrahedra per cell)")
+    ap.add_argument("--tet-cheb", type=int, default=16, help="Chebyshev degree of the 3D mixed solve")
+    ap.add_argument("--tet-cheb-ratio", type=float, default=10000.0, help="its interval lmax/lmin")
     return ap.parse_args()
 
 
@@ -441,9 +448,57 @@ def run_ours(args, dist):
     return out
 
 
+def run_tet(args):
+    """Secondary measurement, not the headline: s/solve to args.tol of the solid
+    cantilever of linear tetrahedra (scripts/Elasticity/beam3d_example_2.py set-up),
+    plain FP64 PCG with the node-block Jacobi preconditioner against the FP64 CG with
+    the FP32 Chebyshev preconditioner.  Device time (CUDA events on the handle
+    stream) of the solve, inputs resident; the matrices are far larger than L2."""
+    import numpy as np
+
+    from finite_elements_gb300 import _lib, meshgen
+    from finite_elements_gb300.engine import GpuSystem
+
+    prob = meshgen.cantilever_3d(*args.tet_dims)
+    s = GpuSystem(prob)
+    runs = {"plain": dict(precision="fp64", cheb_degree=0),
+            "mixed": dict(precision="mixed-cg64", cheb_degree=args.tet_cheb, cheb_ratio=args.tet_cheb_ratio)}
+    res = {}
+    for name, kw in runs.items():
+        ms, xs = [], None
+        for k in range(args.warmup + args.steps):
+            x, st = s.solve(tol=args.tol, **kw)
+            if st.status != _lib.FE_OK:
+                raise RuntimeError(f"{name} solve failed: {st.as_dict()}")
+            if k >= args.warmup:
+                ms.append(st.solve_ms)
+            xs = x[: prob.n_dof]
+        res[name] = {"s": statistics.mean(ms) / 1e3, "iterations": st.iterations, "relres": st.relres,
+                     "assemble_ms": st.assemble_ms, "x": xs}
+    diff = float(np.linalg.norm(res["mixed"]["x"] - res["plain"]["x"]) / np.linalg.norm(res["plain"]["x"]))
+    out = {"metric": f"s/solve to {args.tol:g} rel. residual, 3D tetrahedral elasticity: mixed-cg64 vs plain PCG",
+           "value": res["mixed"]["s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": False, "dtype": "f64 recurrence, f32 preconditioner", "data": "synthetic",
+           "config": {"workload": f"solid cantilever {args.tet_dims[0]}x{args.tet_dims[1]}x{args.tet_dims[2]} cells "
+                                  f"x 6 tetrahedra ({prob.n_elements:,} elements, {prob.n_dof:,} DOF), "
+                                  "x = 0 clamped, tip edge loaded in z", "l2": "inputs larger than L2",
+                      "chebyshev": [args.tet_cheb, args.tet_cheb_ratio]},
+           "plain_s": res["plain"]["s"], "speedup_vs_plain": res["plain"]["s"] / res["mixed"]["s"],
+           "iterations": {k: v["iterations"] for k, v in res.items()},
+           "relres": {k: v["relres"] for k, v in res.items()},
+           "rel_diff_mixed_vs_plain": diff, "assemble_ms": res["plain"]["assemble_ms"]}
+    s.close()
+    return out
+
+
 def main():
     args = parse_args()
     dist = Dist()
+    if args.workload == "tet":
+        if dist.rank == 0:
+            print(json.dumps(run_tet(args)))
+        dist.close()
+        return
     if args.impl == "reference":
         if dist.rank == 0:
             model, ncpu = cpu_info()
