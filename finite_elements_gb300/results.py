@@ -117,6 +117,34 @@ class ElasticityResults2D(Result):
         n, d = len(self.mesh.nodes), self._ncomp
         return np.asarray(self.result_vector[: d * n], np.float64).reshape(n, d)
 
+    @property
+    def displacements_per_element(self):
+        """(E, npe*d) element DOF vectors, node-major (results.py:677-700), real part."""
+        coords, conn = mesh_arrays(self.mesh)
+        u = np.real(self.displacement_vectors_per_node)
+        return u[np.asarray(conn, np.int64)].reshape(conn.shape[0], -1)
+
+    def deformed_nodes_m(self, amplitude=1):
+        """(n, d) node coordinates moved by amplitude times the displacement
+        (results.py:587-616), in mesh.nodes order."""
+        coords, _ = mesh_arrays(self.mesh)
+        return coords[:, : self._ncomp] + amplitude * np.real(self.displacement_vectors_per_node)
+
+    @property
+    def deformed_nodes(self):
+        return self.deformed_nodes_m()
+
+    def deformed_mesh_m(self, amplitude=1):
+        """The mesh on the deformed nodes, as an ArrayMesh with the same connectivity
+        and node order (results.py:549-585)."""
+        from .mesh import ArrayMesh
+        _, conn = mesh_arrays(self.mesh)
+        return ArrayMesh(self.deformed_nodes_m(amplitude), conn)
+
+    @property
+    def deformed_mesh(self):
+        return self.deformed_mesh_m()
+
     def displacement_per_node_x(self):
         return self.displacement_vectors_per_node[:, 0]
 

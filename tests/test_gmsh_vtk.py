@@ -73,3 +73,23 @@ def test_vtk_file(tmp_path):
     i = lines.index("VECTORS Displacement_Vectors float")
     np.testing.assert_allclose([list(map(float, l.split())) for l in lines[i + 1:i + 1 + n]],
                                np.column_stack([u, np.zeros(n)]))
+
+
+def test_result_accessors_on_the_host():
+    """Deformed nodes and per-element displacement vectors need no device work."""
+    import numpy as np
+    from finite_elements_gb300 import meshgen
+    from finite_elements_gb300.mesh import ArrayMesh
+    from finite_elements_gb300.results import ElasticityResults2D, ElasticityResults3D
+    c, conn = meshgen.rect_grid(3, 2, 3.0, 2.0)
+    u = np.arange(2 * len(c), dtype=float) * 1e-3
+    r = ElasticityResults2D(ArrayMesh(c, conn), list(u) + [7.0], False, True)
+    np.testing.assert_array_equal(r.deformed_nodes_m(2.0), c + 2.0 * u.reshape(-1, 2))
+    np.testing.assert_array_equal(r.displacements_per_element[1], u.reshape(-1, 2)[conn[1]].reshape(-1))
+    assert r.deformed_mesh.conn.shape == conn.shape
+    c3, t3 = meshgen.box_tets(2, 1, 1, 2.0, 1.0, 1.0)
+    u3 = np.linspace(0, 1, 3 * len(c3))
+    r3 = ElasticityResults3D(ArrayMesh(c3, t3), list(u3), False, True)
+    assert r3.displacements_per_element.shape == (t3.shape[0], 12)
+    np.testing.assert_array_equal(r3.displacement_per_node_z(), u3[2::3])
+    np.testing.assert_array_equal(r3.deformed_nodes, c3 + u3.reshape(-1, 3))

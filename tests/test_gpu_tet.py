@@ -166,3 +166,28 @@ def test_larger_cantilever_precisions_agree(gpu_lib):
         r = (F - K @ x[:n])[free]
         assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(F[free])
     s.close()
+
+
+def test_largest_modes_and_drop_in_modal_analysis(gpu_lib):
+    """'largest' on the tetrahedral beam, and modal_analysis through the drop-in
+    objects (scripts/ModalAnalysis/beam3d_1.py: order='smallest')."""
+    from finite_elements_gb300 import elements as El, mesh as M
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    from finite_elements_gb300.engine import GpuSystem
+    from oracle import fe_oracle as O
+    prob = free_beam_3d(6, 2, 2)
+    s = GpuSystem(prob)
+    vals, _, res = s.modal(4, which="largest", steps=prob.n_dof)
+    exact, _ = O.generalized_eigenpairs(prob, 4, which="largest")
+    np.testing.assert_allclose(vals, exact, rtol=1e-8)
+    assert res.max() <= 1e-9
+    s.close()
+    nodes = [M.Node3D(*c) for c in prob.coords.tolist()]
+    elems = [El.ElasticityTetrahedralElement3D(M.TetrahedralElement([nodes[i] for i in row]), 210e9, 0.25, 7860.0)
+             for row in prob.conn.tolist()]
+    mesh = M.Mesh([M.ElementsGroup(elems)])
+    fea = FiniteElementAnalysis(mesh, [], [], [], [], [], [], [], [], plane_strain=False, plane_stress=True)
+    vals, vecs = fea.modal_analysis(order="smallest", k=10)
+    exact, _ = O.generalized_eigenpairs(prob, 10)
+    assert vecs.shape == (10, prob.n_dof)
+    np.testing.assert_allclose(vals[6:], exact[6:], rtol=1e-8)
