@@ -39,6 +39,16 @@ class SolverConvergenceError(RuntimeError):
     """PCG stopped at its iteration cap above the requested tolerance."""
 
 
+class FeSolveError(RuntimeError):
+    """Strict mode (``solver={"strict": True}``): a singular or non-finite system raises
+    this instead of returning the NaN vector spsolve would return."""
+
+    def __init__(self, status, stats):
+        RuntimeError.__init__(self, f"solve failed with status {status}: {stats}")
+        self.status = status
+        self.stats = stats
+
+
 def _element_kind(element):
     if hasattr(element, "mu_total"):
         return MAGNETIC
@@ -50,7 +60,9 @@ def _element_kind(element):
 
 class FiniteElementAnalysis:
     """See the module docstring.  ``solver`` (optional) overrides the solve options
-    (``precision`` "fp64" / "mixed", ``tol``, ``cheb_degree``, ``max_iter``, ``x0`` ...)."""
+    (``precision`` "fp64" / "mixed" / "mixed-cg64", ``tol``, ``cheb_degree``,
+    ``max_iter``, ``x0`` ...; ``strict`` raises FeSolveError on a singular or
+    non-finite system instead of returning NaN)."""
 
     def __init__(self, mesh, element_loads, edge_loads, node_loads, magnet_loads,
                  continuity_conditions, node_boundary_conditions, edge_boundary_conditions,
@@ -264,9 +276,12 @@ class FiniteElementAnalysis:
         sysm = self.system()
         self._boundary_conditions = list(zip(sysm.bc_dof.tolist(), sysm.bc_value.tolist()))
         opts = dict(self.solver)
+        strict = opts.pop("strict", False)
         x, st = sysm.solve(**opts)
         self.last_stats = st.as_dict()
         from . import _lib
+        if strict and st.status in (_lib.FE_BREAKDOWN, _lib.FE_NONFINITE):
+            raise FeSolveError(_lib.STATUS_NAMES.get(st.status, st.status), self.last_stats)
         if st.status in (_lib.FE_BREAKDOWN, _lib.FE_NONFINITE):
             # scipy's spsolve warns and returns NaN for an exactly singular matrix; the
             # reference turns the warning into NotImplementedError when it is raised

@@ -110,3 +110,21 @@ def test_node_without_elements_gives_nan_like_spsolve(gpu_lib):
         res = fea.solve()
     assert np.isnan(np.array(res.result_vector)).all()
     assert any(issubclass(x.category, spla.MatrixRankWarning) for x in w)
+
+
+def test_strict_mode_raises_on_a_singular_system(gpu_lib):
+    """solver={"strict": True}: the singular system of the test above raises
+    FeSolveError with the BREAKDOWN status instead of returning NaN."""
+    from finite_elements_gb300.analysis import FeSolveError, FiniteElementAnalysis
+    from finite_elements_gb300.problem import Problem
+    prob, _, _ = gc.load("ex2_strain")
+    coords = np.vstack([prob.coords, [[50.0, 50.0]]])
+    p2 = Problem("elastic", coords, prob.conn, E=prob.E, nu=prob.nu, thickness=prob.thickness,
+                 rho=prob.rho, plane_strain=True, plane_stress=False,
+                 node_load_node=prob.node_load_node, node_load_dim=prob.node_load_dim,
+                 node_load_value=prob.node_load_value, node_bc_node=prob.node_bc_node,
+                 node_bc_dim=prob.node_bc_dim, node_bc_value=prob.node_bc_value)
+    fea = FiniteElementAnalysis.from_problem(p2, solver={"strict": True})
+    with pytest.raises(FeSolveError) as e:
+        fea.solve()
+    assert "FE_BREAKDOWN" in str(e.value)
