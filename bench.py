@@ -48,7 +48,7 @@ def parse_args():
     ap.add_argument("--ny", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--cheb", type=int, default=64, help="Chebyshev degree of the mixed solve's preconditioner")
+    ap.add_argument("--cheb", type=int, default=96, help="Chebyshev degree of the mixed solve's preconditioner")
     ap.add_argument("--cheb-ratio", type=float, default=100000.0, help="Chebyshev interval lmax/lmin (mixed)")
     ap.add_argument("--plain-cheb", type=int, default=32, help="Chebyshev degree of the plain FP64 PCG")
     ap.add_argument("--plain-cheb-ratio", type=float, default=30000.0, help="Chebyshev interval (plain FP64)")
@@ -67,7 +67,7 @@ def parse_args():
                     help="tet: the secondary 3D line (solid cantilever of linear tetrahedra)")
     ap.add_argument("--tet-dims", type=int, nargs=3, default=(320, 64, 64),
                     help="cells of the tetrahedral cantilever (6 tetrahedra per cell)")
-    ap.add_argument("--tet-cheb", type=int, default=16, help="Chebyshev degree of the 3D mixed solve")
+    ap.add_argument("--tet-cheb", type=int, default=24, help="Chebyshev degree of the 3D mixed solve")
     ap.add_argument("--tet-cheb-ratio", type=float, default=10000.0, help="its interval lmax/lmin")
     return ap.parse_args()
 

@@ -843,12 +843,12 @@ struct Sys {
 struct Cheb {
     int k = 1;                 // Chebyshev terms (1 = plain node-block Jacobi)
     double theta = 1, delta = 1;
-    double c1[64], c2[64];     // coefficients of steps 1..k-1
+    double c1[128], c2[128];   // coefficients of steps 1..k-1
 };
 
 Cheb make_cheb(int degree, double lmax, double ratio) {
     Cheb c;
-    c.k = std::max(1, std::min(degree, 64));
+    c.k = std::max(1, std::min(degree, 128));
     if (c.k <= 1 || !(lmax > 0)) {
         c.k = 1;
         return c;

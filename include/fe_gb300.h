@@ -79,7 +79,7 @@ typedef struct fe_handle_s *fe_handle;
 
 typedef struct fe_solve_opts {
     int32_t precision;     /* FE_PREC_FP64, FE_PREC_MIXED or FE_PREC_MIXED_CG64          */
-    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it (k <= 64) */
+    int32_t cheb_degree;   /* <= 1: node-block Jacobi; k >= 2: k-step Chebyshev on it (k <= 128) */
     int32_t max_iter;      /* cap on PCG iterations, all refinement steps together       */
     int32_t max_outer;     /* cap on refinement steps (mixed) or restarts (FP64)          */
     double  tol;           /* target ||b - A x||_2 / ||b||_2, FP64 true residual          */
