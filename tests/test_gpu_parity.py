@@ -115,7 +115,7 @@ def test_solve_mixed_matches_spsolve(systems, name, cheb):
 
 
 @pytest.mark.parametrize("name", gc.solvable_names())
-@pytest.mark.parametrize("cheb", [0, 4, 24, 64])
+@pytest.mark.parametrize("cheb", [0, 4, 24, 64, 128])
 def test_solve_mixed_cg64_matches_spsolve(systems, name, cheb):
     """FP64 CG recurrence with the FP32 preconditioner: FP64 accuracy."""
     s, prob, ref = systems[name]
