@@ -415,7 +415,42 @@ def case_elastic_cont_mismatch():
     return prob, [0, ne]
 
 
-def cases():
+def case_beam3d_msh(ref_root):
+    """scripts/Elasticity/beam3d_example_2.py on the reference's own mesh file
+    scripts/InputFiles/3D/beam3d_1.msh (Gmsh order kept): E=30e6, nu=0.25, rho=2.7,
+    plane stress, -1000 in dimension 3 at the nodes with x = 10 and z = 2, the nodes
+    with x = 0 clamped in dimensions 1, 2, 3."""
+    from finite_elements_gb300 import gmsh
+    m = gmsh.read_msh(os.path.join(ref_root, "scripts", "InputFiles", "3D", "beam3d_1.msh"))
+    c, tets = m.coords, m.tetrahedra
+    ne = tets.shape[0]
+    tip = np.flatnonzero((c[:, 0] == 10) & (c[:, 2] == 2))
+    x0 = np.flatnonzero(c[:, 0] == 0)
+    prob = Problem(ELASTIC3D, c, tets, E=30e6, nu=0.25, rho=2.7, plane_strain=False, plane_stress=True,
+                   node_load_node=tip, node_load_dim=np.full(tip.size, 3), node_load_value=np.full(tip.size, -1000.0),
+                   node_bc_node=np.repeat(x0, 3), node_bc_dim=np.tile([1, 2, 3], x0.size),
+                   node_bc_value=np.zeros(3 * x0.size))
+    return prob, [int(v) for v in m.tet_group_ptr]
+
+
+def case_beam2d_msh(ref_root):
+    """scripts/Elasticity/beam2d_example_3.py on the reference's own mesh file
+    scripts/InputFiles/2D/beam_2d_0.5.msh (Gmsh order kept): E=30e6, nu=0.25, t=1,
+    rho=2.7, plane stress, -1000 in dimension 2 at node (10, 1), the nodes with x = 0
+    clamped."""
+    from finite_elements_gb300 import gmsh
+    m = gmsh.read_msh(os.path.join(ref_root, "scripts", "InputFiles", "2D", "beam_2d_0.5.msh"))
+    c = m.coords[:, :2]
+    tip = np.flatnonzero((c[:, 0] == 10) & (c[:, 1] == 1))
+    x0 = np.flatnonzero(c[:, 0] == 0)
+    prob = Problem(ELASTIC, c, m.triangles, E=30e6, nu=0.25, thickness=1.0, rho=2.7, plane_strain=False,
+                   plane_stress=True, node_load_node=tip, node_load_dim=[2], node_load_value=[-1000.0],
+                   node_bc_node=np.repeat(x0, 2), node_bc_dim=np.tile([1, 2], x0.size),
+                   node_bc_value=np.zeros(2 * x0.size))
+    return prob, [int(v) for v in m.group_ptr]
+
+
+def cases(ref_root):
     yield "ex1_stress", case_ex1("stress")
     yield "ex1_strain", case_ex1("strain")
     yield "ex2_strain", case_ex2()
@@ -434,6 +469,8 @@ def cases():
     yield "mag_magnet", case_mag_magnet()
     yield "mag_periodic", case_mag_periodic()
     yield "elastic_cont_mismatch", case_elastic_cont_mismatch()
+    yield "beam3d_msh", case_beam3d_msh(ref_root)
+    yield "beam2d_msh", case_beam2d_msh(ref_root)
 
 
 def main():
@@ -446,7 +483,7 @@ def main():
     import finite_elements.loads         # noqa: F401
     fe = sys.modules["finite_elements"]
     only = set(sys.argv[2:])
-    for name, (prob, groups) in cases():
+    for name, (prob, groups) in cases(ref):
         if only and name not in only:
             continue
         out = run_reference(fe, prob, groups)
