@@ -73,6 +73,21 @@ class Vector2D(Point2D):
     def Dot(self, other):
         return self.x * other[0] + self.y * other[1]
 
+    def dot(self, other):
+        return self.x * other[0] + self.y * other[1]
+
+    def Norm(self):
+        return math.sqrt(self.x ** 2 + self.y ** 2)
+
+    def norm(self):
+        return math.sqrt(self.x ** 2 + self.y ** 2)
+
+    def normalize(self):
+        """In place, as volmdlr's Vector2D.normalize."""
+        n = self.norm()
+        self.x /= n
+        self.y /= n
+
     def __truediv__(self, k):
         return Vector2D(self.x / k, self.y / k)
 
@@ -185,7 +200,7 @@ class TriangularElement2D:
     @property
     def center(self):
         xy = self._xy()
-        return Point2D(sum(p[0] for p in xy) / 3.0, sum(p[1] for p in xy) / 3.0)
+        return Vector2D(sum(p[0] for p in xy) / 3.0, sum(p[1] for p in xy) / 3.0)
 
     @property
     def linear_elements(self):

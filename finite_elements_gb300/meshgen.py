@@ -272,3 +272,24 @@ def cantilever_3d(nx, ny, nz, length=10.0, width=2.0, height=2.0, E=210e9, nu=0.
                    node_load_value=np.full(tip.size, load),
                    node_bc_node=np.repeat(clamped, 3), node_bc_dim=np.tile([1, 2, 3], clamped.size),
                    node_bc_value=np.zeros(3 * clamped.size))
+
+
+# ---------------------------------------------------------------- 2D: a motor-like annulus
+
+def annulus(radii, nt):
+    """Polar grid on the radii r_0 < r_1 < ... < r_m and nt sectors (periodic in the
+    angle): node (i, j) at radius r_i and angle 2 pi j / nt has id i * nt + j; each cell
+    is split into the two triangles (i,j)(i,j+1)(i+1,j) and (i+1,j+1)(i+1,j)(i,j+1).
+    Returns (coords (n,2), conn (2 m nt, 3)); the triangles of radial layer i are
+    conn[2 nt i : 2 nt (i+1)]."""
+    radii = np.asarray(radii, np.float64)
+    m = radii.size - 1
+    th = 2 * math.pi * np.arange(nt) / nt
+    R, T = np.meshgrid(radii, th, indexing="ij")
+    coords = np.stack([(R * np.cos(T)).reshape(-1), (R * np.sin(T)).reshape(-1)], axis=1)
+    i, j = np.meshgrid(np.arange(m), np.arange(nt), indexing="ij")
+    i, j = i.reshape(-1), j.reshape(-1)
+    jn = (j + 1) % nt
+    a, b, c, d = i * nt + j, i * nt + jn, (i + 1) * nt + j, (i + 1) * nt + jn
+    conn = np.stack([np.stack([a, b, c], 1), np.stack([d, c, b], 1)], 1).reshape(-1, 3).astype(np.int32)
+    return coords, conn

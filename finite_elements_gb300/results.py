@@ -2,7 +2,11 @@
 per-element results of elasticity and magnetostatic solutions."""
 from __future__ import annotations
 
+import math
+
 import numpy as np
+
+MU = 4 * math.pi * 1e-7   # finite_elements/core.py:31
 
 
 class Result:
@@ -239,3 +243,57 @@ class MagneticResults(Result):
     @property
     def magnetic_field_norm(self):
         return np.hypot(self.magnetic_field_per_element[:, 0], self.magnetic_field_per_element[:, 1])
+
+    # ---- air-gap quantities (results.py:82-243), host arithmetic on the device's B field
+
+    def _elements(self):
+        return [el for g in self.mesh.elements_groups for el in g.elements]
+
+    def _group_range(self, group):
+        """Element range of a group of the mesh: the group object itself, or its name."""
+        start = 0
+        for g in self.mesh.elements_groups:
+            n = len(g.elements)
+            if g is group or (isinstance(group, str) and getattr(g, "name", None) == group):
+                return range(start, start + n)
+            start += n
+        raise ValueError(f"no elements group {getattr(group, 'name', group)!r} in the mesh")
+
+    def _polar(self, idx):
+        """Element centres (x1 + x2 + x3) / 3, their norm, and (B . e_r, B . e_theta)
+        with e_r the unit centre direction and e_theta = (-e_r[1], e_r[0])."""
+        coords, conn = mesh_arrays(self.mesh)
+        p = coords[np.asarray(conn, np.int64)[idx]]
+        cx = (p[:, 0, 0] + p[:, 1, 0] + p[:, 2, 0]) / 3.0
+        cy = (p[:, 0, 1] + p[:, 1, 1] + p[:, 2, 1]) / 3.0
+        r = np.sqrt(cx ** 2 + cy ** 2)
+        ex, ey = cx / r, cy / r
+        b = self.magnetic_field_per_element[idx]
+        br = b[:, 0] * ex + b[:, 1] * ey
+        bt = b[:, 0] * -ey + b[:, 1] * ex
+        return r, br, bt, b, p
+
+    def brbtetha(self, gap_elements_group):
+        """B_r * B_theta of every element of the group (results.py:82-106)."""
+        _, br, bt, _, _ = self._polar(np.array(list(self._group_range(gap_elements_group)), np.int64))
+        return list(br * bt)
+
+    def maxwell_stress_tensor(self, element):
+        """[sigma_rr, sigma_r_theta, sigma_theta_theta] of one element (results.py:154-181)."""
+        k = next(i for i, el in enumerate(self._elements()) if el is element)
+        _, br, bt, b, _ = self._polar(np.array([k]))
+        nb2 = np.sqrt(b[0, 0] ** 2 + b[0, 1] ** 2) ** 2
+        return [1 / MU * br[0] ** 2 - 1 / (2 * MU) * nb2, 1 / MU * br[0] * bt[0],
+                1 / MU * bt[0] ** 2 - 1 / (2 * MU) * nb2]
+
+    def torque(self, air_gap_elements_group_name, length_motor, radius_stator, radius_rotor):
+        """Arkkio's torque (results.py:183-243): length / (mu0 (r_s - r_r)) times the sum
+        over the air-gap elements of |centre| B_r B_theta area, summed in element order."""
+        idx = np.array(list(self._group_range(air_gap_elements_group_name)), np.int64)
+        r, br, bt, _, p = self._polar(idx)
+        area = np.abs((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1])
+                      - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])) / 2.0
+        somme = 0
+        for term in (r * br * bt * area).tolist():
+            somme += term
+        return length_motor / (MU * (radius_stator - radius_rotor)) * somme

@@ -77,7 +77,7 @@ def install_stubs():
                         "volmdlr.mesh": vmm, "matplotlib": mpl, "pkg_resources": pkr})
 
 
-def reference_objects(fe, prob: Problem, groups):
+def reference_objects(fe, prob: Problem, groups, names=None):
     """Build the reference's object graph for ``prob``: nodes, elements (wrapped as
     the reference's element classes), groups, mesh, loads and conditions."""
     if prob.kind == ELASTIC3D:
@@ -94,7 +94,7 @@ def reference_objects(fe, prob: Problem, groups):
                 for k, t in enumerate(tris)]
         else:
             elems = [fe.elements.MagneticElement2D(t, float(prob.mu[k])) for k, t in enumerate(tris)]
-    egroups = [fmesh.ElementsGroup(elems[a:b], f"g{g}") for g, (a, b) in
+    egroups = [fmesh.ElementsGroup(elems[a:b], names[g] if names else f"g{g}") for g, (a, b) in
                enumerate(zip(groups[:-1], groups[1:]))]
     mesh = fmesh.Mesh(egroups)
     mesh.nodes = nodes
@@ -122,8 +122,8 @@ def reference_objects(fe, prob: Problem, groups):
     return mesh, elems, node_loads, element_loads, edge_loads, node_bcs, elem_bcs, edge_bcs, magnets, conts
 
 
-def run_reference(fe, prob: Problem, groups):
-    mesh, elems, nl, el, edl, nbc, ebc, edbc, mag, cont = reference_objects(fe, prob, groups)
+def run_reference(fe, prob: Problem, groups, names=None, motor=None):
+    mesh, elems, nl, el, edl, nbc, ebc, edbc, mag, cont = reference_objects(fe, prob, groups, names)
     kw = {}
     if prob.elastic:
         kw = dict(plane_strain=prob.plane_strain, plane_stress=prob.plane_stress)
@@ -155,6 +155,13 @@ def run_reference(fe, prob: Problem, groups):
         out["Ke"] = np.array([e.elementary_matrix() for e in elems])
     if prob.kind != ELASTIC3D:
         out["factors"] = np.array([e.element_to_node_factors() for e in elems])
+    if motor is not None:
+        # the reference's air-gap post-processing on its own solution (results.py:82-243)
+        mr = fe.results.MagneticResults(mesh, list(out["x"]))
+        gap = next(g for g in mesh.elements_groups if g.name == motor["gap"])
+        out["brbtetha"] = np.array(mr.brbtetha(gap))
+        out["torque"] = np.array(mr.torque(motor["gap"], motor["length"], motor["r_stator"], motor["r_rotor"]))
+        out["maxwell"] = np.array([mr.maxwell_stress_tensor(gap.elements[k]) for k in motor["maxwell_elements"]])
     bcs = analysis._boundary_conditions
     out["bc_dof"] = np.array([analysis.positions[(mesh.node_to_index[b.application],
                                                   b.dimension)] for b in bcs], np.int64)
@@ -450,6 +457,33 @@ def case_beam2d_msh(ref_root):
     return prob, [int(v) for v in m.group_ptr]
 
 
+def case_motor():
+    """A motor-like annulus (scripts/Magnetic, the air-gap post-processing of
+    results.py:82-243): an iron rotor ring with two magnets, the air gap in two radial
+    layers, an iron stator ring carrying two opposite phase currents; A = 0 on the
+    outer radius.  Groups "Rotor", "Gap ring", "Stator"."""
+    nt = 48
+    radii = [0.02, 0.028, 0.036, 0.0395, 0.04, 0.0405, 0.044, 0.052, 0.06]
+    coords, conn = meshgen.annulus(radii, nt)
+    ne = conn.shape[0]
+    layer = np.repeat(np.arange(len(radii) - 1), 2 * nt)
+    mu = np.where((layer <= 2) | (layer >= 5), 1000.0, 1.0) * meshgen.MU0
+    rotor_mag = np.flatnonzero((layer == 2) & (np.arange(ne) % (2 * nt) < 12))
+    rotor_mag2 = np.flatnonzero((layer == 2) & (np.arange(ne) % (2 * nt) >= 48) & (np.arange(ne) % (2 * nt) < 60))
+    phase_a = np.flatnonzero((layer == 5) & (np.arange(ne) % (2 * nt) >= 6) & (np.arange(ne) % (2 * nt) < 18))
+    phase_b = np.flatnonzero((layer == 5) & (np.arange(ne) % (2 * nt) >= 54) & (np.arange(ne) % (2 * nt) < 66))
+    outer = np.arange((len(radii) - 1) * nt, len(radii) * nt)
+    prob = Problem("magnetic", coords, conn, mu=mu,
+                   element_loads=[ElementLoadSet(phase_a, 40.0, 1), ElementLoadSet(phase_b, -40.0, 1)],
+                   magnet_loads=[MagnetLoadSet(rotor_mag, np.zeros(0, np.int64), (8e5, 3e5)),
+                                 MagnetLoadSet(rotor_mag2, np.zeros(0, np.int64), (-8e5, -3e5))],
+                   node_bc_node=outer, node_bc_dim=np.ones(nt, np.int64), node_bc_value=np.zeros(nt))
+    groups = [0, 6 * nt, 10 * nt, ne]       # rotor: layers 0-2, gap: layers 3-4, stator: 5-7
+    motor = {"gap": "Gap ring", "length": 0.1, "r_stator": 0.0405, "r_rotor": 0.0395,
+             "maxwell_elements": [0, 17, 95, 150]}
+    return prob, groups, ["Rotor", "Gap ring", "Stator"], motor
+
+
 def cases(ref_root):
     yield "ex1_stress", case_ex1("stress")
     yield "ex1_strain", case_ex1("strain")
@@ -471,6 +505,7 @@ def cases(ref_root):
     yield "elastic_cont_mismatch", case_elastic_cont_mismatch()
     yield "beam3d_msh", case_beam3d_msh(ref_root)
     yield "beam2d_msh", case_beam2d_msh(ref_root)
+    yield "motor", case_motor()
 
 
 def main():
@@ -481,13 +516,22 @@ def main():
     import finite_elements.conditions    # noqa: F401
     import finite_elements.elements      # noqa: F401
     import finite_elements.loads         # noqa: F401
+    import finite_elements.results       # noqa: F401
     fe = sys.modules["finite_elements"]
     only = set(sys.argv[2:])
-    for name, (prob, groups) in cases(ref):
+    for name, case in cases(ref):
         if only and name not in only:
             continue
-        out = run_reference(fe, prob, groups)
+        prob, groups = case[0], case[1]
+        names = case[2] if len(case) > 2 else None
+        motor = case[3] if len(case) > 3 else None
+        out = run_reference(fe, prob, groups, names, motor)
         arrays = problem_arrays(prob, groups)
+        if names:
+            arrays["group_names"] = np.array(names)
+        if motor:
+            arrays["motor"] = np.array([motor["length"], motor["r_stator"], motor["r_rotor"]])
+            arrays["motor_maxwell_elements"] = np.array(motor["maxwell_elements"], np.int64)
         arrays.update({"ref_" + k: v for k, v in out.items()})
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
         print(f"{name}: n_dof={prob.n_dof} nnz={out['K_data'].size} "

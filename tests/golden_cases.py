@@ -54,4 +54,9 @@ def load(name):
                                         "element_bc_value", "edge_bc_nodes", "edge_bc_dim",
                                         "edge_bc_value")})
     ref = {k[4:]: z[k] for k in z.files if k.startswith("ref_")}
+    if "group_names" in z.files:
+        ref["_group_names"] = z["group_names"]
+    if "motor" in z.files:
+        ref["_motor"] = z["motor"]
+        ref["_motor_maxwell_elements"] = z["motor_maxwell_elements"]
     return prob, z["groups"], ref

@@ -120,7 +120,9 @@ def build_objects(name):
                      for k, t in enumerate(tris)]
         else:
             elems = [El.MagneticElement2D(t, prob.mu[k]) for k, t in enumerate(tris)]
-    mesh = M.Mesh([M.ElementsGroup(elems[a:b]) for a, b in zip(groups[:-1], groups[1:])])
+    names = ref.get("_group_names")
+    mesh = M.Mesh([M.ElementsGroup(elems[a:b], str(names[g]) if names is not None else "")
+                   for g, (a, b) in enumerate(zip(groups[:-1], groups[1:]))])
     mesh.nodes = nodes
     mesh.node_to_index = {p: i for i, p in enumerate(nodes)}
     kw = dict(

@@ -73,3 +73,30 @@ def test_results_classes(gpu_lib):
     res = FiniteElementAnalysis(mesh=mesh, **kw).solve()
     mr = MagneticResults(res.mesh, res.result_vector)
     assert relmax(mr.magnetic_field_per_element, O.magnetic_field(prob, ref["x"])) <= 1e-9
+
+
+def test_air_gap_post_processing_matches_the_reference(gpu_lib):
+    """MagneticResults.brbtetha / maxwell_stress_tensor / torque (results.py:82-243) on
+    the GPU solution and the GPU B field of the motor-like annulus, against the values
+    the reference computed on its own solution.  Tolerance: 1e-9 relative to the sum of
+    the magnitudes of the terms (each quantity is a short sum of products of B)."""
+    from test_abi_host import build_objects
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    from finite_elements_gb300.results import MagneticResults
+    prob, ref, mesh, kw = build_objects("motor")
+    length, r_s, r_r = ref["_motor"].tolist()
+    res = FiniteElementAnalysis(mesh=mesh, **kw).solve()
+    mr = MagneticResults(res.mesh, res.result_vector)
+    gap = next(g for g in mesh.elements_groups if g.name == "Gap ring")
+    brbt = np.array(mr.brbtetha(gap))
+    assert np.abs(brbt - ref["brbtetha"]).max() <= 1e-9 * np.abs(ref["brbtetha"]).max()
+    t = mr.torque("Gap ring", length, r_s, r_r)
+    idx = np.array(list(mr._group_range("Gap ring")))
+    r, br, bt, _, p = mr._polar(idx)
+    area = np.abs((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1])
+                  - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])) / 2.0
+    scale = length / (4e-7 * np.pi * (r_s - r_r)) * np.abs(r * br * bt * area).sum()
+    assert abs(t - float(ref["torque"])) <= 1e-9 * scale
+    for k, row in zip(ref["_motor_maxwell_elements"].tolist(), ref["maxwell"]):
+        got = np.array(mr.maxwell_stress_tensor(gap.elements[k]))
+        assert np.abs(got - row).max() <= 1e-9 * np.abs(row).max()

@@ -90,3 +90,20 @@ def test_golden_cover_the_quirks():
     # element loads overwrite the user load on node 27 dim 2, edge loads overwrite both
     lk, lv = O.node_load_list(prob)
     assert (lk == 27 * 2 + 1).sum() >= 2
+
+
+def test_air_gap_post_processing_on_the_reference_field():
+    """The drop-in's host arithmetic of brbtetha / maxwell_stress_tensor / torque
+    (results.py:82-243), fed the oracle's B field of the reference's solution, gives
+    the reference's values to rounding."""
+    from test_abi_host import build_objects
+    from finite_elements_gb300.results import MagneticResults
+    prob, ref, mesh, kw = build_objects("motor")
+    length, r_s, r_r = ref["_motor"].tolist()
+    mr = MagneticResults(mesh, list(ref["x"]))
+    mr._field = O.magnetic_field(prob, ref["x"])
+    gap = next(g for g in mesh.elements_groups if g.name == "Gap ring")
+    np.testing.assert_allclose(mr.brbtetha(gap), ref["brbtetha"], rtol=1e-12, atol=1e-13)
+    assert abs(mr.torque("Gap ring", length, r_s, r_r) - float(ref["torque"])) <= 1e-11 * abs(float(ref["torque"]))
+    for k, row in zip(ref["_motor_maxwell_elements"].tolist(), ref["maxwell"]):
+        np.testing.assert_allclose(mr.maxwell_stress_tensor(gap.elements[k]), row, rtol=1e-12, atol=1e-6)
