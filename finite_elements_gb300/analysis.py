@@ -25,6 +25,7 @@ from __future__ import annotations
 import warnings
 
 import numpy as np
+import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 from .engine import GpuSystem, check_plane_flags, dirichlet_count
@@ -249,8 +250,175 @@ class FiniteElementAnalysis:
             f'Class {self.__class__.__name__} does not implement {method_name} m matrix')
 
     def element_matrices(self, which="K"):
-        """(E, (3*dim)^2) row-major element matrices from the GPU element kernels."""
+        """(E, (npe*dim)^2) row-major element matrices from the GPU element kernels."""
         return self.system().element_matrices(which)
+
+    # ------------------------------------------------------------ intermediate lists
+    # The reference's building blocks (analysis.py:175-577), for callers that use them.
+    # Triplet lists are numpy arrays here: at the sizes this path serves, Python lists
+    # of the element matrices would not fit in host memory.
+
+    def _element_dofs(self):
+        prob = self.problem()
+        d = prob.dim
+        return (prob.conn.astype(np.int64)[:, :, None] * d + np.arange(d)[None, None, :]).reshape(
+            prob.n_elements, -1)
+
+    def get_row_col_indices(self, element):
+        """row = each local DOF repeated len(L) times, col = L tiled (analysis.py:714-735)."""
+        index = self.mesh.node_to_index
+        d = element.dimension
+        L = [index[p] * d + i for p in element.points for i in range(d)]
+        return [r for r in L for _ in L], L * len(L)
+
+    def _triplets(self, which):
+        ke = self.element_matrices(which).reshape(-1)
+        L = self._element_dofs()
+        n = L.shape[1]
+        return ke, np.repeat(L, n, axis=1).reshape(-1), np.tile(L, (1, n)).reshape(-1)
+
+    def k_matrix_data(self):
+        """(data, row, col) of every element matrix in group and element order
+        (analysis.py:324-339), the values from the GPU element kernels."""
+        return self._triplets("K")
+
+    def m_matrix_data(self):
+        """As k_matrix_data for the mass matrices (analysis.py:356-369)."""
+        if not self.problem().elastic:
+            raise AttributeError("'MagneticElement2D' object has no attribute 'elementary_mass_matrix'")
+        return self._triplets("M")
+
+    def matrix_dense(self, method_name):
+        """Dense (n*dim)^2 sum of the triplets of ``method_name`` (analysis.py:373-390)."""
+        if not hasattr(self, method_name):
+            raise NotImplementedError(f'Class {self.__class__.__name__} does not implement {method_name}')
+        data, row, col = getattr(self, method_name)()
+        n = self.problem().n_dof
+        m = np.zeros((n, n))
+        np.add.at(m, (np.asarray(row), np.asarray(col)), np.asarray(data))
+        return m
+
+    def matrix_sparse(self, method_name):
+        """csc_matrix of the merged triplets of ``method_name`` (analysis.py:387-405); K
+        and M come from the device's merge (fe_export_csr)."""
+        if method_name == 'k_matrix_data':
+            return self.k_matrix_sparse()
+        if method_name == 'm_matrix_data':
+            return self.m_matrix_sparse()
+        if not hasattr(self, method_name):
+            raise NotImplementedError(f'Class {self.__class__.__name__} does not implement {method_name}')
+        data, row, col = getattr(self, method_name)()
+        merged = {}
+        for v, r, c in zip(np.asarray(data).tolist(), np.asarray(row).tolist(), np.asarray(col).tolist()):
+            merged[(r, c)] = merged[(r, c)] + v if (r, c) in merged else v
+        keys = list(merged)
+        return sp.csc_matrix((list(merged.values()), ([k[0] for k in keys], [k[1] for k in keys])))
+
+    def k_matrix_dense(self):
+        return self.matrix_dense('k_matrix_data')
+
+    def m_matrix_dense(self):
+        return self.matrix_dense('m_matrix_data')
+
+    def elements_permeability(self):
+        """mu_total of the first element of every group (analysis.py:292-306)."""
+        if isinstance(self.mesh, ArrayMesh):
+            prob = self.problem()
+            return [float(prob.mu[int(a)]) for a in self.mesh.group_ptr[:-1]]
+        return [g.elements[0].mu_total for g in self.mesh.elements_groups]
+
+    def c_matrix_boundary_conditions(self):
+        """(data, row, col): for de-duplicated condition i at DOF p, (n*dim + i, p) and
+        (p, n*dim + i), both 1 (analysis.py:241-279)."""
+        sysm = self.system()
+        self._boundary_conditions = list(zip(sysm.bc_dof.tolist(), sysm.bc_value.tolist()))
+        nd = self.problem().n_dof
+        data, row, col = [], [], []
+        for i, p in enumerate(sysm.bc_dof.tolist()):
+            data.extend((1, 1))
+            row.extend((nd + i, p))
+            col.extend((p, nd + i))
+        return data, row, col
+
+    def c_matrix_continuity_conditions(self):
+        """(data, row, col) at the reference's rows n_nodes + len(node_loads) + i
+        (analysis.py:175-199)."""
+        d, r, c = self.system().continuity_triplets()
+        return d.tolist(), r.tolist(), c.tolist()
+
+    def get_source_matrix_length(self):
+        """n*dim + n_continuity + n_bc (analysis.py:737-739); TypeError before
+        create_matrix, as in the reference."""
+        if self._boundary_conditions is None:
+            raise TypeError("object of type 'NoneType' has no len()")
+        prob = self.problem()
+        return prob.n_dof + prob.n_cont + len(self._boundary_conditions)
+
+    def source_c_matrix_boundary_conditions(self):
+        """(values, rows n*dim + i) of the de-duplicated conditions (analysis.py:509-543)."""
+        sysm = self.system()
+        self._boundary_conditions = list(zip(sysm.bc_dof.tolist(), sysm.bc_value.tolist()))
+        nd = self.problem().n_dof
+        return sysm.bc_value.tolist(), [nd + i for i in range(len(sysm.bc_dof))]
+
+    def source_c_matrix_magnet_loads(self):
+        """(values, node rows) of the magnet loads (analysis.py:556-577)."""
+        from .loads import magnet_contributions
+        prob = self.problem()
+        data, rows = [], []
+        for m in prob.magnet_loads:
+            r, v = magnet_contributions(prob.coords, prob.conn, m.elements, m.non_contour_nodes, m.magnetization)
+            data += v.tolist()
+            rows += r.tolist()
+        return data, rows
+
+    def source_c_matrix_loads(self):
+        """(values, DOF rows) of the de-duplicated loads, last value per (node, dimension)
+        in first-insertion order (analysis.py:457-489, :71-110)."""
+        prob, sysm = self.problem(), self.system()
+        keys, vals = sysm.load_list()
+        table = {}
+        for k, v in zip(keys, vals):
+            table[k] = v
+        return list(table.values()), list(table.keys())
+
+    def _node_objects(self, keys_values, cls):
+        nodes = self.mesh.nodes
+        d = self.problem().dim
+        return [cls(nodes[k // d], v, k % d + 1) for k, v in keys_values]
+
+    def loads_element_to_node(self):
+        """NodeLoads of the element loads, per element and point (analysis.py:407-429)."""
+        from .loads import NodeLoad
+        prob, sysm = self.problem(), self.system()
+        n_user = prob.node_load_node.size
+        keys, vals = sysm.load_list()
+        n_el = len(keys) - n_user - 2 * prob.edge_load_dim.size
+        return self._node_objects(zip(keys[n_user:n_user + n_el], vals[n_user:n_user + n_el]), NodeLoad)
+
+    def loads_edge_to_node(self):
+        """NodeLoads of the edge loads, half to each end (analysis.py:431-447)."""
+        from .loads import NodeLoad
+        prob, sysm = self.problem(), self.system()
+        keys, vals = sysm.load_list()
+        m = 2 * prob.edge_load_dim.size
+        return self._node_objects(zip(keys[len(keys) - m:], vals[len(vals) - m:]), NodeLoad)
+
+    def boundary_conditions_element_to_node(self):
+        """NodeBoundaryConditions of the element conditions (analysis.py:201-220)."""
+        from .conditions import NodeBoundaryCondition
+        keys, vals = self.system().condition_list()
+        prob = self.problem()
+        a = prob.node_bc_node.size
+        b = len(keys) - 2 * prob.edge_bc_dim.size
+        return self._node_objects(zip(keys[a:b], vals[a:b]), NodeBoundaryCondition)
+
+    def boundary_conditions_edge_to_node(self):
+        """NodeBoundaryConditions of the edge conditions (analysis.py:222-239)."""
+        from .conditions import NodeBoundaryCondition
+        keys, vals = self.system().condition_list()
+        m = 2 * self.problem().edge_bc_dim.size
+        return self._node_objects(zip(keys[len(keys) - m:], vals[len(vals) - m:]), NodeBoundaryCondition)
 
     def _check_shapes(self):
         """spsolve's check of the reference's create_matrix against its

@@ -102,20 +102,59 @@ class GpuSystem:
             self.handle.call("fe_element_node_factors", elements.size, ptr(elements), ptr(out))
         return out
 
-    def _dirichlet(self):
+    def condition_list(self):
+        """(DOFs, values) of every condition before de-duplication, in the order of
+        c_matrix_boundary_conditions (analysis.py:252-256): node conditions, element
+        conditions times element_to_node_factors (analysis.py:201-220), edge
+        conditions halved (analysis.py:222-239)."""
         p = self.prob
-        table = {}
+        keys, vals = [], []
         for n, d, v in zip(p.node_bc_node.tolist(), p.node_bc_dim.tolist(), p.node_bc_value.tolist()):
-            table[self._dof(n, d)] = v
+            keys.append(self._dof(n, d))
+            vals.append(v)
         if p.element_bc_element.size:
             fac = self._element_factors(p.element_bc_element)
             for k, (e, d, v) in enumerate(zip(p.element_bc_element.tolist(), p.element_bc_dim.tolist(),
                                               p.element_bc_value.tolist())):
                 for i, node in enumerate(p.conn[e].tolist()):
-                    table[self._dof(node, d)] = v * fac[k, i]
+                    keys.append(self._dof(node, d))
+                    vals.append(v * fac[k, i])
         for (a, b), d, v in zip(p.edge_bc_nodes.tolist(), p.edge_bc_dim.tolist(), p.edge_bc_value.tolist()):
-            table[self._dof(a, d)] = v * 0.5
-            table[self._dof(b, d)] = v * 0.5
+            keys += [self._dof(a, d), self._dof(b, d)]
+            vals += [v * 0.5, v * 0.5]
+        return keys, vals
+
+    def load_list(self):
+        """(DOFs, values) of every load before de-duplication, in the order of
+        source_c_matrix_loads (analysis.py:465-469): user NodeLoads, element loads
+        (value * area / total area, loads.py:32-34, times element_to_node_factors per
+        point), edge loads halved.  The device computes the same values during
+        assembly; this host copy serves the reference's intermediate lists."""
+        p = self.prob
+        keys = [self._dof(n, d) for n, d in zip(p.node_load_node.tolist(), p.node_load_dim.tolist())]
+        vals = list(p.node_load_value.tolist())
+        for ls in p.element_loads:
+            pts = p.coords[p.conn[ls.elements]]
+            area = np.abs((pts[:, 1, 0] - pts[:, 0, 0]) * (pts[:, 2, 1] - pts[:, 0, 1])
+                          - (pts[:, 2, 0] - pts[:, 0, 0]) * (pts[:, 1, 1] - pts[:, 0, 1])) / 2.0
+            total = 0
+            for a in area.tolist():
+                total += a
+            fac = self._element_factors(ls.elements)
+            for k, e in enumerate(ls.elements.tolist()):
+                per = ls.value * area[k] / total
+                for i, node in enumerate(p.conn[e].tolist()):
+                    keys.append(self._dof(node, ls.dimension))
+                    vals.append(per * fac[k, i])
+        for (a, b), d, v in zip(p.edge_load_nodes.tolist(), p.edge_load_dim.tolist(), p.edge_load_value.tolist()):
+            keys += [self._dof(a, d), self._dof(b, d)]
+            vals += [v * 0.5, v * 0.5]
+        return keys, vals
+
+    def _dirichlet(self):
+        table = {}
+        for k, v in zip(*self.condition_list()):
+            table[k] = v
         dof = np.fromiter(table.keys(), dtype=np.int64, count=len(table))
         val = np.fromiter(table.values(), dtype=np.float64, count=len(table))
         return dof, val
