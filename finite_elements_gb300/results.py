@@ -9,6 +9,83 @@ import numpy as np
 MU = 4 * math.pi * 1e-7   # finite_elements/core.py:31
 
 
+class PerItem:
+    """Per-element (or per-node) results: an array, one row per element (node) in mesh
+    order, that can also be indexed by the mesh's element (node) objects, as the
+    reference's dicts are ({element: value}, results.py:639-830).  Integer indices,
+    slices and index arrays address rows; ``keys()``, ``values()`` and ``items()``
+    and iteration follow the dict."""
+
+    def __init__(self, values, keys_fn):
+        self._values = values
+        self._keys_fn = keys_fn
+        self._by_id = None
+        self._by_eq = None
+
+    def __array__(self, dtype=None, copy=None):
+        return np.asarray(self._values, dtype=dtype)
+
+    @property
+    def shape(self):
+        return self._values.shape
+
+    @property
+    def ndim(self):
+        return self._values.ndim
+
+    @property
+    def dtype(self):
+        return self._values.dtype
+
+    def __len__(self):
+        return len(self._values)
+
+    def _row(self, key):
+        if self._by_id is None:
+            keys = self._keys_fn()
+            self._by_id = {id(k): i for i, k in enumerate(keys)}
+            self._by_eq = {}
+            for i, k in enumerate(keys):
+                try:
+                    self._by_eq.setdefault(k, i)
+                except TypeError:
+                    pass
+        i = self._by_id.get(id(key))
+        if i is None:
+            i = self._by_eq[key]
+        return i
+
+    def __getitem__(self, key):
+        if isinstance(key, (int, np.integer, slice, tuple, list, np.ndarray)):
+            return self._values[key]
+        return self._values[self._row(key)]
+
+    def keys(self):
+        return list(self._keys_fn())
+
+    def values(self):
+        return list(self._values)
+
+    def items(self):
+        return list(zip(self._keys_fn(), self._values))
+
+    def __iter__(self):
+        return iter(self._keys_fn())
+
+    def __repr__(self):
+        return f"PerItem({self._values!r})"
+
+
+def _element_keys(mesh):
+    if hasattr(mesh, "as_arrays"):
+        return lambda: range(mesh.n_elements)
+    return lambda: [el for g in mesh.elements_groups for el in g.elements]
+
+
+def _node_keys(mesh):
+    return lambda: mesh.nodes
+
+
 class Result:
     """``mesh`` and ``result_vector``: n_nodes*dim displacements (or potentials)
     followed by one Lagrange multiplier per Dirichlet condition.  ``dimension`` comes
@@ -102,37 +179,37 @@ class ElasticityResults2D(Result):
 
     @property
     def strain(self):
-        return self._compute()["strain"]
+        return PerItem(self._compute()["strain"], _element_keys(self.mesh))
 
     @property
     def stress(self):
-        return self._compute()["stress"]
+        return PerItem(self._compute()["stress"], _element_keys(self.mesh))
 
     @property
     def energy_per_element(self):
-        return self._compute()["energy"]
+        return PerItem(self._compute()["energy"], _element_keys(self.mesh))
 
     @property
     def energy(self):
-        return float(np.sum(self.energy_per_element))
+        return float(np.sum(self._compute()["energy"]))
 
     @property
     def displacement_vectors_per_node(self):
         n, d = len(self.mesh.nodes), self._ncomp
-        return np.asarray(self.result_vector[: d * n], np.float64).reshape(n, d)
+        return PerItem(np.asarray(self.result_vector[: d * n], np.float64).reshape(n, d), _node_keys(self.mesh))
 
     @property
     def displacements_per_element(self):
         """(E, npe*d) element DOF vectors, node-major (results.py:677-700), real part."""
         coords, conn = mesh_arrays(self.mesh)
-        u = np.real(self.displacement_vectors_per_node)
-        return u[np.asarray(conn, np.int64)].reshape(conn.shape[0], -1)
+        u = np.real(np.asarray(self.displacement_vectors_per_node))
+        return PerItem(u[np.asarray(conn, np.int64)].reshape(conn.shape[0], -1), _element_keys(self.mesh))
 
     def deformed_nodes_m(self, amplitude=1):
         """(n, d) node coordinates moved by amplitude times the displacement
         (results.py:587-616), in mesh.nodes order."""
         coords, _ = mesh_arrays(self.mesh)
-        return coords[:, : self._ncomp] + amplitude * np.real(self.displacement_vectors_per_node)
+        return coords[:, : self._ncomp] + amplitude * np.real(np.asarray(self.displacement_vectors_per_node))
 
     @property
     def deformed_nodes(self):
@@ -150,28 +227,28 @@ class ElasticityResults2D(Result):
         return self.deformed_mesh_m()
 
     def displacement_per_node_x(self):
-        return self.displacement_vectors_per_node[:, 0]
+        return np.asarray(self.displacement_vectors_per_node)[:, 0]
 
     def displacement_per_node_y(self):
-        return self.displacement_vectors_per_node[:, 1]
+        return np.asarray(self.displacement_vectors_per_node)[:, 1]
 
     def axial_strain_x(self):
-        return self.strain[:, 0]
+        return np.asarray(self.strain)[:, 0]
 
     def axial_strain_y(self):
-        return self.strain[:, 1]
+        return np.asarray(self.strain)[:, 1]
 
     def axial_stress_x(self):
-        return self.stress[:, 0]
+        return np.asarray(self.stress)[:, 0]
 
     def axial_stress_y(self):
-        return self.stress[:, 1]
+        return np.asarray(self.stress)[:, 1]
 
     def shear_strain_xy(self):
-        return self.strain[:, 2]
+        return np.asarray(self.strain)[:, 2]
 
     def shear_stress_xy(self):
-        return self.stress[:, 2]
+        return np.asarray(self.stress)[:, 2]
 
     def generate_vtk_file(self, file_name_output):
         """The mesh with the displacement as point data, ``Displacement_Magnitude``
@@ -181,7 +258,7 @@ class ElasticityResults2D(Result):
         if file_name_output[-3:] != "vtk":
             file_name_output += ".vtk"
         coords, conn = mesh_arrays(self.mesh)
-        u = self.displacement_vectors_per_node
+        u = np.asarray(self.displacement_vectors_per_node)
         write_vtk(file_name_output, coords, conn,
                   point_scalars=[("Displacement_Magnitude", np.sqrt(np.sum(u * u, axis=1)))],
                   point_vectors=[("Displacement_Vectors", u)])
@@ -196,31 +273,31 @@ class ElasticityResults3D(ElasticityResults2D):
     _ncomp = 3
 
     def displacement_per_node_z(self):
-        return self.displacement_vectors_per_node[:, 2]
+        return np.asarray(self.displacement_vectors_per_node)[:, 2]
 
     def axial_strain_z(self):
-        return self.strain[:, 2]
+        return np.asarray(self.strain)[:, 2]
 
     def axial_stress_z(self):
-        return self.stress[:, 2]
+        return np.asarray(self.stress)[:, 2]
 
     def shear_strain_xy(self):
-        return self.strain[:, 3]
+        return np.asarray(self.strain)[:, 3]
 
     def shear_strain_yz(self):
-        return self.strain[:, 4]
+        return np.asarray(self.strain)[:, 4]
 
     def shear_strain_zx(self):
-        return self.strain[:, 5]
+        return np.asarray(self.strain)[:, 5]
 
     def shear_stress_xy(self):
-        return self.stress[:, 3]
+        return np.asarray(self.stress)[:, 3]
 
     def shear_stress_yz(self):
-        return self.stress[:, 4]
+        return np.asarray(self.stress)[:, 4]
 
     def shear_stress_zx(self):
-        return self.stress[:, 5]
+        return np.asarray(self.stress)[:, 5]
 
 
 class MagneticResults(Result):
@@ -232,8 +309,7 @@ class MagneticResults(Result):
         self._system = system
         self._field = None
 
-    @property
-    def magnetic_field_per_element(self):
+    def _b(self):
         if self._field is None:
             if self._system is None:
                 self._system = _system_for(self.mesh)
@@ -241,8 +317,13 @@ class MagneticResults(Result):
         return self._field
 
     @property
+    def magnetic_field_per_element(self):
+        return PerItem(self._b(), _element_keys(self.mesh))
+
+    @property
     def magnetic_field_norm(self):
-        return np.hypot(self.magnetic_field_per_element[:, 0], self.magnetic_field_per_element[:, 1])
+        b = self._b()
+        return np.hypot(b[:, 0], b[:, 1])
 
     # ---- air-gap quantities (results.py:82-243), host arithmetic on the device's B field
 
@@ -268,7 +349,7 @@ class MagneticResults(Result):
         cy = (p[:, 0, 1] + p[:, 1, 1] + p[:, 2, 1]) / 3.0
         r = np.sqrt(cx ** 2 + cy ** 2)
         ex, ey = cx / r, cy / r
-        b = self.magnetic_field_per_element[idx]
+        b = self._b()[idx]
         br = b[:, 0] * ex + b[:, 1] * ey
         bt = b[:, 0] * -ey + b[:, 1] * ex
         return r, br, bt, b, p

@@ -93,3 +93,24 @@ def test_result_accessors_on_the_host():
     assert r3.displacements_per_element.shape == (t3.shape[0], 12)
     np.testing.assert_array_equal(r3.displacement_per_node_z(), u3[2::3])
     np.testing.assert_array_equal(r3.deformed_nodes, c3 + u3.reshape(-1, 3))
+
+
+def test_per_item_results_index_like_the_reference_dicts():
+    """Per-node and per-element results accept the mesh's node and element objects as
+    keys, as the reference's dicts do, and integer rows, as arrays do."""
+    import numpy as np
+    from finite_elements_gb300 import elements as El, mesh as M
+    from finite_elements_gb300.results import ElasticityResults2D
+    pts = [M.Node2D(0, 0), M.Node2D(1, 0), M.Node2D(0, 1), M.Node2D(1, 1)]
+    tris = [El.ElasticityTriangularElement2D(M.TriangularElement2D([pts[0], pts[1], pts[2]]), 1e9, 0.3, 1.0),
+            El.ElasticityTriangularElement2D(M.TriangularElement2D([pts[3], pts[2], pts[1]]), 1e9, 0.3, 1.0)]
+    mesh = M.Mesh([M.ElementsGroup(tris)])
+    u = np.arange(8, dtype=float)
+    r = ElasticityResults2D(mesh, list(u), False, True)
+    d = r.displacement_vectors_per_node
+    np.testing.assert_array_equal(d[M.Node2D(1, 1)], [6.0, 7.0])        # equal coordinates find the node
+    np.testing.assert_array_equal(d[pts[1]], d[1])
+    assert np.asarray(d).shape == (4, 2) and list(d.keys()) == mesh.nodes
+    e = r.displacements_per_element
+    np.testing.assert_array_equal(e[tris[1]], [6.0, 7.0, 4.0, 5.0, 2.0, 3.0])
+    assert [k for k, _ in e.items()] == tris
