@@ -488,6 +488,20 @@ def run_tet(args):
            "relres": {k: v["relres"] for k, v in res.items()},
            "rel_diff_mixed_vs_plain": diff, "assemble_ms": res["plain"]["assemble_ms"]}
     s.close()
+    if not args.no_cpu_baseline:
+        # the reference path on the host cores: the oracle's restatement (element loop, COO,
+        # csr_matrix, NATURAL spsolve on the saddle system) on a bounded 3D sample
+        from oracle import fe_oracle as O
+        sample = meshgen.cantilever_3d(40, 8, 8)
+        t0 = time.perf_counter()
+        O.solve(sample)
+        dt = time.perf_counter() - t0
+        model, ncpu = cpu_info()
+        out["cpu_baseline"] = {
+            "value": dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"one solve of the tetrahedral cantilever 40x8x8 cells ({sample.n_dof:,} DOF) through "
+                      "the oracle's restatement of the reference path (NATURAL spsolve does not reach 4M DOF "
+                      "in host memory)", "host": f"{model}, {ncpu} cores"}
     return out
 
 
