@@ -63,6 +63,9 @@ def parse_args():
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--cpu-nx", type=int, default=200, help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--l2-keep", type=float, default=-1.0,
+                    help="MB of the FP32 preconditioner matrix kept L2-resident across Chebyshev steps "
+                         "(default: the library's 40 MB; 0 = plain loads)")
     ap.add_argument("--workload", choices=("plane_strain", "tet"), default="plane_strain",
                     help="tet: the secondary 3D line (solid cantilever of linear tetrahedra)")
     ap.add_argument("--tet-dims", type=int, nargs=3, default=(320, 64, 64),
@@ -208,6 +211,8 @@ def run_ours(args, dist):
     prob = meshgen.plane_strain_random(args.nx, args.ny, seed=args.seed)
     s = GpuSystem(prob, assemble=True)           # inputs uploaded: resident in HBM from here
     h = s.handle
+    if args.l2_keep >= 0:
+        h.call("fe_set_l2_keep", int(args.l2_keep * 1e6))
     step_flags = _lib.FE_ASSEMBLE_PATTERN | _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
     # headline: FP64 CG recurrence with the FP32 Chebyshev preconditioner; beside it the
     # FP32-Krylov + iterative-refinement form and the plain FP64 PCG
@@ -402,6 +407,7 @@ def run_ours(args, dist):
                     + (" + learned warm start (predicted every step; kept when its FP64 residual beats the zero "
                        "start)" if net is not None else ""),
             "learned_warm_start": net is not None,
+            "l2_keep_mb": 40.0 if args.l2_keep < 0 else args.l2_keep,
             "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio],
                           "fp32_krylov_ir": [args.ir_cheb, args.ir_cheb_ratio]},
             "tol": args.tol, "step": "pattern + element kernels + reduction + loads + elimination + PCG",

@@ -82,6 +82,7 @@ _SIGNATURES = {
     "fe_get_solution": ([_P, _P], C.c_int),
     "fe_solution_device_ptr": ([_P, C.POINTER(_P)], C.c_int),
     "fe_info": ([_P, _PI64, _PI64, _PI64], C.c_int),
+    "fe_set_l2_keep": ([_P, _I64], C.c_int),
     "fe_event_record": ([_P, _I32], C.c_int),
     "fe_event_elapsed_ms": ([_P, _I32, _I32, _PD], C.c_int),
     "fe_synchronize": ([_P], C.c_int),

@@ -399,6 +399,16 @@ int fe_solution_device_ptr(fe_handle h, const double **ptr) {
     return FE_OK;
 }
 
+int fe_set_l2_keep(fe_handle h, int64_t bytes) {
+    FE_HANDLE_CHECK(h);
+    if (bytes < 0) {
+        set_error("fe_set_l2_keep: negative size");
+        return FE_BAD_INPUT;
+    }
+    h->l2_keep = (uint64_t)bytes;
+    return FE_OK;
+}
+
 int fe_info(fe_handle h, int64_t *n_dof, int64_t *n_bc, int64_t *n_blocks) {
     FE_HANDLE_CHECK(h);
     if (n_dof) *n_dof = h->n_dof;

@@ -132,6 +132,7 @@ struct SolverWork {
         const void *x = nullptr;
         double theta = 0, delta = 0;
         bool prof = false;
+        uint64_t keep = 0;
     } key[3];
     // Kernel timing inside the captured loop (fe_profile_kernels): event records in
     // the first iteration of every chunk, [slot][0] around the run of intermediate
@@ -198,6 +199,11 @@ struct fe_handle_s {
     fe::DBuf<int64_t> comp_ptr, comp_dof;
     fe::DBuf<double> comp_s;
     std::vector<double> mu_host;   // continuity multipliers of the last solve
+
+    // bytes of the FP32 SELL values kept L2-resident across Chebyshev steps (0 = off);
+    // 40 MB measured best at 4M DOF (1.813 s against 1.893 s with plain loads; 80, 110,
+    // 140 and 200 MB gave 1.87 s: the gathered vectors need the rest of the L2)
+    uint64_t l2_keep = 40000000;
 
     // pattern: node-block CSR
     bool pattern_ready = false;

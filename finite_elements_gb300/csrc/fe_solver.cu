@@ -269,7 +269,28 @@ struct Sell {
     const int32_t *off, *col;
     const int16_t *dcol;   // column offsets c - r when every one fits in 16 bits, else null
     int64_t n_slices;
+    // FP32 copy, 2 DOF per node: the first keep bytes of the values are loaded with L2
+    // priority evict_last and the rest (up to total) evict_first, so that a prefix of
+    // the matrix stays in L2 from one Chebyshev step to the next; 0 = plain loads
+    uint32_t keep = 0, total = 0;
 };
+
+// Loads of the FP32 2x2 blocks under the L2 policy of Sell::keep.
+__device__ __forceinline__ uint64_t l2_keep_policy(const void *base, uint32_t keep, uint32_t total) {
+    uint64_t pol;
+    asm("createpolicy.range.global.L2::evict_last.L2::evict_first.b64 %0, [%1], %2, %3;"
+                 : "=l"(pol)
+                 : "l"(base), "r"(keep), "r"(total));
+    return pol;
+}
+
+__device__ __forceinline__ float4 ld_block_hint(const float *p, uint64_t pol) {
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
 
 // Calls f(std::true_type) when an FP32 kernel can read the 16-bit column offsets,
 // else f(std::false_type); FP64 kernels always read the int32 columns.
@@ -292,7 +313,7 @@ void with_col16(const Sell &A, F f) {
 // zero block) multiplies x_r; there is no diagonal term.  Rows past the last node
 // (padding of the final slice) gather their own padding row -- the solver's vectors
 // are allocated for whole slices -- and their result is discarded.
-template <int D, typename T, bool C16 = false>
+template <int D, typename T, bool C16 = false, bool KEEP = false>
 __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const Sell &A, const T *__restrict__ val,
                                                   const T *__restrict__ diag, const T *__restrict__ x) {
     constexpr bool DIFF = sizeof(T) == 4;
@@ -307,6 +328,10 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
     const int lane = (int)(r & 31);
     const int64_t base = A.off[sl];
     const int w = (A.off[sl + 1] - (int)base) >> 5;
+    // KEEP (FP32, 2 DOF per node): the block loads carry the L2 policy of A.keep
+    constexpr bool HINT = KEEP && D == 2 && sizeof(T) == 4;
+    uint64_t pol = 0;
+    if constexpr (HINT) pol = l2_keep_policy(val, A.keep, A.total);
     // FP32: four entries per trip, their column loads and then their gathers all in
     // flight before the first product (entries past w read the row itself and add
     // 0).  FP64 is bound by the FP64 FMA rate and runs one entry per trip.
@@ -328,7 +353,16 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
 #pragma unroll
                     for (int a = 0; a < D; ++a) xv[u].v[a] -= xr.v[a];
                 }
-                block_mac<D, T>(val + (base + 32 * (int64_t)(k + u) + lane) * D * D, xv[u], acc);
+                const T *blk = val + (base + 32 * (int64_t)(k + u) + lane) * D * D;
+                if constexpr (HINT) {
+                    const float4 b = ld_block_hint(blk, pol);
+                    acc.v[0] = fmaf(b.x, xv[u].v[0], acc.v[0]);
+                    acc.v[1] = fmaf(b.z, xv[u].v[0], acc.v[1]);
+                    acc.v[0] = fmaf(b.y, xv[u].v[1], acc.v[0]);
+                    acc.v[1] = fmaf(b.w, xv[u].v[1], acc.v[1]);
+                } else {
+                    block_mac<D, T>(blk, xv[u], acc);
+                }
             }
         }
     }
@@ -525,8 +559,8 @@ k_pcg_update(int64_t n_nodes, double *__restrict__ x, T *__restrict__ r, const T
 // MODE 1: last step of an iteration (reduces rdot.z_{k+1} in FP64, finishes the
 //         iteration; rdot is the recurrence's residual);
 // MODE 2: intermediate step.
-template <int D, typename T, typename RD, int MODE, bool FIRST, bool C16>
-__global__ void __launch_bounds__(kVecThreads, kSellBlocks<D, T>)   // FP32: 8 blocks per SM, one wave
+template <int D, typename T, typename RD, int MODE, bool FIRST, bool C16, bool KEEP = false>
+__global__ void __launch_bounds__(kVecThreads, KEEP ? 6 : kSellBlocks<D, T>)   // FP32: 8 blocks per SM, one wave
 k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
             const T *__restrict__ dinv, const T *__restrict__ rres, const T *__restrict__ z_in,
             T *__restrict__ zprev_out, double c1, double c2, double *partials, PcgScalars *sc,
@@ -537,7 +571,7 @@ k_cheb_step(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restr
     double lrz = 0.0;
     FE_SELL_LOOP {
         const bool valid = row < n_nodes;
-        NodeVec<D, T> az = sell_row<D, T, C16>(row, valid, A, val, diag, z_in);
+        NodeVec<D, T> az = sell_row<D, T, C16, KEEP>(row, valid, A, val, diag, z_in);
         if (valid) {
             NodeVec<D, T> rv = ld<D, T>(rres, row), zv = ld<D, T>(z_in, row), zp;
             if (FIRST) {
@@ -872,6 +906,15 @@ Sys<T> make_sys(fe_handle_s *h) {
     SolverWork &w = h->w;
     s.x = w.x.p;
     s.A = Sell{h->sell_off.p, h->sell_col.p, h->sell_c16 ? h->sell_dcol.p : nullptr, h->n_slices};
+    if constexpr (sizeof(T) == 4) {
+        if (D == 2 && h->l2_keep > 0) {
+            const uint64_t total = (uint64_t)h->sell_val32.n * sizeof(float);
+            if (total <= 0xffffffffULL) {
+                s.A.total = (uint32_t)total;
+                s.A.keep = (uint32_t)std::min<uint64_t>(h->l2_keep, total);
+            }
+        }
+    }
     if constexpr (sizeof(T) == 8) {
         s.sval = h->sell_val64.p, s.diag = h->diag64.p;
         s.val = h->aval.p, s.dinv = h->dinv.p;
@@ -891,6 +934,14 @@ void launch_cheb_step(fe_handle_s *h, const Sys<T> &s, bool first, const T *zin,
                       double *part, PcgScalars *sc, int grid, const RD *rdot) {
     with_col16<T>(s.A, [&](auto c16) {
         constexpr bool C = decltype(c16)::value;
+        if constexpr (MODE == 2 && D == 2 && sizeof(T) == 4) {
+            // intermediate steps with an L2-resident prefix of the matrix: 6 blocks per SM
+            if (!first && s.A.keep > 0) {
+                k_cheb_step<D, T, RD, MODE, false, C, true><<<std::min(grid, 152 * 6), kVecThreads, 0, h->stream>>>(
+                    h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
+                return;
+            }
+        }
         if (first)
             k_cheb_step<D, T, RD, MODE, true, C><<<grid, kVecThreads, 0, h->stream>>>(
                 h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
@@ -1101,7 +1152,7 @@ int run_chunks(fe_handle_s *h, int slot, const void *key_ptr, int G, const Cheb 
     SolverWork::Key &kk = w.key[slot];
     const bool prof = w.prof && w.pev[0];
     bool same = w.graph[slot] && kk.k == cb.k && kk.G == G && kk.chunk == chunk && kk.x == key_ptr &&
-                kk.theta == cb.theta && kk.delta == cb.delta && kk.prof == prof;
+                kk.theta == cb.theta && kk.delta == cb.delta && kk.prof == prof && kk.keep == h->l2_keep;
     if (!same) {
         if (w.graph[slot]) {
             cudaGraphExecDestroy(w.graph[slot]);
@@ -1123,7 +1174,7 @@ int run_chunks(fe_handle_s *h, int slot, const void *key_ptr, int G, const Cheb 
             return FE_CUDA_ERR;
         }
         kk.k = cb.k, kk.G = G, kk.chunk = chunk, kk.x = key_ptr, kk.theta = cb.theta, kk.delta = cb.delta;
-        kk.prof = prof;
+        kk.prof = prof, kk.keep = h->l2_keep;
     }
     const int per_iter = 3 + (cb.k - 1);
     bool launched = false;

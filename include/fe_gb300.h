@@ -195,6 +195,11 @@ int fe_export_element_matrices(fe_handle h, int32_t which, double *out_host);
  * u then lambda, as solve() returns them (analysis.py:816-830), followed by the
  * n_cont continuity multipliers when fe_set_continuity set any. */
 int fe_solve(fe_handle h, const fe_solve_opts *opts, double *x_host, fe_solve_stats *stats);
+/* L2 residency of the FP32 preconditioner matrix (2 DOF per node): the first `bytes`
+ * of its values are loaded with L2 priority evict_last and the rest evict_first, so
+ * that this prefix stays in L2 from one Chebyshev step to the next.  Default 40 MB
+ * (40000000); 0 = plain loads.  No counterpart in the reference. */
+int fe_set_l2_keep(fe_handle h, int64_t bytes);
 /* Copy the last solution (n_dof + n_bc [+ n_cont] values) to the host. */
 int fe_get_solution(fe_handle h, double *x_host);
 /* Device address of the last solution u (n_dof doubles), valid until the next solve. */
