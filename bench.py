@@ -30,8 +30,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # DRAM bytes (read + write) per launch of the roofline kernel (the intermediate FP32
-# Chebyshev step) from one ncu capture of this workload, keyed by grid (summary in
-# profiles/cheb_step_fp32_plane_strain_4M.md); None when the workload differs.
+# Chebyshev step with plain loads, --l2-keep 0) from one ncu capture of this workload,
+# keyed by grid (summary in profiles/cheb_step_fp32_plane_strain_4M.md); None when the
+# workload or the load policy differs.
 NCU_TRAFFIC = {(2000, 1000): 278_710_784}
 
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
@@ -368,7 +369,9 @@ def run_ours(args, dist):
     spmvmp_gbs, spmvmp_frac = roof(spmv_bytes(8), prof_mixed["spmv_us"])
     cheb64_gbs, cheb64_frac = roof(cheb_bytes(8), prof_plain["cheb_us"])
     spmv64_gbs, spmv64_frac = roof(spmv_bytes(8), prof_plain["spmv_us"])
-    traffic = NCU_TRAFFIC.get((args.nx, args.ny))
+    # the capture is of the step with plain loads; with an L2-resident prefix the DRAM
+    # traffic of the step is lower and not captured (null)
+    traffic = NCU_TRAFFIC.get((args.nx, args.ny)) if args.l2_keep == 0 else None
     s.close()
 
     # ---- end to end through the C ABI, host buffers in and out
