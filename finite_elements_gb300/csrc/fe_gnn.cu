@@ -3,7 +3,7 @@
 // predicts the shape u_hat of the displacement field; the warm start is
 // x0 = g + s u_hat with g the prescribed values and s = (u_hat . b~) / (u_hat . A u_hat),
 // the scale that minimises the A-norm error along u_hat (b~ = b - A g, zero on the
-// constrained DOFs).  PCG from x0 to the same tolerance stays the judge of accuracy.
+// constrained DOFs).  PCG from x0 to the same tolerance still decides the accuracy.
 //
 // Network (hidden width 64, 6 layers):
 //   h0 = relu(f W0 + b0)                       f: 16 node features
