@@ -91,3 +91,25 @@ def test_problem_shapes():
     prob = Problem(ELASTIC3D, np.zeros((4, 3)), [[0, 1, 2, 3]], E=1.0, nu=0.3, rho=1.0,
                    plane_strain=True, plane_stress=False)
     assert prob.dim == 3 and prob.npe == 4 and prob.n_dof == 12 and prob.elastic
+
+
+def test_annulus_mesh():
+    import math
+    c, conn = meshgen.annulus([0.5, 0.75, 1.0], 24)
+    assert conn.shape == (2 * 2 * 24, 3)
+    p = c[conn]
+    det = (p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])
+    area = np.abs(det).sum() / 2
+    # the polygonal annulus: 24 sectors of (R^2 - r^2) sin(2 pi / 24) / 2
+    assert abs(area - 24 * (1.0 - 0.25) * math.sin(2 * math.pi / 24) / 2) <= 1e-12
+    edges = np.sort(conn[:, [[0, 1], [1, 2], [0, 2]]].reshape(-1, 2), axis=1)
+    _, counts = np.unique(edges, axis=0, return_counts=True)
+    assert set(counts.tolist()) <= {1, 2} and (counts == 1).sum() == 2 * 24   # inner and outer circles
+
+
+def test_dirichlet_count_matches_the_oracle():
+    import golden_cases as gc
+    from finite_elements_gb300.engine import dirichlet_count
+    for name in gc.names():
+        prob, _, ref = gc.load(name)
+        assert dirichlet_count(prob) == ref["bc_dof"].size, name
