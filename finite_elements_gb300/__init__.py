@@ -1,11 +1,11 @@
-"""GB300 (sm_103a) assembly-and-solve path for linear triangles, drop-in for
-finite_elements' FiniteElementAnalysis.
+"""GB300 (sm_103a) assembly-and-solve path for linear triangles and tetrahedra, drop-in
+for finite_elements' FiniteElementAnalysis.
 
 The compute path is libfe_gb300.so (hand-written CUDA, C ABI in include/fe_gb300.h);
 the Python modules hold the reference's object API and its list bookkeeping.
 """
 from . import conditions, core, elements, loads, mesh, results  # noqa: F401
-from .problem import ELASTIC, MAGNETIC, ElementLoadSet, Problem  # noqa: F401
+from .problem import ELASTIC, ELASTIC3D, MAGNETIC, ElementLoadSet, MagnetLoadSet, Problem  # noqa: F401
 
 __version__ = "0.1.0"
 
