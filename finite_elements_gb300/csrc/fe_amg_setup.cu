@@ -1,0 +1,451 @@
+// Setup of a smoothed-aggregation multigrid hierarchy (Vanek, Mandel and Brezina,
+// Computing 56, 1996) on the host, from the node-block CSR of the eliminated system
+// matrix: the stage before a device V-cycle preconditioner.
+//
+// Per level, with d x d blocks and a near-null space B (n d x m, the rigid-body modes
+// on the fine level):
+//   strength      block (i, j), i != j, is strong when sum|A_ij| >= theta sqrt(sum|A_ii| sum|A_jj|)
+//   aggregation   in node order, a node whose strong neighbours are all free starts an
+//                 aggregate with them; the nodes left join the aggregate of their first
+//                 aggregated strong neighbour (in column order), else form a singleton
+//   P_tent        per aggregate, the thin QR of B on its DOFs (modified Gram-Schmidt,
+//                 non-negative diag(R), dropped columns kept as zeros); R is the
+//                 coarse near-null space
+//   P             (I - 4/(3 lmax) D^-1 A) P_tent, D^-1 the block-diagonal
+//                 pseudo-inverse, lmax of D^-1 A by 30 power iterations from
+//                 x_i = 1 + (i mod 7) / 7
+//   A_c           P^T A P, m x m blocks
+// down to at most `coarse_dofs` DOFs (or 12 levels).  Host code only: no device call.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fe_internal.h"
+
+namespace fe {
+namespace {
+
+struct BlockCsr {
+    int64_t n = 0;             // block rows
+    int rd = 0, cd = 0;        // block size rd x cd
+    std::vector<int64_t> ptr;  // n + 1
+    std::vector<int32_t> col;
+    std::vector<double> val;   // nnzb * rd * cd, row-major blocks
+    int64_t nnzb() const { return (int64_t)col.size(); }
+};
+
+struct AmgLevel {
+    BlockCsr A;                 // d x d blocks
+    BlockCsr P;                 // d x m blocks, columns = aggregates
+    std::vector<int32_t> agg;   // aggregate of each node
+    double lmax = 0.0;
+};
+
+// Pseudo-inverse of a symmetric d x d block by cyclic Jacobi: V diag(1/l) V^T over the
+// eigenvalues above 1e-12 of the largest in magnitude.
+void sym_pinv(const double *a, int d, double *out) {
+    double A[36], V[36];
+    for (int i = 0; i < d * d; ++i) A[i] = a[i];
+    for (int i = 0; i < d; ++i)
+        for (int j = 0; j < d; ++j) V[i * d + j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < d; ++p)
+            for (int q = p + 1; q < d; ++q) off += A[p * d + q] * A[p * d + q];
+        if (off < 1e-30) break;
+        for (int p = 0; p < d; ++p)
+            for (int q = p + 1; q < d; ++q) {
+                const double apq = A[p * d + q];
+                if (apq == 0.0) continue;
+                const double th = (A[q * d + q] - A[p * d + p]) / (2.0 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < d; ++k) {
+                    const double akp = A[k * d + p], akq = A[k * d + q];
+                    A[k * d + p] = c * akp - s * akq;
+                    A[k * d + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < d; ++k) {
+                    const double apk = A[p * d + k], aqk = A[q * d + k];
+                    A[p * d + k] = c * apk - s * aqk;
+                    A[q * d + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < d; ++k) {
+                    const double vkp = V[k * d + p], vkq = V[k * d + q];
+                    V[k * d + p] = c * vkp - s * vkq;
+                    V[k * d + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    double lmax = 0.0;
+    for (int i = 0; i < d; ++i) lmax = std::max(lmax, std::fabs(A[i * d + i]));
+    for (int i = 0; i < d * d; ++i) out[i] = 0.0;
+    for (int k = 0; k < d; ++k) {
+        const double l = A[k * d + k];
+        if (std::fabs(l) <= 1e-12 * lmax || l == 0.0) continue;
+        for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j) out[i * d + j] += V[i * d + k] * V[j * d + k] / l;
+    }
+}
+
+std::vector<double> block_diag_pinv(const BlockCsr &A) {
+    const int d = A.rd;
+    std::vector<double> dinv((size_t)A.n * d * d, 0.0);
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s)
+            if (A.col[s] == i) sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
+    return dinv;
+}
+
+// y = A x (d x d blocks)
+void spmv(const BlockCsr &A, const std::vector<double> &x, std::vector<double> &y) {
+    const int d = A.rd;
+    y.assign((size_t)A.n * d, 0.0);
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
+            const double *b = &A.val[(size_t)s * d * d];
+            const int64_t c = A.col[s];
+            for (int a = 0; a < d; ++a) {
+                double acc = 0.0;
+                for (int k = 0; k < d; ++k) acc += b[a * d + k] * x[(size_t)c * d + k];
+                y[(size_t)i * d + a] += acc;
+            }
+        }
+}
+
+void apply_dinv(const std::vector<double> &dinv, int d, std::vector<double> &v) {
+    const int64_t n = (int64_t)v.size() / d;
+    double t[6];
+    for (int64_t i = 0; i < n; ++i) {
+        for (int a = 0; a < d; ++a) {
+            double acc = 0.0;
+            for (int k = 0; k < d; ++k) acc += dinv[(size_t)i * d * d + a * d + k] * v[(size_t)i * d + k];
+            t[a] = acc;
+        }
+        for (int a = 0; a < d; ++a) v[(size_t)i * d + a] = t[a];
+    }
+}
+
+double lmax_power(const BlockCsr &A, const std::vector<double> &dinv) {
+    const int d = A.rd;
+    const int64_t nd = A.n * d;
+    std::vector<double> x((size_t)nd), y;
+    for (int64_t i = 0; i < nd; ++i) x[i] = 1.0 + (double)(i % 7) / 7.0;
+    for (int it = 0; it < 30; ++it) {
+        spmv(A, x, y);
+        apply_dinv(dinv, d, y);
+        double nrm = 0.0;
+        for (double v : y) nrm += v * v;
+        nrm = std::sqrt(nrm);
+        for (int64_t i = 0; i < nd; ++i) x[i] = y[i] / nrm;
+    }
+    spmv(A, x, y);
+    apply_dinv(dinv, d, y);
+    double num = 0.0, den = 0.0;
+    for (int64_t i = 0; i < nd; ++i) num += x[i] * y[i], den += x[i] * x[i];
+    return num / den;
+}
+
+std::vector<int32_t> aggregate(const BlockCsr &A, double theta, int32_t *n_agg) {
+    const int d = A.rd;
+    const int64_t n = A.n;
+    std::vector<double> nrm((size_t)A.nnzb()), dg((size_t)n, 0.0);
+    for (int64_t s = 0; s < A.nnzb(); ++s) {
+        double t = 0.0;
+        for (int k = 0; k < d * d; ++k) t += std::fabs(A.val[(size_t)s * d * d + k]);
+        nrm[s] = t;
+    }
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s)
+            if (A.col[s] == i) dg[i] = nrm[s];
+    std::vector<int64_t> sptr((size_t)n + 1, 0);
+    std::vector<int32_t> scol;
+    for (int64_t i = 0; i < n; ++i) {
+        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
+            const int64_t j = A.col[s];
+            if (j != i && nrm[s] >= theta * std::sqrt(dg[i] * dg[j])) scol.push_back((int32_t)j);
+        }
+        sptr[i + 1] = (int64_t)scol.size();
+    }
+    std::vector<int32_t> agg((size_t)n, -1);
+    int32_t na = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        bool free_all = true;
+        for (int64_t s = sptr[i]; s < sptr[i + 1] && free_all; ++s) free_all = agg[scol[s]] < 0;
+        if (!free_all) continue;
+        agg[i] = na;
+        for (int64_t s = sptr[i]; s < sptr[i + 1]; ++s) agg[scol[s]] = na;
+        ++na;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        int32_t a = -1;
+        for (int64_t s = sptr[i]; s < sptr[i + 1] && a < 0; ++s)
+            if (agg[scol[s]] >= 0) a = agg[scol[s]];
+        agg[i] = a >= 0 ? a : na++;
+    }
+    *n_agg = na;
+    return agg;
+}
+
+// Thin QR by modified Gram-Schmidt (k x m, column-major in Q), diag(R) >= 0, columns
+// whose remainder is below 1e-12 of their norm dropped to zero.
+void qr_mgs(const std::vector<double> &X, int k, int m, std::vector<double> &Q, double *R) {
+    Q.assign((size_t)k * m, 0.0);
+    for (int i = 0; i < m * m; ++i) R[i] = 0.0;
+    std::vector<double> v((size_t)k);
+    for (int j = 0; j < m; ++j) {
+        double n0 = 0.0;
+        for (int r = 0; r < k; ++r) v[r] = X[(size_t)r * m + j], n0 += v[r] * v[r];
+        n0 = std::sqrt(n0);
+        for (int i = 0; i < j; ++i) {
+            double dot = 0.0;
+            for (int r = 0; r < k; ++r) dot += Q[(size_t)i * k + r] * v[r];
+            R[i * m + j] = dot;
+            for (int r = 0; r < k; ++r) v[r] -= dot * Q[(size_t)i * k + r];
+        }
+        double nv = 0.0;
+        for (int r = 0; r < k; ++r) nv += v[r] * v[r];
+        nv = std::sqrt(nv);
+        if (nv > 0.0 && nv > 1e-12 * std::max(n0, 1e-300)) {
+            R[j * m + j] = nv;
+            for (int r = 0; r < k; ++r) Q[(size_t)j * k + r] = v[r] / nv;
+        }
+    }
+}
+
+// Sorts the (column, block) pairs of one row by column.
+void sort_row(std::vector<int32_t> &cols, std::vector<double> &vals, int bs) {
+    std::vector<int> idx(cols.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return cols[a] < cols[b]; });
+    std::vector<int32_t> c2(cols.size());
+    std::vector<double> v2(vals.size());
+    for (size_t i = 0; i < idx.size(); ++i) {
+        c2[i] = cols[idx[i]];
+        std::memcpy(&v2[i * bs], &vals[(size_t)idx[i] * bs], bs * sizeof(double));
+    }
+    cols.swap(c2);
+    vals.swap(v2);
+}
+
+// C = A B for block CSR (A: ra x ca blocks, B: ca x cb blocks); columns sorted.
+BlockCsr spgemm(const BlockCsr &A, const BlockCsr &B, int64_t n_cols) {
+    BlockCsr C;
+    C.n = A.n, C.rd = A.rd, C.cd = B.cd;
+    C.ptr.assign((size_t)A.n + 1, 0);
+    const int ra = A.rd, ca = A.cd, cb = B.cd, bs = ra * cb;
+    std::vector<int64_t> slot((size_t)n_cols, -1);
+    std::vector<int32_t> cols;
+    std::vector<double> vals;
+    for (int64_t i = 0; i < A.n; ++i) {
+        cols.clear(), vals.clear();
+        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
+            const int64_t j = A.col[s];
+            const double *a = &A.val[(size_t)s * ra * ca];
+            for (int64_t t = B.ptr[j]; t < B.ptr[j + 1]; ++t) {
+                const int32_t c = B.col[t];
+                const double *b = &B.val[(size_t)t * ca * cb];
+                if (slot[c] < 0) {
+                    slot[c] = (int64_t)cols.size();
+                    cols.push_back(c);
+                    vals.resize(vals.size() + bs, 0.0);
+                }
+                double *o = &vals[(size_t)slot[c] * bs];
+                for (int x = 0; x < ra; ++x)
+                    for (int z = 0; z < cb; ++z) {
+                        double acc = 0.0;
+                        for (int y = 0; y < ca; ++y) acc += a[x * ca + y] * b[y * cb + z];
+                        o[x * cb + z] += acc;
+                    }
+            }
+        }
+        for (int32_t c : cols) slot[c] = -1;
+        sort_row(cols, vals, bs);
+        C.col.insert(C.col.end(), cols.begin(), cols.end());
+        C.val.insert(C.val.end(), vals.begin(), vals.end());
+        C.ptr[i + 1] = (int64_t)C.col.size();
+    }
+    return C;
+}
+
+// Block transpose: (n x n_cols blocks of rd x cd) -> (n_cols x n blocks of cd x rd)
+BlockCsr transpose(const BlockCsr &A, int64_t n_cols) {
+    BlockCsr T;
+    T.n = n_cols, T.rd = A.cd, T.cd = A.rd;
+    T.ptr.assign((size_t)n_cols + 1, 0);
+    for (int32_t c : A.col) ++T.ptr[(size_t)c + 1];
+    for (int64_t i = 0; i < n_cols; ++i) T.ptr[i + 1] += T.ptr[i];
+    T.col.resize(A.col.size());
+    T.val.resize(A.val.size());
+    std::vector<int64_t> fill(T.ptr.begin(), T.ptr.end() - 1);
+    const int bs = A.rd * A.cd;
+    for (int64_t i = 0; i < A.n; ++i)
+        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
+            const int64_t o = fill[A.col[s]]++;
+            T.col[o] = (int32_t)i;
+            for (int x = 0; x < A.rd; ++x)
+                for (int z = 0; z < A.cd; ++z) T.val[(size_t)o * bs + z * A.rd + x] = A.val[(size_t)s * bs + x * A.cd + z];
+        }
+    return T;
+}
+
+}  // namespace
+}  // namespace fe
+
+struct fe_amg_s {
+    std::vector<fe::AmgLevel> levels;
+    fe::BlockCsr coarse;
+};
+
+using namespace fe;
+
+extern "C" {
+
+int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
+                      const double *vals, int32_t m, const double *nullspace, double theta, int64_t coarse_dofs,
+                      fe_amg *out) {
+    if (!out || n_nodes < 0 || d < 1 || d > 6 || m < 1 || m > 6 || (n_nodes > 0 && (!blk_ptr || !blk_col ||
+                                                                                     !vals || !nullspace))) {
+        set_error("fe_amg_build_host: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    *out = nullptr;
+    fe_amg_s *h = new fe_amg_s();
+    BlockCsr A;
+    A.n = n_nodes, A.rd = A.cd = d;
+    A.ptr.assign(blk_ptr, blk_ptr + n_nodes + 1);
+    A.col.assign(blk_col, blk_col + A.ptr[n_nodes]);
+    A.val.assign(vals, vals + (size_t)A.ptr[n_nodes] * d * d);
+    std::vector<double> B(nullspace, nullspace + (size_t)n_nodes * d * m);
+    int bm = m;
+    while (A.n * A.rd > coarse_dofs && h->levels.size() < 12) {
+        AmgLevel L;
+        const int dd = A.rd;
+        std::vector<double> dinv = block_diag_pinv(A);
+        L.lmax = lmax_power(A, dinv);
+        int32_t na = 0;
+        L.agg = aggregate(A, theta, &na);
+        // tentative prolongator and coarse near-null space
+        BlockCsr Pt;
+        Pt.n = A.n, Pt.rd = dd, Pt.cd = bm;
+        Pt.ptr.resize((size_t)A.n + 1);
+        Pt.col.resize((size_t)A.n);
+        Pt.val.assign((size_t)A.n * dd * bm, 0.0);
+        for (int64_t i = 0; i <= A.n; ++i) Pt.ptr[i] = i;
+        std::vector<double> Bc((size_t)na * bm * bm, 0.0);
+        std::vector<std::vector<int64_t>> members((size_t)na);
+        for (int64_t i = 0; i < A.n; ++i) members[L.agg[i]].push_back(i);
+        std::vector<double> X, Q;
+        for (int32_t a = 0; a < na; ++a) {
+            const auto &nodes = members[a];
+            const int k = (int)nodes.size() * dd;
+            X.assign((size_t)k * bm, 0.0);
+            for (size_t t = 0; t < nodes.size(); ++t)
+                for (int c = 0; c < dd; ++c)
+                    for (int j = 0; j < bm; ++j)
+                        X[(t * dd + c) * bm + j] = B[((size_t)nodes[t] * dd + c) * bm + j];
+            double R[36];
+            qr_mgs(X, k, bm, Q, R);
+            for (size_t t = 0; t < nodes.size(); ++t) {
+                const int64_t i = nodes[t];
+                Pt.col[i] = a;
+                for (int c = 0; c < dd; ++c)
+                    for (int j = 0; j < bm; ++j)
+                        Pt.val[((size_t)i * dd + c) * bm + j] = Q[(size_t)j * k + t * dd + c];
+            }
+            for (int r = 0; r < bm * bm; ++r) Bc[(size_t)a * bm * bm + r] = R[r];
+        }
+        // smoothed prolongator P = P_tent - w D^-1 (A P_tent)
+        BlockCsr AP = spgemm(A, Pt, na);
+        const double w = 4.0 / (3.0 * L.lmax);
+        BlockCsr P = AP;
+        const int bs = dd * bm;
+        for (int64_t i = 0; i < A.n; ++i)
+            for (int64_t s = P.ptr[i]; s < P.ptr[i + 1]; ++s) {
+                double t[36];
+                const double *di = &dinv[(size_t)i * dd * dd];
+                for (int x = 0; x < dd; ++x)
+                    for (int z = 0; z < bm; ++z) {
+                        double acc = 0.0;
+                        for (int y = 0; y < dd; ++y) acc += di[x * dd + y] * AP.val[(size_t)s * bs + y * bm + z];
+                        t[x * bm + z] = -w * acc;
+                    }
+                if (P.col[s] == Pt.col[i])
+                    for (int r = 0; r < bs; ++r) t[r] += Pt.val[(size_t)i * bs + r];
+                for (int r = 0; r < bs; ++r) P.val[(size_t)s * bs + r] = t[r];
+            }
+        // Galerkin coarse operator P^T (A P)
+        BlockCsr APs = spgemm(A, P, na);
+        BlockCsr PT = transpose(P, na);
+        BlockCsr Ac = spgemm(PT, APs, na);
+        L.A = std::move(A);
+        L.P = std::move(P);
+        h->levels.push_back(std::move(L));
+        A = std::move(Ac);
+        B.swap(Bc);
+        (void)bm;
+    }
+    h->coarse = std::move(A);
+    *out = h;
+    return FE_OK;
+}
+
+int fe_amg_levels(fe_amg h, int32_t *n_levels) {
+    if (!h || !n_levels) {
+        set_error("fe_amg_levels: null argument");
+        return FE_BAD_INPUT;
+    }
+    *n_levels = (int32_t)h->levels.size();
+    return FE_OK;
+}
+
+// Level l < n_levels: its matrix and prolongator; l == n_levels: the coarsest matrix
+// (no prolongator: nnzb_P = 0, n_coarse = 0).
+int fe_amg_level_info(fe_amg h, int32_t l, int64_t *n_nodes, int32_t *d, int64_t *nnzb_A, int64_t *nnzb_P,
+                      int64_t *n_coarse, int32_t *m, double *lmax) {
+    if (!h || l < 0 || l > (int32_t)h->levels.size()) {
+        set_error("fe_amg_level_info: bad level");
+        return FE_BAD_INPUT;
+    }
+    const bool last = l == (int32_t)h->levels.size();
+    const BlockCsr &A = last ? h->coarse : h->levels[l].A;
+    if (n_nodes) *n_nodes = A.n;
+    if (d) *d = A.rd;
+    if (nnzb_A) *nnzb_A = A.nnzb();
+    if (nnzb_P) *nnzb_P = last ? 0 : h->levels[l].P.nnzb();
+    if (n_coarse) *n_coarse = last ? 0 : (l + 1 < (int32_t)h->levels.size() ? h->levels[l + 1].A.n : h->coarse.n);
+    if (m) *m = last ? 0 : h->levels[l].P.cd;
+    if (lmax) *lmax = last ? 0.0 : h->levels[l].lmax;
+    return FE_OK;
+}
+
+int fe_amg_level_matrix(fe_amg h, int32_t l, int32_t which, int64_t *ptr, int32_t *col, double *val) {
+    if (!h || l < 0 || l > (int32_t)h->levels.size() || (which == 1 && l == (int32_t)h->levels.size())) {
+        set_error("fe_amg_level_matrix: bad level");
+        return FE_BAD_INPUT;
+    }
+    const BlockCsr &M = which == 1 ? h->levels[l].P : (l == (int32_t)h->levels.size() ? h->coarse : h->levels[l].A);
+    if (ptr) std::copy(M.ptr.begin(), M.ptr.end(), ptr);
+    if (col) std::copy(M.col.begin(), M.col.end(), col);
+    if (val) std::copy(M.val.begin(), M.val.end(), val);
+    return FE_OK;
+}
+
+int fe_amg_level_aggregates(fe_amg h, int32_t l, int32_t *agg) {
+    if (!h || !agg || l < 0 || l >= (int32_t)h->levels.size()) {
+        set_error("fe_amg_level_aggregates: bad level");
+        return FE_BAD_INPUT;
+    }
+    std::copy(h->levels[l].agg.begin(), h->levels[l].agg.end(), agg);
+    return FE_OK;
+}
+
+int fe_amg_destroy(fe_amg h) {
+    delete h;
+    return FE_OK;
+}
+
+}  // extern "C"

@@ -267,6 +267,26 @@ int fe_post_magnetic(fe_handle h, const double *a_host, double *field_host);
  * hidden width 64, BF16 tensor-core GEMMs with FP32 accumulation) predicts the shape
  * u_hat of the displacement; x0 = g + s u_hat with s the A-norm optimal scale.
  * Elasticity meshes only. */
+/* ---- smoothed-aggregation multigrid setup on the host (no counterpart in the
+ * reference, which factorises directly; the setup stage of a multilevel preconditioner
+ * for the device solve).  Input: the node-block CSR of a symmetric system matrix
+ * (n_nodes block rows of d x d blocks, blk_ptr[n_nodes+1], blk_col, vals row-major
+ * blocks) and a near-null space (n_nodes*d x m, row-major: the rigid-body modes for
+ * elasticity).  Levels down to at most coarse_dofs DOFs (or 12).  Level l < n_levels
+ * has its matrix (which = 0, d_l x d_l blocks) and its prolongator (which = 1, d_l x m
+ * blocks, columns = aggregates); level n_levels is the coarsest matrix. */
+typedef struct fe_amg_s *fe_amg;
+int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
+                      const double *vals, int32_t m, const double *nullspace, double theta,
+                      int64_t coarse_dofs, fe_amg *out);
+int fe_amg_levels(fe_amg a, int32_t *n_levels);
+int fe_amg_level_info(fe_amg a, int32_t level, int64_t *n_nodes, int32_t *d, int64_t *nnzb_A,
+                      int64_t *nnzb_P, int64_t *n_coarse, int32_t *m, double *lmax);
+int fe_amg_level_matrix(fe_amg a, int32_t level, int32_t which, int64_t *ptr_host, int32_t *col_host,
+                        double *val_host);
+int fe_amg_level_aggregates(fe_amg a, int32_t level, int32_t *agg_host);
+int fe_amg_destroy(fe_amg a);
+
 typedef struct fe_gnn_s *fe_gnn;
 int fe_gnn_create(fe_gnn *out);
 int fe_gnn_destroy(fe_gnn g);

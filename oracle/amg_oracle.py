@@ -41,9 +41,14 @@ def block_diag_inv(A, d):
     return sp.csr_matrix((Di.reshape(-1), (rows, cols)), shape=A.shape)
 
 
-def lmax_power(A, Minv, it=30, seed=0):
+def power_start(n):
+    """Deterministic start vector of the power iterations: 1 + (i mod 7) / 7."""
+    return 1.0 + (np.arange(n) % 7) / 7.0
+
+
+def lmax_power(A, Minv, it=30):
     """Largest eigenvalue of Minv A by power iteration (Rayleigh quotient)."""
-    x = np.random.default_rng(seed).standard_normal(A.shape[0])
+    x = power_start(A.shape[0])
     for _ in range(it):
         x = Minv @ (A @ x)
         x /= np.linalg.norm(x)
@@ -101,6 +106,26 @@ def aggregate(A, d, theta=0.08):
     return agg, na
 
 
+def qr_positive(X, tol=1e-12):
+    """Thin QR by modified Gram-Schmidt with a non-negative diagonal of R; a column
+    whose remainder is below tol times its norm gives a zero column of Q and a zero
+    row of R (rank-deficient aggregates keep the block size)."""
+    k, m = X.shape
+    Q = np.zeros((k, m))
+    R = np.zeros((m, m))
+    for j in range(m):
+        v = X[:, j].astype(np.float64).copy()
+        nrm0 = np.sqrt(v @ v)
+        for i in range(j):
+            R[i, j] = Q[:, i] @ v
+            v -= R[i, j] * Q[:, i]
+        nrm = np.sqrt(v @ v)
+        if nrm > tol * max(nrm0, 1e-300) and nrm > 0:
+            R[j, j] = nrm
+            Q[:, j] = v / nrm
+    return Q, R
+
+
 def tentative(agg, na, B, d):
     """P_tent (n d x na m) and the coarse near-null space (na m x m)."""
     m = B.shape[1]
@@ -111,7 +136,7 @@ def tentative(agg, na, B, d):
     for a in range(na):
         nodes = order[starts[a]:starts[a + 1]]
         dofs = (nodes[:, None] * d + np.arange(d)[None, :]).reshape(-1)
-        Q, Rr = np.linalg.qr(B[dofs], mode="reduced")
+        Q, Rr = qr_positive(B[dofs])
         if Q.shape[1] < m:
             Q = np.hstack([Q, np.zeros((Q.shape[0], m - Q.shape[1]))])
             Rr = np.vstack([Rr, np.zeros((m - Rr.shape[0], m))])
