@@ -19,12 +19,39 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "fe_internal.h"
 
 namespace fe {
 namespace {
+
+// Work split into a fixed number of chunks (independent of the thread count, so that
+// chunked sums and concatenations are the same on every machine), run on up to
+// hardware_concurrency threads.
+constexpr int kChunks = 64;
+
+template <typename F>
+void parallel_chunks(int64_t n, F f) {
+    const int nt = std::max(1, std::min<int>(kChunks, (int)std::thread::hardware_concurrency()));
+    auto run = [&](int t) {
+        for (int c = t; c < kChunks; c += nt) {
+            const int64_t lo = n * c / kChunks, hi = n * (c + 1) / kChunks;
+            f(lo, hi, c);
+        }
+    };
+    if (nt == 1 || n < 4096) {
+        run(0);
+        if (nt > 1)
+            for (int t = 1; t < nt; ++t) run(t);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(run, t);
+    run(0);
+    for (auto &x : th) x.join();
+}
 
 struct BlockCsr {
     int64_t n = 0;             // block rows
@@ -92,58 +119,70 @@ void sym_pinv(const double *a, int d, double *out) {
 std::vector<double> block_diag_pinv(const BlockCsr &A) {
     const int d = A.rd;
     std::vector<double> dinv((size_t)A.n * d * d, 0.0);
-    for (int64_t i = 0; i < A.n; ++i)
-        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s)
-            if (A.col[s] == i) sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
+    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
+            for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s)
+                if (A.col[s] == i) sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
+    });
     return dinv;
 }
 
-// y = A x (d x d blocks)
-void spmv(const BlockCsr &A, const std::vector<double> &x, std::vector<double> &y) {
-    const int d = A.rd;
-    y.assign((size_t)A.n * d, 0.0);
-    for (int64_t i = 0; i < A.n; ++i)
+// y_i = D_i^-1 (A x)_i for the rows of one chunk (D block rows of size D; DD the
+// compile-time block size when known, else 0)
+template <int DD>
+void dinv_spmv_rows(const BlockCsr &A, const std::vector<double> &dinv, const double *x, double *y, int64_t lo,
+                    int64_t hi) {
+    const int d = DD > 0 ? DD : A.rd;
+    double acc[6], t[6];
+    for (int64_t i = lo; i < hi; ++i) {
+        for (int a = 0; a < d; ++a) acc[a] = 0.0;
         for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
             const double *b = &A.val[(size_t)s * d * d];
-            const int64_t c = A.col[s];
-            for (int a = 0; a < d; ++a) {
-                double acc = 0.0;
-                for (int k = 0; k < d; ++k) acc += b[a * d + k] * x[(size_t)c * d + k];
-                y[(size_t)i * d + a] += acc;
-            }
+            const double *xc = x + (size_t)A.col[s] * d;
+            for (int a = 0; a < d; ++a)
+                for (int k = 0; k < d; ++k) acc[a] += b[a * d + k] * xc[k];
         }
-}
-
-void apply_dinv(const std::vector<double> &dinv, int d, std::vector<double> &v) {
-    const int64_t n = (int64_t)v.size() / d;
-    double t[6];
-    for (int64_t i = 0; i < n; ++i) {
+        const double *di = &dinv[(size_t)i * d * d];
         for (int a = 0; a < d; ++a) {
-            double acc = 0.0;
-            for (int k = 0; k < d; ++k) acc += dinv[(size_t)i * d * d + a * d + k] * v[(size_t)i * d + k];
-            t[a] = acc;
+            double v = 0.0;
+            for (int k = 0; k < d; ++k) v += di[a * d + k] * acc[k];
+            t[a] = v;
         }
-        for (int a = 0; a < d; ++a) v[(size_t)i * d + a] = t[a];
+        for (int a = 0; a < d; ++a) y[(size_t)i * d + a] = t[a];
     }
 }
 
+// Largest eigenvalue of D^-1 A: 30 power iterations from x_i = 1 + (i mod 7) / 7, then
+// the Rayleigh quotient; sums are taken per chunk and added in chunk order.
 double lmax_power(const BlockCsr &A, const std::vector<double> &dinv) {
     const int d = A.rd;
     const int64_t nd = A.n * d;
-    std::vector<double> x((size_t)nd), y;
+    std::vector<double> x((size_t)nd), y((size_t)nd);
     for (int64_t i = 0; i < nd; ++i) x[i] = 1.0 + (double)(i % 7) / 7.0;
+    double part[kChunks], part2[kChunks];
+    auto step = [&]() {
+        parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int c) {
+            if (d == 2) dinv_spmv_rows<2>(A, dinv, x.data(), y.data(), lo, hi);
+            else if (d == 3) dinv_spmv_rows<3>(A, dinv, x.data(), y.data(), lo, hi);
+            else dinv_spmv_rows<0>(A, dinv, x.data(), y.data(), lo, hi);
+            double a = 0.0, b = 0.0;
+            for (int64_t k = lo * d; k < hi * d; ++k) a += y[k] * y[k], b += x[k] * y[k];
+            part[c] = a, part2[c] = b;
+        });
+    };
     for (int it = 0; it < 30; ++it) {
-        spmv(A, x, y);
-        apply_dinv(dinv, d, y);
+        step();
         double nrm = 0.0;
-        for (double v : y) nrm += v * v;
+        for (int c = 0; c < kChunks; ++c) nrm += part[c];
         nrm = std::sqrt(nrm);
-        for (int64_t i = 0; i < nd; ++i) x[i] = y[i] / nrm;
+        parallel_chunks(nd, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t k = lo; k < hi; ++k) x[k] = y[k] / nrm;
+        });
     }
-    spmv(A, x, y);
-    apply_dinv(dinv, d, y);
+    step();
     double num = 0.0, den = 0.0;
-    for (int64_t i = 0; i < nd; ++i) num += x[i] * y[i], den += x[i] * x[i];
+    for (int c = 0; c < kChunks; ++c) num += part2[c];
+    for (int64_t i = 0; i < nd; ++i) den += x[i] * x[i];
     return num / den;
 }
 
@@ -216,57 +255,68 @@ void qr_mgs(const std::vector<double> &X, int k, int m, std::vector<double> &Q, 
     }
 }
 
-// Sorts the (column, block) pairs of one row by column.
-void sort_row(std::vector<int32_t> &cols, std::vector<double> &vals, int bs) {
-    std::vector<int> idx(cols.size());
-    for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return cols[a] < cols[b]; });
-    std::vector<int32_t> c2(cols.size());
-    std::vector<double> v2(vals.size());
-    for (size_t i = 0; i < idx.size(); ++i) {
-        c2[i] = cols[idx[i]];
-        std::memcpy(&v2[i * bs], &vals[(size_t)idx[i] * bs], bs * sizeof(double));
-    }
-    cols.swap(c2);
-    vals.swap(v2);
-}
-
-// C = A B for block CSR (A: ra x ca blocks, B: ca x cb blocks); columns sorted.
+// C = A B for block CSR (A: ra x ca blocks, B: ca x cb blocks); columns sorted.  Rows
+// are computed per chunk into chunk-local buffers, then concatenated in order.
 BlockCsr spgemm(const BlockCsr &A, const BlockCsr &B, int64_t n_cols) {
     BlockCsr C;
     C.n = A.n, C.rd = A.rd, C.cd = B.cd;
     C.ptr.assign((size_t)A.n + 1, 0);
     const int ra = A.rd, ca = A.cd, cb = B.cd, bs = ra * cb;
-    std::vector<int64_t> slot((size_t)n_cols, -1);
-    std::vector<int32_t> cols;
-    std::vector<double> vals;
-    for (int64_t i = 0; i < A.n; ++i) {
-        cols.clear(), vals.clear();
-        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
-            const int64_t j = A.col[s];
-            const double *a = &A.val[(size_t)s * ra * ca];
-            for (int64_t t = B.ptr[j]; t < B.ptr[j + 1]; ++t) {
-                const int32_t c = B.col[t];
-                const double *b = &B.val[(size_t)t * ca * cb];
-                if (slot[c] < 0) {
-                    slot[c] = (int64_t)cols.size();
-                    cols.push_back(c);
-                    vals.resize(vals.size() + bs, 0.0);
-                }
-                double *o = &vals[(size_t)slot[c] * bs];
-                for (int x = 0; x < ra; ++x)
-                    for (int z = 0; z < cb; ++z) {
-                        double acc = 0.0;
-                        for (int y = 0; y < ca; ++y) acc += a[x * ca + y] * b[y * cb + z];
-                        o[x * cb + z] += acc;
+    struct Part {
+        std::vector<int32_t> col;
+        std::vector<double> val;
+        std::vector<int64_t> len;
+    };
+    std::vector<Part> parts(kChunks);
+    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int c) {
+        Part &pt = parts[c];
+        std::vector<int64_t> slot((size_t)n_cols, -1);
+        std::vector<int32_t> cols;
+        std::vector<double> vals;
+        std::vector<int> order;
+        for (int64_t i = lo; i < hi; ++i) {
+            cols.clear(), vals.clear();
+            for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
+                const int64_t j = A.col[s];
+                const double *a = &A.val[(size_t)s * ra * ca];
+                for (int64_t t = B.ptr[j]; t < B.ptr[j + 1]; ++t) {
+                    const int32_t cc = B.col[t];
+                    const double *b = &B.val[(size_t)t * ca * cb];
+                    if (slot[cc] < 0) {
+                        slot[cc] = (int64_t)cols.size();
+                        cols.push_back(cc);
+                        vals.resize(vals.size() + bs, 0.0);
                     }
+                    double *o = &vals[(size_t)slot[cc] * bs];
+                    for (int x = 0; x < ra; ++x)
+                        for (int z = 0; z < cb; ++z) {
+                            double acc = 0.0;
+                            for (int y = 0; y < ca; ++y) acc += a[x * ca + y] * b[y * cb + z];
+                            o[x * cb + z] += acc;
+                        }
+                }
             }
+            order.resize(cols.size());
+            for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
+            for (size_t k = 1; k < order.size(); ++k) {   // insertion sort: rows are short
+                const int v = order[k];
+                size_t m = k;
+                while (m > 0 && cols[order[m - 1]] > cols[v]) order[m] = order[m - 1], --m;
+                order[m] = v;
+            }
+            for (int k : order) {
+                pt.col.push_back(cols[k]);
+                pt.val.insert(pt.val.end(), vals.begin() + (size_t)k * bs, vals.begin() + (size_t)(k + 1) * bs);
+                slot[cols[k]] = -1;
+            }
+            pt.len.push_back((int64_t)cols.size());
         }
-        for (int32_t c : cols) slot[c] = -1;
-        sort_row(cols, vals, bs);
-        C.col.insert(C.col.end(), cols.begin(), cols.end());
-        C.val.insert(C.val.end(), vals.begin(), vals.end());
-        C.ptr[i + 1] = (int64_t)C.col.size();
+    });
+    int64_t row = 0;
+    for (int c = 0; c < kChunks; ++c) {
+        for (int64_t l : parts[c].len) C.ptr[row + 1] = C.ptr[row] + l, ++row;
+        C.col.insert(C.col.end(), parts[c].col.begin(), parts[c].col.end());
+        C.val.insert(C.val.end(), parts[c].val.begin(), parts[c].val.end());
     }
     return C;
 }
@@ -363,7 +413,8 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
         const double w = 4.0 / (3.0 * L.lmax);
         BlockCsr P = AP;
         const int bs = dd * bm;
-        for (int64_t i = 0; i < A.n; ++i)
+        parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
             for (int64_t s = P.ptr[i]; s < P.ptr[i + 1]; ++s) {
                 double t[36];
                 const double *di = &dinv[(size_t)i * dd * dd];
@@ -377,6 +428,7 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
                     for (int r = 0; r < bs; ++r) t[r] += Pt.val[(size_t)i * bs + r];
                 for (int r = 0; r < bs; ++r) P.val[(size_t)s * bs + r] = t[r];
             }
+        });
         // Galerkin coarse operator P^T (A P)
         BlockCsr APs = spgemm(A, P, na);
         BlockCsr PT = transpose(P, na);
