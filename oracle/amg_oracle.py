@@ -193,6 +193,20 @@ def rigid_modes_2d(xy):
     return B
 
 
+def rigid_modes_3d(xyz):
+    """The six rigid-body modes of 3D elasticity at the nodes xyz (n, 3), node-major:
+    three translations and the rotations about z, x and y."""
+    n = xyz.shape[0]
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    B = np.zeros((3 * n, 6))
+    for k in range(3):
+        B[k::3, k] = 1.0
+    B[0::3, 3], B[1::3, 3] = -y, x
+    B[1::3, 4], B[2::3, 4] = -z, y
+    B[0::3, 5], B[2::3, 5] = z, -x
+    return B
+
+
 def pcg(A, b, M, tol=1e-8, maxit=20000):
     """PCG from x = 0 to ||r|| <= tol ||b||: (x, iterations)."""
     x = np.zeros_like(b)

@@ -109,3 +109,39 @@ def test_pcg_with_the_library_hierarchy():
     x, it = AMG.pcg(A, b, model)
     assert abs(it - it_model) <= 1, (it, it_model)
     assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b)
+
+
+def _check_against_model(A, B, d):
+    ours = build(A, B, d)
+    model = AMG.SmoothedAggregation(A, B, d=d)
+    assert len(ours) == len(model.levels) + 1
+    dd = d
+    for l, (Aref, Minv, lm, P) in enumerate(model.levels):
+        agg, na = AMG.aggregate(Aref, dd)
+        np.testing.assert_array_equal(ours[l]["agg"], agg)
+        assert abs(ours[l]["lmax"] - lm) <= 1e-10 * lm
+        assert abs(ours[l]["P"] - P).max() <= 1e-10 * abs(P).max()
+        dd = B.shape[1]
+    Ac = model.levels[-1][3].T @ model.levels[-1][0] @ model.levels[-1][3]
+    assert abs(ours[-1]["A"] - Ac).max() <= 1e-10 * abs(Ac).max()
+    return model
+
+
+def test_tetrahedra_with_six_rigid_modes():
+    prob = meshgen.cantilever_3d(12, 4, 4, jitter=0.2, seed=3)
+    A, b, free, *_ = O.reduced_system(prob)
+    A = A.tocsr()
+    B = AMG.rigid_modes_3d(prob.coords[free[0::3] // 3])
+    model = _check_against_model(A, B, 3)
+    x, it = AMG.pcg(A, b, model)
+    assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b) and it <= 40, it
+
+
+def test_magnetostatics_with_the_constant_mode():
+    prob = meshgen.magnetostatic(60, 30, seed=1)
+    A, b, free, *_ = O.reduced_system(prob)
+    A = A.tocsr()
+    B = np.ones((A.shape[0], 1))
+    model = _check_against_model(A, B, 1)
+    x, it = AMG.pcg(A, b, model)
+    assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b) and it <= 40, it
