@@ -22,6 +22,7 @@
 #include <thread>
 #include <vector>
 
+#include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
 namespace fe {
@@ -65,6 +66,8 @@ struct BlockCsr {
 struct AmgLevel {
     BlockCsr A;                 // d x d blocks
     BlockCsr P;                 // d x m blocks, columns = aggregates
+    BlockCsr PT;                // m x d blocks: the restriction
+    std::vector<double> dinv;   // block-diagonal pseudo-inverse of A
     std::vector<int32_t> agg;   // aggregate of each node
     double lmax = 0.0;
 };
@@ -342,13 +345,102 @@ BlockCsr transpose(const BlockCsr &A, int64_t n_cols) {
     return T;
 }
 
+// Dense inverse of a small matrix (row-major, n x n) by Gauss-Jordan with partial
+// pivoting; false when a pivot vanishes.
+bool dense_inverse(std::vector<double> a, int n, std::vector<double> &inv) {
+    inv.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(a[(size_t)r * n + c]) > std::fabs(a[(size_t)p * n + c])) p = r;
+        if (a[(size_t)p * n + c] == 0.0) return false;
+        if (p != c)
+            for (int k = 0; k < n; ++k) {
+                std::swap(a[(size_t)p * n + k], a[(size_t)c * n + k]);
+                std::swap(inv[(size_t)p * n + k], inv[(size_t)c * n + k]);
+            }
+        const double piv = a[(size_t)c * n + c];
+        for (int k = 0; k < n; ++k) a[(size_t)c * n + k] /= piv, inv[(size_t)c * n + k] /= piv;
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = a[(size_t)r * n + c];
+            if (f == 0.0) continue;
+            for (int k = 0; k < n; ++k) {
+                a[(size_t)r * n + k] -= f * a[(size_t)c * n + k];
+                inv[(size_t)r * n + k] -= f * inv[(size_t)c * n + k];
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace
 }  // namespace fe
 
 struct fe_amg_s {
     std::vector<fe::AmgLevel> levels;
     fe::BlockCsr coarse;
+    std::vector<double> coarse_inv;   // dense inverse of the coarsest matrix + 1e-12 max|diag| I
 };
+
+namespace fe {
+namespace {
+
+// k Chebyshev steps on D^-1 A z = D^-1 r over [1.05 lmax / 30, 1.05 lmax], from x0 (or
+// zero): z_1 = x0 + D^-1 (r - A x0) / theta, then the three-term updates.
+void chebyshev_host(const AmgLevel &L, int k, const std::vector<double> &r, std::vector<double> &z, bool from_x0) {
+    const BlockCsr &A = L.A;
+    const int d = A.rd;
+    const int64_t n = A.n;
+    const double hi = 1.05 * L.lmax, lo = hi / 30.0;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    if (!from_x0) z.assign((size_t)n * d, 0.0);
+    std::vector<double> dir((size_t)n * d, 0.0), zn((size_t)n * d);
+    double rho = 1.0 / sigma;
+    for (int64_t i = 0; i < n; ++i)
+        amg::row_chebyshev(A.ptr.data(), A.col.data(), A.val.data(), L.dinv.data(), d, r.data(), z.data(),
+                           dir.data(), zn.data(), 0.0, 1.0 / theta, true, i);
+    z.swap(zn);
+    for (int s = 1; s < k; ++s) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        const double a = rn * rho, b = 2.0 * rn / delta;
+        rho = rn;
+        for (int64_t i = 0; i < n; ++i)
+            amg::row_chebyshev(A.ptr.data(), A.col.data(), A.val.data(), L.dinv.data(), d, r.data(), z.data(),
+                               dir.data(), zn.data(), a, b, false, i);
+        z.swap(zn);
+    }
+}
+
+void vcycle_host(const fe_amg_s *h, size_t l, int k, const std::vector<double> &r, std::vector<double> &x) {
+    if (l == h->levels.size()) {
+        const int64_t n = (int64_t)r.size();
+        x.assign((size_t)n, 0.0);
+        for (int64_t i = 0; i < n; ++i) {
+            double acc = 0.0;
+            for (int64_t j = 0; j < n; ++j) acc += h->coarse_inv[(size_t)i * n + j] * r[j];
+            x[i] = acc;
+        }
+        return;
+    }
+    const AmgLevel &L = h->levels[l];
+    const BlockCsr &A = L.A;
+    const int d = A.rd, m = L.P.cd;
+    chebyshev_host(L, k, r, x, false);
+    std::vector<double> t((size_t)A.n * d), rc((size_t)L.PT.n * m), xc;
+    for (int64_t i = 0; i < A.n; ++i)
+        amg::row_residual(A.ptr.data(), A.col.data(), A.val.data(), d, r.data(), x.data(), t.data(), i);
+    for (int64_t I = 0; I < L.PT.n; ++I)
+        amg::row_restrict(L.PT.ptr.data(), L.PT.col.data(), L.PT.val.data(), m, d, t.data(), rc.data(), I);
+    vcycle_host(h, l + 1, k, rc, xc);
+    for (int64_t i = 0; i < A.n; ++i)
+        amg::row_prolong_add(L.P.ptr.data(), L.P.col.data(), L.P.val.data(), d, m, xc.data(), x.data(), i);
+    chebyshev_host(L, k, r, x, true);
+}
+
+}  // namespace
+}  // namespace fe
 
 using namespace fe;
 
@@ -435,13 +527,57 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
         BlockCsr Ac = spgemm(PT, APs, na);
         L.A = std::move(A);
         L.P = std::move(P);
+        L.PT = std::move(PT);
+        L.dinv = std::move(dinv);
         h->levels.push_back(std::move(L));
         A = std::move(Ac);
         B.swap(Bc);
         (void)bm;
     }
     h->coarse = std::move(A);
+    {
+        // dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal
+        // entry (zero rows of rank-deficient aggregates)
+        const BlockCsr &C = h->coarse;
+        const int64_t n = C.n * C.rd;
+        if (n > 4096) {
+            fe_amg_destroy(h);
+            set_error("fe_amg_build_host: coarsest level too large for its dense solve");
+            return FE_BAD_INPUT;
+        }
+        std::vector<double> dense((size_t)n * n, 0.0);
+        double dmax = 0.0;
+        const int cd = C.rd;
+        for (int64_t i = 0; i < C.n; ++i)
+            for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
+                for (int a = 0; a < cd; ++a)
+                    for (int b = 0; b < cd; ++b) {
+                        const double v = C.val[(size_t)s * cd * cd + a * cd + b];
+                        dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
+                    }
+        for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
+        for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
+        if (n > 0 && !dense_inverse(dense, (int)n, h->coarse_inv)) {
+            fe_amg_destroy(h);
+            set_error("fe_amg_build_host: singular coarsest matrix");
+            return FE_BREAKDOWN;
+        }
+    }
     *out = h;
+    return FE_OK;
+}
+
+// One V-cycle x = M^-1 r on the host (k Chebyshev steps before and after each coarse
+// correction), the arithmetic of the device cycle row by row.
+int fe_amg_vcycle_host(fe_amg h, int32_t k_smooth, const double *r, double *x) {
+    if (!h || !r || !x || k_smooth < 1) {
+        set_error("fe_amg_vcycle_host: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    const int64_t n = h->levels.empty() ? h->coarse.n * h->coarse.rd : h->levels[0].A.n * h->levels[0].A.rd;
+    std::vector<double> rv(r, r + n), xv;
+    vcycle_host(h, 0, k_smooth, rv, xv);
+    std::copy(xv.begin(), xv.end(), x);
     return FE_OK;
 }
 

@@ -285,6 +285,10 @@ int fe_amg_level_info(fe_amg a, int32_t level, int64_t *n_nodes, int32_t *d, int
 int fe_amg_level_matrix(fe_amg a, int32_t level, int32_t which, int64_t *ptr_host, int32_t *col_host,
                         double *val_host);
 int fe_amg_level_aggregates(fe_amg a, int32_t level, int32_t *agg_host);
+/* One V-cycle x = M^-1 r on the host with k_smooth Chebyshev steps (on D^-1 A over
+ * [1.05 lmax/30, 1.05 lmax]) before and after each coarse correction and a dense solve
+ * of the coarsest level: the arithmetic the device cycle runs row by row. */
+int fe_amg_vcycle_host(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
 int fe_amg_destroy(fe_amg a);
 
 typedef struct fe_gnn_s *fe_gnn;

@@ -145,3 +145,59 @@ def test_magnetostatics_with_the_constant_mode():
     model = _check_against_model(A, B, 1)
     x, it = AMG.pcg(A, b, model)
     assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b) and it <= 40, it
+
+
+def _library_handle(A, B, d):
+    lib = _lib.load()
+    n, ptr, col, val = to_block_csr(A, d)
+    Bc = np.ascontiguousarray(B, np.float64)
+    h = ctypes.c_void_p()
+    _lib.check(lib.fe_amg_build_host(n, d, _lib.ptr(ptr), _lib.ptr(col), _lib.ptr(val), B.shape[1], _lib.ptr(Bc),
+                                     0.08, 400, ctypes.byref(h)), "fe_amg_build_host")
+    return lib, h
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_host_vcycle_matches_the_model(case):
+    """fe_amg_vcycle_host (the row operations of the device cycle, run serially) gives
+    the model's V-cycle on the same hierarchy, and PCG preconditioned by it converges
+    in the model's iteration count."""
+    if case == "plane_strain":
+        prob = meshgen.plane_strain_random(60, 30, seed=4)
+        d, modes = 2, lambda xy: AMG.rigid_modes_2d(xy)
+    elif case == "tet":
+        prob = meshgen.cantilever_3d(10, 4, 4, jitter=0.2, seed=5)
+        d, modes = 3, lambda xy: AMG.rigid_modes_3d(xy)
+    else:
+        prob = meshgen.magnetostatic(50, 25, seed=2)
+        d, modes = 1, None
+    A, b, free, *_ = O.reduced_system(prob)
+    A = A.tocsr()
+    B = np.ones((A.shape[0], 1)) if modes is None else modes(prob.coords[free[0::d] // d])
+    lib, h = _library_handle(A, B, d)
+    ours = build(A, B, d)
+    model = AMG.SmoothedAggregation(A, B, d=d)
+    dd, levels = d, []
+    for lev in ours[:-1]:
+        levels.append((lev["A"], AMG.block_diag_inv(lev["A"], dd), lev["lmax"], lev["P"]))
+        dd = B.shape[1]
+    model.levels = levels
+    model.smooth = [AMG.chebyshev(Al, Minv, lm, 30.0, model.k) for Al, Minv, lm, _ in levels]
+    import scipy.sparse.linalg as spla
+    Ac = sp.csc_matrix(ours[-1]["A"])
+    model.lu = spla.splu(sp.csc_matrix(Ac + 1e-12 * abs(Ac.diagonal()).max() * sp.eye(Ac.shape[0])))
+    r = np.random.default_rng(0).standard_normal(A.shape[0])
+    x = np.empty_like(r)
+    _lib.check(lib.fe_amg_vcycle_host(h, 3, _lib.ptr(r), _lib.ptr(x)), "fe_amg_vcycle_host")
+    xm = model(r)
+    assert np.linalg.norm(x - xm) <= 1e-9 * np.linalg.norm(xm)
+
+    def M(v):
+        v = np.ascontiguousarray(v)
+        out = np.empty_like(v)
+        lib.fe_amg_vcycle_host(h, 3, _lib.ptr(v), _lib.ptr(out))
+        return out
+    xs, it = AMG.pcg(A, b, M)
+    _, it_model = AMG.pcg(A, b, model)
+    assert abs(it - it_model) <= 1 and np.linalg.norm(A @ xs - b) <= 1e-8 * np.linalg.norm(b)
+    lib.fe_amg_destroy(h)
