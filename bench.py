@@ -30,10 +30,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # DRAM bytes (read + write) per launch of the roofline kernel (the intermediate FP32
-# Chebyshev step with plain loads, --l2-keep 0) from one ncu capture of this workload,
-# keyed by grid (summary in profiles/cheb_step_fp32_plane_strain_4M.md); None when the
-# workload or the load policy differs.
-NCU_TRAFFIC = {(2000, 1000): 278_710_784}
+# Chebyshev step) from ncu captures of this workload, keyed by (grid, bytes of the
+# L2-resident prefix): plain loads (profiles/cheb_step_fp32_plane_strain_4M.md) and the
+# default 40 MB prefix (steady state of a run of steps,
+# profiles/cheb_step_fp32_keep_plane_strain_4M.md); None for other workloads.
+NCU_TRAFFIC = {(2000, 1000, 0): 278_710_784, (2000, 1000, 40_000_000): 265_900_000}
 
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
 UNIT = "s/solve"
@@ -62,7 +63,6 @@ def parse_args():
     ap.add_argument("--quick-plain", action="store_true",
                     help="with --quick: time the plain FP64 PCG step instead of the headline")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
-    ap.add_argument("--cpu-nx", type=int, default=200, help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--l2-keep", type=float, default=-1.0,
                     help="MB of the FP32 preconditioner matrix kept L2-resident across Chebyshev steps "
@@ -166,26 +166,26 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- CPU baseline (oracle)
 
-def cpu_reference_sample(nx, seed):
-    """The reference's path restated by the oracle -- COO triplets, scipy csr_matrix,
-    spsolve(NATURAL) on the saddle system -- timed on one plane-strain nx x nx/2
-    instance of the same family (one host core: SuperLU is single-threaded)."""
-    from finite_elements_gb300 import meshgen
+def cpu_direct_solve(prob):
+    """The reference path on the host cores at the workload's full size, measured: the
+    oracle's restatement of finite_elements' element and assembly code (vectorised over
+    elements, so faster than the reference's per-element loop), Dirichlet elimination,
+    and SuperLU -- the library of the reference's spsolve call (analysis.py:820-822) --
+    on the eliminated SPD system, ordered by minimum degree on A^T + A.  The reference's
+    own call (NATURAL order on the saddle system) does not fit in host memory at 4M DOF;
+    this is the fastest direct method scipy offers for the same system.  SuperLU runs on
+    one core.  Returns ([u, lambda], seconds, timings)."""
     from oracle import fe_oracle as O
-    prob = meshgen.plane_strain_random(nx, nx // 2, seed=seed)
+    tm = {}
     t0 = time.perf_counter()
-    O.solve(prob)
-    dt = time.perf_counter() - t0
-    return dt, prob.n_dof
+    x = O.solve_reduced(prob, "direct", timings=tm)
+    return x, time.perf_counter() - t0, tm
 
 
-def scale_to_workload(sample_s, sample_dof, full_dof):
-    """A CPU sample's seconds per solve carried to the full workload in proportion to the
-    DOF count.  This is a lower bound for the reference path: its NATURAL-order sparse LU
-    factorises a banded matrix whose bandwidth grows with the grid's side, so its time
-    grows about as DOF^2 (1.4 s -> 5.7 s from 20,022 to 40,602 DOF of this family), and
-    at 4M DOF the factor does not fit in host memory at all."""
-    return sample_s * full_dof / sample_dof
+CPU_METHOD = ("reduced-system direct: oracle assembly (COO, csr_matrix), Dirichlet elimination, SuperLU "
+              "splu on the eliminated SPD system (MMD_AT_PLUS_A order, symmetric mode) -- not the "
+              "reference's exact call, spsolve NATURAL on the saddle system, which does not fit in host "
+              "memory at this size")
 
 
 def cpu_info():
@@ -339,11 +339,14 @@ def run_ours(args, dist):
     prof_plain = profile_read(_lib.FE_PREC_FP64)
     h.call("fe_profile_kernels", 0)
 
-    # ---- FP64 oracle solution (tight tolerance) for the error of the mixed result
-    x_ref, st_ref = s.solve(precision="fp64", tol=1e-11, cheb_degree=args.plain_cheb,
-                            cheb_ratio=args.plain_cheb_ratio, accept_stagnation=True)
     n = prob.n_dof
-    err = float(np.linalg.norm(x_mixed[:n] - x_ref[:n]) / np.linalg.norm(x_ref[:n]))
+    err, err_ref = None, None
+    if dist.world > 1 or args.no_cpu_baseline:
+        # no CPU solve on this run: the error against the library's own FP64 PCG to 1e-11
+        x_ref, _ = s.solve(precision="fp64", tol=1e-11, cheb_degree=args.plain_cheb,
+                           cheb_ratio=args.plain_cheb_ratio, accept_stagnation=True)
+        err = float(np.linalg.norm(x_mixed[:n] - x_ref[:n]) / np.linalg.norm(x_ref[:n]))
+        err_ref = "the library's FP64 PCG to 1e-11 on the GPU (no CPU solve on this run)"
 
     # ---- roofline.  Algorithmic bytes per launch (2x2 node blocks, s = value size):
     # off-diagonal blocks (4 s value bytes + 4 column bytes each, 2 for the FP32 kernels'
@@ -378,9 +381,8 @@ def run_ours(args, dist):
     spmvmp_gbs, spmvmp_frac = roof(spmv_bytes(8), prof_mixed["spmv_us"])
     cheb64_gbs, cheb64_frac = roof(cheb_bytes(8), prof_plain["cheb_us"])
     spmv64_gbs, spmv64_frac = roof(spmv_bytes(8), prof_plain["spmv_us"])
-    # the capture is of the step with plain loads; with an L2-resident prefix the DRAM
-    # traffic of the step is lower and not captured (null)
-    traffic = NCU_TRAFFIC.get((args.nx, args.ny)) if args.l2_keep == 0 else None
+    keep_bytes = 40_000_000 if args.l2_keep < 0 else int(args.l2_keep * 1e6)
+    traffic = NCU_TRAFFIC.get((args.nx, args.ny, keep_bytes))
     s.close()
 
     # ---- end to end through the C ABI, host buffers in and out
@@ -410,11 +412,9 @@ def run_ours(args, dist):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 CG recurrence (x, r, p, q, one SpMV per iteration) + f32 Chebyshev preconditioner",
         "data": f"synthetic, seeded (seed {args.seed})",
-        "config": {
-            "workload": f"plane strain {args.nx}x{args.ny} grid, {2 * args.nx * args.ny:,} triangles, "
-                        f"{prob.n_dof:,} DOF, E=10^U(9,12) per element, nu~U(0.2,0.45), left edge clamped, "
-                        f"random top-edge traction",
-            "mode": "mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
+        "config": workload_config(args, prob.n_dof, dist.world),
+        "solver": {
+            "mode":"mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
                     "preconditioner in FP32 on the prescaled FP32 copy"
                     + (" + learned warm start (predicted every step; kept when its FP64 residual beats the zero "
                        "start)" if net is not None else ""),
@@ -422,13 +422,11 @@ def run_ours(args, dist):
             "l2_keep_mb": 40.0 if args.l2_keep < 0 else args.l2_keep,
             "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio],
                           "fp32_krylov_ir": [args.ir_cheb, args.ir_cheb_ratio]},
-            "tol": args.tol, "step": "pattern + element kernels + reduction + loads + elimination + PCG",
-            "l2": "inputs larger than L2 (BSR values alone 448 MB FP64 / 224 MB FP32)",
-            "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
+            "step": "pattern + element kernels + reduction + loads + elimination + PCG",
         },
         "iterations": stats[-1].iterations, "restarts": stats[-1].outer, "learned_x0_used": stats[-1].x0_used,
         "assemble_ms": stats[-1].assemble_ms, "solve_ms": stats[-1].solve_ms,
-        "relres": stats[-1].relres, "err_vs_fp64": err,
+        "relres": stats[-1].relres, "err_vs_fp64": err, "err_vs_fp64_reference": err_ref,
         "plain_fp64": {"s_per_solve": plain_s, "iterations": pstats[-1].iterations if pstats else None,
                        "relres": pstats[-1].relres if pstats else None},
         "speedup_vs_plain": plain_s / value if value > 0 else None,
@@ -463,6 +461,17 @@ def run_ours(args, dist):
         "gpu_launches": int(n_launch),
         "clocks": clk,
     }
+    if dist.world == 1 and not args.no_cpu_baseline:
+        # the CPU baseline at the full workload, measured, and the FP64 oracle solution the
+        # mixed result's error is taken against
+        x_cpu, dt, tm = cpu_direct_solve(prob)
+        model, ncpu = cpu_info()
+        out["cpu_baseline"] = {"value": dt, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"the full workload ({prob.n_dof:,} DOF), one solve: {CPU_METHOD}",
+                               "assemble_s": tm["assemble_s"], "solve_s": tm["solve_s"],
+                               "relres": tm["relres"], "host": f"{model}, {ncpu} cores"}
+        out["err_vs_fp64"] = float(np.linalg.norm(x_mixed[:n] - x_cpu[:n]) / np.linalg.norm(x_cpu[:n]))
+        out["err_vs_fp64_reference"] = "the CPU FP64 direct solve of the cpu_baseline leg (SuperLU)"
     return out
 
 
@@ -516,12 +525,44 @@ def run_tet(args):
         dt = time.perf_counter() - t0
         model, ncpu = cpu_info()
         out["cpu_baseline"] = {
-            "value": scale_to_workload(dt, sample.n_dof, prob.n_dof), "unit": UNIT, "cores": 1, "kind": "port",
+            "value": dt, "unit": f"s/solve of the {sample.n_dof:,}-DOF sample (not scaled)", "cores": 1,
+            "kind": "port",
             "sample": f"one solve of the tetrahedral cantilever 40x8x8 cells ({sample.n_dof:,} DOF) through "
-                      "the oracle's restatement of the reference path, scaled to the workload's DOF in "
-                      "proportion (a lower bound: NATURAL spsolve does not reach 4M DOF in host memory)",
-            "sample_s": dt, "sample_dof": sample.n_dof, "host": f"{model}, {ncpu} cores"}
+                      "the oracle's restatement of the reference path (NATURAL spsolve on the saddle system); "
+                      "a direct solve of the 3D workload itself does not fit the bench's time on the host",
+            "host": f"{model}, {ncpu} cores"}
     return out
+
+
+def workload_config(args, n_dof, world):
+    """The configuration both arms name: the workload, its tolerance and placement."""
+    return {"workload": f"plane strain {args.nx}x{args.ny} grid, {2 * args.nx * args.ny:,} triangles, "
+                        f"{n_dof:,} DOF, E=10^U(9,12) per element, nu~U(0.2,0.45), left edge clamped, "
+                        f"random top-edge traction, seed {args.seed}",
+            "tol": args.tol,
+            "l2": "inputs larger than L2 (BSR values alone 448 MB FP64 / 224 MB FP32)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
+
+
+def run_reference(args, dist):
+    """The reference's path on the host cores, measured on the full workload: one solve
+    (assembly + elimination + SuperLU), however many steps were asked for -- a full solve
+    takes minutes, so the --steps K --warmup W run would not end in the time allowed;
+    the line says so in steps / steps_requested.  No sample is scaled."""
+    from finite_elements_gb300 import meshgen
+    prob = meshgen.plane_strain_random(args.nx, args.ny, seed=args.seed)
+    x, dt, tm = cpu_direct_solve(prob)
+    model, ncpu = cpu_info()
+    base = {"value": dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"the full workload ({prob.n_dof:,} DOF), one solve: {CPU_METHOD}",
+            "assemble_s": tm["assemble_s"], "solve_s": tm["solve_s"], "relres": tm["relres"],
+            "host": f"{model}, {ncpu} cores"}
+    return {"impl": "reference", "metric": METRIC, "value": dt, "unit": UNIT, "n_gpus": dist.world,
+            "steps": 1, "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "ms_per_step": dt * 1e3, "higher_is_better": False, "dtype": "f64", "data": f"synthetic, seeded "
+            f"(seed {args.seed})", "config": workload_config(args, prob.n_dof, dist.world),
+            "path": CPU_METHOD, "cpu_baseline": base,
+            "e2e": {"value": dt, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
@@ -534,44 +575,11 @@ def main():
         return
     if args.impl == "reference":
         if dist.rank == 0:
-            model, ncpu = cpu_info()
-            times = []
-            if args.warmup + args.steps > 10 and args.cpu_nx == 200:
-                args.cpu_nx = 120   # keep the whole reference run within a few minutes
-            full_dof = 2 * (args.nx + 1) * (args.ny + 1)
-            for k in range(args.warmup + args.steps):
-                dt, ndof = cpu_reference_sample(args.cpu_nx, args.seed + k)
-                if k >= args.warmup:
-                    times.append(dt)
-            sample_s = sum(times) / len(times)
-            v = scale_to_workload(sample_s, ndof, full_dof)
-            sample = (f"one solve per step of plane strain {args.cpu_nx}x{args.cpu_nx // 2} ({ndof:,} DOF) of "
-                      f"the same family, scaled to the workload's {full_dof:,} DOF in proportion (a lower "
-                      "bound: the full NATURAL spsolve does not fit in host memory)")
-            print(json.dumps({
-                "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist.world,
-                "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
-                "config": {"workload": f"plane strain {args.nx}x{args.ny}, {full_dof:,} DOF",
-                           "sample": sample, "path": "oracle restatement of finite_elements' "
-                           "create_matrix/create_source_matrix + scipy spsolve(permc_spec='NATURAL')"},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
-                                 "sample_s": sample_s, "sample_dof": ndof, "host": f"{model}, {ncpu} cores"},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+            print(json.dumps(run_reference(args, dist)))
         dist.close()
         return
     out = run_ours(args, dist)
     if dist.rank == 0:
-        if dist.world == 1 and not args.no_cpu_baseline:
-            model, ncpu = cpu_info()
-            dt, ndof = cpu_reference_sample(args.cpu_nx, args.seed)
-            full_dof = 2 * (args.nx + 1) * (args.ny + 1)
-            out["cpu_baseline"] = {
-                "value": scale_to_workload(dt, ndof, full_dof), "unit": UNIT, "cores": 1, "kind": "port",
-                "sample": f"one solve of plane strain {args.cpu_nx}x{args.cpu_nx // 2} ({ndof:,} DOF) "
-                          "through the oracle's restatement of the reference path (COO, csr_matrix, "
-                          f"spsolve NATURAL), scaled to the workload's {full_dof:,} DOF in proportion (a "
-                          "lower bound: NATURAL spsolve on 4M DOF does not fit in host memory)",
-                "sample_s": dt, "sample_dof": ndof, "host": f"{model}, {ncpu} cores"}
         print(json.dumps(out))
     dist.close()
 

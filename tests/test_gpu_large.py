@@ -139,3 +139,27 @@ def test_permuted_numbering_uses_int32_columns_and_gives_the_same_solution(gpu_l
         assert np.linalg.norm(u1 - u0) <= 1e-8 * np.linalg.norm(u0)
     s0.close()
     s1.close()
+
+
+def test_c3_2m_triangles_mixed_solve_against_a_cpu_direct_solve(gpu_lib):
+    """The 2M-triangle plane-strain configuration (1414 x 707, 2,003,640 DOF, a draw of
+    the benchmark's family) solved at the benchmark's settings -- FP64 CG recurrence,
+    FP32 Chebyshev(96) preconditioner over [lmax/1e5, lmax], tol 1e-8 -- against the
+    oracle's FP64 direct solve of the eliminated system on the host (SuperLU): the
+    displacements within 1e-7 and the multipliers within 1e-6 of the direct solution."""
+    from finite_elements_gb300 import meshgen
+    from finite_elements_gb300.engine import GpuSystem
+    from oracle import fe_oracle as O
+    prob = meshgen.plane_strain_random(1414, 707, seed=1)
+    assert prob.n_elements == 1_999_396 and prob.n_dof == 2_003_640
+    s = GpuSystem(prob)
+    try:
+        x, st = s.solve(precision="mixed-cg64", tol=1e-8, cheb_degree=96, cheb_ratio=1e5)
+    finally:
+        s.close()
+    assert st.status == 0 and st.relres <= 1e-8, st.as_dict()
+    ref = O.solve_reduced(prob, "direct")
+    n = prob.n_dof
+    err_u = np.linalg.norm(x[:n] - ref[:n]) / np.linalg.norm(ref[:n])
+    err_l = np.linalg.norm(x[n:] - ref[n:]) / np.linalg.norm(ref[n:])
+    assert err_u <= 1e-7 and err_l <= 1e-6, (err_u, err_l)

@@ -60,7 +60,7 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
     port = free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-nx", "20"]
+           "--gpus", "2", "--steps", "4", "--warmup", "3", "--nx", "20", "--ny", "10"]
     env = dict(os.environ)
     env.pop("CUDA_VISIBLE_DEVICES", None)
     p = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
@@ -70,9 +70,11 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
     rec = json.loads(lines[0])
     assert rec["impl"] == "reference" and rec["n_gpus"] == 2 and rec["value"] > 0
     assert rec["cpu_baseline"]["kind"] == "port" and rec["e2e"]["h2d_bytes_per_step"] == 0
-    # the sample's time carried to the 2000 x 1000 workload's DOF in proportion
+    # one measured solve of the whole workload (here 20 x 10): nothing is scaled, and the
+    # line says that one solve was timed of the four steps asked for
     cb = rec["cpu_baseline"]
-    assert cb["sample_dof"] == 2 * 21 * 11
-    full = 2 * 2001 * 1001
-    assert abs(rec["value"] - cb["sample_s"] * full / cb["sample_dof"]) <= 1e-9 * rec["value"]
+    assert rec["steps"] == 1 and rec["steps_requested"] == 4 and rec["warmup_requested"] == 3
+    assert f"{2 * 21 * 11:,} DOF" in rec["config"]["workload"] and "full workload" in cb["sample"]
+    assert abs(cb["assemble_s"] + cb["solve_s"] - rec["value"]) <= 0.05 * rec["value"] + 1e-3
+    assert cb["relres"] < 1e-10
     assert rec["e2e"]["value"] == rec["value"] == cb["value"]
