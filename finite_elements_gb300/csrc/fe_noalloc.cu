@@ -17,7 +17,12 @@
 // * every call shares it: calls whose kernels overlap on the GPU (other streams, other
 //   threads) race and corrupt each other's offsets -- serialise them;
 // * the first call on a device looks the array's device address up (a runtime API
-//   call); make that first call before capturing any stream into a CUDA graph.
+//   call); make that first call before capturing any stream into a CUDA graph;
+// * that address is cached for the life of the process: a cudaDeviceReset (or any
+//   teardown of the device's primary context) invalidates it, and the entry point must
+//   not be called again in that process afterwards;
+// * offsets[n] = -1 flags a total beyond int32: the offsets past that point have
+//   wrapped, so check offsets[n] before using any of them.
 #include <mutex>
 
 #include "fe_internal.h"

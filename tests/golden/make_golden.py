@@ -509,7 +509,11 @@ def cases(ref_root):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # the reference checkout: the first argument, $FE_REFERENCE_ROOT, or a directory
+    # named "reference" beside this repository
+    here = os.path.dirname(os.path.abspath(__file__))
+    ref = (sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FE_REFERENCE_ROOT")
+           or os.path.join(os.path.dirname(os.path.dirname(here)), "reference"))
     install_stubs()
     sys.path.insert(0, ref)
     import finite_elements.analysis      # noqa: F401  (the reference's own modules)

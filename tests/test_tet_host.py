@@ -10,7 +10,10 @@ from finite_elements_gb300 import gmsh, meshgen
 from finite_elements_gb300.problem import ELASTIC3D, ElementLoadSet, Problem
 from oracle import fe_oracle as O
 
-REF_3D = "/root/reference/scripts/InputFiles/3D"
+from conftest import reference_root
+
+_REF = reference_root()
+REF_3D = os.path.join(_REF, "scripts", "InputFiles", "3D") if _REF else ""
 
 
 def test_box_tets_fill_the_box_and_conform():
@@ -67,7 +70,8 @@ def test_gmsh_tetrahedra_write_read(tmp_path):
     assert am.coords.shape == c.shape and am.conn.shape == conn.shape
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_3D), reason="the reference's input files are not here")
+@pytest.mark.skipif(not os.path.isdir(REF_3D),
+                    reason="the reference checkout's scripts/InputFiles/3D is not present (set FE_REFERENCE_ROOT)")
 @pytest.mark.parametrize("name,n_nodes,n_tets", [("beam3d_0.5", 46, 104), ("beam3d_1", 110, 253),
                                                  ("cube", 721, 2576)])
 def test_gmsh_reads_the_reference_3d_inputs(name, n_nodes, n_tets):

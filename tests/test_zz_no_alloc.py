@@ -62,6 +62,10 @@ def test_noalloc_scan_empty_and_oversize(gpu_lib):
     torch = pytest.importorskip("torch")
     out = _noalloc_scan(gpu_lib, torch, np.zeros(0, np.int32))
     np.testing.assert_array_equal(out, [0])
+    # a total beyond int32 is flagged by offsets[n] = -1 (the earlier offsets that still
+    # fit are exact)
+    out = _noalloc_scan(gpu_lib, torch, np.full(3, 1 << 30, np.int32))
+    assert out[3] == -1 and out[0] == 0 and out[1] == 1 << 30
     limit = (1 << 15) * 2048
     # rejected before any GPU work: the null buffers are never touched
     status = gpu_lib.fe_scan_counts_noalloc(None, None, limit + 1, None)
