@@ -1118,6 +1118,7 @@ int build_system(fe_handle_s *h, double ka, double mb, bool use_bc) {
     h->launches += (use_bc && h->n_bc > 0 ? 1 : 0) + (h->nnzb > 0 ? 1 : 0) + 2 + (h->f_ready ? 1 : 0);
     FE_CHECK(build_sell(h));
     h->w.lmax[0] = h->w.lmax[1] = 0.0;   // a new matrix: new Chebyshev bounds
+    h->sys_generation += 1;
     h->sys_ready = true;
     return FE_OK;
 }

@@ -216,6 +216,7 @@ struct fe_handle_s {
 
     // values
     bool k_ready = false, m_ready = false, f_ready = false, sys_ready = false;
+    uint64_t sys_generation = 0;   // counts the system matrices built (build_system)
     bool singular = false;                // a diagonal block could not be inverted
     fe::DBuf<double> ke;                  // [n_elem][(3d)^2]
     fe::DBuf<double> me_scale;            // [n_elem] rho*A*t/12
@@ -280,6 +281,9 @@ int recover_multipliers(fe_handle_s *h);
 // Continuity conditions (fe_continuity.cu): host set-up and the projected FP64 PCG
 int set_continuity(fe_handle_s *h, int64_t n, const int64_t *dof1, const int64_t *dof2, const double *value);
 int solve_continuity(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
+// Largest eigenvalue of the m x m tridiagonal Lanczos matrix of the CG coefficients
+// alpha[0..m), beta[0..m) (bisection on the Sturm sequence), fe_solver.cu.
+double lanczos_lmax(const double *alpha, const double *beta, int m);
 int set_rhs_additions(fe_handle_s *h, int64_t n, const int64_t *dof, const double *value);
 int apply_rhs_additions(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);

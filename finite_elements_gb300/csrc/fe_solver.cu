@@ -31,10 +31,14 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "fe_internal.h"
+#include "fe_sell.cuh"
 
 namespace fe {
 namespace {
@@ -42,6 +46,36 @@ namespace {
 constexpr int kVecThreads = 256;
 
 inline int vec_grid(int64_t n_nodes) { return grid_for(n_nodes, kVecThreads, 152 * 8); }
+
+// At most one resident wave of a grid-stride kernel: the SMs times the blocks of
+// kVecThreads that stay resident per SM for that kernel (its registers and shared
+// memory decide), looked up once per kernel and device.  Used for the Chebyshev steps:
+// the FP64 step keeps 5 blocks per SM resident, and its 1216-block grid (8 per SM) ran
+// as 1.6 waves, 161 us against 157 us in one wave at the 4M-DOF workload.  The FP64
+// PCG SpMV measured the other way (138 us with 1216 blocks, 142.5 us in one wave) and
+// keeps the larger grid.
+int wave_grid(const void *kernel, int grid) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> waves;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return grid;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = waves.find({dev, kernel});
+    if (it == waves.end()) {
+        // the first lookup may come while the stream is being captured into a graph: the
+        // queries enqueue nothing, so this thread allows them for their duration
+        cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+        cudaThreadExchangeStreamCaptureMode(&mode);
+        int sms = 0, per_sm = 0;
+        const bool ok = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+                        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kVecThreads, 0) ==
+                            cudaSuccess;
+        cudaThreadExchangeStreamCaptureMode(&mode);
+        if (!ok || sms <= 0 || per_sm <= 0) return grid;
+        it = waves.emplace(std::make_pair(dev, kernel), sms * per_sm).first;
+    }
+    return std::max(1, std::min(grid, it->second));
+}
 
 // ---------------------------------------------------------------- reductions
 
@@ -100,68 +134,6 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, u
         *ticket = 0;
     }
     return true;
-}
-
-// ---------------------------------------------------------------- node vectors
-
-template <int D, typename T>
-struct NodeVec {
-    T v[D];
-};
-
-template <int D, typename T>
-__device__ __forceinline__ NodeVec<D, T> ld(const T *__restrict__ a, int64_t r) {
-    NodeVec<D, T> o;
-    if constexpr (D == 2 && sizeof(T) == 8) {
-        double2 t = reinterpret_cast<const double2 *>(a)[r];
-        o.v[0] = t.x, o.v[1] = t.y;
-    } else if constexpr (D == 2) {
-        float2 t = reinterpret_cast<const float2 *>(a)[r];
-        o.v[0] = t.x, o.v[1] = t.y;
-    } else {
-#pragma unroll
-        for (int k = 0; k < D; ++k) o.v[k] = a[r * D + k];
-    }
-    return o;
-}
-
-template <int D, typename T>
-__device__ __forceinline__ void st(T *__restrict__ a, int64_t r, const NodeVec<D, T> &o) {
-    if constexpr (D == 2 && sizeof(T) == 8) {
-        reinterpret_cast<double2 *>(a)[r] = make_double2(o.v[0], o.v[1]);
-    } else if constexpr (D == 2) {
-        reinterpret_cast<float2 *>(a)[r] = make_float2(o.v[0], o.v[1]);
-    } else {
-#pragma unroll
-        for (int k = 0; k < D; ++k) a[r * D + k] = o.v[k];
-    }
-}
-
-// y = M^-1 x for one node (M^-1 stored row-major per node)
-template <int D, typename T>
-__device__ __forceinline__ NodeVec<D, T> apply_dinv(const T *__restrict__ dinv, int64_t r, const NodeVec<D, T> &x) {
-    NodeVec<D, T> y;
-    if constexpr (D == 2) {
-        if constexpr (sizeof(T) == 8) {
-            const double2 m0 = reinterpret_cast<const double2 *>(dinv)[2 * r];
-            const double2 m1 = reinterpret_cast<const double2 *>(dinv)[2 * r + 1];
-            y.v[0] = m0.x * x.v[0] + m0.y * x.v[1];
-            y.v[1] = m1.x * x.v[0] + m1.y * x.v[1];
-        } else {
-            const float4 m = reinterpret_cast<const float4 *>(dinv)[r];
-            y.v[0] = m.x * x.v[0] + m.y * x.v[1];
-            y.v[1] = m.z * x.v[0] + m.w * x.v[1];
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < D; ++i) {
-            T acc = dinv[r * D * D + i * D] * x.v[0];
-#pragma unroll
-            for (int k = 1; k < D; ++k) acc += dinv[r * D * D + i * D + k] * x.v[k];
-            y.v[i] = acc;
-        }
-    }
-    return y;
 }
 
 // ---------------------------------------------------------------- SpMV row kernel
@@ -228,35 +200,6 @@ __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, cons
     const int64_t rows_padded = ((n_nodes + groups - 1) / groups) * groups;                 \
     for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (G); row < rows_padded; row += groups)
 
-// acc += B x for one D x D block, as a chain of fused multiply-adds into the
-// accumulator: 2 D FMAs per block, the least work for the FP64 pipe that bounds the
-// FP64 SpMV on this GPU.
-template <int D, typename T>
-__device__ __forceinline__ void block_mac(const T *__restrict__ blk, const NodeVec<D, T> &x, NodeVec<D, T> &acc) {
-    if constexpr (D == 2) {
-        if constexpr (sizeof(T) == 8) {
-            const double2 b0 = __ldg(reinterpret_cast<const double2 *>(blk));
-            const double2 b1 = __ldg(reinterpret_cast<const double2 *>(blk) + 1);
-            acc.v[0] = fma(b0.x, x.v[0], acc.v[0]);
-            acc.v[1] = fma(b1.x, x.v[0], acc.v[1]);
-            acc.v[0] = fma(b0.y, x.v[1], acc.v[0]);
-            acc.v[1] = fma(b1.y, x.v[1], acc.v[1]);
-        } else {
-            const float4 b = __ldg(reinterpret_cast<const float4 *>(blk));
-            acc.v[0] = fmaf(b.x, x.v[0], acc.v[0]);
-            acc.v[1] = fmaf(b.z, x.v[0], acc.v[1]);
-            acc.v[0] = fmaf(b.y, x.v[1], acc.v[0]);
-            acc.v[1] = fmaf(b.w, x.v[1], acc.v[1]);
-        }
-    } else {
-        // column by column, as the D = 2 chains
-#pragma unroll
-        for (int b = 0; b < D; ++b)
-#pragma unroll
-            for (int a = 0; a < D; ++a) acc.v[a] = fma(__ldg(blk + a * D + b), x.v[b], acc.v[a]);
-    }
-}
-
 // Resident blocks per SM the SELL kernels are compiled for: FP32 with 1 or 2 DOF per
 // node 8 (32 registers, the 1216-block grid is one wave); FP64, and FP32 with 3 DOF
 // per node (whose 3 x 3 blocks and 3-vectors do not fit 32 registers), 0, i.e.
@@ -264,110 +207,6 @@ __device__ __forceinline__ void block_mac(const T *__restrict__ blk, const NodeV
 // lose the occupancy, 5 makes the Chebyshev step spill).
 template <int D, typename T>
 constexpr int kSellBlocks = (sizeof(T) == 4 && D <= 2) ? 8 : 0;
-
-struct Sell {
-    const int32_t *off, *col;
-    const int16_t *dcol;   // column offsets c - r when every one fits in 16 bits, else null
-    int64_t n_slices;
-    // FP32 copy, 2 DOF per node: the first keep bytes of the values are loaded with L2
-    // priority evict_last and the rest (up to total) evict_first, so that a prefix of
-    // the matrix stays in L2 from one Chebyshev step to the next; 0 = plain loads
-    uint32_t keep = 0, total = 0;
-};
-
-// Loads of the FP32 2x2 blocks under the L2 policy of Sell::keep.
-__device__ __forceinline__ uint64_t l2_keep_policy(const void *base, uint32_t keep, uint32_t total) {
-    uint64_t pol;
-    asm("createpolicy.range.global.L2::evict_last.L2::evict_first.b64 %0, [%1], %2, %3;"
-                 : "=l"(pol)
-                 : "l"(base), "r"(keep), "r"(total));
-    return pol;
-}
-
-__device__ __forceinline__ float4 ld_block_hint(const float *p, uint64_t pol) {
-    float4 v;
-    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-                 : "l"(p), "l"(pol));
-    return v;
-}
-
-// Calls f(std::true_type) when an FP32 kernel can read the 16-bit column offsets,
-// else f(std::false_type); FP64 kernels always read the int32 columns.
-template <typename T, typename F>
-void with_col16(const Sell &A, F f) {
-    if constexpr (sizeof(T) == 4) {
-        if (A.dcol) {
-            f(std::true_type{});
-            return;
-        }
-    }
-    f(std::false_type{});
-}
-
-// Row r of A x from the SELL-32 copy: one lane per block row, one warp per slice of
-// 32 rows, entry k of the slice at base + 32 k + lane, so each warp load of columns
-// and blocks is one contiguous segment.  FP64: the diagonal block comes from diag and
-// every entry multiplies x_c.  FP32 (difference form): an entry with column c != r
-// multiplies x_c - x_r, an entry with column r (the row-sum entry, or padding with a
-// zero block) multiplies x_r; there is no diagonal term.  Rows past the last node
-// (padding of the final slice) gather their own padding row -- the solver's vectors
-// are allocated for whole slices -- and their result is discarded.
-template <int D, typename T, bool C16 = false, bool KEEP = false>
-__device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const Sell &A, const T *__restrict__ val,
-                                                  const T *__restrict__ diag, const T *__restrict__ x) {
-    constexpr bool DIFF = sizeof(T) == 4;
-    NodeVec<D, T> xr, acc;
-#pragma unroll
-    for (int a = 0; a < D; ++a) xr.v[a] = T(0), acc.v[a] = T(0);
-    if (valid) {
-        xr = ld<D, T>(x, r);
-        if constexpr (!DIFF) block_mac<D, T>(diag + r * D * D, xr, acc);
-    }
-    const int64_t sl = r >> 5;
-    const int lane = (int)(r & 31);
-    const int64_t base = A.off[sl];
-    const int w = (A.off[sl + 1] - (int)base) >> 5;
-    // KEEP (FP32, 2 DOF per node): the block loads carry the L2 policy of A.keep
-    constexpr bool HINT = KEEP && D == 2 && sizeof(T) == 4;
-    uint64_t pol = 0;
-    if constexpr (HINT) pol = l2_keep_policy(val, A.keep, A.total);
-    // FP32: four entries per trip, their column loads and then their gathers all in
-    // flight before the first product (entries past w read the row itself and add
-    // 0).  FP64 is bound by the FP64 FMA rate and runs one entry per trip.
-    constexpr int U = sizeof(T) == 4 ? 4 : 1;
-    for (int k = 0; k < w; k += U) {
-        int c[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            c[u] = (k + u < w) ? (C16 ? (int)r + (int)__ldg(A.dcol + base + 32 * (int64_t)(k + u) + lane)
-                                      : __ldg(A.col + base + 32 * (int64_t)(k + u) + lane))
-                               : (int)r;
-        NodeVec<D, T> xv[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) xv[u] = ld<D, T>(x, c[u]);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            if (k + u < w) {
-                if (DIFF && c[u] != (int)r) {
-#pragma unroll
-                    for (int a = 0; a < D; ++a) xv[u].v[a] -= xr.v[a];
-                }
-                const T *blk = val + (base + 32 * (int64_t)(k + u) + lane) * D * D;
-                if constexpr (HINT) {
-                    const float4 b = ld_block_hint(blk, pol);
-                    acc.v[0] = fmaf(b.x, xv[u].v[0], acc.v[0]);
-                    acc.v[1] = fmaf(b.z, xv[u].v[0], acc.v[1]);
-                    acc.v[0] = fmaf(b.y, xv[u].v[1], acc.v[0]);
-                    acc.v[1] = fmaf(b.w, xv[u].v[1], acc.v[1]);
-                } else {
-                    block_mac<D, T>(blk, xv[u], acc);
-                }
-            }
-        }
-    }
-    return acc;
-}
 
 // Rows of the SELL copy handled by this thread (grid-stride in whole warps, so a
 // warp always covers one slice).
@@ -942,12 +781,9 @@ void launch_cheb_step(fe_handle_s *h, const Sys<T> &s, bool first, const T *zin,
                 return;
             }
         }
-        if (first)
-            k_cheb_step<D, T, RD, MODE, true, C><<<grid, kVecThreads, 0, h->stream>>>(
-                h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
-        else
-            k_cheb_step<D, T, RD, MODE, false, C><<<grid, kVecThreads, 0, h->stream>>>(
-                h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
+        const auto kern = first ? k_cheb_step<D, T, RD, MODE, true, C> : k_cheb_step<D, T, RD, MODE, false, C>;
+        kern<<<wave_grid((const void *)kern, grid), kVecThreads, 0, h->stream>>>(
+            h->n_nodes, s.A, s.sval, s.diag, s.dinv, s.rh, zin, zout, c1, c2, part, sc, rdot);
     });
 }
 
@@ -975,6 +811,7 @@ void enqueue_cheb_steps(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScal
 }
 
 inline int sell_grid(const fe_handle_s *h) { return grid_for(h->n_slices * 32, kVecThreads, 152 * 8); }
+
 
 template <int D, typename T>
 void enqueue_iteration(fe_handle_s *h, const Sys<T> &s, const Cheb &cb, PcgScalars *sc, double *part,
@@ -1223,40 +1060,6 @@ int run_loop_mp(fe_handle_s *h, const SysMP &s, const Cheb &cb, int chunk) {
     return run_chunks(
         h, 2, s.d.p, G, cb, chunk,
         [&](cudaEvent_t *ev) { enqueue_iteration_mp<D>(h, s, cb, w.sc.p, w.partials.p, ev); }, nullptr);
-}
-
-// Largest eigenvalue of the tridiagonal Lanczos matrix built from CG coefficients,
-// by bisection on the Sturm sequence.
-double lanczos_lmax(const double *alpha, const double *beta, int m) {
-    if (m <= 0) return 0.0;
-    std::vector<double> dg(m), off(m > 1 ? m - 1 : 1);
-    for (int j = 0; j < m; ++j) {
-        dg[j] = 1.0 / alpha[j] + (j > 0 ? beta[j - 1] / alpha[j - 1] : 0.0);
-        if (j + 1 < m) off[j] = sqrt(std::max(beta[j], 0.0)) / alpha[j];
-    }
-    double hi = 0.0;
-    for (int j = 0; j < m; ++j) {
-        double rr = fabs(dg[j]) + (j > 0 ? fabs(off[j - 1]) : 0) + (j + 1 < m ? fabs(off[j]) : 0);
-        hi = std::max(hi, rr);
-    }
-    double lo = 0.0;
-    auto count_below = [&](double x) {
-        int c = 0;
-        double q = dg[0] - x;
-        if (q < 0) ++c;
-        for (int j = 1; j < m; ++j) {
-            if (q == 0) q = 1e-300;
-            q = dg[j] - x - off[j - 1] * off[j - 1] / q;
-            if (q < 0) ++c;
-        }
-        return c;
-    };
-    for (int it = 0; it < 200; ++it) {
-        double mid = 0.5 * (lo + hi);
-        if (count_below(mid) < m) lo = mid;
-        else hi = mid;
-    }
-    return hi;
 }
 
 template <typename F>
@@ -1676,6 +1479,40 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
 }
 
 }  // namespace
+
+// Largest eigenvalue of the tridiagonal Lanczos matrix built from CG coefficients,
+// by bisection on the Sturm sequence.
+double lanczos_lmax(const double *alpha, const double *beta, int m) {
+    if (m <= 0) return 0.0;
+    std::vector<double> dg(m), off(m > 1 ? m - 1 : 1);
+    for (int j = 0; j < m; ++j) {
+        dg[j] = 1.0 / alpha[j] + (j > 0 ? beta[j - 1] / alpha[j - 1] : 0.0);
+        if (j + 1 < m) off[j] = sqrt(std::max(beta[j], 0.0)) / alpha[j];
+    }
+    double hi = 0.0;
+    for (int j = 0; j < m; ++j) {
+        double rr = fabs(dg[j]) + (j > 0 ? fabs(off[j - 1]) : 0) + (j + 1 < m ? fabs(off[j]) : 0);
+        hi = std::max(hi, rr);
+    }
+    double lo = 0.0;
+    auto count_below = [&](double x) {
+        int c = 0;
+        double q = dg[0] - x;
+        if (q < 0) ++c;
+        for (int j = 1; j < m; ++j) {
+            if (q == 0) q = 1e-300;
+            q = dg[j] - x - off[j - 1] * off[j - 1] / q;
+            if (q < 0) ++c;
+        }
+        return c;
+    };
+    for (int it = 0; it < 200; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (count_below(mid) < m) lo = mid;
+        else hi = mid;
+    }
+    return hi;
+}
 
 // ---------------------------------------------------------------- entry points
 
