@@ -110,6 +110,8 @@ _SIGNATURES = {
     "fe_batch_set_tiles": ([_P, _I32, _I64], C.c_int),
     "fe_batch_autotune": ([_P, _PI32, _PI64, _PD], C.c_int),
     "fe_batch_solve": ([_P, _D, _I32, _P, _P, _P, _P, _PD], C.c_int),
+    "fe_batch_set_preconditioner": ([_P, _I32, _D], C.c_int),
+    "fe_batch_last_run": ([_P, _PI32, _PI32, _PI32, _PI32], C.c_int),
     "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
     "fe_amg_build_host": ([_I64, _I32, _P, _P, _P, _I32, _P, _D, _I64, C.POINTER(_P)], C.c_int),
     "fe_amg_levels": ([_P, _PI32], C.c_int),

@@ -1,9 +1,12 @@
-"""Batched solves of many independent elasticity problems in one set of launches.
+"""Batched solves of many independent elasticity problems.
 
 ``BatchedSystem(problems)`` concatenates the problems into one block-diagonal union
 (node and element indices shifted, loads and conditions kept in instance order), so
 the whole batch is assembled by one fe_assemble and solved by the batched PCG of
-fe_batch_* with per-instance step sizes and convergence.
+fe_batch_*: the mixed-precision PCG of the single solve (FP64 recurrence, FP32
+node-block Jacobi + Chebyshev preconditioner) with per-instance step sizes, Chebyshev
+intervals and convergence, run by one persistent kernel per chunk of iterations that a
+CUDA graph replays.
 """
 from __future__ import annotations
 
@@ -94,13 +97,29 @@ class BatchedSystem:
         self.b = b
 
     def autotune(self):
-        lanes, rows, us = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_double()
-        _lib.check(self._lib.fe_batch_autotune(self.b, ctypes.byref(lanes), ctypes.byref(rows), ctypes.byref(us)),
+        """Blocks per SM and SELL slices per work item of the persistent kernel, timed on
+        this batch; the fastest pair is kept."""
+        bps, spi, us = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_double()
+        _lib.check(self._lib.fe_batch_autotune(self.b, ctypes.byref(bps), ctypes.byref(spi), ctypes.byref(us)),
                    "fe_batch_autotune")
-        return {"lanes": lanes.value, "rows_per_chunk": rows.value, "us_per_iteration": us.value}
+        return {"blocks_per_sm": bps.value, "slices_per_item": spi.value, "us_per_iteration": us.value}
 
-    def set_tiles(self, lanes, rows_per_chunk):
-        _lib.check(self._lib.fe_batch_set_tiles(self.b, lanes, rows_per_chunk), "fe_batch_set_tiles")
+    def set_tiles(self, blocks_per_sm, slices_per_item):
+        _lib.check(self._lib.fe_batch_set_tiles(self.b, blocks_per_sm, slices_per_item), "fe_batch_set_tiles")
+
+    def set_preconditioner(self, cheb_degree, cheb_ratio=1e4):
+        """Chebyshev terms (1 = node-block Jacobi alone) and each instance's interval ratio."""
+        _lib.check(self._lib.fe_batch_set_preconditioner(self.b, cheb_degree, cheb_ratio),
+                   "fe_batch_set_preconditioner")
+
+    def last_run(self):
+        """Replays of the captured chunk, persistent-kernel launches, whether the chunks
+        replay from a CUDA graph, and the cooperative grid of the last solve."""
+        g, k, u, grid = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(self._lib.fe_batch_last_run(self.b, ctypes.byref(g), ctypes.byref(k), ctypes.byref(u),
+                                               ctypes.byref(grid)), "fe_batch_last_run")
+        return {"graph_launches": g.value, "kernel_launches": k.value, "uses_graph": bool(u.value),
+                "grid": grid.value}
 
     def solve(self, tol=1e-8, max_iter=0, want_x=True):
         """Per-instance displacements (list of arrays, n_dof_i each) or None, and

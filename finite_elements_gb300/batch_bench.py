@@ -1,6 +1,7 @@
 """Batched solve of many uneven plane-stress instances against solving them one at a
-time, both on the GPU with the library's FP64 PCG (node-block Jacobi) to the same
-relative residual.
+time, both on the GPU with the library's mixed-precision PCG (FP64 recurrence, FP32
+node-block Jacobi + Chebyshev preconditioner of the same degree) to the same relative
+residual.
 
     python -m finite_elements_gb300.batch_bench [--n 512] [--seed 0] [--tol 1e-8]
     python -m torch.distributed.run --nproc-per-node N --master-addr 127.0.0.1 \
@@ -37,15 +38,22 @@ def run_sharded(a, probs_all, world):
     import torch.distributed as td
 
     from . import _lib
+    if world > len(probs_all):
+        # an empty shard would have no batch to build while the other ranks wait in the
+        # barrier: refuse before any rank joins the group
+        raise SystemExit(f"batch_bench: {world} ranks for {len(probs_all)} instances; use at most one rank "
+                         "per instance")
     td.init_process_group("gloo")
     rank = td.get_rank()
     _lib.check(_lib.load().fe_set_device(int(os.environ.get("LOCAL_RANK", rank))), "fe_set_device")
     shard = shard_instances([p.n_dof for p in probs_all], world)[rank]
     probs = [probs_all[i] for i in shard]
     w = BatchedSystem(probs[:4])
+    w.set_preconditioner(a.cheb, a.cheb_ratio)
     w.solve(tol=a.tol, want_x=False)
     w.close()
     b = BatchedSystem(probs)
+    b.set_preconditioner(a.cheb, a.cheb_ratio)
     tiles = b.autotune()
     b.solve(tol=a.tol, want_x=False)                      # graph capture
     h = b.system.handle
@@ -53,6 +61,7 @@ def run_sharded(a, probs_all, world):
     h.call("fe_event_record", 0)
     h.call("fe_assemble", 1 | 4 | 8)
     h.call("fe_event_record", 1)
+    h.call("fe_synchronize")
     ms = ctypes.c_double()
     h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
     parts, st = b.solve(tol=a.tol, want_x=False)
@@ -79,6 +88,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--single", type=int, default=-1, help="instances solved one at a time (-1: all)")
+    ap.add_argument("--cheb", type=int, default=16, help="Chebyshev terms of the preconditioner (1: Jacobi)")
+    ap.add_argument("--cheb-ratio", type=float, default=1e4)
     a = ap.parse_args()
     probs = meshgen.batch_c4(a.n, seed=a.seed)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -89,28 +100,34 @@ def main():
     tri = int(sum(p.n_elements for p in probs))
     # warm-up of the library (kernels, allocator) on a small batch
     w = BatchedSystem(probs[:4])
+    w.set_preconditioner(a.cheb, a.cheb_ratio)
     w.solve(tol=a.tol, want_x=False)
     w.close()
 
     t0 = time.perf_counter()
     b = BatchedSystem(probs)
+    b.set_preconditioner(a.cheb, a.cheb_ratio)
     t_setup = time.perf_counter() - t0
     tiles = b.autotune()
     b.solve(tol=a.tol, want_x=False)                      # graph capture
-    t1 = time.perf_counter()
-    parts, st = b.solve(tol=a.tol, want_x=True)
-    t_solve_wall = time.perf_counter() - t1
-    ok = int((st["status"] == 0).sum())
-    worst = float(st["relres"].max())
-    # assembly of the union on the device (pattern + elements + reduction + loads + BC)
+    # timed: assembly of the union on the device (pattern + elements + reduction + loads +
+    # conditions + SELL copies), then the solve, which re-runs the per-instance
+    # Chebyshev-interval probe for the new system
     import ctypes
     h = b.system.handle
     h.call("fe_event_record", 0)
     h.call("fe_assemble", 1 | 4 | 8)
     h.call("fe_event_record", 1)
+    h.call("fe_synchronize")
     ms = ctypes.c_double()
     h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
     asm_ms = ms.value
+    t1 = time.perf_counter()
+    parts, st = b.solve(tol=a.tol, want_x=True)
+    t_solve_wall = time.perf_counter() - t1
+    run = b.last_run()
+    ok = int((st["status"] == 0).sum())
+    worst = float(st["relres"].max())
     b.close()
 
     n_single = len(probs) if a.single < 0 else min(a.single, len(probs))
@@ -119,7 +136,8 @@ def main():
     single_dof = 0
     for p in probs[:n_single]:
         s = GpuSystem(p)
-        _, s1 = s.solve(precision="fp64", tol=a.tol, want_host=True)
+        _, s1 = s.solve(precision="mixed-cg64", tol=a.tol, cheb_degree=a.cheb if a.cheb > 1 else 0,
+                        cheb_ratio=a.cheb_ratio, want_host=True)
         single_dev_ms += s1.solve_ms + s1.assemble_ms
         single_dof += p.n_dof
         s.close()
@@ -129,7 +147,8 @@ def main():
         "workload": f"{a.n} plane-stress instances, {tri:,} triangles, {dof:,} DOF in total "
                     f"(2e3..2e5 triangles each, seed {a.seed})",
         "tol": a.tol, "instances_converged": ok, "worst_relres": worst,
-        "tiles": tiles, "max_iterations": int(st["iterations"].max()),
+        "tiles": tiles, "max_iterations": int(st["iterations"].max()), "persistent_kernel": run,
+        "preconditioner": {"chebyshev_terms": a.cheb, "ratio": a.cheb_ratio},
         "batched": {"assemble_ms": asm_ms, "solve_ms": st["solve_ms"],
                     "dof_per_s_device": dof / batched_dev_s,
                     "solve_wall_s": t_solve_wall, "setup_wall_s": t_setup},

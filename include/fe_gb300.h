@@ -317,21 +317,36 @@ int fe_gnn_adam_step(fe_gnn g, float lr, float beta1, float beta2, float eps);
  * reference, which solves one analysis per spsolve call, analysis.py:816-830).  The
  * instances are concatenated into one handle (fe_mesh_create on the union mesh with
  * disjoint node ranges, then the usual setters and fe_assemble); node_ptr_host[i] ..
- * node_ptr_host[i+1] are instance i's nodes.  The batched FP64 PCG (node-block
- * Jacobi) runs each phase for all instances in one launch with per-instance
- * reductions, step sizes and convergence; converged instances drop out. */
+ * node_ptr_host[i+1] are instance i's nodes.  The batched solve is the mixed-precision
+ * PCG of FE_PREC_MIXED_CG64 per instance -- FP64 recurrence, node-block Jacobi +
+ * Chebyshev preconditioner in FP32 with each instance's own Chebyshev interval -- run by
+ * one persistent cooperative kernel per chunk of iterations (grid barriers between its
+ * phases, with bounded waits), replayed from a CUDA graph.  Reductions are per
+ * instance and deterministic; converged instances drop out. */
 typedef struct fe_batch_s *fe_batch;
 int fe_batch_create(fe_handle h, int32_t n_instances, const int64_t *node_ptr_host, fe_batch *out);
 int fe_batch_destroy(fe_batch b);
-/* Lanes per block row (1, 2, 4) and rows per persistent-kernel chunk. */
-int fe_batch_set_tiles(fe_batch b, int32_t lanes, int64_t rows_per_chunk);
-/* Time 20 iterations for each (lanes, rows per chunk) candidate and keep the fastest. */
-int fe_batch_autotune(fe_batch b, int32_t *lanes_out, int64_t *rows_out, double *us_per_iter_out);
-/* Solve every instance to ||b_i - A_i x_i|| <= tol ||b_i||; per-instance iterations,
- * status and final true relative residual (each optional), the union solution
- * (n_dof values, optional) and the device time of the solve. */
+/* Resident blocks per SM of the persistent kernel (0 = as many as fit) and SELL slices
+ * (32 node rows each) per work item of a warp. */
+int fe_batch_set_tiles(fe_batch b, int32_t blocks_per_sm, int64_t slices_per_item);
+/* Chebyshev terms of the preconditioner (1 = node-block Jacobi alone, up to 128) and the
+ * ratio lmax / lmin of each instance's interval; default 16 and 1e4. */
+int fe_batch_set_preconditioner(fe_batch b, int32_t cheb_degree, double cheb_ratio);
+/* Time a chunk of iterations for each (blocks per SM, slices per item) candidate and keep
+ * the fastest. */
+int fe_batch_autotune(fe_batch b, int32_t *blocks_per_sm_out, int64_t *slices_per_item_out,
+                      double *us_per_iter_out);
+/* Solve every instance to ||b_i - A_i x_i|| <= tol ||b_i|| (FP64 true residual);
+ * per-instance iterations, status and final true relative residual (each optional), the
+ * union solution (n_dof values, optional) and the device time of the solve (including
+ * the per-instance Chebyshev-interval probe after a new assembly). */
 int fe_batch_solve(fe_batch b, double tol, int32_t max_iter, int32_t *iterations_host, int32_t *status_host,
                    double *relres_host, double *x_host, double *ms_out);
+/* The last fe_batch_solve: replays of the captured chunk, launches of the persistent
+ * kernel, whether chunks replay from a CUDA graph (1) or launch directly (0), and the
+ * cooperative grid (each optional). */
+int fe_batch_last_run(fe_batch b, int32_t *graph_launches, int32_t *kernel_launches, int32_t *uses_graph,
+                      int32_t *grid);
 
 /* No counterpart in the reference.  Exclusive scan of n int32 counts into n+1 int32
  * offsets (offsets_dev[0] = 0, offsets_dev[n] = total; -1 there if the total does not
@@ -343,7 +358,11 @@ int fe_batch_solve(fe_batch b, double tol, int32_t max_iter, int32_t *iterations
  * array inside the library (256 KiB per GPU, kept until exit), so n is limited to
  * 67,108,864 (FE_BAD_INPUT beyond).  Calls that overlap on the GPU share that array
  * and race.  The first call on each device looks the array up: make it before any
- * stream capture.  Same results as the scan behind fe_export_csr's row pointers. */
+ * stream capture.  That address is kept for the life of the process: after a
+ * cudaDeviceReset (or any teardown of the device's primary context) this entry point
+ * must not be called again in the same process.  Check offsets_dev[n] before using any
+ * offset: when it is -1 the running sums passed 2^31 - 1 and the offsets after that
+ * point have wrapped.  Same results as the scan behind fe_export_csr's row pointers. */
 int fe_scan_counts_noalloc(const int32_t *counts_dev, int32_t *offsets_dev, int64_t n, void *stream);
 
 #ifdef __cplusplus
