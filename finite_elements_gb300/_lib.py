@@ -22,6 +22,7 @@ FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
 FE_PREC_FP64, FE_PREC_MIXED, FE_PREC_MIXED_CG64 = 0, 1, 2
 FE_MODAL_SMALLEST, FE_MODAL_LARGEST = 0, 1
 FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP, FE_SOLVE_X0_IF_BETTER = 1, 2, 4
+FE_SOLVE_MULTIGRID = 8
 
 STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",
                 FE_NONFINITE: "FE_NONFINITE", FE_BAD_INPUT: "FE_BAD_INPUT",

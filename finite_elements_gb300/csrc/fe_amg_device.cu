@@ -1,0 +1,392 @@
+// Multigrid-preconditioned PCG on the device: the smoothed-aggregation hierarchy of
+// the eliminated system (set up on the host, fe_amg_setup.cu), uploaded, and a V-cycle
+// whose kernels are loops of the row operations of fe_amg_rows.cuh -- the operations
+// the host cycle fe_amg_vcycle_host runs serially.  FP64 throughout.
+//
+// WORK IN PROGRESS: not yet run on a GPU.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fe_amg.h"
+#include "fe_amg_rows.cuh"
+#include "fe_internal.h"
+
+namespace fe {
+namespace {
+
+constexpr int kAT = 256;
+inline int grid_a(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kAT - 1) / kAT, 152 * 8)); }
+
+struct DevCsr {
+    int64_t n = 0;
+    int rd = 0, cd = 0;
+    DBuf<int64_t> ptr;
+    DBuf<int32_t> col;
+    DBuf<double> val;
+};
+
+struct DevLevel {
+    DevCsr A, P, PT;
+    DBuf<double> dinv;
+    double lmax = 0.0;
+    DBuf<double> r, x, t, dir, zn;   // n * d each (r, x: the level's right-hand side and iterate)
+};
+
+struct DevAmg {
+    std::vector<DevLevel> L;
+    int64_t nc = 0;                  // coarsest DOFs
+    DBuf<double> cinv, rc, xc;
+    ~DevAmg() {
+        for (auto &l : L) {
+            dfree(l.A.ptr), dfree(l.A.col), dfree(l.A.val), dfree(l.P.ptr), dfree(l.P.col), dfree(l.P.val);
+            dfree(l.PT.ptr), dfree(l.PT.col), dfree(l.PT.val), dfree(l.dinv);
+            dfree(l.r), dfree(l.x), dfree(l.t), dfree(l.dir), dfree(l.zn);
+        }
+        dfree(cinv), dfree(rc), dfree(xc);
+    }
+};
+
+__global__ void ka_chebyshev(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                             const double *__restrict__ val, const double *__restrict__ dinv, int d,
+                             const double *__restrict__ r, const double *__restrict__ zin, double *__restrict__ dir,
+                             double *__restrict__ zout, double a, double b, int first) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        amg::row_chebyshev(ptr, col, val, dinv, d, r, zin, dir, zout, a, b, first != 0, i);
+}
+
+__global__ void ka_residual(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                            const double *__restrict__ val, int d, const double *__restrict__ r,
+                            const double *__restrict__ x, double *__restrict__ t) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        amg::row_residual(ptr, col, val, d, r, x, t, i);
+}
+
+__global__ void ka_restrict(int64_t nc, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                            const double *__restrict__ val, int m, int d, const double *__restrict__ t,
+                            double *__restrict__ rc) {
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nc; I += (int64_t)gridDim.x * blockDim.x)
+        amg::row_restrict(ptr, col, val, m, d, t, rc, I);
+}
+
+__global__ void ka_prolong_add(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                               const double *__restrict__ val, int d, int m, const double *__restrict__ xc,
+                               double *__restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        amg::row_prolong_add(ptr, col, val, d, m, xc, x, i);
+}
+
+// q = A p with the level-0 matrix (block rows of size d)
+__global__ void ka_spmv(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                        const double *__restrict__ val, int d, const double *__restrict__ p, double *__restrict__ q) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double out[6];
+        amg::row_product(ptr, col, val, d, d, p, i, out);
+        for (int k = 0; k < d; ++k) q[i * d + k] = out[k];
+    }
+}
+
+// x = Ainv r (dense, n x n)
+__global__ void ka_dense(int64_t n, const double *__restrict__ ainv, const double *__restrict__ r,
+                         double *__restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int64_t j = 0; j < n; ++j) acc += ainv[i * n + j] * r[j];
+        x[i] = acc;
+    }
+}
+
+// deterministic dot products: per-block partials, then one block in block order
+__device__ __forceinline__ double block_sum_a(double v) {
+    __shared__ double sh[kAT / 32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < kAT / 32 ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    __syncthreads();
+    return t;
+}
+
+__global__ void ka_dot(int64_t n, const double *__restrict__ a, const double *__restrict__ b, double *part) {
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    s = block_sum_a(s);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void ka_dot_final(int nb, const double *__restrict__ part, double *out) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) s += part[i];
+    s = block_sum_a(s);
+    if (threadIdx.x == 0) *out = s;
+}
+
+// x += alpha p, r -= alpha q
+__global__ void ka_update(int64_t n, double alpha, const double *__restrict__ p, const double *__restrict__ q,
+                          double *__restrict__ x, double *__restrict__ r) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = fma(alpha, p[i], x[i]);
+        r[i] = fma(-alpha, q[i], r[i]);
+    }
+}
+
+// p = z + beta p
+__global__ void ka_direction(int64_t n, double beta, const double *__restrict__ z, double *__restrict__ p) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fma(beta, p[i], z[i]);
+}
+
+int upload_csr(const BlockCsr &H, DevCsr &D, cudaStream_t s) {
+    D.n = H.n, D.rd = H.rd, D.cd = H.cd;
+    FE_CHECK(dalloc(D.ptr, H.ptr.size()));
+    FE_CHECK(dalloc(D.col, std::max<size_t>(H.col.size(), 1)));
+    FE_CHECK(dalloc(D.val, std::max<size_t>(H.val.size(), 1)));
+    FE_CUDA(cudaMemcpyAsync(D.ptr.p, H.ptr.data(), H.ptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    if (!H.col.empty()) {
+        FE_CUDA(cudaMemcpyAsync(D.col.p, H.col.data(), H.col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemcpyAsync(D.val.p, H.val.data(), H.val.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    return FE_OK;
+}
+
+// Chebyshev smoothing of level l into L.x (from zero, or from L.x with from_x0)
+int chebyshev_dev(fe_handle_s *h, DevLevel &L, int k, bool from_x0) {
+    cudaStream_t s = h->stream;
+    const int d = L.A.rd;
+    const int64_t n = L.A.n, nd = n * d;
+    const double hi = 1.05 * L.lmax, lo = hi / 30.0;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    if (!from_x0) FE_CUDA(cudaMemsetAsync(L.x.p, 0, nd * sizeof(double), s));
+    double *cur = L.x.p, *nxt = L.zn.p;
+    double rho = 1.0 / sigma;
+    ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.A.val.p, L.dinv.p, d, L.r.p, cur, L.dir.p, nxt,
+                                           0.0, 1.0 / theta, 1);
+    std::swap(cur, nxt);
+    for (int st = 1; st < k; ++st) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        const double a = rn * rho, b = 2.0 * rn / delta;
+        rho = rn;
+        ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.A.val.p, L.dinv.p, d, L.r.p, cur, L.dir.p,
+                                               nxt, a, b, 0);
+        std::swap(cur, nxt);
+    }
+    FE_LAUNCH_CHECK();
+    h->launches += k;
+    if (cur != L.x.p) FE_CUDA(cudaMemcpyAsync(L.x.p, cur, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return FE_OK;
+}
+
+// V-cycle on level l: L.r -> L.x
+int vcycle_dev(fe_handle_s *h, DevAmg &G, size_t l, int k) {
+    cudaStream_t s = h->stream;
+    if (l == G.L.size()) {
+        ka_dense<<<grid_a(G.nc), kAT, 0, s>>>(G.nc, G.cinv.p, G.rc.p, G.xc.p);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    DevLevel &L = G.L[l];
+    const int d = L.A.rd, m = L.P.cd;
+    const int64_t n = L.A.n;
+    FE_CHECK(chebyshev_dev(h, L, k, false));
+    ka_residual<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.A.val.p, d, L.r.p, L.x.p, L.t.p);
+    double *rc = l + 1 < G.L.size() ? G.L[l + 1].r.p : G.rc.p;
+    double *xc = l + 1 < G.L.size() ? G.L[l + 1].x.p : G.xc.p;
+    ka_restrict<<<grid_a(L.PT.n), kAT, 0, s>>>(L.PT.n, L.PT.ptr.p, L.PT.col.p, L.PT.val.p, m, d, L.t.p, rc);
+    FE_LAUNCH_CHECK();
+    h->launches += 2;
+    FE_CHECK(vcycle_dev(h, G, l + 1, k));
+    ka_prolong_add<<<grid_a(n), kAT, 0, s>>>(n, L.P.ptr.p, L.P.col.p, L.P.val.p, d, m, xc, L.x.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    return chebyshev_dev(h, L, k, true);
+}
+
+}  // namespace
+
+// PCG on the eliminated system preconditioned by one V-cycle (k = 3 Chebyshev steps per
+// smoothing), FP64, from x = 0 (opts.x0 is not used); the hierarchy is built on the
+// host from the device system matrix and the rigid-body (elasticity) or constant
+// (magnetostatics) modes, with the rows of the constrained DOFs zeroed.
+int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
+    cudaStream_t s = h->stream;
+    const int D = h->dim;
+    const int64_t n = h->n_nodes, nd = h->n_dof;
+    FE_CUDA(cudaEventRecord(h->events[6], s));
+    // the system matrix and the constrained DOFs on the host
+    std::vector<int32_t> ptr32((size_t)n + 1), col((size_t)std::max<int64_t>(h->nnzb, 1));
+    std::vector<double> val((size_t)std::max<int64_t>(h->nnzb * D * D, 1)), xy((size_t)n * h->cdim);
+    FE_CUDA(cudaMemcpyAsync(ptr32.data(), h->blk_ptr.p, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (h->nnzb > 0) {
+        FE_CUDA(cudaMemcpyAsync(col.data(), h->blk_col.p, h->nnzb * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaMemcpyAsync(val.data(), h->aval.p, h->nnzb * D * D * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    FE_CUDA(cudaMemcpyAsync(xy.data(), h->coords.p, xy.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    std::vector<int64_t> ptr(ptr32.begin(), ptr32.end());
+    const int m = D == 2 ? 3 : D == 3 ? 6 : 1;
+    std::vector<double> B((size_t)nd * m, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        const double x = xy[(size_t)i * h->cdim], y = xy[(size_t)i * h->cdim + 1];
+        const double z = h->cdim == 3 ? xy[(size_t)i * h->cdim + 2] : 0.0;
+        double *b = &B[(size_t)i * D * m];
+        if (D == 1) {
+            b[0] = 1.0;
+        } else if (D == 2) {
+            b[0 * m + 0] = 1.0, b[1 * m + 1] = 1.0, b[0 * m + 2] = -y, b[1 * m + 2] = x;
+        } else {
+            for (int k = 0; k < 3; ++k) b[k * m + k] = 1.0;
+            b[0 * m + 3] = -y, b[1 * m + 3] = x;
+            b[1 * m + 4] = -z, b[2 * m + 4] = y;
+            b[0 * m + 5] = z, b[2 * m + 5] = -x;
+        }
+    }
+    for (int64_t dof : h->bc_dof_host)
+        for (int j = 0; j < m; ++j) B[(size_t)dof * m + j] = 0.0;
+    fe_amg H = nullptr;
+    FE_CHECK(fe_amg_build_host(n, D, ptr.data(), col.data(), val.data(), m, B.data(), 0.08, 400, &H));
+    struct HostGuard {
+        fe_amg p;
+        ~HostGuard() { fe_amg_destroy(p); }
+    } hg{H};
+    // upload
+    DevAmg G;
+    G.L.resize(H->levels.size());
+    for (size_t l = 0; l < H->levels.size(); ++l) {
+        const AmgLevel &HL = H->levels[l];
+        DevLevel &L = G.L[l];
+        FE_CHECK(upload_csr(HL.A, L.A, s));
+        FE_CHECK(upload_csr(HL.P, L.P, s));
+        FE_CHECK(upload_csr(HL.PT, L.PT, s));
+        FE_CHECK(dalloc(L.dinv, std::max<size_t>(HL.dinv.size(), 1)));
+        FE_CUDA(cudaMemcpyAsync(L.dinv.p, HL.dinv.data(), HL.dinv.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        L.lmax = HL.lmax;
+        const size_t v = (size_t)std::max<int64_t>(HL.A.n * HL.A.rd, 1);
+        FE_CHECK(dalloc(L.r, v));
+        FE_CHECK(dalloc(L.x, v));
+        FE_CHECK(dalloc(L.t, v));
+        FE_CHECK(dalloc(L.dir, v));
+        FE_CHECK(dalloc(L.zn, v));
+    }
+    G.nc = H->coarse.n * H->coarse.rd;
+    FE_CHECK(dalloc(G.cinv, std::max<size_t>(H->coarse_inv.size(), 1)));
+    FE_CHECK(dalloc(G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
+    FE_CHECK(dalloc(G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
+    if (!H->coarse_inv.empty())
+        FE_CUDA(cudaMemcpyAsync(G.cinv.p, H->coarse_inv.data(), H->coarse_inv.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, s));
+    if (G.L.empty()) {
+        set_error("fe_solve: the multigrid hierarchy has a single level (use the other preconditioners)");
+        return FE_BAD_INPUT;
+    }
+    // PCG: level 0's r and x hold the V-cycle's input and output
+    DevLevel &L0 = G.L[0];
+    DBuf<double> r, p, q, part, sc;
+    struct Free {
+        DBuf<double> *b[5];
+        ~Free() {
+            for (auto *x : b) dfree(*x);
+        }
+    } fg{{&r, &p, &q, &part, &sc}};
+    const int gn = grid_a(nd);
+    FE_CHECK(dalloc(h->w.x, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(dalloc(r, (size_t)nd));
+    FE_CHECK(dalloc(p, (size_t)nd));
+    FE_CHECK(dalloc(q, (size_t)nd));
+    FE_CHECK(dalloc(part, (size_t)gn));
+    FE_CHECK(dalloc(sc, 4));
+    double *x = h->w.x.p;
+    auto dot = [&](const double *a, const double *b, double *out) -> int {
+        ka_dot<<<gn, kAT, 0, s>>>(nd, a, b, part.p);
+        ka_dot_final<<<1, kAT, 0, s>>>(gn, part.p, out);
+        FE_LAUNCH_CHECK();
+        h->launches += 2;
+        return FE_OK;
+    };
+    auto precond = [&]() -> int {   // L0.x = M^-1 r
+        FE_CUDA(cudaMemcpyAsync(L0.r.p, r.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        return vcycle_dev(h, G, 0, 3);
+    };
+    FE_CUDA(cudaMemsetAsync(x, 0, nd * sizeof(double), s));
+    FE_CUDA(cudaMemcpyAsync(r.p, h->b.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    FE_CHECK(precond());
+    FE_CUDA(cudaMemcpyAsync(p.p, L0.x.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    FE_CHECK(dot(r.p, L0.x.p, sc.p));
+    FE_CHECK(dot(r.p, r.p, sc.p + 1));
+    double host[4];
+    FE_CUDA(cudaMemcpyAsync(host, sc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    double rz = host[0];
+    const double bb = host[1];
+    const double tol = o->tol > 0 ? o->tol : 1e-10;
+    const int max_iter = o->max_iter > 0 ? o->max_iter : 10000;
+    int it = 0, status = bb > 0.0 ? FE_MAXITER : FE_OK;
+    double rr = bb;
+    while (status == FE_MAXITER && it < max_iter) {
+        ka_spmv<<<grid_a(n), kAT, 0, s>>>(n, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, p.p, q.p);
+        FE_LAUNCH_CHECK();
+        FE_CHECK(dot(p.p, q.p, sc.p + 2));
+        FE_CUDA(cudaMemcpyAsync(host + 2, sc.p + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        if (!(host[2] > 0.0) || !std::isfinite(host[2])) {
+            status = std::isfinite(host[2]) ? FE_BREAKDOWN : FE_NONFINITE;
+            break;
+        }
+        const double alpha = rz / host[2];
+        ka_update<<<gn, kAT, 0, s>>>(nd, alpha, p.p, q.p, x, r.p);
+        FE_LAUNCH_CHECK();
+        h->launches += 2;
+        ++it;
+        FE_CHECK(dot(r.p, r.p, sc.p + 1));
+        FE_CHECK(precond());
+        FE_CHECK(dot(r.p, L0.x.p, sc.p));
+        FE_CUDA(cudaMemcpyAsync(host, sc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        rr = host[1];
+        if (!std::isfinite(rr) || !std::isfinite(host[0])) {
+            status = FE_NONFINITE;
+            break;
+        }
+        if (rr <= tol * tol * bb) {
+            status = FE_OK;
+            break;
+        }
+        const double beta = host[0] / rz;
+        rz = host[0];
+        ka_direction<<<gn, kAT, 0, s>>>(nd, beta, L0.x.p, p.p);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+    }
+    // true residual b - A x in FP64
+    ka_residual<<<grid_a(n), kAT, 0, s>>>(n, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, h->b.p, x, q.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    FE_CHECK(dot(q.p, q.p, sc.p + 3));
+    FE_CUDA(cudaMemcpyAsync(host + 3, sc.p + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    rr = host[3];
+    st->iterations = it;
+    st->spmv = it + 1;
+    st->outer = 0;
+    st->fp64_iterations = 0;
+    st->x0_used = 0;
+    st->bnorm = std::sqrt(bb);
+    st->relres = bb > 0.0 ? std::sqrt(std::max(rr, 0.0) / bb) : 0.0;
+    st->status = status;
+    FE_CHECK(recover_multipliers(h));
+    FE_CUDA(cudaEventRecord(h->events[7], s));
+    FE_CUDA(cudaEventSynchronize(h->events[7]));
+    float ms = 0;
+    FE_CUDA(cudaEventElapsedTime(&ms, h->events[6], h->events[7]));
+    st->solve_ms = ms;
+    st->assemble_ms = h->last_assemble_ms;
+    h->have_solution = true;
+    return FE_OK;
+}
+
+}  // namespace fe

@@ -22,6 +22,7 @@
 #include <thread>
 #include <vector>
 
+#include "fe_amg.h"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
@@ -53,24 +54,6 @@ void parallel_chunks(int64_t n, F f) {
     run(0);
     for (auto &x : th) x.join();
 }
-
-struct BlockCsr {
-    int64_t n = 0;             // block rows
-    int rd = 0, cd = 0;        // block size rd x cd
-    std::vector<int64_t> ptr;  // n + 1
-    std::vector<int32_t> col;
-    std::vector<double> val;   // nnzb * rd * cd, row-major blocks
-    int64_t nnzb() const { return (int64_t)col.size(); }
-};
-
-struct AmgLevel {
-    BlockCsr A;                 // d x d blocks
-    BlockCsr P;                 // d x m blocks, columns = aggregates
-    BlockCsr PT;                // m x d blocks: the restriction
-    std::vector<double> dinv;   // block-diagonal pseudo-inverse of A
-    std::vector<int32_t> agg;   // aggregate of each node
-    double lmax = 0.0;
-};
 
 // Pseudo-inverse of a symmetric d x d block by cyclic Jacobi: V diag(1/l) V^T over the
 // eigenvalues above 1e-12 of the largest in magnitude.
@@ -378,11 +361,7 @@ bool dense_inverse(std::vector<double> a, int n, std::vector<double> &inv) {
 }  // namespace
 }  // namespace fe
 
-struct fe_amg_s {
-    std::vector<fe::AmgLevel> levels;
-    fe::BlockCsr coarse;
-    std::vector<double> coarse_inv;   // dense inverse of the coarsest matrix + 1e-12 max|diag| I
-};
+
 
 namespace fe {
 namespace {

@@ -280,6 +280,8 @@ int recover_multipliers(fe_handle_s *h);
 // Continuity conditions (fe_continuity.cu): host set-up and the projected FP64 PCG
 int set_continuity(fe_handle_s *h, int64_t n, const int64_t *dof1, const int64_t *dof2, const double *value);
 int solve_continuity(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
+// FP64 PCG with a smoothed-aggregation V-cycle preconditioner (fe_amg_device.cu)
+int solve_multigrid(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
 int set_rhs_additions(fe_handle_s *h, int64_t n, const int64_t *dof, const double *value);
 int apply_rhs_additions(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);

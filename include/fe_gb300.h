@@ -64,6 +64,9 @@ extern "C" {
 #define FE_SOLVE_RESTART_EACH_STEP 2   /* mixed: restart the Krylov space at every refinement
                                           step (classic iterative refinement) instead of
                                           continuing along the current direction          */
+#define FE_SOLVE_MULTIGRID        8    /* FP64 PCG preconditioned by a smoothed-aggregation
+                                          V-cycle (hierarchy set up on the host); work in
+                                          progress, not yet run on a GPU                    */
 
 /* solver precision */
 #define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
