@@ -264,12 +264,6 @@ int fe_post_elastic(fe_handle h, const double *u_host, double *strain_host, doub
                     double *energy_host);
 int fe_post_magnetic(fe_handle h, const double *a_host, double *field_host);
 
-/* ---- learned warm start (no counterpart in the reference: an addition on top of the
- * PCG that replaces spsolve in analysis.py:816-830; PCG from its x0 still decides
- * the accuracy).  A graph network over the mesh nodes (6 message-passing layers,
- * hidden width 64, BF16 tensor-core GEMMs with FP32 accumulation) predicts the shape
- * u_hat of the displacement; x0 = g + s u_hat with s the A-norm optimal scale.
- * Elasticity meshes only. */
 /* ---- smoothed-aggregation multigrid setup on the host (no counterpart in the
  * reference, which factorises directly; the setup stage of a multilevel preconditioner
  * for the device solve).  Input: the node-block CSR of a symmetric system matrix
@@ -294,6 +288,12 @@ int fe_amg_level_aggregates(fe_amg a, int32_t level, int32_t *agg_host);
 int fe_amg_vcycle_host(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
 int fe_amg_destroy(fe_amg a);
 
+/* ---- learned warm start (no counterpart in the reference: an addition on top of the
+ * PCG that replaces spsolve in analysis.py:816-830; PCG from its x0 still decides
+ * the accuracy).  A graph network over the mesh nodes (6 message-passing layers,
+ * hidden width 64, BF16 tensor-core GEMMs with FP32 accumulation) predicts the shape
+ * u_hat of the displacement; x0 = g + s u_hat with s the A-norm optimal scale.
+ * Elasticity meshes only. */
 typedef struct fe_gnn_s *fe_gnn;
 int fe_gnn_create(fe_gnn *out);
 int fe_gnn_destroy(fe_gnn g);

@@ -3,7 +3,7 @@ systems of this path.
 
 TEST INFRASTRUCTURE ONLY.  Nothing in ``finite_elements_gb300`` imports this module.
 The reference solves with a direct factorisation (scipy spsolve, analysis.py:798-830)
-and has no multigrid; this model is the checker for a device multilevel
+and has no multigrid; this model is the oracle for a device multilevel
 preconditioner, the step beyond the Chebyshev preconditioner on the device.  It
 restates published smoothed aggregation (Vanek, Mandel and Brezina, "Algebraic
 multigrid by smoothed aggregation for second and fourth order elliptic problems",

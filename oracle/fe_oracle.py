@@ -1,7 +1,7 @@
 """CPU oracle for the finite_elements assembly-and-solve path.
 
 TEST INFRASTRUCTURE ONLY.  Nothing in ``finite_elements_gb300`` imports this module:
-it is the checker that ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
+it is the oracle that ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
 legs of ``bench.py`` compare the CUDA path against.
 
 It restates, in numpy, what the reference computes (file:line of the reference
