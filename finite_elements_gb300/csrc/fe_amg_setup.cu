@@ -19,10 +19,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <thread>
 #include <vector>
 
 #include "fe_amg.h"
+#include "fe_amg_par.cuh"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
@@ -418,6 +420,239 @@ void vcycle_host(const fe_amg_s *h, size_t l, int k, const std::vector<double> &
     chebyshev_host(L, k, r, x, true);
 }
 
+
+// Dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal entry
+// (zero rows of rank-deficient aggregates).
+int coarse_inverse(fe_amg_s *h, const char *who) {
+    const BlockCsr &C = h->coarse;
+    const int64_t n = C.n * C.rd;
+    if (n > 4096) {
+        set_error(std::string(who) + ": coarsest level too large for its dense solve");
+        return FE_BAD_INPUT;
+    }
+    std::vector<double> dense((size_t)n * n, 0.0);
+    double dmax = 0.0;
+    const int cd = C.rd;
+    for (int64_t i = 0; i < C.n; ++i)
+        for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
+            for (int a = 0; a < cd; ++a)
+                for (int b = 0; b < cd; ++b) {
+                    const double v = C.val[(size_t)s * cd * cd + a * cd + b];
+                    dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
+                }
+    for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
+    for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
+    if (n > 0 && !dense_inverse(dense, (int)n, h->coarse_inv)) {
+        set_error(std::string(who) + ": singular coarsest matrix");
+        return FE_BREAKDOWN;
+    }
+    return FE_OK;
+}
+
+// ---------------------------------------------------------------- parallel setup (host)
+// The passes of the device setup, run over the rows with the row operations of
+// fe_amg_par.cuh: every pass reads what earlier passes wrote, so its rows are
+// independent and the result is the same in any row order.
+
+// Exclusive prefix sum of counts into offsets (n + 1 values).
+std::vector<int64_t> offsets_of(const std::vector<int64_t> &cnt) {
+    std::vector<int64_t> off(cnt.size() + 1, 0);
+    for (size_t i = 0; i < cnt.size(); ++i) off[i + 1] = off[i] + cnt[i];
+    return off;
+}
+
+// C = A B row by row: bound, sorted distinct columns, values.
+BlockCsr product_rows(const BlockCsr &A, const BlockCsr &B) {
+    BlockCsr C;
+    C.n = A.n, C.rd = A.rd, C.cd = B.cd;
+    std::vector<int64_t> bound((size_t)A.n), cnt((size_t)A.n);
+    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i) bound[i] = amg::row_product_bound(A.ptr.data(), A.col.data(), B.ptr.data(), i);
+    });
+    const std::vector<int64_t> boff = offsets_of(bound);
+    std::vector<int32_t> cand((size_t)std::max<int64_t>(boff.back(), 1));
+    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
+            cnt[i] = amg::row_product_columns(A.ptr.data(), A.col.data(), B.ptr.data(), B.col.data(), i,
+                                              cand.data() + boff[i]);
+    });
+    C.ptr = offsets_of(cnt);
+    C.col.resize((size_t)C.ptr.back());
+    C.val.resize((size_t)C.ptr.back() * C.rd * C.cd);
+    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i) {
+            std::copy(cand.begin() + boff[i], cand.begin() + boff[i] + cnt[i], C.col.begin() + C.ptr[i]);
+            amg::row_product_values(A.ptr.data(), A.col.data(), A.val.data(), A.rd, A.cd, B.ptr.data(), B.col.data(),
+                                    B.val.data(), B.cd, C.ptr.data(), C.col.data(), C.val.data(), i);
+        }
+    });
+    return C;
+}
+
+// P^T from P, A's pattern and the aggregates' member lists.
+BlockCsr restriction_rows(const BlockCsr &A, const BlockCsr &P, const std::vector<int64_t> &mptr,
+                          const std::vector<int32_t> &mem, int64_t na) {
+    BlockCsr R;
+    R.n = na, R.rd = P.cd, R.cd = P.rd;
+    std::vector<int64_t> bound((size_t)na), cnt((size_t)na);
+    parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t c = lo; c < hi; ++c) bound[c] = amg::row_restriction_bound(mptr.data(), mem.data(), A.ptr.data(), c);
+    });
+    const std::vector<int64_t> boff = offsets_of(bound);
+    std::vector<int32_t> cand((size_t)std::max<int64_t>(boff.back(), 1));
+    parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t c = lo; c < hi; ++c)
+            cnt[c] = amg::row_restriction_columns(mptr.data(), mem.data(), A.ptr.data(), A.col.data(), c,
+                                                  cand.data() + boff[c]);
+    });
+    R.ptr = offsets_of(cnt);
+    R.col.resize((size_t)R.ptr.back());
+    R.val.resize((size_t)R.ptr.back() * R.rd * R.cd);
+    parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t c = lo; c < hi; ++c) {
+            std::copy(cand.begin() + boff[c], cand.begin() + boff[c] + cnt[c], R.col.begin() + R.ptr[c]);
+            amg::row_restriction_values(R.ptr.data(), R.col.data(), R.val.data(), P.ptr.data(), P.col.data(),
+                                        P.val.data(), P.rd, P.cd, c);
+        }
+    });
+    return R;
+}
+
+// Aggregates by the distance-2 independent set; agg[i] for every node, the roots in
+// aggregate order.  Returns the number of rounds, or -1 if a node was left out.
+int aggregate_parallel(const BlockCsr &A, double theta, std::vector<int32_t> &agg, std::vector<int32_t> &roots,
+                       std::vector<double> &nrm, std::vector<uint8_t> &strong) {
+    const int64_t n = A.n;
+    const int d = A.rd;
+    nrm.assign((size_t)A.nnzb(), 0.0);
+    strong.assign((size_t)A.nnzb(), 0);
+    std::vector<double> dg((size_t)n);
+    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
+            amg::row_block_norms(A.ptr.data(), A.col.data(), A.val.data(), d, i, nrm.data(), dg.data());
+    });
+    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
+            amg::row_strength(A.ptr.data(), A.col.data(), nrm.data(), dg.data(), theta, i, strong.data());
+    });
+    std::vector<uint32_t> state((size_t)n, amg::kUndecided);
+    std::vector<uint64_t> key((size_t)n), m1((size_t)n), m2((size_t)n);
+    int64_t part[kChunks];
+    int rounds = 0;
+    for (;;) {
+        ++rounds;
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i) key[i] = amg::mis_key(state[i], i);
+        });
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i)
+                amg::row_max_key(A.ptr.data(), A.col.data(), strong.data(), key.data(), i, m1.data());
+        });
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i)
+                amg::row_max_key(A.ptr.data(), A.col.data(), strong.data(), m1.data(), i, m2.data());
+        });
+        for (int c = 0; c < kChunks; ++c) part[c] = 0;
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int c) {
+            int64_t u = 0;
+            for (int64_t i = lo; i < hi; ++i) u += amg::mis_decide(m2.data(), i, state.data());
+            part[c] = u;
+        });
+        int64_t undecided = 0;
+        for (int c = 0; c < kChunks; ++c) undecided += part[c];
+        if (undecided == 0) break;
+    }
+    std::vector<int32_t> rank((size_t)n, -1);
+    roots.clear();
+    for (int64_t i = 0; i < n; ++i)
+        if (state[i] == amg::kIn) rank[i] = (int32_t)roots.size(), roots.push_back((int32_t)i);
+    std::vector<int32_t> agg1((size_t)n);
+    agg.assign((size_t)n, -1);
+    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
+            amg::row_join_root(A.ptr.data(), A.col.data(), strong.data(), nrm.data(), state.data(), rank.data(), i,
+                               agg1.data());
+    });
+    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+        for (int64_t i = lo; i < hi; ++i)
+            amg::row_join_neighbour(A.ptr.data(), A.col.data(), strong.data(), nrm.data(), agg1.data(), i,
+                                    agg.data());
+    });
+    for (int64_t i = 0; i < n; ++i)
+        if (agg[i] < 0) return -1;
+    return rounds;
+}
+
+// The hierarchy by the parallel passes.  Returns FE_OK or a failure status.
+int build_parallel(fe_amg_s *h, BlockCsr A, std::vector<double> B, int bm, double theta, int64_t coarse_dofs) {
+    while (A.n * A.rd > coarse_dofs && h->levels.size() < 12) {
+        AmgLevel L;
+        const int dd = A.rd;
+        std::vector<double> dinv = block_diag_pinv(A);
+        L.lmax = lmax_power(A, dinv);
+        std::vector<int32_t> roots;
+        std::vector<double> nrm;
+        std::vector<uint8_t> strong;
+        if (aggregate_parallel(A, theta, L.agg, roots, nrm, strong) < 0) {
+            set_error("fe_amg_build_parallel_host: a node was left without an aggregate");
+            return FE_BREAKDOWN;
+        }
+        const int64_t na = (int64_t)roots.size();
+        // member lists in increasing node order
+        std::vector<int64_t> bound((size_t)na), cnt((size_t)na);
+        parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t c = lo; c < hi; ++c) bound[c] = amg::agg_member_bound(A.ptr.data(), A.col.data(), roots.data(), c);
+        });
+        const std::vector<int64_t> boff = offsets_of(bound);
+        std::vector<int32_t> cand((size_t)std::max<int64_t>(boff.back(), 1));
+        parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t c = lo; c < hi; ++c)
+                cnt[c] = amg::agg_members(A.ptr.data(), A.col.data(), roots.data(), L.agg.data(), c, cand.data() + boff[c]);
+        });
+        const std::vector<int64_t> mptr = offsets_of(cnt);
+        if (mptr.back() != A.n) {
+            set_error("fe_amg_build_parallel_host: aggregate members do not cover the nodes");
+            return FE_BREAKDOWN;
+        }
+        std::vector<int32_t> mem((size_t)A.n);
+        for (int64_t c = 0; c < na; ++c)
+            std::copy(cand.begin() + boff[c], cand.begin() + boff[c] + cnt[c], mem.begin() + mptr[c]);
+        // tentative prolongator: one QR per aggregate, in place on B's rows
+        BlockCsr Pt;
+        Pt.n = A.n, Pt.rd = dd, Pt.cd = bm;
+        Pt.ptr.resize((size_t)A.n + 1);
+        for (int64_t i = 0; i <= A.n; ++i) Pt.ptr[i] = i;
+        Pt.col.assign(L.agg.begin(), L.agg.end());
+        Pt.val = B;
+        std::vector<double> Bc((size_t)na * bm * bm);
+        parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t c = lo; c < hi; ++c)
+                amg::aggregate_qr(mem.data() + mptr[c], mptr[c + 1] - mptr[c], dd, bm, Pt.val.data(),
+                                  Bc.data() + (size_t)c * bm * bm);
+        });
+        // smoothed prolongator and Galerkin product
+        BlockCsr P = product_rows(A, Pt);
+        const double w = 4.0 / (3.0 * L.lmax);
+        parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i)
+                amg::row_smooth_prolongator(P.ptr.data(), P.col.data(), P.val.data(), dinv.data(), Pt.val.data(),
+                                            L.agg.data(), dd, bm, w, i);
+        });
+        BlockCsr AP = product_rows(A, P);
+        BlockCsr PT = restriction_rows(A, P, mptr, mem, na);
+        BlockCsr Ac = product_rows(PT, AP);
+        L.A = std::move(A);
+        L.P = std::move(P);
+        L.PT = std::move(PT);
+        L.dinv = std::move(dinv);
+        h->levels.push_back(std::move(L));
+        A = std::move(Ac);
+        B.swap(Bc);
+    }
+    h->coarse = std::move(A);
+    return coarse_inverse(h, "fe_amg_build_parallel_host");
+}
+
 }  // namespace
 }  // namespace fe
 
@@ -514,33 +749,37 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
         (void)bm;
     }
     h->coarse = std::move(A);
-    {
-        // dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal
-        // entry (zero rows of rank-deficient aggregates)
-        const BlockCsr &C = h->coarse;
-        const int64_t n = C.n * C.rd;
-        if (n > 4096) {
-            fe_amg_destroy(h);
-            set_error("fe_amg_build_host: coarsest level too large for its dense solve");
-            return FE_BAD_INPUT;
-        }
-        std::vector<double> dense((size_t)n * n, 0.0);
-        double dmax = 0.0;
-        const int cd = C.rd;
-        for (int64_t i = 0; i < C.n; ++i)
-            for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
-                for (int a = 0; a < cd; ++a)
-                    for (int b = 0; b < cd; ++b) {
-                        const double v = C.val[(size_t)s * cd * cd + a * cd + b];
-                        dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
-                    }
-        for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
-        for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
-        if (n > 0 && !dense_inverse(dense, (int)n, h->coarse_inv)) {
-            fe_amg_destroy(h);
-            set_error("fe_amg_build_host: singular coarsest matrix");
-            return FE_BREAKDOWN;
-        }
+    const int st = coarse_inverse(h, "fe_amg_build_host");
+    if (st != FE_OK) {
+        fe_amg_destroy(h);
+        return st;
+    }
+    *out = h;
+    return FE_OK;
+}
+
+// The same hierarchy inputs, set up by the parallel passes of the device setup
+// (independent-set aggregation, row-wise products) run on the host.
+int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
+                               const double *vals, int32_t m, const double *nullspace, double theta,
+                               int64_t coarse_dofs, fe_amg *out) {
+    if (!out || n_nodes < 0 || d < 1 || d > 6 || m < 1 || m > 6 || (n_nodes > 0 && (!blk_ptr || !blk_col ||
+                                                                                     !vals || !nullspace))) {
+        set_error("fe_amg_build_parallel_host: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    *out = nullptr;
+    fe_amg_s *h = new fe_amg_s();
+    BlockCsr A;
+    A.n = n_nodes, A.rd = A.cd = d;
+    A.ptr.assign(blk_ptr, blk_ptr + n_nodes + 1);
+    A.col.assign(blk_col, blk_col + A.ptr[n_nodes]);
+    A.val.assign(vals, vals + (size_t)A.ptr[n_nodes] * d * d);
+    std::vector<double> B(nullspace, nullspace + (size_t)n_nodes * d * m);
+    const int st = build_parallel(h, std::move(A), std::move(B), m, theta, coarse_dofs);
+    if (st != FE_OK) {
+        fe_amg_destroy(h);
+        return st;
     }
     *out = h;
     return FE_OK;

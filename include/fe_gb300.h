@@ -276,6 +276,15 @@ typedef struct fe_amg_s *fe_amg;
 int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
                       const double *vals, int32_t m, const double *nullspace, double theta,
                       int64_t coarse_dofs, fe_amg *out);
+/* The same, set up by the passes of the device setup run on the host: aggregates from a
+ * distance-2 maximal independent set of the strong graph (rounds of (state, hash,
+ * index) maxima over two hops; every node then joins the strongest root next to it, the
+ * rest the strongest neighbour that joined), one QR per aggregate, row-wise sparse
+ * products (sorted distinct columns, then the values).  Its result does not depend on
+ * the order in which rows are processed. */
+int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
+                               const double *vals, int32_t m, const double *nullspace, double theta,
+                               int64_t coarse_dofs, fe_amg *out);
 int fe_amg_levels(fe_amg a, int32_t *n_levels);
 int fe_amg_level_info(fe_amg a, int32_t level, int64_t *n_nodes, int32_t *d, int64_t *nnzb_A,
                       int64_t *nnzb_P, int64_t *n_coarse, int32_t *m, double *lmax);
