@@ -114,6 +114,7 @@ _SIGNATURES = {
     "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
     "fe_amg_build_host": ([_I64, _I32, _P, _P, _P, _I32, _P, _D, _I64, C.POINTER(_P)], C.c_int),
     "fe_amg_build_parallel_host": ([_I64, _I32, _P, _P, _P, _I32, _P, _D, _I64, C.POINTER(_P)], C.c_int),
+    "fe_amg_build_device": ([_P, _D, _I64, C.POINTER(_P)], C.c_int),
     "fe_amg_levels": ([_P, _PI32], C.c_int),
     "fe_amg_level_info": ([_P, _I32, _PI64, _PI32, _PI64, _PI64, _PI64, _PI32, _PD], C.c_int),
     "fe_amg_level_matrix": ([_P, _I32, _I32, _P, _P, _P], C.c_int),

@@ -1,0 +1,56 @@
+// The smoothed-aggregation hierarchy in device memory: set up by fe_amg_device_setup.cu,
+// applied as a V-cycle by fe_amg_device.cu.
+#pragma once
+
+#include <vector>
+
+#include "fe_amg.h"
+#include "fe_internal.h"
+
+namespace fe {
+
+struct DevCsr {
+    int64_t n = 0;
+    int rd = 0, cd = 0;
+    DBuf<int64_t> ptr;   // n + 1
+    DBuf<int32_t> col;
+    DBuf<double> val;    // row-major rd x cd blocks
+    int64_t nnzb = 0;
+    void release() { dfree(ptr), dfree(col), dfree(val); }
+};
+
+struct DevLevel {
+    DevCsr A, P, PT;
+    DBuf<double> dinv;
+    DBuf<int32_t> agg;
+    double lmax = 0.0;
+    DBuf<double> r, x, t, dir, zn;   // n * d each (r, x: the level's right-hand side and iterate)
+    void release() {
+        A.release(), P.release(), PT.release();
+        dfree(dinv), dfree(agg), dfree(r), dfree(x), dfree(t), dfree(dir), dfree(zn);
+    }
+};
+
+struct DevAmg {
+    std::vector<DevLevel> L;
+    DevCsr coarse;
+    int64_t nc = 0;                  // coarsest DOFs
+    DBuf<double> cinv, rc, xc;
+    int mis_rounds = 0;              // independent-set rounds, all levels
+    ~DevAmg() {
+        for (auto &l : L) l.release();
+        coarse.release();
+        dfree(cinv), dfree(rc), dfree(xc);
+    }
+};
+
+// Device setup of the hierarchy of the handle's eliminated system (near-null space: the
+// rigid-body modes for elasticity, the constant for magnetostatics, zero on the
+// constrained DOFs), the same passes as fe_amg_build_parallel_host.
+int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G);
+// Copy of a device hierarchy into host form (accessors of the fe_amg_* ABI).
+int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s);
+// Dense inverse of the coarsest matrix (+ 1e-12 of its largest diagonal entry).
+int coarse_inverse_of(const BlockCsr &C, std::vector<double> &inv, const char *who);
+
+}  // namespace fe

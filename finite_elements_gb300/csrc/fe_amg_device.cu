@@ -1,5 +1,5 @@
 // Multigrid-preconditioned PCG on the device: the smoothed-aggregation hierarchy of
-// the eliminated system (set up on the host, fe_amg_setup.cu), uploaded, and a V-cycle
+// the eliminated system (set up on the device, fe_amg_device_setup.cu) and a V-cycle
 // whose kernels are loops of the row operations of fe_amg_rows.cuh -- the operations
 // the host cycle fe_amg_vcycle_host runs serially.  FP64 throughout.
 //
@@ -8,7 +8,7 @@
 #include <cmath>
 #include <vector>
 
-#include "fe_amg.h"
+#include "fe_amg_dev.h"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
@@ -17,35 +17,6 @@ namespace {
 
 constexpr int kAT = 256;
 inline int grid_a(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kAT - 1) / kAT, 152 * 8)); }
-
-struct DevCsr {
-    int64_t n = 0;
-    int rd = 0, cd = 0;
-    DBuf<int64_t> ptr;
-    DBuf<int32_t> col;
-    DBuf<double> val;
-};
-
-struct DevLevel {
-    DevCsr A, P, PT;
-    DBuf<double> dinv;
-    double lmax = 0.0;
-    DBuf<double> r, x, t, dir, zn;   // n * d each (r, x: the level's right-hand side and iterate)
-};
-
-struct DevAmg {
-    std::vector<DevLevel> L;
-    int64_t nc = 0;                  // coarsest DOFs
-    DBuf<double> cinv, rc, xc;
-    ~DevAmg() {
-        for (auto &l : L) {
-            dfree(l.A.ptr), dfree(l.A.col), dfree(l.A.val), dfree(l.P.ptr), dfree(l.P.col), dfree(l.P.val);
-            dfree(l.PT.ptr), dfree(l.PT.col), dfree(l.PT.val), dfree(l.dinv);
-            dfree(l.r), dfree(l.x), dfree(l.t), dfree(l.dir), dfree(l.zn);
-        }
-        dfree(cinv), dfree(rc), dfree(xc);
-    }
-};
 
 __global__ void ka_chebyshev(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
                              const double *__restrict__ val, const double *__restrict__ dinv, int d,
@@ -141,19 +112,6 @@ __global__ void ka_direction(int64_t n, double beta, const double *__restrict__ 
         p[i] = fma(beta, p[i], z[i]);
 }
 
-int upload_csr(const BlockCsr &H, DevCsr &D, cudaStream_t s) {
-    D.n = H.n, D.rd = H.rd, D.cd = H.cd;
-    FE_CHECK(dalloc(D.ptr, H.ptr.size()));
-    FE_CHECK(dalloc(D.col, std::max<size_t>(H.col.size(), 1)));
-    FE_CHECK(dalloc(D.val, std::max<size_t>(H.val.size(), 1)));
-    FE_CUDA(cudaMemcpyAsync(D.ptr.p, H.ptr.data(), H.ptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    if (!H.col.empty()) {
-        FE_CUDA(cudaMemcpyAsync(D.col.p, H.col.data(), H.col.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemcpyAsync(D.val.p, H.val.data(), H.val.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-    }
-    return FE_OK;
-}
-
 // Chebyshev smoothing of level l into L.x (from zero, or from L.x with from_x0)
 int chebyshev_dev(fe_handle_s *h, DevLevel &L, int k, bool from_x0) {
     cudaStream_t s = h->stream;
@@ -218,68 +176,19 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     const int D = h->dim;
     const int64_t n = h->n_nodes, nd = h->n_dof;
     FE_CUDA(cudaEventRecord(h->events[6], s));
-    // the system matrix and the constrained DOFs on the host
-    std::vector<int32_t> ptr32((size_t)n + 1), col((size_t)std::max<int64_t>(h->nnzb, 1));
-    std::vector<double> val((size_t)std::max<int64_t>(h->nnzb * D * D, 1)), xy((size_t)n * h->cdim);
-    FE_CUDA(cudaMemcpyAsync(ptr32.data(), h->blk_ptr.p, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    if (h->nnzb > 0) {
-        FE_CUDA(cudaMemcpyAsync(col.data(), h->blk_col.p, h->nnzb * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        FE_CUDA(cudaMemcpyAsync(val.data(), h->aval.p, h->nnzb * D * D * sizeof(double), cudaMemcpyDeviceToHost, s));
-    }
-    FE_CUDA(cudaMemcpyAsync(xy.data(), h->coords.p, xy.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    std::vector<int64_t> ptr(ptr32.begin(), ptr32.end());
-    const int m = D == 2 ? 3 : D == 3 ? 6 : 1;
-    std::vector<double> B((size_t)nd * m, 0.0);
-    for (int64_t i = 0; i < n; ++i) {
-        const double x = xy[(size_t)i * h->cdim], y = xy[(size_t)i * h->cdim + 1];
-        const double z = h->cdim == 3 ? xy[(size_t)i * h->cdim + 2] : 0.0;
-        double *b = &B[(size_t)i * D * m];
-        if (D == 1) {
-            b[0] = 1.0;
-        } else if (D == 2) {
-            b[0 * m + 0] = 1.0, b[1 * m + 1] = 1.0, b[0 * m + 2] = -y, b[1 * m + 2] = x;
-        } else {
-            for (int k = 0; k < 3; ++k) b[k * m + k] = 1.0;
-            b[0 * m + 3] = -y, b[1 * m + 3] = x;
-            b[1 * m + 4] = -z, b[2 * m + 4] = y;
-            b[0 * m + 5] = z, b[2 * m + 5] = -x;
-        }
-    }
-    for (int64_t dof : h->bc_dof_host)
-        for (int j = 0; j < m; ++j) B[(size_t)dof * m + j] = 0.0;
-    fe_amg H = nullptr;
-    FE_CHECK(fe_amg_build_host(n, D, ptr.data(), col.data(), val.data(), m, B.data(), 0.08, 400, &H));
-    struct HostGuard {
-        fe_amg p;
-        ~HostGuard() { fe_amg_destroy(p); }
-    } hg{H};
-    // upload
+    // the hierarchy, set up on the device, and the cycle's vectors
     DevAmg G;
-    G.L.resize(H->levels.size());
-    for (size_t l = 0; l < H->levels.size(); ++l) {
-        const AmgLevel &HL = H->levels[l];
-        DevLevel &L = G.L[l];
-        FE_CHECK(upload_csr(HL.A, L.A, s));
-        FE_CHECK(upload_csr(HL.P, L.P, s));
-        FE_CHECK(upload_csr(HL.PT, L.PT, s));
-        FE_CHECK(dalloc(L.dinv, std::max<size_t>(HL.dinv.size(), 1)));
-        FE_CUDA(cudaMemcpyAsync(L.dinv.p, HL.dinv.data(), HL.dinv.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-        L.lmax = HL.lmax;
-        const size_t v = (size_t)std::max<int64_t>(HL.A.n * HL.A.rd, 1);
+    FE_CHECK(amg_setup_device(h, 0.08, 400, G));
+    for (auto &L : G.L) {
+        const size_t v = (size_t)std::max<int64_t>(L.A.n * L.A.rd, 1);
         FE_CHECK(dalloc(L.r, v));
         FE_CHECK(dalloc(L.x, v));
         FE_CHECK(dalloc(L.t, v));
         FE_CHECK(dalloc(L.dir, v));
         FE_CHECK(dalloc(L.zn, v));
     }
-    G.nc = H->coarse.n * H->coarse.rd;
-    FE_CHECK(dalloc(G.cinv, std::max<size_t>(H->coarse_inv.size(), 1)));
     FE_CHECK(dalloc(G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
     FE_CHECK(dalloc(G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
-    if (!H->coarse_inv.empty())
-        FE_CUDA(cudaMemcpyAsync(G.cinv.p, H->coarse_inv.data(), H->coarse_inv.size() * sizeof(double),
-                                cudaMemcpyHostToDevice, s));
     if (G.L.empty()) {
         set_error("fe_solve: the multigrid hierarchy has a single level (use the other preconditioners)");
         return FE_BAD_INPUT;

@@ -88,6 +88,67 @@ FE_HD int64_t find_sorted(const int32_t *a, int64_t lo, int64_t hi, int32_t v) {
     return (lo < end && a[lo] == v) ? lo : -1;
 }
 
+// ------------------------------------------------------------------ block inverses
+
+// Pseudo-inverse of a symmetric d x d block by cyclic Jacobi: V diag(1/l) V^T over the
+// eigenvalues above 1e-12 of the largest in magnitude.
+FE_HD void sym_pinv(const double *a, int d, double *out) {
+    double A[36], V[36];
+    for (int i = 0; i < d * d; ++i) A[i] = a[i];
+    for (int i = 0; i < d; ++i)
+        for (int j = 0; j < d; ++j) V[i * d + j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < d; ++p)
+            for (int q = p + 1; q < d; ++q) off += A[p * d + q] * A[p * d + q];
+        if (off < 1e-30) break;
+        for (int p = 0; p < d; ++p)
+            for (int q = p + 1; q < d; ++q) {
+                const double apq = A[p * d + q];
+                if (apq == 0.0) continue;
+                const double th = (A[q * d + q] - A[p * d + p]) / (2.0 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < d; ++k) {
+                    const double akp = A[k * d + p], akq = A[k * d + q];
+                    A[k * d + p] = c * akp - s * akq;
+                    A[k * d + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < d; ++k) {
+                    const double apk = A[p * d + k], aqk = A[q * d + k];
+                    A[p * d + k] = c * apk - s * aqk;
+                    A[q * d + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < d; ++k) {
+                    const double vkp = V[k * d + p], vkq = V[k * d + q];
+                    V[k * d + p] = c * vkp - s * vkq;
+                    V[k * d + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    double lmax = 0.0;
+    for (int i = 0; i < d; ++i) lmax = fabs(A[i * d + i]) > lmax ? fabs(A[i * d + i]) : lmax;
+    for (int i = 0; i < d * d; ++i) out[i] = 0.0;
+    for (int k = 0; k < d; ++k) {
+        const double l = A[k * d + k];
+        if (fabs(l) <= 1e-12 * lmax || l == 0.0) continue;
+        for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j) out[i * d + j] += V[i * d + k] * V[j * d + k] / l;
+    }
+}
+
+// y_i = D_i^-1 (A x)_i (d x d blocks)
+FE_HD void row_dinv_product(const int64_t *ptr, const int32_t *col, const double *val, const double *dinv, int d,
+                            const double *x, int64_t i, double *y) {
+    double acc[6];
+    row_product(ptr, col, val, d, d, x, i, acc);
+    for (int a = 0; a < d; ++a) {
+        double v = 0.0;
+        for (int k = 0; k < d; ++k) v += dinv[i * d * d + a * d + k] * acc[k];
+        y[i * d + a] = v;
+    }
+}
+
 // ------------------------------------------------------------------ strength
 
 // ||A_s||_1 (sum of absolute entries) of every block slot of row i; dg[i] = that of the

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "fe_amg.h"
+#include "fe_amg_dev.h"
 #include "fe_amg_par.cuh"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
@@ -57,60 +58,13 @@ void parallel_chunks(int64_t n, F f) {
     for (auto &x : th) x.join();
 }
 
-// Pseudo-inverse of a symmetric d x d block by cyclic Jacobi: V diag(1/l) V^T over the
-// eigenvalues above 1e-12 of the largest in magnitude.
-void sym_pinv(const double *a, int d, double *out) {
-    double A[36], V[36];
-    for (int i = 0; i < d * d; ++i) A[i] = a[i];
-    for (int i = 0; i < d; ++i)
-        for (int j = 0; j < d; ++j) V[i * d + j] = i == j ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        double off = 0.0;
-        for (int p = 0; p < d; ++p)
-            for (int q = p + 1; q < d; ++q) off += A[p * d + q] * A[p * d + q];
-        if (off < 1e-30) break;
-        for (int p = 0; p < d; ++p)
-            for (int q = p + 1; q < d; ++q) {
-                const double apq = A[p * d + q];
-                if (apq == 0.0) continue;
-                const double th = (A[q * d + q] - A[p * d + p]) / (2.0 * apq);
-                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < d; ++k) {
-                    const double akp = A[k * d + p], akq = A[k * d + q];
-                    A[k * d + p] = c * akp - s * akq;
-                    A[k * d + q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < d; ++k) {
-                    const double apk = A[p * d + k], aqk = A[q * d + k];
-                    A[p * d + k] = c * apk - s * aqk;
-                    A[q * d + k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < d; ++k) {
-                    const double vkp = V[k * d + p], vkq = V[k * d + q];
-                    V[k * d + p] = c * vkp - s * vkq;
-                    V[k * d + q] = s * vkp + c * vkq;
-                }
-            }
-    }
-    double lmax = 0.0;
-    for (int i = 0; i < d; ++i) lmax = std::max(lmax, std::fabs(A[i * d + i]));
-    for (int i = 0; i < d * d; ++i) out[i] = 0.0;
-    for (int k = 0; k < d; ++k) {
-        const double l = A[k * d + k];
-        if (std::fabs(l) <= 1e-12 * lmax || l == 0.0) continue;
-        for (int i = 0; i < d; ++i)
-            for (int j = 0; j < d; ++j) out[i * d + j] += V[i * d + k] * V[j * d + k] / l;
-    }
-}
-
 std::vector<double> block_diag_pinv(const BlockCsr &A) {
     const int d = A.rd;
     std::vector<double> dinv((size_t)A.n * d * d, 0.0);
     parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
         for (int64_t i = lo; i < hi; ++i)
             for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s)
-                if (A.col[s] == i) sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
+                if (A.col[s] == i) amg::sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
     });
     return dinv;
 }
@@ -366,6 +320,37 @@ bool dense_inverse(std::vector<double> a, int n, std::vector<double> &inv) {
 
 
 namespace fe {
+
+// Dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal entry
+// (zero rows of rank-deficient aggregates).
+int coarse_inverse_of(const BlockCsr &C, std::vector<double> &inv, const char *who) {
+    const int64_t n = C.n * C.rd;
+    if (n > 4096) {
+        set_error(std::string(who) + ": coarsest level too large for its dense solve");
+        return FE_BAD_INPUT;
+    }
+    std::vector<double> dense((size_t)n * n, 0.0);
+    double dmax = 0.0;
+    const int cd = C.rd;
+    for (int64_t i = 0; i < C.n; ++i)
+        for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
+            for (int a = 0; a < cd; ++a)
+                for (int b = 0; b < cd; ++b) {
+                    const double v = C.val[(size_t)s * cd * cd + a * cd + b];
+                    dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
+                }
+    for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
+    for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
+    if (n > 0 && !dense_inverse(dense, (int)n, inv)) {
+        set_error(std::string(who) + ": singular coarsest matrix");
+        return FE_BREAKDOWN;
+    }
+    return FE_OK;
+}
+
+}  // namespace fe
+
+namespace fe {
 namespace {
 
 // k Chebyshev steps on D^-1 A z = D^-1 r over [1.05 lmax / 30, 1.05 lmax], from x0 (or
@@ -421,33 +406,8 @@ void vcycle_host(const fe_amg_s *h, size_t l, int k, const std::vector<double> &
 }
 
 
-// Dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal entry
-// (zero rows of rank-deficient aggregates).
-int coarse_inverse(fe_amg_s *h, const char *who) {
-    const BlockCsr &C = h->coarse;
-    const int64_t n = C.n * C.rd;
-    if (n > 4096) {
-        set_error(std::string(who) + ": coarsest level too large for its dense solve");
-        return FE_BAD_INPUT;
-    }
-    std::vector<double> dense((size_t)n * n, 0.0);
-    double dmax = 0.0;
-    const int cd = C.rd;
-    for (int64_t i = 0; i < C.n; ++i)
-        for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
-            for (int a = 0; a < cd; ++a)
-                for (int b = 0; b < cd; ++b) {
-                    const double v = C.val[(size_t)s * cd * cd + a * cd + b];
-                    dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
-                }
-    for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
-    for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
-    if (n > 0 && !dense_inverse(dense, (int)n, h->coarse_inv)) {
-        set_error(std::string(who) + ": singular coarsest matrix");
-        return FE_BREAKDOWN;
-    }
-    return FE_OK;
-}
+// Dense inverse of the coarsest matrix of h.
+int coarse_inverse(fe_amg_s *h, const char *who) { return coarse_inverse_of(h->coarse, h->coarse_inv, who); }
 
 // ---------------------------------------------------------------- parallel setup (host)
 // The passes of the device setup, run over the rows with the row operations of

@@ -285,6 +285,11 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
 int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
                                const double *vals, int32_t m, const double *nullspace, double theta,
                                int64_t coarse_dofs, fe_amg *out);
+/* The same passes on the device, from the assembled system of h (near-null space: the
+ * rigid-body modes, or the constant for magnetostatics, zero on the constrained DOFs);
+ * the hierarchy is copied to the host for the accessors below.  Work in progress: not
+ * yet run on a GPU. */
+int fe_amg_build_device(fe_handle h, double theta, int64_t coarse_dofs, fe_amg *out);
 int fe_amg_levels(fe_amg a, int32_t *n_levels);
 int fe_amg_level_info(fe_amg a, int32_t level, int64_t *n_nodes, int32_t *d, int64_t *nnzb_A,
                       int64_t *nnzb_P, int64_t *n_coarse, int32_t *m, double *lmax);
