@@ -24,10 +24,14 @@ struct DevLevel {
     DBuf<double> dinv;
     DBuf<int32_t> agg;
     double lmax = 0.0;
-    DBuf<double> r, x, t, dir, zn;   // n * d each (r, x: the level's right-hand side and iterate)
+    // the V-cycle runs in FP32: values of A, P, P^T and D^-1, and the level's vectors
+    // (n * d each; r, x: the level's right-hand side and iterate)
+    DBuf<float> a32, p32, pt32, dinv32;
+    DBuf<float> r, x, t, dir, zn;
     void release() {
         A.release(), P.release(), PT.release();
-        dfree(dinv), dfree(agg), dfree(r), dfree(x), dfree(t), dfree(dir), dfree(zn);
+        dfree(dinv), dfree(agg), dfree(a32), dfree(p32), dfree(pt32), dfree(dinv32);
+        dfree(r), dfree(x), dfree(t), dfree(dir), dfree(zn);
     }
 };
 
@@ -35,7 +39,8 @@ struct DevAmg {
     std::vector<DevLevel> L;
     DevCsr coarse;
     int64_t nc = 0;                  // coarsest DOFs
-    DBuf<double> cinv, rc, xc;
+    DBuf<double> cinv;               // dense inverse of the coarsest matrix (FP64)
+    DBuf<float> rc, xc;
     int mis_rounds = 0;              // independent-set rounds, all levels
     ~DevAmg() {
         for (auto &l : L) l.release();

@@ -1,7 +1,9 @@
 // Multigrid-preconditioned PCG on the device: the smoothed-aggregation hierarchy of
 // the eliminated system (set up on the device, fe_amg_device_setup.cu) and a V-cycle
 // whose kernels are loops of the row operations of fe_amg_rows.cuh -- the operations
-// the host cycle fe_amg_vcycle_host runs serially.  FP64 throughout.
+// the host cycle fe_amg_vcycle_host runs serially.  The PCG recurrence, its SpMV and
+// the true residual are FP64; the V-cycle runs in FP32 on FP32 copies of the levels
+// (a CPU emulation of the cycle in FP32 gave the FP64 cycle's PCG iteration counts).
 //
 // WORK IN PROGRESS: not yet run on a GPU.
 #include <algorithm>
@@ -19,32 +21,43 @@ constexpr int kAT = 256;
 inline int grid_a(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kAT - 1) / kAT, 152 * 8)); }
 
 __global__ void ka_chebyshev(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                             const double *__restrict__ val, const double *__restrict__ dinv, int d,
-                             const double *__restrict__ r, const double *__restrict__ zin, double *__restrict__ dir,
-                             double *__restrict__ zout, double a, double b, int first) {
+                             const float *__restrict__ val, const float *__restrict__ dinv, int d,
+                             const float *__restrict__ r, const float *__restrict__ zin, float *__restrict__ dir,
+                             float *__restrict__ zout, float a, float b, int first) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         amg::row_chebyshev(ptr, col, val, dinv, d, r, zin, dir, zout, a, b, first != 0, i);
 }
 
+template <typename T>
 __global__ void ka_residual(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                            const double *__restrict__ val, int d, const double *__restrict__ r,
-                            const double *__restrict__ x, double *__restrict__ t) {
+                            const T *__restrict__ val, int d, const T *__restrict__ r, const T *__restrict__ x,
+                            T *__restrict__ t) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         amg::row_residual(ptr, col, val, d, r, x, t, i);
 }
 
 __global__ void ka_restrict(int64_t nc, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                            const double *__restrict__ val, int m, int d, const double *__restrict__ t,
-                            double *__restrict__ rc) {
+                            const float *__restrict__ val, int m, int d, const float *__restrict__ t,
+                            float *__restrict__ rc) {
     for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nc; I += (int64_t)gridDim.x * blockDim.x)
         amg::row_restrict(ptr, col, val, m, d, t, rc, I);
 }
 
 __global__ void ka_prolong_add(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                               const double *__restrict__ val, int d, int m, const double *__restrict__ xc,
-                               double *__restrict__ x) {
+                               const float *__restrict__ val, int d, int m, const float *__restrict__ xc,
+                               float *__restrict__ x) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         amg::row_prolong_add(ptr, col, val, d, m, xc, x, i);
+}
+
+__global__ void ka_to_f32(int64_t n, const double *__restrict__ in, float *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+__global__ void ka_to_f64(int64_t n, const float *__restrict__ in, double *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
 }
 
 // q = A p with the level-0 matrix (block rows of size d)
@@ -57,13 +70,13 @@ __global__ void ka_spmv(int64_t n, const int64_t *__restrict__ ptr, const int32_
     }
 }
 
-// x = Ainv r (dense, n x n)
-__global__ void ka_dense(int64_t n, const double *__restrict__ ainv, const double *__restrict__ r,
-                         double *__restrict__ x) {
+// x = Ainv r (dense, n x n, FP64 inverse and sums)
+__global__ void ka_dense(int64_t n, const double *__restrict__ ainv, const float *__restrict__ r,
+                         float *__restrict__ x) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0.0;
-        for (int64_t j = 0; j < n; ++j) acc += ainv[i * n + j] * r[j];
-        x[i] = acc;
+        for (int64_t j = 0; j < n; ++j) acc += ainv[i * n + j] * (double)r[j];
+        x[i] = (float)acc;
     }
 }
 
@@ -112,34 +125,34 @@ __global__ void ka_direction(int64_t n, double beta, const double *__restrict__ 
         p[i] = fma(beta, p[i], z[i]);
 }
 
-// Chebyshev smoothing of level l into L.x (from zero, or from L.x with from_x0)
+// Chebyshev smoothing of level l into L.x (from zero, or from L.x with from_x0), FP32
 int chebyshev_dev(fe_handle_s *h, DevLevel &L, int k, bool from_x0) {
     cudaStream_t s = h->stream;
     const int d = L.A.rd;
     const int64_t n = L.A.n, nd = n * d;
     const double hi = 1.05 * L.lmax, lo = hi / 30.0;
     const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
-    if (!from_x0) FE_CUDA(cudaMemsetAsync(L.x.p, 0, nd * sizeof(double), s));
-    double *cur = L.x.p, *nxt = L.zn.p;
+    if (!from_x0) FE_CUDA(cudaMemsetAsync(L.x.p, 0, nd * sizeof(float), s));
+    float *cur = L.x.p, *nxt = L.zn.p;
     double rho = 1.0 / sigma;
-    ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.A.val.p, L.dinv.p, d, L.r.p, cur, L.dir.p, nxt,
-                                           0.0, 1.0 / theta, 1);
+    ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.a32.p, L.dinv32.p, d, L.r.p, cur, L.dir.p, nxt,
+                                           0.0f, (float)(1.0 / theta), 1);
     std::swap(cur, nxt);
     for (int st = 1; st < k; ++st) {
         const double rn = 1.0 / (2.0 * sigma - rho);
         const double a = rn * rho, b = 2.0 * rn / delta;
         rho = rn;
-        ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.A.val.p, L.dinv.p, d, L.r.p, cur, L.dir.p,
-                                               nxt, a, b, 0);
+        ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.a32.p, L.dinv32.p, d, L.r.p, cur, L.dir.p,
+                                               nxt, (float)a, (float)b, 0);
         std::swap(cur, nxt);
     }
     FE_LAUNCH_CHECK();
     h->launches += k;
-    if (cur != L.x.p) FE_CUDA(cudaMemcpyAsync(L.x.p, cur, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (cur != L.x.p) FE_CUDA(cudaMemcpyAsync(L.x.p, cur, nd * sizeof(float), cudaMemcpyDeviceToDevice, s));
     return FE_OK;
 }
 
-// V-cycle on level l: L.r -> L.x
+// V-cycle on level l: L.r -> L.x, FP32
 int vcycle_dev(fe_handle_s *h, DevAmg &G, size_t l, int k) {
     cudaStream_t s = h->stream;
     if (l == G.L.size()) {
@@ -152,25 +165,48 @@ int vcycle_dev(fe_handle_s *h, DevAmg &G, size_t l, int k) {
     const int d = L.A.rd, m = L.P.cd;
     const int64_t n = L.A.n;
     FE_CHECK(chebyshev_dev(h, L, k, false));
-    ka_residual<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.A.val.p, d, L.r.p, L.x.p, L.t.p);
-    double *rc = l + 1 < G.L.size() ? G.L[l + 1].r.p : G.rc.p;
-    double *xc = l + 1 < G.L.size() ? G.L[l + 1].x.p : G.xc.p;
-    ka_restrict<<<grid_a(L.PT.n), kAT, 0, s>>>(L.PT.n, L.PT.ptr.p, L.PT.col.p, L.PT.val.p, m, d, L.t.p, rc);
+    ka_residual<float><<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.a32.p, d, L.r.p, L.x.p, L.t.p);
+    float *rc = l + 1 < G.L.size() ? G.L[l + 1].r.p : G.rc.p;
+    float *xc = l + 1 < G.L.size() ? G.L[l + 1].x.p : G.xc.p;
+    ka_restrict<<<grid_a(L.PT.n), kAT, 0, s>>>(L.PT.n, L.PT.ptr.p, L.PT.col.p, L.pt32.p, m, d, L.t.p, rc);
     FE_LAUNCH_CHECK();
     h->launches += 2;
     FE_CHECK(vcycle_dev(h, G, l + 1, k));
-    ka_prolong_add<<<grid_a(n), kAT, 0, s>>>(n, L.P.ptr.p, L.P.col.p, L.P.val.p, d, m, xc, L.x.p);
+    ka_prolong_add<<<grid_a(n), kAT, 0, s>>>(n, L.P.ptr.p, L.P.col.p, L.p32.p, d, m, xc, L.x.p);
     FE_LAUNCH_CHECK();
     h->launches += 1;
     return chebyshev_dev(h, L, k, true);
 }
 
+// FP32 copies of a level's values and its cycle vectors
+int prepare_cycle(fe_handle_s *h, DevLevel &L) {
+    cudaStream_t s = h->stream;
+    const int d = L.A.rd, m = L.P.cd;
+    const int64_t na = L.A.nnzb * d * d, np = L.P.nnzb * d * m, nt = L.PT.nnzb * m * d, ndi = L.A.n * d * d;
+    FE_CHECK(dalloc(L.a32, (size_t)std::max<int64_t>(na, 1)));
+    FE_CHECK(dalloc(L.p32, (size_t)std::max<int64_t>(np, 1)));
+    FE_CHECK(dalloc(L.pt32, (size_t)std::max<int64_t>(nt, 1)));
+    FE_CHECK(dalloc(L.dinv32, (size_t)std::max<int64_t>(ndi, 1)));
+    ka_to_f32<<<grid_a(na), kAT, 0, s>>>(na, L.A.val.p, L.a32.p);
+    ka_to_f32<<<grid_a(np), kAT, 0, s>>>(np, L.P.val.p, L.p32.p);
+    ka_to_f32<<<grid_a(nt), kAT, 0, s>>>(nt, L.PT.val.p, L.pt32.p);
+    ka_to_f32<<<grid_a(ndi), kAT, 0, s>>>(ndi, L.dinv.p, L.dinv32.p);
+    FE_LAUNCH_CHECK();
+    const size_t v = (size_t)std::max<int64_t>(L.A.n * d, 1);
+    FE_CHECK(dalloc(L.r, v));
+    FE_CHECK(dalloc(L.x, v));
+    FE_CHECK(dalloc(L.t, v));
+    FE_CHECK(dalloc(L.dir, v));
+    FE_CHECK(dalloc(L.zn, v));
+    return FE_OK;
+}
+
 }  // namespace
 
-// PCG on the eliminated system preconditioned by one V-cycle (k = 3 Chebyshev steps per
-// smoothing), FP64, from x = 0 (opts.x0 is not used); the hierarchy is built on the
-// host from the device system matrix and the rigid-body (elasticity) or constant
-// (magnetostatics) modes, with the rows of the constrained DOFs zeroed.
+// PCG on the eliminated system preconditioned by one FP32 V-cycle (k = 3 Chebyshev steps
+// per smoothing), FP64 recurrence, from x = 0 (opts.x0 is not used); the hierarchy is
+// set up on the device from the system matrix and the rigid-body (elasticity) or
+// constant (magnetostatics) modes, with the rows of the constrained DOFs zeroed.
 int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     cudaStream_t s = h->stream;
     const int D = h->dim;
@@ -179,14 +215,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     // the hierarchy, set up on the device, and the cycle's vectors
     DevAmg G;
     FE_CHECK(amg_setup_device(h, 0.08, 400, G));
-    for (auto &L : G.L) {
-        const size_t v = (size_t)std::max<int64_t>(L.A.n * L.A.rd, 1);
-        FE_CHECK(dalloc(L.r, v));
-        FE_CHECK(dalloc(L.x, v));
-        FE_CHECK(dalloc(L.t, v));
-        FE_CHECK(dalloc(L.dir, v));
-        FE_CHECK(dalloc(L.zn, v));
-    }
+    for (auto &L : G.L) FE_CHECK(prepare_cycle(h, L));
     FE_CHECK(dalloc(G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
     FE_CHECK(dalloc(G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
     if (G.L.empty()) {
@@ -195,18 +224,19 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     }
     // PCG: level 0's r and x hold the V-cycle's input and output
     DevLevel &L0 = G.L[0];
-    DBuf<double> r, p, q, part, sc;
+    DBuf<double> r, p, q, z, part, sc;
     struct Free {
-        DBuf<double> *b[5];
+        DBuf<double> *b[6];
         ~Free() {
             for (auto *x : b) dfree(*x);
         }
-    } fg{{&r, &p, &q, &part, &sc}};
+    } fg{{&r, &p, &q, &z, &part, &sc}};
     const int gn = grid_a(nd);
     FE_CHECK(dalloc(h->w.x, (size_t)std::max<int64_t>(nd, 1)));
     FE_CHECK(dalloc(r, (size_t)nd));
     FE_CHECK(dalloc(p, (size_t)nd));
     FE_CHECK(dalloc(q, (size_t)nd));
+    FE_CHECK(dalloc(z, (size_t)nd));
     FE_CHECK(dalloc(part, (size_t)gn));
     FE_CHECK(dalloc(sc, 4));
     double *x = h->w.x.p;
@@ -217,15 +247,20 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         h->launches += 2;
         return FE_OK;
     };
-    auto precond = [&]() -> int {   // L0.x = M^-1 r
-        FE_CUDA(cudaMemcpyAsync(L0.r.p, r.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        return vcycle_dev(h, G, 0, 3);
+    auto precond = [&]() -> int {   // z = M^-1 r: the FP32 V-cycle on r rounded to FP32
+        ka_to_f32<<<gn, kAT, 0, s>>>(nd, r.p, L0.r.p);
+        FE_LAUNCH_CHECK();
+        FE_CHECK(vcycle_dev(h, G, 0, 3));
+        ka_to_f64<<<gn, kAT, 0, s>>>(nd, L0.x.p, z.p);
+        FE_LAUNCH_CHECK();
+        h->launches += 2;
+        return FE_OK;
     };
     FE_CUDA(cudaMemsetAsync(x, 0, nd * sizeof(double), s));
     FE_CUDA(cudaMemcpyAsync(r.p, h->b.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
     FE_CHECK(precond());
-    FE_CUDA(cudaMemcpyAsync(p.p, L0.x.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    FE_CHECK(dot(r.p, L0.x.p, sc.p));
+    FE_CUDA(cudaMemcpyAsync(p.p, z.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    FE_CHECK(dot(r.p, z.p, sc.p));
     FE_CHECK(dot(r.p, r.p, sc.p + 1));
     double host[4];
     FE_CUDA(cudaMemcpyAsync(host, sc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -253,7 +288,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         ++it;
         FE_CHECK(dot(r.p, r.p, sc.p + 1));
         FE_CHECK(precond());
-        FE_CHECK(dot(r.p, L0.x.p, sc.p));
+        FE_CHECK(dot(r.p, z.p, sc.p));
         FE_CUDA(cudaMemcpyAsync(host, sc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
         FE_CUDA(cudaStreamSynchronize(s));
         rr = host[1];
@@ -267,12 +302,12 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         }
         const double beta = host[0] / rz;
         rz = host[0];
-        ka_direction<<<gn, kAT, 0, s>>>(nd, beta, L0.x.p, p.p);
+        ka_direction<<<gn, kAT, 0, s>>>(nd, beta, z.p, p.p);
         FE_LAUNCH_CHECK();
         h->launches += 1;
     }
     // true residual b - A x in FP64
-    ka_residual<<<grid_a(n), kAT, 0, s>>>(n, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, h->b.p, x, q.p);
+    ka_residual<double><<<grid_a(n), kAT, 0, s>>>(n, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, h->b.p, x, q.p);
     FE_LAUNCH_CHECK();
     h->launches += 1;
     FE_CHECK(dot(q.p, q.p, sc.p + 3));
