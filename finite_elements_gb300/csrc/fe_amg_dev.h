@@ -5,19 +5,17 @@
 #include <vector>
 
 #include "fe_amg.h"
+#include "fe_amg_passes.cuh"
 #include "fe_internal.h"
 
 namespace fe {
 
-struct DevCsr {
-    int64_t n = 0;
-    int rd = 0, cd = 0;
-    DBuf<int64_t> ptr;   // n + 1
-    DBuf<int32_t> col;
-    DBuf<double> val;    // row-major rd x cd blocks
-    int64_t nnzb = 0;
-    void release() { dfree(ptr), dfree(col), dfree(val); }
-};
+using DevCsr = amg::Csr;
+
+inline void drelease(DevCsr &c) {
+    dfree(c.ptr), dfree(c.col), dfree(c.val);
+    c.nnzb = 0;
+}
 
 struct DevLevel {
     DevCsr A, P, PT;
@@ -29,7 +27,7 @@ struct DevLevel {
     DBuf<float> a32, p32, pt32, dinv32;
     DBuf<float> r, x, t, dir, zn;
     void release() {
-        A.release(), P.release(), PT.release();
+        drelease(A), drelease(P), drelease(PT);
         dfree(dinv), dfree(agg), dfree(a32), dfree(p32), dfree(pt32), dfree(dinv32);
         dfree(r), dfree(x), dfree(t), dfree(dir), dfree(zn);
     }
@@ -44,14 +42,14 @@ struct DevAmg {
     int mis_rounds = 0;              // independent-set rounds, all levels
     ~DevAmg() {
         for (auto &l : L) l.release();
-        coarse.release();
+        drelease(coarse);
         dfree(cinv), dfree(rc), dfree(xc);
     }
 };
 
 // Device setup of the hierarchy of the handle's eliminated system (near-null space: the
 // rigid-body modes for elasticity, the constant for magnetostatics, zero on the
-// constrained DOFs), the same passes as fe_amg_build_parallel_host.
+// constrained DOFs): amg::setup_hierarchy on the device executor.
 int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G);
 // Copy of a device hierarchy into host form (accessors of the fe_amg_* ABI).
 int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s);

@@ -18,6 +18,7 @@
 // down to at most `coarse_dofs` DOFs (or 12 levels).  Host code only: no device call.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -26,6 +27,7 @@
 #include "fe_amg.h"
 #include "fe_amg_dev.h"
 #include "fe_amg_par.cuh"
+#include "fe_amg_passes.cuh"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
@@ -410,206 +412,117 @@ void vcycle_host(const fe_amg_s *h, size_t l, int k, const std::vector<double> &
 int coarse_inverse(fe_amg_s *h, const char *who) { return coarse_inverse_of(h->coarse, h->coarse_inv, who); }
 
 // ---------------------------------------------------------------- parallel setup (host)
-// The passes of the device setup, run over the rows with the row operations of
-// fe_amg_par.cuh: every pass reads what earlier passes wrote, so its rows are
-// independent and the result is the same in any row order.
+// amg::setup_hierarchy (fe_amg_passes.cuh), the device setup's sequence of passes, on
+// a host executor: passes over row chunks on host threads, serial scans, dot products
+// summed per chunk in chunk order.
 
-// Exclusive prefix sum of counts into offsets (n + 1 values).
-std::vector<int64_t> offsets_of(const std::vector<int64_t> &cnt) {
-    std::vector<int64_t> off(cnt.size() + 1, 0);
-    for (size_t i = 0; i < cnt.size(); ++i) off[i + 1] = off[i] + cnt[i];
-    return off;
-}
-
-// C = A B row by row: bound, sorted distinct columns, values.
-BlockCsr product_rows(const BlockCsr &A, const BlockCsr &B) {
-    BlockCsr C;
-    C.n = A.n, C.rd = A.rd, C.cd = B.cd;
-    std::vector<int64_t> bound((size_t)A.n), cnt((size_t)A.n);
-    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i) bound[i] = amg::row_product_bound(A.ptr.data(), A.col.data(), B.ptr.data(), i);
-    });
-    const std::vector<int64_t> boff = offsets_of(bound);
-    std::vector<int32_t> cand((size_t)std::max<int64_t>(boff.back(), 1));
-    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i)
-            cnt[i] = amg::row_product_columns(A.ptr.data(), A.col.data(), B.ptr.data(), B.col.data(), i,
-                                              cand.data() + boff[i]);
-    });
-    C.ptr = offsets_of(cnt);
-    C.col.resize((size_t)C.ptr.back());
-    C.val.resize((size_t)C.ptr.back() * C.rd * C.cd);
-    parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i) {
-            std::copy(cand.begin() + boff[i], cand.begin() + boff[i] + cnt[i], C.col.begin() + C.ptr[i]);
-            amg::row_product_values(A.ptr.data(), A.col.data(), A.val.data(), A.rd, A.cd, B.ptr.data(), B.col.data(),
-                                    B.val.data(), B.cd, C.ptr.data(), C.col.data(), C.val.data(), i);
+struct HostEx {
+    template <class T>
+    int alloc(DBuf<T> &b, size_t n) {
+        if (b.p && b.n >= n) return FE_OK;
+        std::free(b.p);
+        b.p = (T *)std::malloc(std::max<size_t>(n, 1) * sizeof(T));
+        b.n = b.p ? n : 0;
+        if (!b.p) {
+            set_error("multigrid setup: out of host memory");
+            return FE_BAD_INPUT;
         }
-    });
-    return C;
-}
-
-// P^T from P, A's pattern and the aggregates' member lists.
-BlockCsr restriction_rows(const BlockCsr &A, const BlockCsr &P, const std::vector<int64_t> &mptr,
-                          const std::vector<int32_t> &mem, int64_t na) {
-    BlockCsr R;
-    R.n = na, R.rd = P.cd, R.cd = P.rd;
-    std::vector<int64_t> bound((size_t)na), cnt((size_t)na);
-    parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t c = lo; c < hi; ++c) bound[c] = amg::row_restriction_bound(mptr.data(), mem.data(), A.ptr.data(), c);
-    });
-    const std::vector<int64_t> boff = offsets_of(bound);
-    std::vector<int32_t> cand((size_t)std::max<int64_t>(boff.back(), 1));
-    parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t c = lo; c < hi; ++c)
-            cnt[c] = amg::row_restriction_columns(mptr.data(), mem.data(), A.ptr.data(), A.col.data(), c,
-                                                  cand.data() + boff[c]);
-    });
-    R.ptr = offsets_of(cnt);
-    R.col.resize((size_t)R.ptr.back());
-    R.val.resize((size_t)R.ptr.back() * R.rd * R.cd);
-    parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t c = lo; c < hi; ++c) {
-            std::copy(cand.begin() + boff[c], cand.begin() + boff[c] + cnt[c], R.col.begin() + R.ptr[c]);
-            amg::row_restriction_values(R.ptr.data(), R.col.data(), R.val.data(), P.ptr.data(), P.col.data(),
-                                        P.val.data(), P.rd, P.cd, c);
+        return FE_OK;
+    }
+    template <class T>
+    void release(DBuf<T> &b) {
+        std::free(b.p);
+        b.p = nullptr;
+        b.n = 0;
+    }
+    template <class T>
+    int copy(T *dst, const T *src, size_t n) {
+        if (n) std::memcpy(dst, src, n * sizeof(T));
+        return FE_OK;
+    }
+    template <class T>
+    int read(T *dst, const T *src, size_t n) {
+        return copy(dst, src, n);
+    }
+    template <class F>
+    int rows(int64_t n, const F &f) {
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i) f(i);
+        });
+        return FE_OK;
+    }
+    int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) {
+        int64_t run = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t v = in[i];
+            out[i] = run;
+            run += v;
         }
-    });
-    return R;
-}
-
-// Aggregates by the distance-2 independent set; agg[i] for every node, the roots in
-// aggregate order.  Returns the number of rounds, or -1 if a node was left out.
-int aggregate_parallel(const BlockCsr &A, double theta, std::vector<int32_t> &agg, std::vector<int32_t> &roots,
-                       std::vector<double> &nrm, std::vector<uint8_t> &strong) {
-    const int64_t n = A.n;
-    const int d = A.rd;
-    nrm.assign((size_t)A.nnzb(), 0.0);
-    strong.assign((size_t)A.nnzb(), 0);
-    std::vector<double> dg((size_t)n);
-    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i)
-            amg::row_block_norms(A.ptr.data(), A.col.data(), A.val.data(), d, i, nrm.data(), dg.data());
-    });
-    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i)
-            amg::row_strength(A.ptr.data(), A.col.data(), nrm.data(), dg.data(), theta, i, strong.data());
-    });
-    std::vector<uint32_t> state((size_t)n, amg::kUndecided);
-    std::vector<uint64_t> key((size_t)n), m1((size_t)n), m2((size_t)n);
-    int64_t part[kChunks];
-    int rounds = 0;
-    for (;;) {
-        ++rounds;
-        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t i = lo; i < hi; ++i) key[i] = amg::mis_key(state[i], i);
-        });
-        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t i = lo; i < hi; ++i)
-                amg::row_max_key(A.ptr.data(), A.col.data(), strong.data(), key.data(), i, m1.data());
-        });
-        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t i = lo; i < hi; ++i)
-                amg::row_max_key(A.ptr.data(), A.col.data(), strong.data(), m1.data(), i, m2.data());
-        });
-        for (int c = 0; c < kChunks; ++c) part[c] = 0;
+        out[n] = run;
+        *total = run;
+        return FE_OK;
+    }
+    int dot(const double *a, const double *b, int64_t n, double *out) {
+        double part[kChunks];
+        for (int c = 0; c < kChunks; ++c) part[c] = 0.0;
         parallel_chunks(n, [&](int64_t lo, int64_t hi, int c) {
-            int64_t u = 0;
-            for (int64_t i = lo; i < hi; ++i) u += amg::mis_decide(m2.data(), i, state.data());
-            part[c] = u;
+            double t = 0.0;
+            for (int64_t i = lo; i < hi; ++i) t += a[i] * b[i];
+            part[c] = t;
         });
-        int64_t undecided = 0;
-        for (int c = 0; c < kChunks; ++c) undecided += part[c];
-        if (undecided == 0) break;
+        double t = 0.0;
+        for (int c = 0; c < kChunks; ++c) t += part[c];
+        *out = t;
+        return FE_OK;
     }
-    std::vector<int32_t> rank((size_t)n, -1);
-    roots.clear();
-    for (int64_t i = 0; i < n; ++i)
-        if (state[i] == amg::kIn) rank[i] = (int32_t)roots.size(), roots.push_back((int32_t)i);
-    std::vector<int32_t> agg1((size_t)n);
-    agg.assign((size_t)n, -1);
-    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i)
-            amg::row_join_root(A.ptr.data(), A.col.data(), strong.data(), nrm.data(), state.data(), rank.data(), i,
-                               agg1.data());
-    });
-    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
-        for (int64_t i = lo; i < hi; ++i)
-            amg::row_join_neighbour(A.ptr.data(), A.col.data(), strong.data(), nrm.data(), agg1.data(), i,
-                                    agg.data());
-    });
-    for (int64_t i = 0; i < n; ++i)
-        if (agg[i] < 0) return -1;
-    return rounds;
+};
+
+BlockCsr to_block_csr(const amg::Csr &c) {
+    BlockCsr H;
+    H.n = c.n, H.rd = c.rd, H.cd = c.cd;
+    H.ptr.assign(c.ptr.p, c.ptr.p + c.n + 1);
+    H.col.assign(c.col.p, c.col.p + c.nnzb);
+    H.val.assign(c.val.p, c.val.p + c.nnzb * c.rd * c.cd);
+    return H;
 }
 
-// The hierarchy by the parallel passes.  Returns FE_OK or a failure status.
-int build_parallel(fe_amg_s *h, BlockCsr A, std::vector<double> B, int bm, double theta, int64_t coarse_dofs) {
-    while (A.n * A.rd > coarse_dofs && h->levels.size() < 12) {
-        AmgLevel L;
-        const int dd = A.rd;
-        std::vector<double> dinv = block_diag_pinv(A);
-        L.lmax = lmax_power(A, dinv);
-        std::vector<int32_t> roots;
-        std::vector<double> nrm;
-        std::vector<uint8_t> strong;
-        if (aggregate_parallel(A, theta, L.agg, roots, nrm, strong) < 0) {
-            set_error("fe_amg_build_parallel_host: a node was left without an aggregate");
-            return FE_BREAKDOWN;
-        }
-        const int64_t na = (int64_t)roots.size();
-        // member lists in increasing node order
-        std::vector<int64_t> bound((size_t)na), cnt((size_t)na);
-        parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t c = lo; c < hi; ++c) bound[c] = amg::agg_member_bound(A.ptr.data(), A.col.data(), roots.data(), c);
-        });
-        const std::vector<int64_t> boff = offsets_of(bound);
-        std::vector<int32_t> cand((size_t)std::max<int64_t>(boff.back(), 1));
-        parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t c = lo; c < hi; ++c)
-                cnt[c] = amg::agg_members(A.ptr.data(), A.col.data(), roots.data(), L.agg.data(), c, cand.data() + boff[c]);
-        });
-        const std::vector<int64_t> mptr = offsets_of(cnt);
-        if (mptr.back() != A.n) {
-            set_error("fe_amg_build_parallel_host: aggregate members do not cover the nodes");
-            return FE_BREAKDOWN;
-        }
-        std::vector<int32_t> mem((size_t)A.n);
-        for (int64_t c = 0; c < na; ++c)
-            std::copy(cand.begin() + boff[c], cand.begin() + boff[c] + cnt[c], mem.begin() + mptr[c]);
-        // tentative prolongator: one QR per aggregate, in place on B's rows
-        BlockCsr Pt;
-        Pt.n = A.n, Pt.rd = dd, Pt.cd = bm;
-        Pt.ptr.resize((size_t)A.n + 1);
-        for (int64_t i = 0; i <= A.n; ++i) Pt.ptr[i] = i;
-        Pt.col.assign(L.agg.begin(), L.agg.end());
-        Pt.val = B;
-        std::vector<double> Bc((size_t)na * bm * bm);
-        parallel_chunks(na, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t c = lo; c < hi; ++c)
-                amg::aggregate_qr(mem.data() + mptr[c], mptr[c + 1] - mptr[c], dd, bm, Pt.val.data(),
-                                  Bc.data() + (size_t)c * bm * bm);
-        });
-        // smoothed prolongator and Galerkin product
-        BlockCsr P = product_rows(A, Pt);
-        const double w = 4.0 / (3.0 * L.lmax);
-        parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t i = lo; i < hi; ++i)
-                amg::row_smooth_prolongator(P.ptr.data(), P.col.data(), P.val.data(), dinv.data(), Pt.val.data(),
-                                            L.agg.data(), dd, bm, w, i);
-        });
-        BlockCsr AP = product_rows(A, P);
-        BlockCsr PT = restriction_rows(A, P, mptr, mem, na);
-        BlockCsr Ac = product_rows(PT, AP);
-        L.A = std::move(A);
-        L.P = std::move(P);
-        L.PT = std::move(PT);
-        L.dinv = std::move(dinv);
-        h->levels.push_back(std::move(L));
-        A = std::move(Ac);
-        B.swap(Bc);
+// The hierarchy by the parallel passes on the host.  Returns FE_OK or a failure status.
+int build_parallel(fe_amg_s *h, int64_t n, int d, const int64_t *ptr, const int32_t *col, const double *vals,
+                   const double *nullspace, int m, double theta, int64_t coarse_dofs) {
+    HostEx ex;
+    amg::Csr A;
+    DBuf<double> B;
+    A.n = n, A.rd = A.cd = d, A.nnzb = ptr[n];
+    int st = FE_OK;
+    if ((st = ex.alloc(A.ptr, (size_t)n + 1)) || (st = ex.alloc(A.col, (size_t)std::max<int64_t>(A.nnzb, 1))) ||
+        (st = ex.alloc(A.val, (size_t)std::max<int64_t>(A.nnzb * d * d, 1))) ||
+        (st = ex.alloc(B, (size_t)std::max<int64_t>(n * d * m, 1)))) {
+        amg::release(ex, A);
+        ex.release(B);
+        return st;
     }
-    h->coarse = std::move(A);
+    ex.copy(A.ptr.p, ptr, (size_t)n + 1);
+    ex.copy(A.col.p, col, (size_t)A.nnzb);
+    ex.copy(A.val.p, vals, (size_t)(A.nnzb * d * d));
+    ex.copy(B.p, nullspace, (size_t)(n * d * m));
+    std::vector<amg::Level> levels;
+    amg::Csr coarse;
+    int rounds = 0;
+    st = amg::setup_hierarchy(ex, A, B, m, theta, coarse_dofs, levels, coarse, &rounds);
+    for (auto &l : levels) {
+        if (st == FE_OK) {
+            AmgLevel L;
+            L.A = to_block_csr(l.A), L.P = to_block_csr(l.P), L.PT = to_block_csr(l.PT);
+            L.dinv.assign(l.dinv.p, l.dinv.p + l.A.n * l.A.rd * l.A.rd);
+            L.agg.assign(l.agg.p, l.agg.p + l.A.n);
+            L.lmax = l.lmax;
+            h->levels.push_back(std::move(L));
+        }
+        amg::release(ex, l);
+    }
+    if (st != FE_OK) return st;
+    h->coarse = to_block_csr(coarse);
+    amg::release(ex, coarse);
     return coarse_inverse(h, "fe_amg_build_parallel_host");
 }
 
@@ -730,13 +643,7 @@ int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_pt
     }
     *out = nullptr;
     fe_amg_s *h = new fe_amg_s();
-    BlockCsr A;
-    A.n = n_nodes, A.rd = A.cd = d;
-    A.ptr.assign(blk_ptr, blk_ptr + n_nodes + 1);
-    A.col.assign(blk_col, blk_col + A.ptr[n_nodes]);
-    A.val.assign(vals, vals + (size_t)A.ptr[n_nodes] * d * d);
-    std::vector<double> B(nullspace, nullspace + (size_t)n_nodes * d * m);
-    const int st = build_parallel(h, std::move(A), std::move(B), m, theta, coarse_dofs);
+    const int st = build_parallel(h, n_nodes, d, blk_ptr, blk_col, vals, nullspace, m, theta, coarse_dofs);
     if (st != FE_OK) {
         fe_amg_destroy(h);
         return st;
