@@ -16,6 +16,23 @@ from .engine import GpuSystem
 from .problem import ELASTIC, ElementLoadSet, Problem
 
 
+def shard_instances(n_dof, world):
+    """Independent instances split across `world` ranks (one GPU each, no data exchange
+    between them): largest first, each to the least-loaded rank (ties: the lower rank).
+    Returns, per rank, its instance indices in increasing order.  Every rank's DOF total
+    is then within the largest instance of every other rank's."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(n_dof)), key=lambda i: (-int(n_dof[i]), i))
+    load = [0] * world
+    out = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += int(n_dof[i])
+    return [sorted(o) for o in out]
+
+
 def union_problem(problems):
     """(union Problem, node_ptr, element_ptr) of a list of elasticity Problems that
     share the plane mode."""

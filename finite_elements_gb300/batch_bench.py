@@ -3,6 +3,8 @@ time, both on the GPU with the library's FP64 PCG (node-block Jacobi) to the sam
 relative residual.
 
     python -m finite_elements_gb300.batch_bench [--n 512] [--seed 0] [--tol 1e-8]
+    python -m torch.distributed.run --nproc-per-node N --master-addr 127.0.0.1 \
+        -m finite_elements_gb300.batch_bench      # the instances sharded over N GPUs
 
 Instances: triangle counts log-uniform in [2e3, 2e5], structured grids of aspect
 ratio U(1, 8), E ~ U(50, 300) GPa, nu ~ U(0.2, 0.4), random right-edge loads.  Prints
@@ -14,13 +16,61 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import time
 
 import numpy as np
 
 from . import meshgen
-from .batch import BatchedSystem
+from .batch import BatchedSystem, shard_instances
 from .engine import GpuSystem
+
+
+def run_sharded(a, probs_all, world):
+    """One rank of N: the instances of its shard (shard_instances) batched on its own GPU;
+    the ranks share only the barriers around the timed region and the reductions of the
+    results.  Rank 0 prints the line: DOF/s = all instances' DOF over the slowest rank's
+    device time (strong scaling: the total work is fixed)."""
+    import ctypes
+
+    import torch
+    import torch.distributed as td
+
+    from . import _lib
+    td.init_process_group("gloo")
+    rank = td.get_rank()
+    _lib.check(_lib.load().fe_set_device(int(os.environ.get("LOCAL_RANK", rank))), "fe_set_device")
+    shard = shard_instances([p.n_dof for p in probs_all], world)[rank]
+    probs = [probs_all[i] for i in shard]
+    w = BatchedSystem(probs[:4])
+    w.solve(tol=a.tol, want_x=False)
+    w.close()
+    b = BatchedSystem(probs)
+    tiles = b.autotune()
+    b.solve(tol=a.tol, want_x=False)                      # graph capture
+    h = b.system.handle
+    td.barrier()
+    h.call("fe_event_record", 0)
+    h.call("fe_assemble", 1 | 4 | 8)
+    h.call("fe_event_record", 1)
+    ms = ctypes.c_double()
+    h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
+    parts, st = b.solve(tol=a.tol, want_x=False)
+    dev_s = (ms.value + st["solve_ms"]) / 1e3
+    b.close()
+    t = torch.tensor([dev_s, float(st["relres"].max()), float(st["iterations"].max())], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    c = torch.tensor([float(sum(p.n_dof for p in probs)), float((st["status"] == 0).sum()), float(len(probs))],
+                     dtype=torch.float64)
+    td.all_reduce(c, op=td.ReduceOp.SUM)
+    if rank == 0:
+        print(json.dumps({
+            "workload": f"{len(probs_all)} plane-stress instances sharded over {world} GPUs (seed {a.seed})",
+            "n_gpus": world, "scaling": "strong", "tol": a.tol,
+            "instances": int(c[2]), "instances_converged": int(c[1]), "worst_relres": float(t[1]),
+            "max_iterations": int(t[2]), "tiles_rank0": tiles,
+            "slowest_rank_device_s": float(t[0]), "dof_per_s_device": float(c[0]) / float(t[0])}))
+    td.destroy_process_group()
 
 
 def main():
@@ -31,6 +81,10 @@ def main():
     ap.add_argument("--single", type=int, default=-1, help="instances solved one at a time (-1: all)")
     a = ap.parse_args()
     probs = meshgen.batch_c4(a.n, seed=a.seed)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        run_sharded(a, probs, world)
+        return
     dof = int(sum(p.n_dof for p in probs))
     tri = int(sum(p.n_elements for p in probs))
     # warm-up of the library (kernels, allocator) on a small batch
