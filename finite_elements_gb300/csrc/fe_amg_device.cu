@@ -8,6 +8,7 @@
 // WORK IN PROGRESS: not yet run on a GPU.
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "fe_amg_dev.h"
@@ -247,13 +248,52 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         h->launches += 2;
         return FE_OK;
     };
-    auto precond = [&]() -> int {   // z = M^-1 r: the FP32 V-cycle on r rounded to FP32
+    auto enqueue_cycle = [&]() -> int {   // z = M^-1 r: the FP32 V-cycle on r rounded to FP32
         ka_to_f32<<<gn, kAT, 0, s>>>(nd, r.p, L0.r.p);
         FE_LAUNCH_CHECK();
         FE_CHECK(vcycle_dev(h, G, 0, 3));
         ka_to_f64<<<gn, kAT, 0, s>>>(nd, L0.x.p, z.p);
         FE_LAUNCH_CHECK();
         h->launches += 2;
+        return FE_OK;
+    };
+    // the cycle's fixed sequence of launches (about ten per level) captured once as a
+    // CUDA graph, launched once per PCG iteration
+    cudaGraphExec_t cycle = nullptr;
+    struct GraphFree {
+        cudaGraphExec_t *g;
+        ~GraphFree() {
+            if (*g) cudaGraphExecDestroy(*g);
+        }
+    } gf{&cycle};
+    int64_t per_cycle = 0;
+    {
+        const int64_t l0 = h->launches;
+        cudaGraph_t g = nullptr;
+        FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_cycle();
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (rc != FE_OK) {
+            if (ce == cudaSuccess && g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ce != cudaSuccess) {
+            set_error(std::string("multigrid cycle capture: ") + cudaGetErrorString(ce));
+            return FE_CUDA_ERR;
+        }
+        ce = cudaGraphInstantiate(&cycle, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            cycle = nullptr;
+            set_error(std::string("multigrid cycle instantiate: ") + cudaGetErrorString(ce));
+            return FE_CUDA_ERR;
+        }
+        per_cycle = h->launches - l0;
+        h->launches = l0;
+    }
+    auto precond = [&]() -> int {
+        FE_CUDA(cudaGraphLaunch(cycle, s));
+        h->launches += per_cycle;
         return FE_OK;
     };
     FE_CUDA(cudaMemsetAsync(x, 0, nd * sizeof(double), s));
