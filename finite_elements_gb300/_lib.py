@@ -120,6 +120,7 @@ _SIGNATURES = {
     "fe_amg_level_matrix": ([_P, _I32, _I32, _P, _P, _P], C.c_int),
     "fe_amg_level_aggregates": ([_P, _I32, _P], C.c_int),
     "fe_amg_vcycle_host": ([_P, _I32, _P, _P], C.c_int),
+    "fe_amg_vcycle_host_f32": ([_P, _I32, _P, _P], C.c_int),
     "fe_amg_destroy": ([_P], C.c_int),
 }
 

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "fe_amg_dev.h"
+#include "fe_amg_cycle.cuh"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
@@ -21,45 +22,40 @@ namespace {
 constexpr int kAT = 256;
 inline int grid_a(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kAT - 1) / kAT, 152 * 8)); }
 
-__global__ void ka_chebyshev(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                             const float *__restrict__ val, const float *__restrict__ dinv, int d,
-                             const float *__restrict__ r, const float *__restrict__ zin, float *__restrict__ dir,
-                             float *__restrict__ zout, float a, float b, int first) {
+// the executor of the shared FP32 cycle (fe_amg_cycle.cuh): one grid-stride kernel per pass
+template <typename F>
+__global__ void ka_rows(int64_t n, F f) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        amg::row_chebyshev(ptr, col, val, dinv, d, r, zin, dir, zout, a, b, first != 0, i);
+        f(i);
 }
 
-template <typename T>
-__global__ void ka_residual(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                            const T *__restrict__ val, int d, const T *__restrict__ r, const T *__restrict__ x,
-                            T *__restrict__ t) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        amg::row_residual(ptr, col, val, d, r, x, t, i);
-}
+// t = r - A x in FP64 (the true residual of the PCG)
+struct PassResidual64 {
+    const int64_t *ptr; const int32_t *col; const double *val; int d; const double *r; const double *x; double *t;
+    FE_HD void operator()(int64_t i) const { amg::row_residual(ptr, col, val, d, r, x, t, i); }
+};
 
-__global__ void ka_restrict(int64_t nc, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                            const float *__restrict__ val, int m, int d, const float *__restrict__ t,
-                            float *__restrict__ rc) {
-    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nc; I += (int64_t)gridDim.x * blockDim.x)
-        amg::row_restrict(ptr, col, val, m, d, t, rc, I);
-}
-
-__global__ void ka_prolong_add(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                               const float *__restrict__ val, int d, int m, const float *__restrict__ xc,
-                               float *__restrict__ x) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        amg::row_prolong_add(ptr, col, val, d, m, xc, x, i);
-}
-
-__global__ void ka_to_f32(int64_t n, const double *__restrict__ in, float *__restrict__ out) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (float)in[i];
-}
-
-__global__ void ka_to_f64(int64_t n, const float *__restrict__ in, double *__restrict__ out) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (double)in[i];
-}
+struct CycleEx {
+    fe_handle_s *h;
+    template <class F>
+    int rows(int64_t n, const F &f) {
+        if (n <= 0) return FE_OK;
+        ka_rows<F><<<grid_a(n), kAT, 0, h->stream>>>(n, f);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    template <class T>
+    int copy(T *dst, const T *src, size_t n) {
+        if (n) FE_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+        return FE_OK;
+    }
+    template <class T>
+    int fill_zero(T *p, size_t n) {
+        if (n) FE_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), h->stream));
+        return FE_OK;
+    }
+};
 
 // q = A p with the level-0 matrix (block rows of size d)
 __global__ void ka_spmv(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
@@ -68,16 +64,6 @@ __global__ void ka_spmv(int64_t n, const int64_t *__restrict__ ptr, const int32_
         double out[6];
         amg::row_product(ptr, col, val, d, d, p, i, out);
         for (int k = 0; k < d; ++k) q[i * d + k] = out[k];
-    }
-}
-
-// x = Ainv r (dense, n x n, FP64 inverse and sums)
-__global__ void ka_dense(int64_t n, const double *__restrict__ ainv, const float *__restrict__ r,
-                         float *__restrict__ x) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0.0;
-        for (int64_t j = 0; j < n; ++j) acc += ainv[i * n + j] * (double)r[j];
-        x[i] = (float)acc;
     }
 }
 
@@ -126,73 +112,19 @@ __global__ void ka_direction(int64_t n, double beta, const double *__restrict__ 
         p[i] = fma(beta, p[i], z[i]);
 }
 
-// Chebyshev smoothing of level l into L.x (from zero, or from L.x with from_x0), FP32
-int chebyshev_dev(fe_handle_s *h, DevLevel &L, int k, bool from_x0) {
-    cudaStream_t s = h->stream;
-    const int d = L.A.rd;
-    const int64_t n = L.A.n, nd = n * d;
-    const double hi = 1.05 * L.lmax, lo = hi / 30.0;
-    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
-    if (!from_x0) FE_CUDA(cudaMemsetAsync(L.x.p, 0, nd * sizeof(float), s));
-    float *cur = L.x.p, *nxt = L.zn.p;
-    double rho = 1.0 / sigma;
-    ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.a32.p, L.dinv32.p, d, L.r.p, cur, L.dir.p, nxt,
-                                           0.0f, (float)(1.0 / theta), 1);
-    std::swap(cur, nxt);
-    for (int st = 1; st < k; ++st) {
-        const double rn = 1.0 / (2.0 * sigma - rho);
-        const double a = rn * rho, b = 2.0 * rn / delta;
-        rho = rn;
-        ka_chebyshev<<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.a32.p, L.dinv32.p, d, L.r.p, cur, L.dir.p,
-                                               nxt, (float)a, (float)b, 0);
-        std::swap(cur, nxt);
-    }
-    FE_LAUNCH_CHECK();
-    h->launches += k;
-    if (cur != L.x.p) FE_CUDA(cudaMemcpyAsync(L.x.p, cur, nd * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    return FE_OK;
-}
-
-// V-cycle on level l: L.r -> L.x, FP32
-int vcycle_dev(fe_handle_s *h, DevAmg &G, size_t l, int k) {
-    cudaStream_t s = h->stream;
-    if (l == G.L.size()) {
-        ka_dense<<<grid_a(G.nc), kAT, 0, s>>>(G.nc, G.cinv.p, G.rc.p, G.xc.p);
-        FE_LAUNCH_CHECK();
-        h->launches += 1;
-        return FE_OK;
-    }
-    DevLevel &L = G.L[l];
-    const int d = L.A.rd, m = L.P.cd;
-    const int64_t n = L.A.n;
-    FE_CHECK(chebyshev_dev(h, L, k, false));
-    ka_residual<float><<<grid_a(n), kAT, 0, s>>>(n, L.A.ptr.p, L.A.col.p, L.a32.p, d, L.r.p, L.x.p, L.t.p);
-    float *rc = l + 1 < G.L.size() ? G.L[l + 1].r.p : G.rc.p;
-    float *xc = l + 1 < G.L.size() ? G.L[l + 1].x.p : G.xc.p;
-    ka_restrict<<<grid_a(L.PT.n), kAT, 0, s>>>(L.PT.n, L.PT.ptr.p, L.PT.col.p, L.pt32.p, m, d, L.t.p, rc);
-    FE_LAUNCH_CHECK();
-    h->launches += 2;
-    FE_CHECK(vcycle_dev(h, G, l + 1, k));
-    ka_prolong_add<<<grid_a(n), kAT, 0, s>>>(n, L.P.ptr.p, L.P.col.p, L.p32.p, d, m, xc, L.x.p);
-    FE_LAUNCH_CHECK();
-    h->launches += 1;
-    return chebyshev_dev(h, L, k, true);
-}
-
 // FP32 copies of a level's values and its cycle vectors
 int prepare_cycle(fe_handle_s *h, DevLevel &L) {
-    cudaStream_t s = h->stream;
     const int d = L.A.rd, m = L.P.cd;
     const int64_t na = L.A.nnzb * d * d, np = L.P.nnzb * d * m, nt = L.PT.nnzb * m * d, ndi = L.A.n * d * d;
     FE_CHECK(dalloc(L.a32, (size_t)std::max<int64_t>(na, 1)));
     FE_CHECK(dalloc(L.p32, (size_t)std::max<int64_t>(np, 1)));
     FE_CHECK(dalloc(L.pt32, (size_t)std::max<int64_t>(nt, 1)));
     FE_CHECK(dalloc(L.dinv32, (size_t)std::max<int64_t>(ndi, 1)));
-    ka_to_f32<<<grid_a(na), kAT, 0, s>>>(na, L.A.val.p, L.a32.p);
-    ka_to_f32<<<grid_a(np), kAT, 0, s>>>(np, L.P.val.p, L.p32.p);
-    ka_to_f32<<<grid_a(nt), kAT, 0, s>>>(nt, L.PT.val.p, L.pt32.p);
-    ka_to_f32<<<grid_a(ndi), kAT, 0, s>>>(ndi, L.dinv.p, L.dinv32.p);
-    FE_LAUNCH_CHECK();
+    CycleEx ex{h};
+    FE_CHECK(ex.rows(na, amg::PassToF32{L.A.val.p, L.a32.p}));
+    FE_CHECK(ex.rows(np, amg::PassToF32{L.P.val.p, L.p32.p}));
+    FE_CHECK(ex.rows(nt, amg::PassToF32{L.PT.val.p, L.pt32.p}));
+    FE_CHECK(ex.rows(ndi, amg::PassToF32{L.dinv.p, L.dinv32.p}));
     const size_t v = (size_t)std::max<int64_t>(L.A.n * d, 1);
     FE_CHECK(dalloc(L.r, v));
     FE_CHECK(dalloc(L.x, v));
@@ -248,14 +180,22 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         h->launches += 2;
         return FE_OK;
     };
+    // the levels as the shared cycle sees them
+    std::vector<amg::CycleLevel> views(G.L.size());
+    for (size_t l = 0; l < G.L.size(); ++l) {
+        const DevLevel &D = G.L[l];
+        amg::CycleLevel &V = views[l];
+        V.n = D.A.n, V.d = D.A.rd, V.m = D.P.cd, V.lmax = D.lmax, V.nc = D.PT.n;
+        V.aptr = D.A.ptr.p, V.acol = D.A.col.p, V.a = D.a32.p, V.dinv = D.dinv32.p;
+        V.pptr = D.P.ptr.p, V.pcol = D.P.col.p, V.p = D.p32.p;
+        V.tptr = D.PT.ptr.p, V.tcol = D.PT.col.p, V.pt = D.pt32.p;
+        V.r = D.r.p, V.x = D.x.p, V.t = D.t.p, V.dir = D.dir.p, V.zn = D.zn.p;
+    }
+    amg::CycleCoarse coarse;
+    coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
+    CycleEx cex{h};
     auto enqueue_cycle = [&]() -> int {   // z = M^-1 r: the FP32 V-cycle on r rounded to FP32
-        ka_to_f32<<<gn, kAT, 0, s>>>(nd, r.p, L0.r.p);
-        FE_LAUNCH_CHECK();
-        FE_CHECK(vcycle_dev(h, G, 0, 3));
-        ka_to_f64<<<gn, kAT, 0, s>>>(nd, L0.x.p, z.p);
-        FE_LAUNCH_CHECK();
-        h->launches += 2;
-        return FE_OK;
+        return amg::precondition(cex, views, coarse, 3, r.p, z.p);
     };
     // the cycle's fixed sequence of launches (about ten per level) captured once as a
     // CUDA graph, launched once per PCG iteration
@@ -347,9 +287,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         h->launches += 1;
     }
     // true residual b - A x in FP64
-    ka_residual<double><<<grid_a(n), kAT, 0, s>>>(n, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, h->b.p, x, q.p);
-    FE_LAUNCH_CHECK();
-    h->launches += 1;
+    FE_CHECK(cex.rows(n, PassResidual64{L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, h->b.p, x, q.p}));
     FE_CHECK(dot(q.p, q.p, sc.p + 3));
     FE_CUDA(cudaMemcpyAsync(host + 3, sc.p + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));

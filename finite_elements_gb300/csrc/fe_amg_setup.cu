@@ -27,6 +27,7 @@
 #include "fe_amg.h"
 #include "fe_amg_dev.h"
 #include "fe_amg_par.cuh"
+#include "fe_amg_cycle.cuh"
 #include "fe_amg_passes.cuh"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
@@ -444,6 +445,11 @@ struct HostEx {
     int read(T *dst, const T *src, size_t n) {
         return copy(dst, src, n);
     }
+    template <class T>
+    int fill_zero(T *p, size_t n) {
+        if (n) std::memset(p, 0, n * sizeof(T));
+        return FE_OK;
+    }
     template <class F>
     int rows(int64_t n, const F &f) {
         parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
@@ -650,6 +656,44 @@ int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_pt
     }
     *out = h;
     return FE_OK;
+}
+
+// One V-cycle of the device's FP32 sequence (amg::precondition, fe_amg_cycle.cuh) run
+// on the host: FP32 copies of the levels, r rounded to FP32, x widened to FP64.
+int fe_amg_vcycle_host_f32(fe_amg h, int32_t k_smooth, const double *r, double *x) {
+    if (!h || !r || !x || k_smooth < 1 || h->levels.empty()) {
+        set_error("fe_amg_vcycle_host_f32: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    auto f32 = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
+    const size_t nl = h->levels.size();
+    std::vector<std::vector<float>> store;
+    store.reserve(nl * 9 + 2);
+    std::vector<amg::CycleLevel> levels(nl);
+    for (size_t l = 0; l < nl; ++l) {
+        const AmgLevel &H = h->levels[l];
+        amg::CycleLevel &L = levels[l];
+        L.n = H.A.n, L.d = H.A.rd, L.m = H.P.cd, L.lmax = H.lmax, L.nc = H.PT.n;
+        L.aptr = H.A.ptr.data(), L.acol = H.A.col.data();
+        L.pptr = H.P.ptr.data(), L.pcol = H.P.col.data();
+        L.tptr = H.PT.ptr.data(), L.tcol = H.PT.col.data();
+        store.push_back(f32(H.A.val)), L.a = store.back().data();
+        store.push_back(f32(H.dinv)), L.dinv = store.back().data();
+        store.push_back(f32(H.P.val)), L.p = store.back().data();
+        store.push_back(f32(H.PT.val)), L.pt = store.back().data();
+        float **vec[5] = {&L.r, &L.x, &L.t, &L.dir, &L.zn};
+        for (float **v : vec) {
+            store.emplace_back((size_t)std::max<int64_t>(L.n * L.d, 1), 0.0f);
+            *v = store.back().data();
+        }
+    }
+    amg::CycleCoarse C;
+    C.n = h->coarse.n * h->coarse.rd;
+    C.inv = h->coarse_inv.data();
+    store.emplace_back((size_t)std::max<int64_t>(C.n, 1), 0.0f), C.r = store.back().data();
+    store.emplace_back((size_t)std::max<int64_t>(C.n, 1), 0.0f), C.x = store.back().data();
+    HostEx ex;
+    return amg::precondition(ex, levels, C, k_smooth, r, x);
 }
 
 // One V-cycle x = M^-1 r on the host (k Chebyshev steps before and after each coarse

@@ -300,6 +300,9 @@ int fe_amg_level_aggregates(fe_amg a, int32_t level, int32_t *agg_host);
  * [1.05 lmax/30, 1.05 lmax]) before and after each coarse correction and a dense solve
  * of the coarsest level: the arithmetic the device cycle runs row by row. */
 int fe_amg_vcycle_host(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
+/* The device's FP32 cycle (FP32 copies of the levels, r rounded to FP32, FP64 coarsest
+ * inverse) run on the host: the sequence of passes the multigrid solve launches. */
+int fe_amg_vcycle_host_f32(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
 int fe_amg_destroy(fe_amg a);
 
 /* ---- learned warm start (no counterpart in the reference: an addition on top of the

@@ -210,3 +210,36 @@ def test_same_hierarchy_on_every_run():
         assert (a["A"] != b_["A"]).nnz == 0
         if "P" in a:
             assert (a["P"] != b_["P"]).nnz == 0 and np.array_equal(a["agg"], b_["agg"])
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_fp32_cycle_of_the_device_sequence(case):
+    """fe_amg_vcycle_host_f32 (the device's FP32 cycle, fe_amg_cycle.cuh, run on the
+    host) against the FP64 host cycle: one cycle within 1e-4, and PCG iteration counts
+    within one of the FP64 cycle's for elasticity; for the magnetostatic case (mu_r up
+    to 1000) the FP32 cycle needs 16 iterations where FP64 needs 13, so there the bound
+    is 25% more, plus one."""
+    A, b, B, d = problem(case)
+    lib, h, _ = build(A, B, d)
+    try:
+        r = np.random.default_rng(3).standard_normal(A.shape[0])
+        x64, x32 = np.empty_like(r), np.empty_like(r)
+        _lib.check(lib.fe_amg_vcycle_host(h, 3, _lib.ptr(r), _lib.ptr(x64)), "fe_amg_vcycle_host")
+        _lib.check(lib.fe_amg_vcycle_host_f32(h, 3, _lib.ptr(r), _lib.ptr(x32)), "fe_amg_vcycle_host_f32")
+        assert np.linalg.norm(x32 - x64) <= 1e-4 * np.linalg.norm(x64)
+        counts = {}
+        for fn in ("fe_amg_vcycle_host", "fe_amg_vcycle_host_f32"):
+            f = getattr(lib, fn)
+
+            def M(v, f=f):
+                v = np.ascontiguousarray(v)
+                out = np.empty_like(v)
+                f(h, 3, _lib.ptr(v), _lib.ptr(out))
+                return out
+            x, it = AMG.pcg(A, b, M)
+            assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b)
+            counts[fn] = it
+        slack = 0.25 * counts["fe_amg_vcycle_host"] if case == "magnetic" else 0
+        assert abs(counts["fe_amg_vcycle_host_f32"] - counts["fe_amg_vcycle_host"]) <= 1 + slack, counts
+    finally:
+        lib.fe_amg_destroy(h)
