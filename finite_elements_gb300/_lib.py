@@ -121,6 +121,7 @@ _SIGNATURES = {
     "fe_amg_level_aggregates": ([_P, _I32, _P], C.c_int),
     "fe_amg_vcycle_host": ([_P, _I32, _P, _P], C.c_int),
     "fe_amg_vcycle_host_f32": ([_P, _I32, _P, _P], C.c_int),
+    "fe_amg_pcg_host": ([_P, _I32, _P, _D, _I32, _P, _P, _P, _P], C.c_int),
     "fe_amg_destroy": ([_P], C.c_int),
 }
 

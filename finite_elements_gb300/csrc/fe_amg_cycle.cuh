@@ -9,6 +9,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <utility>
 #include <vector>
 
@@ -127,6 +128,101 @@ int precondition(Ex &ex, const std::vector<CycleLevel> &levels, const CycleCoars
     FE_CHECK(ex.rows(nd, PassToF32{r, L0.r}));
     FE_CHECK(vcycle(ex, levels, C, 0, k));
     return ex.rows(nd, PassToF64{L0.x, z});
+}
+
+}  // namespace amg
+}  // namespace fe
+
+namespace fe {
+namespace amg {
+
+// ------------------------------------------------------------------ the PCG around the cycle
+
+struct PassSpmv64 {
+    const int64_t *ptr; const int32_t *col; const double *val; int d; const double *p; double *q;
+    FE_HD void operator()(int64_t i) const {
+        double out[6];
+        row_product(ptr, col, val, d, d, p, i, out);
+        for (int k = 0; k < d; ++k) q[i * d + k] = out[k];
+    }
+};
+
+// x += alpha p, r -= alpha q
+struct PassUpdate {
+    double alpha; const double *p; const double *q; double *x; double *r;
+    FE_HD void operator()(int64_t i) const {
+        x[i] = fma(alpha, p[i], x[i]);
+        r[i] = fma(-alpha, q[i], r[i]);
+    }
+};
+
+// p = z + beta p
+struct PassDirection {
+    double beta; const double *z; double *p;
+    FE_HD void operator()(int64_t i) const { p[i] = fma(beta, p[i], z[i]); }
+};
+
+struct PassResidual64 {
+    const int64_t *ptr; const int32_t *col; const double *val; int d; const double *r; const double *x; double *t;
+    FE_HD void operator()(int64_t i) const { row_residual(ptr, col, val, d, r, x, t, i); }
+};
+
+// Work vectors of the PCG, n d doubles each.
+struct PcgVectors {
+    double *x, *r, *p, *q, *z;
+};
+
+// PCG on A x = b from x = 0 with z = precond() (reading v.r, writing v.z), to
+// ||r|| <= tol ||b|| on the recurrence; relres is the true residual recomputed in FP64.
+// status: FE_OK, FE_MAXITER, FE_BREAKDOWN (p.Ap <= 0) or FE_NONFINITE.
+template <class Ex, class Precond>
+int pcg(Ex &ex, int64_t n, int d, const int64_t *ptr, const int32_t *col, const double *val, const double *b,
+        const PcgVectors &v, Precond precond, double tol, int max_iter, int *iters, double *relres, int *status) {
+    const int64_t nd = n * d;
+    FE_CHECK(ex.fill_zero(v.x, (size_t)nd));
+    FE_CHECK(ex.copy(v.r, b, (size_t)nd));
+    FE_CHECK(precond());
+    FE_CHECK(ex.copy(v.p, v.z, (size_t)nd));
+    double rz = 0.0, bb = 0.0;
+    FE_CHECK(ex.dot(v.r, v.z, nd, &rz));
+    FE_CHECK(ex.dot(v.r, v.r, nd, &bb));
+    int it = 0, st = bb > 0.0 ? FE_MAXITER : FE_OK;
+    while (st == FE_MAXITER && it < max_iter) {
+        FE_CHECK(ex.rows(n, PassSpmv64{ptr, col, val, d, v.p, v.q}));
+        double pq = 0.0;
+        FE_CHECK(ex.dot(v.p, v.q, nd, &pq));
+        if (!(pq > 0.0) || !std::isfinite(pq)) {
+            st = std::isfinite(pq) ? FE_BREAKDOWN : FE_NONFINITE;
+            break;
+        }
+        FE_CHECK(ex.rows(nd, PassUpdate{rz / pq, v.p, v.q, v.x, v.r}));
+        ++it;
+        double rr = 0.0, rzn = 0.0;
+        FE_CHECK(ex.dot(v.r, v.r, nd, &rr));
+        if (!std::isfinite(rr)) {
+            st = FE_NONFINITE;
+            break;
+        }
+        if (rr <= tol * tol * bb) {
+            st = FE_OK;
+            break;
+        }
+        FE_CHECK(precond());
+        FE_CHECK(ex.dot(v.r, v.z, nd, &rzn));
+        if (!std::isfinite(rzn)) {
+            st = FE_NONFINITE;
+            break;
+        }
+        FE_CHECK(ex.rows(nd, PassDirection{rzn / rz, v.z, v.p}));
+        rz = rzn;
+    }
+    FE_CHECK(ex.rows(n, PassResidual64{ptr, col, val, d, b, v.x, v.q}));
+    double tr = 0.0;
+    FE_CHECK(ex.dot(v.q, v.q, nd, &tr));
+    *iters = it;
+    *relres = bb > 0.0 ? std::sqrt(std::max(tr, 0.0) / bb) : 0.0;
+    *status = st;
+    return FE_OK;
 }
 
 }  // namespace amg

@@ -1,9 +1,9 @@
 // Multigrid-preconditioned PCG on the device: the smoothed-aggregation hierarchy of
 // the eliminated system (set up on the device, fe_amg_device_setup.cu) and a V-cycle
-// whose kernels are loops of the row operations of fe_amg_rows.cuh -- the operations
-// the host cycle fe_amg_vcycle_host runs serially.  The PCG recurrence, its SpMV and
-// the true residual are FP64; the V-cycle runs in FP32 on FP32 copies of the levels
-// (a CPU emulation of the cycle in FP32 gave the FP64 cycle's PCG iteration counts).
+// and the PCG around its FP32 V-cycle, both written once over an executor
+// (fe_amg_cycle.cuh; fe_amg_pcg_host runs the same sequence on the host).  The PCG
+// recurrence, its SpMV and the true residual are FP64; the V-cycle runs in FP32 on FP32
+// copies of the levels and is captured once per solve as a CUDA graph.
 //
 // WORK IN PROGRESS: not yet run on a GPU.
 #include <algorithm>
@@ -27,44 +27,6 @@ template <typename F>
 __global__ void ka_rows(int64_t n, F f) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         f(i);
-}
-
-// t = r - A x in FP64 (the true residual of the PCG)
-struct PassResidual64 {
-    const int64_t *ptr; const int32_t *col; const double *val; int d; const double *r; const double *x; double *t;
-    FE_HD void operator()(int64_t i) const { amg::row_residual(ptr, col, val, d, r, x, t, i); }
-};
-
-struct CycleEx {
-    fe_handle_s *h;
-    template <class F>
-    int rows(int64_t n, const F &f) {
-        if (n <= 0) return FE_OK;
-        ka_rows<F><<<grid_a(n), kAT, 0, h->stream>>>(n, f);
-        FE_LAUNCH_CHECK();
-        h->launches += 1;
-        return FE_OK;
-    }
-    template <class T>
-    int copy(T *dst, const T *src, size_t n) {
-        if (n) FE_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
-        return FE_OK;
-    }
-    template <class T>
-    int fill_zero(T *p, size_t n) {
-        if (n) FE_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), h->stream));
-        return FE_OK;
-    }
-};
-
-// q = A p with the level-0 matrix (block rows of size d)
-__global__ void ka_spmv(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
-                        const double *__restrict__ val, int d, const double *__restrict__ p, double *__restrict__ q) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double out[6];
-        amg::row_product(ptr, col, val, d, d, p, i, out);
-        for (int k = 0; k < d; ++k) q[i * d + k] = out[k];
-    }
 }
 
 // deterministic dot products: per-block partials, then one block in block order
@@ -97,20 +59,41 @@ __global__ void ka_dot_final(int nb, const double *__restrict__ part, double *ou
     if (threadIdx.x == 0) *out = s;
 }
 
-// x += alpha p, r -= alpha q
-__global__ void ka_update(int64_t n, double alpha, const double *__restrict__ p, const double *__restrict__ q,
-                          double *__restrict__ x, double *__restrict__ r) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = fma(alpha, p[i], x[i]);
-        r[i] = fma(-alpha, q[i], r[i]);
+struct CycleEx {
+    fe_handle_s *h;
+    DBuf<double> part, sc;
+    ~CycleEx() { dfree(part), dfree(sc); }
+    int dot(const double *a, const double *b, int64_t n, double *out) {
+        const int g = grid_a(n);
+        FE_CHECK(dalloc(part, (size_t)g));
+        FE_CHECK(dalloc(sc, 1));
+        ka_dot<<<g, kAT, 0, h->stream>>>(n, a, b, part.p);
+        ka_dot_final<<<1, kAT, 0, h->stream>>>(g, part.p, sc.p);
+        FE_LAUNCH_CHECK();
+        h->launches += 2;
+        FE_CUDA(cudaMemcpyAsync(out, sc.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        FE_CUDA(cudaStreamSynchronize(h->stream));
+        return FE_OK;
     }
-}
-
-// p = z + beta p
-__global__ void ka_direction(int64_t n, double beta, const double *__restrict__ z, double *__restrict__ p) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = fma(beta, p[i], z[i]);
-}
+    template <class F>
+    int rows(int64_t n, const F &f) {
+        if (n <= 0) return FE_OK;
+        ka_rows<F><<<grid_a(n), kAT, 0, h->stream>>>(n, f);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    template <class T>
+    int copy(T *dst, const T *src, size_t n) {
+        if (n) FE_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+        return FE_OK;
+    }
+    template <class T>
+    int fill_zero(T *p, size_t n) {
+        if (n) FE_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), h->stream));
+        return FE_OK;
+    }
+};
 
 // FP32 copies of a level's values and its cycle vectors
 int prepare_cycle(fe_handle_s *h, DevLevel &L) {
@@ -155,48 +138,34 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         set_error("fe_solve: the multigrid hierarchy has a single level (use the other preconditioners)");
         return FE_BAD_INPUT;
     }
-    // PCG: level 0's r and x hold the V-cycle's input and output
+    // PCG vectors; the solution goes to the handle's x
     DevLevel &L0 = G.L[0];
-    DBuf<double> r, p, q, z, part, sc;
+    DBuf<double> r, p, q, z;
     struct Free {
-        DBuf<double> *b[6];
+        DBuf<double> *b[4];
         ~Free() {
             for (auto *x : b) dfree(*x);
         }
-    } fg{{&r, &p, &q, &z, &part, &sc}};
-    const int gn = grid_a(nd);
+    } fg{{&r, &p, &q, &z}};
     FE_CHECK(dalloc(h->w.x, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(dalloc(r, (size_t)nd));
-    FE_CHECK(dalloc(p, (size_t)nd));
-    FE_CHECK(dalloc(q, (size_t)nd));
-    FE_CHECK(dalloc(z, (size_t)nd));
-    FE_CHECK(dalloc(part, (size_t)gn));
-    FE_CHECK(dalloc(sc, 4));
-    double *x = h->w.x.p;
-    auto dot = [&](const double *a, const double *b, double *out) -> int {
-        ka_dot<<<gn, kAT, 0, s>>>(nd, a, b, part.p);
-        ka_dot_final<<<1, kAT, 0, s>>>(gn, part.p, out);
-        FE_LAUNCH_CHECK();
-        h->launches += 2;
-        return FE_OK;
-    };
+    FE_CHECK(dalloc(r, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(dalloc(p, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(dalloc(q, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(dalloc(z, (size_t)std::max<int64_t>(nd, 1)));
     // the levels as the shared cycle sees them
     std::vector<amg::CycleLevel> views(G.L.size());
     for (size_t l = 0; l < G.L.size(); ++l) {
-        const DevLevel &D = G.L[l];
+        const DevLevel &Dl = G.L[l];
         amg::CycleLevel &V = views[l];
-        V.n = D.A.n, V.d = D.A.rd, V.m = D.P.cd, V.lmax = D.lmax, V.nc = D.PT.n;
-        V.aptr = D.A.ptr.p, V.acol = D.A.col.p, V.a = D.a32.p, V.dinv = D.dinv32.p;
-        V.pptr = D.P.ptr.p, V.pcol = D.P.col.p, V.p = D.p32.p;
-        V.tptr = D.PT.ptr.p, V.tcol = D.PT.col.p, V.pt = D.pt32.p;
-        V.r = D.r.p, V.x = D.x.p, V.t = D.t.p, V.dir = D.dir.p, V.zn = D.zn.p;
+        V.n = Dl.A.n, V.d = Dl.A.rd, V.m = Dl.P.cd, V.lmax = Dl.lmax, V.nc = Dl.PT.n;
+        V.aptr = Dl.A.ptr.p, V.acol = Dl.A.col.p, V.a = Dl.a32.p, V.dinv = Dl.dinv32.p;
+        V.pptr = Dl.P.ptr.p, V.pcol = Dl.P.col.p, V.p = Dl.p32.p;
+        V.tptr = Dl.PT.ptr.p, V.tcol = Dl.PT.col.p, V.pt = Dl.pt32.p;
+        V.r = Dl.r.p, V.x = Dl.x.p, V.t = Dl.t.p, V.dir = Dl.dir.p, V.zn = Dl.zn.p;
     }
     amg::CycleCoarse coarse;
     coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
     CycleEx cex{h};
-    auto enqueue_cycle = [&]() -> int {   // z = M^-1 r: the FP32 V-cycle on r rounded to FP32
-        return amg::precondition(cex, views, coarse, 3, r.p, z.p);
-    };
     // the cycle's fixed sequence of launches (about ten per level) captured once as a
     // CUDA graph, launched once per PCG iteration
     cudaGraphExec_t cycle = nullptr;
@@ -211,7 +180,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         const int64_t l0 = h->launches;
         cudaGraph_t g = nullptr;
         FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_cycle();
+        const int rc = amg::precondition(cex, views, coarse, 3, r.p, z.p);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc != FE_OK) {
             if (ce == cudaSuccess && g) cudaGraphDestroy(g);
@@ -236,69 +205,22 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         h->launches += per_cycle;
         return FE_OK;
     };
-    FE_CUDA(cudaMemsetAsync(x, 0, nd * sizeof(double), s));
-    FE_CUDA(cudaMemcpyAsync(r.p, h->b.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    FE_CHECK(precond());
-    FE_CUDA(cudaMemcpyAsync(p.p, z.p, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    FE_CHECK(dot(r.p, z.p, sc.p));
-    FE_CHECK(dot(r.p, r.p, sc.p + 1));
-    double host[4];
-    FE_CUDA(cudaMemcpyAsync(host, sc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    double rz = host[0];
-    const double bb = host[1];
     const double tol = o->tol > 0 ? o->tol : 1e-10;
     const int max_iter = o->max_iter > 0 ? o->max_iter : 10000;
-    int it = 0, status = bb > 0.0 ? FE_MAXITER : FE_OK;
-    double rr = bb;
-    while (status == FE_MAXITER && it < max_iter) {
-        ka_spmv<<<grid_a(n), kAT, 0, s>>>(n, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, p.p, q.p);
-        FE_LAUNCH_CHECK();
-        FE_CHECK(dot(p.p, q.p, sc.p + 2));
-        FE_CUDA(cudaMemcpyAsync(host + 2, sc.p + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
-        FE_CUDA(cudaStreamSynchronize(s));
-        if (!(host[2] > 0.0) || !std::isfinite(host[2])) {
-            status = std::isfinite(host[2]) ? FE_BREAKDOWN : FE_NONFINITE;
-            break;
-        }
-        const double alpha = rz / host[2];
-        ka_update<<<gn, kAT, 0, s>>>(nd, alpha, p.p, q.p, x, r.p);
-        FE_LAUNCH_CHECK();
-        h->launches += 2;
-        ++it;
-        FE_CHECK(dot(r.p, r.p, sc.p + 1));
-        FE_CHECK(precond());
-        FE_CHECK(dot(r.p, z.p, sc.p));
-        FE_CUDA(cudaMemcpyAsync(host, sc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-        FE_CUDA(cudaStreamSynchronize(s));
-        rr = host[1];
-        if (!std::isfinite(rr) || !std::isfinite(host[0])) {
-            status = FE_NONFINITE;
-            break;
-        }
-        if (rr <= tol * tol * bb) {
-            status = FE_OK;
-            break;
-        }
-        const double beta = host[0] / rz;
-        rz = host[0];
-        ka_direction<<<gn, kAT, 0, s>>>(nd, beta, z.p, p.p);
-        FE_LAUNCH_CHECK();
-        h->launches += 1;
-    }
-    // true residual b - A x in FP64
-    FE_CHECK(cex.rows(n, PassResidual64{L0.A.ptr.p, L0.A.col.p, L0.A.val.p, D, h->b.p, x, q.p}));
-    FE_CHECK(dot(q.p, q.p, sc.p + 3));
-    FE_CUDA(cudaMemcpyAsync(host + 3, sc.p + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    rr = host[3];
+    int it = 0, status = FE_OK;
+    double relres = 0.0;
+    const amg::PcgVectors v{h->w.x.p, r.p, p.p, q.p, z.p};
+    FE_CHECK(amg::pcg(cex, n, D, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, h->b.p, v, precond, tol, max_iter, &it,
+                      &relres, &status));
+    double bb = 0.0;
+    FE_CHECK(cex.dot(h->b.p, h->b.p, nd, &bb));
     st->iterations = it;
     st->spmv = it + 1;
     st->outer = 0;
     st->fp64_iterations = 0;
     st->x0_used = 0;
     st->bnorm = std::sqrt(bb);
-    st->relres = bb > 0.0 ? std::sqrt(std::max(rr, 0.0) / bb) : 0.0;
+    st->relres = relres;
     st->status = status;
     FE_CHECK(recover_multipliers(h));
     FE_CUDA(cudaEventRecord(h->events[7], s));

@@ -658,6 +658,51 @@ int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_pt
     return FE_OK;
 }
 
+}  // extern "C"
+
+namespace fe {
+namespace {
+
+// FP32 copies of a host hierarchy and its cycle vectors, viewed as the shared cycle
+// (fe_amg_cycle.cuh) sees the device's.
+struct HostCycle {
+    std::vector<std::vector<float>> store;
+    std::vector<amg::CycleLevel> levels;
+    amg::CycleCoarse coarse;
+    explicit HostCycle(const fe_amg_s *h) {
+        auto f32 = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
+        const size_t nl = h->levels.size();
+        store.reserve(nl * 9 + 2);
+        levels.resize(nl);
+        for (size_t l = 0; l < nl; ++l) {
+            const AmgLevel &H = h->levels[l];
+            amg::CycleLevel &L = levels[l];
+            L.n = H.A.n, L.d = H.A.rd, L.m = H.P.cd, L.lmax = H.lmax, L.nc = H.PT.n;
+            L.aptr = H.A.ptr.data(), L.acol = H.A.col.data();
+            L.pptr = H.P.ptr.data(), L.pcol = H.P.col.data();
+            L.tptr = H.PT.ptr.data(), L.tcol = H.PT.col.data();
+            store.push_back(f32(H.A.val)), L.a = store.back().data();
+            store.push_back(f32(H.dinv)), L.dinv = store.back().data();
+            store.push_back(f32(H.P.val)), L.p = store.back().data();
+            store.push_back(f32(H.PT.val)), L.pt = store.back().data();
+            float **vec[5] = {&L.r, &L.x, &L.t, &L.dir, &L.zn};
+            for (float **v : vec) {
+                store.emplace_back((size_t)std::max<int64_t>(L.n * L.d, 1), 0.0f);
+                *v = store.back().data();
+            }
+        }
+        coarse.n = h->coarse.n * h->coarse.rd;
+        coarse.inv = h->coarse_inv.data();
+        store.emplace_back((size_t)std::max<int64_t>(coarse.n, 1), 0.0f), coarse.r = store.back().data();
+        store.emplace_back((size_t)std::max<int64_t>(coarse.n, 1), 0.0f), coarse.x = store.back().data();
+    }
+};
+
+}  // namespace
+}  // namespace fe
+
+extern "C" {
+
 // One V-cycle of the device's FP32 sequence (amg::precondition, fe_amg_cycle.cuh) run
 // on the host: FP32 copies of the levels, r rounded to FP32, x widened to FP64.
 int fe_amg_vcycle_host_f32(fe_amg h, int32_t k_smooth, const double *r, double *x) {
@@ -665,35 +710,31 @@ int fe_amg_vcycle_host_f32(fe_amg h, int32_t k_smooth, const double *r, double *
         set_error("fe_amg_vcycle_host_f32: bad arguments");
         return FE_BAD_INPUT;
     }
-    auto f32 = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
-    const size_t nl = h->levels.size();
-    std::vector<std::vector<float>> store;
-    store.reserve(nl * 9 + 2);
-    std::vector<amg::CycleLevel> levels(nl);
-    for (size_t l = 0; l < nl; ++l) {
-        const AmgLevel &H = h->levels[l];
-        amg::CycleLevel &L = levels[l];
-        L.n = H.A.n, L.d = H.A.rd, L.m = H.P.cd, L.lmax = H.lmax, L.nc = H.PT.n;
-        L.aptr = H.A.ptr.data(), L.acol = H.A.col.data();
-        L.pptr = H.P.ptr.data(), L.pcol = H.P.col.data();
-        L.tptr = H.PT.ptr.data(), L.tcol = H.PT.col.data();
-        store.push_back(f32(H.A.val)), L.a = store.back().data();
-        store.push_back(f32(H.dinv)), L.dinv = store.back().data();
-        store.push_back(f32(H.P.val)), L.p = store.back().data();
-        store.push_back(f32(H.PT.val)), L.pt = store.back().data();
-        float **vec[5] = {&L.r, &L.x, &L.t, &L.dir, &L.zn};
-        for (float **v : vec) {
-            store.emplace_back((size_t)std::max<int64_t>(L.n * L.d, 1), 0.0f);
-            *v = store.back().data();
-        }
-    }
-    amg::CycleCoarse C;
-    C.n = h->coarse.n * h->coarse.rd;
-    C.inv = h->coarse_inv.data();
-    store.emplace_back((size_t)std::max<int64_t>(C.n, 1), 0.0f), C.r = store.back().data();
-    store.emplace_back((size_t)std::max<int64_t>(C.n, 1), 0.0f), C.x = store.back().data();
+    HostCycle c(h);
     HostEx ex;
-    return amg::precondition(ex, levels, C, k_smooth, r, x);
+    return amg::precondition(ex, c.levels, c.coarse, k_smooth, r, x);
+}
+
+// The device's multigrid PCG (amg::pcg around the FP32 cycle) run on the host, on the
+// hierarchy's level-0 matrix: x from zero, to ||r|| <= tol ||b||.
+int fe_amg_pcg_host(fe_amg h, int32_t k_smooth, const double *b, double tol, int32_t max_iter, double *x,
+                    int32_t *iters, double *relres, int32_t *status) {
+    if (!h || !b || !x || !iters || !relres || !status || k_smooth < 1 || h->levels.empty() || max_iter < 1) {
+        set_error("fe_amg_pcg_host: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    HostCycle c(h);
+    HostEx ex;
+    const BlockCsr &A = h->levels[0].A;
+    const size_t nd = (size_t)(A.n * A.rd);
+    std::vector<double> r(nd), p(nd), q(nd), z(nd);
+    const amg::PcgVectors v{x, r.data(), p.data(), q.data(), z.data()};
+    auto precond = [&]() { return amg::precondition(ex, c.levels, c.coarse, k_smooth, v.r, v.z); };
+    int it = 0, st = 0;
+    FE_CHECK(amg::pcg(ex, A.n, A.rd, A.ptr.data(), A.col.data(), A.val.data(), b, v, precond, tol, max_iter, &it,
+                      relres, &st));
+    *iters = it, *status = st;
+    return FE_OK;
 }
 
 // One V-cycle x = M^-1 r on the host (k Chebyshev steps before and after each coarse

@@ -303,6 +303,12 @@ int fe_amg_vcycle_host(fe_amg a, int32_t k_smooth, const double *r_host, double 
 /* The device's FP32 cycle (FP32 copies of the levels, r rounded to FP32, FP64 coarsest
  * inverse) run on the host: the sequence of passes the multigrid solve launches. */
 int fe_amg_vcycle_host_f32(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
+/* The device's multigrid PCG (FP64 recurrence around the FP32 cycle) run on the host on
+ * the hierarchy's level-0 matrix: x (host, n DOFs) from zero to ||r|| <= tol ||b||;
+ * iterations, the true relative residual and the status (FE_OK, FE_MAXITER,
+ * FE_BREAKDOWN, FE_NONFINITE) come back through the pointers. */
+int fe_amg_pcg_host(fe_amg a, int32_t k_smooth, const double *b_host, double tol, int32_t max_iter, double *x_host,
+                    int32_t *iterations, double *relres, int32_t *status);
 int fe_amg_destroy(fe_amg a);
 
 /* ---- learned warm start (no counterpart in the reference: an addition on top of the

@@ -243,3 +243,36 @@ def test_fp32_cycle_of_the_device_sequence(case):
         assert abs(counts["fe_amg_vcycle_host_f32"] - counts["fe_amg_vcycle_host"]) <= 1 + slack, counts
     finally:
         lib.fe_amg_destroy(h)
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_multigrid_pcg_sequence_on_the_host(case):
+    """fe_amg_pcg_host: the device solve's PCG around the FP32 cycle (fe_amg_cycle.cuh)
+    run on the host, against the model's PCG with the same FP32 cycle: the same
+    iteration count, a true residual below the tolerance, and the solution of the
+    direct solve."""
+    import ctypes
+
+    import scipy.sparse.linalg as spla
+    A, b, B, d = problem(case)
+    lib, h, _ = build(A, B, d)
+    try:
+        x = np.empty_like(b)
+        it, rel, st = ctypes.c_int32(), ctypes.c_double(), ctypes.c_int32()
+        bb = np.ascontiguousarray(b)
+        _lib.check(lib.fe_amg_pcg_host(h, 3, _lib.ptr(bb), 1e-10, 500, _lib.ptr(x), ctypes.byref(it),
+                                       ctypes.byref(rel), ctypes.byref(st)), "fe_amg_pcg_host")
+        assert st.value == 0 and rel.value <= 2e-10, (st.value, rel.value)
+        assert np.linalg.norm(A @ x - b) <= 2e-10 * np.linalg.norm(b)
+
+        def M(v):
+            v = np.ascontiguousarray(v)
+            out = np.empty_like(v)
+            lib.fe_amg_vcycle_host_f32(h, 3, _lib.ptr(v), _lib.ptr(out))
+            return out
+        _, it_model = AMG.pcg(A, b, M, tol=1e-10)
+        assert abs(it.value - it_model) <= 1, (it.value, it_model)
+        xd = spla.spsolve(A.tocsc(), b)
+        assert np.linalg.norm(x - xd) <= 1e-7 * np.linalg.norm(xd)
+    finally:
+        lib.fe_amg_destroy(h)
