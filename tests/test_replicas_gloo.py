@@ -70,3 +70,9 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
     rec = json.loads(lines[0])
     assert rec["impl"] == "reference" and rec["n_gpus"] == 2 and rec["value"] > 0
     assert rec["cpu_baseline"]["kind"] == "port" and rec["e2e"]["h2d_bytes_per_step"] == 0
+    # the sample's time carried to the 2000 x 1000 workload's DOF in proportion
+    cb = rec["cpu_baseline"]
+    assert cb["sample_dof"] == 2 * 21 * 11
+    full = 2 * 2001 * 1001
+    assert abs(rec["value"] - cb["sample_s"] * full / cb["sample_dof"]) <= 1e-9 * rec["value"]
+    assert rec["e2e"]["value"] == rec["value"] == cb["value"]
