@@ -344,6 +344,7 @@ FE_HD void row_product_values(const int64_t *aptr, const int32_t *acol, const do
         for (int64_t t = bptr[j]; t < bptr[j + 1]; ++t) {
             const double *b = &bval[t * ca * cb];
             const int64_t p = find_sorted(ccol, cptr[i], cptr[i + 1], bcol[t]);
+            if (p < 0) continue;   // cannot happen: the columns come from these products
             double *o = &cval[p * bs];
             for (int x = 0; x < ra; ++x)
                 for (int z = 0; z < cb; ++z) {
