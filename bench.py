@@ -62,6 +62,8 @@ def parse_args():
                     help="headline steps only (no plain / oracle / e2e legs), for profiler runs")
     ap.add_argument("--quick-plain", action="store_true",
                     help="with --quick: time the plain FP64 PCG step instead of the headline")
+    ap.add_argument("--quick-multigrid", action="store_true",
+                    help="time only the multigrid-preconditioned solve (device setup + FP32 V-cycle PCG)")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--l2-keep", type=float, default=-1.0,
@@ -259,6 +261,23 @@ def run_ours(args, dist):
         h.call("fe_profile_read", precision, ctypes.byref(cm), ctypes.byref(cn), ctypes.byref(sm), ctypes.byref(sn))
         return {"cheb_us": 1e3 * cm.value / max(cn.value, 1), "cheb_n": cn.value,
                 "spmv_us": 1e3 * sm.value / max(sn.value, 1), "spmv_n": sn.value}
+
+    if args.quick_multigrid:
+        # the multigrid step: assembly, device setup of the hierarchy, PCG with the V-cycle
+        mg = dict(precision="fp64", tol=args.tol, want_host=False, multigrid=True)
+        for _ in range(args.warmup):
+            device_step(mg)
+        h.call("fe_synchronize")
+        h.call("fe_event_record", 0)
+        mst = [device_step(mg) for _ in range(args.steps)]
+        h.call("fe_event_record", 1)
+        h.call("fe_synchronize")
+        ms = ctypes.c_double()
+        h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
+        s.close()
+        return {"metric": METRIC, "multigrid_s_per_solve": ms.value / 1e3 / args.steps, "quick": True,
+                "iterations": mst[-1].iterations, "relres": mst[-1].relres,
+                "solve_ms": mst[-1].solve_ms, "assemble_ms": mst[-1].assemble_ms}
 
     if args.quick and args.quick_plain:
         # profiler runs of the plain FP64 step: no event records, no other legs

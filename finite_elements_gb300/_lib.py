@@ -22,6 +22,7 @@ FE_MAT_K_AUGMENTED, FE_MAT_K_CSC, FE_MAT_M_CSC = 1, 2, 3
 FE_PREC_FP64, FE_PREC_MIXED, FE_PREC_MIXED_CG64 = 0, 1, 2
 FE_MODAL_SMALLEST, FE_MODAL_LARGEST = 0, 1
 FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP, FE_SOLVE_X0_IF_BETTER = 1, 2, 4
+FE_SOLVE_MULTIGRID = 8
 
 STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",
                 FE_NONFINITE: "FE_NONFINITE", FE_BAD_INPUT: "FE_BAD_INPUT",
@@ -114,11 +115,15 @@ _SIGNATURES = {
     "fe_batch_last_run": ([_P, _PI32, _PI32, _PI32, _PI32], C.c_int),
     "fe_scan_counts_noalloc": ([_P, _P, _I64, _P], C.c_int),
     "fe_amg_build_host": ([_I64, _I32, _P, _P, _P, _I32, _P, _D, _I64, C.POINTER(_P)], C.c_int),
+    "fe_amg_build_parallel_host": ([_I64, _I32, _P, _P, _P, _I32, _P, _D, _I64, C.POINTER(_P)], C.c_int),
+    "fe_amg_build_device": ([_P, _D, _I64, C.POINTER(_P)], C.c_int),
     "fe_amg_levels": ([_P, _PI32], C.c_int),
     "fe_amg_level_info": ([_P, _I32, _PI64, _PI32, _PI64, _PI64, _PI64, _PI32, _PD], C.c_int),
     "fe_amg_level_matrix": ([_P, _I32, _I32, _P, _P, _P], C.c_int),
     "fe_amg_level_aggregates": ([_P, _I32, _P], C.c_int),
     "fe_amg_vcycle_host": ([_P, _I32, _P, _P], C.c_int),
+    "fe_amg_vcycle_host_f32": ([_P, _I32, _P, _P], C.c_int),
+    "fe_amg_pcg_host": ([_P, _I32, _P, _D, _I32, _P, _P, _P, _P], C.c_int),
     "fe_amg_destroy": ([_P], C.c_int),
 }
 

@@ -1,0 +1,59 @@
+// The smoothed-aggregation hierarchy in device memory: set up by fe_amg_device_setup.cu,
+// applied as a V-cycle by fe_amg_device.cu.
+#pragma once
+
+#include <vector>
+
+#include "fe_amg.h"
+#include "fe_amg_passes.cuh"
+#include "fe_internal.h"
+
+namespace fe {
+
+using DevCsr = amg::Csr;
+
+inline void drelease(DevCsr &c) {
+    dfree(c.ptr), dfree(c.col), dfree(c.val);
+    c.nnzb = 0;
+}
+
+struct DevLevel {
+    DevCsr A, P, PT;
+    DBuf<double> dinv;
+    DBuf<int32_t> agg;
+    double lmax = 0.0;
+    // the V-cycle runs in FP32: values of A, P, P^T and D^-1, and the level's vectors
+    // (n * d each; r, x: the level's right-hand side and iterate)
+    DBuf<float> a32, p32, pt32, dinv32;
+    DBuf<float> r, x, t, dir, zn;
+    void release() {
+        drelease(A), drelease(P), drelease(PT);
+        dfree(dinv), dfree(agg), dfree(a32), dfree(p32), dfree(pt32), dfree(dinv32);
+        dfree(r), dfree(x), dfree(t), dfree(dir), dfree(zn);
+    }
+};
+
+struct DevAmg {
+    std::vector<DevLevel> L;
+    DevCsr coarse;
+    int64_t nc = 0;                  // coarsest DOFs
+    DBuf<double> cinv;               // dense inverse of the coarsest matrix (FP64)
+    DBuf<float> rc, xc;
+    int mis_rounds = 0;              // independent-set rounds, all levels
+    ~DevAmg() {
+        for (auto &l : L) l.release();
+        drelease(coarse);
+        dfree(cinv), dfree(rc), dfree(xc);
+    }
+};
+
+// Device setup of the hierarchy of the handle's eliminated system (near-null space: the
+// rigid-body modes for elasticity, the constant for magnetostatics, zero on the
+// constrained DOFs): amg::setup_hierarchy on the device executor.
+int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G);
+// Copy of a device hierarchy into host form (accessors of the fe_amg_* ABI).
+int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s);
+// Dense inverse of the coarsest matrix (+ 1e-12 of its largest diagonal entry).
+int coarse_inverse_of(const BlockCsr &C, std::vector<double> &inv, const char *who);
+
+}  // namespace fe

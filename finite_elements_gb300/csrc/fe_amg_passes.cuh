@@ -1,0 +1,440 @@
+// The parallel smoothed-aggregation setup written once for two executors: the device
+// (fe_amg_device_setup.cu: each pass a grid-stride kernel over its rows, int64 scans
+// on the device) and the host (fe_amg_setup.cu: the same passes over row chunks on
+// host threads).  Every pass is a functor over one row (or one aggregate) built on the
+// row operations of fe_amg_par.cuh; the sequence of passes, the buffer sizes and the
+// scans that size them are this file's, shared by both, so the host run (checked on
+// the CPU against the model) exercises the device's bookkeeping too.
+//
+// An executor Ex provides:
+//   template <class T> int alloc(DBuf<T> &b, size_t n);  template <class T> void release(DBuf<T> &b);
+//   template <class T> int copy(T *dst, const T *src, size_t n);       // same memory space
+//   template <class T> int read(T *host_dst, const T *src, size_t n);  // to the host, synchronous
+//   template <class F> int rows(int64_t n, const F &f);                // f(i) for i < n, any order
+//   int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total);   // exclusive, out[n] = total
+//   int dot(const double *a, const double *b, int64_t n, double *out);      // host value
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fe_amg.h"
+#include "fe_amg_par.cuh"
+#include "fe_internal.h"
+
+namespace fe {
+namespace amg {
+
+// ------------------------------------------------------------------ storage
+
+struct Csr {
+    int64_t n = 0;
+    int rd = 0, cd = 0;
+    int64_t nnzb = 0;
+    DBuf<int64_t> ptr;   // n + 1
+    DBuf<int32_t> col;
+    DBuf<double> val;    // nnzb row-major rd x cd blocks
+};
+
+struct Level {
+    Csr A, P, PT;
+    DBuf<double> dinv;
+    DBuf<int32_t> agg;
+    double lmax = 0.0;
+};
+
+template <class Ex>
+void release(Ex &ex, Csr &c) {
+    ex.release(c.ptr), ex.release(c.col), ex.release(c.val);
+    c.nnzb = 0;
+}
+
+template <class Ex>
+void release(Ex &ex, Level &l) {
+    release(ex, l.A), release(ex, l.P), release(ex, l.PT);
+    ex.release(l.dinv), ex.release(l.agg);
+}
+
+// ------------------------------------------------------------------ passes
+
+struct PassDinv {
+    const int64_t *ptr; const int32_t *col; const double *val; int d; double *dinv;
+    FE_HD void operator()(int64_t i) const {
+        double *o = &dinv[i * d * d];
+        for (int k = 0; k < d * d; ++k) o[k] = 0.0;
+        for (int64_t s = ptr[i]; s < ptr[i + 1]; ++s)
+            if (col[s] == i) sym_pinv(&val[s * d * d], d, o);
+    }
+};
+
+struct PassPowerStart {
+    double *x;
+    FE_HD void operator()(int64_t i) const { x[i] = 1.0 + (double)(i % 7) / 7.0; }
+};
+
+struct PassDinvProduct {
+    const int64_t *ptr; const int32_t *col; const double *val; const double *dinv; int d; const double *x; double *y;
+    FE_HD void operator()(int64_t i) const { row_dinv_product(ptr, col, val, dinv, d, x, i, y); }
+};
+
+struct PassScale {
+    const double *y; double c; double *x;
+    FE_HD void operator()(int64_t i) const { x[i] = y[i] * c; }
+};
+
+struct PassBlockNorms {
+    const int64_t *ptr; const int32_t *col; const double *val; int d; double *nrm; double *dg;
+    FE_HD void operator()(int64_t i) const { row_block_norms(ptr, col, val, d, i, nrm, dg); }
+};
+
+struct PassStrength {
+    const int64_t *ptr; const int32_t *col; const double *nrm; const double *dg; double theta; uint8_t *strong;
+    FE_HD void operator()(int64_t i) const { row_strength(ptr, col, nrm, dg, theta, i, strong); }
+};
+
+struct PassStateInit {
+    uint32_t *state;
+    FE_HD void operator()(int64_t i) const { state[i] = kUndecided; }
+};
+
+struct PassMisKey {
+    const uint32_t *state; uint64_t *key;
+    FE_HD void operator()(int64_t i) const { key[i] = mis_key(state[i], i); }
+};
+
+struct PassMaxKey {
+    const int64_t *ptr; const int32_t *col; const uint8_t *strong; const uint64_t *in; uint64_t *out;
+    FE_HD void operator()(int64_t i) const { row_max_key(ptr, col, strong, in, i, out); }
+};
+
+// decides node i; flag[i] = 1 while it stays undecided
+struct PassMisDecide {
+    const uint64_t *m2; uint32_t *state; int64_t *flag;
+    FE_HD void operator()(int64_t i) const { flag[i] = mis_decide(m2, i, state); }
+};
+
+struct PassRootFlags {
+    const uint32_t *state; int64_t *flag;
+    FE_HD void operator()(int64_t i) const { flag[i] = state[i] == kIn ? 1 : 0; }
+};
+
+struct PassRoots {
+    const uint32_t *state; const int64_t *off; int32_t *rank; int32_t *roots;
+    FE_HD void operator()(int64_t i) const {
+        if (state[i] == kIn) {
+            rank[i] = (int32_t)off[i];
+            roots[off[i]] = (int32_t)i;
+        } else {
+            rank[i] = -1;
+        }
+    }
+};
+
+struct PassJoinRoot {
+    const int64_t *ptr; const int32_t *col; const uint8_t *strong; const double *nrm; const uint32_t *state;
+    const int32_t *rank; int32_t *agg1;
+    FE_HD void operator()(int64_t i) const { row_join_root(ptr, col, strong, nrm, state, rank, i, agg1); }
+};
+
+// flag[i] = 1 for a node left without an aggregate
+struct PassJoinNeighbour {
+    const int64_t *ptr; const int32_t *col; const uint8_t *strong; const double *nrm; const int32_t *agg1;
+    int32_t *agg; int64_t *flag;
+    FE_HD void operator()(int64_t i) const {
+        row_join_neighbour(ptr, col, strong, nrm, agg1, i, agg);
+        flag[i] = agg[i] < 0 ? 1 : 0;
+    }
+};
+
+struct PassMemberBound {
+    const int64_t *ptr; const int32_t *col; const int32_t *roots; int64_t *bound;
+    FE_HD void operator()(int64_t c) const { bound[c] = agg_member_bound(ptr, col, roots, c); }
+};
+
+struct PassMembers {
+    const int64_t *ptr; const int32_t *col; const int32_t *roots; const int32_t *agg; const int64_t *boff;
+    int32_t *cand; int64_t *cnt;
+    FE_HD void operator()(int64_t c) const { cnt[c] = agg_members(ptr, col, roots, agg, c, cand + boff[c]); }
+};
+
+// packed rows: dst[off[r] ..] = src[boff[r] ..], off[r+1] - off[r] entries
+struct PassPackRows {
+    const int64_t *boff; const int64_t *off; const int32_t *src; int32_t *dst;
+    FE_HD void operator()(int64_t r) const {
+        const int64_t len = off[r + 1] - off[r];
+        for (int64_t k = 0; k < len; ++k) dst[off[r] + k] = src[boff[r] + k];
+    }
+};
+
+struct PassIota {
+    int64_t *p;
+    FE_HD void operator()(int64_t i) const { p[i] = i; }
+};
+
+struct PassQr {
+    const int64_t *mptr; const int32_t *mem; int d; int m; double *pt; double *Bc;
+    FE_HD void operator()(int64_t c) const { aggregate_qr(mem + mptr[c], mptr[c + 1] - mptr[c], d, m, pt, Bc + c * m * m); }
+};
+
+struct PassProdBound {
+    const int64_t *aptr; const int32_t *acol; const int64_t *bptr; int64_t *bound;
+    FE_HD void operator()(int64_t i) const { bound[i] = row_product_bound(aptr, acol, bptr, i); }
+};
+
+struct PassProdCols {
+    const int64_t *aptr; const int32_t *acol; const int64_t *bptr; const int32_t *bcol; const int64_t *boff;
+    int32_t *cand; int64_t *cnt;
+    FE_HD void operator()(int64_t i) const { cnt[i] = row_product_columns(aptr, acol, bptr, bcol, i, cand + boff[i]); }
+};
+
+struct PassProdVals {
+    const int64_t *aptr; const int32_t *acol; const double *aval; int ra; int ca; const int64_t *bptr;
+    const int32_t *bcol; const double *bval; int cb; const int64_t *cptr; const int32_t *ccol; double *cval;
+    FE_HD void operator()(int64_t i) const {
+        row_product_values(aptr, acol, aval, ra, ca, bptr, bcol, bval, cb, cptr, ccol, cval, i);
+    }
+};
+
+struct PassSmooth {
+    const int64_t *pptr; const int32_t *pcol; double *pval; const double *dinv; const double *ptent;
+    const int32_t *agg; int d; int m; double w;
+    FE_HD void operator()(int64_t i) const { row_smooth_prolongator(pptr, pcol, pval, dinv, ptent, agg, d, m, w, i); }
+};
+
+struct PassRestrBound {
+    const int64_t *mptr; const int32_t *mem; const int64_t *aptr; int64_t *bound;
+    FE_HD void operator()(int64_t c) const { bound[c] = row_restriction_bound(mptr, mem, aptr, c); }
+};
+
+struct PassRestrCols {
+    const int64_t *mptr; const int32_t *mem; const int64_t *aptr; const int32_t *acol; const int64_t *boff;
+    int32_t *cand; int64_t *cnt;
+    FE_HD void operator()(int64_t c) const { cnt[c] = row_restriction_columns(mptr, mem, aptr, acol, c, cand + boff[c]); }
+};
+
+struct PassRestrVals {
+    const int64_t *rptr; const int32_t *rcol; double *rval; const int64_t *pptr; const int32_t *pcol;
+    const double *pval; int d; int m;
+    FE_HD void operator()(int64_t c) const { row_restriction_values(rptr, rcol, rval, pptr, pcol, pval, d, m, c); }
+};
+
+// ------------------------------------------------------------------ orchestration
+
+template <class Ex>
+struct Work {
+    DBuf<int64_t> bound, boff, cnt, flag;
+    DBuf<int32_t> cand;
+    Ex &ex;
+    explicit Work(Ex &e) : ex(e) {}
+    ~Work() { ex.release(bound), ex.release(boff), ex.release(cnt), ex.release(flag), ex.release(cand); }
+};
+
+// Rows whose entries are sorted distinct candidates: bound pass, scan, candidate pass
+// (count per row), scan into C.ptr, pack into C.col.
+template <class Ex, class Bound, class Cols>
+int distinct_rows(Ex &ex, int64_t n, Bound bound, Cols cols, Csr &C, Work<Ex> &W) {
+    FE_CHECK(ex.alloc(W.bound, (size_t)std::max<int64_t>(n, 1)));
+    FE_CHECK(ex.alloc(W.boff, (size_t)n + 1));
+    FE_CHECK(ex.alloc(W.cnt, (size_t)std::max<int64_t>(n, 1)));
+    bound.bound = W.bound.p;
+    FE_CHECK(ex.rows(n, bound));
+    int64_t total = 0;
+    FE_CHECK(ex.scan(W.bound.p, n, W.boff.p, &total));
+    FE_CHECK(ex.alloc(W.cand, (size_t)std::max<int64_t>(total, 1)));
+    cols.boff = W.boff.p, cols.cand = W.cand.p, cols.cnt = W.cnt.p;
+    FE_CHECK(ex.rows(n, cols));
+    FE_CHECK(ex.alloc(C.ptr, (size_t)n + 1));
+    int64_t nnzb = 0;
+    FE_CHECK(ex.scan(W.cnt.p, n, C.ptr.p, &nnzb));
+    C.nnzb = nnzb;
+    FE_CHECK(ex.alloc(C.col, (size_t)std::max<int64_t>(nnzb, 1)));
+    FE_CHECK(ex.rows(n, PassPackRows{W.boff.p, C.ptr.p, W.cand.p, C.col.p}));
+    return FE_OK;
+}
+
+// C = A B
+template <class Ex>
+int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W) {
+    C.n = A.n, C.rd = A.rd, C.cd = B.cd;
+    FE_CHECK(distinct_rows(ex, A.n, PassProdBound{A.ptr.p, A.col.p, B.ptr.p, nullptr},
+                           PassProdCols{A.ptr.p, A.col.p, B.ptr.p, B.col.p, nullptr, nullptr, nullptr}, C, W));
+    FE_CHECK(ex.alloc(C.val, (size_t)std::max<int64_t>(C.nnzb * C.rd * C.cd, 1)));
+    FE_CHECK(ex.rows(A.n, PassProdVals{A.ptr.p, A.col.p, A.val.p, A.rd, A.cd, B.ptr.p, B.col.p, B.val.p, B.cd,
+                                       C.ptr.p, C.col.p, C.val.p}));
+    return FE_OK;
+}
+
+// largest eigenvalue of D^-1 A: 30 power iterations from 1 + (i mod 7) / 7, then the
+// Rayleigh quotient
+template <class Ex>
+int lmax_of(Ex &ex, const Csr &A, const double *dinv, double *lmax) {
+    const int d = A.rd;
+    const int64_t nd = A.n * d;
+    DBuf<double> x, y;
+    struct Free {
+        Ex &ex;
+        DBuf<double> &x, &y;
+        ~Free() { ex.release(x), ex.release(y); }
+    } fr{ex, x, y};
+    FE_CHECK(ex.alloc(x, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(ex.alloc(y, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(ex.rows(nd, PassPowerStart{x.p}));
+    const PassDinvProduct prod{A.ptr.p, A.col.p, A.val.p, dinv, d, x.p, y.p};
+    for (int it = 0; it < 30; ++it) {
+        FE_CHECK(ex.rows(A.n, prod));
+        double yy = 0.0;
+        FE_CHECK(ex.dot(y.p, y.p, nd, &yy));
+        if (!(yy > 0.0)) break;
+        FE_CHECK(ex.rows(nd, PassScale{y.p, 1.0 / std::sqrt(yy), x.p}));
+    }
+    FE_CHECK(ex.rows(A.n, prod));
+    double num = 0.0, den = 0.0;
+    FE_CHECK(ex.dot(x.p, y.p, nd, &num));
+    FE_CHECK(ex.dot(x.p, x.p, nd, &den));
+    *lmax = num / den;
+    if (!std::isfinite(*lmax) || !(*lmax > 0.0)) {
+        set_error("multigrid setup: the largest eigenvalue estimate is not positive");
+        return FE_BREAKDOWN;
+    }
+    return FE_OK;
+}
+
+// The hierarchy of A (consumed) with near-null space B (n d x m, consumed): levels down
+// to at most coarse_dofs DOFs (or 12 levels); the coarsest operator in `coarse`.
+template <class Ex>
+int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t coarse_dofs, std::vector<Level> &levels,
+                    Csr &coarse, int *mis_rounds) {
+    const int kMaxRounds = 256;
+    DBuf<double> Bc, nrm, dg;
+    DBuf<uint8_t> strong;
+    DBuf<uint32_t> state;
+    DBuf<uint64_t> key, m1, m2;
+    DBuf<int32_t> rank, roots, agg1;
+    DBuf<int64_t> roff;
+    Work<Ex> W(ex);
+    struct Free {
+        Ex &ex;
+        Csr &A;
+        DBuf<double> &B, &Bc, &nrm, &dg;
+        DBuf<uint8_t> &strong;
+        DBuf<uint32_t> &state;
+        DBuf<uint64_t> &key, &m1, &m2;
+        DBuf<int32_t> &rank, &roots, &agg1;
+        DBuf<int64_t> &roff;
+        ~Free() {
+            release(ex, A);
+            ex.release(B), ex.release(Bc), ex.release(nrm), ex.release(dg), ex.release(strong), ex.release(state);
+            ex.release(key), ex.release(m1), ex.release(m2), ex.release(rank), ex.release(roots), ex.release(agg1);
+            ex.release(roff);
+        }
+    } fr{ex, A, B, Bc, nrm, dg, strong, state, key, m1, m2, rank, roots, agg1, roff};
+    *mis_rounds = 0;
+    while (A.n * A.rd > coarse_dofs && levels.size() < 12) {
+        Level L;
+        Csr Mem, Pt, AP, Ac;   // member lists, tentative prolongator, A P, Galerkin product
+        struct LevelFree {
+            Ex &ex;
+            Level &L;
+            Csr &Mem, &Pt, &AP, &Ac;
+            ~LevelFree() { release(ex, L), release(ex, Mem), release(ex, Pt), release(ex, AP), release(ex, Ac); }
+        } lf{ex, L, Mem, Pt, AP, Ac};
+        const int dd = A.rd;
+        const int64_t n = A.n;
+        FE_CHECK(ex.alloc(L.dinv, (size_t)std::max<int64_t>(n * dd * dd, 1)));
+        FE_CHECK(ex.rows(n, PassDinv{A.ptr.p, A.col.p, A.val.p, dd, L.dinv.p}));
+        FE_CHECK(lmax_of(ex, A, L.dinv.p, &L.lmax));
+        // strength and the distance-2 independent set
+        FE_CHECK(ex.alloc(nrm, (size_t)std::max<int64_t>(A.nnzb, 1)));
+        FE_CHECK(ex.alloc(strong, (size_t)std::max<int64_t>(A.nnzb, 1)));
+        FE_CHECK(ex.alloc(dg, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.rows(n, PassBlockNorms{A.ptr.p, A.col.p, A.val.p, dd, nrm.p, dg.p}));
+        FE_CHECK(ex.rows(n, PassStrength{A.ptr.p, A.col.p, nrm.p, dg.p, theta, strong.p}));
+        FE_CHECK(ex.alloc(state, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(key, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(m1, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(m2, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(W.flag, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(roff, (size_t)n + 1));
+        FE_CHECK(ex.rows(n, PassStateInit{state.p}));
+        for (int round = 1;; ++round) {
+            if (round > kMaxRounds) {
+                set_error("multigrid setup: the independent set did not settle");
+                return FE_BREAKDOWN;
+            }
+            FE_CHECK(ex.rows(n, PassMisKey{state.p, key.p}));
+            FE_CHECK(ex.rows(n, PassMaxKey{A.ptr.p, A.col.p, strong.p, key.p, m1.p}));
+            FE_CHECK(ex.rows(n, PassMaxKey{A.ptr.p, A.col.p, strong.p, m1.p, m2.p}));
+            FE_CHECK(ex.rows(n, PassMisDecide{m2.p, state.p, W.flag.p}));
+            int64_t undecided = 0;
+            FE_CHECK(ex.scan(W.flag.p, n, roff.p, &undecided));
+            ++*mis_rounds;
+            if (undecided == 0) break;
+        }
+        // roots in node order, then the two joins
+        FE_CHECK(ex.rows(n, PassRootFlags{state.p, W.flag.p}));
+        int64_t na = 0;
+        FE_CHECK(ex.scan(W.flag.p, n, roff.p, &na));
+        if (na == 0) {
+            set_error("multigrid setup: no aggregate root");
+            return FE_BREAKDOWN;
+        }
+        FE_CHECK(ex.alloc(rank, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(roots, (size_t)na));
+        FE_CHECK(ex.alloc(agg1, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(L.agg, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.rows(n, PassRoots{state.p, roff.p, rank.p, roots.p}));
+        FE_CHECK(ex.rows(n, PassJoinRoot{A.ptr.p, A.col.p, strong.p, nrm.p, state.p, rank.p, agg1.p}));
+        FE_CHECK(ex.rows(n, PassJoinNeighbour{A.ptr.p, A.col.p, strong.p, nrm.p, agg1.p, L.agg.p, W.flag.p}));
+        int64_t left = 0;
+        FE_CHECK(ex.scan(W.flag.p, n, roff.p, &left));
+        if (left != 0) {
+            set_error("multigrid setup: a node was left without an aggregate");
+            return FE_BREAKDOWN;
+        }
+        // members of every aggregate in node order (rows = aggregates, no values)
+        Mem.n = na;
+        FE_CHECK(distinct_rows(ex, na, PassMemberBound{A.ptr.p, A.col.p, roots.p, nullptr},
+                               PassMembers{A.ptr.p, A.col.p, roots.p, L.agg.p, nullptr, nullptr, nullptr}, Mem, W));
+        if (Mem.nnzb != n) {
+            set_error("multigrid setup: aggregate members do not cover the nodes");
+            return FE_BREAKDOWN;
+        }
+        // tentative prolongator: B's rows, one QR per aggregate in place
+        Pt.n = n, Pt.rd = dd, Pt.cd = m, Pt.nnzb = n;
+        FE_CHECK(ex.alloc(Pt.ptr, (size_t)n + 1));
+        FE_CHECK(ex.alloc(Pt.col, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.alloc(Pt.val, (size_t)std::max<int64_t>(n * dd * m, 1)));
+        FE_CHECK(ex.rows(n + 1, PassIota{Pt.ptr.p}));
+        FE_CHECK(ex.copy(Pt.col.p, L.agg.p, (size_t)n));
+        FE_CHECK(ex.copy(Pt.val.p, B.p, (size_t)(n * dd * m)));
+        FE_CHECK(ex.alloc(Bc, (size_t)std::max<int64_t>(na * m * m, 1)));
+        FE_CHECK(ex.rows(na, PassQr{Mem.ptr.p, Mem.col.p, dd, m, Pt.val.p, Bc.p}));
+        // P = P_t - w D^-1 A P_t
+        FE_CHECK(product(ex, A, Pt, L.P, W));
+        const double w = 4.0 / (3.0 * L.lmax);
+        FE_CHECK(ex.rows(n, PassSmooth{L.P.ptr.p, L.P.col.p, L.P.val.p, L.dinv.p, Pt.val.p, L.agg.p, dd, m, w}));
+        // restriction P^T and Galerkin product P^T (A P)
+        FE_CHECK(product(ex, A, L.P, AP, W));
+        L.PT.n = na, L.PT.rd = m, L.PT.cd = dd;
+        FE_CHECK(distinct_rows(ex, na, PassRestrBound{Mem.ptr.p, Mem.col.p, A.ptr.p, nullptr},
+                               PassRestrCols{Mem.ptr.p, Mem.col.p, A.ptr.p, A.col.p, nullptr, nullptr, nullptr}, L.PT,
+                               W));
+        FE_CHECK(ex.alloc(L.PT.val, (size_t)std::max<int64_t>(L.PT.nnzb * m * dd, 1)));
+        FE_CHECK(ex.rows(na, PassRestrVals{L.PT.ptr.p, L.PT.col.p, L.PT.val.p, L.P.ptr.p, L.P.col.p, L.P.val.p, dd, m}));
+        FE_CHECK(product(ex, L.PT, AP, Ac, W));
+        // the level keeps A; the next level starts from A_c and the coarse near-null space
+        L.A = A;
+        A = Ac;
+        Ac = Csr();
+        std::swap(B, Bc);
+        levels.push_back(L);
+        L = Level();
+    }
+    coarse = A;
+    A = Csr();
+    return FE_OK;
+}
+
+}  // namespace amg
+}  // namespace fe

@@ -18,10 +18,17 @@
 // down to at most `coarse_dofs` DOFs (or 12 levels).  Host code only: no device call.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <thread>
 #include <vector>
 
+#include "fe_amg.h"
+#include "fe_amg_dev.h"
+#include "fe_amg_par.cuh"
+#include "fe_amg_cycle.cuh"
+#include "fe_amg_passes.cuh"
 #include "fe_amg_rows.cuh"
 #include "fe_internal.h"
 
@@ -54,78 +61,13 @@ void parallel_chunks(int64_t n, F f) {
     for (auto &x : th) x.join();
 }
 
-struct BlockCsr {
-    int64_t n = 0;             // block rows
-    int rd = 0, cd = 0;        // block size rd x cd
-    std::vector<int64_t> ptr;  // n + 1
-    std::vector<int32_t> col;
-    std::vector<double> val;   // nnzb * rd * cd, row-major blocks
-    int64_t nnzb() const { return (int64_t)col.size(); }
-};
-
-struct AmgLevel {
-    BlockCsr A;                 // d x d blocks
-    BlockCsr P;                 // d x m blocks, columns = aggregates
-    BlockCsr PT;                // m x d blocks: the restriction
-    std::vector<double> dinv;   // block-diagonal pseudo-inverse of A
-    std::vector<int32_t> agg;   // aggregate of each node
-    double lmax = 0.0;
-};
-
-// Pseudo-inverse of a symmetric d x d block by cyclic Jacobi: V diag(1/l) V^T over the
-// eigenvalues above 1e-12 of the largest in magnitude.
-void sym_pinv(const double *a, int d, double *out) {
-    double A[36], V[36];
-    for (int i = 0; i < d * d; ++i) A[i] = a[i];
-    for (int i = 0; i < d; ++i)
-        for (int j = 0; j < d; ++j) V[i * d + j] = i == j ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        double off = 0.0;
-        for (int p = 0; p < d; ++p)
-            for (int q = p + 1; q < d; ++q) off += A[p * d + q] * A[p * d + q];
-        if (off < 1e-30) break;
-        for (int p = 0; p < d; ++p)
-            for (int q = p + 1; q < d; ++q) {
-                const double apq = A[p * d + q];
-                if (apq == 0.0) continue;
-                const double th = (A[q * d + q] - A[p * d + p]) / (2.0 * apq);
-                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < d; ++k) {
-                    const double akp = A[k * d + p], akq = A[k * d + q];
-                    A[k * d + p] = c * akp - s * akq;
-                    A[k * d + q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < d; ++k) {
-                    const double apk = A[p * d + k], aqk = A[q * d + k];
-                    A[p * d + k] = c * apk - s * aqk;
-                    A[q * d + k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < d; ++k) {
-                    const double vkp = V[k * d + p], vkq = V[k * d + q];
-                    V[k * d + p] = c * vkp - s * vkq;
-                    V[k * d + q] = s * vkp + c * vkq;
-                }
-            }
-    }
-    double lmax = 0.0;
-    for (int i = 0; i < d; ++i) lmax = std::max(lmax, std::fabs(A[i * d + i]));
-    for (int i = 0; i < d * d; ++i) out[i] = 0.0;
-    for (int k = 0; k < d; ++k) {
-        const double l = A[k * d + k];
-        if (std::fabs(l) <= 1e-12 * lmax || l == 0.0) continue;
-        for (int i = 0; i < d; ++i)
-            for (int j = 0; j < d; ++j) out[i * d + j] += V[i * d + k] * V[j * d + k] / l;
-    }
-}
-
 std::vector<double> block_diag_pinv(const BlockCsr &A) {
     const int d = A.rd;
     std::vector<double> dinv((size_t)A.n * d * d, 0.0);
     parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int) {
         for (int64_t i = lo; i < hi; ++i)
             for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s)
-                if (A.col[s] == i) sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
+                if (A.col[s] == i) amg::sym_pinv(&A.val[(size_t)s * d * d], d, &dinv[(size_t)i * d * d]);
     });
     return dinv;
 }
@@ -378,11 +320,38 @@ bool dense_inverse(std::vector<double> a, int n, std::vector<double> &inv) {
 }  // namespace
 }  // namespace fe
 
-struct fe_amg_s {
-    std::vector<fe::AmgLevel> levels;
-    fe::BlockCsr coarse;
-    std::vector<double> coarse_inv;   // dense inverse of the coarsest matrix + 1e-12 max|diag| I
-};
+
+
+namespace fe {
+
+// Dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal entry
+// (zero rows of rank-deficient aggregates).
+int coarse_inverse_of(const BlockCsr &C, std::vector<double> &inv, const char *who) {
+    const int64_t n = C.n * C.rd;
+    if (n > 4096) {
+        set_error(std::string(who) + ": coarsest level too large for its dense solve");
+        return FE_BAD_INPUT;
+    }
+    std::vector<double> dense((size_t)n * n, 0.0);
+    double dmax = 0.0;
+    const int cd = C.rd;
+    for (int64_t i = 0; i < C.n; ++i)
+        for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
+            for (int a = 0; a < cd; ++a)
+                for (int b = 0; b < cd; ++b) {
+                    const double v = C.val[(size_t)s * cd * cd + a * cd + b];
+                    dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
+                }
+    for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
+    for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
+    if (n > 0 && !dense_inverse(dense, (int)n, inv)) {
+        set_error(std::string(who) + ": singular coarsest matrix");
+        return FE_BREAKDOWN;
+    }
+    return FE_OK;
+}
+
+}  // namespace fe
 
 namespace fe {
 namespace {
@@ -437,6 +406,130 @@ void vcycle_host(const fe_amg_s *h, size_t l, int k, const std::vector<double> &
     for (int64_t i = 0; i < A.n; ++i)
         amg::row_prolong_add(L.P.ptr.data(), L.P.col.data(), L.P.val.data(), d, m, xc.data(), x.data(), i);
     chebyshev_host(L, k, r, x, true);
+}
+
+
+// Dense inverse of the coarsest matrix of h.
+int coarse_inverse(fe_amg_s *h, const char *who) { return coarse_inverse_of(h->coarse, h->coarse_inv, who); }
+
+// ---------------------------------------------------------------- parallel setup (host)
+// amg::setup_hierarchy (fe_amg_passes.cuh), the device setup's sequence of passes, on
+// a host executor: passes over row chunks on host threads, serial scans, dot products
+// summed per chunk in chunk order.
+
+struct HostEx {
+    template <class T>
+    int alloc(DBuf<T> &b, size_t n) {
+        if (b.p && b.n >= n) return FE_OK;
+        std::free(b.p);
+        b.p = (T *)std::malloc(std::max<size_t>(n, 1) * sizeof(T));
+        b.n = b.p ? n : 0;
+        if (!b.p) {
+            set_error("multigrid setup: out of host memory");
+            return FE_BAD_INPUT;
+        }
+        return FE_OK;
+    }
+    template <class T>
+    void release(DBuf<T> &b) {
+        std::free(b.p);
+        b.p = nullptr;
+        b.n = 0;
+    }
+    template <class T>
+    int copy(T *dst, const T *src, size_t n) {
+        if (n) std::memcpy(dst, src, n * sizeof(T));
+        return FE_OK;
+    }
+    template <class T>
+    int read(T *dst, const T *src, size_t n) {
+        return copy(dst, src, n);
+    }
+    template <class T>
+    int fill_zero(T *p, size_t n) {
+        if (n) std::memset(p, 0, n * sizeof(T));
+        return FE_OK;
+    }
+    template <class F>
+    int rows(int64_t n, const F &f) {
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i) f(i);
+        });
+        return FE_OK;
+    }
+    int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) {
+        int64_t run = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t v = in[i];
+            out[i] = run;
+            run += v;
+        }
+        out[n] = run;
+        *total = run;
+        return FE_OK;
+    }
+    int dot(const double *a, const double *b, int64_t n, double *out) {
+        double part[kChunks];
+        for (int c = 0; c < kChunks; ++c) part[c] = 0.0;
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int c) {
+            double t = 0.0;
+            for (int64_t i = lo; i < hi; ++i) t += a[i] * b[i];
+            part[c] = t;
+        });
+        double t = 0.0;
+        for (int c = 0; c < kChunks; ++c) t += part[c];
+        *out = t;
+        return FE_OK;
+    }
+};
+
+BlockCsr to_block_csr(const amg::Csr &c) {
+    BlockCsr H;
+    H.n = c.n, H.rd = c.rd, H.cd = c.cd;
+    H.ptr.assign(c.ptr.p, c.ptr.p + c.n + 1);
+    H.col.assign(c.col.p, c.col.p + c.nnzb);
+    H.val.assign(c.val.p, c.val.p + c.nnzb * c.rd * c.cd);
+    return H;
+}
+
+// The hierarchy by the parallel passes on the host.  Returns FE_OK or a failure status.
+int build_parallel(fe_amg_s *h, int64_t n, int d, const int64_t *ptr, const int32_t *col, const double *vals,
+                   const double *nullspace, int m, double theta, int64_t coarse_dofs) {
+    HostEx ex;
+    amg::Csr A;
+    DBuf<double> B;
+    A.n = n, A.rd = A.cd = d, A.nnzb = ptr[n];
+    int st = FE_OK;
+    if ((st = ex.alloc(A.ptr, (size_t)n + 1)) || (st = ex.alloc(A.col, (size_t)std::max<int64_t>(A.nnzb, 1))) ||
+        (st = ex.alloc(A.val, (size_t)std::max<int64_t>(A.nnzb * d * d, 1))) ||
+        (st = ex.alloc(B, (size_t)std::max<int64_t>(n * d * m, 1)))) {
+        amg::release(ex, A);
+        ex.release(B);
+        return st;
+    }
+    ex.copy(A.ptr.p, ptr, (size_t)n + 1);
+    ex.copy(A.col.p, col, (size_t)A.nnzb);
+    ex.copy(A.val.p, vals, (size_t)(A.nnzb * d * d));
+    ex.copy(B.p, nullspace, (size_t)(n * d * m));
+    std::vector<amg::Level> levels;
+    amg::Csr coarse;
+    int rounds = 0;
+    st = amg::setup_hierarchy(ex, A, B, m, theta, coarse_dofs, levels, coarse, &rounds);
+    for (auto &l : levels) {
+        if (st == FE_OK) {
+            AmgLevel L;
+            L.A = to_block_csr(l.A), L.P = to_block_csr(l.P), L.PT = to_block_csr(l.PT);
+            L.dinv.assign(l.dinv.p, l.dinv.p + l.A.n * l.A.rd * l.A.rd);
+            L.agg.assign(l.agg.p, l.agg.p + l.A.n);
+            L.lmax = l.lmax;
+            h->levels.push_back(std::move(L));
+        }
+        amg::release(ex, l);
+    }
+    if (st != FE_OK) return st;
+    h->coarse = to_block_csr(coarse);
+    amg::release(ex, coarse);
+    return coarse_inverse(h, "fe_amg_build_parallel_host");
 }
 
 }  // namespace
@@ -535,35 +628,112 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
         (void)bm;
     }
     h->coarse = std::move(A);
-    {
-        // dense inverse of the coarsest matrix, shifted by 1e-12 of its largest diagonal
-        // entry (zero rows of rank-deficient aggregates)
-        const BlockCsr &C = h->coarse;
-        const int64_t n = C.n * C.rd;
-        if (n > 4096) {
-            fe_amg_destroy(h);
-            set_error("fe_amg_build_host: coarsest level too large for its dense solve");
-            return FE_BAD_INPUT;
-        }
-        std::vector<double> dense((size_t)n * n, 0.0);
-        double dmax = 0.0;
-        const int cd = C.rd;
-        for (int64_t i = 0; i < C.n; ++i)
-            for (int64_t s = C.ptr[i]; s < C.ptr[i + 1]; ++s)
-                for (int a = 0; a < cd; ++a)
-                    for (int b = 0; b < cd; ++b) {
-                        const double v = C.val[(size_t)s * cd * cd + a * cd + b];
-                        dense[(size_t)(i * cd + a) * n + (int64_t)C.col[s] * cd + b] += v;
-                    }
-        for (int64_t i = 0; i < n; ++i) dmax = std::max(dmax, std::fabs(dense[(size_t)i * n + i]));
-        for (int64_t i = 0; i < n; ++i) dense[(size_t)i * n + i] += 1e-12 * dmax;
-        if (n > 0 && !dense_inverse(dense, (int)n, h->coarse_inv)) {
-            fe_amg_destroy(h);
-            set_error("fe_amg_build_host: singular coarsest matrix");
-            return FE_BREAKDOWN;
-        }
+    const int st = coarse_inverse(h, "fe_amg_build_host");
+    if (st != FE_OK) {
+        fe_amg_destroy(h);
+        return st;
     }
     *out = h;
+    return FE_OK;
+}
+
+// The same hierarchy inputs, set up by the parallel passes of the device setup
+// (independent-set aggregation, row-wise products) run on the host.
+int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
+                               const double *vals, int32_t m, const double *nullspace, double theta,
+                               int64_t coarse_dofs, fe_amg *out) {
+    if (!out || n_nodes < 0 || d < 1 || d > 6 || m < 1 || m > 6 || (n_nodes > 0 && (!blk_ptr || !blk_col ||
+                                                                                     !vals || !nullspace))) {
+        set_error("fe_amg_build_parallel_host: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    *out = nullptr;
+    fe_amg_s *h = new fe_amg_s();
+    const int st = build_parallel(h, n_nodes, d, blk_ptr, blk_col, vals, nullspace, m, theta, coarse_dofs);
+    if (st != FE_OK) {
+        fe_amg_destroy(h);
+        return st;
+    }
+    *out = h;
+    return FE_OK;
+}
+
+}  // extern "C"
+
+namespace fe {
+namespace {
+
+// FP32 copies of a host hierarchy and its cycle vectors, viewed as the shared cycle
+// (fe_amg_cycle.cuh) sees the device's.
+struct HostCycle {
+    std::vector<std::vector<float>> store;
+    std::vector<amg::CycleLevel> levels;
+    amg::CycleCoarse coarse;
+    explicit HostCycle(const fe_amg_s *h) {
+        auto f32 = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
+        const size_t nl = h->levels.size();
+        store.reserve(nl * 9 + 2);
+        levels.resize(nl);
+        for (size_t l = 0; l < nl; ++l) {
+            const AmgLevel &H = h->levels[l];
+            amg::CycleLevel &L = levels[l];
+            L.n = H.A.n, L.d = H.A.rd, L.m = H.P.cd, L.lmax = H.lmax, L.nc = H.PT.n;
+            L.aptr = H.A.ptr.data(), L.acol = H.A.col.data();
+            L.pptr = H.P.ptr.data(), L.pcol = H.P.col.data();
+            L.tptr = H.PT.ptr.data(), L.tcol = H.PT.col.data();
+            store.push_back(f32(H.A.val)), L.a = store.back().data();
+            store.push_back(f32(H.dinv)), L.dinv = store.back().data();
+            store.push_back(f32(H.P.val)), L.p = store.back().data();
+            store.push_back(f32(H.PT.val)), L.pt = store.back().data();
+            float **vec[5] = {&L.r, &L.x, &L.t, &L.dir, &L.zn};
+            for (float **v : vec) {
+                store.emplace_back((size_t)std::max<int64_t>(L.n * L.d, 1), 0.0f);
+                *v = store.back().data();
+            }
+        }
+        coarse.n = h->coarse.n * h->coarse.rd;
+        coarse.inv = h->coarse_inv.data();
+        store.emplace_back((size_t)std::max<int64_t>(coarse.n, 1), 0.0f), coarse.r = store.back().data();
+        store.emplace_back((size_t)std::max<int64_t>(coarse.n, 1), 0.0f), coarse.x = store.back().data();
+    }
+};
+
+}  // namespace
+}  // namespace fe
+
+extern "C" {
+
+// One V-cycle of the device's FP32 sequence (amg::precondition, fe_amg_cycle.cuh) run
+// on the host: FP32 copies of the levels, r rounded to FP32, x widened to FP64.
+int fe_amg_vcycle_host_f32(fe_amg h, int32_t k_smooth, const double *r, double *x) {
+    if (!h || !r || !x || k_smooth < 1 || h->levels.empty()) {
+        set_error("fe_amg_vcycle_host_f32: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    HostCycle c(h);
+    HostEx ex;
+    return amg::precondition(ex, c.levels, c.coarse, k_smooth, r, x);
+}
+
+// The device's multigrid PCG (amg::pcg around the FP32 cycle) run on the host, on the
+// hierarchy's level-0 matrix: x from zero, to ||r|| <= tol ||b||.
+int fe_amg_pcg_host(fe_amg h, int32_t k_smooth, const double *b, double tol, int32_t max_iter, double *x,
+                    int32_t *iters, double *relres, int32_t *status) {
+    if (!h || !b || !x || !iters || !relres || !status || k_smooth < 1 || h->levels.empty() || max_iter < 1) {
+        set_error("fe_amg_pcg_host: bad arguments");
+        return FE_BAD_INPUT;
+    }
+    HostCycle c(h);
+    HostEx ex;
+    const BlockCsr &A = h->levels[0].A;
+    const size_t nd = (size_t)(A.n * A.rd);
+    std::vector<double> r(nd), p(nd), q(nd), z(nd);
+    const amg::PcgVectors v{x, r.data(), p.data(), q.data(), z.data()};
+    auto precond = [&]() { return amg::precondition(ex, c.levels, c.coarse, k_smooth, v.r, v.z); };
+    int it = 0, st = 0;
+    FE_CHECK(amg::pcg(ex, A.n, A.rd, A.ptr.data(), A.col.data(), A.val.data(), b, v, precond, tol, max_iter, &it,
+                      relres, &st));
+    *iters = it, *status = st;
     return FE_OK;
 }
 

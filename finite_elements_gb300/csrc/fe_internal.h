@@ -284,6 +284,8 @@ int solve_continuity(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *
 // Largest eigenvalue of the m x m tridiagonal Lanczos matrix of the CG coefficients
 // alpha[0..m), beta[0..m) (bisection on the Sturm sequence), fe_solver.cu.
 double lanczos_lmax(const double *alpha, const double *beta, int m);
+// FP64 PCG with a smoothed-aggregation V-cycle preconditioner (fe_amg_device.cu)
+int solve_multigrid(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
 int set_rhs_additions(fe_handle_s *h, int64_t n, const int64_t *dof, const double *value);
 int apply_rhs_additions(fe_handle_s *h);
 int autotune_spmv(fe_handle_s *h, int precision, int *lanes, double *ms);

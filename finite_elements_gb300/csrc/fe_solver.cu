@@ -1548,6 +1548,7 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
     }
     // continuity conditions: the projected FP64 PCG, whatever the precision asked
     if (h->n_cont > 0) return solve_continuity(h, o, st);
+    if (o->flags & FE_SOLVE_MULTIGRID) return solve_multigrid(h, o, st);
     int lanes = 2;
     FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
     FE_CUDA(cudaEventRecord(h->events[6], h->stream));

@@ -279,10 +279,13 @@ class GpuSystem:
 
     def solve(self, precision="fp64", tol=None, cheb_degree=0, max_iter=0, x0=None, lanes=0,
               accept_stagnation=False, inner_tol=0.0, cheb_ratio=0.0, chunk=0, max_outer=0,
-              want_host=True, restart_each_step=False, x0_device_ptr=None, x0_if_better=False):
+              want_host=True, restart_each_step=False, x0_device_ptr=None, x0_if_better=False,
+              multigrid=False):
         """Solve the eliminated system on the GPU.  precision: "fp64", "mixed" or
         "mixed-cg64" (see PRECISIONS).  x0 / x0_device_ptr: warm start; with
         x0_if_better it is kept only when its true residual beats the zero start.
+        multigrid: FP64 PCG preconditioned by a smoothed-aggregation V-cycle (work in
+        progress; precision, Chebyshev and warm-start options are not used).
         Returns (x, stats): x holds n_dof + n_bc values (u then the multipliers) or
         None with want_host=False."""
         o = SolveOpts()
@@ -306,7 +309,8 @@ class GpuSystem:
         o.chunk = chunk
         o.flags = ((_lib.FE_SOLVE_ACCEPT_STAGNATION if accept_stagnation else 0)
                    | (_lib.FE_SOLVE_RESTART_EACH_STEP if restart_each_step else 0)
-                   | (_lib.FE_SOLVE_X0_IF_BETTER if x0_if_better else 0))
+                   | (_lib.FE_SOLVE_X0_IF_BETTER if x0_if_better else 0)
+                   | (_lib.FE_SOLVE_MULTIGRID if multigrid else 0))
         st = SolveStats()
         x = np.empty(self.prob.n_dof + len(self.bc_dof) + self.prob.n_cont) if want_host else None
         lib = _lib.load()

@@ -64,6 +64,9 @@ extern "C" {
 #define FE_SOLVE_RESTART_EACH_STEP 2   /* mixed: restart the Krylov space at every refinement
                                           step (classic iterative refinement) instead of
                                           continuing along the current direction          */
+#define FE_SOLVE_MULTIGRID        8    /* FP64 PCG preconditioned by a smoothed-aggregation
+                                          V-cycle (hierarchy set up on the host); work in
+                                          progress, not yet run on a GPU                    */
 
 /* solver precision */
 #define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
@@ -273,6 +276,20 @@ typedef struct fe_amg_s *fe_amg;
 int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
                       const double *vals, int32_t m, const double *nullspace, double theta,
                       int64_t coarse_dofs, fe_amg *out);
+/* The same, set up by the passes of the device setup run on the host: aggregates from a
+ * distance-2 maximal independent set of the strong graph (rounds of (state, hash,
+ * index) maxima over two hops; every node then joins the strongest root next to it, the
+ * rest the strongest neighbour that joined), one QR per aggregate, row-wise sparse
+ * products (sorted distinct columns, then the values).  Its result does not depend on
+ * the order in which rows are processed. */
+int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const int32_t *blk_col,
+                               const double *vals, int32_t m, const double *nullspace, double theta,
+                               int64_t coarse_dofs, fe_amg *out);
+/* The same passes on the device, from the assembled system of h (near-null space: the
+ * rigid-body modes, or the constant for magnetostatics, zero on the constrained DOFs);
+ * the hierarchy is copied to the host for the accessors below.  Work in progress: not
+ * yet run on a GPU. */
+int fe_amg_build_device(fe_handle h, double theta, int64_t coarse_dofs, fe_amg *out);
 int fe_amg_levels(fe_amg a, int32_t *n_levels);
 int fe_amg_level_info(fe_amg a, int32_t level, int64_t *n_nodes, int32_t *d, int64_t *nnzb_A,
                       int64_t *nnzb_P, int64_t *n_coarse, int32_t *m, double *lmax);
@@ -283,6 +300,15 @@ int fe_amg_level_aggregates(fe_amg a, int32_t level, int32_t *agg_host);
  * [1.05 lmax/30, 1.05 lmax]) before and after each coarse correction and a dense solve
  * of the coarsest level: the arithmetic the device cycle runs row by row. */
 int fe_amg_vcycle_host(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
+/* The device's FP32 cycle (FP32 copies of the levels, r rounded to FP32, FP64 coarsest
+ * inverse) run on the host: the sequence of passes the multigrid solve launches. */
+int fe_amg_vcycle_host_f32(fe_amg a, int32_t k_smooth, const double *r_host, double *x_host);
+/* The device's multigrid PCG (FP64 recurrence around the FP32 cycle) run on the host on
+ * the hierarchy's level-0 matrix: x (host, n DOFs) from zero to ||r|| <= tol ||b||;
+ * iterations, the true relative residual and the status (FE_OK, FE_MAXITER,
+ * FE_BREAKDOWN, FE_NONFINITE) come back through the pointers. */
+int fe_amg_pcg_host(fe_amg a, int32_t k_smooth, const double *b_host, double tol, int32_t max_iter, double *x_host,
+                    int32_t *iterations, double *relres, int32_t *status);
 int fe_amg_destroy(fe_amg a);
 
 /* ---- learned warm start (no counterpart in the reference: an addition on top of the

@@ -1,0 +1,278 @@
+"""The parallel multigrid setup of libfe_gb300 (fe_amg_build_parallel_host: the passes
+of the device setup, run over the rows on the host) on the benchmark family, checked
+against the CPU model on its own aggregates:
+
+* the aggregates come from a distance-2 maximal independent set of the strong graph:
+  no two roots within two strong hops, every node within two hops of a root, every
+  node in the aggregate of a root or of a strong neighbour;
+* the prolongator equals the model's (I - w D^-1 A) P_tent on those aggregates and the
+  coarse operators P^T A P, within 1e-10;
+* PCG with the V-cycle on this hierarchy converges to 1e-8 in about the iterations of
+  the greedy hierarchy."""
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from finite_elements_gb300 import _lib, meshgen
+from oracle import amg_oracle as AMG
+from oracle import fe_oracle as O
+from test_amg_setup_host import from_block_csr, to_block_csr
+
+
+def read_levels(lib, h):
+    nl = ctypes.c_int32()
+    lib.fe_amg_levels(h, ctypes.byref(nl))
+    levels = []
+    for l in range(nl.value + 1):
+        nn, dd, na_, np_, nc, m = (ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64(),
+                                   ctypes.c_int64(), ctypes.c_int32())
+        lm = ctypes.c_double()
+        lib.fe_amg_level_info(h, l, nn, dd, na_, np_, nc, m, ctypes.byref(lm))
+        p = np.empty(nn.value + 1, np.int64)
+        c = np.empty(max(na_.value, 1), np.int32)
+        v = np.empty(max(na_.value, 1) * dd.value ** 2)
+        lib.fe_amg_level_matrix(h, l, 0, _lib.ptr(p), _lib.ptr(c), _lib.ptr(v))
+        lev = {"A": from_block_csr(p, c[:na_.value], v[:na_.value * dd.value ** 2], dd.value, dd.value, nn.value),
+               "lmax": lm.value, "d": dd.value}
+        if l < nl.value:
+            pp = np.empty(nn.value + 1, np.int64)
+            pc = np.empty(np_.value, np.int32)
+            pv = np.empty(np_.value * dd.value * m.value)
+            lib.fe_amg_level_matrix(h, l, 1, _lib.ptr(pp), _lib.ptr(pc), _lib.ptr(pv))
+            lev["P"] = from_block_csr(pp, pc, pv, dd.value, m.value, nc.value)
+            agg = np.empty(nn.value, np.int32)
+            lib.fe_amg_level_aggregates(h, l, _lib.ptr(agg))
+            lev["agg"] = agg
+        levels.append(lev)
+    return levels
+
+
+def build(A, B, d, fn="fe_amg_build_parallel_host"):
+    lib = _lib.load()
+    n, ptr, col, val = to_block_csr(A, d)
+    Bc = np.ascontiguousarray(B, np.float64)
+    h = ctypes.c_void_p()
+    _lib.check(getattr(lib, fn)(n, d, _lib.ptr(ptr), _lib.ptr(col), _lib.ptr(val), B.shape[1], _lib.ptr(Bc),
+                                0.08, 400, ctypes.byref(h)), fn)
+    return lib, h, read_levels(lib, h)
+
+
+def strong_graph(A, d, theta=0.08):
+    Ab = sp.bsr_matrix(A, blocksize=(d, d))
+    Ab.sort_indices()
+    n = A.shape[0] // d
+    nrm = np.abs(Ab.data).sum(axis=(1, 2))
+    rows = np.repeat(np.arange(n), np.diff(Ab.indptr))
+    cols = Ab.indices
+    dg = np.zeros(n)
+    dg[rows[rows == cols]] = nrm[rows == cols]
+    keep = (rows != cols) & (nrm >= theta * np.sqrt(dg[rows] * dg[cols]))
+    return sp.csr_matrix((np.ones(keep.sum()), (rows[keep], cols[keep])), shape=(n, n))
+
+
+def problem(case, scale=1):
+    if case == "plane_strain":
+        prob = meshgen.plane_strain_random(60 * scale, 30 * scale, seed=4)
+        d, modes = 2, AMG.rigid_modes_2d
+    elif case == "tet":
+        prob = meshgen.cantilever_3d(10, 4, 4, jitter=0.2, seed=5)
+        d, modes = 3, AMG.rigid_modes_3d
+    else:
+        prob = meshgen.magnetostatic(50, 25, seed=2)
+        d, modes = 1, None
+    A, b, free, *_ = O.reduced_system(prob)
+    A = A.tocsr()
+    B = np.ones((A.shape[0], 1)) if modes is None else modes(prob.coords[free[0::d] // d])
+    return A, b, B, d
+
+
+def lowbias32(x):
+    """The published 32-bit integer hash lowbias32 (C. Wellons)."""
+    x = x.astype(np.uint64)
+    m = np.uint64(0xFFFFFFFF)
+    x ^= x >> np.uint64(16)
+    x = (x * np.uint64(0x7feb352d)) & m
+    x ^= x >> np.uint64(15)
+    x = (x * np.uint64(0x846ca68b)) & m
+    x ^= x >> np.uint64(16)
+    return x
+
+
+def mis2_roots(S):
+    """Distance-2 maximal independent set by rounds of two-hop maxima of the keys
+    (state, hash >> 2, index), state 2 = in, 1 = undecided, 0 = out."""
+    n = S.shape[0]
+    idx = np.arange(n, dtype=np.uint64)
+    low = (lowbias32(idx) >> np.uint64(2)) << np.uint64(32) | idx
+    state = np.ones(n, np.uint64)
+    Sc = S.tocsr()
+    rows = np.repeat(np.arange(n), np.diff(Sc.indptr))
+
+    def hop_max(v):
+        out = v.copy()
+        np.maximum.at(out, rows, v[Sc.indices])
+        return out
+    while (state == 1).any():
+        key = state << np.uint64(62) | low
+        m2 = hop_max(hop_max(key))
+        und = state == 1
+        own = und & (m2 == key)
+        out = und & ~own & ((m2 >> np.uint64(62)) == 2)
+        state[own] = 2
+        state[out] = 0
+    return np.flatnonzero(state == 2)
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_aggregates_form_a_distance_two_independent_set(case):
+    A, b, B, d = problem(case)
+    lib, h, levels = build(A, B, d)
+    try:
+        Al, dl = A, d
+        for l, lev in enumerate(levels[:-1]):
+            S = strong_graph(Al, dl)
+            n = S.shape[0]
+            agg = lev["agg"]
+            roots = mis2_roots(S)
+            # aggregate k is the k-th root's, in increasing node order
+            np.testing.assert_array_equal(agg[roots], np.arange(roots.size))
+            assert agg.min() >= 0 and agg.max() == roots.size - 1
+            one = ((S + sp.eye(n)) > 0).astype(np.int8)
+            two = ((one @ one) > 0).astype(np.int8).tocsr()
+            # independent: no other root within two strong hops of a root
+            assert two[roots][:, roots].nnz == roots.size
+            # maximal: every node within two hops of a root, and in the aggregate of a
+            # root or strong neighbour within those two hops
+            near = two[:, roots]
+            assert (np.diff(near.indptr) > 0).all()
+            for i in range(n):
+                assert agg[i] in agg[roots[near[i].indices]]
+            Al, dl = levels[l + 1]["A"], B.shape[1]
+    finally:
+        lib.fe_amg_destroy(h)
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_operators_match_the_model_on_the_same_aggregates(case):
+    A, b, B, d = problem(case)
+    lib, h, levels = build(A, B, d)
+    try:
+        Al, Bl, dl = A, B, d
+        for l, lev in enumerate(levels[:-1]):
+            Minv = AMG.block_diag_inv(Al, dl)
+            lm = AMG.lmax_power(Al, Minv)
+            assert abs(lev["lmax"] - lm) <= 1e-10 * lm
+            assert abs(lev["A"] - Al).max() <= 1e-10 * abs(Al).max()
+            agg = lev["agg"].astype(np.int64)
+            na = int(agg.max()) + 1
+            Pt, Bc = AMG.tentative(agg, na, Bl, dl)
+            P = (Pt - (4.0 / (3.0 * lm)) * (Minv @ (Al @ Pt))).tocsr()
+            assert abs(lev["P"] - P).max() <= 1e-10 * abs(P).max()
+            Ac = (lev["P"].T @ Al @ lev["P"]).tocsr()
+            assert abs(levels[l + 1]["A"] - Ac).max() <= 1e-10 * abs(Ac).max()
+            Al, Bl, dl = levels[l + 1]["A"], Bc, B.shape[1]
+    finally:
+        lib.fe_amg_destroy(h)
+
+
+@pytest.mark.parametrize("case,limit", [("plane_strain", 40), ("tet", 40), ("magnetic", 40)])
+def test_pcg_with_the_parallel_hierarchy(case, limit):
+    """The library's host V-cycle on the parallel hierarchy: PCG to 1e-8 within the
+    limit and within 25% (+2) of the greedy hierarchy's count."""
+    A, b, B, d = problem(case)
+    counts = {}
+    for fn in ("fe_amg_build_parallel_host", "fe_amg_build_host"):
+        lib, h, _ = build(A, B, d, fn)
+
+        def M(v):
+            v = np.ascontiguousarray(v)
+            out = np.empty_like(v)
+            lib.fe_amg_vcycle_host(h, 3, _lib.ptr(v), _lib.ptr(out))
+            return out
+        x, it = AMG.pcg(A, b, M)
+        lib.fe_amg_destroy(h)
+        assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b)
+        counts[fn] = it
+    assert counts["fe_amg_build_parallel_host"] <= limit, counts
+    assert counts["fe_amg_build_parallel_host"] <= 1.25 * counts["fe_amg_build_host"] + 2, counts
+
+
+def test_same_hierarchy_on_every_run():
+    A, b, B, d = problem("plane_strain")
+    runs = []
+    for _ in range(2):
+        lib, h, levels = build(A, B, d)
+        runs.append(levels)
+        lib.fe_amg_destroy(h)
+    for a, b_ in zip(*runs):
+        assert (a["A"] != b_["A"]).nnz == 0
+        if "P" in a:
+            assert (a["P"] != b_["P"]).nnz == 0 and np.array_equal(a["agg"], b_["agg"])
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_fp32_cycle_of_the_device_sequence(case):
+    """fe_amg_vcycle_host_f32 (the device's FP32 cycle, fe_amg_cycle.cuh, run on the
+    host) against the FP64 host cycle: one cycle within 1e-4, and PCG iteration counts
+    within one of the FP64 cycle's for elasticity; for the magnetostatic case (mu_r up
+    to 1000) the FP32 cycle needs 16 iterations where FP64 needs 13, so there the bound
+    is 25% more, plus one."""
+    A, b, B, d = problem(case)
+    lib, h, _ = build(A, B, d)
+    try:
+        r = np.random.default_rng(3).standard_normal(A.shape[0])
+        x64, x32 = np.empty_like(r), np.empty_like(r)
+        _lib.check(lib.fe_amg_vcycle_host(h, 3, _lib.ptr(r), _lib.ptr(x64)), "fe_amg_vcycle_host")
+        _lib.check(lib.fe_amg_vcycle_host_f32(h, 3, _lib.ptr(r), _lib.ptr(x32)), "fe_amg_vcycle_host_f32")
+        assert np.linalg.norm(x32 - x64) <= 1e-4 * np.linalg.norm(x64)
+        counts = {}
+        for fn in ("fe_amg_vcycle_host", "fe_amg_vcycle_host_f32"):
+            f = getattr(lib, fn)
+
+            def M(v, f=f):
+                v = np.ascontiguousarray(v)
+                out = np.empty_like(v)
+                f(h, 3, _lib.ptr(v), _lib.ptr(out))
+                return out
+            x, it = AMG.pcg(A, b, M)
+            assert np.linalg.norm(A @ x - b) <= 1e-8 * np.linalg.norm(b)
+            counts[fn] = it
+        slack = 0.25 * counts["fe_amg_vcycle_host"] if case == "magnetic" else 0
+        assert abs(counts["fe_amg_vcycle_host_f32"] - counts["fe_amg_vcycle_host"]) <= 1 + slack, counts
+    finally:
+        lib.fe_amg_destroy(h)
+
+
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+def test_multigrid_pcg_sequence_on_the_host(case):
+    """fe_amg_pcg_host: the device solve's PCG around the FP32 cycle (fe_amg_cycle.cuh)
+    run on the host, against the model's PCG with the same FP32 cycle: the same
+    iteration count, a true residual below the tolerance, and the solution of the
+    direct solve."""
+    import ctypes
+
+    import scipy.sparse.linalg as spla
+    A, b, B, d = problem(case)
+    lib, h, _ = build(A, B, d)
+    try:
+        x = np.empty_like(b)
+        it, rel, st = ctypes.c_int32(), ctypes.c_double(), ctypes.c_int32()
+        bb = np.ascontiguousarray(b)
+        _lib.check(lib.fe_amg_pcg_host(h, 3, _lib.ptr(bb), 1e-10, 500, _lib.ptr(x), ctypes.byref(it),
+                                       ctypes.byref(rel), ctypes.byref(st)), "fe_amg_pcg_host")
+        assert st.value == 0 and rel.value <= 2e-10, (st.value, rel.value)
+        assert np.linalg.norm(A @ x - b) <= 2e-10 * np.linalg.norm(b)
+
+        def M(v):
+            v = np.ascontiguousarray(v)
+            out = np.empty_like(v)
+            lib.fe_amg_vcycle_host_f32(h, 3, _lib.ptr(v), _lib.ptr(out))
+            return out
+        _, it_model = AMG.pcg(A, b, M, tol=1e-10)
+        assert abs(it.value - it_model) <= 1, (it.value, it_model)
+        xd = spla.spsolve(A.tocsc(), b)
+        assert np.linalg.norm(x - xd) <= 1e-7 * np.linalg.norm(xd)
+    finally:
+        lib.fe_amg_destroy(h)
