@@ -172,21 +172,30 @@ struct PcgVectors {
     double *x, *r, *p, *q, *z;
 };
 
-// PCG on A x = b from x = 0 with z = precond() (reading v.r, writing v.z), to
-// ||r|| <= tol ||b|| on the recurrence; relres is the true residual recomputed in FP64.
-// status: FE_OK, FE_MAXITER, FE_BREAKDOWN (p.Ap <= 0) or FE_NONFINITE.
+// PCG on A x = b with z = precond() (reading v.r, writing v.z), to ||r|| <= tol ||b||
+// on the recurrence; relres is the true residual recomputed in FP64.  From x = 0, or
+// with from_x from the x already in v.x (r = b - A x).  status: FE_OK, FE_MAXITER,
+// FE_BREAKDOWN (p.Ap <= 0) or FE_NONFINITE.
 template <class Ex, class Precond>
 int pcg(Ex &ex, int64_t n, int d, const int64_t *ptr, const int32_t *col, const double *val, const double *b,
-        const PcgVectors &v, Precond precond, double tol, int max_iter, int *iters, double *relres, int *status) {
+        const PcgVectors &v, Precond precond, double tol, int max_iter, int *iters, double *relres, int *status,
+        bool from_x = false) {
     const int64_t nd = n * d;
-    FE_CHECK(ex.fill_zero(v.x, (size_t)nd));
-    FE_CHECK(ex.copy(v.r, b, (size_t)nd));
-    FE_CHECK(precond());
-    FE_CHECK(ex.copy(v.p, v.z, (size_t)nd));
-    double rz = 0.0, bb = 0.0;
-    FE_CHECK(ex.dot(v.r, v.z, nd, &rz));
-    FE_CHECK(ex.dot(v.r, v.r, nd, &bb));
-    int it = 0, st = bb > 0.0 ? FE_MAXITER : FE_OK;
+    if (from_x) {
+        FE_CHECK(ex.rows(n, PassResidual64{ptr, col, val, d, b, v.x, v.r}));
+    } else {
+        FE_CHECK(ex.fill_zero(v.x, (size_t)nd));
+        FE_CHECK(ex.copy(v.r, b, (size_t)nd));
+    }
+    double rz = 0.0, bb = 0.0, rr0 = 0.0;
+    FE_CHECK(ex.dot(b, b, nd, &bb));
+    FE_CHECK(ex.dot(v.r, v.r, nd, &rr0));
+    int it = 0, st = (bb > 0.0 && rr0 > tol * tol * bb) ? FE_MAXITER : FE_OK;
+    if (st == FE_MAXITER) {
+        FE_CHECK(precond());
+        FE_CHECK(ex.copy(v.p, v.z, (size_t)nd));
+        FE_CHECK(ex.dot(v.r, v.z, nd, &rz));
+    }
     while (st == FE_MAXITER && it < max_iter) {
         FE_CHECK(ex.rows(n, PassSpmv64{ptr, col, val, d, v.p, v.q}));
         double pq = 0.0;

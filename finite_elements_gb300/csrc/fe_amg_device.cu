@@ -4,11 +4,11 @@
 // (fe_amg_cycle.cuh; fe_amg_pcg_host runs the same sequence on the host).  The PCG
 // recurrence, its SpMV and the true residual are FP64; the V-cycle runs in FP32 on FP32
 // copies of the levels and is captured once per solve as a CUDA graph.
-//
-// WORK IN PROGRESS: not yet run on a GPU.
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "fe_amg_dev.h"
@@ -59,10 +59,239 @@ __global__ void ka_dot_final(int nb, const double *__restrict__ part, double *ou
     if (threadIdx.x == 0) *out = s;
 }
 
+// ---------------------------------------------------------------- cycle passes, G lanes per row
+// The V-cycle's block-row passes with G lanes of a warp sharing a block row (a strided
+// share of its blocks each, then a shuffle sum): coalesced block loads where one thread
+// per row reads its row's blocks alone.  RD x CD are the block sizes, G is chosen per
+// matrix from its mean row length.
+
+#define FE_LANE_ROWS(G, n)                                                                 \
+    const int sub = threadIdx.x & ((G)-1);                                                 \
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / (G);                        \
+    const int64_t rows_padded = (((n) + groups - 1) / groups) * groups;                    \
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / (G); i < rows_padded; i += groups)
+
+// acc = (B x)_i over the blocks of row i, summed over the G lanes (every lane of the warp
+// calls this; lanes of rows past the end pass valid = false)
+template <int RD, int CD, int G>
+__device__ __forceinline__ void lanes_product(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                              const float *__restrict__ val, const float *__restrict__ x, int64_t i,
+                                              bool valid, int sub, float (&acc)[RD]) {
+#pragma unroll
+    for (int a = 0; a < RD; ++a) acc[a] = 0.0f;
+    if (valid) {
+        const int64_t s1 = ptr[i + 1];
+        for (int64_t s = ptr[i] + sub; s < s1; s += G) {
+            const float *b = val + s * RD * CD;
+            const float *xc = x + (int64_t)__ldg(col + s) * CD;
+            float xv[CD];
+#pragma unroll
+            for (int k = 0; k < CD; ++k) xv[k] = xc[k];
+#pragma unroll
+            for (int a = 0; a < RD; ++a)
+#pragma unroll
+                for (int k = 0; k < CD; ++k) acc[a] = fmaf(__ldg(b + a * CD + k), xv[k], acc[a]);
+        }
+    }
+    if constexpr (G > 1) {
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int a = 0; a < RD; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], o);
+    }
+}
+
+template <int D, int G>
+__global__ void __launch_bounds__(kAT) ka_cheb(int64_t n, amg::PassCheb f) {
+    FE_LANE_ROWS(G, n) {
+        const bool valid = i < n;
+        float az[D];
+        lanes_product<D, D, G>(f.ptr, f.col, f.val, f.zin, i, valid, sub, az);
+        if (valid && sub == 0) {
+            float t[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) t[k] = f.r[i * D + k] - az[k];
+#pragma unroll
+            for (int p = 0; p < D; ++p) {
+                float res = 0.0f;
+#pragma unroll
+                for (int k = 0; k < D; ++k) res += f.dinv[i * D * D + p * D + k] * t[k];
+                const float dn = f.first ? f.b * res : f.a * f.dir[i * D + p] + f.b * res;
+                f.dir[i * D + p] = dn;
+                f.zout[i * D + p] = f.zin[i * D + p] + dn;
+            }
+        }
+    }
+}
+
+template <int D, int G>
+__global__ void __launch_bounds__(kAT) ka_residual(int64_t n, amg::PassResidual32 f) {
+    FE_LANE_ROWS(G, n) {
+        const bool valid = i < n;
+        float ax[D];
+        lanes_product<D, D, G>(f.ptr, f.col, f.val, f.x, i, valid, sub, ax);
+        if (valid && sub == 0)
+#pragma unroll
+            for (int k = 0; k < D; ++k) f.t[i * D + k] = f.r[i * D + k] - ax[k];
+    }
+}
+
+// rows of P^T (aggregates): M x D blocks
+template <int M, int D, int G>
+__global__ void __launch_bounds__(kAT) ka_restrict(int64_t n, amg::PassRestrict32 f) {
+    FE_LANE_ROWS(G, n) {
+        const bool valid = i < n;
+        float o[M];
+        lanes_product<M, D, G>(f.ptr, f.col, f.val, f.t, i, valid, sub, o);
+        if (valid && sub == 0)
+#pragma unroll
+            for (int k = 0; k < M; ++k) f.rc[i * M + k] = o[k];
+    }
+}
+
+// rows of P: D x M blocks
+template <int D, int M, int G>
+__global__ void __launch_bounds__(kAT) ka_prolong(int64_t n, amg::PassProlong32 f) {
+    FE_LANE_ROWS(G, n) {
+        const bool valid = i < n;
+        float px[D];
+        lanes_product<D, M, G>(f.ptr, f.col, f.val, f.xc, i, valid, sub, px);
+        if (valid && sub == 0)
+#pragma unroll
+            for (int k = 0; k < D; ++k) f.x[i * D + k] += px[k];
+    }
+}
+
+// x = inv r on the coarsest level: a warp per row, FP64 sums
+__global__ void __launch_bounds__(kAT) ka_dense(amg::PassDense f) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < f.n; i += warps) {
+        double acc = 0.0;
+        for (int64_t j = lane; j < f.n; j += 32) acc = fma(f.inv[i * f.n + j], (double)f.r[j], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) f.x[i] = (float)acc;
+    }
+}
+
+// lanes per block row for a mean of `mean` blocks per row
+inline int lanes_for(double mean) { return mean < 4 ? 2 : mean < 10 ? 4 : mean < 24 ? 8 : 32; }
+
+template <typename F>
+int with_lanes(int G, F f) {
+    switch (G) {
+        case 2: return f(std::integral_constant<int, 2>{});
+        case 4: return f(std::integral_constant<int, 4>{});
+        case 8: return f(std::integral_constant<int, 8>{});
+        default: return f(std::integral_constant<int, 32>{});
+    }
+}
+
+// Calls f(integral_constant RD, integral_constant CD) for the block shapes of the
+// hierarchies: 1 x 1 (magnetostatics), 2 x 2 / 2 x 3 / 3 x 2 / 3 x 3 (plane elasticity),
+// 3 x 3 / 3 x 6 / 6 x 3 / 6 x 6 (tetrahedra).
+template <typename F>
+int with_shape(int rd, int cd, F f) {
+    using std::integral_constant;
+    if (rd == 1 && cd == 1) return f(integral_constant<int, 1>{}, integral_constant<int, 1>{});
+    if (rd == 2 && cd == 2) return f(integral_constant<int, 2>{}, integral_constant<int, 2>{});
+    if (rd == 2 && cd == 3) return f(integral_constant<int, 2>{}, integral_constant<int, 3>{});
+    if (rd == 3 && cd == 2) return f(integral_constant<int, 3>{}, integral_constant<int, 2>{});
+    if (rd == 3 && cd == 3) return f(integral_constant<int, 3>{}, integral_constant<int, 3>{});
+    if (rd == 3 && cd == 6) return f(integral_constant<int, 3>{}, integral_constant<int, 6>{});
+    if (rd == 6 && cd == 3) return f(integral_constant<int, 6>{}, integral_constant<int, 3>{});
+    if (rd == 6 && cd == 6) return f(integral_constant<int, 6>{}, integral_constant<int, 6>{});
+    set_error("multigrid cycle: unsupported block shape");
+    return FE_BAD_INPUT;
+}
+
+inline int grid_lanes(int64_t n, int G) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n * G + kAT - 1) / kAT, 152 * 8));
+}
+
 struct CycleEx {
     fe_handle_s *h;
     DBuf<double> part, sc;
+    // lanes per row of each matrix the cycle multiplies, keyed by its row pointer
+    std::vector<std::pair<const int64_t *, int>> lanes;
     ~CycleEx() { dfree(part), dfree(sc); }
+    int lanes_of(const int64_t *ptr) const {
+        for (const auto &p : lanes)
+            if (p.first == ptr) return p.second;
+        return 32;
+    }
+    int rows(int64_t n, const amg::PassCheb &f) {
+        if (n <= 0) return FE_OK;
+        const int G = lanes_of(f.ptr);
+        FE_CHECK(with_shape(f.d, f.d, [&](auto r, auto c) {
+            constexpr int D = decltype(r)::value;
+            if constexpr (D != decltype(c)::value) {
+                return (int)FE_BAD_INPUT;
+            } else {
+                return with_lanes(G, [&](auto g) {
+                    ka_cheb<D, decltype(g)::value><<<grid_lanes(n, G), kAT, 0, h->stream>>>(n, f);
+                    return (int)FE_OK;
+                });
+            }
+        }));
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    int rows(int64_t n, const amg::PassResidual32 &f) {
+        if (n <= 0) return FE_OK;
+        const int G = lanes_of(f.ptr);
+        FE_CHECK(with_shape(f.d, f.d, [&](auto r, auto c) {
+            constexpr int D = decltype(r)::value;
+            if constexpr (D != decltype(c)::value) {
+                return (int)FE_BAD_INPUT;
+            } else {
+                return with_lanes(G, [&](auto g) {
+                    ka_residual<D, decltype(g)::value><<<grid_lanes(n, G), kAT, 0, h->stream>>>(n, f);
+                    return (int)FE_OK;
+                });
+            }
+        }));
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    int rows(int64_t n, const amg::PassRestrict32 &f) {
+        if (n <= 0) return FE_OK;
+        const int G = lanes_of(f.ptr);
+        FE_CHECK(with_shape(f.m, f.d, [&](auto r, auto c) {
+            return with_lanes(G, [&](auto g) {
+                ka_restrict<decltype(r)::value, decltype(c)::value, decltype(g)::value>
+                    <<<grid_lanes(n, G), kAT, 0, h->stream>>>(n, f);
+                return (int)FE_OK;
+            });
+        }));
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    int rows(int64_t n, const amg::PassProlong32 &f) {
+        if (n <= 0) return FE_OK;
+        const int G = lanes_of(f.ptr);
+        FE_CHECK(with_shape(f.d, f.m, [&](auto r, auto c) {
+            return with_lanes(G, [&](auto g) {
+                ka_prolong<decltype(r)::value, decltype(c)::value, decltype(g)::value>
+                    <<<grid_lanes(n, G), kAT, 0, h->stream>>>(n, f);
+                return (int)FE_OK;
+            });
+        }));
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
+    int rows(int64_t n, const amg::PassDense &f) {
+        if (n <= 0) return FE_OK;
+        ka_dense<<<grid_lanes(n, 32), kAT, 0, h->stream>>>(f);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
     int dot(const double *a, const double *b, int64_t n, double *out) {
         const int g = grid_a(n);
         FE_CHECK(dalloc(part, (size_t)g));
@@ -130,7 +359,11 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     FE_CUDA(cudaEventRecord(h->events[6], s));
     // the hierarchy, set up on the device, and the cycle's vectors
     DevAmg G;
-    FE_CHECK(amg_setup_device(h, 0.08, 400, G));
+    // down to at most 3000 DOFs (an eighth of small systems): below that the aggregates of
+    // the plane-strain family stop shrinking while the coarse operators fill in (4M DOF:
+    // 647 -> 365 -> 321 -> 217 nodes with rows of 100-200 blocks), and the dense inverse
+    // of a ~2000-DOF level costs less than the products of those levels
+    FE_CHECK(amg_setup_device(h, 0.08, std::min<int64_t>(3000, std::max<int64_t>(100, nd / 8)), G));
     for (auto &L : G.L) FE_CHECK(prepare_cycle(h, L));
     FE_CHECK(dalloc(G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
     FE_CHECK(dalloc(G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
@@ -166,6 +399,12 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     amg::CycleCoarse coarse;
     coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
     CycleEx cex{h};
+    for (const DevLevel &Dl : G.L) {
+        const double n_rows = (double)std::max<int64_t>(Dl.A.n, 1), n_aggr = (double)std::max<int64_t>(Dl.PT.n, 1);
+        cex.lanes.push_back({Dl.A.ptr.p, lanes_for((double)Dl.A.nnzb / n_rows)});
+        cex.lanes.push_back({Dl.P.ptr.p, lanes_for((double)Dl.P.nnzb / n_rows)});
+        cex.lanes.push_back({Dl.PT.ptr.p, lanes_for((double)Dl.PT.nnzb / n_aggr)});
+    }
     // the cycle's fixed sequence of launches (about ten per level) captured once as a
     // CUDA graph, launched once per PCG iteration
     cudaGraphExec_t cycle = nullptr;
@@ -207,18 +446,31 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     };
     const double tol = o->tol > 0 ? o->tol : 1e-10;
     const int max_iter = o->max_iter > 0 ? o->max_iter : 10000;
-    int it = 0, status = FE_OK;
+    const int max_restart = o->max_outer > 0 ? o->max_outer : 4;
+    int status = FE_OK, total = 0, restarts = 0, x0_used = 0;
     double relres = 0.0;
+    // the start: the prescribed values on constrained DOFs, and opts.x0 where given (with
+    // FE_SOLVE_X0_IF_BETTER only when its FP64 residual beats the zero start)
+    FE_CHECK(solve_start_point(h, o, h->w.x.p, &x0_used));
     const amg::PcgVectors v{h->w.x.p, r.p, p.p, q.p, z.p};
-    FE_CHECK(amg::pcg(cex, n, D, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, h->b.p, v, precond, tol, max_iter, &it,
-                      &relres, &status));
+    // PCG from x; when the recurrence met tol but the FP64 true residual did not (the
+    // recurrence drifts from b - A x by about eps cond(A)), restart from the true residual
+    for (;;) {
+        int it = 0;
+        FE_CHECK(amg::pcg(cex, n, D, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, h->b.p, v, precond, tol,
+                          max_iter - total, &it, &relres, &status, true));
+        total += it;
+        if (status != FE_OK || relres <= tol || restarts >= max_restart || total >= max_iter) break;
+        ++restarts;
+    }
+    if (status == FE_OK && relres > tol && !(o->flags & FE_SOLVE_ACCEPT_STAGNATION)) status = FE_MAXITER;
     double bb = 0.0;
     FE_CHECK(cex.dot(h->b.p, h->b.p, nd, &bb));
-    st->iterations = it;
-    st->spmv = it + 1;
-    st->outer = 0;
+    st->iterations = total;
+    st->spmv = total + 1 + restarts;
+    st->outer = restarts;
     st->fp64_iterations = 0;
-    st->x0_used = 0;
+    st->x0_used = x0_used;
     st->bnorm = std::sqrt(bb);
     st->relres = relres;
     st->status = status;

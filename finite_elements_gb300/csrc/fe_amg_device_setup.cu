@@ -1,10 +1,9 @@
 // Device setup of the smoothed-aggregation hierarchy: amg::setup_hierarchy
 // (fe_amg_passes.cuh, the passes fe_amg_build_parallel_host runs on the host) on the
 // device executor -- every pass one grid-stride kernel over its rows, int64 prefix
-// sums on the device between the passes that size the next ones.  Only the coarsest
-// matrix (a few hundred DOFs) goes to the host, for its dense inverse.
-//
-// WORK IN PROGRESS: not yet run on a GPU.
+// sums on the device between the passes that size the next ones -- and the dense
+// inverse of the coarsest matrix (at most 4096 DOFs) by Gauss-Jordan elimination on the
+// device.
 #include <algorithm>
 #include <cmath>
 #include <functional>
@@ -12,6 +11,7 @@
 
 #include "fe_amg_dev.h"
 #include "fe_amg_par.cuh"
+#include "fe_grid_sync.cuh"
 
 namespace fe {
 namespace {
@@ -139,6 +139,57 @@ __global__ void kd_dot_final(int nb, const double *__restrict__ part, double *ou
     if (threadIdx.x == 0) *out = s;
 }
 
+// y = D^-1 A x (FP64) with G lanes of a warp per block row (a strided share of its
+// blocks each, then a shuffle sum): the power iterations of the lmax estimates
+template <int D, int G>
+__global__ void __launch_bounds__(kST) kd_dinv_product(int64_t n, amg::PassDinvProduct f) {
+    const int sub = threadIdx.x & (G - 1);
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+    const int64_t rows_padded = ((n + groups - 1) / groups) * groups;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; i < rows_padded; i += groups) {
+        double acc[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) acc[a] = 0.0;
+        if (i < n) {
+            for (int64_t s = f.ptr[i] + sub; s < f.ptr[i + 1]; s += G) {
+                const double *b = f.val + s * D * D;
+                const double *xc = f.x + (int64_t)f.col[s] * D;
+#pragma unroll
+                for (int a = 0; a < D; ++a)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) acc[a] = fma(b[a * D + k], xc[k], acc[a]);
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int a = 0; a < D; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], o);
+        if (i < n && sub == 0)
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                double v = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) v = fma(f.dinv[i * D * D + a * D + k], acc[k], v);
+                f.y[i * D + a] = v;
+            }
+    }
+}
+
+template <int D>
+int launch_dinv_product(int64_t n, const amg::PassDinvProduct &f, cudaStream_t s) {
+    const double mean = n > 0 ? (double)f.nnzb / (double)n : 0.0;
+    const int G = mean < 4 ? 2 : mean < 10 ? 4 : mean < 24 ? 8 : 32;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n * G + kST - 1) / kST, 152 * 8));
+    switch (G) {
+        case 2: kd_dinv_product<D, 2><<<grid, kST, 0, s>>>(n, f); break;
+        case 4: kd_dinv_product<D, 4><<<grid, kST, 0, s>>>(n, f); break;
+        case 8: kd_dinv_product<D, 8><<<grid, kST, 0, s>>>(n, f); break;
+        default: kd_dinv_product<D, 32><<<grid, kST, 0, s>>>(n, f); break;
+    }
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
 struct DevEx {
     cudaStream_t s;
     DBuf<int64_t> scan_tmp;
@@ -166,6 +217,20 @@ struct DevEx {
         k_rows<F><<<grid_s(n), kST, 0, s>>>(n, f);
         FE_LAUNCH_CHECK();
         return FE_OK;
+    }
+    // the power iterations' product with lanes per row; other block sizes row by row
+    int rows(int64_t n, const amg::PassDinvProduct &f) {
+        if (n <= 0) return FE_OK;
+        switch (f.d) {
+            case 1: return launch_dinv_product<1>(n, f, s);
+            case 2: return launch_dinv_product<2>(n, f, s);
+            case 3: return launch_dinv_product<3>(n, f, s);
+            case 6: return launch_dinv_product<6>(n, f, s);
+            default:
+                k_rows<amg::PassDinvProduct><<<grid_s(n), kST, 0, s>>>(n, f);
+                FE_LAUNCH_CHECK();
+                return FE_OK;
+        }
     }
     int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) { return scan64(in, n, out, total, scan_tmp, s); }
     int dot(const double *a, const double *b, int64_t n, double *out) {
@@ -228,6 +293,120 @@ int csr_to_host(const DevCsr &D, BlockCsr &H, cudaStream_t s) {
     return FE_OK;
 }
 
+// ---------------------------------------------------------------- coarsest inverse
+// Dense inverse of the coarsest matrix by Gauss-Jordan elimination without pivoting
+// (the matrix is symmetric positive definite once 1e-12 of its largest diagonal entry
+// is added, as the host version does), in place, one pivot k after the other:
+//   others:  a_ij -= a_ik a_kj / a_kk      (i != k, j != k)
+//   row k:   a_kj /= a_kk (j != k);  column k: a_ik = -a_ik / a_kk (i != k);  a_kk = 1 / a_kk
+
+constexpr int kMaxCoarse = 4096;   // DOFs of the coarsest level (a 128 MB inverse)
+
+__global__ void kc_dense_fill(int64_t nb_rows, int cd, const int64_t *__restrict__ ptr,
+                              const int32_t *__restrict__ col, const double *__restrict__ val, int64_t n,
+                              double *__restrict__ M) {
+    FE_ROWS(i, nb_rows)
+    for (int64_t s = ptr[i]; s < ptr[i + 1]; ++s)
+        for (int a = 0; a < cd; ++a)
+            for (int b = 0; b < cd; ++b) M[(i * cd + a) * n + (int64_t)col[s] * cd + b] = val[(s * cd + a) * cd + b];
+}
+
+// one block: the diagonal gets 1e-12 of its largest magnitude added
+__global__ void kc_regularise(int64_t n, double *M) {
+    __shared__ double sh[kST / 32];
+    double m = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(M[i * n + i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < kST / 32; ++w) t = fmax(t, sh[w]);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M[i * n + i] += 1e-12 * t;
+}
+
+// All pivots in one cooperative launch: thread t owns the elements e = t, t + T, ... of
+// the row-major matrix; per pivot, the other elements are updated from the pivot row
+// and column (read through L2: their owners rewrite them), a grid barrier, then the
+// owners of the pivot row and column rescale them, and another barrier.  A zero or
+// non-finite pivot stops every block at the same step (*singular = 1).
+__global__ void __launch_bounds__(kST) kc_gauss_jordan(int64_t n, double *M, unsigned *bar, int *err,
+                                                       int *singular) {
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    const int64_t nn = n * n;
+    for (int64_t k = 0; k < n; ++k) {
+        const double p = __ldcg(M + k * n + k);
+        if (p == 0.0 || !isfinite(p)) {
+            if (t0 == 0) *singular = 1;
+            return;
+        }
+        const double ip = 1.0 / p;
+        for (int64_t e = t0; e < nn; e += nt) {
+            const int64_t i = e / n, j = e - i * n;
+            if (i == k || j == k) continue;
+            __stcg(M + e, fma(-__ldcg(M + i * n + k) * ip, __ldcg(M + k * n + j), __ldcg(M + e)));
+        }
+        if (!grid_sync_bounded(bar, err)) return;
+        for (int64_t e = t0; e < nn; e += nt) {
+            const int64_t i = e / n, j = e - i * n;
+            if (i == k && j == k) __stcg(M + e, ip);
+            else if (i == k) __stcg(M + e, __ldcg(M + e) * ip);
+            else if (j == k) __stcg(M + e, -__ldcg(M + e) * ip);
+        }
+        if (!grid_sync_bounded(bar, err)) return;
+    }
+}
+
+int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
+    const int64_t n = C.n * C.rd;
+    if (n > kMaxCoarse) {
+        set_error("multigrid setup: coarsest level too large for its dense solve");
+        return FE_BAD_INPUT;
+    }
+    G.nc = n;
+    FE_CHECK(dalloc(G.cinv, (size_t)std::max<int64_t>(n * n, 1)));
+    if (n == 0) return FE_OK;
+    DBuf<int> flag;   // [0] singular, [1] [2] the grid barrier, [3] its error word
+    FE_CHECK(dalloc(flag, 4));
+    struct Free {
+        DBuf<int> &f;
+        ~Free() { dfree(f); }
+    } fr{flag};
+    FE_CUDA(cudaMemsetAsync(flag.p, 0, 4 * sizeof(int), s));
+    FE_CUDA(cudaMemsetAsync(G.cinv.p, 0, (size_t)n * n * sizeof(double), s));
+    kc_dense_fill<<<grid_s(C.n), kST, 0, s>>>(C.n, C.rd, C.ptr.p, C.col.p, C.val.p, n, G.cinv.p);
+    kc_regularise<<<1, kST, 0, s>>>(n, G.cinv.p);
+    FE_LAUNCH_CHECK();
+    // the cooperative grid: every SM's resident blocks of the kernel
+    int dev = 0, sms = 0, per_sm = 0;
+    FE_CUDA(cudaGetDevice(&dev));
+    FE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)kc_gauss_jordan, kST, 0));
+    const int64_t want = (n * n + kST - 1) / kST;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1)));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kST);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FE_CUDA(cudaLaunchKernelEx(&cfg, kc_gauss_jordan, n, G.cinv.p, (unsigned *)(flag.p + 1), flag.p + 3, flag.p));
+    int host[4] = {0, 0, 0, 0};
+    FE_CUDA(cudaMemcpyAsync(host, flag.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    if (host[3]) {
+        set_error("multigrid setup: a grid barrier of the coarsest inverse timed out");
+        return FE_CUDA_ERR;
+    }
+    if (host[0]) {
+        set_error("multigrid setup: singular coarsest matrix");
+        return FE_BREAKDOWN;
+    }
+    return FE_OK;
+}
+
 }  // namespace
 
 int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G) {
@@ -263,18 +442,8 @@ int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &
         G.L.push_back(L);
     }
     FE_CHECK(st);
-    // coarsest level: its dense inverse on the host
-    BlockCsr C;
-    FE_CHECK(csr_to_host(G.coarse, C, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    std::vector<double> inv;
-    FE_CHECK(coarse_inverse_of(C, inv, "multigrid setup"));
-    G.nc = C.n * C.rd;
-    FE_CHECK(dalloc(G.cinv, std::max<size_t>(inv.size(), 1)));
-    if (!inv.empty())
-        FE_CUDA(cudaMemcpyAsync(G.cinv.p, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    return FE_OK;
+    // coarsest level: its dense inverse, on the device
+    return coarse_inverse_device(G.coarse, G, s);
 }
 
 int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s) {

@@ -73,8 +73,10 @@ struct PassPowerStart {
     FE_HD void operator()(int64_t i) const { x[i] = 1.0 + (double)(i % 7) / 7.0; }
 };
 
+// nnzb: the matrix's block count (a device executor sizes its lanes per row with it)
 struct PassDinvProduct {
     const int64_t *ptr; const int32_t *col; const double *val; const double *dinv; int d; const double *x; double *y;
+    int64_t nnzb;
     FE_HD void operator()(int64_t i) const { row_dinv_product(ptr, col, val, dinv, d, x, i, y); }
 };
 
@@ -280,7 +282,7 @@ int lmax_of(Ex &ex, const Csr &A, const double *dinv, double *lmax) {
     FE_CHECK(ex.alloc(x, (size_t)std::max<int64_t>(nd, 1)));
     FE_CHECK(ex.alloc(y, (size_t)std::max<int64_t>(nd, 1)));
     FE_CHECK(ex.rows(nd, PassPowerStart{x.p}));
-    const PassDinvProduct prod{A.ptr.p, A.col.p, A.val.p, dinv, d, x.p, y.p};
+    const PassDinvProduct prod{A.ptr.p, A.col.p, A.val.p, dinv, d, x.p, y.p, A.nnzb};
     for (int it = 0; it < 30; ++it) {
         FE_CHECK(ex.rows(A.n, prod));
         double yy = 0.0;

@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "fe_internal.h"
+#include "fe_grid_sync.cuh"
 #include "fe_sell.cuh"
 
 namespace fe {
@@ -44,7 +45,6 @@ constexpr int kWarps = kBT / 32;
 constexpr int kMaxTerms = 128;                 // Chebyshev terms per preconditioner application
 constexpr int kHist = 64;                      // CG coefficients kept per instance for the Lanczos estimate
 constexpr int kProbe = 40;                     // iterations of the Jacobi-PCG probe
-constexpr unsigned kSpinLimit = 1u << 24;      // polls of a grid barrier before it gives up (~1 s)
 
 struct BatchArgs {
     int64_t n_nodes = 0, n_slices = 0, n_slots = 0;
@@ -76,37 +76,9 @@ struct BatchArgs {
 
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
-// Grid-wide barrier of a cooperative launch (all blocks resident).  Thread 0 of each
-// block arrives with an atomic and waits for the generation to move; the wait polls at
-// most kSpinLimit times.  Returns false in every thread of the block once any block has
-// given up; the caller then leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(const BatchArgs &a) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = a.bar + 1;
-        const unsigned g = *gen;
-        __threadfence();
-        if (atomicAdd(a.bar, 1u) == gridDim.x - 1) {
-            atomicExch(a.bar, 0u);
-            __threadfence();
-            atomicAdd(a.bar + 1, 1u);
-        } else {
-            unsigned spins = 0;
-            while (*gen == g) {
-                if (++spins > kSpinLimit || ld_volatile(a.err)) {
-                    atomicExch(a.err, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        ok = ld_volatile(a.err) == 0;
-    }
-    __syncthreads();
-    return ok;
-}
+// The grid barrier between phases (fe_grid_sync.cuh): false once any block has given up
+// waiting, and the caller then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(const BatchArgs &a) { return grid_sync_bounded(a.bar, a.err); }
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -284,6 +284,9 @@ int solve_continuity(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *
 // Largest eigenvalue of the m x m tridiagonal Lanczos matrix of the CG coefficients
 // alpha[0..m), beta[0..m) (bisection on the Sturm sequence), fe_solver.cu.
 double lanczos_lmax(const double *alpha, const double *beta, int m);
+// The start of a solve: opts.x0 (or 0) with the prescribed values; with
+// FE_SOLVE_X0_IF_BETTER the start of smaller FP64 residual (fe_solver.cu).
+int solve_start_point(fe_handle_s *h, const fe_solve_opts *o, double *x, int *x0_used);
 // FP64 PCG with a smoothed-aggregation V-cycle preconditioner (fe_amg_device.cu)
 int solve_multigrid(fe_handle_s *h, const fe_solve_opts *opts, fe_solve_stats *stats);
 int set_rhs_additions(fe_handle_s *h, int64_t n, const int64_t *dof, const double *value);

@@ -1480,6 +1480,13 @@ int solve_mixed(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
 
 }  // namespace
 
+// The start of a solve (x = opts.x0 or 0, the prescribed values on constrained DOFs;
+// with FE_SOLVE_X0_IF_BETTER the start whose FP64 residual is smaller), for solvers
+// outside this file.
+int solve_start_point(fe_handle_s *h, const fe_solve_opts *o, double *x, int *x0_used) {
+    return with_dim(h->dim, [&](auto d) { return start_point<decltype(d)::value, 2>(h, o, x, x0_used); });
+}
+
 // Largest eigenvalue of the tridiagonal Lanczos matrix built from CG coefficients,
 // by bisection on the Sturm sequence.
 double lanczos_lmax(const double *alpha, const double *beta, int m) {

@@ -284,8 +284,9 @@ class GpuSystem:
         """Solve the eliminated system on the GPU.  precision: "fp64", "mixed" or
         "mixed-cg64" (see PRECISIONS).  x0 / x0_device_ptr: warm start; with
         x0_if_better it is kept only when its true residual beats the zero start.
-        multigrid: FP64 PCG preconditioned by a smoothed-aggregation V-cycle (work in
-        progress; precision, Chebyshev and warm-start options are not used).
+        multigrid: PCG with an FP64 recurrence preconditioned by one FP32
+        smoothed-aggregation V-cycle per iteration, the hierarchy set up on the device
+        (precision and Chebyshev options are not used; x0 and x0_if_better are).
         Returns (x, stats): x holds n_dof + n_bc values (u then the multipliers) or
         None with want_host=False."""
         o = SolveOpts()

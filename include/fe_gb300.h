@@ -64,9 +64,13 @@ extern "C" {
 #define FE_SOLVE_RESTART_EACH_STEP 2   /* mixed: restart the Krylov space at every refinement
                                           step (classic iterative refinement) instead of
                                           continuing along the current direction          */
-#define FE_SOLVE_MULTIGRID        8    /* FP64 PCG preconditioned by a smoothed-aggregation
-                                          V-cycle (hierarchy set up on the host); work in
-                                          progress, not yet run on a GPU                    */
+#define FE_SOLVE_MULTIGRID        8    /* PCG with an FP64 recurrence preconditioned by one
+                                          FP32 smoothed-aggregation V-cycle per iteration
+                                          (hierarchy set up on the device at every solve;
+                                          Chebyshev(3) smoothing on node-block Jacobi, a
+                                          dense coarsest solve); precision and Chebyshev
+                                          options are not used, x0 and
+                                          FE_SOLVE_X0_IF_BETTER are                        */
 
 /* solver precision */
 #define FE_PREC_FP64   0   /* FP64 PCG: the drop-in for spsolve                            */
@@ -286,9 +290,9 @@ int fe_amg_build_parallel_host(int64_t n_nodes, int32_t d, const int64_t *blk_pt
                                const double *vals, int32_t m, const double *nullspace, double theta,
                                int64_t coarse_dofs, fe_amg *out);
 /* The same passes on the device, from the assembled system of h (near-null space: the
- * rigid-body modes, or the constant for magnetostatics, zero on the constrained DOFs);
- * the hierarchy is copied to the host for the accessors below.  Work in progress: not
- * yet run on a GPU. */
+ * rigid-body modes, or the constant for magnetostatics, zero on the constrained DOFs),
+ * with the coarsest inverse computed on the device; the hierarchy is copied to the host
+ * for the accessors below. */
 int fe_amg_build_device(fe_handle h, double theta, int64_t coarse_dofs, fe_amg *out);
 int fe_amg_levels(fe_amg a, int32_t *n_levels);
 int fe_amg_level_info(fe_amg a, int32_t level, int64_t *n_nodes, int32_t *d, int64_t *nnzb_A,

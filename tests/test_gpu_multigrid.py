@@ -1,4 +1,4 @@
-"""Multigrid-preconditioned FP64 PCG (smoothed-aggregation V-cycle, work in progress)
+"""Multigrid-preconditioned PCG (FP64 recurrence, FP32 smoothed-aggregation V-cycle)
 against the oracle's direct solve: plane strain, tetrahedra and magnetostatics, each
 to ||x - x_ref|| <= 1e-9 ||x_ref|| in a few tens of iterations."""
 import numpy as np
