@@ -63,7 +63,10 @@ def parse_args():
     ap.add_argument("--quick-plain", action="store_true",
                     help="with --quick: time the plain FP64 PCG step instead of the headline")
     ap.add_argument("--quick-multigrid", action="store_true",
-                    help="time only the multigrid-preconditioned solve (device setup + FP32 V-cycle PCG)")
+                    help="--quick with --solver multigrid")
+    ap.add_argument("--solver", choices=("multigrid", "chebyshev"), default="multigrid",
+                    help="preconditioner of the headline mixed-precision solve: the FP32 smoothed-aggregation "
+                         "V-cycle (set up on the device every step) or node-block Jacobi + Chebyshev in FP32")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--l2-keep", type=float, default=-1.0,
@@ -75,7 +78,10 @@ def parse_args():
                     help="cells of the tetrahedral cantilever (6 tetrahedra per cell)")
     ap.add_argument("--tet-cheb", type=int, default=24, help="Chebyshev degree of the 3D mixed solve")
     ap.add_argument("--tet-cheb-ratio", type=float, default=10000.0, help="its interval lmax/lmin")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.quick_multigrid:
+        a.quick, a.solver = True, "multigrid"
+    return a
 
 
 # ---------------------------------------------------------------- multi-process plumbing
@@ -226,10 +232,13 @@ def run_ours(args, dist):
     if args.l2_keep >= 0:
         h.call("fe_set_l2_keep", int(args.l2_keep * 1e6))
     step_flags = _lib.FE_ASSEMBLE_PATTERN | _lib.FE_ASSEMBLE_K | _lib.FE_ASSEMBLE_F
-    # headline: FP64 CG recurrence with the FP32 Chebyshev preconditioner; beside it the
+    # headline: FP64 CG recurrence with an FP32 preconditioner -- the smoothed-aggregation
+    # V-cycle, or node-block Jacobi + Chebyshev -- and the other one beside it, the
     # FP32-Krylov + iterative-refinement form and the plain FP64 PCG
-    mode = dict(precision="mixed-cg64", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
-                want_host=False)
+    mg_mode = dict(precision="mixed-cg64", tol=args.tol, multigrid=True, want_host=False)
+    cheb_mode = dict(precision="mixed-cg64", tol=args.tol, cheb_degree=args.cheb, cheb_ratio=args.cheb_ratio,
+                     want_host=False)
+    mode, other = (mg_mode, cheb_mode) if args.solver == "multigrid" else (cheb_mode, mg_mode)
     ir_mode = dict(precision="mixed", tol=args.tol, cheb_degree=args.ir_cheb, cheb_ratio=args.ir_cheb_ratio,
                    want_host=False)
     plain = dict(precision="fp64", tol=args.tol, cheb_degree=args.plain_cheb, cheb_ratio=args.plain_cheb_ratio,
@@ -261,23 +270,6 @@ def run_ours(args, dist):
         h.call("fe_profile_read", precision, ctypes.byref(cm), ctypes.byref(cn), ctypes.byref(sm), ctypes.byref(sn))
         return {"cheb_us": 1e3 * cm.value / max(cn.value, 1), "cheb_n": cn.value,
                 "spmv_us": 1e3 * sm.value / max(sn.value, 1), "spmv_n": sn.value}
-
-    if args.quick_multigrid:
-        # the multigrid step: assembly, device setup of the hierarchy, PCG with the V-cycle
-        mg = dict(precision="fp64", tol=args.tol, want_host=False, multigrid=True)
-        for _ in range(args.warmup):
-            device_step(mg)
-        h.call("fe_synchronize")
-        h.call("fe_event_record", 0)
-        mst = [device_step(mg) for _ in range(args.steps)]
-        h.call("fe_event_record", 1)
-        h.call("fe_synchronize")
-        ms = ctypes.c_double()
-        h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
-        s.close()
-        return {"metric": METRIC, "multigrid_s_per_solve": ms.value / 1e3 / args.steps, "quick": True,
-                "iterations": mst[-1].iterations, "relres": mst[-1].relres,
-                "solve_ms": mst[-1].solve_ms, "assemble_ms": mst[-1].assemble_ms}
 
     if args.quick and args.quick_plain:
         # profiler runs of the plain FP64 step: no event records, no other legs
@@ -316,6 +308,14 @@ def run_ours(args, dist):
     prof_mixed = profile_read(_lib.FE_PREC_MIXED_CG64)
     ms = ctypes.c_double()
     h.call("fe_event_elapsed_ms", 0, 1, ctypes.byref(ms))
+    mg_prof = None
+    if args.solver == "multigrid":
+        v = [ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(),
+             ctypes.c_int64()]
+        h.call("fe_profile_read_multigrid", *[ctypes.byref(x) for x in v])
+        mg_prof = {"smooth_us": 1e3 * v[0].value / max(v[1].value, 1), "smooth_n": v[1].value,
+                   "setup_ms": v[2].value / max(v[3].value, 1), "cycle_ms": v[4].value / max(v[5].value, 1),
+                   "cycles": v[5].value}
     dist.barrier()
     t_total = dist.max(ms.value / 1e3)
     value = t_total / (args.steps * dist.world)
@@ -323,8 +323,10 @@ def run_ours(args, dist):
     h.call("fe_get_solution", _lib.ptr(x_mixed))
     if args.quick:
         s.close()
-        return {"metric": METRIC, "value": value, "unit": UNIT, "quick": True,
-                "iterations": stats[-1].iterations, "gpu_launches": int(n_launch)}
+        return {"metric": METRIC, "value": value, "unit": UNIT, "quick": True, "solver": args.solver,
+                "iterations": stats[-1].iterations, "relres": stats[-1].relres, "solve_ms": stats[-1].solve_ms,
+                "assemble_ms": stats[-1].assemble_ms, "learned_x0_used": stats[-1].x0_used,
+                "gpu_launches": int(n_launch)}
 
     # ---- mixed precision without the learned warm start, same step
     h.call("fe_synchronize")
@@ -334,6 +336,21 @@ def run_ours(args, dist):
     h.call("fe_synchronize")
     h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
     mixed_only_s = ms.value / 1e3 / max(args.plain_steps, 1)
+
+    # ---- the other preconditioner of the mixed solve, same step (with the live timing
+    # of the Chebyshev solve's kernels)
+    device_step(other)
+    h.call("fe_synchronize")
+    h.call("fe_profile_kernels", 1)
+    h.call("fe_event_record", 2)
+    ostats = [device_step(other) for _ in range(max(args.plain_steps, 1))]
+    h.call("fe_event_record", 3)
+    h.call("fe_synchronize")
+    h.call("fe_event_elapsed_ms", 2, 3, ctypes.byref(ms))
+    other_s = ms.value / 1e3 / max(args.plain_steps, 1)
+    if args.solver == "multigrid":
+        prof_mixed = profile_read(_lib.FE_PREC_MIXED_CG64)
+    h.call("fe_profile_kernels", 0)
 
     # ---- FP32 Krylov vectors and SpMV with FP64 iterative refinement, same step
     device_step(ir_mode)
@@ -396,12 +413,46 @@ def run_ours(args, dist):
         gbs = bytes_ / (us * 1e-6) / 1e9 if us > 0 else None
         return gbs, (gbs / hbm_peak if gbs else None)
 
+    # the V-cycle's level-0 Chebyshev step (ka_cheb<2,4>): FP32 2x2 blocks of the whole
+    # eliminated K (16 B) and their int32 columns, int64 row pointers, and per node the
+    # FP32 block-Jacobi inverse (16 B), r, z_k and z_k+1 (8 B each) and the direction
+    # (written by the first of the three steps, read and written by the other two)
+    def smooth_bytes():
+        return nnzb * 20 + (n_nodes + 1) * 8 + n_nodes * (16 + 3 * 8) + n_nodes * (8 + 16 + 16) / 3
+
     cheb_gbs, cheb_frac = roof(cheb_bytes(4), prof_mixed["cheb_us"])
     spmvmp_gbs, spmvmp_frac = roof(spmv_bytes(8), prof_mixed["spmv_us"])
     cheb64_gbs, cheb64_frac = roof(cheb_bytes(8), prof_plain["cheb_us"])
     spmv64_gbs, spmv64_frac = roof(spmv_bytes(8), prof_plain["spmv_us"])
     keep_bytes = 40_000_000 if args.l2_keep < 0 else int(args.l2_keep * 1e6)
     traffic = NCU_TRAFFIC.get((args.nx, args.ny, keep_bytes))
+    cheb_line = {"bound": "hbm", "kernel": "k_cheb_step<2,float,double,2,0> (intermediate FP32 Chebyshev step of "
+                                           f"the Chebyshev-preconditioned solve: {max(args.cheb - 2, 0)} of the "
+                                           f"{args.cheb + 2} kernels of its iteration)",
+                 "achieved": cheb_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": cheb_frac,
+                 "peak_source": peak_src, "traffic": traffic,
+                 "bytes_per_launch": cheb_bytes(4), "launch_us": prof_mixed["cheb_us"],
+                 "launches_timed": prof_mixed["cheb_n"],
+                 "timing": "CUDA events captured in the PCG graph around the run of intermediate Chebyshev steps "
+                           "of the first iteration of each 16-iteration chunk, during the timed solves of that "
+                           "solver; launch_us = that time / the launches it covers"}
+    if mg_prof is not None:
+        sm_gbs, sm_frac = roof(smooth_bytes(), mg_prof["smooth_us"])
+        roofline = {"bound": "hbm",
+                    "kernel": "ka_cheb<2,4> (level-0 Chebyshev smoothing step of the FP32 V-cycle, 4 lanes per "
+                              "block row; 6 of the cycle's launches at level 0)",
+                    "achieved": sm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": sm_frac, "peak_source": peak_src,
+                    "traffic": None, "bytes_per_launch": smooth_bytes(), "launch_us": mg_prof["smooth_us"],
+                    "launches_timed": mg_prof["smooth_n"],
+                    "share_of_step": (mg_prof["smooth_us"] * 2 * 1e-6 * mg_prof["cycles"] / args.steps / value
+                                      if value > 0 else None),
+                    "timing": "CUDA events captured in the V-cycle graph around level 0's pre-smoothing, read "
+                              "after every cycle of the timed solves; launch_us = that time / 3 launches"}
+        mg_section = {"setup_ms_per_solve": mg_prof["setup_ms"], "cycle_ms": mg_prof["cycle_ms"],
+                      "cycles_per_solve": mg_prof["cycles"] / max(args.steps, 1),
+                      "level0_smoothing_us_per_launch": mg_prof["smooth_us"]}
+    else:
+        roofline, mg_section = cheb_line, None
     s.close()
 
     # ---- end to end through the C ABI, host buffers in and out
@@ -429,19 +480,26 @@ def run_ours(args, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 CG recurrence (x, r, p, q, one SpMV per iteration) + f32 Chebyshev preconditioner",
+        "dtype": "f64 CG recurrence (x, r, p, q, one SpMV per iteration) + f32 preconditioner"
+                 + (" (V-cycle)" if args.solver == "multigrid" else " (Chebyshev)"),
         "data": f"synthetic, seeded (seed {args.seed})",
         "config": workload_config(args, prob.n_dof, dist.world),
         "solver": {
-            "mode":"mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
-                    "preconditioner in FP32 on the prescaled FP32 copy"
+            "mode": ("mixed precision: FP64 CG recurrence on the FP64 copy of the eliminated system, "
+                     "preconditioned by one FP32 smoothed-aggregation V-cycle per iteration (hierarchy set up on "
+                     "the device every step, Chebyshev(3) smoothing on node-block Jacobi, dense coarsest solve)"
+                     if args.solver == "multigrid" else
+                     "mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
+                     "preconditioner in FP32 on the prescaled FP32 copy")
                     + (" + learned warm start (predicted every step; kept when its FP64 residual beats the zero "
                        "start)" if net is not None else ""),
+            "preconditioner": args.solver,
             "learned_warm_start": net is not None,
             "l2_keep_mb": 40.0 if args.l2_keep < 0 else args.l2_keep,
             "chebyshev": {"mixed": [args.cheb, args.cheb_ratio], "plain": [args.plain_cheb, args.plain_cheb_ratio],
                           "fp32_krylov_ir": [args.ir_cheb, args.ir_cheb_ratio]},
-            "step": "pattern + element kernels + reduction + loads + elimination + PCG",
+            "step": "pattern + element kernels + reduction + loads + elimination + "
+                    + ("multigrid setup + " if args.solver == "multigrid" else "") + "PCG",
         },
         "iterations": stats[-1].iterations, "restarts": stats[-1].outer, "learned_x0_used": stats[-1].x0_used,
         "assemble_ms": stats[-1].assemble_ms, "solve_ms": stats[-1].solve_ms,
@@ -450,19 +508,15 @@ def run_ours(args, dist):
                        "relres": pstats[-1].relres if pstats else None},
         "speedup_vs_plain": plain_s / value if value > 0 else None,
         "mixed_without_learned": {"s_per_solve": mixed_only_s, "iterations": nstats[-1].iterations},
+        ("mixed_chebyshev" if args.solver == "multigrid" else "mixed_multigrid"): {
+            "s_per_solve": other_s, "iterations": ostats[-1].iterations, "relres": ostats[-1].relres},
         "fp32_krylov_ir": {"s_per_solve": ir_s, "iterations": istats[-1].iterations,
                            "refinement_steps": istats[-1].outer},
-        "roofline": {"bound": "hbm", "kernel": "k_cheb_step<2,float,double,2,0> (intermediate FP32 Chebyshev step: "
-                                                f"{max(args.cheb - 2, 0)} of the {args.cheb + 2} kernels of an iteration)",
-                     "achieved": cheb_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": cheb_frac,
-                     "peak_source": peak_src, "traffic": traffic,
-                     "bytes_per_launch": cheb_bytes(4), "launch_us": prof_mixed["cheb_us"],
-                     "launches_timed": prof_mixed["cheb_n"],
-                     "timing": "CUDA events captured in the PCG graph around the run of intermediate "
-                               "Chebyshev steps of the first iteration of each 16-iteration chunk, during the "
-                               "timed solves; launch_us = that time / the launches it covers"},
+        "roofline": roofline,
+        "multigrid": mg_section,
         "kernels": {
-            "mixed_pcg_spmv": {"kernel": "k_pcg_spmv<2,double> (the recurrence's FP64 SpMV)",
+            "mixed_cheb_step": cheb_line,
+            "mixed_pcg_spmv": {"kernel": "k_pcg_spmv<2,double> (the Chebyshev-preconditioned solve's FP64 SpMV)",
                                "launch_us": prof_mixed["spmv_us"], "bytes_per_launch": spmv_bytes(8),
                                "achieved_gbs": spmvmp_gbs, "frac": spmvmp_frac,
                                "launches_timed": prof_mixed["spmv_n"]},

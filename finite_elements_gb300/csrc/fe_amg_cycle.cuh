@@ -6,6 +6,8 @@
 //
 // An executor provides, beside what fe_amg_passes.cuh lists:
 //   template <class T> int fill_zero(T *p, size_t n);
+//   void mark(int k);   // timing marks: 0 / 1 around level 0's pre-smoothing, 2 / 3 around
+//                       // the whole cycle (the device records events; the host ignores them)
 #pragma once
 
 #include <algorithm>
@@ -111,7 +113,9 @@ int vcycle(Ex &ex, const std::vector<CycleLevel> &levels, const CycleCoarse &C, 
     const CycleLevel &L = levels[l];
     float *rc = l + 1 < levels.size() ? levels[l + 1].r : C.r;
     float *xc = l + 1 < levels.size() ? levels[l + 1].x : C.x;
+    if (l == 0) ex.mark(0);
     FE_CHECK(chebyshev_cycle(ex, L, k, false));
+    if (l == 0) ex.mark(1);
     FE_CHECK(ex.rows(L.n, PassResidual32{L.aptr, L.acol, L.a, L.d, L.r, L.x, L.t}));
     FE_CHECK(ex.rows(L.nc, PassRestrict32{L.tptr, L.tcol, L.pt, L.m, L.d, L.t, rc}));
     FE_CHECK(vcycle(ex, levels, C, l + 1, k));
@@ -125,9 +129,12 @@ int precondition(Ex &ex, const std::vector<CycleLevel> &levels, const CycleCoars
                  double *z) {
     const CycleLevel &L0 = levels[0];
     const int64_t nd = L0.n * L0.d;
+    ex.mark(2);
     FE_CHECK(ex.rows(nd, PassToF32{r, L0.r}));
     FE_CHECK(vcycle(ex, levels, C, 0, k));
-    return ex.rows(nd, PassToF64{L0.x, z});
+    FE_CHECK(ex.rows(nd, PassToF64{L0.x, z}));
+    ex.mark(3);
+    return FE_OK;
 }
 
 }  // namespace amg

@@ -215,6 +215,10 @@ struct CycleEx {
     DBuf<double> part, sc;
     // lanes per row of each matrix the cycle multiplies, keyed by its row pointer
     std::vector<std::pair<const int64_t *, int>> lanes;
+    cudaEvent_t *marks = nullptr;   // events of the timing marks while profiling
+    void mark(int k) {
+        if (marks) cudaEventRecordWithFlags(marks[k], h->stream, cudaEventRecordExternal);
+    }
     ~CycleEx() { dfree(part), dfree(sc); }
     int lanes_of(const int64_t *ptr) const {
         for (const auto &p : lanes)
@@ -358,6 +362,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     const int64_t n = h->n_nodes, nd = h->n_dof;
     FE_CUDA(cudaEventRecord(h->events[6], s));
     // the hierarchy, set up on the device, and the cycle's vectors
+    const bool prof = h->w.prof && h->w.pev[0];
     DevAmg G;
     // down to at most 3000 DOFs (an eighth of small systems): below that the aggregates of
     // the plane-strain family stop shrinking while the coarse operators fill in (4M DOF:
@@ -399,6 +404,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     amg::CycleCoarse coarse;
     coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
     CycleEx cex{h};
+    if (prof) cex.marks = h->w.pev;
     for (const DevLevel &Dl : G.L) {
         const double n_rows = (double)std::max<int64_t>(Dl.A.n, 1), n_aggr = (double)std::max<int64_t>(Dl.PT.n, 1);
         cex.lanes.push_back({Dl.A.ptr.p, lanes_for((double)Dl.A.nnzb / n_rows)});
@@ -439,9 +445,26 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         per_cycle = h->launches - l0;
         h->launches = l0;
     }
+    if (prof) {
+        // the setup: from the solve's start to here
+        FE_CUDA(cudaEventRecord(h->events[7], s));
+        FE_CUDA(cudaEventSynchronize(h->events[7]));
+        float a = 0.f;
+        FE_CUDA(cudaEventElapsedTime(&a, h->events[6], h->events[7]));
+        h->w.mg_ms[1] += a, h->w.mg_n[1] += 1;
+    }
+    const int64_t smooth_launches = 3;   // Chebyshev steps of level 0's pre-smoothing
     auto precond = [&]() -> int {
         FE_CUDA(cudaGraphLaunch(cycle, s));
         h->launches += per_cycle;
+        if (prof) {
+            FE_CUDA(cudaEventSynchronize(h->w.pev[3]));
+            float a = 0.f, c = 0.f;
+            if (cudaEventElapsedTime(&a, h->w.pev[0], h->w.pev[1]) == cudaSuccess)
+                h->w.mg_ms[0] += a, h->w.mg_n[0] += smooth_launches;
+            if (cudaEventElapsedTime(&c, h->w.pev[2], h->w.pev[3]) == cudaSuccess)
+                h->w.mg_ms[2] += c, h->w.mg_n[2] += 1;
+        }
         return FE_OK;
     };
     const double tol = o->tol > 0 ? o->tol : 1e-10;

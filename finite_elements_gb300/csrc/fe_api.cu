@@ -511,4 +511,16 @@ int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *ch
     return FE_OK;
 }
 
+int fe_profile_read_multigrid(fe_handle h, double *smooth_ms, int64_t *smooth_n, double *setup_ms, int64_t *setups,
+                              double *cycle_ms, int64_t *cycles) {
+    FE_HANDLE_CHECK(h);
+    if (smooth_ms) *smooth_ms = h->w.mg_ms[0];
+    if (smooth_n) *smooth_n = h->w.mg_n[0];
+    if (setup_ms) *setup_ms = h->w.mg_ms[1];
+    if (setups) *setups = h->w.mg_n[1];
+    if (cycle_ms) *cycle_ms = h->w.mg_ms[2];
+    if (cycles) *cycles = h->w.mg_n[2];
+    return FE_OK;
+}
+
 }  // extern "C"

@@ -141,6 +141,11 @@ struct SolverWork {
     bool prof = false;
     cudaEvent_t pev[4] = {nullptr, nullptr, nullptr, nullptr};
     double prof_ms[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+    // The multigrid solve's times while profiling: [0] level 0's pre-smoothing (ms, its
+    // Chebyshev launches), [1] the device setup of the hierarchy (ms, solves), [2] the
+    // whole V-cycle (ms, cycles)
+    double mg_ms[3] = {0.0, 0.0, 0.0};
+    int64_t mg_n[3] = {0, 0, 0};
     int64_t prof_n[3][2] = {{0, 0}, {0, 0}, {0, 0}};
 };
 

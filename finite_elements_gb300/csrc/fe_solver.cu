@@ -1639,6 +1639,7 @@ int profile_kernels(fe_handle_s *h, int enable) {
     w.prof = enable != 0;
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 2; ++b) w.prof_ms[a][b] = 0.0, w.prof_n[a][b] = 0;
+    for (int a = 0; a < 3; ++a) w.mg_ms[a] = 0.0, w.mg_n[a] = 0;
     return FE_OK;
 }
 

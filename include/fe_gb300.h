@@ -241,6 +241,12 @@ int fe_sell_info(fe_handle h, int64_t *n_entries, int32_t *col16);
 int fe_profile_kernels(fe_handle h, int32_t enable);
 int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *cheb_n, double *spmv_ms,
                     int64_t *spmv_n);
+/* The multigrid solve's times summed since fe_profile_kernels(h, 1): level 0's
+ * pre-smoothing in the V-cycle (ms, and its Chebyshev launches), the device setup of the
+ * hierarchy (ms, solves) and the whole V-cycle (ms, cycles); events recorded inside the
+ * captured cycle and read after each of its launches. */
+int fe_profile_read_multigrid(fe_handle h, double *smooth_ms, int64_t *smooth_n, double *setup_ms, int64_t *setups,
+                              double *cycle_ms, int64_t *cycles);
 
 /* ---- modal analysis (analysis.py:741-796 modal_analysis: scipy eigsh/eigs on
  * k_matrix_sparse and m_matrix_sparse, i.e. K and M without Dirichlet conditions).
