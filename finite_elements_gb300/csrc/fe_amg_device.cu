@@ -477,16 +477,26 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     FE_CHECK(solve_start_point(h, o, h->w.x.p, &x0_used));
     const amg::PcgVectors v{h->w.x.p, r.p, p.p, q.p, z.p};
     // PCG from x; when the recurrence met tol but the FP64 true residual did not (the
-    // recurrence drifts from b - A x by about eps cond(A)), restart from the true residual
+    // recurrence drifts from b - A x by about eps cond(A)), restart from the true residual;
+    // a restart that gains less than 2x marks the rounding floor (FE_OK with
+    // FE_SOLVE_ACCEPT_STAGNATION, else FE_MAXITER), as in the other solvers
+    double prev = INFINITY;
+    bool stagnated = false;
     for (;;) {
         int it = 0;
         FE_CHECK(amg::pcg(cex, n, D, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, h->b.p, v, precond, tol,
                           max_iter - total, &it, &relres, &status, true));
         total += it;
         if (status != FE_OK || relres <= tol || restarts >= max_restart || total >= max_iter) break;
+        if (relres > 0.5 * prev) {
+            stagnated = true;
+            break;
+        }
+        prev = relres;
         ++restarts;
     }
-    if (status == FE_OK && relres > tol && !(o->flags & FE_SOLVE_ACCEPT_STAGNATION)) status = FE_MAXITER;
+    if (status == FE_OK && relres > tol && !(stagnated && (o->flags & FE_SOLVE_ACCEPT_STAGNATION)))
+        status = FE_MAXITER;
     double bb = 0.0;
     FE_CHECK(cex.dot(h->b.p, h->b.p, nd, &bb));
     st->iterations = total;

@@ -296,9 +296,10 @@ int csr_to_host(const DevCsr &D, BlockCsr &H, cudaStream_t s) {
 // ---------------------------------------------------------------- coarsest inverse
 // Dense inverse of the coarsest matrix by Gauss-Jordan elimination without pivoting
 // (the matrix is symmetric positive definite once 1e-12 of its largest diagonal entry
-// is added, as the host version does), in place, one pivot k after the other:
-//   others:  a_ij -= a_ik a_kj / a_kk      (i != k, j != k)
-//   row k:   a_kj /= a_kk (j != k);  column k: a_ik = -a_ik / a_kk (i != k);  a_kk = 1 / a_kk
+// is added, as the host version does), in place, one pivot k after the other, every new
+// value from old ones:
+//   others:  a_ij - a_ik a_kj / a_kk      (i != k, j != k)
+//   row k:   a_kj / a_kk (j != k);  column k: -a_ik / a_kk (i != k);  pivot: 1 / a_kk
 
 constexpr int kMaxCoarse = 4096;   // DOFs of the coarsest level (a 128 MB inverse)
 
@@ -324,35 +325,50 @@ __global__ void kc_regularise(int64_t n, double *M) {
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M[i * n + i] += 1e-12 * t;
 }
 
-// All pivots in one cooperative launch: thread t owns the elements e = t, t + T, ... of
-// the row-major matrix; per pivot, the other elements are updated from the pivot row
-// and column (read through L2: their owners rewrite them), a grid barrier, then the
-// owners of the pivot row and column rescale them, and another barrier.  A zero or
-// non-finite pivot stops every block at the same step (*singular = 1).
-__global__ void __launch_bounds__(kST) kc_gauss_jordan(int64_t n, double *M, unsigned *bar, int *err,
+// All pivots in one cooperative launch, one grid barrier per pivot.  Warp w owns rows
+// w, w + W, ... and lane l the columns l, l + 32, ... of them, so every element has one
+// owner for the whole elimination.  Pivot k's new values come from old values only --
+// the element itself, a_ik, a_kj and a_kk -- and the old pivot row and column are read
+// from buffers (piv[k & 1]) that the owners filled while computing the previous pivot,
+// so a pivot's updates do not race with its readers; the owners of row and column k + 1
+// fill piv[(k + 1) & 1] on the way.  piv[b] holds the row (n values) then the column.
+// A zero or non-finite pivot stops every block at the same step (*singular = 1).
+__global__ void __launch_bounds__(kST) kc_gauss_jordan(int64_t n, double *M, double *piv, unsigned *bar, int *err,
                                                        int *singular) {
-    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
-    const int64_t nn = n * n;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t k = 0; k < n; ++k) {
-        const double p = __ldcg(M + k * n + k);
+        const double *row = piv + (k & 1) * 2 * n, *colv = row + n;
+        double *nrow = piv + ((k + 1) & 1) * 2 * n, *ncol = nrow + n;
+        const double p = __ldcg(row + k);
         if (p == 0.0 || !isfinite(p)) {
-            if (t0 == 0) *singular = 1;
+            if (w0 == 0 && lane == 0) *singular = 1;
             return;
         }
         const double ip = 1.0 / p;
-        for (int64_t e = t0; e < nn; e += nt) {
-            const int64_t i = e / n, j = e - i * n;
-            if (i == k || j == k) continue;
-            __stcg(M + e, fma(-__ldcg(M + i * n + k) * ip, __ldcg(M + k * n + j), __ldcg(M + e)));
+        for (int64_t i = w0; i < n; i += W) {
+            const double aik = __ldcg(colv + i);
+            for (int64_t j = lane; j < n; j += 32) {
+                const double akj = __ldcg(row + j);
+                double v;
+                if (i == k) v = j == k ? ip : akj * ip;
+                else if (j == k) v = -aik * ip;
+                else v = fma(-aik * ip, akj, M[i * n + j]);
+                M[i * n + j] = v;
+                if (i == k + 1) nrow[j] = v;
+                if (j == k + 1) ncol[i] = v;
+            }
         }
         if (!grid_sync_bounded(bar, err)) return;
-        for (int64_t e = t0; e < nn; e += nt) {
-            const int64_t i = e / n, j = e - i * n;
-            if (i == k && j == k) __stcg(M + e, ip);
-            else if (i == k) __stcg(M + e, __ldcg(M + e) * ip);
-            else if (j == k) __stcg(M + e, -__ldcg(M + e) * ip);
-        }
-        if (!grid_sync_bounded(bar, err)) return;
+    }
+}
+
+// piv[0] = row 0 and column 0 of M (the first pivot's)
+__global__ void kc_first_pivot(int64_t n, const double *__restrict__ M, double *__restrict__ piv) {
+    FE_ROWS(j, n) {
+        piv[j] = M[j];
+        piv[n + j] = M[j * n];
     }
 }
 
@@ -366,22 +382,26 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
     FE_CHECK(dalloc(G.cinv, (size_t)std::max<int64_t>(n * n, 1)));
     if (n == 0) return FE_OK;
     DBuf<int> flag;   // [0] singular, [1] [2] the grid barrier, [3] its error word
+    DBuf<double> piv;   // the pivot row and column, two generations
     FE_CHECK(dalloc(flag, 4));
+    FE_CHECK(dalloc(piv, (size_t)4 * n));
     struct Free {
         DBuf<int> &f;
-        ~Free() { dfree(f); }
-    } fr{flag};
+        DBuf<double> &p;
+        ~Free() { dfree(f), dfree(p); }
+    } fr{flag, piv};
     FE_CUDA(cudaMemsetAsync(flag.p, 0, 4 * sizeof(int), s));
     FE_CUDA(cudaMemsetAsync(G.cinv.p, 0, (size_t)n * n * sizeof(double), s));
     kc_dense_fill<<<grid_s(C.n), kST, 0, s>>>(C.n, C.rd, C.ptr.p, C.col.p, C.val.p, n, G.cinv.p);
     kc_regularise<<<1, kST, 0, s>>>(n, G.cinv.p);
+    kc_first_pivot<<<grid_s(n), kST, 0, s>>>(n, G.cinv.p, piv.p);
     FE_LAUNCH_CHECK();
     // the cooperative grid: every SM's resident blocks of the kernel
     int dev = 0, sms = 0, per_sm = 0;
     FE_CUDA(cudaGetDevice(&dev));
     FE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)kc_gauss_jordan, kST, 0));
-    const int64_t want = (n * n + kST - 1) / kST;
+    const int64_t want = (n + kST / 32 - 1) / (kST / 32);   // a warp per row
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1)));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -392,7 +412,8 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    FE_CUDA(cudaLaunchKernelEx(&cfg, kc_gauss_jordan, n, G.cinv.p, (unsigned *)(flag.p + 1), flag.p + 3, flag.p));
+    FE_CUDA(cudaLaunchKernelEx(&cfg, kc_gauss_jordan, n, G.cinv.p, piv.p, (unsigned *)(flag.p + 1), flag.p + 3,
+                               flag.p));
     int host[4] = {0, 0, 0, 0};
     FE_CUDA(cudaMemcpyAsync(host, flag.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
