@@ -190,6 +190,312 @@ int launch_dinv_product(int64_t n, const amg::PassDinvProduct &f, cudaStream_t s
     return FE_OK;
 }
 
+// ---------------------------------------------------------------- sparse products, a warp per row
+// Rows of C = A B whose product lists are long (the Galerkin products and the coarser
+// levels) get a warp each instead of a thread: the candidates are gathered into shared
+// memory by the 32 lanes, bitonic-sorted there and compacted; the values are summed per
+// output entry in the order of the factors' entries (the order of the thread-per-row
+// version), each lane owning the output entries p = lane, lane + 32, ... after a stable
+// counting sort of the product terms by output entry.  Rows beyond the shared-memory
+// capacity fall back to the row operation of one lane.
+
+constexpr int kPW = 2;          // warps per block of the warp-per-row product kernels
+constexpr int kColCap = 4096;   // candidates a warp sorts in shared memory
+constexpr int kTermCap = 1024;  // product terms (and output entries) a warp orders in shared memory
+
+// ascending bitonic sort of a[0..m), m a power of two, by the lanes of a warp
+__device__ void warp_bitonic(int32_t *a, int m) {
+    const int lane = threadIdx.x & 31;
+    for (int k = 2; k <= m; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < m; i += 32) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const int32_t x = a[i], y = a[l];
+                    if ((x > y) == ((i & k) == 0)) a[i] = y, a[l] = x;
+                }
+            }
+            __syncwarp();
+        }
+}
+
+__global__ void __launch_bounds__(kPW * 32) kd_prod_cols_warp(int64_t n, amg::PassProdCols f) {
+    __shared__ int32_t sh[kPW][kColCap];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    int32_t *a = sh[wl];
+    const int64_t W = (int64_t)gridDim.x * kPW;
+    for (int64_t i = (int64_t)blockIdx.x * kPW + wl; i < n; i += W) {
+        const int64_t bound = f.boff[i + 1] - f.boff[i];
+        int32_t *out = f.cand + f.boff[i];
+        if (bound > kColCap) continue;   // kd_prod_cols_long's row
+        int m = 1;
+        while (m < bound) m <<= 1;
+        int64_t base = 0;
+        for (int64_t s = f.aptr[i]; s < f.aptr[i + 1]; ++s) {
+            const int32_t c = f.acol[s];
+            const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
+            for (int64_t t = lane; t < len; t += 32) a[base + t] = f.bcol[t0 + t];
+            base += len;
+        }
+        for (int64_t t = bound + lane; t < m; t += 32) a[t] = 0x7fffffff;
+        __syncwarp();
+        warp_bitonic(a, m);
+        int64_t run = 0;
+        for (int64_t t0 = 0; t0 < bound; t0 += 32) {
+            const int64_t t = t0 + lane;
+            const bool keep = t < bound && (t == 0 || a[t] != a[t - 1]);
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            if (keep) out[run + __popc(mask & ((1u << lane) - 1u))] = a[t];
+            run += __popc(mask);
+        }
+        if (lane == 0) f.cnt[i] = run;
+        __syncwarp();
+    }
+}
+
+// C row i's values; RA x CA times CA x CB blocks (0: the sizes of f at run time)
+template <int RA, int CA, int CB>
+__global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::PassProdVals f) {
+    __shared__ int32_t s_pos[kPW][kTermCap], s_ord[kPW][kTermCap], s_s[kPW][kTermCap], s_t[kPW][kTermCap];
+    __shared__ int32_t s_cnt[kPW][kTermCap], s_off[kPW][kTermCap];
+    const int ra = RA ? RA : f.ra, ca = CA ? CA : f.ca, cb = CB ? CB : f.cb;
+    const int bs = ra * cb;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    int32_t *pos = s_pos[wl], *ord = s_ord[wl], *ss = s_s[wl], *ts = s_t[wl], *cnt = s_cnt[wl], *off = s_off[wl];
+    const int64_t W = (int64_t)gridDim.x * kPW;
+    for (int64_t i = (int64_t)blockIdx.x * kPW + wl; i < n; i += W) {
+        const int64_t T = f.boff[i + 1] - f.boff[i];
+        const int64_t c0 = f.cptr[i], lc = f.cptr[i + 1] - c0;
+        if (T > kTermCap || lc > kTermCap) continue;   // kd_prod_vals_long's row
+        // the terms in factor order, with their output entries
+        for (int64_t p = lane; p < lc; p += 32) cnt[p] = 0;
+        int64_t base = 0;
+        for (int64_t s = f.aptr[i]; s < f.aptr[i + 1]; ++s) {
+            const int32_t c = f.acol[s];
+            const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
+            for (int64_t t = lane; t < len; t += 32) {
+                const int64_t p = amg::find_sorted(f.ccol, c0, c0 + lc, f.bcol[t0 + t]);
+                pos[base + t] = p < 0 ? -1 : (int32_t)(p - c0);
+                ss[base + t] = (int32_t)s;
+                ts[base + t] = (int32_t)(t0 + t);
+            }
+            base += len;
+        }
+        __syncwarp();
+        for (int64_t t = lane; t < T; t += 32)
+            if (pos[t] >= 0) atomicAdd(&cnt[pos[t]], 1);
+        __syncwarp();
+        // exclusive scan of the counts into off
+        int carry = 0;
+        for (int64_t p0 = 0; p0 < lc; p0 += 32) {
+            const int64_t p = p0 + lane;
+            const int v = p < lc ? cnt[p] : 0;
+            int x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (p < lc) off[p] = carry + x - v;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        // stable scatter of the term indices by output entry (off[p] ends at its range's end)
+        for (int64_t t0 = 0; t0 < T; t0 += 32) {
+            const int64_t t = t0 + lane;
+            const int p = t < T ? pos[t] : -1;
+            const int key = p >= 0 ? p : -1 - lane;   // lanes without a term match no one
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            if (p >= 0) ord[off[p] + __popc(peers & ((1u << lane) - 1u))] = (int32_t)t;
+            __syncwarp();
+            if (p >= 0 && lane == 31 - __clz(peers)) off[p] += __popc(peers);
+            __syncwarp();
+        }
+        // each lane sums its output entries' terms in order
+        for (int64_t p = lane; p < lc; p += 32) {
+            double acc[RA && CB ? RA * CB : 36];
+            for (int k = 0; k < bs; ++k) acc[k] = 0.0;
+            for (int q = off[p] - cnt[p]; q < off[p]; ++q) {
+                const int t = ord[q];
+                const double *a = f.aval + (int64_t)ss[t] * ra * ca;
+                const double *b = f.bval + (int64_t)ts[t] * ca * cb;
+                for (int x = 0; x < ra; ++x)
+                    for (int z = 0; z < cb; ++z) {
+                        double v = 0.0;
+                        for (int y = 0; y < ca; ++y) v += a[x * ca + y] * b[y * cb + z];
+                        acc[x * cb + z] += v;
+                    }
+            }
+            double *o = f.cval + (c0 + p) * bs;
+            for (int k = 0; k < bs; ++k) o[k] = acc[k];
+        }
+        __syncwarp();
+    }
+}
+
+// mean product terms per row at and above which the products take a warp per row
+constexpr double kWarpRowMean = 48.0;
+
+inline int warp_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kPW - 1) / kPW, 152 * 32)); }
+
+// Rows beyond the short kernels' capacity: one warp per block and the buffers in dynamic
+// shared memory, 16-bit where they fit -- up to kLongTerms candidates (product terms),
+// kLongOut output entries and kLongA entries of the row of A; beyond that the row
+// operation of one lane.
+constexpr int kLongTerms = 8192, kLongOut = 2048, kLongA = 512;
+constexpr size_t kLongColsSmem = kLongTerms * sizeof(int32_t);
+constexpr size_t kLongValsSmem = 2 * kLongTerms * sizeof(int16_t) + 2 * kLongOut * sizeof(int32_t) +
+                                 (kLongA + 1) * sizeof(int32_t);
+
+__global__ void __launch_bounds__(32) kd_prod_cols_long(int64_t n, amg::PassProdCols f) {
+    extern __shared__ int32_t a[];
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const int64_t bound = f.boff[i + 1] - f.boff[i];
+        if (bound <= kColCap) continue;   // the short kernel's row
+        int32_t *out = f.cand + f.boff[i];
+        if (bound > kLongTerms) {
+            if (lane == 0) f.cnt[i] = amg::row_product_columns(f.aptr, f.acol, f.bptr, f.bcol, i, out);
+            __syncwarp();
+            continue;
+        }
+        int m = 1;
+        while (m < bound) m <<= 1;
+        int64_t base = 0;
+        for (int64_t s = f.aptr[i]; s < f.aptr[i + 1]; ++s) {
+            const int32_t c = f.acol[s];
+            const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
+            for (int64_t t = lane; t < len; t += 32) a[base + t] = f.bcol[t0 + t];
+            base += len;
+        }
+        for (int64_t t = bound + lane; t < m; t += 32) a[t] = 0x7fffffff;
+        __syncwarp();
+        warp_bitonic(a, m);
+        int64_t run = 0;
+        for (int64_t t0 = 0; t0 < bound; t0 += 32) {
+            const int64_t t = t0 + lane;
+            const bool keep = t < bound && (t == 0 || a[t] != a[t - 1]);
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            if (keep) out[run + __popc(mask & ((1u << lane) - 1u))] = a[t];
+            run += __popc(mask);
+        }
+        if (lane == 0) f.cnt[i] = run;
+        __syncwarp();
+    }
+}
+
+template <int RA, int CA, int CB>
+__global__ void __launch_bounds__(32) kd_prod_vals_long(int64_t n, amg::PassProdVals f) {
+    extern __shared__ int32_t dsm[];
+    int32_t *cnt = dsm, *off = cnt + kLongOut, *aoff = off + kLongOut;
+    int16_t *pos = reinterpret_cast<int16_t *>(aoff + kLongA + 1), *ord = pos + kLongTerms;
+    const int ra = RA ? RA : f.ra, ca = CA ? CA : f.ca, cb = CB ? CB : f.cb;
+    const int bs = ra * cb;
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const int64_t T = f.boff[i + 1] - f.boff[i];
+        const int64_t c0 = f.cptr[i], lc = f.cptr[i + 1] - c0;
+        if (T <= kTermCap && lc <= kTermCap) continue;   // the short kernel's row
+        const int64_t a0 = f.aptr[i], la = f.aptr[i + 1] - a0;
+        if (T > kLongTerms || lc > kLongOut || la > kLongA) {
+            if (lane == 0)
+                amg::row_product_values(f.aptr, f.acol, f.aval, f.ra, f.ca, f.bptr, f.bcol, f.bval, f.cb, f.cptr,
+                                        f.ccol, f.cval, i);
+            __syncwarp();
+            continue;
+        }
+        // first term of each entry of A's row (a serial prefix over <= kLongA entries)
+        if (lane == 0) {
+            int32_t run = 0;
+            for (int64_t q = 0; q < la; ++q) {
+                aoff[q] = run;
+                const int32_t c = f.acol[a0 + q];
+                run += (int32_t)(f.bptr[c + 1] - f.bptr[c]);
+            }
+            aoff[la] = run;
+        }
+        for (int64_t p = lane; p < lc; p += 32) cnt[p] = 0;
+        __syncwarp();
+        for (int64_t q = 0; q < la; ++q) {
+            const int32_t c = f.acol[a0 + q];
+            const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
+            for (int64_t t = lane; t < len; t += 32) {
+                const int64_t p = amg::find_sorted(f.ccol, c0, c0 + lc, f.bcol[t0 + t]);
+                pos[aoff[q] + t] = p < 0 ? (int16_t)-1 : (int16_t)(p - c0);
+            }
+        }
+        __syncwarp();
+        for (int64_t t = lane; t < T; t += 32)
+            if (pos[t] >= 0) atomicAdd(&cnt[pos[t]], 1);
+        __syncwarp();
+        int carry = 0;
+        for (int64_t p0 = 0; p0 < lc; p0 += 32) {
+            const int64_t p = p0 + lane;
+            const int v = p < lc ? cnt[p] : 0;
+            int x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (p < lc) off[p] = carry + x - v;
+            carry += __shfl_sync(0xffffffffu, x, 31);
+        }
+        __syncwarp();
+        for (int64_t t0 = 0; t0 < T; t0 += 32) {
+            const int64_t t = t0 + lane;
+            const int p = t < T ? pos[t] : -1;
+            const int key = p >= 0 ? p : -1 - lane;
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            if (p >= 0) ord[off[p] + __popc(peers & ((1u << lane) - 1u))] = (int16_t)t;
+            __syncwarp();
+            if (p >= 0 && lane == 31 - __clz(peers)) off[p] += __popc(peers);
+            __syncwarp();
+        }
+        for (int64_t p = lane; p < lc; p += 32) {
+            double acc[RA && CB ? RA * CB : 36];
+            for (int k = 0; k < bs; ++k) acc[k] = 0.0;
+            for (int q = off[p] - cnt[p]; q < off[p]; ++q) {
+                const int t = ord[q];
+                // the entry of A's row the term belongs to: the last q' with aoff[q'] <= t
+                int lo = 0, hi = (int)la - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (aoff[mid] <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int64_t sidx = a0 + lo;
+                const int64_t tidx = f.bptr[f.acol[sidx]] + (t - aoff[lo]);
+                const double *a = f.aval + sidx * ra * ca;
+                const double *b = f.bval + tidx * ca * cb;
+                for (int x = 0; x < ra; ++x)
+                    for (int z = 0; z < cb; ++z) {
+                        double v = 0.0;
+                        for (int y = 0; y < ca; ++y) v += a[x * ca + y] * b[y * cb + z];
+                        acc[x * cb + z] += v;
+                    }
+            }
+            double *o = f.cval + (c0 + p) * bs;
+            for (int k = 0; k < bs; ++k) o[k] = acc[k];
+        }
+        __syncwarp();
+    }
+}
+
+template <int RA, int CA, int CB>
+int launch_prod_vals(int64_t n, const amg::PassProdVals &f, cudaStream_t s) {
+    kd_prod_vals_warp<RA, CA, CB><<<warp_grid(n), kPW * 32, 0, s>>>(n, f);
+    FE_LAUNCH_CHECK();
+    static_assert(kLongTerms <= 32767 && kLongOut <= 32767, "16-bit term and entry indices");
+    FE_CUDA(cudaFuncSetAttribute(kd_prod_vals_long<RA, CA, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kLongValsSmem));
+    kd_prod_vals_long<RA, CA, CB><<<(int)std::max<int64_t>(1, std::min<int64_t>(n, 152 * 16)), 32, kLongValsSmem, s>>>(
+        n, f);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+
 struct DevEx {
     cudaStream_t s;
     DBuf<int64_t> scan_tmp;
@@ -231,6 +537,38 @@ struct DevEx {
                 FE_LAUNCH_CHECK();
                 return FE_OK;
         }
+    }
+    // the sparse products: a warp per row where rows are long, else row by row
+    int rows(int64_t n, const amg::PassProdCols &f) {
+        if (n <= 0) return FE_OK;
+        if ((double)f.total < kWarpRowMean * (double)n) {
+            k_rows<amg::PassProdCols><<<grid_s(n), kST, 0, s>>>(n, f);
+        } else {
+            kd_prod_cols_warp<<<warp_grid(n), kPW * 32, 0, s>>>(n, f);
+            FE_LAUNCH_CHECK();
+            FE_CUDA(cudaFuncSetAttribute(kd_prod_cols_long, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kLongColsSmem));
+            kd_prod_cols_long<<<(int)std::max<int64_t>(1, std::min<int64_t>(n, 152 * 16)), 32, kLongColsSmem, s>>>(
+                n, f);
+        }
+        FE_LAUNCH_CHECK();
+        return FE_OK;
+    }
+    int rows(int64_t n, const amg::PassProdVals &f) {
+        if (n <= 0) return FE_OK;
+        if (!f.boff || (double)f.total < kWarpRowMean * (double)n) {
+            k_rows<amg::PassProdVals><<<grid_s(n), kST, 0, s>>>(n, f);
+        } else if (f.ra == 2 && f.ca == 2 && f.cb == 3) {
+            return launch_prod_vals<2, 2, 3>(n, f, s);
+        } else if (f.ra == 3 && f.ca == 2 && f.cb == 3) {
+            return launch_prod_vals<3, 2, 3>(n, f, s);
+        } else if (f.ra == 3 && f.ca == 3 && f.cb == 3) {
+            return launch_prod_vals<3, 3, 3>(n, f, s);
+        } else {
+            return launch_prod_vals<0, 0, 0>(n, f, s);
+        }
+        FE_LAUNCH_CHECK();
+        return FE_OK;
     }
     int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) { return scan64(in, n, out, total, scan_tmp, s); }
     int dot(const double *a, const double *b, int64_t n, double *out) {
@@ -325,37 +663,39 @@ __global__ void kc_regularise(int64_t n, double *M) {
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M[i * n + i] += 1e-12 * t;
 }
 
-// All pivots in one cooperative launch, one grid barrier per pivot.  Warp w owns rows
-// w, w + W, ... and lane l the columns l, l + 32, ... of them, so every element has one
-// owner for the whole elimination.  Pivot k's new values come from old values only --
-// the element itself, a_ik, a_kj and a_kk -- and the old pivot row and column are read
-// from buffers (piv[k & 1]) that the owners filled while computing the previous pivot,
-// so a pivot's updates do not race with its readers; the owners of row and column k + 1
-// fill piv[(k + 1) & 1] on the way.  piv[b] holds the row (n values) then the column.
-// A zero or non-finite pivot stops every block at the same step (*singular = 1).
+// All pivots in one cooperative launch, one grid barrier per pivot.  Block b owns rows
+// b, b + B, ... and its threads the columns of them, so every element has one owner for
+// the whole elimination.  Pivot k's new values come from old values only -- the element
+// itself, a_ik, a_kj and a_kk -- and the old pivot row and column are read from buffers
+// (piv[k & 1]) that the owners filled while computing the previous pivot, so a pivot's
+// updates do not race with its readers; the owners of row and column k + 1 fill
+// piv[(k + 1) & 1] on the way.  piv[b] holds the row (n values) then the column.  Each
+// block stages the pivot row in shared memory.  A zero or non-finite pivot stops every
+// block at the same step (*singular = 1).
 __global__ void __launch_bounds__(kST) kc_gauss_jordan(int64_t n, double *M, double *piv, unsigned *bar, int *err,
                                                        int *singular) {
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    __shared__ double srow[kMaxCoarse];
     for (int64_t k = 0; k < n; ++k) {
         const double *row = piv + (k & 1) * 2 * n, *colv = row + n;
         double *nrow = piv + ((k + 1) & 1) * 2 * n, *ncol = nrow + n;
-        const double p = __ldcg(row + k);
+        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) srow[j] = __ldcg(row + j);
+        __syncthreads();
+        const double p = srow[k];
         if (p == 0.0 || !isfinite(p)) {
-            if (w0 == 0 && lane == 0) *singular = 1;
+            if (blockIdx.x == 0 && threadIdx.x == 0) *singular = 1;
             return;
         }
         const double ip = 1.0 / p;
-        for (int64_t i = w0; i < n; i += W) {
-            const double aik = __ldcg(colv + i);
-            for (int64_t j = lane; j < n; j += 32) {
-                const double akj = __ldcg(row + j);
+        for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+            const double f = -__ldcg(colv + i) * ip;
+            double *Mi = M + i * n;
+#pragma unroll 4
+            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
                 double v;
-                if (i == k) v = j == k ? ip : akj * ip;
-                else if (j == k) v = -aik * ip;
-                else v = fma(-aik * ip, akj, M[i * n + j]);
-                M[i * n + j] = v;
+                if (i == k) v = j == k ? ip : srow[j] * ip;
+                else if (j == k) v = f;
+                else v = fma(f, srow[j], Mi[j]);
+                Mi[j] = v;
                 if (i == k + 1) nrow[j] = v;
                 if (j == k + 1) ncol[i] = v;
             }
@@ -401,7 +741,9 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
     FE_CUDA(cudaGetDevice(&dev));
     FE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)kc_gauss_jordan, kST, 0));
-    const int64_t want = (n + kST / 32 - 1) / (kST / 32);   // a warp per row
+    // two blocks per SM: the pivot's FP64 work is spread over every SM, and a barrier
+    // with fewer arrivals ends sooner
+    const int64_t want = std::min<int64_t>(n, (int64_t)sms * 2);
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1)));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);

@@ -157,6 +157,7 @@ struct PassMemberBound {
 struct PassMembers {
     const int64_t *ptr; const int32_t *col; const int32_t *roots; const int32_t *agg; const int64_t *boff;
     int32_t *cand; int64_t *cnt;
+    int64_t total = 0;   // the bounds' sum (set by distinct_rows)
     FE_HD void operator()(int64_t c) const { cnt[c] = agg_members(ptr, col, roots, agg, c, cand + boff[c]); }
 };
 
@@ -184,15 +185,22 @@ struct PassProdBound {
     FE_HD void operator()(int64_t i) const { bound[i] = row_product_bound(aptr, acol, bptr, i); }
 };
 
+// total: the bounds' sum (set by distinct_rows); a device executor picks a warp per
+// row when rows are long
 struct PassProdCols {
     const int64_t *aptr; const int32_t *acol; const int64_t *bptr; const int32_t *bcol; const int64_t *boff;
     int32_t *cand; int64_t *cnt;
+    int64_t total = 0;
     FE_HD void operator()(int64_t i) const { cnt[i] = row_product_columns(aptr, acol, bptr, bcol, i, cand + boff[i]); }
 };
 
+// boff / total: the row offsets and the sum of the rows' product counts (PassProdBound),
+// for a device executor that gives long rows a warp each
 struct PassProdVals {
     const int64_t *aptr; const int32_t *acol; const double *aval; int ra; int ca; const int64_t *bptr;
     const int32_t *bcol; const double *bval; int cb; const int64_t *cptr; const int32_t *ccol; double *cval;
+    const int64_t *boff = nullptr;
+    int64_t total = 0;
     FE_HD void operator()(int64_t i) const {
         row_product_values(aptr, acol, aval, ra, ca, bptr, bcol, bval, cb, cptr, ccol, cval, i);
     }
@@ -212,6 +220,7 @@ struct PassRestrBound {
 struct PassRestrCols {
     const int64_t *mptr; const int32_t *mem; const int64_t *aptr; const int32_t *acol; const int64_t *boff;
     int32_t *cand; int64_t *cnt;
+    int64_t total = 0;   // the bounds' sum (set by distinct_rows)
     FE_HD void operator()(int64_t c) const { cnt[c] = row_restriction_columns(mptr, mem, aptr, acol, c, cand + boff[c]); }
 };
 
@@ -235,7 +244,7 @@ struct Work {
 // Rows whose entries are sorted distinct candidates: bound pass, scan, candidate pass
 // (count per row), scan into C.ptr, pack into C.col.
 template <class Ex, class Bound, class Cols>
-int distinct_rows(Ex &ex, int64_t n, Bound bound, Cols cols, Csr &C, Work<Ex> &W) {
+int distinct_rows(Ex &ex, int64_t n, Bound bound, Cols cols, Csr &C, Work<Ex> &W, int64_t *total_out = nullptr) {
     FE_CHECK(ex.alloc(W.bound, (size_t)std::max<int64_t>(n, 1)));
     FE_CHECK(ex.alloc(W.boff, (size_t)n + 1));
     FE_CHECK(ex.alloc(W.cnt, (size_t)std::max<int64_t>(n, 1)));
@@ -244,7 +253,8 @@ int distinct_rows(Ex &ex, int64_t n, Bound bound, Cols cols, Csr &C, Work<Ex> &W
     int64_t total = 0;
     FE_CHECK(ex.scan(W.bound.p, n, W.boff.p, &total));
     FE_CHECK(ex.alloc(W.cand, (size_t)std::max<int64_t>(total, 1)));
-    cols.boff = W.boff.p, cols.cand = W.cand.p, cols.cnt = W.cnt.p;
+    cols.boff = W.boff.p, cols.cand = W.cand.p, cols.cnt = W.cnt.p, cols.total = total;
+    if (total_out) *total_out = total;
     FE_CHECK(ex.rows(n, cols));
     FE_CHECK(ex.alloc(C.ptr, (size_t)n + 1));
     int64_t nnzb = 0;
@@ -259,11 +269,14 @@ int distinct_rows(Ex &ex, int64_t n, Bound bound, Cols cols, Csr &C, Work<Ex> &W
 template <class Ex>
 int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W) {
     C.n = A.n, C.rd = A.rd, C.cd = B.cd;
+    int64_t total = 0;
     FE_CHECK(distinct_rows(ex, A.n, PassProdBound{A.ptr.p, A.col.p, B.ptr.p, nullptr},
-                           PassProdCols{A.ptr.p, A.col.p, B.ptr.p, B.col.p, nullptr, nullptr, nullptr}, C, W));
+                           PassProdCols{A.ptr.p, A.col.p, B.ptr.p, B.col.p, nullptr, nullptr, nullptr}, C, W, &total));
     FE_CHECK(ex.alloc(C.val, (size_t)std::max<int64_t>(C.nnzb * C.rd * C.cd, 1)));
-    FE_CHECK(ex.rows(A.n, PassProdVals{A.ptr.p, A.col.p, A.val.p, A.rd, A.cd, B.ptr.p, B.col.p, B.val.p, B.cd,
-                                       C.ptr.p, C.col.p, C.val.p}));
+    PassProdVals vals{A.ptr.p, A.col.p, A.val.p, A.rd, A.cd, B.ptr.p, B.col.p, B.val.p, B.cd,
+                      C.ptr.p, C.col.p, C.val.p};
+    vals.boff = W.boff.p, vals.total = total;
+    FE_CHECK(ex.rows(A.n, vals));
     return FE_OK;
 }
 
