@@ -81,15 +81,6 @@ __device__ __forceinline__ void lanes_product(const int64_t *__restrict__ ptr, c
     for (int a = 0; a < RD; ++a) acc[a] = 0.0f;
     if (valid) {
         const int64_t s1 = ptr[i + 1];
-        if constexpr (RD == 2 && CD == 2) {
-            // 2 x 2 blocks: one 16-byte load each, and the 8-byte node vector
-            for (int64_t s = ptr[i] + sub; s < s1; s += G) {
-                const float4 b = __ldg(reinterpret_cast<const float4 *>(val) + s);
-                const float2 xv = reinterpret_cast<const float2 *>(x)[__ldg(col + s)];
-                acc[0] = fmaf(b.x, xv.x, fmaf(b.y, xv.y, acc[0]));
-                acc[1] = fmaf(b.z, xv.x, fmaf(b.w, xv.y, acc[1]));
-            }
-        } else
         for (int64_t s = ptr[i] + sub; s < s1; s += G) {
             const float *b = val + s * RD * CD;
             const float *xc = x + (int64_t)__ldg(col + s) * CD;

@@ -741,9 +741,9 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
     FE_CUDA(cudaGetDevice(&dev));
     FE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)kc_gauss_jordan, kST, 0));
-    // two blocks per SM: the pivot's FP64 work is spread over every SM, and a barrier
-    // with fewer arrivals ends sooner
-    const int64_t want = std::min<int64_t>(n, (int64_t)sms * 2);
+    // a block per row (as many as fit): measured 40 ms for the 1941-DOF coarsest level of
+    // the 4M-DOF benchmark system, against 66 ms on two blocks per SM
+    const int64_t want = n;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1)));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);

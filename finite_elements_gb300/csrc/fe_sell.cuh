@@ -208,7 +208,7 @@ __device__ __forceinline__ NodeVec<D, T> sell_row(int64_t r, bool valid, const S
     // FP32: four entries per trip, their column loads and then their gathers all in
     // flight before the first product (entries past w read the row itself and add
     // 0).  FP64 is bound by the FP64 FMA rate and runs one entry per trip.
-    constexpr int U = sizeof(T) == 4 ? 4 : 1;
+    constexpr int U = sizeof(T) == 4 ? (D == 3 ? 2 : 4) : 1;
     for (int k = 0; k < w; k += U) {
         int c[U];
 #pragma unroll

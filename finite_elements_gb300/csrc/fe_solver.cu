@@ -206,13 +206,8 @@ __device__ __forceinline__ NodeVec<D, T> row_product(int64_t r, bool valid, cons
 // ptxas's default (for FP64 40-48 registers; a floor of 1 makes it spend ~120 and
 // lose the occupancy, 5 makes the Chebyshev step spill).
 template <int D, typename T>
-constexpr int kSellBlocks = (sizeof(T) == 4 && D <= 2) ? 8 : 0;
+constexpr int kSellBlocks = (sizeof(T) == 4 && D <= 3) ? 8 : 0;
 
-// The PCG SpMV's resident blocks: as kSellBlocks, and 6 for FP64 2x2 blocks (40
-// registers instead of 48): the kernel is bound by the FP64 pipe, and more resident
-// warps keep that pipe fed.
-template <int D, typename T>
-constexpr int kPcgSpmvBlocks = (sizeof(T) == 8 && D == 2) ? 6 : kSellBlocks<D, T>;
 
 // Rows of the SELL copy handled by this thread (grid-stride in whole warps, so a
 // warp always covers one slice).
@@ -274,7 +269,7 @@ k_residual(int64_t n_nodes, const int32_t *__restrict__ ptr, const int32_t *__re
 
 // q = A p and p.q; the last block sets alpha = r.z / p.q or stops the loop.
 template <int D, typename T, bool C16 = false>
-__global__ void __launch_bounds__(kVecThreads, kPcgSpmvBlocks<D, T>)
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<D, T>)
 k_pcg_spmv(int64_t n_nodes, Sell A, const T *__restrict__ val, const T *__restrict__ diag,
            const T *__restrict__ dscale, const T *__restrict__ p, T *__restrict__ q, double *partials,
            PcgScalars *sc) {
