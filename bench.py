@@ -64,6 +64,8 @@ def parse_args():
                     help="with --quick: time the plain FP64 PCG step instead of the headline")
     ap.add_argument("--quick-multigrid", action="store_true",
                     help="--quick with --solver multigrid")
+    ap.add_argument("--profile", action="store_true",
+                    help="with --quick: keep the live kernel and setup-phase timing on and report it")
     ap.add_argument("--solver", choices=("multigrid", "chebyshev"), default="multigrid",
                     help="preconditioner of the headline mixed-precision solve: the FP32 smoothed-aggregation "
                          "V-cycle (set up on the device every step) or node-block Jacobi + Chebyshev in FP32")
@@ -288,7 +290,8 @@ def run_ours(args, dist):
 
     # event records around the first iteration of every chunk of the captured PCG
     # loop time the kernels inside the measured solves (not in profiler runs)
-    h.call("fe_profile_kernels", 0 if args.quick else 1)
+    live_prof = 0 if (args.quick and not args.profile) else 1
+    h.call("fe_profile_kernels", live_prof)
     for _ in range(args.warmup):
         device_step(mode, learned=True)
 
@@ -296,7 +299,7 @@ def run_ours(args, dist):
     clocks = ClockSampler(dist.local_rank)
     dist.barrier()
     h.call("fe_synchronize")
-    h.call("fe_profile_kernels", 0 if args.quick else 1)   # reset the kernel-time sums
+    h.call("fe_profile_kernels", live_prof)   # reset the kernel-time sums
     l0 = launches()
     clocks.start()
     h.call("fe_event_record", 0)
@@ -313,9 +316,12 @@ def run_ours(args, dist):
         v = [ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(),
              ctypes.c_int64()]
         h.call("fe_profile_read_multigrid", *[ctypes.byref(x) for x in v])
+        ph = (ctypes.c_double * _lib.FE_MG_PHASES)()
+        h.call("fe_profile_read_multigrid_phases", ph, _lib.FE_MG_PHASES)
         mg_prof = {"smooth_us": 1e3 * v[0].value / max(v[1].value, 1), "smooth_n": v[1].value,
                    "setup_ms": v[2].value / max(v[3].value, 1), "cycle_ms": v[4].value / max(v[5].value, 1),
-                   "cycles": v[5].value}
+                   "cycles": v[5].value,
+                   "setup_phases_ms": {name: ph[k] / max(v[3].value, 1) for k, name in enumerate(_lib.MG_PHASE_NAMES)}}
     dist.barrier()
     t_total = dist.max(ms.value / 1e3)
     value = t_total / (args.steps * dist.world)
@@ -326,7 +332,7 @@ def run_ours(args, dist):
         return {"metric": METRIC, "value": value, "unit": UNIT, "quick": True, "solver": args.solver,
                 "iterations": stats[-1].iterations, "relres": stats[-1].relres, "solve_ms": stats[-1].solve_ms,
                 "assemble_ms": stats[-1].assemble_ms, "learned_x0_used": stats[-1].x0_used,
-                "gpu_launches": int(n_launch)}
+                "gpu_launches": int(n_launch), "multigrid_profile": mg_prof if args.profile else None}
 
     # ---- mixed precision without the learned warm start, same step
     h.call("fe_synchronize")
@@ -413,12 +419,12 @@ def run_ours(args, dist):
         gbs = bytes_ / (us * 1e-6) / 1e9 if us > 0 else None
         return gbs, (gbs / hbm_peak if gbs else None)
 
-    # the V-cycle's level-0 Chebyshev step (ka_cheb<2,4>): FP32 2x2 blocks of the whole
-    # eliminated K (16 B) and their int32 columns, int64 row pointers, and per node the
-    # FP32 block-Jacobi inverse (16 B), r, z_k and z_k+1 (8 B each) and the direction
-    # (written by the first of the three steps, read and written by the other two)
+    # the V-cycle's level-0 Chebyshev step: k_cheb_step on the prescaled FP32 SELL copy of
+    # the eliminated K, as in the Chebyshev solve's steps, with D^-1 r, z_k read and z_k+1
+    # written; the old iterate z_k-1 is read by the second of the two timed launches only
+    # (the first one's is zero)
     def smooth_bytes():
-        return nnzb * 20 + (n_nodes + 1) * 8 + n_nodes * (16 + 3 * 8) + n_nodes * (8 + 16 + 16) / 3
+        return cheb_bytes(4) - n_nodes * 2 * 4 / 2
 
     cheb_gbs, cheb_frac = roof(cheb_bytes(4), prof_mixed["cheb_us"])
     spmvmp_gbs, spmvmp_frac = roof(spmv_bytes(8), prof_mixed["spmv_us"])
@@ -439,16 +445,18 @@ def run_ours(args, dist):
     if mg_prof is not None:
         sm_gbs, sm_frac = roof(smooth_bytes(), mg_prof["smooth_us"])
         roofline = {"bound": "hbm",
-                    "kernel": "ka_cheb<2,4> (level-0 Chebyshev smoothing step of the FP32 V-cycle, 4 lanes per "
-                              "block row; 6 of the cycle's launches at level 0)",
+                    "kernel": "k_cheb_step<2,float,float,0,*,1> (level-0 Chebyshev smoothing step of the FP32 "
+                              "V-cycle on the prescaled FP32 SELL copy; 5 of the cycle's launches)",
                     "achieved": sm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": sm_frac, "peak_source": peak_src,
                     "traffic": None, "bytes_per_launch": smooth_bytes(), "launch_us": mg_prof["smooth_us"],
                     "launches_timed": mg_prof["smooth_n"],
-                    "share_of_step": (mg_prof["smooth_us"] * 2 * 1e-6 * mg_prof["cycles"] / args.steps / value
+                    "share_of_step": (mg_prof["smooth_us"] * 5 * 1e-6 * mg_prof["cycles"] / args.steps / value
                                       if value > 0 else None),
-                    "timing": "CUDA events captured in the V-cycle graph around level 0's pre-smoothing, read "
-                              "after every cycle of the timed solves; launch_us = that time / 3 launches"}
-        mg_section = {"setup_ms_per_solve": mg_prof["setup_ms"], "cycle_ms": mg_prof["cycle_ms"],
+                    "timing": "CUDA events captured in the V-cycle graph around the two Chebyshev steps of level "
+                              "0's pre-smoothing, read after every cycle of the timed solves; launch_us = that "
+                              "time / 2 launches"}
+        mg_section = {"setup_ms_per_solve": mg_prof["setup_ms"], "setup_phases_ms": mg_prof["setup_phases_ms"],
+                      "cycle_ms": mg_prof["cycle_ms"],
                       "cycles_per_solve": mg_prof["cycles"] / max(args.steps, 1),
                       "level0_smoothing_us_per_launch": mg_prof["smooth_us"]}
     else:

@@ -23,6 +23,9 @@ FE_PREC_FP64, FE_PREC_MIXED, FE_PREC_MIXED_CG64 = 0, 1, 2
 FE_MODAL_SMALLEST, FE_MODAL_LARGEST = 0, 1
 FE_SOLVE_ACCEPT_STAGNATION, FE_SOLVE_RESTART_EACH_STEP, FE_SOLVE_X0_IF_BETTER = 1, 2, 4
 FE_SOLVE_MULTIGRID = 8
+FE_MG_PHASES = 10
+MG_PHASE_NAMES = ("input", "dinv_lmax", "aggregation", "tentative_qr", "prolongator", "a_p", "restriction",
+                  "galerkin", "coarsest_inverse", "cycle_prepare")
 
 STATUS_NAMES = {FE_OK: "FE_OK", FE_MAXITER: "FE_MAXITER", FE_BREAKDOWN: "FE_BREAKDOWN",
                 FE_NONFINITE: "FE_NONFINITE", FE_BAD_INPUT: "FE_BAD_INPUT",
@@ -94,6 +97,7 @@ _SIGNATURES = {
     "fe_profile_kernels": ([_P, _I32], C.c_int),
     "fe_profile_read": ([_P, _I32, _PD, _PI64, _PD, _PI64], C.c_int),
     "fe_profile_read_multigrid": ([_P, _PD, _PI64, _PD, _PI64, _PD, _PI64], C.c_int),
+    "fe_profile_read_multigrid_phases": ([_P, _PD, C.c_int32], C.c_int),
     "fe_post_elastic": ([_P, _P, _P, _P, _P], C.c_int),
     "fe_post_magnetic": ([_P, _P, _P], C.c_int),
     "fe_gnn_create": ([C.POINTER(_P)], C.c_int),

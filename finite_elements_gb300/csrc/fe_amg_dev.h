@@ -2,6 +2,7 @@
 // applied as a V-cycle by fe_amg_device.cu.
 #pragma once
 
+#include <utility>
 #include <vector>
 
 #include "fe_amg.h"
@@ -47,10 +48,37 @@ struct DevAmg {
     }
 };
 
+// Events recorded on the stream where each setup phase starts (amg::SetupPhase), while
+// profiling: a phase runs from its mark to the next one.
+struct SetupTrace {
+    std::vector<std::pair<cudaEvent_t, int>> marks;
+    void mark(cudaStream_t s, int k) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, s);
+        marks.push_back({e, k});
+    }
+    // waits for the last mark, adds each phase's time to ms[k] (k < n)
+    int collect(double *ms, int n) {
+        if (marks.empty()) return FE_OK;
+        FE_CUDA(cudaEventSynchronize(marks.back().first));
+        for (size_t i = 0; i + 1 < marks.size(); ++i) {
+            float a = 0.f;
+            if (marks[i].second < n && cudaEventElapsedTime(&a, marks[i].first, marks[i + 1].first) == cudaSuccess)
+                ms[marks[i].second] += a;
+        }
+        return FE_OK;
+    }
+    ~SetupTrace() {
+        for (auto &m : marks) cudaEventDestroy(m.first);
+    }
+};
+
 // Device setup of the hierarchy of the handle's eliminated system (near-null space: the
 // rigid-body modes for elasticity, the constant for magnetostatics, zero on the
-// constrained DOFs): amg::setup_hierarchy on the device executor.
-int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G);
+// constrained DOFs): amg::setup_hierarchy on the device executor; phases marked in
+// trace when given.
+int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G, SetupTrace *trace = nullptr);
 // Copy of a device hierarchy into host form (accessors of the fe_amg_* ABI).
 int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s);
 // Dense inverse of the coarsest matrix (+ 1e-12 of its largest diagonal entry).

@@ -17,6 +17,8 @@
 #include "fe_internal.h"
 
 namespace fe {
+static_assert(amg::kSetupPhases == FE_MG_PHASES, "setup phases of fe_profile_read_multigrid_phases");
+static_assert(amg::kSetupPhases <= 16, "SolverWork::mg_phase_ms");
 namespace {
 
 constexpr int kAT = 256;
@@ -213,6 +215,8 @@ inline int grid_lanes(int64_t n, int G) {
 struct CycleEx {
     fe_handle_s *h;
     DBuf<double> part, sc;
+    // row pointer of the level-0 operator, whose FP64 products run on the handle's SELL copy
+    const int64_t *sell_ptr = nullptr;
     // lanes per row of each matrix the cycle multiplies, keyed by its row pointer
     std::vector<std::pair<const int64_t *, int>> lanes;
     cudaEvent_t *marks = nullptr;   // events of the timing marks while profiling
@@ -289,6 +293,14 @@ struct CycleEx {
         h->launches += 1;
         return FE_OK;
     }
+    int rows(int64_t n, const amg::PassSpmv64 &f) {
+        if (n <= 0) return FE_OK;
+        if (sell_ptr && f.ptr == sell_ptr) return spmv64(h, f.p, f.q);
+        ka_rows<amg::PassSpmv64><<<grid_a(n), kAT, 0, h->stream>>>(n, f);
+        FE_LAUNCH_CHECK();
+        h->launches += 1;
+        return FE_OK;
+    }
     int rows(int64_t n, const amg::PassDense &f) {
         if (n <= 0) return FE_OK;
         ka_dense<<<grid_lanes(n, 32), kAT, 0, h->stream>>>(f);
@@ -328,10 +340,12 @@ struct CycleEx {
     }
 };
 
-// FP32 copies of a level's values and its cycle vectors
-int prepare_cycle(fe_handle_s *h, DevLevel &L) {
+// FP32 copies of a level's values and its cycle vectors (with_a: of A and D^-1 too;
+// level 0 smooths on the handle's SELL copy instead)
+int prepare_cycle(fe_handle_s *h, DevLevel &L, bool with_a) {
     const int d = L.A.rd, m = L.P.cd;
-    const int64_t na = L.A.nnzb * d * d, np = L.P.nnzb * d * m, nt = L.PT.nnzb * m * d, ndi = L.A.n * d * d;
+    const int64_t na = with_a ? L.A.nnzb * d * d : 0, np = L.P.nnzb * d * m, nt = L.PT.nnzb * m * d,
+                  ndi = with_a ? L.A.n * d * d : 0;
     FE_CHECK(dalloc(L.a32, (size_t)std::max<int64_t>(na, 1)));
     FE_CHECK(dalloc(L.p32, (size_t)std::max<int64_t>(np, 1)));
     FE_CHECK(dalloc(L.pt32, (size_t)std::max<int64_t>(nt, 1)));
@@ -347,6 +361,55 @@ int prepare_cycle(fe_handle_s *h, DevLevel &L) {
     FE_CHECK(dalloc(L.t, v));
     FE_CHECK(dalloc(L.dir, v));
     FE_CHECK(dalloc(L.zn, v));
+    return FE_OK;
+}
+
+// Chebyshev(k) smoothing of level 0 on the SELL copy, over the interval of the shared
+// cycle ([1.05 lmax / 30, 1.05 lmax]): from zero (z_1 = D^-1 r / theta needs no product;
+// start) or from the iterate in *cur (then the first step is a full one).  The iterates
+// ping-pong between *cur and *other; on return *cur holds the last.
+int level0_chebyshev(fe_handle_s *h, const amg::CycleLevel &L, const double *r64, int k, bool from_zero,
+                     float **cur, float **other, CycleEx &ex) {
+    const double hi = 1.05 * L.lmax, lo = hi / 30.0;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    if (from_zero) {
+        FE_CHECK(mg_level0_start(h, r64, L.r, *cur, 1.0 / theta));
+        ex.mark(0);
+    } else {
+        FE_CHECK(mg_level0_cheb(h, true, L.r, *cur, *other, 0.0, 1.0 / theta));
+        std::swap(*cur, *other);
+    }
+    for (int st = 1; st < k; ++st) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        const double a = rn * rho, b = 2.0 * rn / delta;
+        rho = rn;
+        // from zero, the second step's old iterate is z_0 = 0 (first)
+        FE_CHECK(mg_level0_cheb(h, from_zero && st == 1, L.r, *cur, *other, a, b));
+        std::swap(*cur, *other);
+    }
+    if (from_zero) ex.mark(1);
+    return FE_OK;
+}
+
+// z = M^-1 r: the shared FP32 V-cycle below level 0, level 0 on the SELL copy (its
+// right-hand side D^-1 r in L0.r, iterates in L0.x / L0.zn)
+int precondition_sell(CycleEx &ex, const std::vector<amg::CycleLevel> &levels, const amg::CycleCoarse &C, int k,
+                      const double *r, double *z) {
+    fe_handle_s *h = ex.h;
+    const amg::CycleLevel &L = levels[0];
+    float *rc = levels.size() > 1 ? levels[1].r : C.r;
+    float *xc = levels.size() > 1 ? levels[1].x : C.x;
+    ex.mark(2);
+    float *cur = L.x, *other = L.zn;
+    FE_CHECK(level0_chebyshev(h, L, r, k, true, &cur, &other, ex));
+    FE_CHECK(mg_level0_residual(h, L.r, cur, L.t));
+    FE_CHECK(ex.rows(L.nc, amg::PassRestrict32{L.tptr, L.tcol, L.pt, L.m, L.d, L.t, rc}));
+    FE_CHECK(amg::vcycle(ex, levels, C, 1, k));
+    FE_CHECK(ex.rows(L.n, amg::PassProlong32{L.pptr, L.pcol, L.p, L.d, L.m, xc, cur}));
+    FE_CHECK(level0_chebyshev(h, L, r, k, false, &cur, &other, ex));
+    FE_CHECK(ex.rows(L.n * L.d, amg::PassToF64{cur, z}));
+    ex.mark(3);
     return FE_OK;
 }
 
@@ -369,8 +432,11 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     // DOF: 647 -> 365 -> 321 -> 217 nodes with rows of 100-200 blocks; the Galerkin
     // product of the 647-node level alone took 140 ms, against 40 ms for the dense
     // inverse of the 1941-DOF level)
-    FE_CHECK(amg_setup_device(h, 0.08, std::min<int64_t>(3000, std::max<int64_t>(100, nd / 8)), G));
-    for (auto &L : G.L) FE_CHECK(prepare_cycle(h, L));
+    SetupTrace trace;
+    FE_CHECK(amg_setup_device(h, 0.08, std::min<int64_t>(3000, std::max<int64_t>(100, nd / 8)), G,
+                              prof ? &trace : nullptr));
+    if (prof) trace.mark(s, amg::kPhaseCycle);
+    for (size_t l = 0; l < G.L.size(); ++l) FE_CHECK(prepare_cycle(h, G.L[l], l > 0));
     FE_CHECK(dalloc(G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
     FE_CHECK(dalloc(G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
     if (G.L.empty()) {
@@ -405,6 +471,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     amg::CycleCoarse coarse;
     coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
     CycleEx cex{h};
+    cex.sell_ptr = L0.A.ptr.p;
     if (prof) cex.marks = h->w.pev;
     for (const DevLevel &Dl : G.L) {
         const double n_rows = (double)std::max<int64_t>(Dl.A.n, 1), n_aggr = (double)std::max<int64_t>(Dl.PT.n, 1);
@@ -426,7 +493,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         const int64_t l0 = h->launches;
         cudaGraph_t g = nullptr;
         FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        const int rc = amg::precondition(cex, views, coarse, 3, r.p, z.p);
+        const int rc = precondition_sell(cex, views, coarse, 3, r.p, z.p);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc != FE_OK) {
             if (ce == cudaSuccess && g) cudaGraphDestroy(g);
@@ -447,14 +514,16 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         h->launches = l0;
     }
     if (prof) {
-        // the setup: from the solve's start to here
+        // the setup: from the solve's start to here, and per phase
+        trace.mark(s, amg::kSetupPhases);
+        FE_CHECK(trace.collect(h->w.mg_phase_ms, 16));
         FE_CUDA(cudaEventRecord(h->events[7], s));
         FE_CUDA(cudaEventSynchronize(h->events[7]));
         float a = 0.f;
         FE_CUDA(cudaEventElapsedTime(&a, h->events[6], h->events[7]));
         h->w.mg_ms[1] += a, h->w.mg_n[1] += 1;
     }
-    const int64_t smooth_launches = 3;   // Chebyshev steps of level 0's pre-smoothing
+    const int64_t smooth_launches = 2;   // SELL Chebyshev steps of level 0's pre-smoothing
     auto precond = [&]() -> int {
         FE_CUDA(cudaGraphLaunch(cycle, s));
         h->launches += per_cycle;

@@ -500,7 +500,11 @@ struct DevEx {
     cudaStream_t s;
     DBuf<int64_t> scan_tmp;
     DBuf<double> part, sc;
+    SetupTrace *trace = nullptr;
     explicit DevEx(cudaStream_t st) : s(st) {}
+    void phase(int k) {
+        if (trace) trace->mark(s, k);
+    }
     ~DevEx() { dfree(scan_tmp), dfree(part), dfree(sc); }
     template <class T>
     int alloc(DBuf<T> &b, size_t n) { return dalloc(b, n); }
@@ -772,9 +776,11 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
 
 }  // namespace
 
-int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G) {
+int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G, SetupTrace *trace) {
     cudaStream_t s = h->stream;
     DevEx ex(s);
+    ex.trace = trace;
+    ex.phase(amg::kPhaseInput);
     const int D = h->dim;
     const int64_t n0 = h->n_nodes;
     const int m = D == 2 ? 3 : D == 3 ? 6 : 1;
@@ -806,6 +812,7 @@ int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &
     }
     FE_CHECK(st);
     // coarsest level: its dense inverse, on the device
+    ex.phase(amg::kPhaseCoarse);
     return coarse_inverse_device(G.coarse, G, s);
 }
 

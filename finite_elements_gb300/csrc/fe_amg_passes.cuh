@@ -13,6 +13,8 @@
 //   template <class F> int rows(int64_t n, const F &f);                // f(i) for i < n, any order
 //   int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total);   // exclusive, out[n] = total
 //   int dot(const double *a, const double *b, int64_t n, double *out);      // host value
+//   void phase(int k);   // setup phase k (SetupPhase) starts here (timed by the device
+//                        // executor when profiling, ignored by the host one)
 #pragma once
 
 #include <algorithm>
@@ -25,6 +27,23 @@
 
 namespace fe {
 namespace amg {
+
+// Phases of the setup, per level in this order, then the coarsest inverse and the
+// cycle's preparation (FP32 copies, capture); kPhaseInput is level 0's own copy of the
+// operator and its near-null space.
+enum SetupPhase : int {
+    kPhaseInput = 0,
+    kPhaseDiag,          // D^-1 and the power iterations for lmax
+    kPhaseAggregate,     // strength, the distance-2 independent set, the joins
+    kPhaseTentative,     // member lists and the QR of every aggregate
+    kPhaseProlongator,   // A P_t and the damped-Jacobi smoothing
+    kPhaseAP,            // A P
+    kPhaseRestriction,   // P^T: structure and values
+    kPhaseGalerkin,      // P^T (A P)
+    kPhaseCoarse,        // dense inverse of the coarsest level
+    kPhaseCycle,         // FP32 copies, cycle vectors, graph capture
+    kSetupPhases
+};
 
 // ------------------------------------------------------------------ storage
 
@@ -356,10 +375,12 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
         } lf{ex, L, Mem, Pt, AP, Ac};
         const int dd = A.rd;
         const int64_t n = A.n;
+        ex.phase(kPhaseDiag);
         FE_CHECK(ex.alloc(L.dinv, (size_t)std::max<int64_t>(n * dd * dd, 1)));
         FE_CHECK(ex.rows(n, PassDinv{A.ptr.p, A.col.p, A.val.p, dd, L.dinv.p}));
         FE_CHECK(lmax_of(ex, A, L.dinv.p, &L.lmax));
         // strength and the distance-2 independent set
+        ex.phase(kPhaseAggregate);
         FE_CHECK(ex.alloc(nrm, (size_t)std::max<int64_t>(A.nnzb, 1)));
         FE_CHECK(ex.alloc(strong, (size_t)std::max<int64_t>(A.nnzb, 1)));
         FE_CHECK(ex.alloc(dg, (size_t)std::max<int64_t>(n, 1)));
@@ -408,6 +429,7 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
             return FE_BREAKDOWN;
         }
         // members of every aggregate in node order (rows = aggregates, no values)
+        ex.phase(kPhaseTentative);
         Mem.n = na;
         FE_CHECK(distinct_rows(ex, na, PassMemberBound{A.ptr.p, A.col.p, roots.p, nullptr},
                                PassMembers{A.ptr.p, A.col.p, roots.p, L.agg.p, nullptr, nullptr, nullptr}, Mem, W));
@@ -426,17 +448,21 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
         FE_CHECK(ex.alloc(Bc, (size_t)std::max<int64_t>(na * m * m, 1)));
         FE_CHECK(ex.rows(na, PassQr{Mem.ptr.p, Mem.col.p, dd, m, Pt.val.p, Bc.p}));
         // P = P_t - w D^-1 A P_t
+        ex.phase(kPhaseProlongator);
         FE_CHECK(product(ex, A, Pt, L.P, W));
         const double w = 4.0 / (3.0 * L.lmax);
         FE_CHECK(ex.rows(n, PassSmooth{L.P.ptr.p, L.P.col.p, L.P.val.p, L.dinv.p, Pt.val.p, L.agg.p, dd, m, w}));
         // restriction P^T and Galerkin product P^T (A P)
+        ex.phase(kPhaseAP);
         FE_CHECK(product(ex, A, L.P, AP, W));
+        ex.phase(kPhaseRestriction);
         L.PT.n = na, L.PT.rd = m, L.PT.cd = dd;
         FE_CHECK(distinct_rows(ex, na, PassRestrBound{Mem.ptr.p, Mem.col.p, A.ptr.p, nullptr},
                                PassRestrCols{Mem.ptr.p, Mem.col.p, A.ptr.p, A.col.p, nullptr, nullptr, nullptr}, L.PT,
                                W));
         FE_CHECK(ex.alloc(L.PT.val, (size_t)std::max<int64_t>(L.PT.nnzb * m * dd, 1)));
         FE_CHECK(ex.rows(na, PassRestrVals{L.PT.ptr.p, L.PT.col.p, L.PT.val.p, L.P.ptr.p, L.P.col.p, L.P.val.p, dd, m}));
+        ex.phase(kPhaseGalerkin);
         FE_CHECK(product(ex, L.PT, AP, Ac, W));
         // the level keeps A; the next level starts from A_c and the coarse near-null space
         L.A = A;

@@ -418,7 +418,8 @@ int coarse_inverse(fe_amg_s *h, const char *who) { return coarse_inverse_of(h->c
 // summed per chunk in chunk order.
 
 struct HostEx {
-    void mark(int) {}   // the device cycle's timing marks: nothing to time here
+    void mark(int) {}    // the device cycle's timing marks: nothing to time here
+    void phase(int) {}   // nor the setup's phases
     template <class T>
     int alloc(DBuf<T> &b, size_t n) {
         if (b.p && b.n >= n) return FE_OK;

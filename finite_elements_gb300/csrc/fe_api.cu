@@ -523,4 +523,14 @@ int fe_profile_read_multigrid(fe_handle h, double *smooth_ms, int64_t *smooth_n,
     return FE_OK;
 }
 
+int fe_profile_read_multigrid_phases(fe_handle h, double *ms, int32_t n) {
+    FE_HANDLE_CHECK(h);
+    if (n > 0 && !ms) {
+        set_error("fe_profile_read_multigrid_phases: null output");
+        return FE_BAD_INPUT;
+    }
+    for (int k = 0; k < n && k < FE_MG_PHASES; ++k) ms[k] = h->w.mg_phase_ms[k];
+    return FE_OK;
+}
+
 }  // extern "C"

@@ -146,6 +146,7 @@ struct SolverWork {
     // whole V-cycle (ms, cycles)
     double mg_ms[3] = {0.0, 0.0, 0.0};
     int64_t mg_n[3] = {0, 0, 0};
+    double mg_phase_ms[16] = {};   // multigrid setup time per phase (amg::SetupPhase)
     int64_t prof_n[3][2] = {{0, 0}, {0, 0}, {0, 0}};
 };
 
@@ -301,5 +302,12 @@ int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);
 int profile_kernels(fe_handle_s *h, int enable);
 void release_solver(fe_handle_s *h);
 int spmv64(fe_handle_s *h, const double *x, double *y);
+// Level 0 of the multigrid V-cycle on the handle's prescaled FP32 SELL copy
+// (fe_solver.cu), enqueued on the handle's stream: rh = D^-1 (float)r and
+// z1 = rh * inv_theta; one Chebyshev step z_out = z_in + c1 (z_in - z_out) +
+// c2 (rh - D^-1 A z_in) (first: the old iterate taken as 0); t = r - A x from rh.
+int mg_level0_start(fe_handle_s *h, const double *r, float *rh, float *z1, double inv_theta);
+int mg_level0_cheb(fe_handle_s *h, bool first, const float *rh, const float *zin, float *zout, double c1, double c2);
+int mg_level0_residual(fe_handle_s *h, const float *rh, const float *x, float *t);
 
 }  // namespace fe

@@ -1633,6 +1633,94 @@ int spmv64(fe_handle_s *h, const double *x, double *y) {
     return FE_OK;
 }
 
+// ---------------------------------------------------------------- multigrid level 0 on SELL
+// The V-cycle's finest level is the eliminated system itself, so its smoothing and
+// residual run on the handle's prescaled FP32 SELL copy (D^-1 A_rm, D^-1 S_r with the
+// node-block Jacobi inverse D^-1) with the Chebyshev step kernel of the mixed solver.
+
+namespace {
+
+// rh = D^-1 r (r rounded to FP32) and z_1 = rh / theta: the first Chebyshev step from
+// z_0 = 0, which needs no product
+template <int D>
+__global__ void __launch_bounds__(kVecThreads)
+k_mg_level0_start(int64_t n_nodes, const double *__restrict__ r, const float *__restrict__ dinv,
+                  float *__restrict__ rh, float *__restrict__ z1, float inv_theta) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const NodeVec<D, double> r64 = ld<D, double>(r, i);
+        NodeVec<D, float> rv;
+#pragma unroll
+        for (int a = 0; a < D; ++a) rv.v[a] = (float)r64.v[a];
+        NodeVec<D, float> zv = apply_dinv<D, float>(dinv, i, rv);
+        st<D, float>(rh, i, zv);
+#pragma unroll
+        for (int a = 0; a < D; ++a) zv.v[a] *= inv_theta;
+        st<D, float>(z1, i, zv);
+    }
+}
+
+// t = r - A x = A_rr (D^-1 r - D^-1 A x), given rh = D^-1 r
+template <int D, bool C16>
+__global__ void __launch_bounds__(kVecThreads, kSellBlocks<D, float>)
+k_mg_level0_residual(int64_t n_nodes, Sell A, const float *__restrict__ val, const float *__restrict__ diag,
+                     const float *__restrict__ dblk, const float *__restrict__ rh, const float *__restrict__ x,
+                     float *__restrict__ t) {
+    FE_SELL_LOOP {
+        const bool valid = row < n_nodes;
+        const NodeVec<D, float> ax = sell_row<D, float, C16>(row, valid, A, val, diag, x);
+        if (valid) {
+            NodeVec<D, float> rv = ld<D, float>(rh, row);
+#pragma unroll
+            for (int a = 0; a < D; ++a) rv.v[a] -= ax.v[a];
+            st<D, float>(t, row, apply_dinv<D, float>(dblk, row, rv));
+        }
+    }
+}
+
+}  // namespace
+
+int mg_level0_start(fe_handle_s *h, const double *r, float *rh, float *z1, double inv_theta) {
+    FE_CHECK(with_dim(h->dim, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        k_mg_level0_start<D><<<vec_grid(h->n_nodes), kVecThreads, 0, h->stream>>>(h->n_nodes, r, h->dinv32.p, rh, z1,
+                                                                                  (float)inv_theta);
+        return FE_OK;
+    }));
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    return FE_OK;
+}
+
+int mg_level0_cheb(fe_handle_s *h, bool first, const float *rh, const float *zin, float *zout, double c1, double c2) {
+    FE_CHECK(with_dim(h->dim, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        Sys<float> s = make_sys<D, float>(h);
+        s.rh = const_cast<float *>(rh);
+        launch_cheb_step<D, float, float, 0>(h, s, first, zin, zout, c1, c2, nullptr, nullptr, sell_grid(h),
+                                             (const float *)nullptr);
+        return FE_OK;
+    }));
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    return FE_OK;
+}
+
+int mg_level0_residual(fe_handle_s *h, const float *rh, const float *x, float *t) {
+    FE_CHECK(with_dim(h->dim, [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        const Sys<float> s = make_sys<D, float>(h);
+        with_col16<float>(s.A, [&](auto c16) {
+            k_mg_level0_residual<D, decltype(c16)::value><<<sell_grid(h), kVecThreads, 0, h->stream>>>(
+                h->n_nodes, s.A, s.sval, s.diag, s.dblk, rh, x, t);
+        });
+        return FE_OK;
+    }));
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    return FE_OK;
+}
+
 int profile_kernels(fe_handle_s *h, int enable) {
     SolverWork &w = h->w;
     if (enable && !w.pev[0])
@@ -1641,6 +1729,7 @@ int profile_kernels(fe_handle_s *h, int enable) {
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 2; ++b) w.prof_ms[a][b] = 0.0, w.prof_n[a][b] = 0;
     for (int a = 0; a < 3; ++a) w.mg_ms[a] = 0.0, w.mg_n[a] = 0;
+    for (double &t : w.mg_phase_ms) t = 0.0;
     return FE_OK;
 }
 

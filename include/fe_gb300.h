@@ -247,6 +247,17 @@ int fe_profile_read(fe_handle h, int32_t precision, double *cheb_ms, int64_t *ch
  * captured cycle and read after each of its launches. */
 int fe_profile_read_multigrid(fe_handle h, double *smooth_ms, int64_t *smooth_n, double *setup_ms, int64_t *setups,
                               double *cycle_ms, int64_t *cycles);
+/* The multigrid setup's time per phase (ms, summed over levels and solves since
+ * fe_profile_kernels(h, 1)), into ms[0 .. min(n, FE_MG_PHASES)):
+ *   0 level 0's copy of the operator and near-null space, 1 D^-1 and the power
+ *   iterations, 2 aggregation (strength, distance-2 independent set, joins), 3 member
+ *   lists and per-aggregate QR, 4 A P_t and the smoothing of P, 5 A P, 6 P^T, 7 the
+ *   Galerkin product P^T (A P), 8 the coarsest dense inverse, 9 the cycle's FP32 copies
+ *   and graph capture.
+ * Stream time between events recorded where each phase starts (host work and waits
+ * included). */
+#define FE_MG_PHASES 10
+int fe_profile_read_multigrid_phases(fe_handle h, double *ms, int32_t n);
 
 /* ---- modal analysis (analysis.py:741-796 modal_analysis: scipy eigsh/eigs on
  * k_matrix_sparse and m_matrix_sparse, i.e. K and M without Dirichlet conditions).
