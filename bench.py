@@ -71,6 +71,10 @@ def parse_args():
                          "V-cycle (set up on the device every step) or node-block Jacobi + Chebyshev in FP32")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed plain FP64 solves beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=512,
+                    help="instances of the batched-solve leg (0: no batched leg)")
+    ap.add_argument("--batch-single", type=int, default=64,
+                    help="of them, solved one at a time for the comparison (-1: all)")
     ap.add_argument("--l2-keep", type=float, default=-1.0,
                     help="MB of the FP32 preconditioner matrix kept L2-resident across Chebyshev steps "
                          "(default: the library's 40 MB; 0 = plain loads)")
@@ -542,6 +546,14 @@ def run_ours(args, dist):
         "gpu_launches": int(n_launch),
         "clocks": clk,
     }
+    if dist.world == 1 and args.batch_n > 0:
+        # hundreds of uneven instances in one batched system (persistent kernel, CUDA
+        # graph, autotuned tiles) against the same instances solved one at a time
+        from finite_elements_gb300 import batch_bench, meshgen as mg
+        ba = argparse.Namespace(tol=args.tol, single=args.batch_single, cheb=16, cheb_ratio=1e4)
+        out["batched"] = dict(batch_bench.measure(ba, mg.batch_c4(args.batch_n, seed=args.seed)),
+                              method="python -m finite_elements_gb300.batch_bench --n "
+                                     f"{args.batch_n} --single {args.batch_single} --seed {args.seed}")
     if dist.world == 1 and not args.no_cpu_baseline:
         # the CPU baseline at the full workload, measured, and the FP64 oracle solution the
         # mixed result's error is taken against

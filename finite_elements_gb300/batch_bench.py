@@ -82,20 +82,9 @@ def run_sharded(a, probs_all, world):
     td.destroy_process_group()
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--n", type=int, default=512)
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--single", type=int, default=-1, help="instances solved one at a time (-1: all)")
-    ap.add_argument("--cheb", type=int, default=16, help="Chebyshev terms of the preconditioner (1: Jacobi)")
-    ap.add_argument("--cheb-ratio", type=float, default=1e4)
-    a = ap.parse_args()
-    probs = meshgen.batch_c4(a.n, seed=a.seed)
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    if world > 1:
-        run_sharded(a, probs, world)
-        return
+def measure(a, probs):
+    """The batched solve of `probs` on this GPU against `a.single` of them (-1: all) solved
+    one at a time; returns the result line as a dict."""
     dof = int(sum(p.n_dof for p in probs))
     tri = int(sum(p.n_elements for p in probs))
     # warm-up of the library (kernels, allocator) on a small batch
@@ -158,7 +147,24 @@ def main():
     }
     out["speedup_device"] = out["batched"]["dof_per_s_device"] / out["one_at_a_time"]["dof_per_s_device"]
     out["speedup_wall"] = out["batched"]["dof_per_s_device"] / out["one_at_a_time"]["dof_per_s_wall"]
-    print(json.dumps(out))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--single", type=int, default=-1, help="instances solved one at a time (-1: all)")
+    ap.add_argument("--cheb", type=int, default=16, help="Chebyshev terms of the preconditioner (1: Jacobi)")
+    ap.add_argument("--cheb-ratio", type=float, default=1e4)
+    a = ap.parse_args()
+    probs = meshgen.batch_c4(a.n, seed=a.seed)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        run_sharded(a, probs, world)
+        return
+    print(json.dumps(measure(a, probs)))
 
 
 if __name__ == "__main__":

@@ -13,8 +13,41 @@ namespace fe {
 
 using DevCsr = amg::Csr;
 
-inline void drelease(DevCsr &c) {
-    dfree(c.ptr), dfree(c.col), dfree(c.val);
+// The multigrid solve's device buffers: stream-ordered allocations on the handle's
+// stream from the handle's memory pool, which keeps the memory between solves, so a
+// setup's hundred-odd allocations and frees map no pages and never synchronise the
+// device.  palloc grows a buffer like dalloc; pfree returns it on the stream.
+struct MgMem {
+    cudaStream_t s = nullptr;
+    cudaMemPool_t pool = nullptr;
+};
+
+// the handle's pool (created on first use, release threshold unbounded)
+int mg_memory(fe_handle_s *h, MgMem *out);
+
+template <typename T>
+int palloc(const MgMem &m, DBuf<T> &b, size_t n) {
+    if (b.p && b.n >= n) return FE_OK;
+    if (b.p) {
+        cudaFreeAsync(b.p, m.s);
+        b.p = nullptr;
+        b.n = 0;
+    }
+    if (n == 0) return FE_OK;
+    FE_CUDA(cudaMallocFromPoolAsync((void **)&b.p, n * sizeof(T), m.pool, m.s));
+    b.n = n;
+    return FE_OK;
+}
+
+template <typename T>
+void pfree(const MgMem &m, DBuf<T> &b) {
+    if (b.p) cudaFreeAsync(b.p, m.s);
+    b.p = nullptr;
+    b.n = 0;
+}
+
+inline void drelease(const MgMem &m, DevCsr &c) {
+    pfree(m, c.ptr), pfree(m, c.col), pfree(m, c.val);
     c.nnzb = 0;
 }
 
@@ -27,14 +60,15 @@ struct DevLevel {
     // (n * d each; r, x: the level's right-hand side and iterate)
     DBuf<float> a32, p32, pt32, dinv32;
     DBuf<float> r, x, t, dir, zn;
-    void release() {
-        drelease(A), drelease(P), drelease(PT);
-        dfree(dinv), dfree(agg), dfree(a32), dfree(p32), dfree(pt32), dfree(dinv32);
-        dfree(r), dfree(x), dfree(t), dfree(dir), dfree(zn);
+    void release(const MgMem &m) {
+        drelease(m, A), drelease(m, P), drelease(m, PT);
+        pfree(m, dinv), pfree(m, agg), pfree(m, a32), pfree(m, p32), pfree(m, pt32), pfree(m, dinv32);
+        pfree(m, r), pfree(m, x), pfree(m, t), pfree(m, dir), pfree(m, zn);
     }
 };
 
 struct DevAmg {
+    MgMem mem;                       // where every buffer below comes from
     std::vector<DevLevel> L;
     DevCsr coarse;
     int64_t nc = 0;                  // coarsest DOFs
@@ -42,9 +76,9 @@ struct DevAmg {
     DBuf<float> rc, xc;
     int mis_rounds = 0;              // independent-set rounds, all levels
     ~DevAmg() {
-        for (auto &l : L) l.release();
-        drelease(coarse);
-        dfree(cinv), dfree(rc), dfree(xc);
+        for (auto &l : L) l.release(mem);
+        drelease(mem, coarse);
+        pfree(mem, cinv), pfree(mem, rc), pfree(mem, xc);
     }
 };
 

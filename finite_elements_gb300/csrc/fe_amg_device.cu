@@ -214,6 +214,7 @@ inline int grid_lanes(int64_t n, int G) {
 
 struct CycleEx {
     fe_handle_s *h;
+    MgMem mem;
     DBuf<double> part, sc;
     // row pointer of the level-0 operator, whose FP64 products run on the handle's SELL copy
     const int64_t *sell_ptr = nullptr;
@@ -223,7 +224,7 @@ struct CycleEx {
     void mark(int k) {
         if (marks) cudaEventRecordWithFlags(marks[k], h->stream, cudaEventRecordExternal);
     }
-    ~CycleEx() { dfree(part), dfree(sc); }
+    ~CycleEx() { pfree(mem, part), pfree(mem, sc); }
     int lanes_of(const int64_t *ptr) const {
         for (const auto &p : lanes)
             if (p.first == ptr) return p.second;
@@ -310,8 +311,8 @@ struct CycleEx {
     }
     int dot(const double *a, const double *b, int64_t n, double *out) {
         const int g = grid_a(n);
-        FE_CHECK(dalloc(part, (size_t)g));
-        FE_CHECK(dalloc(sc, 1));
+        FE_CHECK(palloc(mem, part, (size_t)g));
+        FE_CHECK(palloc(mem, sc, 1));
         ka_dot<<<g, kAT, 0, h->stream>>>(n, a, b, part.p);
         ka_dot_final<<<1, kAT, 0, h->stream>>>(g, part.p, sc.p);
         FE_LAUNCH_CHECK();
@@ -342,25 +343,25 @@ struct CycleEx {
 
 // FP32 copies of a level's values and its cycle vectors (with_a: of A and D^-1 too;
 // level 0 smooths on the handle's SELL copy instead)
-int prepare_cycle(fe_handle_s *h, DevLevel &L, bool with_a) {
+int prepare_cycle(fe_handle_s *h, const MgMem &mem, DevLevel &L, bool with_a) {
     const int d = L.A.rd, m = L.P.cd;
     const int64_t na = with_a ? L.A.nnzb * d * d : 0, np = L.P.nnzb * d * m, nt = L.PT.nnzb * m * d,
                   ndi = with_a ? L.A.n * d * d : 0;
-    FE_CHECK(dalloc(L.a32, (size_t)std::max<int64_t>(na, 1)));
-    FE_CHECK(dalloc(L.p32, (size_t)std::max<int64_t>(np, 1)));
-    FE_CHECK(dalloc(L.pt32, (size_t)std::max<int64_t>(nt, 1)));
-    FE_CHECK(dalloc(L.dinv32, (size_t)std::max<int64_t>(ndi, 1)));
-    CycleEx ex{h};
+    FE_CHECK(palloc(mem, L.a32, (size_t)std::max<int64_t>(na, 1)));
+    FE_CHECK(palloc(mem, L.p32, (size_t)std::max<int64_t>(np, 1)));
+    FE_CHECK(palloc(mem, L.pt32, (size_t)std::max<int64_t>(nt, 1)));
+    FE_CHECK(palloc(mem, L.dinv32, (size_t)std::max<int64_t>(ndi, 1)));
+    CycleEx ex{h, mem};
     FE_CHECK(ex.rows(na, amg::PassToF32{L.A.val.p, L.a32.p}));
     FE_CHECK(ex.rows(np, amg::PassToF32{L.P.val.p, L.p32.p}));
     FE_CHECK(ex.rows(nt, amg::PassToF32{L.PT.val.p, L.pt32.p}));
     FE_CHECK(ex.rows(ndi, amg::PassToF32{L.dinv.p, L.dinv32.p}));
     const size_t v = (size_t)std::max<int64_t>(L.A.n * d, 1);
-    FE_CHECK(dalloc(L.r, v));
-    FE_CHECK(dalloc(L.x, v));
-    FE_CHECK(dalloc(L.t, v));
-    FE_CHECK(dalloc(L.dir, v));
-    FE_CHECK(dalloc(L.zn, v));
+    FE_CHECK(palloc(mem, L.r, v));
+    FE_CHECK(palloc(mem, L.x, v));
+    FE_CHECK(palloc(mem, L.t, v));
+    FE_CHECK(palloc(mem, L.dir, v));
+    FE_CHECK(palloc(mem, L.zn, v));
     return FE_OK;
 }
 
@@ -436,9 +437,9 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     FE_CHECK(amg_setup_device(h, 0.08, std::min<int64_t>(3000, std::max<int64_t>(100, nd / 8)), G,
                               prof ? &trace : nullptr));
     if (prof) trace.mark(s, amg::kPhaseCycle);
-    for (size_t l = 0; l < G.L.size(); ++l) FE_CHECK(prepare_cycle(h, G.L[l], l > 0));
-    FE_CHECK(dalloc(G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
-    FE_CHECK(dalloc(G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
+    for (size_t l = 0; l < G.L.size(); ++l) FE_CHECK(prepare_cycle(h, G.mem, G.L[l], l > 0));
+    FE_CHECK(palloc(G.mem, G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
+    FE_CHECK(palloc(G.mem, G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
     if (G.L.empty()) {
         set_error("fe_solve: the multigrid hierarchy has a single level (use the other preconditioners)");
         return FE_BAD_INPUT;
@@ -447,16 +448,17 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     DevLevel &L0 = G.L[0];
     DBuf<double> r, p, q, z;
     struct Free {
+        const MgMem &m;
         DBuf<double> *b[4];
         ~Free() {
-            for (auto *x : b) dfree(*x);
+            for (auto *x : b) pfree(m, *x);
         }
-    } fg{{&r, &p, &q, &z}};
+    } fg{G.mem, {&r, &p, &q, &z}};
     FE_CHECK(dalloc(h->w.x, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(dalloc(r, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(dalloc(p, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(dalloc(q, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(dalloc(z, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(palloc(G.mem, r, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(palloc(G.mem, p, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(palloc(G.mem, q, (size_t)std::max<int64_t>(nd, 1)));
+    FE_CHECK(palloc(G.mem, z, (size_t)std::max<int64_t>(nd, 1)));
     // the levels as the shared cycle sees them
     std::vector<amg::CycleLevel> views(G.L.size());
     for (size_t l = 0; l < G.L.size(); ++l) {
@@ -470,7 +472,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     }
     amg::CycleCoarse coarse;
     coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
-    CycleEx cex{h};
+    CycleEx cex{h, G.mem};
     cex.sell_ptr = L0.A.ptr.p;
     if (prof) cex.marks = h->w.pev;
     for (const DevLevel &Dl : G.L) {

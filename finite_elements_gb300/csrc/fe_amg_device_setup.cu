@@ -92,9 +92,10 @@ __global__ void ks_tile_scan(const int64_t *__restrict__ in, int64_t n, const in
 }
 
 // out[0..n] = exclusive prefix sums of in[0..n), out[n] the total (also returned)
-int scan64(const int64_t *in, int64_t n, int64_t *out, int64_t *total, DBuf<int64_t> &tmp, cudaStream_t s) {
+int scan64(const int64_t *in, int64_t n, int64_t *out, int64_t *total, DBuf<int64_t> &tmp, const MgMem &mem) {
+    const cudaStream_t s = mem.s;
     const int64_t nt = std::max<int64_t>(1, (n + kScanTile - 1) / kScanTile);
-    FE_CHECK(dalloc(tmp, (size_t)nt));
+    FE_CHECK(palloc(mem, tmp, (size_t)nt));
     ks_tile_sums<<<(unsigned)nt, kST, 0, s>>>(in, n, tmp.p);
     ks_scan_tiles<<<1, 1, 0, s>>>(nt, tmp.p, out, n);
     ks_tile_scan<<<(unsigned)nt, kST, 0, s>>>(in, n, tmp.p, out);
@@ -168,8 +169,12 @@ __global__ void __launch_bounds__(kST) kd_dinv_product(int64_t n, amg::PassDinvP
 #pragma unroll
             for (int a = 0; a < D; ++a) {
                 double v = 0.0;
+                if (f.dinv) {
 #pragma unroll
-                for (int k = 0; k < D; ++k) v = fma(f.dinv[i * D * D + a * D + k], acc[k], v);
+                    for (int k = 0; k < D; ++k) v = fma(f.dinv[i * D * D + a * D + k], acc[k], v);
+                } else {
+                    v = acc[a];
+                }
                 f.y[i * D + a] = v;
             }
     }
@@ -497,19 +502,20 @@ int launch_prod_vals(int64_t n, const amg::PassProdVals &f, cudaStream_t s) {
 
 
 struct DevEx {
+    MgMem mem;
     cudaStream_t s;
     DBuf<int64_t> scan_tmp;
     DBuf<double> part, sc;
     SetupTrace *trace = nullptr;
-    explicit DevEx(cudaStream_t st) : s(st) {}
+    explicit DevEx(const MgMem &m) : mem(m), s(m.s) {}
     void phase(int k) {
         if (trace) trace->mark(s, k);
     }
-    ~DevEx() { dfree(scan_tmp), dfree(part), dfree(sc); }
+    ~DevEx() { pfree(mem, scan_tmp), pfree(mem, part), pfree(mem, sc); }
     template <class T>
-    int alloc(DBuf<T> &b, size_t n) { return dalloc(b, n); }
+    int alloc(DBuf<T> &b, size_t n) { return palloc(mem, b, n); }
     template <class T>
-    void release(DBuf<T> &b) { dfree(b); }
+    void release(DBuf<T> &b) { pfree(mem, b); }
     template <class T>
     int copy(T *dst, const T *src, size_t n) {
         if (n) FE_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -574,11 +580,11 @@ struct DevEx {
         FE_LAUNCH_CHECK();
         return FE_OK;
     }
-    int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) { return scan64(in, n, out, total, scan_tmp, s); }
+    int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) { return scan64(in, n, out, total, scan_tmp, mem); }
     int dot(const double *a, const double *b, int64_t n, double *out) {
         const int g = grid_s(n);
-        FE_CHECK(dalloc(part, (size_t)g));
-        FE_CHECK(dalloc(sc, 1));
+        FE_CHECK(palloc(mem, part, (size_t)g));
+        FE_CHECK(palloc(mem, sc, 1));
         kd_dot<<<g, kST, 0, s>>>(n, a, b, part.p);
         kd_dot_final<<<1, kST, 0, s>>>(g, part.p, sc.p);
         FE_LAUNCH_CHECK();
@@ -636,14 +642,21 @@ int csr_to_host(const DevCsr &D, BlockCsr &H, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------- coarsest inverse
-// Dense inverse of the coarsest matrix by Gauss-Jordan elimination without pivoting
-// (the matrix is symmetric positive definite once 1e-12 of its largest diagonal entry
-// is added, as the host version does), in place, one pivot k after the other, every new
-// value from old ones:
-//   others:  a_ij - a_ik a_kj / a_kk      (i != k, j != k)
-//   row k:   a_kj / a_kk (j != k);  column k: -a_ik / a_kk (i != k);  pivot: 1 / a_kk
+// Dense inverse of the coarsest matrix (symmetric positive definite once 1e-12 of its
+// largest diagonal entry is added, as the host version does) by the sweep operator
+// (Goodnight, "A tutorial on the SWEEP operator", The American Statistician 33, 1979):
+// sweeping pivot p of a symmetric M,
+//   m_pp <- -1 / m_pp,  m_ip <- m_ip / m_pp,  m_pj <- m_pj / m_pp,
+//   m_ij <- m_ij - m_ip m_pj / m_pp              (i, j != p),
+// keeps M symmetric, and sweeping every pivot once leaves -M^-1.  Sweeping a block K of
+// pivots at once, with T = -S^-1 of S = M_KK and C = M_:K,
+//   M_KK <- T,  M_IK <- -C_I T,  M_IJ <- M_IJ + (C_I T) C_J^T       (I, J outside K),
+// equals sweeping its pivots one by one, and turns the work into rank-kSweepB updates.
+// Only the upper triangle is kept (element (i, j), i <= j, stands for both), which
+// halves the FP64 arithmetic against Gauss-Jordan on the full matrix.
 
 constexpr int kMaxCoarse = 4096;   // DOFs of the coarsest level (a 128 MB inverse)
+constexpr int kSweepB = 32;        // pivots per block sweep, and the tile edge of the update
 
 __global__ void kc_dense_fill(int64_t nb_rows, int cd, const int64_t *__restrict__ ptr,
                               const int32_t *__restrict__ col, const double *__restrict__ val, int64_t n,
@@ -667,88 +680,162 @@ __global__ void kc_regularise(int64_t n, double *M) {
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) M[i * n + i] += 1e-12 * t;
 }
 
-// All pivots in one cooperative launch, one grid barrier per pivot.  Block b owns rows
-// b, b + B, ... and its threads the columns of them, so every element has one owner for
-// the whole elimination.  Pivot k's new values come from old values only -- the element
-// itself, a_ik, a_kj and a_kk -- and the old pivot row and column are read from buffers
-// (piv[k & 1]) that the owners filled while computing the previous pivot, so a pivot's
-// updates do not race with its readers; the owners of row and column k + 1 fill
-// piv[(k + 1) & 1] on the way.  piv[b] holds the row (n values) then the column.  Each
-// block stages the pivot row in shared memory.  A zero or non-finite pivot stops every
-// block at the same step (*singular = 1).
-__global__ void __launch_bounds__(kST) kc_gauss_jordan(int64_t n, double *M, double *piv, unsigned *bar, int *err,
-                                                       int *singular) {
-    __shared__ double srow[kMaxCoarse];
-    for (int64_t k = 0; k < n; ++k) {
-        const double *row = piv + (k & 1) * 2 * n, *colv = row + n;
-        double *nrow = piv + ((k + 1) & 1) * 2 * n, *ncol = nrow + n;
-        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) srow[j] = __ldcg(row + j);
-        __syncthreads();
-        const double p = srow[k];
-        if (p == 0.0 || !isfinite(p)) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) *singular = 1;
-            return;
+// the upper-triangle element standing for (i, j)
+__device__ __forceinline__ int64_t upper(int64_t i, int64_t j, int64_t n) { return i <= j ? i * n + j : j * n + i; }
+
+// All block sweeps in one cooperative launch, two grid barriers per block of pivots:
+//  (a) every block computes T = -S^-1 of the pivot block in shared memory (the same
+//      arithmetic in every block), by sweeping its pivots one by one;
+//  (b) a warp per row i outside K: C_i = M_iK and W_i = C_i T into Cs / Ws (zero rows
+//      for i in K), and the new column -W_i into M;
+//  (c) after a barrier, the upper 32 x 32 tiles of M += W C^T (rows and columns in K
+//      skipped), and M_KK <- T;
+// then, after the last block, the full inverse -M from the upper triangle.  A pivot that
+// is not positive (the matrix is not positive definite) stops every block at the same
+// step (*singular = 1); the barriers are bounded (grid_sync_bounded).
+__global__ void __launch_bounds__(kST) kc_sweep(int64_t n, double *M, double *Cs, double *Ws, unsigned *bar, int *err,
+                                                int *singular) {
+    constexpr int B = kSweepB;
+    __shared__ double T[B][B + 1];
+    __shared__ double sw[B][B + 1], sc[B][B + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t nt = (n + B - 1) / B;   // tiles per dimension
+    const int64_t n_upper = nt * (nt + 1) / 2;
+    for (int64_t k0 = 0; k0 < n; k0 += B) {
+        const int bk = (int)(n - k0 < B ? n - k0 : B);
+        // (a) T = -S^-1
+        for (int e = threadIdx.x; e < B * B; e += blockDim.x) {
+            const int a = e / B, b = e % B;
+            T[a][b] = (a < bk && b < bk) ? __ldcg(M + upper(k0 + a, k0 + b, n)) : 0.0;
         }
-        const double ip = 1.0 / p;
-        for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
-            const double f = -__ldcg(colv + i) * ip;
-            double *Mi = M + i * n;
-#pragma unroll 4
-            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-                double v;
-                if (i == k) v = j == k ? ip : srow[j] * ip;
-                else if (j == k) v = f;
-                else v = fma(f, srow[j], Mi[j]);
-                Mi[j] = v;
-                if (i == k + 1) nrow[j] = v;
-                if (j == k + 1) ncol[i] = v;
+        __syncthreads();
+        for (int p = 0; p < bk; ++p) {
+            const double d = T[p][p];
+            if (!(d > 0.0) || !isfinite(d)) {
+                if (blockIdx.x == 0 && threadIdx.x == 0) *singular = 1;
+                return;
             }
+            const double id = 1.0 / d;
+            double v[B * B / kST];
+            int q = 0;
+            for (int e = threadIdx.x; e < bk * B; e += blockDim.x, ++q) {
+                const int a = e / B, b = e % B;
+                if (b >= bk) continue;
+                if (a == p && b == p) v[q] = -id;
+                else if (a == p) v[q] = T[p][b] * id;
+                else if (b == p) v[q] = T[a][p] * id;
+                else v[q] = T[a][b] - T[a][p] * T[p][b] * id;
+            }
+            __syncthreads();
+            q = 0;
+            for (int e = threadIdx.x; e < bk * B; e += blockDim.x, ++q) {
+                const int b = e % B;
+                if (b < bk) T[e / B][b] = v[q];
+            }
+            __syncthreads();
+        }
+        // exactly symmetric T: the upper triangle stands for both
+        for (int e = threadIdx.x; e < B * B; e += blockDim.x) {
+            const int a = e / B, b = e % B;
+            if (a > b) T[a][b] = T[b][a];
+        }
+        __syncthreads();
+        // (b) C and W = C T per row, and the new column -W (rows in K: zeros)
+        const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+        for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; i < n; i += warps) {
+            const bool in_k = i >= k0 && i < k0 + bk;
+            const double c = (!in_k && lane < bk) ? __ldcg(M + upper(i, k0 + lane, n)) : 0.0;
+            double w = 0.0;
+            for (int a = 0; a < bk; ++a) w = fma(__shfl_sync(0xffffffffu, c, a), T[a][lane], w);
+            Cs[i * B + lane] = c;
+            Ws[i * B + lane] = w;
+            if (!in_k && lane < bk) M[upper(i, k0 + lane, n)] = -w;
         }
         if (!grid_sync_bounded(bar, err)) return;
+        // (c) the upper tiles: M_IJ += W_I C_J^T
+        for (int64_t u = blockIdx.x; u < n_upper; u += gridDim.x) {
+            int64_t I = 0, off = 0;
+            while (off + (nt - I) <= u) off += nt - I, ++I;
+            const int64_t J = I + (u - off);
+            const int64_t i0 = I * B, j0 = J * B;
+            // tiles that lie inside the pivot rows or columns have nothing to update
+            const bool skip = (i0 >= k0 && i0 + B <= k0 + bk) || (j0 >= k0 && j0 + B <= k0 + bk);
+            if (skip) continue;
+            for (int e = threadIdx.x; e < B * B; e += blockDim.x) {
+                const int r = e / B, a = e % B;
+                sw[r][a] = i0 + r < n ? __ldcg(Ws + (i0 + r) * B + a) : 0.0;
+                sc[r][a] = j0 + r < n ? __ldcg(Cs + (j0 + r) * B + a) : 0.0;
+            }
+            __syncthreads();
+            const int64_t j = j0 + lane;
+            double acc[B * B / kST];
+#pragma unroll
+            for (int q = 0; q < B * B / kST; ++q) acc[q] = 0.0;
+            for (int a = 0; a < bk; ++a) {
+                const double cv = sc[lane][a];
+#pragma unroll
+                for (int q = 0; q < B * B / kST; ++q) acc[q] = fma(sw[warp + q * (kST / 32)][a], cv, acc[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < B * B / kST; ++q) {
+                const int64_t i = i0 + warp + q * (kST / 32);
+                const bool in_k = (i >= k0 && i < k0 + bk) || (j >= k0 && j < k0 + bk);
+                // coherent read: other blocks wrote this element (the new column, M_KK)
+                if (i < n && j < n && j >= i && !in_k) M[i * n + j] = __ldcg(M + i * n + j) + acc[q];
+            }
+            __syncthreads();
+        }
+        if (blockIdx.x == 0)
+            for (int e = threadIdx.x; e < bk * bk; e += blockDim.x) {
+                const int a = e / bk, b = e % bk;
+                if (a <= b) M[(k0 + a) * n + k0 + b] = T[a][b];
+            }
+        if (!grid_sync_bounded(bar, err)) return;
     }
+    // the inverse: -M, the lower triangle from the upper one first
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x)
+        for (int64_t j = threadIdx.x; j < i; j += blockDim.x) M[i * n + j] = -__ldcg(M + j * n + i);
+    if (!grid_sync_bounded(bar, err)) return;
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x)
+        for (int64_t j = i + threadIdx.x; j < n; j += blockDim.x) M[i * n + j] = -__ldcg(M + i * n + j);
 }
 
-// piv[0] = row 0 and column 0 of M (the first pivot's)
-__global__ void kc_first_pivot(int64_t n, const double *__restrict__ M, double *__restrict__ piv) {
-    FE_ROWS(j, n) {
-        piv[j] = M[j];
-        piv[n + j] = M[j * n];
-    }
-}
-
-int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
+int coarse_inverse_device(const DevCsr &C, DevAmg &G) {
+    const cudaStream_t s = G.mem.s;
     const int64_t n = C.n * C.rd;
     if (n > kMaxCoarse) {
         set_error("multigrid setup: coarsest level too large for its dense solve");
         return FE_BAD_INPUT;
     }
     G.nc = n;
-    FE_CHECK(dalloc(G.cinv, (size_t)std::max<int64_t>(n * n, 1)));
+    FE_CHECK(palloc(G.mem, G.cinv, (size_t)std::max<int64_t>(n * n, 1)));
     if (n == 0) return FE_OK;
-    DBuf<int> flag;   // [0] singular, [1] [2] the grid barrier, [3] its error word
-    DBuf<double> piv;   // the pivot row and column, two generations
-    FE_CHECK(dalloc(flag, 4));
-    FE_CHECK(dalloc(piv, (size_t)4 * n));
+    DBuf<int> flag;      // [0] singular, [1] [2] the grid barrier, [3] its error word
+    DBuf<double> cw;     // the C and W panels, n x kSweepB each
     struct Free {
+        const MgMem &m;
         DBuf<int> &f;
         DBuf<double> &p;
-        ~Free() { dfree(f), dfree(p); }
-    } fr{flag, piv};
+        ~Free() { pfree(m, f), pfree(m, p); }
+    } fr{G.mem, flag, cw};
+    FE_CHECK(palloc(G.mem, flag, 4));
+    FE_CHECK(palloc(G.mem, cw, (size_t)2 * n * kSweepB));
     FE_CUDA(cudaMemsetAsync(flag.p, 0, 4 * sizeof(int), s));
     FE_CUDA(cudaMemsetAsync(G.cinv.p, 0, (size_t)n * n * sizeof(double), s));
     kc_dense_fill<<<grid_s(C.n), kST, 0, s>>>(C.n, C.rd, C.ptr.p, C.col.p, C.val.p, n, G.cinv.p);
     kc_regularise<<<1, kST, 0, s>>>(n, G.cinv.p);
-    kc_first_pivot<<<grid_s(n), kST, 0, s>>>(n, G.cinv.p, piv.p);
     FE_LAUNCH_CHECK();
-    // the cooperative grid: every SM's resident blocks of the kernel
+    // the cooperative grid: at most two blocks per SM (more add barrier arrivals, and
+    // the 32 x 32 tiles of one update number about (n / 32)^2 / 2)
     int dev = 0, sms = 0, per_sm = 0;
     FE_CUDA(cudaGetDevice(&dev));
     FE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)kc_gauss_jordan, kST, 0));
-    // a block per row (as many as fit): measured 40 ms for the 1941-DOF coarsest level of
-    // the 4M-DOF benchmark system, against 66 ms on two blocks per SM
-    const int64_t want = n;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1)));
+    FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)kc_sweep, kST, 0));
+    if (per_sm < 1) {
+        set_error("multigrid setup: the coarsest inverse kernel does not fit on an SM");
+        return FE_CUDA_ERR;
+    }
+    const int grid = sms * std::min(per_sm, 2);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kST);
@@ -758,8 +845,8 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    FE_CUDA(cudaLaunchKernelEx(&cfg, kc_gauss_jordan, n, G.cinv.p, piv.p, (unsigned *)(flag.p + 1), flag.p + 3,
-                               flag.p));
+    FE_CUDA(cudaLaunchKernelEx(&cfg, kc_sweep, n, G.cinv.p, cw.p, cw.p + n * kSweepB, (unsigned *)(flag.p + 1),
+                               flag.p + 3, flag.p));
     int host[4] = {0, 0, 0, 0};
     FE_CUDA(cudaMemcpyAsync(host, flag.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
@@ -768,7 +855,7 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
         return FE_CUDA_ERR;
     }
     if (host[0]) {
-        set_error("multigrid setup: singular coarsest matrix");
+        set_error("multigrid setup: the coarsest matrix is not positive definite");
         return FE_BREAKDOWN;
     }
     return FE_OK;
@@ -776,9 +863,32 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G, cudaStream_t s) {
 
 }  // namespace
 
+int mg_memory(fe_handle_s *h, MgMem *out) {
+    if (!h->mg_pool) {
+        int dev = 0;
+        FE_CUDA(cudaGetDevice(&dev));
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        FE_CUDA(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = ~0ull;
+        if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+            cudaMemPoolDestroy(pool);
+            set_error("multigrid: cannot set the memory pool's release threshold");
+            return FE_CUDA_ERR;
+        }
+        h->mg_pool = pool;
+    }
+    out->s = h->stream;
+    out->pool = h->mg_pool;
+    return FE_OK;
+}
+
 int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &G, SetupTrace *trace) {
-    cudaStream_t s = h->stream;
-    DevEx ex(s);
+    FE_CHECK(mg_memory(h, &G.mem));
+    DevEx ex(G.mem);
     ex.trace = trace;
     ex.phase(amg::kPhaseInput);
     const int D = h->dim;
@@ -790,20 +900,22 @@ int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &
     DBuf<double> B;
     A.n = n0, A.rd = A.cd = D, A.nnzb = h->nnzb;
     int st = FE_OK;
-    if ((st = dalloc(A.ptr, (size_t)n0 + 1)) || (st = dalloc(A.col, (size_t)std::max<int64_t>(h->nnzb, 1))) ||
-        (st = dalloc(A.val, (size_t)std::max<int64_t>(h->nnzb * D * D, 1))) ||
-        (st = dalloc(B, (size_t)std::max<int64_t>(n0 * D * m, 1))) ||
+    if ((st = palloc(G.mem, A.ptr, (size_t)n0 + 1)) ||
+        (st = palloc(G.mem, A.col, (size_t)std::max<int64_t>(h->nnzb, 1))) ||
+        (st = palloc(G.mem, A.val, (size_t)std::max<int64_t>(h->nnzb * D * D, 1))) ||
+        (st = palloc(G.mem, B, (size_t)std::max<int64_t>(n0 * D * m, 1))) ||
         (st = ex.rows(n0 + 1, PassPtr64{h->blk_ptr.p, A.ptr.p})) ||
         (st = ex.copy(A.col.p, h->blk_col.p, (size_t)h->nnzb)) ||
         (st = ex.copy(A.val.p, h->aval.p, (size_t)(h->nnzb * D * D))) ||
         (st = ex.rows(n0, PassNullspace{D, h->cdim, m, h->coords.p, B.p})) ||
         (st = ex.rows(h->n_bc, PassZeroRows{h->bc_dof.p, m, B.p}))) {
-        drelease(A);
-        dfree(B);
+        drelease(G.mem, A);
+        pfree(G.mem, B);
         return st;
     }
     std::vector<amg::Level> levels;
-    st = amg::setup_hierarchy(ex, A, B, m, theta, coarse_dofs, levels, G.coarse, &G.mis_rounds);
+    // level 0's D^-1: the node-block Jacobi inverse of the assembly
+    st = amg::setup_hierarchy(ex, A, B, m, theta, coarse_dofs, levels, G.coarse, &G.mis_rounds, h->dinv.p);
     // the levels move into G (released with it, also after a failure)
     for (auto &l : levels) {
         DevLevel L;
@@ -813,7 +925,7 @@ int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &
     FE_CHECK(st);
     // coarsest level: its dense inverse, on the device
     ex.phase(amg::kPhaseCoarse);
-    return coarse_inverse_device(G.coarse, G, s);
+    return coarse_inverse_device(G.coarse, G);
 }
 
 int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s) {

@@ -137,11 +137,15 @@ FE_HD void sym_pinv(const double *a, int d, double *out) {
     }
 }
 
-// y_i = D_i^-1 (A x)_i (d x d blocks)
+// y_i = D_i^-1 (A x)_i (d x d blocks); y = A x when dinv is null
 FE_HD void row_dinv_product(const int64_t *ptr, const int32_t *col, const double *val, const double *dinv, int d,
                             const double *x, int64_t i, double *y) {
     double acc[6];
     row_product(ptr, col, val, d, d, x, i, acc);
+    if (!dinv) {   // y = A x
+        for (int a = 0; a < d; ++a) y[i * d + a] = acc[a];
+        return;
+    }
     for (int a = 0; a < d; ++a) {
         double v = 0.0;
         for (int k = 0; k < d; ++k) v += dinv[i * d * d + a * d + k] * acc[k];

@@ -87,22 +87,47 @@ struct PassDinv {
     }
 };
 
+// the start vector of the eigenvalue estimate, 1 + (i mod 7) / 7
 struct PassPowerStart {
     double *x;
     FE_HD void operator()(int64_t i) const { x[i] = 1.0 + (double)(i % 7) / 7.0; }
 };
 
-// nnzb: the matrix's block count (a device executor sizes its lanes per row with it)
+// y = D^-1 A x (y = A x when dinv is null); nnzb: the matrix's block count (a device
+// executor sizes its lanes per row with it)
 struct PassDinvProduct {
     const int64_t *ptr; const int32_t *col; const double *val; const double *dinv; int d; const double *x; double *y;
     int64_t nnzb;
     FE_HD void operator()(int64_t i) const { row_dinv_product(ptr, col, val, dinv, d, x, i, y); }
 };
 
-struct PassScale {
-    const double *y; double c; double *x;
-    FE_HD void operator()(int64_t i) const { x[i] = y[i] * c; }
+// z_i = D_i^-1 r_i
+struct PassJacobi {
+    const double *dinv; int d; const double *r; double *z;
+    FE_HD void operator()(int64_t i) const {
+        for (int a = 0; a < d; ++a) {
+            double v = 0.0;
+            for (int k = 0; k < d; ++k) v += dinv[i * d * d + a * d + k] * r[i * d + k];
+            z[i * d + a] = v;
+        }
+    }
 };
+
+// r_i -= alpha q_i, then z_i = D_i^-1 r_i
+struct PassCgStep {
+    double alpha; const double *q; const double *dinv; int d; double *r; double *z;
+    FE_HD void operator()(int64_t i) const {
+        for (int a = 0; a < d; ++a) r[i * d + a] -= alpha * q[i * d + a];
+        PassJacobi{dinv, d, r, z}(i);
+    }
+};
+
+// p = z + beta p
+struct PassCgDirection {
+    double beta; const double *z; double *p;
+    FE_HD void operator()(int64_t i) const { p[i] = z[i] + beta * p[i]; }
+};
+
 
 struct PassBlockNorms {
     const int64_t *ptr; const int32_t *col; const double *val; int d; double *nrm; double *dg;
@@ -299,34 +324,54 @@ int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W) {
     return FE_OK;
 }
 
-// largest eigenvalue of D^-1 A: 30 power iterations from 1 + (i mod 7) / 7, then the
-// Rayleigh quotient
+// Largest eigenvalue of D^-1 A from the Lanczos matrix of kLanczosSteps iterations of
+// CG on A x = b preconditioned by D^-1, b_i = 1 + (i mod 7) / 7: the CG coefficients
+// alpha_j, beta_j give the tridiagonal matrix (diagonal 1/alpha_j + beta_{j-1} /
+// alpha_{j-1}, off-diagonal sqrt(beta_j) / alpha_j; Saad, Iterative Methods for Sparse
+// Linear Systems, 6.7.3), whose largest eigenvalue lanczos_lmax finds.  Its Ritz value
+// approaches lmax from below far faster than power iteration does.
+constexpr int kLanczosSteps = 15;
+
 template <class Ex>
 int lmax_of(Ex &ex, const Csr &A, const double *dinv, double *lmax) {
     const int d = A.rd;
     const int64_t nd = A.n * d;
-    DBuf<double> x, y;
+    DBuf<double> r, z, p, q;
     struct Free {
         Ex &ex;
-        DBuf<double> &x, &y;
-        ~Free() { ex.release(x), ex.release(y); }
-    } fr{ex, x, y};
-    FE_CHECK(ex.alloc(x, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(ex.alloc(y, (size_t)std::max<int64_t>(nd, 1)));
-    FE_CHECK(ex.rows(nd, PassPowerStart{x.p}));
-    const PassDinvProduct prod{A.ptr.p, A.col.p, A.val.p, dinv, d, x.p, y.p, A.nnzb};
-    for (int it = 0; it < 30; ++it) {
+        DBuf<double> &r, &z, &p, &q;
+        ~Free() { ex.release(r), ex.release(z), ex.release(p), ex.release(q); }
+    } fr{ex, r, z, p, q};
+    const size_t v = (size_t)std::max<int64_t>(nd, 1);
+    FE_CHECK(ex.alloc(r, v));
+    FE_CHECK(ex.alloc(z, v));
+    FE_CHECK(ex.alloc(p, v));
+    FE_CHECK(ex.alloc(q, v));
+    FE_CHECK(ex.rows(nd, PassPowerStart{r.p}));
+    FE_CHECK(ex.rows(A.n, PassJacobi{dinv, d, r.p, z.p}));
+    FE_CHECK(ex.copy(p.p, z.p, (size_t)nd));
+    double rz = 0.0;
+    FE_CHECK(ex.dot(r.p, z.p, nd, &rz));
+    const double rz0 = rz;
+    double alpha[kLanczosSteps], beta[kLanczosSteps];
+    int m = 0;
+    const PassDinvProduct prod{A.ptr.p, A.col.p, A.val.p, nullptr, d, p.p, q.p, A.nnzb};
+    for (int j = 0; j < kLanczosSteps && rz > 0.0; ++j) {
         FE_CHECK(ex.rows(A.n, prod));
-        double yy = 0.0;
-        FE_CHECK(ex.dot(y.p, y.p, nd, &yy));
-        if (!(yy > 0.0)) break;
-        FE_CHECK(ex.rows(nd, PassScale{y.p, 1.0 / std::sqrt(yy), x.p}));
+        double pq = 0.0;
+        FE_CHECK(ex.dot(p.p, q.p, nd, &pq));
+        if (!(pq > 0.0) || !std::isfinite(pq)) break;
+        alpha[m] = rz / pq;
+        FE_CHECK(ex.rows(A.n, PassCgStep{alpha[m], q.p, dinv, d, r.p, z.p}));
+        double rzn = 0.0;
+        FE_CHECK(ex.dot(r.p, z.p, nd, &rzn));
+        beta[m] = rzn / rz;
+        ++m;
+        rz = rzn;
+        if (!(rzn > 1e-28 * rz0)) break;   // converged: the Krylov space is exhausted
+        if (j + 1 < kLanczosSteps) FE_CHECK(ex.rows(nd, PassCgDirection{beta[m - 1], z.p, p.p}));
     }
-    FE_CHECK(ex.rows(A.n, prod));
-    double num = 0.0, den = 0.0;
-    FE_CHECK(ex.dot(x.p, y.p, nd, &num));
-    FE_CHECK(ex.dot(x.p, x.p, nd, &den));
-    *lmax = num / den;
+    *lmax = m > 0 ? lanczos_lmax(alpha, beta, m) : 0.0;
     if (!std::isfinite(*lmax) || !(*lmax > 0.0)) {
         set_error("multigrid setup: the largest eigenvalue estimate is not positive");
         return FE_BREAKDOWN;
@@ -336,9 +381,10 @@ int lmax_of(Ex &ex, const Csr &A, const double *dinv, double *lmax) {
 
 // The hierarchy of A (consumed) with near-null space B (n d x m, consumed): levels down
 // to at most coarse_dofs DOFs (or 12 levels); the coarsest operator in `coarse`.
+// dinv0: level 0's block-diagonal inverse when the caller has it already.
 template <class Ex>
 int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t coarse_dofs, std::vector<Level> &levels,
-                    Csr &coarse, int *mis_rounds) {
+                    Csr &coarse, int *mis_rounds, const double *dinv0 = nullptr) {
     const int kMaxRounds = 256;
     DBuf<double> Bc, nrm, dg;
     DBuf<uint8_t> strong;
@@ -377,7 +423,10 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
         const int64_t n = A.n;
         ex.phase(kPhaseDiag);
         FE_CHECK(ex.alloc(L.dinv, (size_t)std::max<int64_t>(n * dd * dd, 1)));
-        FE_CHECK(ex.rows(n, PassDinv{A.ptr.p, A.col.p, A.val.p, dd, L.dinv.p}));
+        if (levels.empty() && dinv0)
+            FE_CHECK(ex.copy(L.dinv.p, dinv0, (size_t)(n * dd * dd)));
+        else
+            FE_CHECK(ex.rows(n, PassDinv{A.ptr.p, A.col.p, A.val.p, dd, L.dinv.p}));
         FE_CHECK(lmax_of(ex, A, L.dinv.p, &L.lmax));
         // strength and the distance-2 independent set
         ex.phase(kPhaseAggregate);

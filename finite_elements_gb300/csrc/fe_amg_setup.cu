@@ -12,8 +12,8 @@
 //                 non-negative diag(R), dropped columns kept as zeros); R is the
 //                 coarse near-null space
 //   P             (I - 4/(3 lmax) D^-1 A) P_tent, D^-1 the block-diagonal
-//                 pseudo-inverse, lmax of D^-1 A by 30 power iterations from
-//                 x_i = 1 + (i mod 7) / 7
+//                 pseudo-inverse, lmax of D^-1 A from 15 CG-Lanczos steps from
+//                 b_i = 1 + (i mod 7) / 7
 //   A_c           P^T A P, m x m blocks
 // down to at most `coarse_dofs` DOFs (or 12 levels).  Host code only: no device call.
 #include <algorithm>
@@ -72,63 +72,58 @@ std::vector<double> block_diag_pinv(const BlockCsr &A) {
     return dinv;
 }
 
-// y_i = D_i^-1 (A x)_i for the rows of one chunk (D block rows of size D; DD the
-// compile-time block size when known, else 0)
-template <int DD>
-void dinv_spmv_rows(const BlockCsr &A, const std::vector<double> &dinv, const double *x, double *y, int64_t lo,
-                    int64_t hi) {
-    const int d = DD > 0 ? DD : A.rd;
-    double acc[6], t[6];
-    for (int64_t i = lo; i < hi; ++i) {
-        for (int a = 0; a < d; ++a) acc[a] = 0.0;
-        for (int64_t s = A.ptr[i]; s < A.ptr[i + 1]; ++s) {
-            const double *b = &A.val[(size_t)s * d * d];
-            const double *xc = x + (size_t)A.col[s] * d;
-            for (int a = 0; a < d; ++a)
-                for (int k = 0; k < d; ++k) acc[a] += b[a * d + k] * xc[k];
-        }
-        const double *di = &dinv[(size_t)i * d * d];
-        for (int a = 0; a < d; ++a) {
-            double v = 0.0;
-            for (int k = 0; k < d; ++k) v += di[a * d + k] * acc[k];
-            t[a] = v;
-        }
-        for (int a = 0; a < d; ++a) y[(size_t)i * d + a] = t[a];
-    }
-}
-
-// Largest eigenvalue of D^-1 A: 30 power iterations from x_i = 1 + (i mod 7) / 7, then
-// the Rayleigh quotient; sums are taken per chunk and added in chunk order.
-double lmax_power(const BlockCsr &A, const std::vector<double> &dinv) {
+// Largest eigenvalue of D^-1 A: the Lanczos matrix of amg::kLanczosSteps CG iterations
+// on A x = b preconditioned by D^-1, b_i = 1 + (i mod 7) / 7 (the sequence of
+// amg::lmax_of); sums are taken per chunk and added in chunk order.
+double lmax_lanczos(const BlockCsr &A, const std::vector<double> &dinv) {
     const int d = A.rd;
-    const int64_t nd = A.n * d;
-    std::vector<double> x((size_t)nd), y((size_t)nd);
-    for (int64_t i = 0; i < nd; ++i) x[i] = 1.0 + (double)(i % 7) / 7.0;
-    double part[kChunks], part2[kChunks];
-    auto step = [&]() {
-        parallel_chunks(A.n, [&](int64_t lo, int64_t hi, int c) {
-            if (d == 2) dinv_spmv_rows<2>(A, dinv, x.data(), y.data(), lo, hi);
-            else if (d == 3) dinv_spmv_rows<3>(A, dinv, x.data(), y.data(), lo, hi);
-            else dinv_spmv_rows<0>(A, dinv, x.data(), y.data(), lo, hi);
-            double a = 0.0, b = 0.0;
-            for (int64_t k = lo * d; k < hi * d; ++k) a += y[k] * y[k], b += x[k] * y[k];
-            part[c] = a, part2[c] = b;
-        });
+    const int64_t n = A.n, nd = n * d;
+    std::vector<double> r((size_t)nd), z((size_t)nd), p((size_t)nd), q((size_t)nd);
+    for (int64_t i = 0; i < nd; ++i) r[i] = 1.0 + (double)(i % 7) / 7.0;
+    auto jacobi = [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) amg::PassJacobi{dinv.data(), d, r.data(), z.data()}(i);
     };
-    for (int it = 0; it < 30; ++it) {
-        step();
-        double nrm = 0.0;
-        for (int c = 0; c < kChunks; ++c) nrm += part[c];
-        nrm = std::sqrt(nrm);
+    auto dot = [&](const std::vector<double> &a, const std::vector<double> &b) {
+        double part[kChunks];
+        parallel_chunks(nd, [&](int64_t lo, int64_t hi, int c) {
+            double t = 0.0;
+            for (int64_t k = lo; k < hi; ++k) t += a[k] * b[k];
+            part[c] = t;
+        });
+        double t = 0.0;
+        for (int c = 0; c < kChunks; ++c) t += part[c];
+        return t;
+    };
+    parallel_chunks(n, [&](int64_t lo, int64_t hi, int) { jacobi(lo, hi); });
+    p = z;
+    double rz = dot(r, z);
+    const double rz0 = rz;
+    double alpha[amg::kLanczosSteps], beta[amg::kLanczosSteps];
+    int m = 0;
+    for (int j = 0; j < amg::kLanczosSteps && rz > 0.0; ++j) {
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i)
+                amg::row_dinv_product(A.ptr.data(), A.col.data(), A.val.data(), nullptr, d, p.data(), i, q.data());
+        });
+        const double pq = dot(p, q);
+        if (!(pq > 0.0) || !std::isfinite(pq)) break;
+        const double a = rz / pq;
+        alpha[m] = a;
+        parallel_chunks(n, [&](int64_t lo, int64_t hi, int) {
+            for (int64_t i = lo; i < hi; ++i)
+                amg::PassCgStep{a, q.data(), dinv.data(), d, r.data(), z.data()}(i);
+        });
+        const double rzn = dot(r, z);
+        beta[m] = rzn / rz;
+        ++m;
+        rz = rzn;
+        if (!(rzn > 1e-28 * rz0)) break;
+        const double b = beta[m - 1];
         parallel_chunks(nd, [&](int64_t lo, int64_t hi, int) {
-            for (int64_t k = lo; k < hi; ++k) x[k] = y[k] / nrm;
+            for (int64_t k = lo; k < hi; ++k) p[k] = z[k] + b * p[k];
         });
     }
-    step();
-    double num = 0.0, den = 0.0;
-    for (int c = 0; c < kChunks; ++c) num += part2[c];
-    for (int64_t i = 0; i < nd; ++i) den += x[i] * x[i];
-    return num / den;
+    return m > 0 ? lanczos_lmax(alpha, beta, m) : 0.0;
 }
 
 std::vector<int32_t> aggregate(const BlockCsr &A, double theta, int32_t *n_agg) {
@@ -562,7 +557,7 @@ int fe_amg_build_host(int64_t n_nodes, int32_t d, const int64_t *blk_ptr, const 
         AmgLevel L;
         const int dd = A.rd;
         std::vector<double> dinv = block_diag_pinv(A);
-        L.lmax = lmax_power(A, dinv);
+        L.lmax = lmax_lanczos(A, dinv);
         int32_t na = 0;
         L.agg = aggregate(A, theta, &na);
         // tentative prolongator and coarse near-null space

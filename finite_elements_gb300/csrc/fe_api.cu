@@ -148,6 +148,7 @@ int fe_destroy(fe_handle h) {
     for (auto &e : h->events)
         if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->mg_pool) cudaMemPoolDestroy(h->mg_pool);
     delete h;
     return FE_OK;
 }

@@ -223,6 +223,9 @@ struct fe_handle_s {
     // values
     bool k_ready = false, m_ready = false, f_ready = false, sys_ready = false;
     uint64_t sys_generation = 0;   // counts the system matrices built (build_system)
+    // memory pool of the multigrid solve's stream-ordered allocations (kept between
+    // solves; created on first use)
+    cudaMemPool_t mg_pool = nullptr;
     bool singular = false;                // a diagonal block could not be inverted
     fe::DBuf<double> ke;                  // [n_elem][(3d)^2]
     fe::DBuf<double> me_scale;            // [n_elem] rho*A*t/12

@@ -15,7 +15,8 @@ Computing 56, 1996):
 * tentative prolongator: per aggregate, the QR factors of the near-null space (the
   rigid-body modes: two translations and the rotation (-y, x) in 2D) restricted to
   its DOFs; the R factors are the coarse near-null space;
-* smoothed prolongator P = (I - 4/(3 lmax) D^-1 A) P_tent, D the block diagonal;
+* smoothed prolongator P = (I - 4/(3 lmax) D^-1 A) P_tent, D the block diagonal, lmax
+  the largest eigenvalue of D^-1 A from 15 Lanczos steps (lmax_lanczos);
 * Galerkin coarse operators P^T A P down to a few hundred DOFs, solved directly;
 * V-cycle with Chebyshev(k) pre- and post-smoothing on D^-1 A, interval
   [lmax/30, 1.05 lmax].
@@ -53,6 +54,45 @@ def lmax_power(A, Minv, it=30):
         x = Minv @ (A @ x)
         x /= np.linalg.norm(x)
     return float(x @ (Minv @ (A @ x)) / (x @ x))
+
+
+def lmax_lanczos(A, Minv, steps=15):
+    """Largest eigenvalue of Minv A from the Lanczos matrix of `steps` iterations of CG
+    on A x = b preconditioned by Minv, b = power_start (the coefficients alpha_j, beta_j
+    give T with diagonal 1/alpha_j + beta_{j-1}/alpha_{j-1} and off-diagonal
+    sqrt(beta_j)/alpha_j; Saad, Iterative Methods for Sparse Linear Systems, 6.7.3).
+    Stops early when p.Ap or r.z vanish."""
+    r = power_start(A.shape[0])
+    z = Minv @ r
+    p = z.copy()
+    rz = float(r @ z)
+    rz0 = rz
+    al, be = [], []
+    for j in range(steps):
+        if not rz > 0:
+            break
+        q = A @ p
+        pq = float(p @ q)
+        if not (pq > 0 and np.isfinite(pq)):
+            break
+        alpha = rz / pq
+        al.append(alpha)
+        r = r - alpha * q
+        z = Minv @ r
+        rzn = float(r @ z)
+        be.append(rzn / rz)
+        rz = rzn
+        if j + 1 < steps:
+            p = z + be[-1] * p
+        if not rzn > 1e-28 * rz0:
+            break
+    m = len(al)
+    if m == 0:
+        raise ValueError("lmax_lanczos: no Lanczos step")
+    dg = np.array([1.0 / al[j] + (be[j - 1] / al[j - 1] if j > 0 else 0.0) for j in range(m)])
+    off = np.array([np.sqrt(max(be[j], 0.0)) / al[j] for j in range(m - 1)])
+    T = np.diag(dg) + np.diag(off, 1) + np.diag(off, -1)
+    return float(np.linalg.eigvalsh(T)[-1])
 
 
 def chebyshev(A, Minv, lmax, ratio, k):
@@ -157,7 +197,7 @@ class SmoothedAggregation:
         A = A.tocsr()
         while A.shape[0] > coarse and len(self.levels) < 12:
             Minv = block_diag_inv(A, d)
-            lm = lmax_power(A, Minv)
+            lm = lmax_lanczos(A, Minv)
             agg, na = aggregate(A, d, theta)
             Pt, Bc = tentative(agg, na, B, d)
             P = (Pt - (4.0 / (3.0 * lm)) * (Minv @ (A @ Pt))).tocsr()

@@ -162,7 +162,7 @@ def test_operators_match_the_model_on_the_same_aggregates(case):
         Al, Bl, dl = A, B, d
         for l, lev in enumerate(levels[:-1]):
             Minv = AMG.block_diag_inv(Al, dl)
-            lm = AMG.lmax_power(Al, Minv)
+            lm = AMG.lmax_lanczos(Al, Minv)
             assert abs(lev["lmax"] - lm) <= 1e-10 * lm
             assert abs(lev["A"] - Al).max() <= 1e-10 * abs(Al).max()
             agg = lev["agg"].astype(np.int64)

@@ -79,3 +79,44 @@ def test_device_setup_matches_the_host_passes(gpu_lib, name):
         if h.value:
             lib.fe_amg_destroy(h)
         s.close()
+
+
+@pytest.mark.parametrize("name", ["plane_strain", "tet", "magnetic"])
+def test_device_coarsest_inverse_is_the_inverse(gpu_lib, name):
+    """With a coarsest size above the system's, the device hierarchy has no level and its
+    coarsest inverse is that of the whole system (3782, 624 and 1891 DOFs: 119, 20 and
+    60 block sweeps of 32 pivots, the last ones partial): the V-cycle is then x = A^-1 r
+    for A with 1e-12 of its largest diagonal entry added to the diagonal (which moves
+    the identity rows of the constrained DOFs), checked by its residual and symmetry."""
+    import ctypes
+
+    from finite_elements_gb300 import _lib
+    from finite_elements_gb300.engine import GpuSystem
+    from test_amg_parallel_host import read_levels
+    prob = _problems()[name]()
+    s = GpuSystem(prob)
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    try:
+        _lib.check(lib.fe_amg_build_device(s.handle.h, 0.08, 1 << 20, ctypes.byref(h)), "fe_amg_build_device")
+        levels = read_levels(lib, h)
+        assert len(levels) == 1
+        import scipy.sparse as sp
+        A = levels[0]["A"].tocsr()
+        A = (A + 1e-12 * abs(A.diagonal()).max() * sp.eye(A.shape[0])).tocsr()
+        rng = np.random.default_rng(2)
+        r1, r2 = rng.standard_normal(A.shape[0]), rng.standard_normal(A.shape[0])
+
+        def apply(v):
+            v = np.ascontiguousarray(v)
+            out = np.empty_like(v)
+            _lib.check(lib.fe_amg_vcycle_host(h, 3, _lib.ptr(v), _lib.ptr(out)), "fe_amg_vcycle_host")
+            return out
+        x1, x2 = apply(r1), apply(r2)
+        assert np.linalg.norm(A @ x1 - r1) <= 1e-9 * np.linalg.norm(r1)
+        assert np.linalg.norm(A @ x2 - r2) <= 1e-9 * np.linalg.norm(r2)
+        assert abs(r2 @ x1 - r1 @ x2) <= 1e-12 * abs(r1) @ abs(x2)
+    finally:
+        if h.value:
+            lib.fe_amg_destroy(h)
+        s.close()
