@@ -507,6 +507,10 @@ struct DevEx {
     DBuf<int64_t> scan_tmp;
     DBuf<double> part, sc;
     SetupTrace *trace = nullptr;
+    // level 0's operator is the handle's eliminated system: its plain products run on
+    // the handle's FP64 SELL copy
+    fe_handle_s *h = nullptr;
+    const int64_t *sell_ptr = nullptr;
     explicit DevEx(const MgMem &m) : mem(m), s(m.s) {}
     void phase(int k) {
         if (trace) trace->mark(s, k);
@@ -537,6 +541,7 @@ struct DevEx {
     // the power iterations' product with lanes per row; other block sizes row by row
     int rows(int64_t n, const amg::PassDinvProduct &f) {
         if (n <= 0) return FE_OK;
+        if (!f.dinv && h && f.ptr == sell_ptr) return spmv64(h, f.x, f.y);
         switch (f.d) {
             case 1: return launch_dinv_product<1>(n, f, s);
             case 2: return launch_dinv_product<2>(n, f, s);
@@ -890,6 +895,7 @@ int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &
     FE_CHECK(mg_memory(h, &G.mem));
     DevEx ex(G.mem);
     ex.trace = trace;
+    ex.h = h;
     ex.phase(amg::kPhaseInput);
     const int D = h->dim;
     const int64_t n0 = h->n_nodes;
@@ -913,6 +919,7 @@ int amg_setup_device(fe_handle_s *h, double theta, int64_t coarse_dofs, DevAmg &
         pfree(G.mem, B);
         return st;
     }
+    ex.sell_ptr = A.ptr.p;
     std::vector<amg::Level> levels;
     // level 0's D^-1: the node-block Jacobi inverse of the assembly
     st = amg::setup_hierarchy(ex, A, B, m, theta, coarse_dofs, levels, G.coarse, &G.mis_rounds, h->dinv.p);

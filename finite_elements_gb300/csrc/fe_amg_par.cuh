@@ -90,50 +90,66 @@ FE_HD int64_t find_sorted(const int32_t *a, int64_t lo, int64_t hi, int32_t v) {
 
 // ------------------------------------------------------------------ block inverses
 
-// Pseudo-inverse of a symmetric d x d block by cyclic Jacobi: V diag(1/l) V^T over the
-// eigenvalues above 1e-12 of the largest in magnitude.
-FE_HD void sym_pinv(const double *a, int d, double *out) {
-    double A[36], V[36];
-    for (int i = 0; i < d * d; ++i) A[i] = a[i];
-    for (int i = 0; i < d; ++i)
-        for (int j = 0; j < d; ++j) V[i * d + j] = i == j ? 1.0 : 0.0;
+// Pseudo-inverse of a symmetric D x D block by cyclic Jacobi: V diag(1/l) V^T over the
+// eigenvalues above 1e-12 of the largest in magnitude.  D is a template argument so
+// that the block and its eigenvectors stay in registers.
+template <int D>
+FE_HD void sym_pinv_n(const double *a, double *out) {
+    double A[D * D], V[D * D];
+    for (int i = 0; i < D * D; ++i) A[i] = a[i];
+    for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) V[i * D + j] = i == j ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0.0;
-        for (int p = 0; p < d; ++p)
-            for (int q = p + 1; q < d; ++q) off += A[p * d + q] * A[p * d + q];
+        for (int p = 0; p < D; ++p)
+            for (int q = p + 1; q < D; ++q) off += A[p * D + q] * A[p * D + q];
         if (off < 1e-30) break;
-        for (int p = 0; p < d; ++p)
-            for (int q = p + 1; q < d; ++q) {
-                const double apq = A[p * d + q];
+        for (int p = 0; p < D; ++p)
+            for (int q = p + 1; q < D; ++q) {
+                const double apq = A[p * D + q];
                 if (apq == 0.0) continue;
-                const double th = (A[q * d + q] - A[p * d + p]) / (2.0 * apq);
+                const double th = (A[q * D + q] - A[p * D + p]) / (2.0 * apq);
                 const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
                 const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < d; ++k) {
-                    const double akp = A[k * d + p], akq = A[k * d + q];
-                    A[k * d + p] = c * akp - s * akq;
-                    A[k * d + q] = s * akp + c * akq;
+                for (int k = 0; k < D; ++k) {
+                    const double akp = A[k * D + p], akq = A[k * D + q];
+                    A[k * D + p] = c * akp - s * akq;
+                    A[k * D + q] = s * akp + c * akq;
                 }
-                for (int k = 0; k < d; ++k) {
-                    const double apk = A[p * d + k], aqk = A[q * d + k];
-                    A[p * d + k] = c * apk - s * aqk;
-                    A[q * d + k] = s * apk + c * aqk;
+                for (int k = 0; k < D; ++k) {
+                    const double apk = A[p * D + k], aqk = A[q * D + k];
+                    A[p * D + k] = c * apk - s * aqk;
+                    A[q * D + k] = s * apk + c * aqk;
                 }
-                for (int k = 0; k < d; ++k) {
-                    const double vkp = V[k * d + p], vkq = V[k * d + q];
-                    V[k * d + p] = c * vkp - s * vkq;
-                    V[k * d + q] = s * vkp + c * vkq;
+                for (int k = 0; k < D; ++k) {
+                    const double vkp = V[k * D + p], vkq = V[k * D + q];
+                    V[k * D + p] = c * vkp - s * vkq;
+                    V[k * D + q] = s * vkp + c * vkq;
                 }
             }
     }
     double lmax = 0.0;
-    for (int i = 0; i < d; ++i) lmax = fabs(A[i * d + i]) > lmax ? fabs(A[i * d + i]) : lmax;
-    for (int i = 0; i < d * d; ++i) out[i] = 0.0;
-    for (int k = 0; k < d; ++k) {
-        const double l = A[k * d + k];
+    for (int i = 0; i < D; ++i) lmax = fabs(A[i * D + i]) > lmax ? fabs(A[i * D + i]) : lmax;
+    for (int i = 0; i < D * D; ++i) out[i] = 0.0;
+    for (int k = 0; k < D; ++k) {
+        const double l = A[k * D + k];
         if (fabs(l) <= 1e-12 * lmax || l == 0.0) continue;
-        for (int i = 0; i < d; ++i)
-            for (int j = 0; j < d; ++j) out[i * d + j] += V[i * d + k] * V[j * d + k] / l;
+        for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j) out[i * D + j] += V[i * D + k] * V[j * D + k] / l;
+    }
+}
+
+// the same for the block sizes of the hierarchies (1, 2, 3, 6); other sizes get zeros
+FE_HD void sym_pinv(const double *a, int d, double *out) {
+    switch (d) {
+        case 1: sym_pinv_n<1>(a, out); return;
+        case 2: sym_pinv_n<2>(a, out); return;
+        case 3: sym_pinv_n<3>(a, out); return;
+        case 4: sym_pinv_n<4>(a, out); return;
+        case 5: sym_pinv_n<5>(a, out); return;
+        case 6: sym_pinv_n<6>(a, out); return;
+        default:
+            for (int i = 0; i < d * d; ++i) out[i] = 0.0;
     }
 }
 
