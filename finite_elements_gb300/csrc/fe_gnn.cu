@@ -19,8 +19,8 @@
 //   L = 1 - (u_hat . b~)^2 / ((u_hat . A u_hat) (b~ . v*)),  v* = u* - g,
 // so training needs only b~ . v* from a solve of the problem.
 //
-// The dense transforms run as BF16 tensor-core MMAs (mma.sync m16n8k16, FP32
-// accumulation) with FP32 master weights and activations; aggregation, reductions,
+// The dense transforms run as BF16 tcgen05 MMAs with FP32 accumulators in tensor
+// memory, FP32 master weights and activations; aggregation, reductions,
 // loss and Adam are FP32 / FP64 CUDA-core kernels.  Elasticity meshes only.
 #include <cuda_bf16.h>
 #include <math.h>
@@ -57,164 +57,316 @@ constexpr int kT = 256;
 
 inline int g1(int64_t n, int t = kT) { return grid_for(n, t, 152 * 8); }
 
-// ---------------------------------------------------------------- tensor-core GEMM
-// Y[N x NO] = X[N x KI] W[KI x NO], X given as two row-major FP32 halves (columns
-// [0, K1) from X1 and [K1, KI) from X2), W given transposed in BF16 (Wt[n][k]).
-// 4 warps per block, 64 rows per tile, each warp 16 rows x NO columns.
+// ---------------------------------------------------------------- tensor-core GEMMs
+// The dense transforms on the 5th-generation tensor cores: BF16 x BF16 -> FP32
+// tcgen05.mma (kind::f16, cta_group::1, M = 128) with the accumulator in tensor memory.
+// Both operands are staged by the block's threads (the FP32 activations are rounded to
+// BF16 on the way) into shared memory in the canonical K-major layout without swizzle:
+// 8-row x 16-byte core matrices, element (r, k) of an R x K operand at byte
+//   (r / 8) * (K * 16) + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
+// i.e. core matrices adjacent in K 128 bytes apart (the descriptor's leading byte
+// offset) and 8-row groups K * 16 bytes apart (its stride byte offset).  One thread
+// issues the K / 16 MMAs of a tile and commits them to an mbarrier; the four warps then
+// read their 32 accumulator lanes (rows) with tcgen05.ld for the epilogue.  Every wait
+// is bounded: a wait that runs out sets *err, and the block frees its tensor memory
+// and leaves.
 
-__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+constexpr int kTcRows = 128;                  // M of every MMA: rows of a tile
+// Dynamic shared memory per block: the operands take at most 48 KB; 64 KB keeps every
+// address an MMA could form from these descriptors inside the block's allocation and
+// leaves at most 3 blocks (3 x 128 tensor-memory columns of the 512) on an SM.
+constexpr size_t kTcSmem = 64 * 1024;
+constexpr unsigned kTcSpin = 1u << 22;        // mbarrier polls (64 ns apart) before giving up
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) of an operand with K columns in the canonical layout
+__device__ __forceinline__ uint32_t tc_off(int r, int k, int K) {
+    return (uint32_t)((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+// shared-memory matrix descriptor: start address, leading (K) and stride (8-row) byte
+// offsets, version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+           ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// waits for the phase with the given parity to complete; false after kTcSpin polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity) {
+    const uint32_t a = smem_addr(mbar);
+    for (unsigned i = 0; i < kTcSpin; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        __nanosleep(64);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// warp 0: ncols tensor-memory columns, their address into *slot
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_free(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's lane (the warp's 32 lanes from taddr)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
 }
 
 enum Epi { EPI_RELU_BIAS = 0, EPI_LAYER = 1, EPI_PLAIN = 2 };
 
+// Y[N x NO] = X[N x KI] W[KI x NO] (+ epilogue), X given as two row-major FP32 halves
+// (columns [0, K1) from X1, [K1, KI) from X2), W given transposed in BF16 (Wt[n][k]).
+// A tile: 128 rows of X (A, K-major) against all of Wt (B, K-major, staged once).
 template <int KI, int K1, int NO, int EPI>
 __global__ void __launch_bounds__(128)
 k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, const __nv_bfloat16 *__restrict__ Wt,
        const float *__restrict__ bias, const float *__restrict__ gterm, const float *__restrict__ hres,
-       float *__restrict__ Z, float *__restrict__ Y) {
-    constexpr int XS = KI + 8, WS = KI + 8;
-    __shared__ __align__(16) __nv_bfloat16 Ws[NO * WS];
-    __shared__ __align__(16) __nv_bfloat16 Xs[64 * XS];
-    for (int i = threadIdx.x; i < NO * KI; i += blockDim.x) {
-        int n = i / KI, k = i - n * KI;
-        Ws[n * WS + k] = Wt[i];
+       float *__restrict__ Z, float *__restrict__ Y, int *err) {
+    static_assert(KI % 16 == 0 && NO % 16 == 0 && NO <= 128 && K1 % 8 == 0, "tile shapes");
+    constexpr uint32_t A_BYTES = kTcRows * KI * 2, NCOL = NO <= 64 ? 64 : 128;
+    static_assert(A_BYTES + NO * KI * 2 <= 48 * 1024, "operands fit the block's shared memory");
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *As = smem, *Bs = smem + A_BYTES;
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // B once: Wt[n][k], 16-byte chunks of 8 k
+    for (int c = threadIdx.x; c < NO * KI / 8; c += blockDim.x) {
+        const int n = c % NO, kc = c / NO;
+        *reinterpret_cast<uint4 *>(Bs + tc_off(n, kc * 8, KI)) = *reinterpret_cast<const uint4 *>(Wt + n * KI + kc * 8);
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    for (int64_t tile = blockIdx.x; tile * 64 < N; tile += gridDim.x) {
-        const int64_t row0 = tile * 64;
-        __syncthreads();
-        for (int i = threadIdx.x; i < 64 * KI; i += blockDim.x) {
-            int r = i / KI, k = i - r * KI;
-            int64_t gr = row0 + r;
-            float v = 0.f;
-            if (gr < N) v = k < K1 ? X1[gr * K1 + k] : X2[gr * (KI - K1) + (k - K1)];
-            Xs[r * XS + k] = __float2bfloat16_rn(v);
-        }
-        __syncthreads();
-        float acc[NO / 8][4];
-#pragma unroll
-        for (int j = 0; j < NO / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-#pragma unroll
-        for (int kk = 0; kk < KI; kk += 16) {
-            const __nv_bfloat16 *xa = Xs + (warp * 16 + g) * XS + kk + 2 * t;
-            uint32_t a0 = *reinterpret_cast<const uint32_t *>(xa);
-            uint32_t a1 = *reinterpret_cast<const uint32_t *>(xa + 8 * XS);
-            uint32_t a2 = *reinterpret_cast<const uint32_t *>(xa + 8);
-            uint32_t a3 = *reinterpret_cast<const uint32_t *>(xa + 8 * XS + 8);
-#pragma unroll
-            for (int nt = 0; nt < NO / 8; ++nt) {
-                const __nv_bfloat16 *wb = Ws + (nt * 8 + g) * WS + kk + 2 * t;
-                uint32_t b0 = *reinterpret_cast<const uint32_t *>(wb);
-                uint32_t b1 = *reinterpret_cast<const uint32_t *>(wb + 8);
-                mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+    if (threadIdx.x == 0) mbar_init(&mbar);
+    if (warp == 0) tmem_alloc(&tmem_slot, NCOL);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint64_t adesc = tc_desc(smem_addr(As), 128, KI * 16), bdesc = tc_desc(smem_addr(Bs), 128, KI * 16);
+    constexpr uint32_t idesc = tc_idesc(kTcRows, NO);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile * kTcRows < N && ok; tile += gridDim.x) {
+        const int64_t row0 = tile * kTcRows;
+        // A: 128 rows x KI, 16-byte chunks of 8 k (consecutive threads, consecutive rows)
+        for (int c = threadIdx.x; c < kTcRows * KI / 8; c += blockDim.x) {
+            const int r = c % kTcRows, k = (c / kTcRows) * 8;
+            const int64_t gr = row0 + r;
+            float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+            if (gr < N) {
+                const float *src = k < K1 ? X1 + gr * K1 + k : X2 + gr * (KI - K1) + (k - K1);
+                v0 = *reinterpret_cast<const float4 *>(src);
+                v1 = *reinterpret_cast<const float4 *>(src + 4);
             }
+            uint4 q;
+            q.x = pack_bf16(v0.x, v0.y), q.y = pack_bf16(v0.z, v0.w);
+            q.z = pack_bf16(v1.x, v1.y), q.w = pack_bf16(v1.z, v1.w);
+            *reinterpret_cast<uint4 *>(As + tc_off(r, k, KI)) = q;
         }
+        fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc_fence_after();
 #pragma unroll
-        for (int nt = 0; nt < NO / 8; ++nt) {
+            for (int kk = 0; kk < KI; kk += 16)   // K = 16: two core matrices, 256 bytes (16 units) on
+                tc_mma(tmem, adesc + (uint64_t)kk, bdesc + (uint64_t)kk, idesc, kk > 0);
+            tc_commit(&mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(&mbar, phase));   // the same verdict in every thread
+        phase ^= 1;
+        tc_fence_after();
+        if (ok) {
+            const int64_t r = row0 + warp * 32 + lane;
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int64_t r = row0 + warp * 16 + g + 8 * half;
-                if (r >= N) continue;
-                const int c = nt * 8 + 2 * t;
-                float v0 = acc[nt][2 * half], v1 = acc[nt][2 * half + 1];
-                if (EPI == EPI_PLAIN) {
-                    Y[r * NO + c] = v0;
-                    Y[r * NO + c + 1] = v1;
-                } else if (EPI == EPI_RELU_BIAS) {
-                    v0 += bias[c];
-                    v1 += bias[c + 1];
-                    Z[r * NO + c] = v0;
-                    Z[r * NO + c + 1] = v1;
-                    Y[r * NO + c] = fmaxf(v0, 0.f);
-                    Y[r * NO + c + 1] = fmaxf(v1, 0.f);
-                } else {
-                    v0 += bias[c] + gterm[c];
-                    v1 += bias[c + 1] + gterm[c + 1];
-                    Z[r * NO + c] = v0;
-                    Z[r * NO + c + 1] = v1;
-                    Y[r * NO + c] = hres[r * NO + c] + fmaxf(v0, 0.f);
-                    Y[r * NO + c + 1] = hres[r * NO + c + 1] + fmaxf(v1, 0.f);
+            for (int c0 = 0; c0 < NO; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+                if (r < N) {
+#pragma unroll
+                    for (int q = 0; q < 16; q += 4) {
+                        const int c = c0 + q;
+                        float4 o = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                        if (EPI == EPI_PLAIN) {
+                            *reinterpret_cast<float4 *>(Y + r * NO + c) = o;
+                        } else {
+                            o.x += bias[c], o.y += bias[c + 1], o.z += bias[c + 2], o.w += bias[c + 3];
+                            if (EPI == EPI_LAYER)
+                                o.x += gterm[c], o.y += gterm[c + 1], o.z += gterm[c + 2], o.w += gterm[c + 3];
+                            *reinterpret_cast<float4 *>(Z + r * NO + c) = o;
+                            float4 y = make_float4(fmaxf(o.x, 0.f), fmaxf(o.y, 0.f), fmaxf(o.z, 0.f), fmaxf(o.w, 0.f));
+                            if (EPI == EPI_LAYER) {
+                                const float4 h = *reinterpret_cast<const float4 *>(hres + r * NO + c);
+                                y.x += h.x, y.y += h.y, y.z += h.z, y.w += h.w;
+                            }
+                            *reinterpret_cast<float4 *>(Y + r * NO + c) = y;
+                        }
+                    }
                 }
             }
+        } else if (threadIdx.x == 0) {
+            atomicExch(err, 1);
         }
+        tc_fence_before();
+        __syncthreads();
     }
+    tc_fence_after();
+    if (warp == 0) tmem_free(tmem, NCOL);
 }
 
-// dW[KI x NO] += X^T dZ over all rows: X given as two FP32 halves as above, dZ
-// [N x NO].  Per block: a BF16 tile of 64 rows of X and of dZ (transposed) in shared
-// memory; the reduction over rows runs on the tensor cores, 16 rows per MMA; each
-// block adds its partial dW with FP32 atomics at the end.
+// dW[KI x NO] += X^T dZ over all rows (X given as two FP32 halves as above, dZ [N x NO]):
+// C (128 x NO) = A B^T with A = X^T (rows of features, zero past KI) and B = dZ^T, both
+// K-major with K = 128 rows of the mesh per tile, accumulated in tensor memory over the
+// block's tiles; each block adds its partial dW with FP32 atomics at the end.
 template <int KI, int K1, int NO>
 __global__ void __launch_bounds__(128)
-k_gemm_wgrad(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2,
-             const float *__restrict__ dZ, float *__restrict__ dW) {
-    constexpr int XS = KI + 8, ZS = 64 + 8;
-    constexpr int MT = KI / 16, NT = NO / 8, TILES = MT * NT, PER_WARP = (TILES + 3) / 4;
-    __shared__ __align__(16) __nv_bfloat16 Xs[64 * XS];
-    __shared__ __align__(16) __nv_bfloat16 Zt[NO * ZS];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    float acc[PER_WARP][4];
+k_gemm_wgrad(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, const float *__restrict__ dZ,
+             float *__restrict__ dW, int *err) {
+    static_assert(KI <= 128 && KI % 16 == 0 && NO % 16 == 0 && NO <= 128 && K1 % 2 == 0, "tile shapes");
+    constexpr int KT = kTcRows;   // rows of the mesh per tile (the MMA's K)
+    constexpr uint32_t A_BYTES = 128 * KT * 2, NCOL = NO <= 64 ? 64 : 128;
+    static_assert(A_BYTES + NO * KT * 2 <= 48 * 1024, "operands fit the block's shared memory");
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *As = smem, *Bs = smem + A_BYTES;
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // feature rows past KI stay zero
+    for (int i = threadIdx.x; i < (int)(A_BYTES / 16); i += blockDim.x)
+        reinterpret_cast<uint4 *>(As)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0) mbar_init(&mbar);
+    if (warp == 0) tmem_alloc(&tmem_slot, NCOL);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint64_t adesc = tc_desc(smem_addr(As), 128, KT * 16), bdesc = tc_desc(smem_addr(Bs), 128, KT * 16);
+    constexpr uint32_t idesc = tc_idesc(128, NO);
+    uint32_t phase = 0, used = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile * KT < N && ok; tile += gridDim.x) {
+        const int64_t row0 = tile * KT;
+        // a thread packs 8 consecutive mesh rows of one feature pair into two 16-byte chunks
+        for (int c = threadIdx.x; c < (KI / 2) * (KT / 8); c += blockDim.x) {
+            const int fp = c % (KI / 2), kg = c / (KI / 2);
+            const int m = 2 * fp;
+            float a0[8], a1[8];
 #pragma unroll
-    for (int j = 0; j < PER_WARP; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    for (int64_t tile = blockIdx.x; tile * 64 < N; tile += gridDim.x) {
-        const int64_t row0 = tile * 64;
-        __syncthreads();
-        for (int i = threadIdx.x; i < 64 * KI; i += blockDim.x) {
-            int r = i / KI, k = i - r * KI;
-            int64_t gr = row0 + r;
-            float v = 0.f;
-            if (gr < N) v = k < K1 ? X1[gr * K1 + k] : X2[gr * (KI - K1) + (k - K1)];
-            Xs[r * XS + k] = __float2bfloat16_rn(v);
-        }
-        for (int i = threadIdx.x; i < 64 * NO; i += blockDim.x) {
-            int r = i / NO, n = i - r * NO;
-            int64_t gr = row0 + r;
-            Zt[n * ZS + r] = __float2bfloat16_rn(gr < N ? dZ[gr * NO + n] : 0.f);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < PER_WARP; ++j) {
-            const int tid = warp + 4 * j;
-            if (tid >= TILES) break;
-            const int mt = tid / NT, nt = tid - mt * NT;
-#pragma unroll
-            for (int kk = 0; kk < 64; kk += 16) {
-                // A[m][q] = X[row kk+q][feature 16 mt + m]
-                const int m0 = mt * 16 + g;
-                const int q0 = kk + 2 * t;
-                uint32_t a0 = pack2(Xs[q0 * XS + m0], Xs[(q0 + 1) * XS + m0]);
-                uint32_t a1 = pack2(Xs[q0 * XS + m0 + 8], Xs[(q0 + 1) * XS + m0 + 8]);
-                uint32_t a2 = pack2(Xs[(q0 + 8) * XS + m0], Xs[(q0 + 9) * XS + m0]);
-                uint32_t a3 = pack2(Xs[(q0 + 8) * XS + m0 + 8], Xs[(q0 + 9) * XS + m0 + 8]);
-                // B[q][n] = dZ[row kk+q][output 8 nt + n]
-                const __nv_bfloat16 *zb = Zt + (nt * 8 + g) * ZS + q0;
-                uint32_t b0 = *reinterpret_cast<const uint32_t *>(zb);
-                uint32_t b1 = *reinterpret_cast<const uint32_t *>(zb + 8);
-                mma_bf16(acc[j], a0, a1, a2, a3, b0, b1);
+            for (int q = 0; q < 8; ++q) {
+                const int64_t gr = row0 + kg * 8 + q;
+                float2 v = make_float2(0.f, 0.f);
+                if (gr < N)
+                    v = m < K1 ? *reinterpret_cast<const float2 *>(X1 + gr * K1 + m)
+                               : *reinterpret_cast<const float2 *>(X2 + gr * (KI - K1) + (m - K1));
+                a0[q] = v.x, a1[q] = v.y;
             }
+            *reinterpret_cast<uint4 *>(As + tc_off(m, kg * 8, KT)) =
+                make_uint4(pack_bf16(a0[0], a0[1]), pack_bf16(a0[2], a0[3]), pack_bf16(a0[4], a0[5]),
+                           pack_bf16(a0[6], a0[7]));
+            *reinterpret_cast<uint4 *>(As + tc_off(m + 1, kg * 8, KT)) =
+                make_uint4(pack_bf16(a1[0], a1[1]), pack_bf16(a1[2], a1[3]), pack_bf16(a1[4], a1[5]),
+                           pack_bf16(a1[6], a1[7]));
+        }
+        for (int c = threadIdx.x; c < (NO / 2) * (KT / 8); c += blockDim.x) {
+            const int np = c % (NO / 2), kg = c / (NO / 2);
+            const int n = 2 * np;
+            float b0[8], b1[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int64_t gr = row0 + kg * 8 + q;
+                const float2 v = gr < N ? *reinterpret_cast<const float2 *>(dZ + gr * NO + n) : make_float2(0.f, 0.f);
+                b0[q] = v.x, b1[q] = v.y;
+            }
+            *reinterpret_cast<uint4 *>(Bs + tc_off(n, kg * 8, KT)) =
+                make_uint4(pack_bf16(b0[0], b0[1]), pack_bf16(b0[2], b0[3]), pack_bf16(b0[4], b0[5]),
+                           pack_bf16(b0[6], b0[7]));
+            *reinterpret_cast<uint4 *>(Bs + tc_off(n + 1, kg * 8, KT)) =
+                make_uint4(pack_bf16(b1[0], b1[1]), pack_bf16(b1[2], b1[3]), pack_bf16(b1[4], b1[5]),
+                           pack_bf16(b1[6], b1[7]));
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int kk = 0; kk < KT; kk += 16)
+                tc_mma(tmem, adesc + (uint64_t)kk, bdesc + (uint64_t)kk, idesc, (used | kk) != 0);
+            tc_commit(&mbar);
+        }
+        used = 1;
+        // the MMAs read the staged tiles: wait before they are overwritten
+        ok = __syncthreads_and(mbar_wait(&mbar, phase));
+        phase ^= 1;
+        tc_fence_after();
+    }
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+    } else if (used && warp * 32 < KI) {
+        const int m = warp * 32 + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < NO; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (m < KI)
+#pragma unroll
+                for (int q = 0; q < 16; ++q) atomicAdd(&dW[m * NO + c0 + q], v[q]);
         }
     }
-#pragma unroll
-    for (int j = 0; j < PER_WARP; ++j) {
-        const int tid = warp + 4 * j;
-        if (tid >= TILES) break;
-        const int mt = tid / NT, nt = tid - mt * NT;
-        const int m = mt * 16 + g, n = nt * 8 + 2 * t;
-        atomicAdd(&dW[m * NO + n], acc[j][0]);
-        atomicAdd(&dW[m * NO + n + 1], acc[j][1]);
-        atomicAdd(&dW[(m + 8) * NO + n], acc[j][2]);
-        atomicAdd(&dW[(m + 8) * NO + n + 1], acc[j][3]);
-    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_free(tmem, NCOL);
 }
 
 // ---------------------------------------------------------------- graph kernels
@@ -691,6 +843,7 @@ struct fe_gnn_s {
     fe::DBuf<float> F, Z0, H, Z, M, dH, dHn, dX, dZ, dM, inv_deg, colsum, gterm, stats, du, dgb;
     fe::DBuf<float> us0, us1;     // decoded field and the smoothing ping-pong buffer
     fe::DBuf<double> gext, Ag, bt, u, Au, x0, acc, gsum;
+    fe::DBuf<int> tc_err;         // set by a tensor-core GEMM whose MMAs did not complete
     double *acc_host = nullptr;
     int steps = 0;
     double last_scale = 0.0, last_num = 0.0, last_den = 0.0;
@@ -704,6 +857,43 @@ namespace {
 
 constexpr int WT_W0 = 0;
 constexpr int WT_L0 = NF * HID;
+// the current layer's W_l as stored, for the data-gradient GEMM (the GEMMs stage their
+// weights in 16-byte pieces: every slot starts on a 16-byte boundary)
+constexpr int WT_DX = WT_L0 + NLAYER * KC * HID;
+constexpr int WT_TOTAL = WT_DX + KC * HID;
+static_assert(WT_L0 % 8 == 0 && (KC * HID) % 8 == 0 && WT_DX % 8 == 0, "16-byte aligned BF16 weight slots");
+
+template <int KI, int K1, int NO, int EPI>
+int launch_gemm(fe_gnn_s *g, int64_t n, const float *X1, const float *X2, const __nv_bfloat16 *Wt,
+                const float *bias, const float *gterm, const float *hres, float *Z, float *Y) {
+    const auto kern = k_gemm<KI, K1, NO, EPI>;
+    FE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, 152 * 3));
+    kern<<<grid, 128, kTcSmem, g->stream>>>(n, X1, X2, Wt, bias, gterm, hres, Z, Y, g->tc_err.p);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+template <int KI, int K1, int NO>
+int launch_wgrad(fe_gnn_s *g, int64_t n, const float *X1, const float *X2, const float *dZ, float *dW) {
+    const auto kern = k_gemm_wgrad<KI, K1, NO>;
+    FE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, 152 * 3));
+    kern<<<grid, 128, kTcSmem, g->stream>>>(n, X1, X2, dZ, dW, g->tc_err.p);
+    FE_LAUNCH_CHECK();
+    return FE_OK;
+}
+
+// the tensor-core GEMMs' error word, read once the stream has been synchronised
+int check_tc(fe_gnn_s *g) {
+    int e = 0;
+    FE_CUDA(cudaMemcpy(&e, g->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        set_error("warm-start network: a tensor-core GEMM's MMAs did not complete");
+        return FE_CUDA_ERR;
+    }
+    return FE_OK;
+}
 
 int gnn_alloc(fe_gnn_s *g, int64_t n) {
     // whole 32-row SELL slices: spmv64 reads the padding rows of the last slice
@@ -786,9 +976,8 @@ int forward(fe_gnn_s *g, fe_handle_s *h) {
     const int64_t n = h->n_nodes;
     cudaStream_t s = g->stream;
     const float *P = g->params.p;
-    const int gg = (int)std::min<int64_t>((n + 63) / 64, 152 * 4);
-    k_gemm<NF, NF, HID, EPI_RELU_BIAS><<<gg, 128, 0, s>>>(n, g->F.p, nullptr, g->wt.p + WT_W0, P + P_B0, nullptr,
-                                                          nullptr, g->Z0.p, Hl(g, 0));
+    FE_CHECK(launch_gemm<NF, NF, HID, EPI_RELU_BIAS>(g, n, g->F.p, nullptr, g->wt.p + WT_W0, P + P_B0, nullptr,
+                                                     nullptr, g->Z0.p, Hl(g, 0)));
     FE_CHECK(dalloc(g->colsum, (size_t)(NLAYER + 1) * HID));
     FE_CHECK(dalloc(g->gterm, (size_t)NLAYER * HID));
     FE_CUDA(cudaMemsetAsync(g->colsum.p, 0, (NLAYER + 1) * HID * sizeof(float), s));
@@ -797,9 +986,9 @@ int forward(fe_gnn_s *g, fe_handle_s *h) {
         k_aggregate<false><<<g1(n * 32), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p, Hl(g, l), Ml(g, l));
         k_colsum<<<std::min<int64_t>((n + 3) / 4, 152 * 4), kT, 0, s>>>(n, Hl(g, l), g->colsum.p + l * HID);
         k_gterm<<<1, HID, 0, s>>>(g->colsum.p + l * HID, 1.f / (float)n, LP + L_U, g->gterm.p + l * HID);
-        k_gemm<KC, HID, HID, EPI_LAYER><<<gg, 128, 0, s>>>(n, Hl(g, l), Ml(g, l), g->wt.p + WT_L0 + l * KC * HID,
-                                                           LP + L_B, g->gterm.p + l * HID, Hl(g, l), Zl(g, l),
-                                                           Hl(g, l + 1));
+        FE_CHECK(launch_gemm<KC, HID, HID, EPI_LAYER>(g, n, Hl(g, l), Ml(g, l), g->wt.p + WT_L0 + l * KC * HID,
+                                                      LP + L_B, g->gterm.p + l * HID, Hl(g, l), Zl(g, l),
+                                                      Hl(g, l + 1)));
     }
     k_decode<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, P + P_BD, h->bc_of_dof.p, g->us0.p);
     float *cur = g->us0.p, *nxt = g->us1.p;
@@ -820,6 +1009,7 @@ int forward(fe_gnn_s *g, fe_handle_s *h) {
     if (!g->acc_host) FE_CUDA(cudaMallocHost((void **)&g->acc_host, 4 * sizeof(double)));
     FE_CUDA(cudaMemcpyAsync(g->acc_host, g->acc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
+    FE_CHECK(check_tc(g));
     g->last_num = g->acc_host[0];
     g->last_den = g->acc_host[1];
     g->last_scale = g->last_den > 0 ? g->last_num / g->last_den : 0.0;
@@ -872,8 +1062,6 @@ int backward(fe_gnn_s *g, fe_handle_s *h, double energy, bool fit, double *loss)
     k_mask2<<<g1(nd), kT, 0, s>>>(nd, h->bc_of_dof.p, cur);
     k_decode_back<<<g1(n * 32), kT, 0, s>>>(n, Hl(g, NLAYER), P + P_WD, cur, g->dHn.p, G + P_WD, G + P_BD);
     FE_CHECK(dalloc(g->dgb, HID * 2));
-    const int gg = (int)std::min<int64_t>((n + 63) / 64, 152 * 4);
-    const int gw = (int)std::min<int64_t>((n + 63) / 64, 152 * 2);
     for (int l = NLAYER - 1; l >= 0; --l) {
         const float *LP = P + P_L0 + l * L_STRIDE;
         float *LG = G + P_L0 + l * L_STRIDE;
@@ -881,12 +1069,12 @@ int backward(fe_gnn_s *g, fe_handle_s *h, double energy, bool fit, double *loss)
         k_relu_grad<<<g1(n * HID), kT, 0, s>>>(n * HID, g->dHn.p, Zl(g, l), g->dZ.p);
         // dX = dZ W_l^T: the GEMM takes its right operand transposed, [out][in], and
         // (W_l^T)^T = W_l in its stored [128][64] layout, so copy W_l to BF16 as it is
-        __nv_bfloat16 *wl = g->wt.p + (size_t)P_TOTAL;
+        __nv_bfloat16 *wl = g->wt.p + WT_DX;
         k_to_bf16<<<16, 256, 0, s>>>(LP + L_W, KC * HID, wl);
-        k_gemm<HID, HID, KC, EPI_PLAIN><<<gg, 128, 0, s>>>(n, g->dZ.p, nullptr, wl, nullptr, nullptr, nullptr,
-                                                            nullptr, g->dX.p);
+        FE_CHECK(launch_gemm<HID, HID, KC, EPI_PLAIN>(g, n, g->dZ.p, nullptr, wl, nullptr, nullptr, nullptr,
+                                                      nullptr, g->dX.p));
         // weight gradients
-        k_gemm_wgrad<KC, HID, HID><<<gw, 128, 0, s>>>(n, Hl(g, l), Ml(g, l), g->dZ.p, LG + L_W);
+        FE_CHECK(launch_wgrad<KC, HID, HID>(g, n, Hl(g, l), Ml(g, l), g->dZ.p, LG + L_W));
         FE_CUDA(cudaMemsetAsync(g->dgb.p + HID, 0, HID * sizeof(float), s));
         k_colsum<<<std::min<int64_t>((n + 3) / 4, 152 * 4), kT, 0, s>>>(n, g->dZ.p, g->dgb.p + HID);
         k_gterm_back<<<1, HID, 0, s>>>(g->colsum.p + l * HID, 1.f / (float)n, LP + L_U, g->dgb.p + HID, LG + L_U,
@@ -902,7 +1090,7 @@ int backward(fe_gnn_s *g, fe_handle_s *h, double energy, bool fit, double *loss)
     }
     // encoder: dZ0 = dH_0 (.) [z0 > 0];  dW0 = F^T dZ0;  db0 = colsum(dZ0)
     k_relu_grad<<<g1(n * HID), kT, 0, s>>>(n * HID, g->dHn.p, g->Z0.p, g->dZ.p);
-    k_gemm_wgrad<NF, NF, HID><<<gw, 128, 0, s>>>(n, g->F.p, nullptr, g->dZ.p, G + P_W0);
+    FE_CHECK(launch_wgrad<NF, NF, HID>(g, n, g->F.p, nullptr, g->dZ.p, G + P_W0));
     k_colsum<<<std::min<int64_t>((n + 3) / 4, 152 * 4), kT, 0, s>>>(n, g->dZ.p, G + P_B0);
     FE_LAUNCH_CHECK();
     h->launches += 2 + NLAYER * 9 + 3;
@@ -928,7 +1116,8 @@ int fe_gnn_create(fe_gnn *out) {
     if (!st) st = dalloc(g->grad, P_TOTAL);
     if (!st) st = dalloc(g->adam_m, P_TOTAL);
     if (!st) st = dalloc(g->adam_v, P_TOTAL);
-    if (!st) st = dalloc(g->wt, (size_t)P_TOTAL + KC * HID);
+    if (!st) st = dalloc(g->wt, (size_t)WT_TOTAL);
+    if (!st) st = dalloc(g->tc_err, 1);
     if (st) {
         fe_gnn_destroy(g);
         return st;
@@ -936,6 +1125,7 @@ int fe_gnn_create(fe_gnn *out) {
     cudaMemset(g->params.p, 0, P_TOTAL * sizeof(float));
     cudaMemset(g->adam_m.p, 0, P_TOTAL * sizeof(float));
     cudaMemset(g->adam_v.p, 0, P_TOTAL * sizeof(float));
+    cudaMemset(g->tc_err.p, 0, sizeof(int));
     *out = g;
     return FE_OK;
 }
@@ -943,7 +1133,7 @@ int fe_gnn_create(fe_gnn *out) {
 int fe_gnn_destroy(fe_gnn g) {
     if (!g) return FE_OK;
     cudaDeviceSynchronize();
-    dfree(g->params), dfree(g->grad), dfree(g->adam_m), dfree(g->adam_v), dfree(g->wt);
+    dfree(g->params), dfree(g->grad), dfree(g->adam_m), dfree(g->adam_v), dfree(g->wt), dfree(g->tc_err);
     dfree(g->F), dfree(g->Z0), dfree(g->H), dfree(g->Z), dfree(g->M), dfree(g->dH), dfree(g->dHn), dfree(g->dX);
     dfree(g->dZ), dfree(g->dM), dfree(g->inv_deg), dfree(g->colsum), dfree(g->gterm), dfree(g->stats);
     dfree(g->du), dfree(g->dgb), dfree(g->gext), dfree(g->Ag), dfree(g->bt), dfree(g->u), dfree(g->Au);
