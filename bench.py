@@ -546,6 +546,13 @@ def run_ours(args, dist):
         "gpu_launches": int(n_launch),
         "clocks": clk,
     }
+    if dist.world == 1 and net is not None:
+        # the learned part's own throughput on the same mesh: inference and one training
+        # step (forward, backward through the tcgen05 GEMMs, Adam)
+        from finite_elements_gb300 import gnn_bench
+        out["learned_network"] = dict(gnn_bench.measure(args.nx, args.ny, reps=3, seed=args.seed),
+                                      method=f"python -m finite_elements_gb300.gnn_bench --nx {args.nx} "
+                                             f"--ny {args.ny} --reps 3")
     if dist.world == 1 and args.batch_n > 0:
         # hundreds of uneven instances in one batched system (persistent kernel, CUDA
         # graph, autotuned tiles) against the same instances solved one at a time

@@ -66,16 +66,18 @@ inline int g1(int64_t n, int t = kT) { return grid_for(n, t, 152 * 8); }
 //   (r / 8) * (K * 16) + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
 // i.e. core matrices adjacent in K 128 bytes apart (the descriptor's leading byte
 // offset) and 8-row groups K * 16 bytes apart (its stride byte offset).  One thread
-// issues the K / 16 MMAs of a tile and commits them to an mbarrier; the four warps then
-// read their 32 accumulator lanes (rows) with tcgen05.ld for the epilogue.  Every wait
+// issues the K / 16 MMAs of a tile and commits them to an mbarrier; the eight warps then
+// read the accumulator with tcgen05.ld for the epilogue, two warps per 32-lane quarter
+// (a warp reaches only its quarter's lanes), each half of the columns.  Every wait
 // is bounded: a wait that runs out sets *err, and the block frees its tensor memory
 // and leaves.
 
 constexpr int kTcRows = 128;                  // M of every MMA: rows of a tile
-// Dynamic shared memory per block: the operands take at most 48 KB; 64 KB keeps every
-// address an MMA could form from these descriptors inside the block's allocation and
-// leaves at most 3 blocks (3 x 128 tensor-memory columns of the 512) on an SM.
-constexpr size_t kTcSmem = 64 * 1024;
+// Dynamic shared memory per block: 48 KB holds the operands of every shape and leaves
+// at most 4 blocks (4 x 128 tensor-memory columns, the SM's 512) on an SM, so that an
+// allocation of tensor memory never waits for another block.
+constexpr size_t kTcSmem = 48 * 1024;
+constexpr int kTcThreads = 256;   // 8 warps: two per 32-lane quarter of the accumulator
 constexpr unsigned kTcSpin = 1u << 22;        // mbarrier polls (64 ns apart) before giving up
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -171,11 +173,11 @@ enum Epi { EPI_RELU_BIAS = 0, EPI_LAYER = 1, EPI_PLAIN = 2 };
 // (columns [0, K1) from X1, [K1, KI) from X2), W given transposed in BF16 (Wt[n][k]).
 // A tile: 128 rows of X (A, K-major) against all of Wt (B, K-major, staged once).
 template <int KI, int K1, int NO, int EPI>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kTcThreads)
 k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, const __nv_bfloat16 *__restrict__ Wt,
        const float *__restrict__ bias, const float *__restrict__ gterm, const float *__restrict__ hres,
        float *__restrict__ Z, float *__restrict__ Y, int *err) {
-    static_assert(KI % 16 == 0 && NO % 16 == 0 && NO <= 128 && K1 % 8 == 0, "tile shapes");
+    static_assert(KI % 16 == 0 && NO % 32 == 0 && NO <= 128 && K1 % 8 == 0, "tile shapes");
     constexpr uint32_t A_BYTES = kTcRows * KI * 2, NCOL = NO <= 64 ? 64 : 128;
     static_assert(A_BYTES + NO * KI * 2 <= 48 * 1024, "operands fit the block's shared memory");
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -228,11 +230,13 @@ k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, co
         phase ^= 1;
         tc_fence_after();
         if (ok) {
-            const int64_t r = row0 + warp * 32 + lane;
+            // warp w: accumulator lanes (rows) 32 (w % 4) .., columns of half w / 4
+            const int quarter = warp & 3, half = warp >> 2;
+            const int64_t r = row0 + quarter * 32 + lane;
 #pragma unroll
-            for (int c0 = 0; c0 < NO; c0 += 16) {
+            for (int c0 = half * (NO / 2); c0 < (half + 1) * (NO / 2); c0 += 16) {
                 float v[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+                tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
                 if (r < N) {
 #pragma unroll
                     for (int q = 0; q < 16; q += 4) {
@@ -270,10 +274,10 @@ k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, co
 // K-major with K = 128 rows of the mesh per tile, accumulated in tensor memory over the
 // block's tiles; each block adds its partial dW with FP32 atomics at the end.
 template <int KI, int K1, int NO>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kTcThreads)
 k_gemm_wgrad(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, const float *__restrict__ dZ,
              float *__restrict__ dW, int *err) {
-    static_assert(KI <= 128 && KI % 16 == 0 && NO % 16 == 0 && NO <= 128 && K1 % 2 == 0, "tile shapes");
+    static_assert(KI <= 128 && KI % 16 == 0 && NO % 32 == 0 && NO <= 128 && K1 % 2 == 0, "tile shapes");
     constexpr int KT = kTcRows;   // rows of the mesh per tile (the MMA's K)
     constexpr uint32_t A_BYTES = 128 * KT * 2, NCOL = NO <= 64 ? 64 : 128;
     static_assert(A_BYTES + NO * KT * 2 <= 48 * 1024, "operands fit the block's shared memory");
@@ -352,12 +356,13 @@ k_gemm_wgrad(int64_t N, const float *__restrict__ X1, const float *__restrict__ 
     }
     if (!ok) {
         if (threadIdx.x == 0) atomicExch(err, 1);
-    } else if (used && warp * 32 < KI) {
-        const int m = warp * 32 + lane;
+    } else if (used && (warp & 3) * 32 < KI) {
+        const int quarter = warp & 3, half = warp >> 2;
+        const int m = quarter * 32 + lane;
 #pragma unroll
-        for (int c0 = 0; c0 < NO; c0 += 16) {
+        for (int c0 = half * (NO / 2); c0 < (half + 1) * (NO / 2); c0 += 16) {
             float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
             if (m < KI)
 #pragma unroll
                 for (int q = 0; q < 16; ++q) atomicAdd(&dW[m * NO + c0 + q], v[q]);
@@ -868,8 +873,8 @@ int launch_gemm(fe_gnn_s *g, int64_t n, const float *X1, const float *X2, const 
                 const float *bias, const float *gterm, const float *hres, float *Z, float *Y) {
     const auto kern = k_gemm<KI, K1, NO, EPI>;
     FE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, 152 * 3));
-    kern<<<grid, 128, kTcSmem, g->stream>>>(n, X1, X2, Wt, bias, gterm, hres, Z, Y, g->tc_err.p);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, 152 * 4));
+    kern<<<grid, kTcThreads, kTcSmem, g->stream>>>(n, X1, X2, Wt, bias, gterm, hres, Z, Y, g->tc_err.p);
     FE_LAUNCH_CHECK();
     return FE_OK;
 }
@@ -878,8 +883,8 @@ template <int KI, int K1, int NO>
 int launch_wgrad(fe_gnn_s *g, int64_t n, const float *X1, const float *X2, const float *dZ, float *dW) {
     const auto kern = k_gemm_wgrad<KI, K1, NO>;
     FE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, 152 * 3));
-    kern<<<grid, 128, kTcSmem, g->stream>>>(n, X1, X2, dZ, dW, g->tc_err.p);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + kTcRows - 1) / kTcRows, 152 * 4));
+    kern<<<grid, kTcThreads, kTcSmem, g->stream>>>(n, X1, X2, dZ, dW, g->tc_err.p);
     FE_LAUNCH_CHECK();
     return FE_OK;
 }
