@@ -35,6 +35,10 @@ sys.path.insert(0, ROOT)
 # default 40 MB prefix (steady state of a run of steps,
 # profiles/cheb_step_fp32_keep_plane_strain_4M.md); None for other workloads.
 NCU_TRAFFIC = {(2000, 1000, 0): 278_710_784, (2000, 1000, 40_000_000): 265_900_000}
+# The same for the multigrid roofline kernel (level 0's Chebyshev smoothing step of the
+# V-cycle), the mean over its two timed launches, the first step from zero and the
+# second, keyed by the grid (profiles/launches_multigrid_plane_strain_4M.md).
+NCU_TRAFFIC_MG = {(2000, 1000): 266_744_832}
 
 METRIC = "s/solve to 1e-8 rel. residual, 4M-DOF elasticity: mixed+learned vs plain PCG"
 UNIT = "s/solve"
@@ -452,7 +456,8 @@ def run_ours(args, dist):
                     "kernel": "k_cheb_step<2,float,float,0,*,1> (level-0 Chebyshev smoothing step of the FP32 "
                               "V-cycle on the prescaled FP32 SELL copy; 5 of the cycle's launches)",
                     "achieved": sm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": sm_frac, "peak_source": peak_src,
-                    "traffic": None, "bytes_per_launch": smooth_bytes(), "launch_us": mg_prof["smooth_us"],
+                    "traffic": NCU_TRAFFIC_MG.get((args.nx, args.ny)), "bytes_per_launch": smooth_bytes(),
+                    "launch_us": mg_prof["smooth_us"],
                     "launches_timed": mg_prof["smooth_n"],
                     "share_of_step": (mg_prof["smooth_us"] * 5 * 1e-6 * mg_prof["cycles"] / args.steps / value
                                       if value > 0 else None),

@@ -279,7 +279,8 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::Pa
             const int32_t c = f.acol[s];
             const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
             for (int64_t t = lane; t < len; t += 32) {
-                const int64_t p = amg::find_sorted(f.ccol, c0, c0 + lc, f.bcol[t0 + t]);
+                const int32_t bc = f.bcol[t0 + t];
+                const int64_t p = (f.upper && bc < i) ? -1 : amg::find_sorted(f.ccol, c0, c0 + lc, bc);
                 pos[base + t] = p < 0 ? -1 : (int32_t)(p - c0);
                 ss[base + t] = (int32_t)s;
                 ts[base + t] = (int32_t)(t0 + t);
@@ -324,13 +325,9 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::Pa
                 const int t = ord[q];
                 const double *a = f.aval + (int64_t)ss[t] * ra * ca;
                 const double *b = f.bval + (int64_t)ts[t] * ca * cb;
-                for (int x = 0; x < ra; ++x)
-                    for (int z = 0; z < cb; ++z) {
-                        double v = 0.0;
-                        for (int y = 0; y < ca; ++y) v += a[x * ca + y] * b[y * cb + z];
-                        acc[x * cb + z] += v;
-                    }
+                amg::block_mul_add(a, b, ra, ca, cb, acc);
             }
+            if (f.upper && f.ccol[c0 + p] < i) continue;   // filled by the mirror pass
             double *o = f.cval + (c0 + p) * bs;
             for (int k = 0; k < bs; ++k) o[k] = acc[k];
         }
@@ -405,7 +402,7 @@ __global__ void __launch_bounds__(32) kd_prod_vals_long(int64_t n, amg::PassProd
         if (T > kLongTerms || lc > kLongOut || la > kLongA) {
             if (lane == 0)
                 amg::row_product_values(f.aptr, f.acol, f.aval, f.ra, f.ca, f.bptr, f.bcol, f.bval, f.cb, f.cptr,
-                                        f.ccol, f.cval, i);
+                                        f.ccol, f.cval, i, f.upper != 0);
             __syncwarp();
             continue;
         }
@@ -425,7 +422,8 @@ __global__ void __launch_bounds__(32) kd_prod_vals_long(int64_t n, amg::PassProd
             const int32_t c = f.acol[a0 + q];
             const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
             for (int64_t t = lane; t < len; t += 32) {
-                const int64_t p = amg::find_sorted(f.ccol, c0, c0 + lc, f.bcol[t0 + t]);
+                const int32_t bc = f.bcol[t0 + t];
+                const int64_t p = (f.upper && bc < i) ? -1 : amg::find_sorted(f.ccol, c0, c0 + lc, bc);
                 pos[aoff[q] + t] = p < 0 ? (int16_t)-1 : (int16_t)(p - c0);
             }
         }
@@ -473,13 +471,9 @@ __global__ void __launch_bounds__(32) kd_prod_vals_long(int64_t n, amg::PassProd
                 const int64_t tidx = f.bptr[f.acol[sidx]] + (t - aoff[lo]);
                 const double *a = f.aval + sidx * ra * ca;
                 const double *b = f.bval + tidx * ca * cb;
-                for (int x = 0; x < ra; ++x)
-                    for (int z = 0; z < cb; ++z) {
-                        double v = 0.0;
-                        for (int y = 0; y < ca; ++y) v += a[x * ca + y] * b[y * cb + z];
-                        acc[x * cb + z] += v;
-                    }
+                amg::block_mul_add(a, b, ra, ca, cb, acc);
             }
+            if (f.upper && f.ccol[c0 + p] < i) continue;   // filled by the mirror pass
             double *o = f.cval + (c0 + p) * bs;
             for (int k = 0; k < bs; ++k) o[k] = acc[k];
         }

@@ -353,26 +353,49 @@ FE_HD int64_t row_product_columns(const int64_t *aptr, const int32_t *acol, cons
 
 // Values of row i of C = A B on its sorted columns ccol[cptr[i] .. cptr[i+1]): each
 // block product (ra x ca times ca x cb) added in the order of A's and then B's entries.
+// o += a b for an ra x ca block a and a ca x cb block b, every product fused into the
+// accumulator (ca FP64 FMAs per entry of o, no separate additions: these products are
+// bound by the FP64 rate).  The device's warp-per-row products use the same sequence.
+FE_HD void block_mul_add(const double *a, const double *b, int ra, int ca, int cb, double *o) {
+    for (int x = 0; x < ra; ++x)
+        for (int z = 0; z < cb; ++z) {
+            double acc = o[x * cb + z];
+            for (int y = 0; y < ca; ++y) acc = fma(a[x * ca + y], b[y * cb + z], acc);
+            o[x * cb + z] = acc;
+        }
+}
+
+// Row i of C = A B (upper: only the entries whose block column is at least i, for a
+// product known to be symmetric; the others are left for PassMirrorLower).
 FE_HD void row_product_values(const int64_t *aptr, const int32_t *acol, const double *aval, int ra, int ca,
                               const int64_t *bptr, const int32_t *bcol, const double *bval, int cb,
-                              const int64_t *cptr, const int32_t *ccol, double *cval, int64_t i) {
+                              const int64_t *cptr, const int32_t *ccol, double *cval, int64_t i,
+                              bool upper = false) {
     const int bs = ra * cb;
     for (int64_t k = cptr[i] * bs; k < cptr[i + 1] * bs; ++k) cval[k] = 0.0;
     for (int64_t s = aptr[i]; s < aptr[i + 1]; ++s) {
         const double *a = &aval[s * ra * ca];
         const int64_t j = acol[s];
         for (int64_t t = bptr[j]; t < bptr[j + 1]; ++t) {
+            if (upper && bcol[t] < i) continue;
             const double *b = &bval[t * ca * cb];
             const int64_t p = find_sorted(ccol, cptr[i], cptr[i + 1], bcol[t]);
             if (p < 0) continue;   // cannot happen: the columns come from these products
-            double *o = &cval[p * bs];
-            for (int x = 0; x < ra; ++x)
-                for (int z = 0; z < cb; ++z) {
-                    double acc = 0.0;
-                    for (int y = 0; y < ca; ++y) acc += a[x * ca + y] * b[y * cb + z];
-                    o[x * cb + z] += acc;
-                }
+            block_mul_add(a, b, ra, ca, cb, &cval[p * bs]);
         }
+    }
+}
+
+// The lower entries of a symmetric product row: block (i, j), j < i, is the transpose
+// of block (j, i).
+FE_HD void row_mirror_lower(const int64_t *ptr, const int32_t *col, double *val, int m, int64_t i) {
+    for (int64_t s = ptr[i]; s < ptr[i + 1]; ++s) {
+        const int64_t j = col[s];
+        if (j >= i) break;   // columns are sorted
+        const int64_t q = find_sorted(col, ptr[j], ptr[j + 1], i);
+        if (q < 0) continue;   // cannot happen: the pattern of a symmetric product is symmetric
+        for (int x = 0; x < m; ++x)
+            for (int z = 0; z < m; ++z) val[s * m * m + x * m + z] = val[q * m * m + z * m + x];
     }
 }
 

@@ -240,14 +240,22 @@ struct PassProdCols {
 
 // boff / total: the row offsets and the sum of the rows' product counts (PassProdBound),
 // for a device executor that gives long rows a warp each
+// upper: the product is symmetric; only the entries on and above the diagonal are
+// computed (PassMirrorLower fills the others)
 struct PassProdVals {
     const int64_t *aptr; const int32_t *acol; const double *aval; int ra; int ca; const int64_t *bptr;
     const int32_t *bcol; const double *bval; int cb; const int64_t *cptr; const int32_t *ccol; double *cval;
     const int64_t *boff = nullptr;
     int64_t total = 0;
+    int upper = 0;
     FE_HD void operator()(int64_t i) const {
-        row_product_values(aptr, acol, aval, ra, ca, bptr, bcol, bval, cb, cptr, ccol, cval, i);
+        row_product_values(aptr, acol, aval, ra, ca, bptr, bcol, bval, cb, cptr, ccol, cval, i, upper != 0);
     }
+};
+
+struct PassMirrorLower {
+    const int64_t *ptr; const int32_t *col; double *val; int m;
+    FE_HD void operator()(int64_t i) const { row_mirror_lower(ptr, col, val, m, i); }
 };
 
 struct PassSmooth {
@@ -309,9 +317,10 @@ int distinct_rows(Ex &ex, int64_t n, Bound bound, Cols cols, Csr &C, Work<Ex> &W
     return FE_OK;
 }
 
-// C = A B
+// C = A B (symmetric: C is known to be symmetric, so its upper entries are computed
+// and the lower ones copied from them)
 template <class Ex>
-int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W) {
+int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W, bool symmetric = false) {
     C.n = A.n, C.rd = A.rd, C.cd = B.cd;
     int64_t total = 0;
     FE_CHECK(distinct_rows(ex, A.n, PassProdBound{A.ptr.p, A.col.p, B.ptr.p, nullptr},
@@ -319,8 +328,9 @@ int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W) {
     FE_CHECK(ex.alloc(C.val, (size_t)std::max<int64_t>(C.nnzb * C.rd * C.cd, 1)));
     PassProdVals vals{A.ptr.p, A.col.p, A.val.p, A.rd, A.cd, B.ptr.p, B.col.p, B.val.p, B.cd,
                       C.ptr.p, C.col.p, C.val.p};
-    vals.boff = W.boff.p, vals.total = total;
+    vals.boff = W.boff.p, vals.total = total, vals.upper = symmetric ? 1 : 0;
     FE_CHECK(ex.rows(A.n, vals));
+    if (symmetric) FE_CHECK(ex.rows(A.n, PassMirrorLower{C.ptr.p, C.col.p, C.val.p, C.rd}));
     return FE_OK;
 }
 
@@ -512,7 +522,7 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
         FE_CHECK(ex.alloc(L.PT.val, (size_t)std::max<int64_t>(L.PT.nnzb * m * dd, 1)));
         FE_CHECK(ex.rows(na, PassRestrVals{L.PT.ptr.p, L.PT.col.p, L.PT.val.p, L.P.ptr.p, L.P.col.p, L.P.val.p, dd, m}));
         ex.phase(kPhaseGalerkin);
-        FE_CHECK(product(ex, L.PT, AP, Ac, W));
+        FE_CHECK(product(ex, L.PT, AP, Ac, W, true));
         // the level keeps A; the next level starts from A_c and the coarse near-null space
         L.A = A;
         A = Ac;
