@@ -562,7 +562,8 @@ def run_ours(args, dist):
         # hundreds of uneven instances in one batched system (persistent kernel, CUDA
         # graph, autotuned tiles) against the same instances solved one at a time
         from finite_elements_gb300 import batch_bench, meshgen as mg
-        ba = argparse.Namespace(tol=args.tol, single=args.batch_single, cheb=16, cheb_ratio=1e4)
+        ba = argparse.Namespace(n=args.batch_n, seed=args.seed, tol=args.tol, single=args.batch_single, cheb=16,
+                                cheb_ratio=1e4)
         out["batched"] = dict(batch_bench.measure(ba, mg.batch_c4(args.batch_n, seed=args.seed)),
                               method="python -m finite_elements_gb300.batch_bench --n "
                                      f"{args.batch_n} --single {args.batch_single} --seed {args.seed}")
