@@ -67,6 +67,16 @@ FE_HD void heap_sort(int32_t *a, int64_t n) {
     }
 }
 
+// Atomic add on an int64 counter, on the device and on the host executor's threads;
+// returns the old value.
+FE_HD int64_t atomic_add_i64(int64_t *p, int64_t v) {
+#ifdef __CUDA_ARCH__
+    return (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+#else
+    return __atomic_fetch_add(p, v, __ATOMIC_RELAXED);
+#endif
+}
+
 // Sort a[0..n) and drop repeats; returns the number of distinct values.
 FE_HD int64_t sort_unique(int32_t *a, int64_t n) {
     if (n <= 1) return n;
@@ -91,19 +101,22 @@ FE_HD int64_t find_sorted(const int32_t *a, int64_t lo, int64_t hi, int32_t v) {
 // ------------------------------------------------------------------ block inverses
 
 // Pseudo-inverse of a symmetric D x D block by cyclic Jacobi: V diag(1/l) V^T over the
-// eigenvalues above 1e-12 of the largest in magnitude.  D is a template argument so
-// that the block and its eigenvectors stay in registers.
+// eigenvalues above 1e-12 of the largest in magnitude.  The sweeps stop once the
+// off-diagonal part is below 1e-30 of the block's squared Frobenius norm (rounding
+// level; Jacobi converges quadratically, a few sweeps), or after 60.  D is a template
+// argument so that the block and its eigenvectors stay in registers.
 template <int D>
 FE_HD void sym_pinv_n(const double *a, double *out) {
     double A[D * D], V[D * D];
-    for (int i = 0; i < D * D; ++i) A[i] = a[i];
+    double fro = 0.0;
+    for (int i = 0; i < D * D; ++i) A[i] = a[i], fro += a[i] * a[i];
     for (int i = 0; i < D; ++i)
         for (int j = 0; j < D; ++j) V[i * D + j] = i == j ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0.0;
         for (int p = 0; p < D; ++p)
             for (int q = p + 1; q < D; ++q) off += A[p * D + q] * A[p * D + q];
-        if (off < 1e-30) break;
+        if (off <= 1e-30 * fro) break;
         for (int p = 0; p < D; ++p)
             for (int q = p + 1; q < D; ++q) {
                 const double apq = A[p * D + q];
@@ -262,31 +275,6 @@ FE_HD void row_join_neighbour(const int64_t *ptr, const int32_t *col, const uint
     agg2[i] = best;
 }
 
-// Candidates for the members of aggregate c: its root, the root's neighbours and theirs
-// (every member lies within two strong hops of the root).
-FE_HD int64_t agg_member_bound(const int64_t *ptr, const int32_t *col, const int32_t *roots, int64_t c) {
-    const int64_t r = roots[c];
-    int64_t b = 1 + (ptr[r + 1] - ptr[r]);
-    for (int64_t s = ptr[r]; s < ptr[r + 1]; ++s) b += ptr[col[s] + 1] - ptr[col[s]];
-    return b;
-}
-
-// The members of aggregate c in increasing node order, written to cand[]; returns
-// their count.  cand holds agg_member_bound entries.
-FE_HD int64_t agg_members(const int64_t *ptr, const int32_t *col, const int32_t *roots, const int32_t *agg, int64_t c,
-                          int32_t *cand) {
-    const int64_t r = roots[c];
-    int64_t n = 0;
-    cand[n++] = (int32_t)r;
-    for (int64_t s = ptr[r]; s < ptr[r + 1]; ++s) {
-        const int64_t j = col[s];
-        if (agg[j] == c) cand[n++] = (int32_t)j;
-        for (int64_t t = ptr[j]; t < ptr[j + 1]; ++t)
-            if (agg[col[t]] == c) cand[n++] = col[t];
-    }
-    return sort_unique(cand, n);
-}
-
 // Thin QR of the aggregate's near-null-space rows, in place: on entry pt[(i d + a) m + b]
 // holds B of member i (rows a < d, columns b < m), on exit the orthonormal factor Q
 // (columns whose remainder falls below 1e-12 of their norm set to zero); R (m x m,
@@ -421,20 +409,8 @@ FE_HD void row_smooth_prolongator(const int64_t *pptr, const int32_t *pcol, doub
 }
 
 // Rows of the restriction P^T: row c holds the nodes i whose prolongator row has the
-// column c, i.e. (A's pattern being symmetric) the neighbours of c's members.
-FE_HD int64_t row_restriction_bound(const int64_t *mptr, const int32_t *mem, const int64_t *aptr, int64_t c) {
-    int64_t b = 0;
-    for (int64_t t = mptr[c]; t < mptr[c + 1]; ++t) b += aptr[mem[t] + 1] - aptr[mem[t]];
-    return b;
-}
-
-FE_HD int64_t row_restriction_columns(const int64_t *mptr, const int32_t *mem, const int64_t *aptr,
-                                      const int32_t *acol, int64_t c, int32_t *cand) {
-    int64_t n = 0;
-    for (int64_t t = mptr[c]; t < mptr[c + 1]; ++t)
-        for (int64_t s = aptr[mem[t]]; s < aptr[mem[t] + 1]; ++s) cand[n++] = acol[s];
-    return sort_unique(cand, n);
-}
+// column c, i.e. (A's pattern being symmetric) the neighbours of c's members -- the
+// columns of the product (member lists) x A, found with the product passes.
 
 // Values of row c of P^T: the transposed block (m x d) of P at (i, c) for every column i.
 FE_HD void row_restriction_values(const int64_t *rptr, const int32_t *rcol, double *rval, const int64_t *pptr,

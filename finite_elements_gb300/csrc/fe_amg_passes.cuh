@@ -193,16 +193,31 @@ struct PassJoinNeighbour {
     }
 };
 
-struct PassMemberBound {
-    const int64_t *ptr; const int32_t *col; const int32_t *roots; int64_t *bound;
-    FE_HD void operator()(int64_t c) const { bound[c] = agg_member_bound(ptr, col, roots, c); }
+// Member lists by a counting sort of the nodes on their aggregates: counts, offsets
+// (a scan), then every node into its aggregate's row through an atomic cursor, then
+// each row sorted, so that the lists come out in node order whatever the order of the
+// atomics.
+struct PassZeroI64 {
+    int64_t *p;
+    FE_HD void operator()(int64_t i) const { p[i] = 0; }
 };
 
-struct PassMembers {
-    const int64_t *ptr; const int32_t *col; const int32_t *roots; const int32_t *agg; const int64_t *boff;
-    int32_t *cand; int64_t *cnt;
-    int64_t total = 0;   // the bounds' sum (set by distinct_rows)
-    FE_HD void operator()(int64_t c) const { cnt[c] = agg_members(ptr, col, roots, agg, c, cand + boff[c]); }
+struct PassMemberCount {
+    const int32_t *agg; int64_t *cnt;
+    FE_HD void operator()(int64_t i) const { atomic_add_i64(&cnt[agg[i]], 1); }
+};
+
+struct PassMemberScatter {
+    const int32_t *agg; const int64_t *mptr; int64_t *cursor; int32_t *mem;
+    FE_HD void operator()(int64_t i) const {
+        const int64_t c = agg[i];
+        mem[mptr[c] + atomic_add_i64(&cursor[c], 1)] = (int32_t)i;
+    }
+};
+
+struct PassSortRows {
+    const int64_t *ptr; int32_t *col;
+    FE_HD void operator()(int64_t r) const { heap_sort(col + ptr[r], ptr[r + 1] - ptr[r]); }
 };
 
 // packed rows: dst[off[r] ..] = src[boff[r] ..], off[r+1] - off[r] entries
@@ -262,18 +277,6 @@ struct PassSmooth {
     const int64_t *pptr; const int32_t *pcol; double *pval; const double *dinv; const double *ptent;
     const int32_t *agg; int d; int m; double w;
     FE_HD void operator()(int64_t i) const { row_smooth_prolongator(pptr, pcol, pval, dinv, ptent, agg, d, m, w, i); }
-};
-
-struct PassRestrBound {
-    const int64_t *mptr; const int32_t *mem; const int64_t *aptr; int64_t *bound;
-    FE_HD void operator()(int64_t c) const { bound[c] = row_restriction_bound(mptr, mem, aptr, c); }
-};
-
-struct PassRestrCols {
-    const int64_t *mptr; const int32_t *mem; const int64_t *aptr; const int32_t *acol; const int64_t *boff;
-    int32_t *cand; int64_t *cnt;
-    int64_t total = 0;   // the bounds' sum (set by distinct_rows)
-    FE_HD void operator()(int64_t c) const { cnt[c] = row_restriction_columns(mptr, mem, aptr, acol, c, cand + boff[c]); }
 };
 
 struct PassRestrVals {
@@ -490,8 +493,17 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
         // members of every aggregate in node order (rows = aggregates, no values)
         ex.phase(kPhaseTentative);
         Mem.n = na;
-        FE_CHECK(distinct_rows(ex, na, PassMemberBound{A.ptr.p, A.col.p, roots.p, nullptr},
-                               PassMembers{A.ptr.p, A.col.p, roots.p, L.agg.p, nullptr, nullptr, nullptr}, Mem, W));
+        FE_CHECK(ex.alloc(W.cnt, (size_t)na));
+        FE_CHECK(ex.rows(na, PassZeroI64{W.cnt.p}));
+        FE_CHECK(ex.rows(n, PassMemberCount{L.agg.p, W.cnt.p}));
+        FE_CHECK(ex.alloc(Mem.ptr, (size_t)na + 1));
+        FE_CHECK(ex.scan(W.cnt.p, na, Mem.ptr.p, &Mem.nnzb));
+        FE_CHECK(ex.alloc(Mem.col, (size_t)std::max<int64_t>(n, 1)));
+        FE_CHECK(ex.rows(na, PassZeroI64{W.cnt.p}));
+        if (Mem.nnzb == n) {
+            FE_CHECK(ex.rows(n, PassMemberScatter{L.agg.p, Mem.ptr.p, W.cnt.p, Mem.col.p}));
+            FE_CHECK(ex.rows(na, PassSortRows{Mem.ptr.p, Mem.col.p}));
+        }
         if (Mem.nnzb != n) {
             set_error("multigrid setup: aggregate members do not cover the nodes");
             return FE_BREAKDOWN;
@@ -516,8 +528,9 @@ int setup_hierarchy(Ex &ex, Csr A, DBuf<double> B, int m, double theta, int64_t 
         FE_CHECK(product(ex, A, L.P, AP, W));
         ex.phase(kPhaseRestriction);
         L.PT.n = na, L.PT.rd = m, L.PT.cd = dd;
-        FE_CHECK(distinct_rows(ex, na, PassRestrBound{Mem.ptr.p, Mem.col.p, A.ptr.p, nullptr},
-                               PassRestrCols{Mem.ptr.p, Mem.col.p, A.ptr.p, A.col.p, nullptr, nullptr, nullptr}, L.PT,
+        // the pattern of P^T: the columns of (member lists) x A, as a product's
+        FE_CHECK(distinct_rows(ex, na, PassProdBound{Mem.ptr.p, Mem.col.p, A.ptr.p, nullptr},
+                               PassProdCols{Mem.ptr.p, Mem.col.p, A.ptr.p, A.col.p, nullptr, nullptr, nullptr}, L.PT,
                                W));
         FE_CHECK(ex.alloc(L.PT.val, (size_t)std::max<int64_t>(L.PT.nnzb * m * dd, 1)));
         FE_CHECK(ex.rows(na, PassRestrVals{L.PT.ptr.p, L.PT.col.p, L.PT.val.p, L.P.ptr.p, L.P.col.p, L.P.val.p, dd, m}));
