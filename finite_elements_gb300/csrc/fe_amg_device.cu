@@ -414,6 +414,19 @@ int precondition_sell(CycleEx &ex, const std::vector<amg::CycleLevel> &levels, c
     return FE_OK;
 }
 
+// z = M^-1 r when the hierarchy has no level (a system of at most a few thousand DOFs):
+// the coarsest level is the system itself and its dense inverse the preconditioner
+int precondition_dense(CycleEx &ex, const amg::CycleCoarse &C, const double *r, double *z) {
+    ex.mark(2);
+    ex.mark(0);
+    FE_CHECK(ex.rows(C.n, amg::PassToF32{r, C.r}));
+    FE_CHECK(ex.rows(C.n, amg::PassDense{C.n, C.inv, C.r, C.x}));
+    FE_CHECK(ex.rows(C.n, amg::PassToF64{C.x, z}));
+    ex.mark(1);
+    ex.mark(3);
+    return FE_OK;
+}
+
 }  // namespace
 
 // PCG on the eliminated system preconditioned by one FP32 V-cycle (k = 3 Chebyshev steps
@@ -440,12 +453,9 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     for (size_t l = 0; l < G.L.size(); ++l) FE_CHECK(prepare_cycle(h, G.mem, G.L[l], l > 0));
     FE_CHECK(palloc(G.mem, G.rc, (size_t)std::max<int64_t>(G.nc, 1)));
     FE_CHECK(palloc(G.mem, G.xc, (size_t)std::max<int64_t>(G.nc, 1)));
-    if (G.L.empty()) {
-        set_error("fe_solve: the multigrid hierarchy has a single level (use the other preconditioners)");
-        return FE_BAD_INPUT;
-    }
+    // the system's operator: level 0, or the coarsest level when there is no other
+    const DevCsr &A0 = G.L.empty() ? G.coarse : G.L[0].A;
     // PCG vectors; the solution goes to the handle's x
-    DevLevel &L0 = G.L[0];
     DBuf<double> r, p, q, z;
     struct Free {
         const MgMem &m;
@@ -473,7 +483,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     amg::CycleCoarse coarse;
     coarse.n = G.nc, coarse.inv = G.cinv.p, coarse.r = G.rc.p, coarse.x = G.xc.p;
     CycleEx cex{h, G.mem};
-    cex.sell_ptr = L0.A.ptr.p;
+    cex.sell_ptr = A0.ptr.p;
     if (prof) cex.marks = h->w.pev;
     for (const DevLevel &Dl : G.L) {
         const double n_rows = (double)std::max<int64_t>(Dl.A.n, 1), n_aggr = (double)std::max<int64_t>(Dl.PT.n, 1);
@@ -495,7 +505,8 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         const int64_t l0 = h->launches;
         cudaGraph_t g = nullptr;
         FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        const int rc = precondition_sell(cex, views, coarse, 3, r.p, z.p);
+        const int rc = G.L.empty() ? precondition_dense(cex, coarse, r.p, z.p)
+                                   : precondition_sell(cex, views, coarse, 3, r.p, z.p);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc != FE_OK) {
             if (ce == cudaSuccess && g) cudaGraphDestroy(g);
@@ -556,7 +567,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     bool stagnated = false;
     for (;;) {
         int it = 0;
-        FE_CHECK(amg::pcg(cex, n, D, L0.A.ptr.p, L0.A.col.p, L0.A.val.p, h->b.p, v, precond, tol,
+        FE_CHECK(amg::pcg(cex, n, D, A0.ptr.p, A0.col.p, A0.val.p, h->b.p, v, precond, tol,
                           max_iter - total, &it, &relres, &status, true));
         total += it;
         if (status != FE_OK || relres <= tol || restarts >= max_restart || total >= max_iter) break;

@@ -167,6 +167,24 @@ def test_solve_is_deterministic(systems):
 
 
 @pytest.mark.parametrize("name", gc.names())
+def test_drop_in_analysis_multigrid(gpu_lib, name):
+    """The drop-in's solve with the multigrid-preconditioned mixed solver
+    (solver={"precision": "mixed-cg64", "multigrid": True}) gives the reference's
+    solution within 1e-9.  These systems are small: their hierarchy has no level, and
+    the preconditioner is the device's dense inverse of the whole system (continuity
+    cases take the projected PCG whatever the flag)."""
+    from test_abi_host import build_objects
+    from finite_elements_gb300.analysis import FiniteElementAnalysis
+    prob, ref, mesh, kw = build_objects(name)
+    if "x" not in ref:
+        pytest.skip("the reference raises on this case (covered by test_drop_in_analysis)")
+    fea = FiniteElementAnalysis(mesh=mesh, solver={"precision": "mixed-cg64", "multigrid": True, "tol": 1e-13,
+                                                   "accept_stagnation": True}, **kw)
+    x = np.array(fea.solve().result_vector)
+    assert np.linalg.norm(x - ref["x"]) <= 1e-9 * np.linalg.norm(ref["x"]), fea.last_stats
+
+
+@pytest.mark.parametrize("name", gc.names())
 def test_drop_in_analysis(gpu_lib, name):
     """The reference's user-facing flow on drop-in objects: create_matrix,
     create_source_matrix, solve -> Result."""
