@@ -20,6 +20,8 @@ using DevCsr = amg::Csr;
 struct MgMem {
     cudaStream_t s = nullptr;
     cudaMemPool_t pool = nullptr;
+    double *pinned = nullptr;   // 8 pinned host doubles for scalar reads (a copy to
+                                // pageable memory would be staged and wait longer)
 };
 
 // the handle's pool (created on first use, release threshold unbounded)

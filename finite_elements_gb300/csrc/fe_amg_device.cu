@@ -317,8 +317,9 @@ struct CycleEx {
         ka_dot_final<<<1, kAT, 0, h->stream>>>(g, part.p, sc.p);
         FE_LAUNCH_CHECK();
         h->launches += 2;
-        FE_CUDA(cudaMemcpyAsync(out, sc.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        FE_CUDA(cudaMemcpyAsync(mem.pinned, sc.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         FE_CUDA(cudaStreamSynchronize(h->stream));
+        *out = mem.pinned[0];
         return FE_OK;
     }
     template <class F>

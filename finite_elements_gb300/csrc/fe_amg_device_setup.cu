@@ -100,8 +100,10 @@ int scan64(const int64_t *in, int64_t n, int64_t *out, int64_t *total, DBuf<int6
     ks_scan_tiles<<<1, 1, 0, s>>>(nt, tmp.p, out, n);
     ks_tile_scan<<<(unsigned)nt, kST, 0, s>>>(in, n, tmp.p, out);
     FE_LAUNCH_CHECK();
-    FE_CUDA(cudaMemcpyAsync(total, out + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    int64_t *pin = reinterpret_cast<int64_t *>(mem.pinned);
+    FE_CUDA(cudaMemcpyAsync(pin, out + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
+    *total = *pin;
     return FE_OK;
 }
 
@@ -587,7 +589,10 @@ struct DevEx {
         kd_dot<<<g, kST, 0, s>>>(n, a, b, part.p);
         kd_dot_final<<<1, kST, 0, s>>>(g, part.p, sc.p);
         FE_LAUNCH_CHECK();
-        return read(out, sc.p, 1);
+        FE_CUDA(cudaMemcpyAsync(mem.pinned, sc.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        *out = mem.pinned[0];
+        return FE_OK;
     }
 };
 
@@ -824,7 +829,8 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G) {
     kc_dense_fill<<<grid_s(C.n), kST, 0, s>>>(C.n, C.rd, C.ptr.p, C.col.p, C.val.p, n, G.cinv.p);
     kc_regularise<<<1, kST, 0, s>>>(n, G.cinv.p);
     FE_LAUNCH_CHECK();
-    // the cooperative grid: at most two blocks per SM (more add barrier arrivals, and
+    // the cooperative grid: at most two blocks per SM (measured 16 ms for the 1,941-DOF
+    // coarsest level of the 4M-DOF system, 22.6 ms on four: more barrier arrivals, and
     // the 32 x 32 tiles of one update number about (n / 32)^2 / 2)
     int dev = 0, sms = 0, per_sm = 0;
     FE_CUDA(cudaGetDevice(&dev));
@@ -880,8 +886,10 @@ int mg_memory(fe_handle_s *h, MgMem *out) {
         }
         h->mg_pool = pool;
     }
+    if (!h->mg_pinned) FE_CUDA(cudaMallocHost((void **)&h->mg_pinned, 8 * sizeof(double)));
     out->s = h->stream;
     out->pool = h->mg_pool;
+    out->pinned = h->mg_pinned;
     return FE_OK;
 }
 

@@ -149,6 +149,7 @@ int fe_destroy(fe_handle h) {
         if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->mg_pool) cudaMemPoolDestroy(h->mg_pool);
+    if (h->mg_pinned) cudaFreeHost(h->mg_pinned);
     delete h;
     return FE_OK;
 }

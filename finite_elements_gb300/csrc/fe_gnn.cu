@@ -202,20 +202,35 @@ k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, co
     bool ok = true;
     for (int64_t tile = blockIdx.x; tile * kTcRows < N && ok; tile += gridDim.x) {
         const int64_t row0 = tile * kTcRows;
-        // A: 128 rows x KI, 16-byte chunks of 8 k (consecutive threads, consecutive rows)
-        for (int c = threadIdx.x; c < kTcRows * KI / 8; c += blockDim.x) {
-            const int r = c % kTcRows, k = (c / kTcRows) * 8;
-            const int64_t gr = row0 + r;
-            float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
-            if (gr < N) {
-                const float *src = k < K1 ? X1 + gr * K1 + k : X2 + gr * (KI - K1) + (k - K1);
-                v0 = *reinterpret_cast<const float4 *>(src);
-                v1 = *reinterpret_cast<const float4 *>(src + 4);
+        // A: 128 rows x KI, 16-byte chunks of 8 k (consecutive threads, consecutive rows);
+        // a thread issues the loads of up to 4 chunks before it converts any of them, so
+        // that 8 loads per thread are in flight
+        constexpr int CHUNKS = kTcRows * KI / 8, PER = CHUNKS / kTcThreads, BATCH = PER < 4 ? PER : 4;
+        static_assert(CHUNKS % kTcThreads == 0 && PER % BATCH == 0, "chunks per thread");
+#pragma unroll
+        for (int j0 = 0; j0 < PER; j0 += BATCH) {
+            float4 v[BATCH][2];
+#pragma unroll
+            for (int j = 0; j < BATCH; ++j) {
+                const int c = threadIdx.x + (j0 + j) * kTcThreads;
+                const int r = c % kTcRows, k = (c / kTcRows) * 8;
+                const int64_t gr = row0 + r;
+                v[j][0] = v[j][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (gr < N) {
+                    const float *src = k < K1 ? X1 + gr * K1 + k : X2 + gr * (KI - K1) + (k - K1);
+                    v[j][0] = *reinterpret_cast<const float4 *>(src);
+                    v[j][1] = *reinterpret_cast<const float4 *>(src + 4);
+                }
             }
-            uint4 q;
-            q.x = pack_bf16(v0.x, v0.y), q.y = pack_bf16(v0.z, v0.w);
-            q.z = pack_bf16(v1.x, v1.y), q.w = pack_bf16(v1.z, v1.w);
-            *reinterpret_cast<uint4 *>(As + tc_off(r, k, KI)) = q;
+#pragma unroll
+            for (int j = 0; j < BATCH; ++j) {
+                const int c = threadIdx.x + (j0 + j) * kTcThreads;
+                const int r = c % kTcRows, k = (c / kTcRows) * 8;
+                uint4 q;
+                q.x = pack_bf16(v[j][0].x, v[j][0].y), q.y = pack_bf16(v[j][0].z, v[j][0].w);
+                q.z = pack_bf16(v[j][1].x, v[j][1].y), q.w = pack_bf16(v[j][1].z, v[j][1].w);
+                *reinterpret_cast<uint4 *>(As + tc_off(r, k, KI)) = q;
+            }
         }
         fence_async_smem();
         __syncthreads();

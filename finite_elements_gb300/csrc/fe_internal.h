@@ -226,6 +226,7 @@ struct fe_handle_s {
     // memory pool of the multigrid solve's stream-ordered allocations (kept between
     // solves; created on first use)
     cudaMemPool_t mg_pool = nullptr;
+    double *mg_pinned = nullptr;   // 8 pinned doubles: the multigrid's scalar reads to the host
     bool singular = false;                // a diagonal block could not be inverted
     fe::DBuf<double> ke;                  // [n_elem][(3d)^2]
     fe::DBuf<double> me_scale;            // [n_elem] rho*A*t/12
