@@ -200,11 +200,11 @@ int launch_dinv_product(int64_t n, const amg::PassDinvProduct &f, cudaStream_t s
 // ---------------------------------------------------------------- sparse products, a warp per row
 // Rows of C = A B whose product lists are long (the Galerkin products and the coarser
 // levels) get a warp each instead of a thread: the candidates are gathered into shared
-// memory by the 32 lanes, bitonic-sorted there and compacted; the values are summed per
-// output entry in the order of the factors' entries (the order of the thread-per-row
-// version), each lane owning the output entries p = lane, lane + 32, ... after a stable
-// counting sort of the product terms by output entry.  Rows beyond the shared-memory
-// capacity fall back to the row operation of one lane.
+// memory by the 32 lanes, bitonic-sorted there and compacted; after a stable counting
+// sort of the product terms by output entry the values are summed term-parallel
+// (kd_prod_vals_warp) or by the lane owning the entry, in the factors' order
+// (kd_prod_vals_long, the thread-per-row order).  Rows beyond the shared-memory capacity
+// fall back to the row operation of one lane.
 
 constexpr int kPW = 2;          // warps per block of the warp-per-row product kernels
 constexpr int kColCap = 4096;   // candidates a warp sorts in shared memory
@@ -319,21 +319,45 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::Pa
             if (p >= 0 && lane == 31 - __clz(peers)) off[p] += __popc(peers);
             __syncwarp();
         }
-        // each lane sums its output entries' terms in order
+        // the values, term-parallel: the terms ordered by output entry are taken 32 at a
+        // time, a lane computes one term's block product, a segmented scan across the
+        // lanes (a fixed shuffle tree) sums the terms of each entry within the chunk, and
+        // the lane ending an entry's segment adds that partial to the entry -- chunk after
+        // chunk, so the sums are deterministic (a lane summing its entries' terms alone
+        // left ~3 of 4 lanes idle: rows have few entries of uneven length)
         for (int64_t p = lane; p < lc; p += 32) {
-            double acc[RA && CB ? RA * CB : 36];
-            for (int k = 0; k < bs; ++k) acc[k] = 0.0;
-            for (int q = off[p] - cnt[p]; q < off[p]; ++q) {
-                const int t = ord[q];
-                const double *a = f.aval + (int64_t)ss[t] * ra * ca;
-                const double *b = f.bval + (int64_t)ts[t] * ca * cb;
-                amg::block_mul_add(a, b, ra, ca, cb, acc);
-            }
             if (f.upper && f.ccol[c0 + p] < i) continue;   // filled by the mirror pass
             double *o = f.cval + (c0 + p) * bs;
-            for (int k = 0; k < bs; ++k) o[k] = acc[k];
+            for (int k = 0; k < bs; ++k) o[k] = 0.0;
         }
         __syncwarp();
+        const int tv = lc > 0 ? off[lc - 1] : 0;   // the terms that reach an entry
+        for (int q0 = 0; q0 < tv; q0 += 32) {
+            const int q = q0 + lane;
+            const bool valid = q < tv;
+            const int t = valid ? ord[q] : 0;
+            const int key = valid ? pos[t] : -1 - lane;   // sorted over the valid lanes
+            double v[RA && CB ? RA * CB : 36];
+            for (int k = 0; k < bs; ++k) v[k] = 0.0;
+            if (valid)
+                amg::block_mul_add(f.aval + (int64_t)ss[t] * ra * ca, f.bval + (int64_t)ts[t] * ca * cb, ra, ca, cb,
+                                   v);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int kup = __shfl_up_sync(0xffffffffu, key, o);
+                const bool take = lane >= o && kup == key;
+                for (int k = 0; k < bs; ++k) {
+                    const double y = __shfl_up_sync(0xffffffffu, v[k], o);
+                    if (take) v[k] += y;
+                }
+            }
+            const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+            if (valid && (lane == 31 || q + 1 >= tv || knext != key)) {
+                double *o = f.cval + (c0 + key) * bs;
+                for (int k = 0; k < bs; ++k) o[k] += v[k];
+            }
+            __syncwarp();
+        }
     }
 }
 
