@@ -361,6 +361,13 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::Pa
     }
 }
 
+template <int RA, int CA, int CB>
+__global__ void __launch_bounds__(kST) kd_prod_vals_thread(int64_t n, amg::PassProdVals f) {
+    FE_ROWS(i, n)
+    amg::row_product_values_t<RA, CA, CB>(f.aptr, f.acol, f.aval, f.ra, f.ca, f.bptr, f.bcol, f.bval, f.cb, f.cptr,
+                                          f.ccol, f.cval, i, f.upper != 0);
+}
+
 // mean product terms per row at and above which the products take a warp per row
 constexpr double kWarpRowMean = 48.0;
 
@@ -592,7 +599,11 @@ struct DevEx {
     int rows(int64_t n, const amg::PassProdVals &f) {
         if (n <= 0) return FE_OK;
         if (!f.boff || (double)f.total < kWarpRowMean * (double)n) {
-            k_rows<amg::PassProdVals><<<grid_s(n), kST, 0, s>>>(n, f);
+            // a thread per row, block sizes fixed at compile time where the hierarchies have them
+            if (f.ra == 2 && f.ca == 2 && f.cb == 3) kd_prod_vals_thread<2, 2, 3><<<grid_s(n), kST, 0, s>>>(n, f);
+            else if (f.ra == 3 && f.ca == 3 && f.cb == 3) kd_prod_vals_thread<3, 3, 3><<<grid_s(n), kST, 0, s>>>(n, f);
+            else if (f.ra == 3 && f.ca == 2 && f.cb == 3) kd_prod_vals_thread<3, 2, 3><<<grid_s(n), kST, 0, s>>>(n, f);
+            else k_rows<amg::PassProdVals><<<grid_s(n), kST, 0, s>>>(n, f);
         } else if (f.ra == 2 && f.ca == 2 && f.cb == 3) {
             return launch_prod_vals<2, 2, 3>(n, f, s);
         } else if (f.ra == 3 && f.ca == 2 && f.cb == 3) {

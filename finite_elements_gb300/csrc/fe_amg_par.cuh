@@ -354,24 +354,65 @@ FE_HD void block_mul_add(const double *a, const double *b, int ra, int ca, int c
 }
 
 // Row i of C = A B (upper: only the entries whose block column is at least i, for a
-// product known to be symmetric; the others are left for PassMirrorLower).
-FE_HD void row_product_values(const int64_t *aptr, const int32_t *acol, const double *aval, int ra, int ca,
-                              const int64_t *bptr, const int32_t *bcol, const double *bval, int cb,
-                              const int64_t *cptr, const int32_t *ccol, double *cval, int64_t i,
-                              bool upper = false) {
+// product known to be symmetric; the others are left for PassMirrorLower).  C's row is
+// the union of the B rows that A's row selects, all sorted, so the entries are produced
+// in column order by a merge: one cursor per entry of A's row into its B row, and each
+// entry summed in registers over A's entries in order (the order of a term-by-term
+// accumulation, without a search or a read-modify-write per term).  RA, CA, CB: the
+// block sizes when known at compile time (0: ra, ca, cb).  Rows of more than kMergeA
+// entries of A take the term-by-term path.
+constexpr int kMergeA = 16;
+
+template <int RA, int CA, int CB>
+FE_HD void row_product_values_t(const int64_t *aptr, const int32_t *acol, const double *aval, int ra_, int ca_,
+                                const int64_t *bptr, const int32_t *bcol, const double *bval, int cb_,
+                                const int64_t *cptr, const int32_t *ccol, double *cval, int64_t i, bool upper) {
+    const int ra = RA ? RA : ra_, ca = CA ? CA : ca_, cb = CB ? CB : cb_;
     const int bs = ra * cb;
+    const int64_t a0 = aptr[i], la = aptr[i + 1] - a0;
+    if (la <= kMergeA) {
+        int64_t cur[kMergeA], end[kMergeA];
+        for (int64_t q = 0; q < la; ++q) {
+            const int64_t j = acol[a0 + q];
+            cur[q] = bptr[j], end[q] = bptr[j + 1];
+        }
+        for (int64_t p = cptr[i]; p < cptr[i + 1]; ++p) {
+            const int32_t c = ccol[p];
+            if (upper && c < i) continue;   // filled by the mirror pass; cursors move on below
+            double acc[RA && CB ? RA * CB : 36];
+            for (int k = 0; k < bs; ++k) acc[k] = 0.0;
+            for (int64_t q = 0; q < la; ++q) {
+                int64_t t = cur[q];
+                while (t < end[q] && bcol[t] < c) ++t;
+                if (t < end[q] && bcol[t] == c) {
+                    block_mul_add(&aval[(a0 + q) * ra * ca], &bval[t * ca * cb], ra, ca, cb, acc);
+                    ++t;
+                }
+                cur[q] = t;
+            }
+            double *o = &cval[p * bs];
+            for (int k = 0; k < bs; ++k) o[k] = acc[k];
+        }
+        return;
+    }
     for (int64_t k = cptr[i] * bs; k < cptr[i + 1] * bs; ++k) cval[k] = 0.0;
-    for (int64_t s = aptr[i]; s < aptr[i + 1]; ++s) {
+    for (int64_t s = a0; s < a0 + la; ++s) {
         const double *a = &aval[s * ra * ca];
         const int64_t j = acol[s];
         for (int64_t t = bptr[j]; t < bptr[j + 1]; ++t) {
             if (upper && bcol[t] < i) continue;
-            const double *b = &bval[t * ca * cb];
             const int64_t p = find_sorted(ccol, cptr[i], cptr[i + 1], bcol[t]);
             if (p < 0) continue;   // cannot happen: the columns come from these products
-            block_mul_add(a, b, ra, ca, cb, &cval[p * bs]);
+            block_mul_add(a, &bval[t * ca * cb], ra, ca, cb, &cval[p * bs]);
         }
     }
+}
+
+FE_HD void row_product_values(const int64_t *aptr, const int32_t *acol, const double *aval, int ra, int ca,
+                              const int64_t *bptr, const int32_t *bcol, const double *bval, int cb,
+                              const int64_t *cptr, const int32_t *ccol, double *cval, int64_t i,
+                              bool upper = false) {
+    row_product_values_t<0, 0, 0>(aptr, acol, aval, ra, ca, bptr, bcol, bval, cb, cptr, ccol, cval, i, upper);
 }
 
 // The lower entries of a symmetric product row: block (i, j), j < i, is the transpose
