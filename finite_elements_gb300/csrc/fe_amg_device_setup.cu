@@ -617,6 +617,15 @@ struct DevEx {
         return FE_OK;
     }
     int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total) { return scan64(in, n, out, total, scan_tmp, mem); }
+    // a . b into device memory, in stream order (deterministic two-stage sum)
+    int dot_to(const double *a, const double *b, int64_t n, double *dst) {
+        const int g = grid_s(n);
+        FE_CHECK(palloc(mem, part, (size_t)g));
+        kd_dot<<<g, kST, 0, s>>>(n, a, b, part.p);
+        kd_dot_final<<<1, kST, 0, s>>>(g, part.p, dst);
+        FE_LAUNCH_CHECK();
+        return FE_OK;
+    }
     int dot(const double *a, const double *b, int64_t n, double *out) {
         const int g = grid_s(n);
         FE_CHECK(palloc(mem, part, (size_t)g));

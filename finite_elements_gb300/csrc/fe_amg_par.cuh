@@ -331,10 +331,33 @@ FE_HD int64_t row_product_bound(const int64_t *aptr, const int32_t *acol, const 
 
 // The distinct columns of row i of C = A B, sorted, in cand[] (row_product_bound
 // entries); returns their count.
+// Rows of A with at most kMergeA entries merge the sorted B rows they select (one cursor
+// each) instead of gathering and sorting: row_product_columns and row_product_values.
+constexpr int kMergeA = 16;
+
 FE_HD int64_t row_product_columns(const int64_t *aptr, const int32_t *acol, const int64_t *bptr, const int32_t *bcol,
                                   int64_t i, int32_t *cand) {
+    const int64_t a0 = aptr[i], la = aptr[i + 1] - a0;
+    if (la <= kMergeA) {
+        int64_t cur[kMergeA], end[kMergeA];
+        for (int64_t q = 0; q < la; ++q) {
+            const int64_t j = acol[a0 + q];
+            cur[q] = bptr[j], end[q] = bptr[j + 1];
+        }
+        int64_t n = 0;
+        for (;;) {
+            int32_t m = 0;
+            bool any = false;
+            for (int64_t q = 0; q < la; ++q)
+                if (cur[q] < end[q] && (!any || bcol[cur[q]] < m)) m = bcol[cur[q]], any = true;
+            if (!any) return n;
+            cand[n++] = m;
+            for (int64_t q = 0; q < la; ++q)
+                if (cur[q] < end[q] && bcol[cur[q]] == m) ++cur[q];
+        }
+    }
     int64_t n = 0;
-    for (int64_t s = aptr[i]; s < aptr[i + 1]; ++s)
+    for (int64_t s = a0; s < a0 + la; ++s)
         for (int64_t t = bptr[acol[s]]; t < bptr[acol[s] + 1]; ++t) cand[n++] = bcol[t];
     return sort_unique(cand, n);
 }
@@ -361,7 +384,6 @@ FE_HD void block_mul_add(const double *a, const double *b, int ra, int ca, int c
 // accumulation, without a search or a read-modify-write per term).  RA, CA, CB: the
 // block sizes when known at compile time (0: ra, ca, cb).  Rows of more than kMergeA
 // entries of A take the term-by-term path.
-constexpr int kMergeA = 16;
 
 template <int RA, int CA, int CB>
 FE_HD void row_product_values_t(const int64_t *aptr, const int32_t *acol, const double *aval, int ra_, int ca_,

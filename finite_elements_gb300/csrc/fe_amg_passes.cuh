@@ -13,6 +13,8 @@
 //   template <class F> int rows(int64_t n, const F &f);                // f(i) for i < n, any order
 //   int scan(const int64_t *in, int64_t n, int64_t *out, int64_t *total);   // exclusive, out[n] = total
 //   int dot(const double *a, const double *b, int64_t n, double *out);      // host value
+//   int dot_to(const double *a, const double *b, int64_t n, double *dst);   // into executor
+//                                                                           // memory, no wait
 //   void phase(int k);   // setup phase k (SetupPhase) starts here (timed by the device
 //                        // executor when profiling, ignored by the host one)
 #pragma once
@@ -122,11 +124,6 @@ struct PassCgStep {
     }
 };
 
-// p = z + beta p
-struct PassCgDirection {
-    double beta; const double *z; double *p;
-    FE_HD void operator()(int64_t i) const { p[i] = z[i] + beta * p[i]; }
-};
 
 
 struct PassBlockNorms {
@@ -345,46 +342,100 @@ int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W, bool symmet
 // approaches lmax from below far faster than power iteration does.
 constexpr int kLanczosSteps = 15;
 
+// The Lanczos estimate's scalars, in executor memory so that the CG steps run without
+// a read to the host: rz, rz0, p.q, r.z of the new residual, a stop flag, the steps done,
+// then alpha_j and beta_j.
+enum : int { kLzRz = 0, kLzRz0, kLzPq, kLzRzn, kLzStop, kLzM, kLzAlpha, kLzBeta = kLzAlpha + kLanczosSteps,
+             kLzSize = kLzBeta + kLanczosSteps };
+
+struct PassLanczosInit {
+    double *S;
+    FE_HD void operator()(int64_t) const {
+        S[kLzRz0] = S[kLzRz];
+        S[kLzStop] = S[kLzRz] > 0.0 ? 0.0 : 1.0;
+        S[kLzM] = 0.0;
+    }
+};
+
+// alpha_j = r.z / p.q; a product that is not positive stops the estimate
+struct PassLanczosAlpha {
+    double *S; int j;
+    FE_HD void operator()(int64_t) const {
+        if (S[kLzStop] != 0.0) return;
+        const double pq = S[kLzPq];
+        if (!(pq > 0.0) || !isfinite(pq)) {
+            S[kLzStop] = 1.0;
+            return;
+        }
+        S[kLzAlpha + j] = S[kLzRz] / pq;
+    }
+};
+
+// r_i -= alpha_j q_i, then z_i = D_i^-1 r_i
+struct PassLanczosStep {
+    const double *S; int j; const double *q; const double *dinv; int d; double *r; double *z;
+    FE_HD void operator()(int64_t i) const {
+        if (S[kLzStop] != 0.0) return;
+        PassCgStep{S[kLzAlpha + j], q, dinv, d, r, z}(i);
+    }
+};
+
+// beta_j = r.z (new) / r.z; the estimate stops once the Krylov space is exhausted
+struct PassLanczosBeta {
+    double *S; int j;
+    FE_HD void operator()(int64_t) const {
+        if (S[kLzStop] != 0.0) return;
+        const double rzn = S[kLzRzn];
+        S[kLzBeta + j] = rzn / S[kLzRz];
+        S[kLzM] = (double)(j + 1);
+        S[kLzRz] = rzn;
+        if (!(rzn > 1e-28 * S[kLzRz0])) S[kLzStop] = 1.0;
+    }
+};
+
+struct PassLanczosDirection {
+    const double *S; int j; const double *z; double *p;
+    FE_HD void operator()(int64_t i) const {
+        if (S[kLzStop] != 0.0) return;
+        p[i] = z[i] + S[kLzBeta + j] * p[i];
+    }
+};
+
 template <class Ex>
 int lmax_of(Ex &ex, const Csr &A, const double *dinv, double *lmax) {
     const int d = A.rd;
     const int64_t nd = A.n * d;
-    DBuf<double> r, z, p, q;
+    DBuf<double> r, z, p, q, S;
     struct Free {
         Ex &ex;
-        DBuf<double> &r, &z, &p, &q;
-        ~Free() { ex.release(r), ex.release(z), ex.release(p), ex.release(q); }
-    } fr{ex, r, z, p, q};
+        DBuf<double> &r, &z, &p, &q, &S;
+        ~Free() { ex.release(r), ex.release(z), ex.release(p), ex.release(q), ex.release(S); }
+    } fr{ex, r, z, p, q, S};
     const size_t v = (size_t)std::max<int64_t>(nd, 1);
     FE_CHECK(ex.alloc(r, v));
     FE_CHECK(ex.alloc(z, v));
     FE_CHECK(ex.alloc(p, v));
     FE_CHECK(ex.alloc(q, v));
+    FE_CHECK(ex.alloc(S, (size_t)kLzSize));
     FE_CHECK(ex.rows(nd, PassPowerStart{r.p}));
     FE_CHECK(ex.rows(A.n, PassJacobi{dinv, d, r.p, z.p}));
     FE_CHECK(ex.copy(p.p, z.p, (size_t)nd));
-    double rz = 0.0;
-    FE_CHECK(ex.dot(r.p, z.p, nd, &rz));
-    const double rz0 = rz;
-    double alpha[kLanczosSteps], beta[kLanczosSteps];
-    int m = 0;
+    FE_CHECK(ex.dot_to(r.p, z.p, nd, S.p + kLzRz));
+    FE_CHECK(ex.rows(1, PassLanczosInit{S.p}));
     const PassDinvProduct prod{A.ptr.p, A.col.p, A.val.p, nullptr, d, p.p, q.p, A.nnzb};
-    for (int j = 0; j < kLanczosSteps && rz > 0.0; ++j) {
+    for (int j = 0; j < kLanczosSteps; ++j) {
         FE_CHECK(ex.rows(A.n, prod));
-        double pq = 0.0;
-        FE_CHECK(ex.dot(p.p, q.p, nd, &pq));
-        if (!(pq > 0.0) || !std::isfinite(pq)) break;
-        alpha[m] = rz / pq;
-        FE_CHECK(ex.rows(A.n, PassCgStep{alpha[m], q.p, dinv, d, r.p, z.p}));
-        double rzn = 0.0;
-        FE_CHECK(ex.dot(r.p, z.p, nd, &rzn));
-        beta[m] = rzn / rz;
-        ++m;
-        rz = rzn;
-        if (!(rzn > 1e-28 * rz0)) break;   // converged: the Krylov space is exhausted
-        if (j + 1 < kLanczosSteps) FE_CHECK(ex.rows(nd, PassCgDirection{beta[m - 1], z.p, p.p}));
+        FE_CHECK(ex.dot_to(p.p, q.p, nd, S.p + kLzPq));
+        FE_CHECK(ex.rows(1, PassLanczosAlpha{S.p, j}));
+        FE_CHECK(ex.rows(A.n, PassLanczosStep{S.p, j, q.p, dinv, d, r.p, z.p}));
+        FE_CHECK(ex.dot_to(r.p, z.p, nd, S.p + kLzRzn));
+        FE_CHECK(ex.rows(1, PassLanczosBeta{S.p, j}));
+        if (j + 1 < kLanczosSteps) FE_CHECK(ex.rows(nd, PassLanczosDirection{S.p, j, z.p, p.p}));
     }
-    *lmax = m > 0 ? lanczos_lmax(alpha, beta, m) : 0.0;
+    double hs[kLzSize];
+    FE_CHECK(ex.read(hs, S.p, (size_t)kLzSize));
+    const int m = (int)hs[kLzM];
+    *lmax = m > 0 ? lanczos_lmax(hs + kLzAlpha, hs + kLzBeta, m) : 0.0;
     if (!std::isfinite(*lmax) || !(*lmax > 0.0)) {
         set_error("multigrid setup: the largest eigenvalue estimate is not positive");
         return FE_BREAKDOWN;

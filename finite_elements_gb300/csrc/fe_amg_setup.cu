@@ -465,6 +465,7 @@ struct HostEx {
         *total = run;
         return FE_OK;
     }
+    int dot_to(const double *a, const double *b, int64_t n, double *dst) { return dot(a, b, n, dst); }
     int dot(const double *a, const double *b, int64_t n, double *out) {
         double part[kChunks];
         for (int c = 0; c < kChunks; ++c) part[c] = 0.0;
