@@ -226,6 +226,21 @@ __device__ void warp_bitonic(int32_t *a, int m) {
         }
 }
 
+// The distinct candidates of a row: inserted into an open-addressing table in shared
+// memory (linear probing on a multiplicative hash, atomicCAS; at most `size` probes, and
+// the table never holds more values than it has slots), compacted, then bitonic-sorted
+// -- only the distinct values, far fewer than the candidates on the coarse levels.
+constexpr int32_t kEmpty = -1;
+
+__device__ __forceinline__ void table_insert(int32_t *tab, int size, int32_t c) {
+    uint32_t h = ((uint32_t)c * 2654435761u) & (uint32_t)(size - 1);
+    for (int probe = 0; probe < size; ++probe) {
+        const int32_t old = atomicCAS(&tab[h], kEmpty, c);
+        if (old == kEmpty || old == c) return;
+        h = (h + 1) & (uint32_t)(size - 1);
+    }
+}
+
 __global__ void __launch_bounds__(kPW * 32) kd_prod_cols_warp(int64_t n, amg::PassProdCols f) {
     __shared__ int32_t sh[kPW][kColCap];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
@@ -235,26 +250,33 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_cols_warp(int64_t n, amg::Pa
         const int64_t bound = f.boff[i + 1] - f.boff[i];
         int32_t *out = f.cand + f.boff[i];
         if (bound > kColCap) continue;   // kd_prod_cols_long's row
-        int m = 1;
-        while (m < bound) m <<= 1;
-        int64_t base = 0;
+        int size = 32;
+        while (size < 2 * bound && size < kColCap) size <<= 1;
+        for (int t = lane; t < size; t += 32) a[t] = kEmpty;
+        __syncwarp();
         for (int64_t s = f.aptr[i]; s < f.aptr[i + 1]; ++s) {
             const int32_t c = f.acol[s];
             const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
-            for (int64_t t = lane; t < len; t += 32) a[base + t] = f.bcol[t0 + t];
-            base += len;
+            for (int64_t t = lane; t < len; t += 32) table_insert(a, size, f.bcol[t0 + t]);
         }
-        for (int64_t t = bound + lane; t < m; t += 32) a[t] = 0x7fffffff;
+        __syncwarp();
+        // compact the occupied slots to the front (each chunk read before it is written)
+        int run = 0;
+        for (int t0 = 0; t0 < size; t0 += 32) {
+            const int32_t v = a[t0 + lane];
+            const bool keep = v != kEmpty;
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            __syncwarp();
+            if (keep) a[run + __popc(mask & ((1u << lane) - 1u))] = v;
+            run += __popc(mask);
+            __syncwarp();
+        }
+        int m = 1;
+        while (m < run) m <<= 1;
+        for (int t = run + lane; t < m; t += 32) a[t] = 0x7fffffff;
         __syncwarp();
         warp_bitonic(a, m);
-        int64_t run = 0;
-        for (int64_t t0 = 0; t0 < bound; t0 += 32) {
-            const int64_t t = t0 + lane;
-            const bool keep = t < bound && (t == 0 || a[t] != a[t - 1]);
-            const unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (keep) out[run + __popc(mask & ((1u << lane) - 1u))] = a[t];
-            run += __popc(mask);
-        }
+        for (int t = lane; t < run; t += 32) out[t] = a[t];
         if (lane == 0) f.cnt[i] = run;
         __syncwarp();
     }

@@ -100,13 +100,58 @@ FE_HD int64_t find_sorted(const int32_t *a, int64_t lo, int64_t hi, int32_t v) {
 
 // ------------------------------------------------------------------ block inverses
 
-// Pseudo-inverse of a symmetric D x D block by cyclic Jacobi: V diag(1/l) V^T over the
-// eigenvalues above 1e-12 of the largest in magnitude.  The sweeps stop once the
+// Inverse of a symmetric D x D block: by Cholesky when it is positive definite (every
+// pivot above 1e-12 of the largest diagonal entry), else the pseudo-inverse by cyclic
+// Jacobi, V diag(1/l) V^T over the eigenvalues above 1e-12 of the largest in magnitude.  The sweeps stop once the
 // off-diagonal part is below 1e-30 of the block's squared Frobenius norm (rounding
 // level; Jacobi converges quadratically, a few sweeps), or after 60.  D is a template
 // argument so that the block and its eigenvectors stay in registers.
 template <int D>
 FE_HD void sym_pinv_n(const double *a, double *out) {
+    // positive definite blocks (nearly all of them): the inverse by Cholesky, when every
+    // pivot is above 1e-12 of the largest diagonal entry; the Jacobi pseudo-inverse below
+    // otherwise (blocks of dropped near-null-space columns are singular)
+    {
+        double dmax = 0.0;
+        for (int i = 0; i < D; ++i) dmax = fabs(a[i * D + i]) > dmax ? fabs(a[i * D + i]) : dmax;
+        double L[D * D];
+        bool ok = dmax > 0.0;
+        for (int j = 0; j < D && ok; ++j) {
+            double s = a[j * D + j];
+            for (int k = 0; k < j; ++k) s -= L[j * D + k] * L[j * D + k];
+            if (!(s > 1e-12 * dmax)) {
+                ok = false;
+                break;
+            }
+            const double l = sqrt(s);
+            L[j * D + j] = l;
+            for (int i = j + 1; i < D; ++i) {
+                double t = a[i * D + j];
+                for (int k = 0; k < j; ++k) t -= L[i * D + k] * L[j * D + k];
+                L[i * D + j] = t / l;
+            }
+        }
+        if (ok) {
+            // W = L^-1 (lower), then out = W^T W
+            double W[D * D];
+            for (int i = 0; i < D * D; ++i) W[i] = 0.0;
+            for (int c = 0; c < D; ++c) {
+                W[c * D + c] = 1.0 / L[c * D + c];
+                for (int i = c + 1; i < D; ++i) {
+                    double t = 0.0;
+                    for (int k = c; k < i; ++k) t += L[i * D + k] * W[k * D + c];
+                    W[i * D + c] = -t / L[i * D + i];
+                }
+            }
+            for (int i = 0; i < D; ++i)
+                for (int j = 0; j < D; ++j) {
+                    double t = 0.0;
+                    for (int k = (i > j ? i : j); k < D; ++k) t += W[k * D + i] * W[k * D + j];
+                    out[i * D + j] = t;
+                }
+            return;
+        }
+    }
     double A[D * D], V[D * D];
     double fro = 0.0;
     for (int i = 0; i < D * D; ++i) A[i] = a[i], fro += a[i] * a[i];
