@@ -442,13 +442,14 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
     // the hierarchy, set up on the device, and the cycle's vectors
     const bool prof = h->w.prof && h->w.pev[0];
     DevAmg G;
-    // down to at most 3000 DOFs (an eighth of small systems): below that the aggregates
-    // of the plane-strain family stop shrinking while the coarse operators fill in (4M
-    // DOF: 647 -> 365 -> 321 -> 217 nodes with rows of 100-200 blocks; the Galerkin
-    // product of the 647-node level alone took 140 ms, against 40 ms for the dense
-    // inverse of the 1941-DOF level)
+    // down to at most 1500 DOFs (an eighth of small systems).  Below ~650 nodes the
+    // aggregates of the plane-strain family stop shrinking while the coarse operators
+    // fill in (4M DOF: 647 -> 365 -> 321 -> 217 nodes, rows of 100-200 blocks), so a
+    // smaller coarsest level costs a level of long products: at 4M DOF the 1095-DOF
+    // coarsest level (6 ms for its inverse, about 4 ms more of products) and the
+    // 1941-DOF one (16 ms) measured the same solve time
     SetupTrace trace;
-    FE_CHECK(amg_setup_device(h, 0.08, std::min<int64_t>(3000, std::max<int64_t>(100, nd / 8)), G,
+    FE_CHECK(amg_setup_device(h, 0.08, std::min<int64_t>(1500, std::max<int64_t>(100, nd / 8)), G,
                               prof ? &trace : nullptr));
     if (prof) trace.mark(s, amg::kPhaseCycle);
     for (size_t l = 0; l < G.L.size(); ++l) FE_CHECK(prepare_cycle(h, G.mem, G.L[l], l > 0));

@@ -404,38 +404,61 @@ constexpr size_t kLongColsSmem = kLongTerms * sizeof(int32_t);
 constexpr size_t kLongValsSmem = 2 * kLongTerms * sizeof(int16_t) + 2 * kLongOut * sizeof(int32_t) +
                                  (kLongA + 1) * sizeof(int32_t);
 
+// Rows past the short kernel's capacity: the candidates are streamed from global memory
+// into a table of kLongTerms slots in dynamic shared memory (one warp per block), which
+// only has to hold the distinct columns -- a few hundred on the coarse levels, however
+// many candidates; a row with more distinct columns than slots (an insert that finds
+// no slot) takes the row operation of one lane.
+__device__ __forceinline__ bool table_insert_checked(int32_t *tab, int size, int32_t c) {
+    uint32_t h = ((uint32_t)c * 2654435761u) & (uint32_t)(size - 1);
+    for (int probe = 0; probe < size; ++probe) {
+        const int32_t old = atomicCAS(&tab[h], kEmpty, c);
+        if (old == kEmpty || old == c) return true;
+        h = (h + 1) & (uint32_t)(size - 1);
+    }
+    return false;
+}
+
 __global__ void __launch_bounds__(32) kd_prod_cols_long(int64_t n, amg::PassProdCols f) {
     extern __shared__ int32_t a[];
     const int lane = threadIdx.x & 31;
+    constexpr int size = kLongTerms;
     for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const int64_t bound = f.boff[i + 1] - f.boff[i];
         if (bound <= kColCap) continue;   // the short kernel's row
         int32_t *out = f.cand + f.boff[i];
-        if (bound > kLongTerms) {
+        for (int t = lane; t < size; t += 32) a[t] = kEmpty;
+        __syncwarp();
+        bool ok = true;
+        for (int64_t s = f.aptr[i]; s < f.aptr[i + 1] && ok; ++s) {
+            const int32_t c = f.acol[s];
+            const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
+            bool mine = true;
+            for (int64_t t = lane; t < len; t += 32) mine = table_insert_checked(a, size, f.bcol[t0 + t]) && mine;
+            ok = __all_sync(0xffffffffu, mine);
+        }
+        __syncwarp();
+        if (!ok) {
             if (lane == 0) f.cnt[i] = amg::row_product_columns(f.aptr, f.acol, f.bptr, f.bcol, i, out);
             __syncwarp();
             continue;
         }
-        int m = 1;
-        while (m < bound) m <<= 1;
-        int64_t base = 0;
-        for (int64_t s = f.aptr[i]; s < f.aptr[i + 1]; ++s) {
-            const int32_t c = f.acol[s];
-            const int64_t t0 = f.bptr[c], len = f.bptr[c + 1] - t0;
-            for (int64_t t = lane; t < len; t += 32) a[base + t] = f.bcol[t0 + t];
-            base += len;
+        int run = 0;
+        for (int t0 = 0; t0 < size; t0 += 32) {
+            const int32_t v = a[t0 + lane];
+            const bool keep = v != kEmpty;
+            const unsigned mask = __ballot_sync(0xffffffffu, keep);
+            __syncwarp();
+            if (keep) a[run + __popc(mask & ((1u << lane) - 1u))] = v;
+            run += __popc(mask);
+            __syncwarp();
         }
-        for (int64_t t = bound + lane; t < m; t += 32) a[t] = 0x7fffffff;
+        int m = 1;
+        while (m < run) m <<= 1;
+        for (int t = run + lane; t < m; t += 32) a[t] = 0x7fffffff;
         __syncwarp();
         warp_bitonic(a, m);
-        int64_t run = 0;
-        for (int64_t t0 = 0; t0 < bound; t0 += 32) {
-            const int64_t t = t0 + lane;
-            const bool keep = t < bound && (t == 0 || a[t] != a[t - 1]);
-            const unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (keep) out[run + __popc(mask & ((1u << lane) - 1u))] = a[t];
-            run += __popc(mask);
-        }
+        for (int t = lane; t < run; t += 32) out[t] = a[t];
         if (lane == 0) f.cnt[i] = run;
         __syncwarp();
     }
@@ -455,9 +478,22 @@ __global__ void __launch_bounds__(32) kd_prod_vals_long(int64_t n, amg::PassProd
         if (T <= kTermCap && lc <= kTermCap) continue;   // the short kernel's row
         const int64_t a0 = f.aptr[i], la = f.aptr[i + 1] - a0;
         if (T > kLongTerms || lc > kLongOut || la > kLongA) {
-            if (lane == 0)
-                amg::row_product_values(f.aptr, f.acol, f.aval, f.ra, f.ca, f.bptr, f.bcol, f.bval, f.cb, f.cptr,
-                                        f.ccol, f.cval, i, f.upper != 0);
+            // beyond the shared-memory buffers: each lane takes output entries and, for
+            // each, finds its column in the B row of every entry of A's row (a binary
+            // search), summing in A's order -- the order of the term-by-term sum
+            for (int64_t p = lane; p < lc; p += 32) {
+                const int32_t c = f.ccol[c0 + p];
+                if (f.upper && c < i) continue;   // filled by the mirror pass
+                double acc[RA && CB ? RA * CB : 36];
+                for (int k = 0; k < bs; ++k) acc[k] = 0.0;
+                for (int64_t q = 0; q < la; ++q) {
+                    const int64_t j = f.acol[a0 + q];
+                    const int64_t t = amg::find_sorted(f.bcol, f.bptr[j], f.bptr[j + 1], c);
+                    if (t >= 0) amg::block_mul_add(f.aval + (a0 + q) * ra * ca, f.bval + t * ca * cb, ra, ca, cb, acc);
+                }
+                double *o = f.cval + (c0 + p) * bs;
+                for (int k = 0; k < bs; ++k) o[k] = acc[k];
+            }
             __syncwarp();
             continue;
         }
