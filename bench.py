@@ -504,7 +504,8 @@ def run_ours(args, dist):
         "solver": {
             "mode": ("mixed precision: FP64 CG recurrence on the FP64 copy of the eliminated system, "
                      "preconditioned by one FP32 smoothed-aggregation V-cycle per iteration (hierarchy set up on "
-                     "the device every step, Chebyshev(3) smoothing on node-block Jacobi, dense coarsest solve)"
+                     "the device every step, Chebyshev smoothing on node-block Jacobi (3 steps on level 0, 2 below), "
+                     "dense coarsest solve)"
                      if args.solver == "multigrid" else
                      "mixed precision: FP64 CG recurrence on the FP64 SELL copy, node-block Jacobi + Chebyshev "
                      "preconditioner in FP32 on the prescaled FP32 copy")

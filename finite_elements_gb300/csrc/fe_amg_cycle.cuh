@@ -41,9 +41,12 @@ struct CycleCoarse {
     float *r = nullptr, *x = nullptr;
 };
 
+// zero: z_in is zero (the first step from zero), so A z_in = 0; an executor may skip the
+// product (the row operation computes it, exactly 0)
 struct PassCheb {
     const int64_t *ptr; const int32_t *col; const float *val; const float *dinv; int d; const float *r;
     const float *zin; float *dir; float *zout; float a; float b; int first;
+    int zero = 0;
     FE_HD void operator()(int64_t i) const { row_chebyshev(ptr, col, val, dinv, d, r, zin, dir, zout, a, b, first != 0, i); }
 };
 
@@ -92,8 +95,9 @@ int chebyshev_cycle(Ex &ex, const CycleLevel &L, int k, bool from_x0) {
     if (!from_x0) FE_CHECK(ex.fill_zero(L.x, (size_t)nd));
     float *cur = L.x, *nxt = L.zn;
     double rho = 1.0 / sigma;
-    FE_CHECK(ex.rows(L.n, PassCheb{L.aptr, L.acol, L.a, L.dinv, L.d, L.r, cur, L.dir, nxt, 0.0f,
-                                   (float)(1.0 / theta), 1}));
+    PassCheb first{L.aptr, L.acol, L.a, L.dinv, L.d, L.r, cur, L.dir, nxt, 0.0f, (float)(1.0 / theta), 1};
+    first.zero = from_x0 ? 0 : 1;
+    FE_CHECK(ex.rows(L.n, first));
     std::swap(cur, nxt);
     for (int st = 1; st < k; ++st) {
         const double rn = 1.0 / (2.0 * sigma - rho);

@@ -22,6 +22,8 @@ static_assert(amg::kSetupPhases <= 16, "SolverWork::mg_phase_ms");
 namespace {
 
 constexpr int kAT = 256;
+// Chebyshev smoothing steps per smoothing: on level 0 and on the coarser levels
+constexpr int kSmooth0 = 3, kSmoothCoarse = 2;
 inline int grid_a(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + kAT - 1) / kAT, 152 * 8)); }
 
 // the executor of the shared FP32 cycle (fe_amg_cycle.cuh): one grid-stride kernel per pass
@@ -108,7 +110,8 @@ __global__ void __launch_bounds__(kAT) ka_cheb(int64_t n, amg::PassCheb f) {
     FE_LANE_ROWS(G, n) {
         const bool valid = i < n;
         float az[D];
-        lanes_product<D, D, G>(f.ptr, f.col, f.val, f.zin, i, valid, sub, az);
+        // the first step from zero: A z_in = 0 without reading the matrix
+        lanes_product<D, D, G>(f.ptr, f.col, f.val, f.zin, i, valid && !f.zero, sub, az);
         if (valid && sub == 0) {
             float t[D];
 #pragma unroll
@@ -397,7 +400,7 @@ int level0_chebyshev(fe_handle_s *h, const amg::CycleLevel &L, const double *r64
 // z = M^-1 r: the shared FP32 V-cycle below level 0, level 0 on the SELL copy (its
 // right-hand side D^-1 r in L0.r, iterates in L0.x / L0.zn)
 int precondition_sell(CycleEx &ex, const std::vector<amg::CycleLevel> &levels, const amg::CycleCoarse &C, int k,
-                      const double *r, double *z) {
+                      int kc, const double *r, double *z) {
     fe_handle_s *h = ex.h;
     const amg::CycleLevel &L = levels[0];
     float *rc = levels.size() > 1 ? levels[1].r : C.r;
@@ -407,7 +410,7 @@ int precondition_sell(CycleEx &ex, const std::vector<amg::CycleLevel> &levels, c
     FE_CHECK(level0_chebyshev(h, L, r, k, true, &cur, &other, ex));
     FE_CHECK(mg_level0_residual(h, L.r, cur, L.t));
     FE_CHECK(ex.rows(L.nc, amg::PassRestrict32{L.tptr, L.tcol, L.pt, L.m, L.d, L.t, rc}));
-    FE_CHECK(amg::vcycle(ex, levels, C, 1, k));
+    FE_CHECK(amg::vcycle(ex, levels, C, 1, kc));
     FE_CHECK(ex.rows(L.n, amg::PassProlong32{L.pptr, L.pcol, L.p, L.d, L.m, xc, cur}));
     FE_CHECK(level0_chebyshev(h, L, r, k, false, &cur, &other, ex));
     FE_CHECK(ex.rows(L.n * L.d, amg::PassToF64{cur, z}));
@@ -508,7 +511,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         cudaGraph_t g = nullptr;
         FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         const int rc = G.L.empty() ? precondition_dense(cex, coarse, r.p, z.p)
-                                   : precondition_sell(cex, views, coarse, 3, r.p, z.p);
+                                   : precondition_sell(cex, views, coarse, kSmooth0, kSmoothCoarse, r.p, z.p);
         cudaError_t ce = cudaStreamEndCapture(s, &g);
         if (rc != FE_OK) {
             if (ce == cudaSuccess && g) cudaGraphDestroy(g);
@@ -538,7 +541,7 @@ int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) 
         FE_CUDA(cudaEventElapsedTime(&a, h->events[6], h->events[7]));
         h->w.mg_ms[1] += a, h->w.mg_n[1] += 1;
     }
-    const int64_t smooth_launches = 2;   // SELL Chebyshev steps of level 0's pre-smoothing
+    const int64_t smooth_launches = kSmooth0 - 1;   // SELL Chebyshev steps of level 0's pre-smoothing
     auto precond = [&]() -> int {
         FE_CUDA(cudaGraphLaunch(cycle, s));
         h->launches += per_cycle;

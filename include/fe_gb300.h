@@ -67,8 +67,9 @@ extern "C" {
 #define FE_SOLVE_MULTIGRID        8    /* PCG with an FP64 recurrence preconditioned by one
                                           FP32 smoothed-aggregation V-cycle per iteration
                                           (hierarchy set up on the device at every solve;
-                                          Chebyshev(3) smoothing on node-block Jacobi, a
-                                          dense coarsest solve); precision and Chebyshev
+                                          Chebyshev smoothing on node-block Jacobi, 3 steps
+                                          on the finest level and 2 below, a dense
+                                          coarsest solve); precision and Chebyshev
                                           options are not used, x0 and
                                           FE_SOLVE_X0_IF_BETTER are                        */
 
