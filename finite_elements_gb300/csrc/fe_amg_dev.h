@@ -14,9 +14,10 @@ namespace fe {
 using DevCsr = amg::Csr;
 
 // The multigrid solve's device buffers: stream-ordered allocations on the handle's
-// stream from the handle's memory pool, which keeps the memory between solves, so a
-// setup's hundred-odd allocations and frees map no pages and never synchronise the
-// device.  palloc grows a buffer like dalloc; pfree returns it on the stream.
+// stream from the device's memory pool, which keeps the memory between solves and
+// handles, so a setup's hundred-odd allocations and frees map no pages and never
+// synchronise the device.  palloc grows a buffer like dalloc; pfree returns it on the
+// stream.
 struct MgMem {
     cudaStream_t s = nullptr;
     cudaMemPool_t pool = nullptr;
@@ -24,7 +25,8 @@ struct MgMem {
                                 // pageable memory would be staged and wait longer)
 };
 
-// the handle's pool (created on first use, release threshold unbounded)
+// the handle's stream and the device's pool (one per device for the process, created on
+// first use, release threshold unbounded; fe_trim_memory_pools gives memory back)
 int mg_memory(fe_handle_s *h, MgMem *out);
 
 template <typename T>

@@ -5,6 +5,7 @@
 // inverse of the coarsest matrix (at most 4096 DOFs) by Gauss-Jordan elimination on the
 // device.
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <functional>
 #include <vector>
@@ -970,10 +971,22 @@ int coarse_inverse_device(const DevCsr &C, DevAmg &G) {
 
 }  // namespace
 
-int mg_memory(fe_handle_s *h, MgMem *out) {
-    if (!h->mg_pool) {
-        int dev = 0;
-        FE_CUDA(cudaGetDevice(&dev));
+// One pool per device for the whole process, shared by the handles (a user who makes a
+// handle per problem reuses the memory of the previous ones); fe_trim_memory_pools
+// gives it back.
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+
+int device_pool(cudaMemPool_t *out) {
+    int dev = 0;
+    FE_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("multigrid: device index out of range");
+        return FE_BAD_INPUT;
+    }
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pools[dev]) {
         cudaMemPoolProps props = {};
         props.allocType = cudaMemAllocationTypePinned;
         props.location.type = cudaMemLocationTypeDevice;
@@ -986,8 +999,14 @@ int mg_memory(fe_handle_s *h, MgMem *out) {
             set_error("multigrid: cannot set the memory pool's release threshold");
             return FE_CUDA_ERR;
         }
-        h->mg_pool = pool;
+        g_pools[dev] = pool;
     }
+    *out = g_pools[dev];
+    return FE_OK;
+}
+
+int mg_memory(fe_handle_s *h, MgMem *out) {
+    if (!h->mg_pool) FE_CHECK(device_pool(&h->mg_pool));
     if (!h->mg_pinned) FE_CUDA(cudaMallocHost((void **)&h->mg_pinned, 8 * sizeof(double)));
     out->s = h->stream;
     out->pool = h->mg_pool;
@@ -1060,6 +1079,16 @@ int amg_download(const DevAmg &G, fe_amg_s *out, cudaStream_t s) {
 }  // namespace fe
 
 using namespace fe;
+
+extern "C" int fe_trim_memory_pools(uint64_t keep_bytes) {
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    for (cudaMemPool_t p : g_pools)
+        if (p && cudaMemPoolTrimTo(p, (size_t)keep_bytes) != cudaSuccess) {
+            set_error("fe_trim_memory_pools: cudaMemPoolTrimTo failed");
+            return FE_CUDA_ERR;
+        }
+    return FE_OK;
+}
 
 extern "C" int fe_amg_build_device(fe_handle h, double theta, int64_t coarse_dofs, fe_amg *out) {
     if (!h || !out) {

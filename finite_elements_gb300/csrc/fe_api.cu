@@ -148,7 +148,6 @@ int fe_destroy(fe_handle h) {
     for (auto &e : h->events)
         if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
-    if (h->mg_pool) cudaMemPoolDestroy(h->mg_pool);
     if (h->mg_pinned) cudaFreeHost(h->mg_pinned);
     delete h;
     return FE_OK;

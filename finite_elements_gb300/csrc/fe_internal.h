@@ -223,8 +223,8 @@ struct fe_handle_s {
     // values
     bool k_ready = false, m_ready = false, f_ready = false, sys_ready = false;
     uint64_t sys_generation = 0;   // counts the system matrices built (build_system)
-    // memory pool of the multigrid solve's stream-ordered allocations (kept between
-    // solves; created on first use)
+    // memory pool of the multigrid solve's stream-ordered allocations: the device's pool,
+    // shared by the process's handles and kept between solves
     cudaMemPool_t mg_pool = nullptr;
     double *mg_pinned = nullptr;   // 8 pinned doubles: the multigrid's scalar reads to the host
     bool singular = false;                // a diagonal block could not be inverted

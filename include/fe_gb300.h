@@ -259,6 +259,11 @@ int fe_profile_read_multigrid(fe_handle h, double *smooth_ms, int64_t *smooth_n,
  * included). */
 #define FE_MG_PHASES 10
 int fe_profile_read_multigrid_phases(fe_handle h, double *ms, int32_t n);
+/* The multigrid solve allocates from one stream-ordered memory pool per device, shared
+ * by the process's handles, which keeps its memory between solves and handles (no page
+ * mapping and no device-wide synchronisation per allocation).  This gives the pools'
+ * unused memory back to the device down to keep_bytes each (cudaMemPoolTrimTo). */
+int fe_trim_memory_pools(uint64_t keep_bytes);
 
 /* ---- modal analysis (analysis.py:741-796 modal_analysis: scipy eigsh/eigs on
  * k_matrix_sparse and m_matrix_sparse, i.e. K and M without Dirichlet conditions).

@@ -120,3 +120,21 @@ def test_device_coarsest_inverse_is_the_inverse(gpu_lib, name):
         if h.value:
             lib.fe_amg_destroy(h)
         s.close()
+
+
+def test_memory_pool_is_shared_and_trimmed(gpu_lib):
+    """Two handles solve through the device's shared multigrid pool, which
+    fe_trim_memory_pools empties between them; the solutions are bitwise equal."""
+    from finite_elements_gb300 import _lib
+    from finite_elements_gb300.engine import GpuSystem
+    prob = _problems()["plane_strain"]()
+    kw = dict(precision="mixed-cg64", tol=1e-10, multigrid=True, accept_stagnation=True)
+    s1 = GpuSystem(prob)
+    x1, st1 = s1.solve(**kw)
+    s1.close()
+    _lib.check(_lib.load().fe_trim_memory_pools(0), "fe_trim_memory_pools")
+    s2 = GpuSystem(prob)
+    x2, st2 = s2.solve(**kw)
+    s2.close()
+    assert st1.status == 0 and st2.status == 0
+    np.testing.assert_array_equal(x1, x2)
