@@ -65,16 +65,19 @@ __global__ void ks_tile_sums(const int64_t *__restrict__ in, int64_t n, int64_t 
     if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
-// serial exclusive scan of the tile sums (a few thousand at most); out[n] = total
-__global__ void ks_scan_tiles(int64_t nt, int64_t *part, int64_t *out, int64_t n) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int64_t run = 0;
-    for (int64_t t = 0; t < nt; ++t) {
-        const int64_t v = part[t];
-        part[t] = run;
-        run += v;
+// exclusive scan of the tile sums by one block, kST at a time with a carry; out[n] = total
+__global__ void __launch_bounds__(kST) ks_scan_tiles(int64_t nt, int64_t *part, int64_t *out, int64_t n) {
+    __shared__ int64_t chunk_total;
+    int64_t carry = 0;
+    for (int64_t c0 = 0; c0 < nt; c0 += blockDim.x) {
+        const int64_t t = c0 + threadIdx.x;
+        const int64_t v = t < nt ? part[t] : 0;
+        const int64_t ex = block_excl_scan(v, &chunk_total);
+        if (t < nt) part[t] = carry + ex;
+        carry += chunk_total;
+        __syncthreads();   // every thread has read chunk_total before the next chunk writes it
     }
-    out[n] = run;
+    if (threadIdx.x == 0) out[n] = carry;
 }
 
 __global__ void ks_tile_scan(const int64_t *__restrict__ in, int64_t n, const int64_t *__restrict__ part,
@@ -98,7 +101,7 @@ int scan64(const int64_t *in, int64_t n, int64_t *out, int64_t *total, DBuf<int6
     const int64_t nt = std::max<int64_t>(1, (n + kScanTile - 1) / kScanTile);
     FE_CHECK(palloc(mem, tmp, (size_t)nt));
     ks_tile_sums<<<(unsigned)nt, kST, 0, s>>>(in, n, tmp.p);
-    ks_scan_tiles<<<1, 1, 0, s>>>(nt, tmp.p, out, n);
+    ks_scan_tiles<<<1, kST, 0, s>>>(nt, tmp.p, out, n);
     ks_tile_scan<<<(unsigned)nt, kST, 0, s>>>(in, n, tmp.p, out);
     FE_LAUNCH_CHECK();
     int64_t *pin = reinterpret_cast<int64_t *>(mem.pinned);

@@ -340,7 +340,7 @@ int product(Ex &ex, const Csr &A, const Csr &B, Csr &C, Work<Ex> &W, bool symmet
 // alpha_{j-1}, off-diagonal sqrt(beta_j) / alpha_j; Saad, Iterative Methods for Sparse
 // Linear Systems, 6.7.3), whose largest eigenvalue lanczos_lmax finds.  Its Ritz value
 // approaches lmax from below far faster than power iteration does.
-constexpr int kLanczosSteps = 15;
+constexpr int kLanczosSteps = 10;
 
 // The Lanczos estimate's scalars, in executor memory so that the CG steps run without
 // a read to the host: rz, rz0, p.q, r.z of the new residual, a stop flag, the steps done,

@@ -12,7 +12,7 @@
 //                 non-negative diag(R), dropped columns kept as zeros); R is the
 //                 coarse near-null space
 //   P             (I - 4/(3 lmax) D^-1 A) P_tent, D^-1 the block-diagonal
-//                 pseudo-inverse, lmax of D^-1 A from 15 CG-Lanczos steps from
+//                 pseudo-inverse, lmax of D^-1 A from 10 CG-Lanczos steps from
 //                 b_i = 1 + (i mod 7) / 7
 //   A_c           P^T A P, m x m blocks
 // down to at most `coarse_dofs` DOFs (or 12 levels).  Host code only: no device call.

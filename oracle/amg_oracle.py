@@ -16,7 +16,7 @@ Computing 56, 1996):
   rigid-body modes: two translations and the rotation (-y, x) in 2D) restricted to
   its DOFs; the R factors are the coarse near-null space;
 * smoothed prolongator P = (I - 4/(3 lmax) D^-1 A) P_tent, D the block diagonal, lmax
-  the largest eigenvalue of D^-1 A from 15 Lanczos steps (lmax_lanczos);
+  the largest eigenvalue of D^-1 A from 10 Lanczos steps (lmax_lanczos);
 * Galerkin coarse operators P^T A P down to a few hundred DOFs, solved directly;
 * V-cycle with Chebyshev(k) pre- and post-smoothing on D^-1 A, interval
   [lmax/30, 1.05 lmax].
@@ -56,7 +56,7 @@ def lmax_power(A, Minv, it=30):
     return float(x @ (Minv @ (A @ x)) / (x @ x))
 
 
-def lmax_lanczos(A, Minv, steps=15):
+def lmax_lanczos(A, Minv, steps=10):
     """Largest eigenvalue of Minv A from the Lanczos matrix of `steps` iterations of CG
     on A x = b preconditioned by Minv, b = power_start (the coefficients alpha_j, beta_j
     give T with diagonal 1/alpha_j + beta_{j-1}/alpha_{j-1} and off-diagonal
