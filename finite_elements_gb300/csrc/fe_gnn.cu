@@ -241,7 +241,7 @@ k_gemm(int64_t N, const float *__restrict__ X1, const float *__restrict__ X2, co
                 tc_mma(tmem, adesc + (uint64_t)kk, bdesc + (uint64_t)kk, idesc, kk > 0);
             tc_commit(&mbar);
         }
-        ok = __syncthreads_and(mbar_wait(&mbar, phase));   // the same verdict in every thread
+        ok = __syncthreads_and(mbar_wait(&mbar, phase));   // the same outcome in every thread
         phase ^= 1;
         tc_fence_after();
         if (ok) {
