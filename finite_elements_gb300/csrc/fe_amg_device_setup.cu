@@ -2,8 +2,7 @@
 // (fe_amg_passes.cuh, the passes fe_amg_build_parallel_host runs on the host) on the
 // device executor -- every pass one grid-stride kernel over its rows, int64 prefix
 // sums on the device between the passes that size the next ones -- and the dense
-// inverse of the coarsest matrix (at most 4096 DOFs) by Gauss-Jordan elimination on the
-// device.
+// inverse of the coarsest matrix (at most 4096 DOFs) by block sweeps on the device.
 #include <algorithm>
 #include <mutex>
 #include <cmath>
@@ -146,8 +145,9 @@ __global__ void kd_dot_final(int nb, const double *__restrict__ part, double *ou
     if (threadIdx.x == 0) *out = s;
 }
 
-// y = D^-1 A x (FP64) with G lanes of a warp per block row (a strided share of its
-// blocks each, then a shuffle sum): the power iterations of the lmax estimates
+// y = D^-1 A x, or y = A x when dinv is null (FP64), with G lanes of a warp per block
+// row (a strided share of its blocks each, then a shuffle sum): the products of the
+// lmax estimates
 template <int D, int G>
 __global__ void __launch_bounds__(kST) kd_dinv_product(int64_t n, amg::PassDinvProduct f) {
     const int sub = threadIdx.x & (G - 1);
@@ -627,7 +627,8 @@ struct DevEx {
         FE_LAUNCH_CHECK();
         return FE_OK;
     }
-    // the power iterations' product with lanes per row; other block sizes row by row
+    // the lmax estimates' products: level 0's on the FP64 SELL copy, the others with
+    // lanes per row (other block sizes row by row)
     int rows(int64_t n, const amg::PassDinvProduct &f) {
         if (n <= 0) return FE_OK;
         if (!f.dinv && h && f.ptr == sell_ptr) return spmv64(h, f.x, f.y);

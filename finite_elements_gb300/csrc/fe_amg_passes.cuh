@@ -35,7 +35,7 @@ namespace amg {
 // operator and its near-null space.
 enum SetupPhase : int {
     kPhaseInput = 0,
-    kPhaseDiag,          // D^-1 and the power iterations for lmax
+    kPhaseDiag,          // D^-1 and the Lanczos estimate of lmax
     kPhaseAggregate,     // strength, the distance-2 independent set, the joins
     kPhaseTentative,     // member lists and the QR of every aggregate
     kPhaseProlongator,   // A P_t and the damped-Jacobi smoothing

@@ -43,7 +43,7 @@ def block_diag_inv(A, d):
 
 
 def power_start(n):
-    """Deterministic start vector of the power iterations: 1 + (i mod 7) / 7."""
+    """Deterministic start vector of the eigenvalue estimates: 1 + (i mod 7) / 7."""
     return 1.0 + (np.arange(n) % 7) / 7.0
 
 
