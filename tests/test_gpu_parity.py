@@ -209,3 +209,27 @@ def test_drop_in_analysis(gpu_lib, name):
     x = np.array(res.result_vector)
     assert np.linalg.norm(x - ref["x"]) <= SOL_TOL * np.linalg.norm(ref["x"])
     assert res.dimension == prob.dim
+
+
+def test_pinned_inputs_give_the_same_solution(gpu_lib):
+    """Inputs page-locked with fe_host_register upload to the same system: the solve is
+    bitwise the one from pageable arrays; unregistering releases them."""
+    from finite_elements_gb300 import _lib, meshgen
+    from finite_elements_gb300.engine import GpuSystem
+    prob = meshgen.plane_strain_random(60, 30, seed=7)
+    kw = dict(precision="fp64", tol=1e-12, accept_stagnation=True)
+    s0 = GpuSystem(prob)
+    x0, _ = s0.solve(**kw)
+    s0.close()
+    lib = _lib.load()
+    arrays = [prob.coords, prob.conn, prob.E, prob.nu, prob.thickness, prob.rho]
+    for a in arrays:
+        _lib.check(lib.fe_host_register(a.ctypes.data, a.nbytes), "fe_host_register")
+    try:
+        s1 = GpuSystem(prob)
+        x1, _ = s1.solve(**kw)
+        s1.close()
+    finally:
+        for a in arrays:
+            _lib.check(lib.fe_host_unregister(a.ctypes.data), "fe_host_unregister")
+    np.testing.assert_array_equal(x0, x1)
