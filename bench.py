@@ -262,7 +262,9 @@ def run_ours(args, dist):
     def device_step(opts, learned=False):
         h.call("fe_assemble", step_flags)
         if learned and net is not None:
-            ptr, _ = net.predict(s)               # the warm start is part of the step
+            # the warm start is part of the step: predicted on the network's stream while
+            # the solve sets up its hierarchy, the solve waiting for it before it reads x0
+            ptr = net.predict_async(s)
             _, st = s.solve(x0_device_ptr=ptr, x0_if_better=True, **opts)
         else:
             _, st = s.solve(**opts)
@@ -488,7 +490,7 @@ def run_ours(args, dist):
         t0 = time.perf_counter()
         se = GpuSystem(prob, assemble=True)
         if net is not None:
-            ptr, _ = net.predict(se)
+            ptr = net.predict_async(se)
             x, st = se.solve(x0_device_ptr=ptr, x0_if_better=True, **e2e_opts)
         else:
             x, st = se.solve(**e2e_opts)

@@ -110,6 +110,7 @@ _SIGNATURES = {
     "fe_gnn_get_params": ([_P, _P, _I64], C.c_int),
     "fe_gnn_features": ([_P, _P, _P], C.c_int),
     "fe_gnn_predict": ([_P, _P, _P, C.POINTER(_P), _PD], C.c_int),
+    "fe_gnn_predict_async": ([_P, _P, C.POINTER(_P)], C.c_int),
     "fe_gnn_target_energy": ([_P, _P, _PD], C.c_int),
     "fe_gnn_loss_grad": ([_P, _P, _D, _PD, _P], C.c_int),
     "fe_gnn_fit_grad": ([_P, _P, _PD, _P], C.c_int),

@@ -807,6 +807,22 @@ __global__ void k_warm_start(int64_t n_dof, const double *__restrict__ g, const 
         x0[i] = g[i] + s * u[i];
 }
 
+// the same with s = (u.b~) / (u.A u) from the device sums acc[0], acc[1] (0 when the
+// denominator is not positive), for predictions that do not wait for the host
+__global__ void k_warm_start_dev(int64_t n_dof, const double *__restrict__ g, const double *__restrict__ u,
+                                 const double *__restrict__ acc, double *__restrict__ x0) {
+    const double den = acc[1];
+    const double s = den > 0 ? acc[0] / den : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof; i += (int64_t)gridDim.x * blockDim.x)
+        x0[i] = g[i] + s * u[i];
+}
+
+// the bounding-box and moment accumulators' starting values
+__global__ void k_init_stats(float *stats) {
+    const float init[8] = {3.4e38f, -3.4e38f, 3.4e38f, -3.4e38f, 0.f, 0.f, 0.f, 0.f};
+    if (threadIdx.x < 8) stats[threadIdx.x] = init[threadIdx.x];
+}
+
 // e = b~ . (x - g)   (energy of the solution's free part: b~ = A v* with v* = x - g)
 __global__ void k_energy(int64_t n_dof, const double *__restrict__ bt, const double *__restrict__ x,
                          const double *__restrict__ g, double *__restrict__ acc) {
@@ -864,6 +880,10 @@ struct fe_gnn_s {
     fe::DBuf<float> us0, us1;     // decoded field and the smoothing ping-pong buffer
     fe::DBuf<double> gext, Ag, bt, u, Au, x0, acc, gsum;
     fe::DBuf<int> tc_err;         // set by a tensor-core GEMM whose MMAs did not complete
+    // asynchronous predictions run on the network's own stream, after `assembled` (the
+    // handle's stream at the call) and until `ready` (which the handle's next solve waits on)
+    cudaStream_t own = nullptr;
+    cudaEvent_t assembled = nullptr, ready = nullptr;
     double *acc_host = nullptr;
     int steps = 0;
     double last_scale = 0.0, last_num = 0.0, last_den = 0.0;
@@ -954,7 +974,7 @@ int refresh_bf16(fe_gnn_s *g) {
 }
 
 // Problem-dependent inputs: g_ext, b~, node features, inverse degrees.
-int prepare(fe_gnn_s *g, fe_handle_s *h) {
+int prepare(fe_gnn_s *g, fe_handle_s *h, cudaStream_t stream = nullptr) {
     if (h->kind != FE_KIND_ELASTIC_TRI) {
         set_error("the warm-start network is defined for elasticity meshes");
         return FE_BAD_INPUT;
@@ -964,17 +984,16 @@ int prepare(fe_gnn_s *g, fe_handle_s *h) {
         return FE_NOT_READY;
     }
     const int64_t n = h->n_nodes, nd = h->n_dof;
-    cudaStream_t s = h->stream;
+    cudaStream_t s = stream ? stream : h->stream;
     g->stream = s;
     FE_CHECK(gnn_alloc(g, n));
     FE_CUDA(cudaMemsetAsync(g->gext.p, 0, nd * sizeof(double), s));
     if (h->n_bc > 0) k_gext<<<g1(h->n_bc), kT, 0, s>>>(h->n_bc, h->bc_dof.p, h->bc_val.p, g->gext.p);
-    FE_CHECK(spmv64(h, g->gext.p, g->Ag.p));
+    FE_CHECK(spmv64_on(h, g->gext.p, g->Ag.p, s));
     k_btilde<<<g1(nd), kT, 0, s>>>(nd, h->b.p, g->Ag.p, h->bc_of_dof.p, g->bt.p);
     FE_CHECK(dalloc(g->stats, 8));
     FE_CHECK(dalloc(g->gsum, 8));
-    float init[8] = {3.4e38f, -3.4e38f, 3.4e38f, -3.4e38f, 0.f, 0.f, 0.f, 0.f};
-    FE_CUDA(cudaMemcpyAsync(g->stats.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    k_init_stats<<<1, 32, 0, s>>>(g->stats.p);
     FE_CUDA(cudaMemsetAsync(g->gsum.p, 0, 8 * sizeof(double), s));
     k_bbox<<<g1(n), kT, 0, s>>>(n, h->coords.p, g->stats.p);
     k_load_moments<<<g1(n), kT, 0, s>>>(n, h->coords.p, g->bt.p, g->stats.p, g->gsum.p);
@@ -982,9 +1001,7 @@ int prepare(fe_gnn_s *g, fe_handle_s *h) {
     k_features<<<g1(n), kT, 0, s>>>(n, h->n_elem, h->coords.p, h->bc_of_dof.p, g->stats.p, g->gsum.p, g->F.p);
     k_inv_deg<<<g1(n), kT, 0, s>>>(n, h->blk_ptr.p, h->blk_col.p, g->inv_deg.p);
     FE_LAUNCH_CHECK();
-    h->launches += 7 + (h->n_bc > 0 ? 1 : 0);
-    // the host copy in init must stay valid until the copy ran
-    FE_CUDA(cudaStreamSynchronize(s));
+    h->launches += 8 + (h->n_bc > 0 ? 1 : 0);
     return FE_OK;
 }
 
@@ -992,7 +1009,8 @@ inline float *Hl(fe_gnn_s *g, int l) { return g->H.p + (size_t)l * g->n_cap * HI
 inline float *Zl(fe_gnn_s *g, int l) { return g->Z.p + (size_t)l * g->n_cap * HID; }
 inline float *Ml(fe_gnn_s *g, int l) { return g->M.p + (size_t)l * g->n_cap * HID; }
 
-int forward(fe_gnn_s *g, fe_handle_s *h) {
+// async: leave the two sums u.b~, u.A u in acc on the device (no read to the host)
+int forward(fe_gnn_s *g, fe_handle_s *h, bool async = false) {
     const int64_t n = h->n_nodes;
     cudaStream_t s = g->stream;
     const float *P = g->params.p;
@@ -1020,12 +1038,13 @@ int forward(fe_gnn_s *g, fe_handle_s *h) {
     FE_LAUNCH_CHECK();
     h->launches += 4 + NLAYER * 4 + NSMOOTH;
     // A u_hat and the two dot products u.b~, u.A u
-    FE_CHECK(spmv64(h, g->u.p, g->Au.p));
+    FE_CHECK(spmv64_on(h, g->u.p, g->Au.p, s));
     FE_CHECK(dalloc(g->acc, 4));
     FE_CUDA(cudaMemsetAsync(g->acc.p, 0, 4 * sizeof(double), s));
     k_dots2<<<g1(h->n_dof), kT, 0, s>>>(h->n_dof, g->u.p, g->bt.p, g->Au.p, g->acc.p);
     FE_LAUNCH_CHECK();
     h->launches += 1;
+    if (async) return FE_OK;
     if (!g->acc_host) FE_CUDA(cudaMallocHost((void **)&g->acc_host, 4 * sizeof(double)));
     FE_CUDA(cudaMemcpyAsync(g->acc_host, g->acc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
@@ -1153,6 +1172,9 @@ int fe_gnn_create(fe_gnn *out) {
 int fe_gnn_destroy(fe_gnn g) {
     if (!g) return FE_OK;
     cudaDeviceSynchronize();
+    if (g->ready) cudaEventDestroy(g->ready);
+    if (g->assembled) cudaEventDestroy(g->assembled);
+    if (g->own) cudaStreamDestroy(g->own);
     dfree(g->params), dfree(g->grad), dfree(g->adam_m), dfree(g->adam_v), dfree(g->wt), dfree(g->tc_err);
     dfree(g->F), dfree(g->Z0), dfree(g->H), dfree(g->Z), dfree(g->M), dfree(g->dH), dfree(g->dHn), dfree(g->dX);
     dfree(g->dZ), dfree(g->dM), dfree(g->inv_deg), dfree(g->colsum), dfree(g->gterm), dfree(g->stats);
@@ -1222,6 +1244,32 @@ int fe_gnn_predict(fe_gnn g, fe_handle h, double *x0_host, const double **x0_dev
     g->stream = nullptr;
     if (x0_dev) *x0_dev = g->x0.p;
     if (scale) *scale = g->last_scale;
+    return FE_OK;
+}
+
+int fe_gnn_predict_async(fe_gnn g, fe_handle h, const double **x0_dev) {
+    if (!g || !h || !x0_dev) {
+        set_error("fe_gnn_predict_async: null argument");
+        return FE_BAD_INPUT;
+    }
+    if (!g->own) {
+        FE_CUDA(cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking));
+        FE_CUDA(cudaEventCreateWithFlags(&g->assembled, cudaEventDisableTiming));
+        FE_CUDA(cudaEventCreateWithFlags(&g->ready, cudaEventDisableTiming));
+    }
+    // after the handle's work so far (the assembly), on the network's stream
+    FE_CUDA(cudaEventRecord(g->assembled, h->stream));
+    FE_CUDA(cudaStreamWaitEvent(g->own, g->assembled, 0));
+    FE_CHECK(prepare(g, h, g->own));
+    FE_CHECK(refresh_bf16(g));
+    FE_CHECK(forward(g, h, true));
+    k_warm_start_dev<<<g1(h->n_dof), kT, 0, g->own>>>(h->n_dof, g->gext.p, g->u.p, g->acc.p, g->x0.p);
+    FE_LAUNCH_CHECK();
+    h->launches += 1;
+    FE_CUDA(cudaEventRecord(g->ready, g->own));
+    h->x0_ready = g->ready;
+    g->stream = nullptr;
+    *x0_dev = g->x0.p;
     return FE_OK;
 }
 

@@ -227,6 +227,9 @@ struct fe_handle_s {
     // shared by the process's handles and kept between solves
     cudaMemPool_t mg_pool = nullptr;
     double *mg_pinned = nullptr;   // 8 pinned doubles: the multigrid's scalar reads to the host
+    // recorded by an asynchronous warm-start prediction on another stream: the next solve
+    // waits for it on the handle's stream before it reads opts.x0 (start_point)
+    cudaEvent_t x0_ready = nullptr;
     bool singular = false;                // a diagonal block could not be inverted
     fe::DBuf<double> ke;                  // [n_elem][(3d)^2]
     fe::DBuf<double> me_scale;            // [n_elem] rho*A*t/12
@@ -306,6 +309,8 @@ int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms);
 int profile_kernels(fe_handle_s *h, int enable);
 void release_solver(fe_handle_s *h);
 int spmv64(fe_handle_s *h, const double *x, double *y);
+// the same, enqueued on another stream (the warm-start network's)
+int spmv64_on(fe_handle_s *h, const double *x, double *y, cudaStream_t stream);
 // Level 0 of the multigrid V-cycle on the handle's prescaled FP32 SELL copy
 // (fe_solver.cu), enqueued on the handle's stream: rh = D^-1 (float)r and
 // z1 = rh * inv_theta; one Chebyshev step z_out = z_in + c1 (z_in - z_out) +

@@ -944,6 +944,10 @@ int read_scalars(fe_handle_s *h);
 // that of the zero start, so a poor warm start costs two residuals and nothing more.
 template <int D, int G>
 int start_point(fe_handle_s *h, const fe_solve_opts *o, double *x, int *x0_used) {
+    if (h->x0_ready) {   // an asynchronous prediction of x0: wait for it here, not earlier
+        FE_CUDA(cudaStreamWaitEvent(h->stream, h->x0_ready, 0));
+        h->x0_ready = nullptr;
+    }
     FE_CHECK(init_solution(h, o, x));
     *x0_used = o->x0 ? 1 : 0;
     if (!o->x0 || !(o->flags & FE_SOLVE_X0_IF_BETTER)) return FE_OK;
@@ -1555,7 +1559,13 @@ int solve(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
         return FE_OK;
     }
     // continuity conditions: the projected FP64 PCG, whatever the precision asked
-    if (h->n_cont > 0) return solve_continuity(h, o, st);
+    if (h->n_cont > 0) {
+        if (h->x0_ready) {
+            FE_CUDA(cudaStreamWaitEvent(h->stream, h->x0_ready, 0));
+            h->x0_ready = nullptr;
+        }
+        return solve_continuity(h, o, st);
+    }
     if (o->flags & FE_SOLVE_MULTIGRID) return solve_multigrid(h, o, st);
     int lanes = 2;
     FE_CHECK(pick_lanes(h, o->precision, o->lanes, &lanes));
@@ -1616,7 +1626,9 @@ int time_spmv(fe_handle_s *h, int precision, int lanes, int reps, double *ms) {
 
 // y = A x with the FP64 SELL copy of the eliminated matrix (used by the warm-start
 // network's loss).  Enqueued on the handle's stream.
-int spmv64(fe_handle_s *h, const double *x, double *y) {
+int spmv64(fe_handle_s *h, const double *x, double *y) { return spmv64_on(h, x, y, h->stream); }
+
+int spmv64_on(fe_handle_s *h, const double *x, double *y, cudaStream_t stream) {
     if (!h->sys_ready) {
         set_error("spmv64: the system is not assembled");
         return FE_NOT_READY;
@@ -1624,8 +1636,8 @@ int spmv64(fe_handle_s *h, const double *x, double *y) {
     Sell A{h->sell_off.p, h->sell_col.p, nullptr, h->n_slices};
     FE_CHECK(with_dim(h->dim, [&](auto dc) {
         constexpr int D = decltype(dc)::value;
-        k_spmv<D, double><<<sell_grid(h), kVecThreads, 0, h->stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
-                                                                        nullptr, x, y);
+        k_spmv<D, double><<<sell_grid(h), kVecThreads, 0, stream>>>(h->n_nodes, A, h->sell_val64.p, h->diag64.p,
+                                                                     nullptr, x, y);
         return FE_OK;
     }));
     FE_LAUNCH_CHECK();

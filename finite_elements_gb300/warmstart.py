@@ -104,6 +104,15 @@ class WarmStartNet:
                                             ctypes.byref(x0), ctypes.byref(s)), "fe_gnn_predict")
         return (out if host else x0.value), s.value
 
+    def predict_async(self, system: GpuSystem):
+        """x0 for the system, enqueued on the network's own stream: returns at once with
+        the device address of n_dof doubles; the system's next solve waits for the
+        prediction before it reads x0 (its multigrid setup runs meanwhile)."""
+        x0 = ctypes.c_void_p()
+        _lib.check(self._lib.fe_gnn_predict_async(self.g, system.handle.h, ctypes.byref(x0)),
+                   "fe_gnn_predict_async")
+        return x0.value
+
     def target_energy(self, system: GpuSystem):
         e = ctypes.c_double()
         _lib.check(self._lib.fe_gnn_target_energy(self.g, system.handle.h, ctypes.byref(e)),

@@ -361,6 +361,12 @@ int fe_gnn_features(fe_gnn g, fe_handle h, float *features_host);  /* see fe_gnn
  * call; a copy also goes to x0_host when not NULL) and the scale s.  Pass *x0_dev to
  * fe_solve as opts.x0 with opts.x0_device = 1. */
 int fe_gnn_predict(fe_gnn g, fe_handle h, double *x0_host, const double **x0_dev, double *scale);
+/* The same prediction enqueued on the network's own stream without waiting for it: it
+ * starts after the handle's work so far (the assembly) and the handle's next solve waits
+ * for it just before it reads opts.x0, so a solve's multigrid setup overlaps with it.
+ * *x0_dev (n_dof doubles) is valid for that solve; the scale stays on the device.  Call
+ * a solve of h (or fe_synchronize on it) before the next prediction or destroying g. */
+int fe_gnn_predict_async(fe_gnn g, fe_handle h, const double **x0_dev);
 /* Training target of h's last solution: b~ . (x - g), the energy of its free part. */
 int fe_gnn_target_energy(fe_gnn g, fe_handle h, double *energy);
 /* Loss 1 - (u.b~)^2 / ((u.A u) energy) and its gradient w.r.t. every parameter

@@ -111,3 +111,26 @@ def test_fit_loss_and_gradient_match_oracle(small):
     cos = float(grad @ gref / (np.linalg.norm(grad) * np.linalg.norm(gref)))
     rel = float(np.linalg.norm(grad - gref) / np.linalg.norm(gref))
     assert cos >= 0.999 and rel <= 3e-2, (cos, rel)
+
+
+def test_async_prediction_gives_the_same_solve(gpu_lib):
+    """fe_gnn_predict_async (on the network's stream, the solve waiting for it before it
+    reads x0) gives the start, and so the multigrid solve, of the synchronous
+    prediction, bitwise."""
+    from finite_elements_gb300 import meshgen
+    from finite_elements_gb300.engine import GpuSystem
+    from finite_elements_gb300.warmstart import DEFAULT_WEIGHTS, WarmStartNet
+    net = WarmStartNet(weights=DEFAULT_WEIGHTS) if os.path.exists(DEFAULT_WEIGHTS) else WarmStartNet(seed=1)
+    prob = meshgen.plane_strain_random(80, 40, seed=11)
+    s = GpuSystem(prob)
+    kw = dict(precision="mixed-cg64", tol=1e-10, multigrid=True, accept_stagnation=True)
+    try:
+        ptr, _ = net.predict(s)
+        x1, st1 = s.solve(x0_device_ptr=ptr, x0_if_better=True, **kw)
+        ptr2 = net.predict_async(s)
+        x2, st2 = s.solve(x0_device_ptr=ptr2, x0_if_better=True, **kw)
+    finally:
+        s.close()
+    assert st1.status == 0 and st2.status == 0
+    assert st1.x0_used == st2.x0_used and st1.iterations == st2.iterations
+    np.testing.assert_array_equal(x1, x2)
