@@ -1253,7 +1253,11 @@ int fe_gnn_predict_async(fe_gnn g, fe_handle h, const double **x0_dev) {
         return FE_BAD_INPUT;
     }
     if (!g->own) {
-        FE_CUDA(cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking));
+        // the lowest priority: blocks of the handle's solve (the multigrid setup's short
+        // kernels) are scheduled before the prediction's
+        int lo = 0, hi = 0;
+        FE_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        FE_CUDA(cudaStreamCreateWithPriority(&g->own, cudaStreamNonBlocking, lo));
         FE_CUDA(cudaEventCreateWithFlags(&g->assembled, cudaEventDisableTiming));
         FE_CUDA(cudaEventCreateWithFlags(&g->ready, cudaEventDisableTiming));
     }
