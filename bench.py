@@ -596,8 +596,12 @@ def run_tet(args):
     """Secondary measurement, not the headline: s/solve to args.tol of the solid
     cantilever of linear tetrahedra (scripts/Elasticity/beam3d_example_2.py set-up),
     plain FP64 PCG with the node-block Jacobi preconditioner against the FP64 CG with
-    the FP32 Chebyshev preconditioner.  Device time (CUDA events on the handle
+    the FP32 Chebyshev preconditioner and against the FP64 CG with the FP32
+    smoothed-aggregation V-cycle (six rigid-body modes; hierarchy set up on the device
+    in every solve, its time included).  Device time (CUDA events on the handle
     stream) of the solve, inputs resident; the matrices are far larger than L2."""
+    import ctypes
+
     import numpy as np
 
     from finite_elements_gb300 import _lib, meshgen
@@ -606,10 +610,14 @@ def run_tet(args):
     prob = meshgen.cantilever_3d(*args.tet_dims)
     s = GpuSystem(prob)
     runs = {"plain": dict(precision="fp64", cheb_degree=0),
-            "mixed": dict(precision="mixed-cg64", cheb_degree=args.tet_cheb, cheb_ratio=args.tet_cheb_ratio)}
+            "mixed": dict(precision="mixed-cg64", cheb_degree=args.tet_cheb, cheb_ratio=args.tet_cheb_ratio),
+            "multigrid": dict(precision="mixed-cg64", multigrid=True)}
     res = {}
+    phases = None
     for name, kw in runs.items():
         ms, xs = [], None
+        if name == "multigrid":
+            s.handle.call("fe_profile_kernels", 1)   # setup phase times (and resets the sums)
         for k in range(args.warmup + args.steps):
             x, st = s.solve(tol=args.tol, **kw)
             if st.status != _lib.FE_OK:
@@ -619,7 +627,19 @@ def run_tet(args):
             xs = x[: prob.n_dof]
         res[name] = {"s": statistics.mean(ms) / 1e3, "iterations": st.iterations, "relres": st.relres,
                      "assemble_ms": st.assemble_ms, "x": xs}
-    diff = float(np.linalg.norm(res["mixed"]["x"] - res["plain"]["x"]) / np.linalg.norm(res["plain"]["x"]))
+        if name == "multigrid":
+            v = [ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(),
+                 ctypes.c_int64()]
+            s.handle.call("fe_profile_read_multigrid", *[ctypes.byref(x) for x in v])
+            ph = (ctypes.c_double * _lib.FE_MG_PHASES)()
+            s.handle.call("fe_profile_read_multigrid_phases", ph, _lib.FE_MG_PHASES)
+            s.handle.call("fe_profile_kernels", 0)
+            n_setup = max(v[3].value, 1)
+            phases = {"setup_ms": v[2].value / n_setup, "cycle_ms": v[4].value / max(v[5].value, 1),
+                      "setup_phases_ms": {nm: ph[k] / n_setup for k, nm in enumerate(_lib.MG_PHASE_NAMES)}}
+    xp = np.linalg.norm(res["plain"]["x"])
+    diff = float(np.linalg.norm(res["mixed"]["x"] - res["plain"]["x"]) / xp)
+    diff_mg = float(np.linalg.norm(res["multigrid"]["x"] - res["plain"]["x"]) / xp)
     out = {"metric": f"s/solve to {args.tol:g} rel. residual, 3D tetrahedral elasticity: mixed-cg64 vs plain PCG",
            "value": res["mixed"]["s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": False, "dtype": "f64 recurrence, f32 preconditioner", "data": "synthetic",
@@ -628,9 +648,13 @@ def run_tet(args):
                                   "x = 0 clamped, tip edge loaded in z", "l2": "inputs larger than L2",
                       "chebyshev": [args.tet_cheb, args.tet_cheb_ratio]},
            "plain_s": res["plain"]["s"], "speedup_vs_plain": res["plain"]["s"] / res["mixed"]["s"],
-           "iterations": {k: v["iterations"] for k, v in res.items()},
-           "relres": {k: v["relres"] for k, v in res.items()},
-           "rel_diff_mixed_vs_plain": diff, "assemble_ms": res["plain"]["assemble_ms"]}
+           "iterations": {k: res[k]["iterations"] for k in ("plain", "mixed")},
+           "relres": {k: res[k]["relres"] for k in ("plain", "mixed")},
+           "rel_diff_mixed_vs_plain": diff, "assemble_ms": res["plain"]["assemble_ms"],
+           "multigrid": {"s_per_solve": res["multigrid"]["s"],
+                         "speedup_vs_plain": res["plain"]["s"] / res["multigrid"]["s"],
+                         "iterations": res["multigrid"]["iterations"], "relres": res["multigrid"]["relres"],
+                         "rel_diff_vs_plain": diff_mg, **(phases or {})}}
     s.close()
     if not args.no_cpu_baseline:
         # the reference path on the host cores: the oracle's restatement (element loop, COO,

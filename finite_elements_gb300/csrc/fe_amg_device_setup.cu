@@ -659,23 +659,31 @@ struct DevEx {
         FE_LAUNCH_CHECK();
         return FE_OK;
     }
+    // a thread per row where rows are short, else a warp per row; block sizes fixed at
+    // compile time for the shapes of the hierarchies (A x P, R x AP and the coarse
+    // levels' products): 1 x 1 (magnetostatics), 2D elasticity's 2 x 2 A with three
+    // rigid-body modes, 3D elasticity's 3 x 3 A with six -- the accumulators then
+    // stay in registers
+    template <int RA, int CA, int CB>
+    int prod_vals_shape(int64_t n, const amg::PassProdVals &f, bool thread) {
+        if (!thread) return launch_prod_vals<RA, CA, CB>(n, f, s);
+        kd_prod_vals_thread<RA, CA, CB><<<grid_s(n), kST, 0, s>>>(n, f);
+        FE_LAUNCH_CHECK();
+        return FE_OK;
+    }
     int rows(int64_t n, const amg::PassProdVals &f) {
         if (n <= 0) return FE_OK;
-        if (!f.boff || (double)f.total < kWarpRowMean * (double)n) {
-            // a thread per row, block sizes fixed at compile time where the hierarchies have them
-            if (f.ra == 2 && f.ca == 2 && f.cb == 3) kd_prod_vals_thread<2, 2, 3><<<grid_s(n), kST, 0, s>>>(n, f);
-            else if (f.ra == 3 && f.ca == 3 && f.cb == 3) kd_prod_vals_thread<3, 3, 3><<<grid_s(n), kST, 0, s>>>(n, f);
-            else if (f.ra == 3 && f.ca == 2 && f.cb == 3) kd_prod_vals_thread<3, 2, 3><<<grid_s(n), kST, 0, s>>>(n, f);
-            else k_rows<amg::PassProdVals><<<grid_s(n), kST, 0, s>>>(n, f);
-        } else if (f.ra == 2 && f.ca == 2 && f.cb == 3) {
-            return launch_prod_vals<2, 2, 3>(n, f, s);
-        } else if (f.ra == 3 && f.ca == 2 && f.cb == 3) {
-            return launch_prod_vals<3, 2, 3>(n, f, s);
-        } else if (f.ra == 3 && f.ca == 3 && f.cb == 3) {
-            return launch_prod_vals<3, 3, 3>(n, f, s);
-        } else {
-            return launch_prod_vals<0, 0, 0>(n, f, s);
-        }
+        const bool thread = !f.boff || (double)f.total < kWarpRowMean * (double)n;
+        const int ra = f.ra, ca = f.ca, cb = f.cb;
+        if (ra == 1 && ca == 1 && cb == 1) return prod_vals_shape<1, 1, 1>(n, f, thread);
+        if (ra == 2 && ca == 2 && cb == 3) return prod_vals_shape<2, 2, 3>(n, f, thread);
+        if (ra == 3 && ca == 2 && cb == 3) return prod_vals_shape<3, 2, 3>(n, f, thread);
+        if (ra == 3 && ca == 3 && cb == 3) return prod_vals_shape<3, 3, 3>(n, f, thread);
+        if (ra == 3 && ca == 3 && cb == 6) return prod_vals_shape<3, 3, 6>(n, f, thread);
+        if (ra == 6 && ca == 3 && cb == 6) return prod_vals_shape<6, 3, 6>(n, f, thread);
+        if (ra == 6 && ca == 6 && cb == 6) return prod_vals_shape<6, 6, 6>(n, f, thread);
+        if (!thread) return launch_prod_vals<0, 0, 0>(n, f, s);
+        k_rows<amg::PassProdVals><<<grid_s(n), kST, 0, s>>>(n, f);
         FE_LAUNCH_CHECK();
         return FE_OK;
     }
