@@ -286,15 +286,33 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_cols_warp(int64_t n, amg::Pa
     }
 }
 
+// Dynamic shared memory of kd_prod_vals_warp, per warp: the 32 block products of a
+// chunk of terms (a row of 33 doubles per block entry, so that lanes reading different
+// entries of the same term hit different banks), six arrays of kTermCap ints (term
+// positions, order, A and B indices, counts, offsets) and the chunk's segment bounds and
+// keys (33 + 33, padded to 80).
+constexpr int kSegStride = 33, kSegInts = 80;
+template <int RA, int CB>
+constexpr int warp_vals_bs() { return RA && CB ? RA * CB : 36; }
+template <int RA, int CB>
+constexpr size_t warp_vals_smem() {
+    return (size_t)kPW * ((size_t)warp_vals_bs<RA, CB>() * kSegStride * sizeof(double) +
+                          (6 * (size_t)kTermCap + kSegInts) * sizeof(int32_t));
+}
+
 // C row i's values; RA x CA times CA x CB blocks (0: the sizes of f at run time)
 template <int RA, int CA, int CB>
 __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::PassProdVals f) {
-    __shared__ int32_t s_pos[kPW][kTermCap], s_ord[kPW][kTermCap], s_s[kPW][kTermCap], s_t[kPW][kTermCap];
-    __shared__ int32_t s_cnt[kPW][kTermCap], s_off[kPW][kTermCap];
+    extern __shared__ __align__(16) unsigned char s_warp_vals[];
+    constexpr int BSM = warp_vals_bs<RA, CB>();
     const int ra = RA ? RA : f.ra, ca = CA ? CA : f.ca, cb = CB ? CB : f.cb;
     const int bs = ra * cb;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    int32_t *pos = s_pos[wl], *ord = s_ord[wl], *ss = s_s[wl], *ts = s_t[wl], *cnt = s_cnt[wl], *off = s_off[wl];
+    double *vbuf = reinterpret_cast<double *>(s_warp_vals) + (size_t)wl * BSM * kSegStride;
+    int32_t *ib = reinterpret_cast<int32_t *>(s_warp_vals + (size_t)kPW * BSM * kSegStride * sizeof(double)) +
+                  (size_t)wl * (6 * kTermCap + kSegInts);
+    int32_t *pos = ib, *ord = ib + kTermCap, *ss = ib + 2 * kTermCap, *ts = ib + 3 * kTermCap;
+    int32_t *cnt = ib + 4 * kTermCap, *off = ib + 5 * kTermCap, *sstart = ib + 6 * kTermCap, *skey = sstart + 40;
     const int64_t W = (int64_t)gridDim.x * kPW;
     for (int64_t i = (int64_t)blockIdx.x * kPW + wl; i < n; i += W) {
         const int64_t T = f.boff[i + 1] - f.boff[i];
@@ -346,11 +364,14 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::Pa
             __syncwarp();
         }
         // the values, term-parallel: the terms ordered by output entry are taken 32 at a
-        // time, a lane computes one term's block product, a segmented scan across the
-        // lanes (a fixed shuffle tree) sums the terms of each entry within the chunk, and
-        // the lane ending an entry's segment adds that partial to the entry -- chunk after
-        // chunk, so the sums are deterministic (a lane summing its entries' terms alone
-        // left ~3 of 4 lanes idle: rows have few entries of uneven length)
+        // time and a lane computes one term's block product into shared memory; the
+        // chunk's terms of one entry are contiguous (a segment), and the lanes then take
+        // (segment, block entry) pairs, each summing its segment's values in term order
+        // and adding that partial to the output -- chunk after chunk, so the sums are
+        // deterministic.  A lane summing whole entries alone left ~3 of 4 lanes idle (rows
+        // have few entries of uneven length); a shuffle scan across the lanes cost 5 FP64
+        // additions per block entry and chunk, more than the products of a 6 x 3 x 6 term,
+        // where this costs about one per block entry and chunk
         for (int64_t p = lane; p < lc; p += 32) {
             if (f.upper && f.ccol[c0 + p] < i) continue;   // filled by the mirror pass
             double *o = f.cval + (c0 + p) * bs;
@@ -360,27 +381,32 @@ __global__ void __launch_bounds__(kPW * 32) kd_prod_vals_warp(int64_t n, amg::Pa
         const int tv = lc > 0 ? off[lc - 1] : 0;   // the terms that reach an entry
         for (int q0 = 0; q0 < tv; q0 += 32) {
             const int q = q0 + lane;
-            const bool valid = q < tv;
+            const bool valid = q < tv;   // the valid lanes are a prefix of the warp
             const int t = valid ? ord[q] : 0;
-            const int key = valid ? pos[t] : -1 - lane;   // sorted over the valid lanes
-            double v[RA && CB ? RA * CB : 36];
+            const int key = valid ? pos[t] : -1;   // non-decreasing over the valid lanes
+            double v[BSM];
             for (int k = 0; k < bs; ++k) v[k] = 0.0;
             if (valid)
                 amg::block_mul_add(f.aval + (int64_t)ss[t] * ra * ca, f.bval + (int64_t)ts[t] * ca * cb, ra, ca, cb,
                                    v);
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int kup = __shfl_up_sync(0xffffffffu, key, o);
-                const bool take = lane >= o && kup == key;
-                for (int k = 0; k < bs; ++k) {
-                    const double y = __shfl_up_sync(0xffffffffu, v[k], o);
-                    if (take) v[k] += y;
-                }
+            for (int k = 0; k < bs; ++k) vbuf[k * kSegStride + lane] = v[k];
+            // segment starts: the first valid lane of each key
+            const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+            const bool start = valid && (lane == 0 || kprev != key);
+            const unsigned starts = __ballot_sync(0xffffffffu, start);
+            if (start) {
+                const int r = __popc(starts & ((1u << lane) - 1u));
+                sstart[r] = lane;
+                skey[r] = key;
             }
-            const int knext = __shfl_down_sync(0xffffffffu, key, 1);
-            if (valid && (lane == 31 || q + 1 >= tv || knext != key)) {
-                double *o = f.cval + (c0 + key) * bs;
-                for (int k = 0; k < bs; ++k) o[k] += v[k];
+            const int nseg = __popc(starts);   // >= 1: lane 0 is valid
+            if (lane == 0) sstart[nseg] = tv - q0 < 32 ? tv - q0 : 32;
+            __syncwarp();
+            for (int j = lane; j < nseg * bs; j += 32) {
+                const int sg = j / bs, k = j - sg * bs;
+                double acc = 0.0;
+                for (int x = sstart[sg]; x < sstart[sg + 1]; ++x) acc += vbuf[k * kSegStride + x];
+                f.cval[(c0 + skey[sg]) * bs + k] += acc;
             }
             __syncwarp();
         }
@@ -578,7 +604,11 @@ __global__ void __launch_bounds__(32) kd_prod_vals_long(int64_t n, amg::PassProd
 
 template <int RA, int CA, int CB>
 int launch_prod_vals(int64_t n, const amg::PassProdVals &f, cudaStream_t s) {
-    kd_prod_vals_warp<RA, CA, CB><<<warp_grid(n), kPW * 32, 0, s>>>(n, f);
+    constexpr size_t smem = warp_vals_smem<RA, CB>();
+    static_assert(smem <= 227 * 1024, "shared memory of kd_prod_vals_warp");
+    FE_CUDA(cudaFuncSetAttribute(kd_prod_vals_warp<RA, CA, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    kd_prod_vals_warp<RA, CA, CB><<<warp_grid(n), kPW * 32, smem, s>>>(n, f);
     FE_LAUNCH_CHECK();
     static_assert(kLongTerms <= 32767 && kLongOut <= 32767, "16-bit term and entry indices");
     FE_CUDA(cudaFuncSetAttribute(kd_prod_vals_long<RA, CA, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
