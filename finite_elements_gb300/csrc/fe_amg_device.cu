@@ -433,8 +433,9 @@ int precondition_dense(CycleEx &ex, const amg::CycleCoarse &C, const double *r, 
 
 }  // namespace
 
-// PCG on the eliminated system preconditioned by one FP32 V-cycle (k = 3 Chebyshev steps
-// per smoothing), FP64 recurrence, from x = 0 (opts.x0 is not used); the hierarchy is
+// PCG on the eliminated system preconditioned by one FP32 V-cycle (Chebyshev smoothing:
+// kSmooth0 steps on level 0, kSmoothCoarse below), FP64 recurrence, from x = 0 or from
+// opts.x0 (with FE_SOLVE_X0_IF_BETTER only when it beats the zero start); the hierarchy is
 // set up on the device from the system matrix and the rigid-body (elasticity) or
 // constant (magnetostatics) modes, with the rows of the constrained DOFs zeroed.
 int solve_multigrid(fe_handle_s *h, const fe_solve_opts *o, fe_solve_stats *st) {
