@@ -1,4 +1,4 @@
-// Row operations of the parallel smoothed-aggregation setup, shared by the host driver
+// Row operations of the parallel smoothed-aggregation setup, shared by the host executor
 // (fe_amg_setup.cu, fe_amg_build_parallel_host) and the device setup: every function
 // computes one row (or one aggregate) from arrays that the pass does not write, so a
 // pass is a loop over rows in any order and its result does not depend on the order.
