@@ -624,7 +624,7 @@ struct DevEx {
     MgMem mem;
     cudaStream_t s;
     DBuf<int64_t> scan_tmp;
-    DBuf<double> part, sc;
+    DBuf<double> part;
     SetupTrace *trace = nullptr;
     // level 0's operator is the handle's eliminated system: its plain products run on
     // the handle's FP64 SELL copy
@@ -634,7 +634,7 @@ struct DevEx {
     void phase(int k) {
         if (trace) trace->mark(s, k);
     }
-    ~DevEx() { pfree(mem, scan_tmp), pfree(mem, part), pfree(mem, sc); }
+    ~DevEx() { pfree(mem, scan_tmp), pfree(mem, part); }
     template <class T>
     int alloc(DBuf<T> &b, size_t n) { return palloc(mem, b, n); }
     template <class T>
@@ -725,18 +725,6 @@ struct DevEx {
         kd_dot<<<g, kST, 0, s>>>(n, a, b, part.p);
         kd_dot_final<<<1, kST, 0, s>>>(g, part.p, dst);
         FE_LAUNCH_CHECK();
-        return FE_OK;
-    }
-    int dot(const double *a, const double *b, int64_t n, double *out) {
-        const int g = grid_s(n);
-        FE_CHECK(palloc(mem, part, (size_t)g));
-        FE_CHECK(palloc(mem, sc, 1));
-        kd_dot<<<g, kST, 0, s>>>(n, a, b, part.p);
-        kd_dot_final<<<1, kST, 0, s>>>(g, part.p, sc.p);
-        FE_LAUNCH_CHECK();
-        FE_CUDA(cudaMemcpyAsync(mem.pinned, sc.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-        FE_CUDA(cudaStreamSynchronize(s));
-        *out = mem.pinned[0];
         return FE_OK;
     }
 };
