@@ -499,10 +499,6 @@ struct Bounds {
     float xmin, xmax, ymin, ymax;
 };
 
-__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
-    // v >= 0: the int order of non-negative floats is their value order
-    atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
-}
 __device__ __forceinline__ void atomic_min_f(float *addr, float v) {
     int old = __float_as_int(*addr);
     while (__int_as_float(old) > v) {

@@ -97,7 +97,8 @@ km_gemv(int64_t n, int nv, const double *__restrict__ V, int64_t ld, const doubl
     }
 }
 
-__global__ void __launch_bounds__(kMT) km_scale(int64_t n, const double *__restrict__ x, double s, double *__restrict__ y) {
+// y = s x; also called in place (y == x), so the pointers are not restrict-qualified
+__global__ void __launch_bounds__(kMT) km_scale(int64_t n, const double *x, double s, double *y) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
         y[r] = s * x[r];
 }
