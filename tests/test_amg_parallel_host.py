@@ -79,6 +79,11 @@ def problem(case, scale=1):
     elif case == "tet":
         prob = meshgen.cantilever_3d(10, 4, 4, jitter=0.2, seed=5)
         d, modes = 3, AMG.rigid_modes_3d
+    elif case == "tet_deep":
+        # 3,528 -> 456 -> 36 DOFs: a level of 6 x 6 blocks (six rigid-body modes) with
+        # its own prolongator and Galerkin product
+        prob = meshgen.cantilever_3d(24, 6, 6, jitter=0.2, seed=5)
+        d, modes = 3, AMG.rigid_modes_3d
     else:
         prob = meshgen.magnetostatic(50, 25, seed=2)
         d, modes = 1, None
@@ -125,7 +130,7 @@ def mis2_roots(S):
     return np.flatnonzero(state == 2)
 
 
-@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "tet_deep", "magnetic"])
 def test_aggregates_form_a_distance_two_independent_set(case):
     A, b, B, d = problem(case)
     lib, h, levels = build(A, B, d)
@@ -154,11 +159,13 @@ def test_aggregates_form_a_distance_two_independent_set(case):
         lib.fe_amg_destroy(h)
 
 
-@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "tet_deep", "magnetic"])
 def test_operators_match_the_model_on_the_same_aggregates(case):
     A, b, B, d = problem(case)
     lib, h, levels = build(A, B, d)
     try:
+        if case == "tet_deep":
+            assert len(levels) >= 3 and levels[1]["d"] == 6
         Al, Bl, dl = A, B, d
         for l, lev in enumerate(levels[:-1]):
             Minv = AMG.block_diag_inv(Al, dl)
@@ -177,7 +184,7 @@ def test_operators_match_the_model_on_the_same_aggregates(case):
         lib.fe_amg_destroy(h)
 
 
-@pytest.mark.parametrize("case,limit", [("plane_strain", 40), ("tet", 40), ("magnetic", 40)])
+@pytest.mark.parametrize("case,limit", [("plane_strain", 40), ("tet", 40), ("tet_deep", 40), ("magnetic", 40)])
 def test_pcg_with_the_parallel_hierarchy(case, limit):
     """The library's host V-cycle on the parallel hierarchy: PCG to 1e-8 within the
     limit and within 25% (+2) of the greedy hierarchy's count."""
@@ -212,7 +219,7 @@ def test_same_hierarchy_on_every_run():
             assert (a["P"] != b_["P"]).nnz == 0 and np.array_equal(a["agg"], b_["agg"])
 
 
-@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "tet_deep", "magnetic"])
 def test_fp32_cycle_of_the_device_sequence(case):
     """fe_amg_vcycle_host_f32 (the device's FP32 cycle, fe_amg_cycle.cuh, run on the
     host) against the FP64 host cycle: one cycle within 1e-4, and PCG iteration counts
@@ -245,7 +252,7 @@ def test_fp32_cycle_of_the_device_sequence(case):
         lib.fe_amg_destroy(h)
 
 
-@pytest.mark.parametrize("case", ["plane_strain", "tet", "magnetic"])
+@pytest.mark.parametrize("case", ["plane_strain", "tet", "tet_deep", "magnetic"])
 def test_multigrid_pcg_sequence_on_the_host(case):
     """fe_amg_pcg_host: the device solve's PCG around the FP32 cycle (fe_amg_cycle.cuh)
     run on the host, against the model's PCG with the same FP32 cycle: the same
